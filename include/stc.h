@@ -1,0 +1,137 @@
+/*
+ * stc.h -- C ABI of the GB300-native STCDB co-occurrence pipeline.
+ *
+ * One context owns one GPU-resident pipeline: the partitioning quadtree
+ * (schema), the per-step leaf lists, the open-addressed meeting table and the
+ * buffer of emitted meetings. Plain pointers and sizes only; no C++ or torch
+ * types cross this boundary.
+ *
+ * Reference interface replaced (paths inside the tengdj/STCDB checkout):
+ *   stc_create          <- partitioner::build_schema (tracing/filter.cpp:27-93,
+ *                          declared tracing/partitioner.h:218) followed by
+ *                          cuda_create_device_bench (cuda/geometry.cu:1395,
+ *                          declared tracing/process.cpp:374)
+ *   stc_step / stc_step_device
+ *                       <- process_with_gpu (cuda/geometry.cu:1573, declared
+ *                          tracing/process.cpp:375) and its CPU twin in
+ *                          tracer::process (tracing/process.cpp:452-459, 608-612):
+ *                          filter + reachability + update_meetings + update_schema
+ *   stc_drain_meetings  <- reading h_meetings_ps[0..kv_count) after
+ *                          update_meetings (tracing/meeting.cpp:11-24)
+ *   stc_get_stats       <- workbench counters grid_check_counter,
+ *                          num_taken_buckets, num_active_meetings
+ *                          (tracing/workbench.h:136, 152-153)
+ *   stc_destroy         <- workbench::clear / gpu_info::clear
+ *                          (tracing/workbench.cpp:62-73)
+ *   stc_last_error      <- (none: the reference exits on CUDA errors,
+ *                          cuda/cuda_util.cuh:19-27)
+ *
+ * Error behaviour: every call returns a status and never exits or hangs.
+ * Device-side loops are bounded; a bound that runs out is reported as
+ * STC_ERR_TIMEOUT or STC_ERR_CAPACITY and the context stays usable for
+ * stc_destroy.
+ *
+ * Threading: a context is driven by one host thread at a time.
+ */
+#ifndef STC_H
+#define STC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum stc_status {
+  STC_OK = 0,
+  STC_ERR_INVALID_ARG = 1,
+  STC_ERR_CUDA = 2,
+  STC_ERR_CAPACITY = 3,   /* a fixed-size device structure overflowed */
+  STC_ERR_TIMEOUT = 4,    /* a bounded device loop ran out of iterations */
+  STC_ERR_UNSUPPORTED = 5,
+  STC_ERR_STATE = 6       /* call out of order, or context already failed */
+} stc_status;
+
+/* Pipeline parameters. Field meanings follow the reference's
+ * `configuration` class (util/config.h:15-114). */
+typedef struct stc_config {
+  uint32_t num_objects;          /* objects per step (config.h:21) */
+  uint32_t min_meet_time;        /* steps a meeting must last (config.h:39) */
+  uint32_t max_meet_time;        /* longer meetings go to the oversize buffer (config.h:40) */
+  uint32_t grid_capacity;        /* quadtree leaf split threshold (config.h:29) */
+  double grid_amplify;           /* leaf list capacity = amplify*grid_capacity (config.h:33) */
+  double reach_distance;         /* metres (config.h:41) */
+  uint64_t num_meeting_buckets;  /* meeting table slots (config.h:31, default 2N config.h:306-308) */
+  uint32_t refine_size;          /* border checking units per object (config.h:34) */
+  uint32_t schema_update_delay;  /* consecutive over/underflows before split/merge (config.h:38) */
+  int32_t dynamic_schema;        /* update the quadtree after every step (config.h:35) */
+  int32_t mbr_filter;            /* drop meetings whose MBR leaves the map box (cuda/geometry.cu:667-670) */
+  uint64_t candidate_capacity;   /* new-meeting candidates per step; 0 = auto */
+  uint64_t emit_capacity;        /* emitted meetings held between drains; 0 = auto */
+  uint32_t device;               /* CUDA device ordinal */
+  uint32_t reserved;
+} stc_config;
+
+/* One finished meeting. pid_lo < pid_hi; start/end are the first and last
+ * step in which the pair was within reach; mbr is the float bounding box of
+ * both objects over those steps (low x, low y, high x, high y). */
+typedef struct stc_meeting {
+  uint32_t pid_lo, pid_hi, start, end;
+  float mbr[4];
+} stc_meeting;
+
+/* Counters of the last completed step. */
+typedef struct stc_stats {
+  uint32_t step;                 /* time stamp of the last step */
+  uint32_t leaves;               /* live quadtree leaves */
+  uint32_t schema_nodes;         /* live quadtree nodes */
+  uint32_t overflow_objects;     /* objects dropped from full leaf lists */
+  uint64_t checking_units;       /* own-leaf + border units (grid_check_counter) */
+  uint64_t border_units;
+  uint64_t pair_tests;           /* candidate pairs tested */
+  uint64_t exact_tests;          /* tests that needed the fp64 reference arithmetic */
+  uint64_t hits;                 /* pairs within reach */
+  uint64_t new_candidates;       /* distinct keys that needed ordered insertion */
+  uint64_t taken_buckets;        /* occupied slots after the step */
+  uint64_t emitted;              /* meetings emitted by the step */
+  uint64_t pending;              /* emitted meetings not yet drained */
+  uint32_t splits, merges;       /* schema updates applied after the step */
+  float step_ms;                 /* device time of the step */
+  float phase_ms[8];             /* partition, border, refine, insert, sweep, schema, copy-in, other */
+} stc_stats;
+
+/* Fills *cfg with the reference defaults for n objects (util/config.h:29-41,
+ * 303-317): grid_capacity 50, grid_amplify 2, refine_size 4, reach 2 m,
+ * min_meet_time 5, max_meet_time 4096, buckets 2n, dynamic schema on. */
+void stc_config_default(stc_config *cfg, uint32_t num_objects);
+
+typedef struct stc_ctx stc_ctx;
+
+/* Builds the quadtree from the step-0 positions xy0 (n (lon, lat) f64 pairs
+ * in host memory) inside the map box mbr (lon/lat low x, low y, high x,
+ * high y) and allocates all device state. */
+stc_status stc_create(const stc_config *cfg, const double mbr[4], const double *xy0, uint32_t n,
+                      stc_ctx **out);
+
+/* Processes one time step. xy: num_objects (lon, lat) f64 pairs, layout
+ * [oid], in host memory (copied in) or device memory (stc_step_device). */
+stc_status stc_step(stc_ctx *ctx, const double *xy, uint32_t t);
+stc_status stc_step_device(stc_ctx *ctx, const double *xy_device, uint32_t t);
+
+/* Copies up to cap emitted meetings (in emission order) into out, removes
+ * them from the context and stores how many were copied in *n. */
+stc_status stc_drain_meetings(stc_ctx *ctx, stc_meeting *out, size_t cap, size_t *n);
+
+stc_status stc_get_stats(stc_ctx *ctx, stc_stats *stats);
+
+/* Last error message of ctx (or of the last failed stc_create when ctx is
+ * NULL). Never NULL. */
+const char *stc_last_error(const stc_ctx *ctx);
+
+void stc_destroy(stc_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STC_H */

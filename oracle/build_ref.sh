@@ -1,0 +1,34 @@
+#!/usr/bin/env bash
+# Compiles the reference's own CPU co-occurrence path from its unmodified
+# sources (read in place, never copied) plus the harness oracle/ref_driver.cpp
+# into oracle/_ref/ref_driver. The reference is only present on the machine
+# that holds the read-only checkout; elsewhere this script exits 0 and does
+# nothing, and the committed fixtures under tests/golden/ stand in for it.
+#
+# Flags: -O2 -ffp-contract=off keeps the floating-point expressions exactly
+# as written (no fused multiply-add), which is what the reference's own
+# x86-64 build (src/Makefile:11, plain g++ without -march) produces.
+set -euo pipefail
+REF=${STC_REFERENCE_DIR:-/root/reference}
+HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+OUT="$HERE/_ref"
+if [ ! -d "$REF/src/tracing" ]; then
+  echo "build_ref: reference sources not present; skipping" >&2
+  exit 0
+fi
+mkdir -p "$OUT"
+CUDA_INC=${CUDA_HOME:-/usr/local/cuda}/include
+SRCS="tracing/filter.cpp tracing/refinement.cpp tracing/meeting.cpp tracing/workbench.cpp tracing/step_merge.cpp"
+OBJS=""
+for s in $SRCS; do
+  o="$OUT/$(basename "${s%.cpp}").o"
+  if [ ! -f "$o" ] || [ "$REF/src/$s" -nt "$o" ]; then
+    g++ -std=c++17 -O2 -ffp-contract=off -w -fopenmp -I"$HERE/ref_stub" -I"$REF/src" -I"$CUDA_INC" \
+      -c "$REF/src/$s" -o "$o" &
+  fi
+  OBJS="$OBJS $o"
+done
+wait
+g++ -std=c++17 -O2 -ffp-contract=off -w -fopenmp -I"$HERE/ref_stub" -I"$REF/src" -I"$CUDA_INC" \
+  "$HERE/ref_driver.cpp" $OBJS -o "$OUT/ref_driver" -lpthread
+echo "build_ref: built $OUT/ref_driver" >&2

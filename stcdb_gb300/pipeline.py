@@ -1,0 +1,209 @@
+"""Python mirror of the C ABI in include/stc.h (ctypes over lib/libstc.so).
+
+`Pipeline` follows the reference's driver loop (tracing/process.cpp:401-612):
+it is created from the step-0 positions like partitioner::build_schema
+(tracing/filter.cpp:27) and then processes one step per call like
+process_with_gpu (cuda/geometry.cu:1573). Every call goes through the CUDA
+library; there is no CPU fallback, and a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, fields, replace
+
+import numpy as np
+
+from ._lib import load_library
+
+MEETING_DTYPE = np.dtype([("pid_lo", "<u4"), ("pid_hi", "<u4"), ("start", "<u4"), ("end", "<u4"),
+                          ("mbr", "<f4", (4,))])
+
+STATUS = {0: "OK", 1: "INVALID_ARG", 2: "CUDA", 3: "CAPACITY", 4: "TIMEOUT", 5: "UNSUPPORTED", 6: "STATE"}
+
+
+class StcError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class _Config(ctypes.Structure):
+    _fields_ = [
+        ("num_objects", ctypes.c_uint32),
+        ("min_meet_time", ctypes.c_uint32),
+        ("max_meet_time", ctypes.c_uint32),
+        ("grid_capacity", ctypes.c_uint32),
+        ("grid_amplify", ctypes.c_double),
+        ("reach_distance", ctypes.c_double),
+        ("num_meeting_buckets", ctypes.c_uint64),
+        ("refine_size", ctypes.c_uint32),
+        ("schema_update_delay", ctypes.c_uint32),
+        ("dynamic_schema", ctypes.c_int32),
+        ("mbr_filter", ctypes.c_int32),
+        ("candidate_capacity", ctypes.c_uint64),
+        ("emit_capacity", ctypes.c_uint64),
+        ("device", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
+    ]
+
+
+class StcStats(ctypes.Structure):
+    _fields_ = [
+        ("step", ctypes.c_uint32),
+        ("leaves", ctypes.c_uint32),
+        ("schema_nodes", ctypes.c_uint32),
+        ("overflow_objects", ctypes.c_uint32),
+        ("checking_units", ctypes.c_uint64),
+        ("border_units", ctypes.c_uint64),
+        ("pair_tests", ctypes.c_uint64),
+        ("exact_tests", ctypes.c_uint64),
+        ("hits", ctypes.c_uint64),
+        ("new_candidates", ctypes.c_uint64),
+        ("taken_buckets", ctypes.c_uint64),
+        ("emitted", ctypes.c_uint64),
+        ("pending", ctypes.c_uint64),
+        ("splits", ctypes.c_uint32),
+        ("merges", ctypes.c_uint32),
+        ("step_ms", ctypes.c_float),
+        ("phase_ms", ctypes.c_float * 8),
+    ]
+
+    def as_dict(self) -> dict:
+        d = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            d[name] = list(v) if name == "phase_ms" else v
+        return d
+
+
+@dataclass(frozen=True)
+class StcConfig:
+    """Pipeline parameters (meanings of util/config.h:15-114)."""
+    num_objects: int
+    reach_distance: float = 2.0
+    min_meet_time: int = 5
+    max_meet_time: int = 4096
+    grid_capacity: int = 50
+    grid_amplify: float = 2.0
+    num_meeting_buckets: int = 0      # 0 = reference default 2N
+    refine_size: int = 4
+    schema_update_delay: int = 1
+    dynamic_schema: bool = True
+    mbr_filter: bool = True
+    candidate_capacity: int = 0
+    emit_capacity: int = 0
+    device: int = 0
+
+    def resolved(self) -> "StcConfig":
+        if self.num_meeting_buckets == 0:
+            return replace(self, num_meeting_buckets=2 * self.num_objects)
+        return self
+
+
+def config_struct(cfg: StcConfig) -> _Config:
+    cfg = cfg.resolved()
+    c = _Config()
+    for f in fields(cfg):
+        setattr(c, f.name, int(getattr(cfg, f.name)) if not isinstance(getattr(cfg, f.name), float)
+                else getattr(cfg, f.name))
+    return c
+
+
+def _lib():
+    lib = load_library("libstc")
+    if not getattr(lib, "_stc_typed", False):
+        lib.stc_config_default.argtypes = [ctypes.POINTER(_Config), ctypes.c_uint32]
+        lib.stc_create.argtypes = [ctypes.POINTER(_Config), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                   ctypes.POINTER(ctypes.c_void_p)]
+        lib.stc_create.restype = ctypes.c_int
+        lib.stc_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32]
+        lib.stc_step.restype = ctypes.c_int
+        lib.stc_step_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32]
+        lib.stc_step_device.restype = ctypes.c_int
+        lib.stc_drain_meetings.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                           ctypes.POINTER(ctypes.c_size_t)]
+        lib.stc_drain_meetings.restype = ctypes.c_int
+        lib.stc_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(StcStats)]
+        lib.stc_get_stats.restype = ctypes.c_int
+        lib.stc_last_error.argtypes = [ctypes.c_void_p]
+        lib.stc_last_error.restype = ctypes.c_char_p
+        lib.stc_destroy.argtypes = [ctypes.c_void_p]
+        lib._stc_typed = True
+    return lib
+
+
+class Pipeline:
+    """One GPU-resident co-occurrence pipeline (an stc_ctx)."""
+
+    def __init__(self, cfg: StcConfig, mbr, xy0: np.ndarray):
+        self.cfg = cfg.resolved()
+        self._lib = _lib()
+        self._c = config_struct(self.cfg)
+        self._mbr = np.ascontiguousarray(mbr, dtype=np.float64)
+        xy0 = np.ascontiguousarray(xy0, dtype=np.float64)
+        h = ctypes.c_void_p()
+        st = self._lib.stc_create(ctypes.byref(self._c), self._mbr.ctypes.data, xy0.ctypes.data,
+                                  xy0.shape[0], ctypes.byref(h))
+        if st != 0:
+            raise StcError(st, self._lib.stc_last_error(h).decode())
+        self._h = h
+
+    def _check(self, st: int):
+        if st != 0:
+            raise StcError(st, self._lib.stc_last_error(self._h).decode())
+
+    def step(self, xy: np.ndarray, t: int) -> None:
+        xy = np.ascontiguousarray(xy, dtype=np.float64)
+        assert xy.shape == (self.cfg.num_objects, 2)
+        self._check(self._lib.stc_step(self._h, xy.ctypes.data, t))
+
+    def step_device(self, xy_device_ptr: int, t: int) -> None:
+        self._check(self._lib.stc_step_device(self._h, ctypes.c_void_p(xy_device_ptr), t))
+
+    def stats(self) -> StcStats:
+        s = StcStats()
+        self._check(self._lib.stc_get_stats(self._h, ctypes.byref(s)))
+        return s
+
+    def drain(self) -> np.ndarray:
+        out = []
+        while True:
+            pend = self.stats().pending
+            cap = max(int(pend), 1)
+            buf = np.zeros(cap, dtype=MEETING_DTYPE)
+            n = ctypes.c_size_t()
+            self._check(self._lib.stc_drain_meetings(self._h, buf.ctypes.data, cap, ctypes.byref(n)))
+            out.append(buf[: n.value])
+            if n.value < cap or n.value == 0:
+                break
+        return np.concatenate(out) if out else np.zeros(0, MEETING_DTYPE)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.stc_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def sort_meetings(m: np.ndarray) -> np.ndarray:
+    """Canonical order for comparing meeting sets."""
+    order = np.lexsort((m["end"], m["start"], m["pid_hi"], m["pid_lo"]))
+    return m[order]
+
+
+def meetings_digest(m: np.ndarray) -> str:
+    """SHA-256 of the sorted tuple set (pid_lo, pid_hi, start, end, mbr bits)."""
+    import hashlib
+    s = sort_meetings(np.ascontiguousarray(m, dtype=MEETING_DTYPE))
+    return hashlib.sha256(s.tobytes()).hexdigest()
