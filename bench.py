@@ -1,0 +1,328 @@
+"""Benchmark of the GB300 co-occurrence pipeline (one JSON line on rank 0).
+
+A step is one time step of the hot path over all objects: partition, border
+lookup, refinement, meeting-table insert, expire/emit sweep and quadtree
+update (the reference's filter + reachability + update_meetings +
+update_schema, tracing/process.cpp:452-459, 608-612).
+
+Workload (default "uniform-10M"): 10,000,000 objects walking a seeded
+200x200 jittered street grid over 40 km x 40 km at U[1,15] m/s, uniform
+starts, reach 10 m, minimum meeting 5 steps, leaf capacity 200, 2^28 table
+slots (about 68M pairs are live per step, so the reference default of 2N
+slots would overflow). This is the pure-uniform window of the batching
+configuration (1M-20M objects, 0-90% hotspot) at the headline 10M objects.
+The 10M-object hotspot configuration (70% in 1000 Zipf hotspots, sigma
+300 m) does not fit one GPU: its live pairs grow with N^2 (measured 3.5e7
+at 1M objects, so ~3.5e9 at 10M), beyond any 32-byte-slot meeting table
+that fits in HBM. "hotspot-1M" runs that model at 1M objects.
+
+value: position updates per second with positions already resident in HBM
+  (stc_step_device), summed device time of K steps (CUDA events on the
+  library's stream). Inputs (160 MB per step) and the meeting table exceed
+  the 129 MB L2, so no flush is inserted between steps.
+e2e: the same metric through the public C ABI with host input: every step
+  copies that step's positions from pinned host memory (stc_step) and drains
+  the emitted meetings back to the host (stc_drain_meetings); wall clock.
+--impl reference: the oracle's C restatement of the reference CPU path with
+  all host threads (the reference's own sources are not on the GPU host).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "pos-updates/s at 10M objs (bit-exact meetings); query p50/p99 under ingest"
+UNIT = "pos-updates/s"
+
+WORKLOADS = {
+    "uniform-10M": dict(objects=10_000_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
+                        buckets=1 << 28),
+    "hotspot-1M": dict(objects=1_000_000, hot=1000, reach=10.0, min_meet=5, grid_capacity=200, amplify=8.0,
+                       buckets=1 << 28),
+    "uniform-100k": dict(objects=100_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
+                         buckets_per_object=8),
+}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_trace_cfg(w, seed):
+    from stcdb_gb300.tracegen import hotspot_grid, uniform_grid
+    if w["hot"]:
+        return hotspot_grid(w["objects"], n_hotspots=w["hot"], seed=seed)
+    return uniform_grid(w["objects"], seed=seed)
+
+
+def make_cfg(w, device=0):
+    from stcdb_gb300.pipeline import StcConfig
+    b = w.get("buckets") or w["buckets_per_object"] * w["objects"]
+    return StcConfig(num_objects=w["objects"], reach_distance=w["reach"], min_meet_time=w["min_meet"],
+                     grid_capacity=w["grid_capacity"], grid_amplify=w["amplify"], num_meeting_buckets=b,
+                     device=device)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def run_gpu(args, w, rank, local):
+    import torch
+    from stcdb_gb300.pipeline import Pipeline
+    from stcdb_gb300.tracegen import TraceGenerator
+
+    torch.cuda.set_device(local)
+    N = w["objects"]
+    K, W = args.steps, args.warmup
+    gen = TraceGenerator(make_trace_cfg(w, seed=1 + rank))
+    mbr = gen.map_box(100.0)
+    total_steps = W + 2 * K
+    host = torch.empty((total_steps, N, 2), dtype=torch.float64, pin_memory=True)
+    hnp = host.numpy()
+    for t in range(total_steps):
+        gen.next(hnp[t])
+    dev = torch.empty((W + K, N, 2), dtype=torch.float64, device=f"cuda:{local}")
+    dev.copy_(host[: W + K])
+    torch.cuda.synchronize()
+    cfg = make_cfg(w, device=local)
+    pipe = Pipeline(cfg, mbr, hnp[0])
+    # warm-up steps (device-resident input)
+    for t in range(W):
+        pipe.step_device(dev[t].data_ptr(), t)
+        pipe.drain()
+    stats = []
+    barrier(args)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for t in range(W, W + K):
+            pipe.step_device(dev[t].data_ptr(), t)
+            stats.append(pipe.stats())
+            pipe.drain()
+        torch.cuda.synchronize()
+    wall_dev = time.perf_counter() - t0
+    barrier(args)
+    dev_ms = sum(s.step_ms for s in stats)
+    # end to end: host positions in, meetings out, through the C ABI
+    e2e_stats = []
+    d2h = 0
+    barrier(args)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for t in range(W + K, W + 2 * K):
+        pipe.step(hnp[t], t)
+        m = pipe.drain()
+        d2h += m.nbytes + 128
+        e2e_stats.append(pipe.stats())
+    torch.cuda.synchronize()
+    wall_e2e = time.perf_counter() - t1
+    pipe.close()
+    return dict(stats=stats, dev_ms=dev_ms, wall_dev=wall_dev, wall_e2e=wall_e2e, e2e_stats=e2e_stats,
+                d2h=d2h, clocks=clk.summary())
+
+
+def barrier(args):
+    if args.world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(args, v):
+    if args.world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def kernel_bytes(s, N, B):
+    """Algorithmic bytes per launch of the step's kernels.
+    partition: 36 N (read positions, write leaf-ordered points, id map)
+    refine:    16 N + 16 H + 8 Q plus the fused probe, 64 B per hit
+    sweep:     32 B per table slot + 64 B per emitted meeting"""
+    H, Q = s.border_units, s.hits
+    return {"partition": 36.0 * N, "refine": 16.0 * N + 16.0 * H + 72.0 * Q,
+            "sweep": 32.0 * B + 64.0 * s.emitted}
+
+
+def cpu_baseline(w, steps, threads, sample_note):
+    import oracle
+    from stcdb_gb300.tracegen import TraceGenerator
+    gen = TraceGenerator(make_trace_cfg(w, seed=1))
+    mbr = gen.map_box(100.0)
+    xs = [gen.next().copy() for _ in range(steps + 1)]
+    cfg = make_cfg(w)
+    o = oracle.Oracle(cfg, mbr, xs[0], threads=threads)
+    o.step(xs[0], 0)  # first step: every pair is new
+    t0 = time.perf_counter()
+    for t in range(1, steps + 1):
+        o.step(xs[t], t)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": w["objects"] * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": sample_note.format(steps=steps, seconds=round(dt, 2))}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default="uniform-10M", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-steps", type=int, default=2, help="steps timed for the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, rank, local = dist_env()
+    args.world = ws
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://")
+    w = WORKLOADS[args.workload]
+    N = w["objects"]
+    threads = os.cpu_count() or 1
+    workload_cfg = {"workload": args.workload, "objects": N, "steps_per_run": args.steps,
+                    "street_grid": "200x200 over 40 km, jitter 20 m", "speed_mps": [1, 15],
+                    "hotspots": w["hot"], "reach_m": w["reach"], "min_meet_steps": w["min_meet"],
+                    "leaf_capacity": w["grid_capacity"], "grid_amplify": w["amplify"],
+                    "meeting_buckets": make_cfg(w).resolved().num_meeting_buckets,
+                    "l2": "inputs and table larger than L2; no flush", "parallelism": f"replicas x{ws}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        steps = args.steps
+        base = cpu_baseline(w, steps, threads,
+                            "oracle C port of the reference CPU path, {steps} full steps after one "
+                            "warm-up step ({seconds} s)")
+        line = {"metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": ws, "steps": steps,
+                "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic (seeded grid-graph traces)", "impl": "reference",
+                "config": workload_cfg, "cpu_baseline": base,
+                "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    r = run_gpu(args, w, rank, local)
+    K = args.steps
+    dev_s = max_over_ranks(args, r["dev_ms"] / 1000.0)
+    e2e_s = max_over_ranks(args, r["wall_e2e"])
+    if rank != 0:
+        return
+    value = N * K * ws / dev_s
+    e2e = N * K * ws / e2e_s
+    s_last = r["stats"][-1]
+    peak, peak_kind = measured_peaks()
+    B = make_cfg(w).resolved().num_meeting_buckets
+    phase_names = ["partition", "border", "refine", "insert", "sweep", "schema"]
+    phase_ms = {nm: sum(s.phase_ms[i] for s in r["stats"]) / K for i, nm in enumerate(phase_names)}
+    kb = {k: sum(kernel_bytes(s, N, B)[k] for s in r["stats"]) / K for k in ("partition", "refine", "sweep")}
+    dom = max(("refine", "sweep", "partition"), key=lambda k: phase_ms[k])
+    achieved = kb[dom] / (phase_ms[dom] / 1e3) / 1e9
+    launches = sum(s.kernel_launches for s in r["stats"])
+    base = None
+    if not args.no_cpu_baseline:
+        base = cpu_baseline(w, args.cpu_steps, threads,
+                            "oracle C port of the reference CPU path, all host threads, {steps} full steps "
+                            "of the same workload after one warm-up step ({seconds} s)")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
+        "ms_per_step": r["dev_ms"] / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded grid-graph traces)", "config": workload_cfg,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 16 * N,
+                "d2h_bytes_per_step": int(r["d2h"] / K)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "algorithmic_bytes": kb[dom], "launch_ms": phase_ms[dom]},
+        "phase_ms": phase_ms,
+        "per_step": {"pair_tests": s_last.pair_tests, "exact_tests": s_last.exact_tests, "hits": s_last.hits,
+                     "new_candidates": s_last.new_candidates, "live_meetings": s_last.taken_buckets,
+                     "emitted": s_last.emitted, "border_units": s_last.border_units, "leaves": s_last.leaves,
+                     "overflow_objects": s_last.overflow_objects, "ambiguous_tests": s_last.ambiguous_tests},
+        "wall_s": {"device_steps": r["wall_dev"], "e2e_steps": r["wall_e2e"]},
+        "clocks": r["clocks"],
+        "cpu_baseline": base,
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

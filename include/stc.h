@@ -97,8 +97,11 @@ typedef struct stc_stats {
   uint64_t emitted;              /* meetings emitted by the step */
   uint64_t pending;              /* emitted meetings not yet drained */
   uint32_t splits, merges;       /* schema updates applied after the step */
+  uint32_t kernel_launches;      /* kernels launched by the step */
+  uint32_t ambiguous_tests;      /* distance decisions within a few ulp of reach, where
+                                    the last bit of sin() could matter */
   float step_ms;                 /* device time of the step */
-  float phase_ms[8];             /* partition, border, refine, insert, sweep, schema, copy-in, other */
+  float phase_ms[8];             /* partition, border+jobs, refine, insert, sweep, schema, copy-in, 0 */
 } stc_stats;
 
 /* Fills *cfg with the reference defaults for n objects (util/config.h:29-41,

@@ -509,7 +509,7 @@ static int refine_unit(oracle_ctx *c, uint64_t u, int atomic_insert, uint64_t *t
         continue;
       }
       slot = (slot + 1) % B;
-      if (++probes > B) return -1;
+      if (++probes > B || probes > (1u << 16)) return -1;  /* table full */
     }
   }
   return 0;
@@ -681,11 +681,11 @@ int oracle_step(oracle_ctx *c, const double *xy, uint32_t t) {
   c->stats.checking_units = c->unit_count;
   c->stats.border_units = c->unit_count - c->N;
   c->stats.overflow_objects = overflow;
-  c->stats.leaves = c->grids_stack_index;
-  c->stats.schema_nodes = c->schema_stack_index;
   if (c->cfg.dynamic_schema) {
     if (update_schema(c)) return -1;
   }
+  c->stats.leaves = c->grids_stack_index;
+  c->stats.schema_nodes = c->schema_stack_index;
   return 0;
 }
 

@@ -31,7 +31,6 @@ CU_SOURCES = [
     "stc_meetings.cu",
     "stc_schema.cu",
     "stc_sort.cu",
-    "stc_lsm.cu",
 ]
 
 

@@ -1,0 +1,386 @@
+// C ABI (include/stc.h): context lifetime and per-step orchestration.
+//
+// One context = one device, one stream, all state resident in HBM. A step
+// launches only device-driven kernels (sizes that depend on the data are read
+// from device memory inside the kernels), then copies the 128-byte control
+// block back once to report counters and errors.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "stc_pipeline.cuh"
+
+using namespace stc;
+
+namespace {
+
+thread_local std::string g_create_error = "no error";
+
+enum Phase { PH_START = 0, PH_COPY, PH_PART, PH_BORDER, PH_REFINE, PH_INSERT, PH_SWEEP, PH_SCHEMA, PH_COUNT };
+
+}  // namespace
+
+struct stc_ctx {
+  stc_config cfg;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[PH_COUNT] = {};
+  std::string err;
+  bool failed = false;
+  bool stepped = false;
+  PipeDev p;
+  DevState *st_host = nullptr;   // pinned mirror
+  double2 *xy_own = nullptr;     // device copy target for host input
+  std::vector<void *> allocs;
+  stc_stats stats;
+  uint32_t last_t = 0;
+};
+
+static const char *error_name(uint32_t e) {
+  switch (e) {
+    case ERR_DESCENT: return "descent reached an invalid quadtree node";
+    case ERR_UNITS: return "border checking units exceed refine_size * num_objects";
+    case ERR_PROBE: return "meeting table probe exceeded the table size (table full)";
+    case ERR_CAND: return "new-meeting candidate capacity exceeded";
+    case ERR_DA: return "ordered insertion exceeded its iteration bound";
+    case ERR_EMIT: return "emit buffer full: drain meetings more often or raise emit_capacity";
+    case ERR_SCHEMA: return "quadtree schema or grid stack exhausted";
+    case ERR_LOOKUP: return "border lookup stack overflow";
+    case ERR_BUILD: return "initial quadtree exceeds schema capacity";
+    case ERR_PASSB: return "inserted meeting not found in pass B";
+    default: return "unknown device error";
+  }
+}
+
+static stc_status status_of(uint32_t e) {
+  switch (e) {
+    case ERR_UNITS: case ERR_PROBE: case ERR_CAND: case ERR_EMIT: case ERR_SCHEMA: case ERR_LOOKUP: case ERR_BUILD:
+      return STC_ERR_CAPACITY;
+    case ERR_DA: return STC_ERR_TIMEOUT;
+    default: return STC_ERR_STATE;
+  }
+}
+
+template <typename T>
+static bool dalloc(stc_ctx *c, T **ptr, size_t count) {
+  size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  void *v = nullptr;
+  cudaError_t e = cudaMalloc(&v, bytes);
+  if (e != cudaSuccess) {
+    char buf[256];
+    snprintf(buf, sizeof(buf), "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+    c->err = buf;
+    *ptr = nullptr;
+    return false;
+  }
+  c->allocs.push_back(v);
+  *ptr = (T *)v;
+  return true;
+}
+
+static stc_status fail(stc_ctx *c, stc_status s, const std::string &msg) {
+  c->err = msg;
+  if (s != STC_ERR_INVALID_ARG) c->failed = true;
+  return s;
+}
+
+static stc_status cuda_fail(stc_ctx *c, cudaError_t e, const char *where) {
+  char buf[256];
+  snprintf(buf, sizeof(buf), "%s: %s", where, cudaGetErrorString(e));
+  return fail(c, STC_ERR_CUDA, buf);
+}
+
+static uint64_t next_pow2(uint64_t v) {
+  uint64_t r = 1;
+  while (r < v) r <<= 1;
+  return r;
+}
+
+extern "C" void stc_config_default(stc_config *cfg, uint32_t n) {
+  if (!cfg) return;
+  memset(cfg, 0, sizeof(*cfg));
+  cfg->num_objects = n;
+  cfg->min_meet_time = 5;
+  cfg->max_meet_time = 4096;
+  cfg->grid_capacity = 50;
+  cfg->grid_amplify = 2.0;
+  cfg->reach_distance = 2.0;
+  cfg->num_meeting_buckets = 2ULL * n;
+  cfg->refine_size = 4;
+  cfg->schema_update_delay = 1;
+  cfg->dynamic_schema = 1;
+  cfg->mbr_filter = 1;
+}
+
+static void destroy_all(stc_ctx *c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (void *v : c->allocs) cudaFree(v);
+  c->allocs.clear();
+  if (c->st_host) cudaFreeHost(c->st_host);
+  for (int i = 0; i < PH_COUNT; i++)
+    if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+extern "C" void stc_destroy(stc_ctx *c) {
+  if (!c) return;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(c->device);
+  destroy_all(c);
+  cudaSetDevice(prev);
+  delete c;
+}
+
+extern "C" const char *stc_last_error(const stc_ctx *c) {
+  if (!c) return g_create_error.c_str();
+  return c->err.empty() ? "no error" : c->err.c_str();
+}
+
+static stc_status read_state(stc_ctx *c, const char *where) {
+  cudaError_t e = cudaMemcpyAsync(c->st_host, c->p.st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, where);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(c, e, where);
+  if (c->st_host->error) {
+    char buf[320];
+    snprintf(buf, sizeof(buf), "%s: %s (code %u, info %u)", where, error_name(c->st_host->error),
+             c->st_host->error, c->st_host->error_info);
+    return fail(c, status_of(c->st_host->error), buf);
+  }
+  return STC_OK;
+}
+
+extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], const double *xy0, uint32_t n,
+                                 stc_ctx **out) {
+  if (out) *out = nullptr;
+  if (!cfg || !mbr || !xy0 || !out) {
+    g_create_error = "stc_create: null argument";
+    return STC_ERR_INVALID_ARG;
+  }
+  const stc_config &k = *cfg;
+  double amp_cap = k.grid_amplify * k.grid_capacity;
+  if (n == 0 || n != k.num_objects || n >= (1u << 31) || k.grid_capacity == 0 || !(k.reach_distance > 0) ||
+      k.num_meeting_buckets == 0 || k.refine_size == 0 || k.schema_update_delay == 0 || !(amp_cap >= 1.0) ||
+      amp_cap >= (double)STC_MAX_LEAF_CAP || !(mbr[2] > mbr[0]) || !(mbr[3] > mbr[1])) {
+    g_create_error = "stc_create: invalid configuration";
+    return STC_ERR_INVALID_ARG;
+  }
+  stc_ctx *c = new (std::nothrow) stc_ctx();
+  if (!c) {
+    g_create_error = "stc_create: out of host memory";
+    return STC_ERR_CAPACITY;
+  }
+  c->cfg = k;
+  c->device = (int)k.device;
+  memset(&c->stats, 0, sizeof(c->stats));
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  for (int i = 0; i < PH_COUNT && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
+  if (e == cudaSuccess) e = cudaMallocHost(&c->st_host, sizeof(DevState));
+  if (e != cudaSuccess) {
+    g_create_error = std::string("stc_create: ") + cudaGetErrorString(e);
+    destroy_all(c);
+    delete c;
+    return STC_ERR_CUDA;
+  }
+
+  PipeDev &p = c->p;
+  memset(&p, 0, sizeof(p));
+  p.N = n;
+  p.leaf_cap = (uint32_t)amp_cap;  // tracing/workbench.cpp:36
+  uint32_t per = n / k.grid_capacity;
+  p.G = 4 * std::max<uint32_t>(100000u, per);  // tracing/workbench.cpp:38
+  p.S = (uint32_t)(1.6 * p.G);                 // tracing/workbench.cpp:41
+  p.B = k.num_meeting_buckets;
+  // every candidate ends in a distinct slot (a claimed empty one or its own
+  // live entry), so B bounds the count; half of it covers any table that is
+  // not already more than half full
+  uint64_t cand_cap = k.candidate_capacity ? k.candidate_capacity : std::max<uint64_t>(1024, p.B / 2);
+  p.cand_cap = cand_cap;
+  p.C = next_pow2(2 * cand_cap);
+  p.E = k.emit_capacity ? k.emit_capacity : std::max<uint64_t>(1u << 20, 4ULL * n);
+  p.U_cap = (uint64_t)k.refine_size * n - n;
+  p.reach = k.reach_distance;
+  p.x_buffer = k.reach_distance * stc_dpml_ref(mbr[1]);  // tracing/filter.cpp:30
+  p.y_buffer = k.reach_distance * stc_dpm_lat();          // tracing/filter.cpp:31
+  p.map_lo_x = mbr[0]; p.map_lo_y = mbr[1]; p.map_hi_x = mbr[2]; p.map_hi_y = mbr[3];
+  p.min_meet_time = k.min_meet_time;
+  p.grid_capacity = k.grid_capacity;
+  p.delay = k.schema_update_delay;
+  p.mbr_filter = k.mbr_filter;
+
+  size_t nu = std::max<size_t>(n, p.U_cap);
+  size_t scan_words = scan_tmp_words(std::max<size_t>({(size_t)n, (size_t)p.G + 1, (size_t)p.S,
+                                                      radix_hist_words(nu)}));
+  bool ok = dalloc(c, &p.st, 1) && dalloc(c, &c->xy_own, n) && dalloc(c, &p.sd.nodes, p.S) &&
+            dalloc(c, &p.sd.meta, p.S) && dalloc(c, &p.sd.schema_stack, p.S) && dalloc(c, &p.sd.grids_stack, p.G) &&
+            dalloc(c, &p.sd.gid_node, p.G) && dalloc(c, &p.sw.bnodes, p.S) && dalloc(c, &p.sw.bmeta, p.S) &&
+            dalloc(c, &p.sw.bcount, p.S) && dalloc(c, &p.sw.bsub_nodes, p.S) &&
+            dalloc(c, &p.sw.bsub_leaves, p.S) && dalloc(c, &p.sw.bpre, p.S) && dalloc(c, &p.sw.bleafbase, p.S) &&
+            dalloc(c, &p.sw.node_of, n) && dalloc(c, &p.sw.ev_flag, p.S) && dalloc(c, &p.sw.ev_pos, p.S) &&
+            dalloc(c, &p.sw.ev_list, p.S) && dalloc(c, &p.sw.old_under, p.S) && dalloc(c, &p.sw.heap, p.S) &&
+            dalloc(c, &p.sw.ev_total, 1) && dalloc(c, &p.sw.queued, p.S) && dalloc(c, &p.leaf_gid, n) &&
+            dalloc(c, &p.lastvalid, n) && dalloc(c, &p.iota, nu) && dalloc(c, &p.sorted_gid, n) &&
+            dalloc(c, &p.sorted_pid, n) && dalloc(c, &p.sort_ktmp, nu) && dalloc(c, &p.sort_vtmp, nu) &&
+            dalloc(c, &p.sort_hist, radix_hist_words(nu)) && dalloc(c, &p.grid_count, (size_t)p.G + 1) &&
+            dalloc(c, &p.grid_start, (size_t)p.G + 1) && dalloc(c, &p.pts, n) && dalloc(c, &p.ptf, n) &&
+            dalloc(c, &p.bcount, (size_t)n + 1) && dalloc(c, &p.boff, (size_t)n + 1) &&
+            dalloc(c, &p.bu_gid, p.U_cap) && dalloc(c, &p.bu_pid, p.U_cap) && dalloc(c, &p.bu_sorted_gid, p.U_cap) &&
+            dalloc(c, &p.bu_sorted_pos, p.U_cap) && dalloc(c, &p.bu_cnt, (size_t)p.G + 1) &&
+            dalloc(c, &p.bu_start, (size_t)p.G + 1) && dalloc(c, &p.job_cnt, (size_t)p.G + 1) &&
+            dalloc(c, &p.job_start, (size_t)p.G + 1) && dalloc(c, &p.slots, p.B) && dalloc(c, &p.cset, p.C) &&
+            dalloc(c, &p.cand_list, p.cand_cap) && dalloc(c, &p.emit, p.E) && dalloc(c, &p.scan_tmp, scan_words) &&
+            dalloc(c, &p.n_dev, 1);
+  if (!ok) {
+    g_create_error = "stc_create: " + c->err;
+    destroy_all(c);
+    delete c;
+    return STC_ERR_CAPACITY;
+  }
+  p.sd.S = p.S;
+  p.sd.G = p.G;
+  p.sw.scan_tmp = p.scan_tmp;
+  cudaStream_t s = c->stream;
+  cudaMemsetAsync(p.st, 0, sizeof(DevState), s);
+  cudaMemsetAsync(p.sw.queued, 0, p.S, s);
+  unsigned long long nn = n;
+  cudaMemcpyAsync(p.n_dev, &nn, sizeof(nn), cudaMemcpyHostToDevice, s);
+  iota_u32(p.iota, nu, s);
+  init_tables(p, s);
+  e = cudaMemcpyAsync(c->xy_own, xy0, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = build_schema(c->xy_own, n, mbr, k.reach_distance, k.grid_capacity, p.sd, p.sw, p.st, c->st_host, s);
+  stc_status rs = STC_OK;
+  if (e != cudaSuccess) rs = cuda_fail(c, e, "stc_create");
+  else rs = read_state(c, "stc_create");
+  if (rs != STC_OK) {
+    g_create_error = c->err;
+    destroy_all(c);
+    delete c;
+    return rs;
+  }
+  c->stats.leaves = c->st_host->grids_stack_index;
+  c->stats.schema_nodes = c->st_host->schema_stack_index;
+  *out = c;
+  return STC_OK;
+}
+
+static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copied) {
+  PipeDev &p = c->p;
+  cudaStream_t s = c->stream;
+  p.xy = xy;
+  unsigned long long launches0 = tl_launches;
+  step_begin(p, s);
+  cudaEventRecord(c->ev[PH_COPY], s);
+  step_partition(p, s);
+  cudaEventRecord(c->ev[PH_PART], s);
+  step_border(p, s);
+  step_jobs(p, s);
+  cudaEventRecord(c->ev[PH_BORDER], s);
+  step_refine(p, t, s);
+  cudaEventRecord(c->ev[PH_REFINE], s);
+  step_insert(p, t, s);
+  cudaEventRecord(c->ev[PH_INSERT], s);
+  step_sweep(p, t, s);
+  cudaEventRecord(c->ev[PH_SWEEP], s);
+  if (c->cfg.dynamic_schema)
+    update_schema(p.sd, p.sw, p.grid_count, p.reach, p.grid_capacity, p.delay, p.st, s);
+  cudaEventRecord(c->ev[PH_SCHEMA], s);
+  stc_status rs = read_state(c, "stc_step");
+  if (rs != STC_OK) return rs;
+  const DevState &h = *c->st_host;
+  stc_stats &o = c->stats;
+  o.step = t;
+  o.leaves = h.grids_stack_index;
+  o.schema_nodes = h.schema_stack_index;
+  o.overflow_objects = h.overflow_objects;
+  o.border_units = h.border_units;
+  o.checking_units = h.border_units + p.N;
+  o.pair_tests = h.tests;
+  o.exact_tests = h.exact_tests;
+  o.hits = h.hits;
+  o.new_candidates = h.cand_count;
+  o.taken_buckets = h.taken;
+  o.emitted = h.step_emitted;
+  o.pending = std::min<unsigned long long>(h.emit_count, p.E);
+  o.splits = h.splits;
+  o.merges = h.merges;
+  float ms[PH_COUNT] = {0};
+  for (int i = PH_COPY; i < PH_COUNT; i++) cudaEventElapsedTime(&ms[i], c->ev[i - 1], c->ev[i]);
+  o.phase_ms[0] = ms[PH_PART];
+  o.phase_ms[1] = ms[PH_BORDER];
+  o.phase_ms[2] = ms[PH_REFINE];
+  o.phase_ms[3] = ms[PH_INSERT];
+  o.phase_ms[4] = ms[PH_SWEEP];
+  o.phase_ms[5] = ms[PH_SCHEMA];
+  o.phase_ms[6] = copied ? ms[PH_COPY] : 0.f;
+  o.phase_ms[7] = 0.f;
+  o.ambiguous_tests = (uint32_t)h.ambiguous;
+  o.kernel_launches = (uint32_t)(tl_launches - launches0);
+  float tot = 0;
+  cudaEventElapsedTime(&tot, c->ev[PH_START], c->ev[PH_SCHEMA]);
+  o.step_ms = tot;
+  c->stepped = true;
+  c->last_t = t;
+  return STC_OK;
+}
+
+extern "C" stc_status stc_step(stc_ctx *c, const double *xy, uint32_t t) {
+  if (!c) return STC_ERR_INVALID_ARG;
+  if (!xy) return fail(c, STC_ERR_INVALID_ARG, "stc_step: null positions");
+  if (c->failed) return STC_ERR_STATE;
+  cudaSetDevice(c->device);
+  cudaEventRecord(c->ev[PH_START], c->stream);
+  cudaError_t e = cudaMemcpyAsync(c->xy_own, xy, (size_t)c->p.N * sizeof(double2), cudaMemcpyHostToDevice,
+                                  c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "stc_step copy-in");
+  return run_step(c, c->xy_own, t, true);
+}
+
+extern "C" stc_status stc_step_device(stc_ctx *c, const double *xy_device, uint32_t t) {
+  if (!c) return STC_ERR_INVALID_ARG;
+  if (!xy_device) return fail(c, STC_ERR_INVALID_ARG, "stc_step_device: null positions");
+  if (c->failed) return STC_ERR_STATE;
+  cudaSetDevice(c->device);
+  cudaEventRecord(c->ev[PH_START], c->stream);
+  return run_step(c, (const double2 *)xy_device, t, false);
+}
+
+extern "C" stc_status stc_get_stats(stc_ctx *c, stc_stats *out) {
+  if (!c || !out) return STC_ERR_INVALID_ARG;
+  *out = c->stats;
+  return STC_OK;
+}
+
+extern "C" stc_status stc_drain_meetings(stc_ctx *c, stc_meeting *out, size_t cap, size_t *n) {
+  if (!c || !n || (!out && cap)) return STC_ERR_INVALID_ARG;
+  *n = 0;
+  cudaSetDevice(c->device);
+  PipeDev &p = c->p;
+  unsigned long long pending = std::min<unsigned long long>(c->st_host->emit_count, p.E);
+  size_t k = (size_t)std::min<unsigned long long>(pending, cap);
+  cudaStream_t s = c->stream;
+  cudaError_t e = cudaSuccess;
+  if (k) e = cudaMemcpyAsync(out, p.emit, k * sizeof(stc_meeting), cudaMemcpyDeviceToHost, s);
+  // shift the rest down in non-overlapping chunks of k records
+  for (size_t src = k; e == cudaSuccess && k && src < pending; src += k) {
+    size_t len = std::min<size_t>(k, pending - src);
+    e = cudaMemcpyAsync(p.emit + (src - k), p.emit + src, len * sizeof(stc_meeting), cudaMemcpyDeviceToDevice, s);
+  }
+  unsigned long long left = pending - k;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&p.st->emit_count, &left, sizeof(left), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "stc_drain_meetings");
+  c->st_host->emit_count = left;
+  c->stats.pending = left;
+  *n = k;
+  return STC_OK;
+}

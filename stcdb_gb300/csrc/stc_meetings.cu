@@ -1,0 +1,264 @@
+// Step kernels (c): ordered insertion of new meetings and the expire/emit
+// sweep of the meeting table.
+//
+// The reference inserts hits one by one in its processing order with linear
+// probing from key % B and clears expired slots without tombstones
+// (tracing/refinement.cpp:37-55, tracing/meeting.cpp:47-67). Which slot a
+// new key lands in -- and therefore whether a later probe for a live meeting
+// crosses a cleared slot and restarts it -- depends on that order. The
+// sequential result is reproduced exactly:
+//
+//   Every candidate key k (distinct per step) walks from k % B over the
+//   table as it stood before the step: slots holding other keys are passed,
+//   a slot holding k itself ends the walk (the meeting is extended there),
+//   and each empty slot is contended. Contention is resolved by priority =
+//   the key's first position in the reference's processing order: a claim
+//   word (key | CLAIM_BIT, priority) is installed with a 128-bit CAS, a
+//   lower priority evicts a higher one, and the evicted key continues its
+//   walk from the next slot. Slots prefer lower priorities and keys prefer
+//   earlier slots, so this deferred acceptance converges to the unique stable
+//   assignment, which is exactly what inserting the keys one by one in
+//   priority order produces.
+//
+// After the claims settle, pass B writes start/end/MBR of every candidate's
+// final slot, and the sweep turns claims into plain keys, keeps active
+// meetings, emits finished ones whose duration reaches min_meet_time
+// (tracing/meeting.cpp:59, plus the map-box filter of cuda/geometry.cu:667)
+// and clears the rest.
+#include "stc_pipeline.cuh"
+
+namespace stc {
+
+__global__ void k_step_begin(DevState *st) {
+  st->error = 0;
+  st->error_info = 0;
+  st->border_units = 0;
+  st->jobs_total = 0;
+  st->job_next = 0;
+  st->cand_count = 0;
+  st->tests = st->exact_tests = st->hits = st->ambiguous = 0;
+  st->taken = 0;
+  st->step_emitted = 0;
+  st->da_iters = 0;
+  st->splits = st->merges = st->events = 0;
+  st->overflow_objects = 0;
+}
+
+void step_begin(PipeDev &p, cudaStream_t s) { STC_KL k_step_begin<<<1, 1, 0, s>>>(p.st); }
+
+__global__ void k_init_slots(Slot *slots, unsigned long long B) {
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < B;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    Slot s;
+    s.key = STC_EMPTY_KEY;
+    s.start = 0xFFFFFFFFu;
+    s.end = 0xFFFFFFFFu;
+    s.lo_x = STC_INIT_LO; s.lo_y = STC_INIT_LO; s.hi_x = STC_INIT_HI; s.hi_y = STC_INIT_HI;
+    slots[i] = s;
+  }
+}
+
+__global__ void k_init_cands(Cand *c, unsigned long long C) {
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < C;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    Cand x;
+    x.key = STC_EMPTY_KEY;
+    x.order = ~0ULL;
+    x.lo_x = STC_INIT_LO; x.lo_y = STC_INIT_LO; x.hi_x = STC_INIT_HI; x.hi_y = STC_INIT_HI;
+    c[i] = x;
+  }
+}
+
+void init_tables(PipeDev &p, cudaStream_t s) {
+  STC_KL k_init_slots<<<STC_NUM_SMS * 8, 256, 0, s>>>(p.slots, p.B);
+  STC_KL k_init_cands<<<STC_NUM_SMS * 8, 256, 0, s>>>(p.cset, p.C);
+}
+
+__device__ __forceinline__ U128 load_pair(const Slot *s) {
+  U128 v;
+  v.lo = *(volatile const unsigned long long *)&s->key;
+  v.hi = *(volatile const unsigned long long *)&s->start;
+  return v;
+}
+
+// Ordered insertion (deferred acceptance, see the file comment).
+__global__ void k_insert_ordered(PipeDev p) {
+  const unsigned long long nc = p.st->cand_count < p.cand_cap ? p.st->cand_count : p.cand_cap;
+  const unsigned long long limit = STC_PROBE_LIMIT * 4;
+  for (unsigned long long c = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
+       c += (unsigned long long)gridDim.x * blockDim.x) {
+    const Cand *cd = &p.cset[p.cand_list[c]];
+    unsigned long long key = cd->key, prio = cd->order;
+    unsigned long long slot = key % p.B;
+    unsigned long long steps = 0;
+    bool done = false;
+    if (stc_failed(p.st)) return;
+    while (!done) {
+      if (++steps > limit) {
+        stc_set_error(p.st, ERR_DA, (uint32_t)c);
+        return;
+      }
+      Slot *s = &p.slots[slot];
+      U128 cur = load_pair(s);
+      if (cur.lo == key) break;  // its own live entry: extended in pass B
+      if (cur.lo != STC_EMPTY_KEY && !(cur.lo & STC_CLAIM_BIT)) {
+        slot = slot + 1 == p.B ? 0 : slot + 1;
+        continue;
+      }
+      // contended empty slot
+      while (true) {
+        if (cur.lo == STC_EMPTY_KEY) {
+          U128 want = {key | STC_CLAIM_BIT, prio};
+          U128 old = atomicCAS((U128 *)s, cur, want);
+          if (old.lo == cur.lo && old.hi == cur.hi) {
+            done = true;
+            break;
+          }
+          cur = old;
+          continue;
+        }
+        // claimed by another key
+        unsigned long long other_prio = cur.hi;
+        if (prio < other_prio) {
+          U128 want = {key | STC_CLAIM_BIT, prio};
+          U128 old = atomicCAS((U128 *)s, cur, want);
+          if (old.lo == cur.lo && old.hi == cur.hi) {
+            // carry the evicted key onward
+            key = cur.lo & ~STC_CLAIM_BIT;
+            prio = other_prio;
+            slot = slot + 1 == p.B ? 0 : slot + 1;
+            break;
+          }
+          cur = old;
+          continue;
+        }
+        slot = slot + 1 == p.B ? 0 : slot + 1;  // lost this slot
+        break;
+      }
+    }
+    if (steps > 1) atomicAdd(&p.st->da_iters, steps - 1);
+  }
+}
+
+// Pass B: write the step's state into every candidate's final slot.
+__global__ void k_pass_b(PipeDev p, uint32_t t) {
+  const unsigned long long nc = p.st->cand_count < p.cand_cap ? p.st->cand_count : p.cand_cap;
+  for (unsigned long long c = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
+       c += (unsigned long long)gridDim.x * blockDim.x) {
+    if (stc_failed(p.st)) return;
+    Cand cd = p.cset[p.cand_list[c]];
+    unsigned long long slot = cd.key % p.B;
+    bool found = false;
+    for (unsigned long long probe = 0; probe < STC_PROBE_LIMIT * 4 && probe < p.B; probe++) {
+      Slot *s = &p.slots[slot];
+      unsigned long long k = s->key;
+      if (k == (cd.key | STC_CLAIM_BIT)) {
+        // new meeting: start = end = t, MBR = init then both points (cuda/geometry.cu:480-489)
+        s->start = t;
+        s->end = t;
+        s->lo_x = fminf(STC_INIT_LO, cd.lo_x);
+        s->lo_y = fminf(STC_INIT_LO, cd.lo_y);
+        s->hi_x = fmaxf(STC_INIT_HI, cd.hi_x);
+        s->hi_y = fmaxf(STC_INIT_HI, cd.hi_y);
+        found = true;
+        break;
+      }
+      if (k == cd.key) {  // extended
+        s->end = t;
+        s->lo_x = fminf(s->lo_x, cd.lo_x);
+        s->lo_y = fminf(s->lo_y, cd.lo_y);
+        s->hi_x = fmaxf(s->hi_x, cd.hi_x);
+        s->hi_y = fmaxf(s->hi_y, cd.hi_y);
+        found = true;
+        break;
+      }
+      slot = slot + 1 == p.B ? 0 : slot + 1;
+    }
+    if (!found) stc_set_error(p.st, ERR_PASSB, (uint32_t)c);
+  }
+}
+
+__global__ void k_cand_reset(PipeDev p) {
+  const unsigned long long nc = p.st->cand_count < p.cand_cap ? p.st->cand_count : p.cand_cap;
+  for (unsigned long long c = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
+       c += (unsigned long long)gridDim.x * blockDim.x) {
+    Cand x;
+    x.key = STC_EMPTY_KEY;
+    x.order = ~0ULL;
+    x.lo_x = STC_INIT_LO; x.lo_y = STC_INIT_LO; x.hi_x = STC_INIT_HI; x.hi_y = STC_INIT_HI;
+    p.cset[p.cand_list[c]] = x;
+  }
+}
+
+void step_insert(PipeDev &p, uint32_t t, cudaStream_t s) {
+  STC_KL k_insert_ordered<<<STC_NUM_SMS * 8, 256, 0, s>>>(p);
+  STC_KL k_pass_b<<<STC_NUM_SMS * 8, 256, 0, s>>>(p, t);
+  STC_KL k_cand_reset<<<STC_NUM_SMS * 8, 256, 0, s>>>(p);
+}
+
+// Sweep (tracing/meeting.cpp:32-76, cuda/geometry.cu:595-736).
+__global__ void __launch_bounds__(256) k_sweep(PipeDev p, uint32_t t) {
+  const uint32_t lane = lane_id();
+  unsigned long long active = 0;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  const unsigned long long B = p.B;
+  // iterate so that whole warps stay converged for the ballot
+  for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < B;
+       base += stride) {
+    unsigned long long i = base + lane;
+    bool emit = false;
+    Slot s;
+    if (i < B) {
+      s = p.slots[i];
+      if (s.key != STC_EMPTY_KEY) {
+        if (s.key & STC_CLAIM_BIT) {
+          p.slots[i].key = s.key & ~STC_CLAIM_BIT;  // new meeting of this step
+          active++;
+        } else if (s.end == t) {
+          active++;
+        } else {
+          if (t - s.start >= p.min_meet_time + 1) {
+            emit = !p.mbr_filter ||
+                   ((double)s.lo_x >= p.map_lo_x && (double)s.hi_x <= p.map_hi_x &&
+                    (double)s.lo_y >= p.map_lo_y && (double)s.hi_y <= p.map_hi_y);
+          }
+          Slot e;
+          e.key = STC_EMPTY_KEY;
+          e.start = 0xFFFFFFFFu;
+          e.end = 0xFFFFFFFFu;
+          e.lo_x = STC_INIT_LO; e.lo_y = STC_INIT_LO; e.hi_x = STC_INIT_HI; e.hi_y = STC_INIT_HI;
+          p.slots[i] = e;
+        }
+      }
+    }
+    uint32_t ball = __ballot_sync(0xffffffffu, emit);
+    if (ball) {
+      unsigned long long basepos = 0;
+      if (lane == 0) basepos = atomicAdd(&p.st->emit_count, (unsigned long long)__popc(ball));
+      basepos = __shfl_sync(0xffffffffu, basepos, 0);
+      if (emit) {
+        unsigned long long pos = basepos + __popc(ball & ((1u << lane) - 1u));
+        if (pos < p.E) {
+          stc_meeting m;
+          cantor_decode(s.key, &m.pid_lo, &m.pid_hi);
+          m.start = s.start;
+          m.end = s.end;
+          m.mbr[0] = s.lo_x; m.mbr[1] = s.lo_y; m.mbr[2] = s.hi_x; m.mbr[3] = s.hi_y;
+          p.emit[pos] = m;
+        } else {
+          stc_set_error(p.st, ERR_EMIT, (uint32_t)(pos - p.E));
+        }
+      }
+      if (lane == 0) atomicAdd(&p.st->step_emitted, (unsigned long long)__popc(ball));
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) active += __shfl_xor_sync(0xffffffffu, active, o);
+  if (lane == 0 && active) atomicAdd(&p.st->taken, active);
+}
+
+void step_sweep(PipeDev &p, uint32_t t, cudaStream_t s) {
+  STC_KL k_sweep<<<STC_NUM_SMS * 16, 256, 0, s>>>(p, t);
+}
+
+}  // namespace stc

@@ -1,0 +1,204 @@
+// Step kernels (a): quadtree partitioning of one step's positions.
+//
+//   k_descend   phased descent of every point to its leaf, tracking the
+//               deepest ancestor whose box keeps the point away from its top
+//               and right border (tracing/filter.cpp:228-243); leaf histogram
+//   sort        stable radix sort of pids by leaf id: leaf member lists in pid
+//               order, exactly the order the reference's single-threaded
+//               insert fills grids[] (tracing/filter.cpp:95-111)
+//   k_gather    leaf-ordered copy of the points as fp32 offsets from the leaf
+//               corner (for the refinement pre-filter) and fp32 lon/lat (MBR)
+//   k_border    depth-first lookup of the top/right leaves within reach of a
+//               border point (tracing/filter.cpp:130-152), counted then filled
+//               in the reference's unit order (pid, then DFS order)
+//   k_jobs      per-leaf work tiles for the refinement
+#include "stc_pipeline.cuh"
+
+namespace stc {
+
+static inline unsigned nblk(size_t n, unsigned t = 256) { return (unsigned)((n + t - 1) / t); }
+
+__device__ __forceinline__ double dpml_fast_d(double lat) {
+  double absla = fabs(lat);
+  if (absla == 90) absla = 89;
+  double arg = RN_DIV(RN_MUL(RN_SUB(90.0, absla), STC_REF_PI), 180.0);
+  return RN_DIV(360.0, RN_MUL(RN_MUL(sin(arg), 40076.0), 1000.0));
+}
+
+__global__ void k_descend(PipeDev p) {
+  uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pid >= p.N) return;
+  double2 q = p.xy[pid];
+  uint32_t cur = 0, lv = 0;
+  NodeMeta m = p.sd.meta[0];
+  if (m.type != NODE_LEAF) {
+    int d = 0;
+    for (; d < STC_MAX_DEPTH; d++) {
+      const Node *n = &p.sd.nodes[cur];
+      int child = (q.y > n->mid_y) * 2 + (q.x > n->mid_x);
+      cur = n->child[child];
+      m = p.sd.meta[cur];
+      if (m.type == NODE_INVALID) {
+        stc_set_error(p.st, ERR_DESCENT, pid);
+        return;
+      }
+      const Node *c = &p.sd.nodes[cur];
+      if (RN_ADD(q.x, p.x_buffer) < c->hi_x && RN_ADD(q.y, p.y_buffer) < c->hi_y) lv = cur;
+      if (m.type == NODE_LEAF) break;
+    }
+    if (d == STC_MAX_DEPTH) {
+      stc_set_error(p.st, ERR_DESCENT, pid);
+      return;
+    }
+  }
+  p.leaf_gid[pid] = m.grid_id;
+  p.lastvalid[pid] = lv != cur ? lv : STC_NONE;
+  atomicAdd(&p.grid_count[m.grid_id], 1u);
+}
+
+__global__ void k_gather(PipeDev p) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.N) return;
+  uint32_t pid = p.sorted_pid[i];
+  uint32_t g = p.sorted_gid[i];
+  const Node *o = &p.sd.nodes[p.sd.gid_node[g]];
+  double2 q = p.xy[pid];
+  float lx = __double2float_rn(RN_SUB(q.x, o->lo_x));
+  float ly = __double2float_rn(RN_SUB(q.y, o->lo_y));
+  p.pts[i] = make_float4(lx, ly, metres_per_deg_lon_f(q.y), __uint_as_float(pid));
+  p.ptf[i] = make_float2(__double2float_rn(q.x), __double2float_rn(q.y));
+}
+
+// box::distance(p, geography=true) <= reach (geometry/geometry.h:174-185).
+// The containment test and the degree offsets are the reference's exact fp64
+// expressions (additions and halvings only); the metric step is classified in
+// fp32 with a relative error below 24 u (u = 2^-24: two roundings of the
+// offsets, the scale factor from sinf, products and sum), so only a band of
+// +-64 u around reach falls through to the reference's fp64 division and
+// square root, and within 1e-12 of reach to the correctly rounded sine.
+__device__ __forceinline__ bool box_within(const Node &c, double x, double y, double reach, float reach_f,
+                                           float s_lon, double dp_fast) {
+  if (x >= c.lo_x && x <= c.hi_x && y >= c.lo_y && y <= c.hi_y) return true;  // distance 0
+  double dx = RN_SUB(fabs(RN_SUB(x, RN_MUL(RN_ADD(c.lo_x, c.hi_x), 0.5))), RN_MUL(RN_SUB(c.hi_x, c.lo_x), 0.5));
+  double dy = RN_SUB(fabs(RN_SUB(y, RN_MUL(RN_ADD(c.lo_y, c.hi_y), 0.5))), RN_MUL(RN_SUB(c.hi_y, c.lo_y), 0.5));
+  if (dx < 0.0) dx = 0.0;
+  if (dy < 0.0) dy = 0.0;
+  float fx = __double2float_rn(dx) * s_lon, fy = __double2float_rn(dy) * STC_SLAT_F;
+  float d2 = fx * fx + fy * fy;
+  const float lo = reach_f * (1.0f - 64.0f * 5.9604645e-08f), hi = reach_f * (1.0f + 64.0f * 5.9604645e-08f);
+  if (d2 <= lo * lo) return true;
+  if (d2 >= hi * hi) return false;
+  double d = stc_box_distance_ref(c.lo_x, c.lo_y, c.hi_x, c.hi_y, x, y, dp_fast);
+  if (fabs(d - reach) > 1e-12 * reach) return d <= reach;
+  return stc_box_distance_ref(c.lo_x, c.lo_y, c.hi_x, c.hi_y, x, y, stc_dpml_ref(y)) <= reach;
+}
+
+#define LOOKUP_STACK 64
+
+template <bool FILL>
+__global__ void k_border(PipeDev p) {
+  uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pid >= p.N) return;
+  uint32_t lv = p.lastvalid[pid];
+  if (lv == STC_NONE) {
+    if (!FILL) p.bcount[pid] = 0;
+    return;
+  }
+  double2 q = p.xy[pid];
+  double dpf = dpml_fast_d(q.y);
+  float s_lon = metres_per_deg_lon_f(q.y);
+  float reach_f = (float)p.reach;
+  uint32_t stk[LOOKUP_STACK];
+  uint8_t nxt[LOOKUP_STACK];
+  int sp = 1;
+  stk[0] = lv;
+  nxt[0] = 0;
+  uint32_t cnt = 0;
+  unsigned long long base = FILL ? p.boff[pid] : 0ULL;
+  while (sp > 0) {
+    int i = nxt[sp - 1];
+    if (i == 4) {
+      sp--;
+      continue;
+    }
+    nxt[sp - 1] = (uint8_t)(i + 1);
+    uint32_t ch = p.sd.nodes[stk[sp - 1]].child[i];
+    Node c = p.sd.nodes[ch];
+    NodeMeta cm = p.sd.meta[ch];
+    if (!box_within(c, q.x, q.y, p.reach, reach_f, s_lon, dpf)) continue;
+    if (cm.type == NODE_LEAF) {
+      // the leaf lies above, or to the right within the point's row
+      if (q.y < c.lo_y || (q.y < c.hi_y && q.x < c.lo_x)) {
+        if (FILL) {
+          unsigned long long at = base + cnt;
+          if (at < p.U_cap) {
+            p.bu_gid[at] = cm.grid_id;
+            p.bu_pid[at] = pid;
+            atomicAdd(&p.bu_cnt[cm.grid_id], 1u);
+          }
+        }
+        cnt++;
+      }
+    } else {
+      if (sp == LOOKUP_STACK) {
+        stc_set_error(p.st, ERR_LOOKUP, pid);
+        return;
+      }
+      stk[sp] = ch;
+      nxt[sp] = 0;
+      sp++;
+    }
+  }
+  if (!FILL) p.bcount[pid] = cnt;
+}
+
+__global__ void k_check_units(PipeDev p) {
+  if (p.st->border_units >= p.U_cap) stc_set_error(p.st, ERR_UNITS, (uint32_t)p.st->border_units);
+}
+
+__global__ void k_jobs(PipeDev p) {
+  uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g > p.G) return;
+  if (g == p.G) {
+    p.job_cnt[g] = 0;
+    return;
+  }
+  uint32_t cnt = p.grid_count[g];
+  uint32_t n = cnt < p.leaf_cap ? cnt : p.leaf_cap;
+  if (cnt > p.leaf_cap) atomicAdd(&p.st->overflow_objects, cnt - p.leaf_cap);
+  uint32_t m = p.bu_cnt[g];
+  uint32_t R = (n + 31) / 32;
+  uint32_t jobs = n ? R * (R + 1) / 2 + ((m + 31) / 32) * R : 0;
+  p.job_cnt[g] = jobs;
+}
+
+void step_partition(PipeDev &p, cudaStream_t s) {
+  cudaMemsetAsync(p.grid_count, 0, (size_t)(p.G + 1) * sizeof(uint32_t), s);
+  STC_KL k_descend<<<nblk(p.N), 256, 0, s>>>(p);
+  int bits = 1;
+  while ((1u << bits) < p.G && bits < 32) bits++;
+  radix_sort_u32(p.leaf_gid, p.iota, p.sorted_gid, p.sorted_pid, p.sort_ktmp, p.sort_vtmp, p.n_dev, p.N, bits,
+                 p.sort_hist, p.scan_tmp, s);
+  exclusive_scan_u32(p.grid_count, p.grid_start, (size_t)p.G + 1, nullptr, p.scan_tmp, s);
+  STC_KL k_gather<<<nblk(p.N), 256, 0, s>>>(p);
+}
+
+void step_border(PipeDev &p, cudaStream_t s) {
+  cudaMemsetAsync(p.bu_cnt, 0, (size_t)(p.G + 1) * sizeof(uint32_t), s);
+  STC_KL k_border<false><<<nblk(p.N, 128), 128, 0, s>>>(p);
+  exclusive_scan_u32(p.bcount, p.boff, p.N, &p.st->border_units, p.scan_tmp, s);
+  STC_KL k_check_units<<<1, 1, 0, s>>>(p);
+  STC_KL k_border<true><<<nblk(p.N, 128), 128, 0, s>>>(p);
+  int bits = 1;
+  while ((1u << bits) < p.G && bits < 32) bits++;
+  radix_sort_u32(p.bu_gid, p.iota, p.bu_sorted_gid, p.bu_sorted_pos, p.sort_ktmp, p.sort_vtmp,
+                 &p.st->border_units, p.U_cap, bits, p.sort_hist, p.scan_tmp, s);
+  exclusive_scan_u32(p.bu_cnt, p.bu_start, (size_t)p.G + 1, nullptr, p.scan_tmp, s);
+}
+
+void step_jobs(PipeDev &p, cudaStream_t s) {
+  STC_KL k_jobs<<<nblk((size_t)p.G + 1), 256, 0, s>>>(p);
+  exclusive_scan_u32(p.job_cnt, p.job_start, (size_t)p.G + 1, &p.st->jobs_total, p.scan_tmp, s);
+}
+
+}  // namespace stc

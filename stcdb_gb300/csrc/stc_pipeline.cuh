@@ -1,0 +1,58 @@
+// Device buffers of one pipeline context and the per-step launchers.
+#pragma once
+#include "stc_common.cuh"
+#include "stc_schema.cuh"
+
+namespace stc {
+
+struct PipeDev {
+  // sizes
+  uint32_t N, leaf_cap, G, S;
+  unsigned long long B;            // meeting table slots
+  unsigned long long C;            // candidate set slots (power of two)
+  unsigned long long cand_cap;     // candidate list capacity
+  unsigned long long E;            // emit buffer capacity
+  unsigned long long U_cap;        // border units (refine_size*N - N - 1)
+  // parameters
+  double reach, x_buffer, y_buffer;
+  double map_lo_x, map_lo_y, map_hi_x, map_hi_y;
+  uint32_t min_meet_time, grid_capacity, delay;
+  int mbr_filter;
+  // state
+  DevState *st;
+  SchemaDev sd;
+  SchemaWork sw;
+  const double2 *xy;               // positions of the current step
+  // partition
+  uint32_t *leaf_gid, *lastvalid, *iota, *sorted_gid, *sorted_pid, *sort_ktmp, *sort_vtmp, *sort_hist;
+  uint32_t *grid_count, *grid_start;   // G, G+1
+  float4 *pts;                          // N sorted: lx, ly, metres/deg lon, pid bits
+  float2 *ptf;                          // N sorted: float lon, lat
+  // border units
+  uint32_t *bcount, *boff;              // N+1
+  uint32_t *bu_gid, *bu_pid;            // U_cap (rank order)
+  uint32_t *bu_sorted_gid, *bu_sorted_pos;  // U_cap grouped by leaf
+  uint32_t *bu_cnt, *bu_start;          // G+1
+  uint32_t *job_cnt, *job_start;        // G+1
+  // meetings
+  Slot *slots;                          // B
+  Cand *cset;                           // C
+  uint32_t *cand_list;                  // cand_cap
+  stc_meeting *emit;                    // E
+  uint32_t *scan_tmp;
+  unsigned long long *n_dev;            // device copy of N (for radix sort)
+};
+
+// stc_partition.cu
+void step_partition(PipeDev &p, cudaStream_t s);
+void step_border(PipeDev &p, cudaStream_t s);
+void step_jobs(PipeDev &p, cudaStream_t s);
+// stc_refine.cu
+void step_refine(PipeDev &p, uint32_t t, cudaStream_t s);
+// stc_meetings.cu
+void step_insert(PipeDev &p, uint32_t t, cudaStream_t s);
+void step_sweep(PipeDev &p, uint32_t t, cudaStream_t s);
+void init_tables(PipeDev &p, cudaStream_t s);
+void step_begin(PipeDev &p, cudaStream_t s);
+
+}  // namespace stc

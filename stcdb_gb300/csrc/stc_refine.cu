@@ -1,0 +1,263 @@
+// Step kernel (b): proximity refinement fused with the first pass of the
+// meeting-table insert.
+//
+// Work tiles: for every leaf with n kept members (the first leaf_cap in pid
+// order, tracing/filter.cpp:100-104) the own-leaf pairs i < j form the upper
+// triangle of a 32 x 32 tiling, and the border units that target the leaf
+// (pid outside the leaf, tracing/filter.cpp:248-259) form extra row tiles
+// against all members. One warp runs one tile: rows in lanes, the 32 column
+// points broadcast with shuffles.
+//
+// Distance decisions equal the reference's fp64 test
+// `p1->distance(p2, true) <= reach` (tracing/refinement.cpp:30-33,
+// geometry/geometry.h:40-48). Each pair is first classified in fp32 from the
+// points' offsets to the leaf corner; the classification is conservative by
+// construction (error bound below), and only pairs inside the uncertainty
+// band are recomputed with the reference's exact fp64 expression.
+//
+// Error bound of the fp32 estimate d_f of the reference distance d, with
+// u = 2^-24, X = |x - corner| <= mx (degrees lon), Y <= my (degrees lat):
+//   offsets round with |err| <= u X, so dx picks up <= 2 u mx degrees and dy
+//   <= 2 u my; the rest (subtraction, scale factor from sinf, products, sum)
+//   is relative and below 30 u. Hence
+//     |d_f - d| <= 30 u d + 2.1 u (2 mx SMAX + 2 my SLAT) = 30 u d + E.
+//   A pair is accepted when d_f^2 <= (r - delta)^2 and rejected when
+//   d_f^2 >= (r + delta)^2 with delta = 4E + 64 u r + 1e-6 r, which leaves
+//   slack for the rounding of the squared thresholds themselves.
+//
+// Hits (tracing/refinement.cpp:34-55) probe the meeting table from
+// key % B. A key found before the first empty slot is extended in place
+// (end = t, MBR); every other key becomes a candidate for the ordered insert
+// of stc_meetings.cu, keyed with its first position in the reference's
+// sequential processing order: unit rank << 24 | member index.
+#include "stc_pipeline.cuh"
+
+namespace stc {
+
+static constexpr int REFINE_THREADS = 256;
+static constexpr unsigned long long JOB_CHUNK = 8;
+
+__device__ __forceinline__ double dpml_fast_r(double lat) {
+  double absla = fabs(lat);
+  if (absla == 90) absla = 89;
+  double arg = RN_DIV(RN_MUL(RN_SUB(90.0, absla), STC_REF_PI), 180.0);
+  return RN_DIV(360.0, RN_MUL(RN_MUL(sin(arg), 40076.0), 1000.0));
+}
+
+// Reference distance decision for p1 (whose latitude sets the scale) and p2.
+__device__ bool exact_within(const PipeDev &p, uint32_t pid1, uint32_t pid2, unsigned long long &amb) {
+  double2 a = p.xy[pid1], b = p.xy[pid2];
+  double d = stc_distance_ref(a.x, a.y, b.x, b.y, dpml_fast_r(a.y));
+  if (fabs(d - p.reach) > 1e-12 * p.reach) return d <= p.reach;
+  d = stc_distance_ref(a.x, a.y, b.x, b.y, stc_dpml_ref(a.y));
+  // within a few ulp of reach the decision depends on the last bit of sin()
+  if (fabs(d - p.reach) <= 8.0 * 2.220446049250313e-16 * p.reach) amb++;
+  return d <= p.reach;
+}
+
+__device__ void cand_insert(const PipeDev &p, unsigned long long key, unsigned long long order, float lox, float loy,
+                            float hix, float hiy) {
+  unsigned long long h = mix64(key) & (p.C - 1);
+  for (unsigned long long probe = 0; probe < STC_PROBE_LIMIT; probe++) {
+    Cand *c = &p.cset[h];
+    unsigned long long k = *(volatile unsigned long long *)&c->key;
+    if (k == STC_EMPTY_KEY) {
+      // the list bounds the set's load factor at cand_cap / C <= 1/2
+      if (*(volatile unsigned long long *)&p.st->cand_count >= p.cand_cap) {
+        stc_set_error(p.st, ERR_CAND, 0u);
+        return;
+      }
+      k = atomicCAS(&c->key, STC_EMPTY_KEY, key);
+      if (k == STC_EMPTY_KEY) {
+        unsigned long long n = agg_inc(&p.st->cand_count);
+        if (n < p.cand_cap) p.cand_list[n] = (uint32_t)h;
+        else stc_set_error(p.st, ERR_CAND, (uint32_t)n);
+        k = key;
+      }
+    }
+    if (k == key) {
+      atomicMin(&c->order, order);
+      if (lox < c->lo_x) atomic_min_f(&c->lo_x, lox);
+      if (loy < c->lo_y) atomic_min_f(&c->lo_y, loy);
+      if (hix > c->hi_x) atomic_max_f(&c->hi_x, hix);
+      if (hiy > c->hi_y) atomic_max_f(&c->hi_y, hiy);
+      return;
+    }
+    h = (h + 1) & (p.C - 1);
+  }
+  stc_set_error(p.st, ERR_CAND, 0xFFFFFFFFu);
+}
+
+__device__ void hit_a(const PipeDev &p, uint32_t a, uint32_t b, unsigned long long order, float2 fa, float2 fb,
+                      uint32_t t) {
+  uint32_t p1 = a < b ? a : b, p2 = a < b ? b : a;
+  unsigned long long key = stc_cantor(p1, p2);
+  float lox = fminf(fa.x, fb.x), loy = fminf(fa.y, fb.y);
+  float hix = fmaxf(fa.x, fb.x), hiy = fmaxf(fa.y, fb.y);
+  unsigned long long slot = key % p.B;
+  for (unsigned long long probe = 0; probe < STC_PROBE_LIMIT && probe < p.B; probe++) {
+    Slot *s = &p.slots[slot];
+    unsigned long long k = s->key;
+    if (k == key) {  // tracing/refinement.cpp:40-42 (+ MBR, cuda/geometry.cu:474-478)
+      s->end = t;
+      if (lox < s->lo_x) atomic_min_f(&s->lo_x, lox);
+      if (loy < s->lo_y) atomic_min_f(&s->lo_y, loy);
+      if (hix > s->hi_x) atomic_max_f(&s->hi_x, hix);
+      if (hiy > s->hi_y) atomic_max_f(&s->hi_y, hiy);
+      return;
+    }
+    if (k == STC_EMPTY_KEY) {
+      cand_insert(p, key, order, lox, loy, hix, hiy);
+      return;
+    }
+    slot = slot + 1 == p.B ? 0 : slot + 1;
+  }
+  stc_set_error(p.st, ERR_PROBE, (uint32_t)(key % p.B));
+}
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+struct Counters {
+  unsigned long long tests, exact, hits, amb;
+};
+
+// One 32x32 tile. Rows: own members (own=true) or border units.
+__device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtile, uint32_t coltile, uint32_t n,
+                         uint32_t t, Counters &ct) {
+  const uint32_t lane = lane_id();
+  const uint32_t base = p.grid_start[g];
+  // column points
+  uint32_t j = coltile * 32 + lane;
+  bool vc = j < n;
+  float4 cp = vc ? p.pts[base + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+  // row points
+  float4 rp;
+  float2 rf = make_float2(0.f, 0.f);
+  uint32_t pid1 = 0;
+  unsigned long long rank = 0;
+  uint32_t i = rowtile * 32 + lane;
+  bool vr;
+  if (own) {
+    vr = i < n;
+    rp = vr ? p.pts[base + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    pid1 = __float_as_uint(rp.w);
+    rank = pid1;  // own-leaf unit of pid1 is grid_check[pid1] (tracing/filter.cpp:107-109)
+  } else {
+    uint32_t ub = p.bu_start[g], ue = p.bu_start[g + 1];
+    uint32_t r = ub + i;
+    vr = r < ue;
+    rp = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (vr) {
+      uint32_t pos = p.bu_sorted_pos[r];
+      pid1 = p.bu_pid[pos];
+      rank = (unsigned long long)p.N + pos;  // border units follow the N own units
+      const Node *o = &p.sd.nodes[p.sd.gid_node[g]];
+      double2 q = p.xy[pid1];
+      rp = make_float4(__double2float_rn(RN_SUB(q.x, o->lo_x)), __double2float_rn(RN_SUB(q.y, o->lo_y)),
+                       metres_per_deg_lon_f(q.y), 0.f);
+      rf = make_float2(__double2float_rn(q.x), __double2float_rn(q.y));
+    }
+  }
+  // tile error margin
+  float mx = warp_max(fmaxf(fabsf(rp.x), fabsf(cp.x)));
+  float my = warp_max(fmaxf(fabsf(rp.y), fabsf(cp.y)));
+  const float u = 5.9604645e-08f;
+  const float r = (float)p.reach;
+  float E = 2.1f * u * (2.0f * mx * STC_SMAX_F + 2.0f * my * STC_SLAT_F);
+  float delta = 4.0f * E + 64.0f * u * r + 1e-6f * r;
+  float lo = fmaxf(r - delta, 0.0f);
+  float lo2 = lo * lo;
+  float hi2 = (r + delta) * (r + delta);
+  bool have_rf = !own;
+  uint32_t kmax = n - coltile * 32;
+  if (kmax > 32) kmax = 32;
+  for (uint32_t k = 0; k < kmax; k++) {
+    float cx = __shfl_sync(0xffffffffu, cp.x, k);
+    float cy = __shfl_sync(0xffffffffu, cp.y, k);
+    uint32_t cpid = __shfl_sync(0xffffffffu, __float_as_uint(cp.w), k);
+    uint32_t jj = coltile * 32 + k;
+    if (!vr || (own && jj <= i)) continue;  // tracing/refinement.cpp:30
+    float dx = (rp.x - cx) * rp.z;
+    float dy = (rp.y - cy) * STC_SLAT_F;
+    float d2 = dx * dx + dy * dy;
+    ct.tests++;
+    bool hit = d2 <= lo2;
+    if (!hit && d2 < hi2) {
+      ct.exact++;
+      hit = exact_within(p, pid1, cpid, ct.amb);
+    }
+    if (hit) {
+      ct.hits++;
+      if (!have_rf) {
+        rf = p.ptf[base + i];
+        have_rf = true;
+      }
+      float2 cf = p.ptf[base + jj];
+      hit_a(p, pid1, cpid, (rank << STC_ORDER_SHIFT) | jj, rf, cf, t);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(REFINE_THREADS) k_refine_a(PipeDev p, uint32_t t) {
+  const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+  const unsigned long long J = p.st->jobs_total;
+  Counters ct = {0, 0, 0, 0};
+  for (unsigned long long chunk = warp; chunk * JOB_CHUNK < J; chunk += nwarps) {
+    if (stc_failed(p.st)) break;  // uniform per warp: every lane reads the same flag
+    unsigned long long j0 = chunk * JOB_CHUNK;
+    unsigned long long j1 = j0 + JOB_CHUNK < J ? j0 + JOB_CHUNK : J;
+    // largest g with job_start[g] <= j0
+    uint32_t lo = 0, hi = p.G;
+    while (hi - lo > 1) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (p.job_start[mid] <= j0) lo = mid; else hi = mid;
+    }
+    uint32_t g = lo;
+    for (unsigned long long job = j0; job < j1; job++) {
+      while (p.job_start[g + 1] <= job) g++;
+      uint32_t local = (uint32_t)(job - p.job_start[g]);
+      uint32_t cnt = p.grid_count[g];
+      uint32_t n = cnt < p.leaf_cap ? cnt : p.leaf_cap;
+      uint32_t R = (n + 31) / 32;
+      uint32_t own = R * (R + 1) / 2;
+      if (local < own) {
+        // row-major upper triangle: row rc has R - rc tiles
+        double b2 = 2.0 * R + 1.0;
+        uint32_t rc = (uint32_t)((b2 - sqrt(b2 * b2 - 8.0 * local)) * 0.5);
+        if (rc > R - 1) rc = R - 1;
+        while (rc > 0 && rc * R - rc * (rc - 1) / 2 > local) rc--;
+        while ((rc + 1) * R - (rc + 1) * rc / 2 <= local) rc++;
+        uint32_t cc = rc + (local - (rc * R - rc * (rc - 1) / 2));
+        run_tile(p, g, true, rc, cc, n, t, ct);
+      } else {
+        uint32_t b = local - own;
+        run_tile(p, g, false, b / R, b % R, n, t, ct);
+      }
+    }
+  }
+  // reduce counters per warp
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ct.tests += __shfl_xor_sync(0xffffffffu, ct.tests, o);
+    ct.exact += __shfl_xor_sync(0xffffffffu, ct.exact, o);
+    ct.hits += __shfl_xor_sync(0xffffffffu, ct.hits, o);
+    ct.amb += __shfl_xor_sync(0xffffffffu, ct.amb, o);
+  }
+  if (lane_id() == 0) {
+    if (ct.tests) atomicAdd(&p.st->tests, ct.tests);
+    if (ct.exact) atomicAdd(&p.st->exact_tests, ct.exact);
+    if (ct.hits) atomicAdd(&p.st->hits, ct.hits);
+    if (ct.amb) atomicAdd(&p.st->ambiguous, ct.amb);
+  }
+}
+
+void step_refine(PipeDev &p, uint32_t t, cudaStream_t s) {
+  STC_KL k_refine_a<<<STC_NUM_SMS * 8, REFINE_THREADS, 0, s>>>(p, t);
+}
+
+}  // namespace stc

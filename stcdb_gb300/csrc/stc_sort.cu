@@ -1,0 +1,217 @@
+// Device-wide exclusive scan and stable LSD radix sort (hand-written; no
+// CUB/thrust). The reference sorts with thrust::sort_by_key
+// (cuda/geometry.cu:1809-1907); here the partition step uses these kernels
+// to group object ids by quadtree leaf in pid order.
+#include "stc_common.cuh"
+
+namespace stc {
+
+thread_local unsigned long long tl_launches = 0;
+
+static constexpr int SCAN_THREADS = 256;
+static constexpr int SCAN_ITEMS = 8;
+static constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+  uint32_t lane = threadIdx.x & 31u;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= (uint32_t)o) v += t;
+  }
+  return v;
+}
+
+// Block-wide exclusive scan of one value per thread; returns exclusive prefix,
+// *total receives the block sum. blockDim.x must be a multiple of 32, <= 1024.
+__device__ uint32_t block_excl_scan(uint32_t v, uint32_t *total) {
+  __shared__ uint32_t warp_sums[32];
+  __shared__ uint32_t block_total;
+  uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t incl = warp_incl_scan(v);
+  if (lane == 31) warp_sums[warp] = incl;
+  __syncthreads();
+  uint32_t nw = blockDim.x >> 5;
+  if (warp == 0) {
+    uint32_t s = lane < nw ? warp_sums[lane] : 0u;
+    uint32_t si = warp_incl_scan(s);
+    if (lane < nw) warp_sums[lane] = si - s;
+    if (lane == 31) block_total = si;
+  }
+  __syncthreads();
+  uint32_t res = incl - v + warp_sums[warp];
+  uint32_t tot = block_total;
+  __syncthreads();
+  *total = tot;
+  return res;
+}
+
+__global__ void k_scan_reduce(const uint32_t *in, size_t n, uint32_t *sums) {
+  size_t base = (size_t)blockIdx.x * SCAN_TILE;
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; i++) {
+    size_t idx = base + (size_t)i * SCAN_THREADS + threadIdx.x;
+    if (idx < n) s += in[idx];
+  }
+  uint32_t tot;
+  block_excl_scan(s, &tot);
+  if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+__global__ void k_scan_sums(uint32_t *sums, size_t nb, unsigned long long *total) {
+  // one block of 1024 threads, each owns a contiguous chunk
+  size_t per = (nb + blockDim.x - 1) / blockDim.x;
+  size_t b0 = (size_t)threadIdx.x * per, b1 = b0 + per < nb ? b0 + per : nb;
+  uint32_t s = 0;
+  for (size_t i = b0; i < b1; i++) s += sums[i];
+  uint32_t tot;
+  uint32_t off = block_excl_scan(s, &tot);
+  for (size_t i = b0; i < b1; i++) {
+    uint32_t v = sums[i];
+    sums[i] = off;
+    off += v;
+  }
+  if (threadIdx.x == 0 && total) *total = tot;
+}
+
+__global__ void k_scan_down(const uint32_t *in, uint32_t *out, size_t n, const uint32_t *sums) {
+  size_t base = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+  uint32_t v[SCAN_ITEMS];
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; i++) {
+    size_t idx = base + i;
+    v[i] = idx < n ? in[idx] : 0u;
+    s += v[i];
+  }
+  uint32_t tot;
+  uint32_t off = block_excl_scan(s, &tot) + sums[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; i++) {
+    size_t idx = base + i;
+    if (idx < n) out[idx] = off;
+    off += v[i];
+  }
+}
+
+size_t scan_tmp_words(size_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
+
+void exclusive_scan_u32(const uint32_t *in, uint32_t *out, size_t n, unsigned long long *total, uint32_t *tmp,
+                        cudaStream_t s) {
+  if (n == 0) {
+    if (total) cudaMemsetAsync(total, 0, sizeof(unsigned long long), s);
+    return;
+  }
+  size_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  STC_KL k_scan_reduce<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, tmp);
+  STC_KL k_scan_sums<<<1, 1024, 0, s>>>(tmp, nb, total);
+  STC_KL k_scan_down<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, out, n, tmp);
+}
+
+// ---------------------------------------------------------------------------
+// Radix sort: 8-bit digits, tiles of 256 threads x 16 items.
+
+static constexpr int RS_THREADS = 256;
+static constexpr int RS_ITEMS = 16;
+static constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+static constexpr int RS_WARPS = RS_THREADS / 32;
+
+size_t radix_hist_words(size_t n_max) { return 256 * ((n_max + RS_TILE - 1) / RS_TILE) + 1; }
+
+__global__ void k_rs_hist(const uint32_t *keys, const unsigned long long *n_dev, size_t n_max, int shift,
+                          uint32_t *hist, uint32_t nb) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  size_t n = (size_t)*n_dev;
+  if (n > n_max) n = n_max;
+  size_t base = (size_t)blockIdx.x * RS_TILE;
+  if (base < n) {
+    for (int i = 0; i < RS_ITEMS; i++) {
+      size_t idx = base + (size_t)i * RS_THREADS + threadIdx.x;
+      if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+    }
+  }
+  __syncthreads();
+  hist[(size_t)threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void k_rs_scatter(const uint32_t *k_in, const uint32_t *v_in, uint32_t *k_out, uint32_t *v_out,
+                             const unsigned long long *n_dev, size_t n_max, int shift, const uint32_t *hist,
+                             uint32_t nb) {
+  __shared__ uint32_t base_off[256];
+  __shared__ uint32_t running[256];
+  __shared__ uint32_t warp_cnt[RS_WARPS][256];
+  size_t n = (size_t)*n_dev;
+  if (n > n_max) n = n_max;
+  size_t tile = (size_t)blockIdx.x * RS_TILE;
+  if (tile >= n) return;
+  base_off[threadIdx.x] = hist[(size_t)threadIdx.x * nb + blockIdx.x];
+  running[threadIdx.x] = 0;
+  uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t lt_mask = (1u << lane) - 1u;
+  for (int it = 0; it < RS_ITEMS; it++) {
+    for (int w = 0; w < RS_WARPS; w++) warp_cnt[w][threadIdx.x] = 0;
+    __syncthreads();
+    size_t idx = tile + (size_t)it * RS_THREADS + threadIdx.x;
+    bool valid = idx < n;
+    uint32_t key = valid ? k_in[idx] : 0u;
+    uint32_t val = valid ? v_in[idx] : 0u;
+    uint32_t digit = valid ? ((key >> shift) & 255u) : (256u + lane);
+    uint32_t peers = __match_any_sync(0xffffffffu, digit);
+    uint32_t rank = __popc(peers & lt_mask);
+    if (valid && rank == 0) warp_cnt[warp][digit] = __popc(peers);
+    __syncthreads();
+    {
+      uint32_t d = threadIdx.x;
+      uint32_t acc = running[d];
+      for (int w = 0; w < RS_WARPS; w++) {
+        uint32_t c = warp_cnt[w][d];
+        warp_cnt[w][d] = acc;
+        acc += c;
+      }
+      running[d] = acc;
+    }
+    __syncthreads();
+    if (valid) {
+      uint32_t pos = base_off[digit] + warp_cnt[warp][digit] + rank;
+      k_out[pos] = key;
+      v_out[pos] = val;
+    }
+    __syncthreads();
+  }
+}
+
+void radix_sort_u32(const uint32_t *k_in, const uint32_t *v_in, uint32_t *k_out, uint32_t *v_out,
+                    uint32_t *k_tmp, uint32_t *v_tmp, const unsigned long long *n_dev, size_t n_max, int bits,
+                    uint32_t *hist, uint32_t *scan_tmp, cudaStream_t s) {
+  uint32_t nb = (uint32_t)((n_max + RS_TILE - 1) / RS_TILE);
+  if (nb == 0) return;
+  int passes = (bits + 7) / 8;
+  if (passes < 1) passes = 1;
+  // ping-pong so that the last pass writes (k_out, v_out)
+  const uint32_t *ki = k_in, *vi = v_in;
+  for (int p = 0; p < passes; p++) {
+    bool to_out = ((passes - 1 - p) % 2) == 0;
+    uint32_t *ko = to_out ? k_out : k_tmp;
+    uint32_t *vo = to_out ? v_out : v_tmp;
+    STC_KL k_rs_hist<<<nb, RS_THREADS, 0, s>>>(ki, n_dev, n_max, 8 * p, hist, nb);
+    exclusive_scan_u32(hist, hist, (size_t)256 * nb, nullptr, scan_tmp, s);
+    STC_KL k_rs_scatter<<<nb, RS_THREADS, 0, s>>>(ki, vi, ko, vo, n_dev, n_max, 8 * p, hist, nb);
+    ki = ko;
+    vi = vo;
+  }
+}
+
+__global__ void k_iota(uint32_t *out, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (uint32_t)i;
+}
+
+void iota_u32(uint32_t *out, size_t n, cudaStream_t s) {
+  if (n == 0) return;
+  STC_KL k_iota<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, n);
+}
+
+}  // namespace stc

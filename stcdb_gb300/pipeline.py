@@ -64,6 +64,8 @@ class StcStats(ctypes.Structure):
         ("pending", ctypes.c_uint64),
         ("splits", ctypes.c_uint32),
         ("merges", ctypes.c_uint32),
+        ("kernel_launches", ctypes.c_uint32),
+        ("ambiguous_tests", ctypes.c_uint32),
         ("step_ms", ctypes.c_float),
         ("phase_ms", ctypes.c_float * 8),
     ]
