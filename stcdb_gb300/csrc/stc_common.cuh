@@ -84,6 +84,7 @@ struct DevState {
   uint32_t build_nodes, build_leaves, build_active, build_level;
   uint32_t work_next;                 // generic persistent-kernel work counter
   uint32_t pad[3];
+  unsigned long long border_points;   // points whose lookup starts above their leaf
 };
 
 __device__ __forceinline__ void stc_set_error(DevState *st, uint32_t code, uint32_t info) {

@@ -232,6 +232,7 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
             dalloc(c, &p.sort_hist, radix_hist_words(nu)) && dalloc(c, &p.grid_count, (size_t)p.G + 1) &&
             dalloc(c, &p.grid_start, (size_t)p.G + 1) && dalloc(c, &p.pts, n) && dalloc(c, &p.ptf, n) &&
             dalloc(c, &p.bcount, (size_t)n + 1) && dalloc(c, &p.boff, (size_t)n + 1) &&
+            dalloc(c, &p.blist, n) && dalloc(c, &p.bres, 4 * (size_t)n) && dalloc(c, &p.sd.fbox, p.S) &&
             dalloc(c, &p.bu_gid, p.U_cap) && dalloc(c, &p.bu_pid, p.U_cap) && dalloc(c, &p.bu_sorted_gid, p.U_cap) &&
             dalloc(c, &p.bu_sorted_pos, p.U_cap) && dalloc(c, &p.bu_cnt, (size_t)p.G + 1) &&
             dalloc(c, &p.bu_start, (size_t)p.G + 1) && dalloc(c, &p.job_cnt, (size_t)p.G + 1) &&
@@ -246,6 +247,16 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
   }
   p.sd.S = p.S;
   p.sd.G = p.G;
+  p.sd.ox = mbr[0];
+  p.sd.oy = mbr[1];
+  {
+    // fp32 band of the border lookup pre-filter: offsets from the map corner
+    // are at most its extent W; each of the ~8 fp32 roundings on the path to
+    // the degree distance adds <= u W, scaled to metres by <= 111.4 km/deg.
+    const double u = 5.9604644775390625e-08;
+    double ext_m = (mbr[2] - mbr[0]) * 111322.3 + (mbr[3] - mbr[1]) * 111322.3;
+    p.border_delta = (float)(32.0 * u * ext_m + 64.0 * u * k.reach_distance + 1e-6 * k.reach_distance);
+  }
   p.sw.scan_tmp = p.scan_tmp;
   cudaStream_t s = c->stream;
   cudaMemsetAsync(p.st, 0, sizeof(DevState), s);

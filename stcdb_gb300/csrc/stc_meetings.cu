@@ -33,6 +33,7 @@ __global__ void k_step_begin(DevState *st) {
   st->error = 0;
   st->error_info = 0;
   st->border_units = 0;
+  st->border_points = 0;
   st->jobs_total = 0;
   st->job_next = 0;
   st->cand_count = 0;
@@ -146,7 +147,14 @@ __global__ void k_pass_b(PipeDev p, uint32_t t) {
   for (unsigned long long c = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
        c += (unsigned long long)gridDim.x * blockDim.x) {
     if (stc_failed(p.st)) return;
-    Cand cd = p.cset[p.cand_list[c]];
+    Cand *cp = &p.cset[p.cand_list[c]];
+    Cand cd = *cp;
+    // pass B is the set's last reader this step: reset the entry for the next one
+    Cand x;
+    x.key = STC_EMPTY_KEY;
+    x.order = ~0ULL;
+    x.lo_x = STC_INIT_LO; x.lo_y = STC_INIT_LO; x.hi_x = STC_INIT_HI; x.hi_y = STC_INIT_HI;
+    *cp = x;
     unsigned long long slot = cd.key % p.B;
     bool found = false;
     for (unsigned long long probe = 0; probe < STC_PROBE_LIMIT * 4 && probe < p.B; probe++) {
@@ -178,22 +186,9 @@ __global__ void k_pass_b(PipeDev p, uint32_t t) {
   }
 }
 
-__global__ void k_cand_reset(PipeDev p) {
-  const unsigned long long nc = p.st->cand_count < p.cand_cap ? p.st->cand_count : p.cand_cap;
-  for (unsigned long long c = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
-       c += (unsigned long long)gridDim.x * blockDim.x) {
-    Cand x;
-    x.key = STC_EMPTY_KEY;
-    x.order = ~0ULL;
-    x.lo_x = STC_INIT_LO; x.lo_y = STC_INIT_LO; x.hi_x = STC_INIT_HI; x.hi_y = STC_INIT_HI;
-    p.cset[p.cand_list[c]] = x;
-  }
-}
-
 void step_insert(PipeDev &p, uint32_t t, cudaStream_t s) {
   STC_KL k_insert_ordered<<<STC_NUM_SMS * 8, 256, 0, s>>>(p);
   STC_KL k_pass_b<<<STC_NUM_SMS * 8, 256, 0, s>>>(p, t);
-  STC_KL k_cand_reset<<<STC_NUM_SMS * 8, 256, 0, s>>>(p);
 }
 
 // Sweep (tracing/meeting.cpp:32-76, cuda/geometry.cu:595-736).

@@ -54,6 +54,7 @@ __global__ void k_descend(PipeDev p) {
   p.leaf_gid[pid] = m.grid_id;
   p.lastvalid[pid] = lv != cur ? lv : STC_NONE;
   atomicAdd(&p.grid_count[m.grid_id], 1u);
+  if (lv != cur) p.blist[agg_inc(&p.st->border_points)] = pid;
 }
 
 __global__ void k_gather(PipeDev p) {
@@ -69,15 +70,13 @@ __global__ void k_gather(PipeDev p) {
   p.ptf[i] = make_float2(__double2float_rn(q.x), __double2float_rn(q.y));
 }
 
-// box::distance(p, geography=true) <= reach (geometry/geometry.h:174-185).
-// The containment test and the degree offsets are the reference's exact fp64
-// expressions (additions and halvings only); the metric step is classified in
-// fp32 with a relative error below 24 u (u = 2^-24: two roundings of the
-// offsets, the scale factor from sinf, products and sum), so only a band of
-// +-64 u around reach falls through to the reference's fp64 division and
-// square root, and within 1e-12 of reach to the correctly rounded sine.
-__device__ __forceinline__ bool box_within(const Node &c, double x, double y, double reach, float reach_f,
-                                           float s_lon, double dp_fast) {
+// box::distance(p, geography=true) <= reach (geometry/geometry.h:174-185),
+// decided exactly: fp64 containment and degree offsets as in the reference,
+// then the metric step in fp32 with a +-64 u relative band (u = 2^-24), then
+// the reference's fp64 division and square root, and within 1e-12 of reach
+// the correctly rounded sine.
+__device__ bool box_within_exact(const Node &c, double x, double y, double reach, float reach_f, float s_lon,
+                                 double &dp_fast) {
   if (x >= c.lo_x && x <= c.hi_x && y >= c.lo_y && y <= c.hi_y) return true;  // distance 0
   double dx = RN_SUB(fabs(RN_SUB(x, RN_MUL(RN_ADD(c.lo_x, c.hi_x), 0.5))), RN_MUL(RN_SUB(c.hi_x, c.lo_x), 0.5));
   double dy = RN_SUB(fabs(RN_SUB(y, RN_MUL(RN_ADD(c.lo_y, c.hi_y), 0.5))), RN_MUL(RN_SUB(c.hi_y, c.lo_y), 0.5));
@@ -88,33 +87,36 @@ __device__ __forceinline__ bool box_within(const Node &c, double x, double y, do
   const float lo = reach_f * (1.0f - 64.0f * 5.9604645e-08f), hi = reach_f * (1.0f + 64.0f * 5.9604645e-08f);
   if (d2 <= lo * lo) return true;
   if (d2 >= hi * hi) return false;
+  if (dp_fast == 0.0) dp_fast = dpml_fast_d(y);
   double d = stc_box_distance_ref(c.lo_x, c.lo_y, c.hi_x, c.hi_y, x, y, dp_fast);
   if (fabs(d - reach) > 1e-12 * reach) return d <= reach;
   return stc_box_distance_ref(c.lo_x, c.lo_y, c.hi_x, c.hi_y, x, y, stc_dpml_ref(y)) <= reach;
 }
 
+// Lookup of one border point (tracing/filter.cpp:130-152): depth-first from
+// last_valid over children 0..3, collecting the leaves within reach that lie
+// above the point or to its right. Node distances are first classified in
+// fp32 from map-relative float boxes; the band of width border_delta around
+// reach (bounding the fp32 rounding of the offsets, see stc_create) goes to
+// box_within_exact. Writes the first `keep` leaf ids to out; returns the
+// count, or 0xFFFFFFFF on stack overflow.
 #define LOOKUP_STACK 64
-
-template <bool FILL>
-__global__ void k_border(PipeDev p) {
-  uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pid >= p.N) return;
-  uint32_t lv = p.lastvalid[pid];
-  if (lv == STC_NONE) {
-    if (!FILL) p.bcount[pid] = 0;
-    return;
-  }
+__device__ uint32_t border_lookup(const PipeDev &p, uint32_t pid, uint32_t lv, uint32_t *out, uint32_t keep) {
   double2 q = p.xy[pid];
-  double dpf = dpml_fast_d(q.y);
+  float px = __double2float_rn(RN_SUB(q.x, p.sd.ox)), py = __double2float_rn(RN_SUB(q.y, p.sd.oy));
   float s_lon = metres_per_deg_lon_f(q.y);
   float reach_f = (float)p.reach;
+  float rlo = fmaxf(reach_f - p.border_delta, 0.0f), rhi = reach_f + p.border_delta;
+  float rlo2 = rlo * rlo, rhi2 = rhi * rhi;
+  // the fp32 band only covers points inside the map box (offsets bounded by its extent)
+  bool fast_ok = q.x >= p.map_lo_x && q.x <= p.map_hi_x && q.y >= p.map_lo_y && q.y <= p.map_hi_y;
+  double dpf = 0.0;
   uint32_t stk[LOOKUP_STACK];
   uint8_t nxt[LOOKUP_STACK];
   int sp = 1;
   stk[0] = lv;
   nxt[0] = 0;
   uint32_t cnt = 0;
-  unsigned long long base = FILL ? p.boff[pid] : 0ULL;
   while (sp > 0) {
     int i = nxt[sp - 1];
     if (i == 4) {
@@ -123,33 +125,78 @@ __global__ void k_border(PipeDev p) {
     }
     nxt[sp - 1] = (uint8_t)(i + 1);
     uint32_t ch = p.sd.nodes[stk[sp - 1]].child[i];
-    Node c = p.sd.nodes[ch];
+    int decided = 0;  // 1 within, -1 outside, 0 undecided
+    if (fast_ok) {
+      float4 fb = p.sd.fbox[ch];
+      float cx = (fb.x + fb.z) * 0.5f, hwx = (fb.z - fb.x) * 0.5f;
+      float cy = (fb.y + fb.w) * 0.5f, hwy = (fb.w - fb.y) * 0.5f;
+      float dx = fmaxf(fabsf(px - cx) - hwx, 0.0f) * s_lon;
+      float dy = fmaxf(fabsf(py - cy) - hwy, 0.0f) * STC_SLAT_F;
+      float d2 = dx * dx + dy * dy;
+      decided = d2 <= rlo2 ? 1 : (d2 >= rhi2 ? -1 : 0);
+    }
+    if (decided < 0) continue;
     NodeMeta cm = p.sd.meta[ch];
-    if (!box_within(c, q.x, q.y, p.reach, reach_f, s_lon, dpf)) continue;
     if (cm.type == NODE_LEAF) {
+      // leaf test needs the exact box; fetch it only for leaves
+      Node c = p.sd.nodes[ch];
+      if (decided == 0 && !box_within_exact(c, q.x, q.y, p.reach, reach_f, s_lon, dpf)) continue;
       // the leaf lies above, or to the right within the point's row
       if (q.y < c.lo_y || (q.y < c.hi_y && q.x < c.lo_x)) {
-        if (FILL) {
-          unsigned long long at = base + cnt;
-          if (at < p.U_cap) {
-            p.bu_gid[at] = cm.grid_id;
-            p.bu_pid[at] = pid;
-            atomicAdd(&p.bu_cnt[cm.grid_id], 1u);
-          }
-        }
+        if (cnt < keep) out[cnt] = cm.grid_id;
         cnt++;
       }
     } else {
-      if (sp == LOOKUP_STACK) {
-        stc_set_error(p.st, ERR_LOOKUP, pid);
-        return;
+      if (decided == 0) {
+        Node c = p.sd.nodes[ch];
+        if (!box_within_exact(c, q.x, q.y, p.reach, reach_f, s_lon, dpf)) continue;
       }
+      if (sp == LOOKUP_STACK) return 0xFFFFFFFFu;
       stk[sp] = ch;
       nxt[sp] = 0;
       sp++;
     }
   }
-  if (!FILL) p.bcount[pid] = cnt;
+  return cnt;
+}
+
+#define BORDER_KEEP 4
+
+__global__ void k_border_count(PipeDev p) {
+  const unsigned long long nb = p.st->border_points;
+  for (unsigned long long b = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; b < nb;
+       b += (unsigned long long)gridDim.x * blockDim.x) {
+    uint32_t pid = p.blist[b];
+    uint32_t c = border_lookup(p, pid, p.lastvalid[pid], p.bres + BORDER_KEEP * b, BORDER_KEEP);
+    if (c == 0xFFFFFFFFu) {
+      stc_set_error(p.st, ERR_LOOKUP, pid);
+      c = 0;
+    }
+    p.bcount[pid] = c;
+  }
+}
+
+__global__ void k_border_fill(PipeDev p) {
+  const unsigned long long nb = p.st->border_points;
+  for (unsigned long long b = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; b < nb;
+       b += (unsigned long long)gridDim.x * blockDim.x) {
+    uint32_t pid = p.blist[b];
+    uint32_t c = p.bcount[pid];
+    unsigned long long base = p.boff[pid];
+    if (base + c > p.U_cap) continue;  // reported by k_check_units
+    const uint32_t *src = p.bres + BORDER_KEEP * b;
+    if (c > BORDER_KEEP) {
+      // rare: more leaves than kept by the counting pass; walk again into place
+      border_lookup(p, pid, p.lastvalid[pid], p.bu_gid + base, c);
+      src = p.bu_gid + base;
+    }
+    for (uint32_t k = 0; k < c; k++) {
+      uint32_t gid = src[k];
+      p.bu_gid[base + k] = gid;
+      p.bu_pid[base + k] = pid;
+      atomicAdd(&p.bu_cnt[gid], 1u);
+    }
+  }
 }
 
 __global__ void k_check_units(PipeDev p) {
@@ -174,6 +221,7 @@ __global__ void k_jobs(PipeDev p) {
 
 void step_partition(PipeDev &p, cudaStream_t s) {
   cudaMemsetAsync(p.grid_count, 0, (size_t)(p.G + 1) * sizeof(uint32_t), s);
+  cudaMemsetAsync(p.bcount, 0, (size_t)p.N * sizeof(uint32_t), s);
   STC_KL k_descend<<<nblk(p.N), 256, 0, s>>>(p);
   int bits = 1;
   while ((1u << bits) < p.G && bits < 32) bits++;
@@ -185,10 +233,10 @@ void step_partition(PipeDev &p, cudaStream_t s) {
 
 void step_border(PipeDev &p, cudaStream_t s) {
   cudaMemsetAsync(p.bu_cnt, 0, (size_t)(p.G + 1) * sizeof(uint32_t), s);
-  STC_KL k_border<false><<<nblk(p.N, 128), 128, 0, s>>>(p);
+  STC_KL k_border_count<<<STC_NUM_SMS * 16, 128, 0, s>>>(p);
   exclusive_scan_u32(p.bcount, p.boff, p.N, &p.st->border_units, p.scan_tmp, s);
   STC_KL k_check_units<<<1, 1, 0, s>>>(p);
-  STC_KL k_border<true><<<nblk(p.N, 128), 128, 0, s>>>(p);
+  STC_KL k_border_fill<<<STC_NUM_SMS * 16, 128, 0, s>>>(p);
   int bits = 1;
   while ((1u << bits) < p.G && bits < 32) bits++;
   radix_sort_u32(p.bu_gid, p.iota, p.bu_sorted_gid, p.bu_sorted_pos, p.sort_ktmp, p.sort_vtmp,

@@ -30,6 +30,9 @@ struct PipeDev {
   float2 *ptf;                          // N sorted: float lon, lat
   // border units
   uint32_t *bcount, *boff;              // N+1
+  uint32_t *blist;                      // N: pids of border points (any order)
+  uint32_t *bres;                       // 4N: first four lookup results per border point
+  float border_delta;                   // fp32 band (metres) of the border lookup pre-filter
   uint32_t *bu_gid, *bu_pid;            // U_cap (rank order)
   uint32_t *bu_sorted_gid, *bu_sorted_pos;  // U_cap grouped by leaf
   uint32_t *bu_cnt, *bu_start;          // G+1

@@ -88,31 +88,46 @@ __device__ void cand_insert(const PipeDev &p, unsigned long long key, unsigned l
   stc_set_error(p.st, ERR_CAND, 0xFFFFFFFFu);
 }
 
-__device__ void hit_a(const PipeDev &p, uint32_t a, uint32_t b, unsigned long long order, float2 fa, float2 fb,
-                      uint32_t t) {
-  uint32_t p1 = a < b ? a : b, p2 = a < b ? b : a;
-  unsigned long long key = stc_cantor(p1, p2);
-  float lox = fminf(fa.x, fb.x), loy = fminf(fa.y, fb.y);
-  float hix = fmaxf(fa.x, fb.x), hiy = fmaxf(fa.y, fb.y);
-  unsigned long long slot = key % p.B;
+// One pair within reach, waiting in its warp's queue.
+struct __align__(16) HitRec {
+  unsigned long long key, order;
+  float lo_x, lo_y, hi_x, hi_y;
+};
+
+static constexpr int QCAP = 64;  // per-warp queue; flushed 32 at a time
+
+__device__ void process_hit(const PipeDev &p, const HitRec &h, uint32_t t) {
+  unsigned long long slot = h.key % p.B;
   for (unsigned long long probe = 0; probe < STC_PROBE_LIMIT && probe < p.B; probe++) {
     Slot *s = &p.slots[slot];
     unsigned long long k = s->key;
-    if (k == key) {  // tracing/refinement.cpp:40-42 (+ MBR, cuda/geometry.cu:474-478)
+    if (k == h.key) {  // tracing/refinement.cpp:40-42 (+ MBR, cuda/geometry.cu:474-478)
       s->end = t;
-      if (lox < s->lo_x) atomic_min_f(&s->lo_x, lox);
-      if (loy < s->lo_y) atomic_min_f(&s->lo_y, loy);
-      if (hix > s->hi_x) atomic_max_f(&s->hi_x, hix);
-      if (hiy > s->hi_y) atomic_max_f(&s->hi_y, hiy);
+      if (h.lo_x < s->lo_x) atomic_min_f(&s->lo_x, h.lo_x);
+      if (h.lo_y < s->lo_y) atomic_min_f(&s->lo_y, h.lo_y);
+      if (h.hi_x > s->hi_x) atomic_max_f(&s->hi_x, h.hi_x);
+      if (h.hi_y > s->hi_y) atomic_max_f(&s->hi_y, h.hi_y);
       return;
     }
     if (k == STC_EMPTY_KEY) {
-      cand_insert(p, key, order, lox, loy, hix, hiy);
+      cand_insert(p, h.key, h.order, h.lo_x, h.lo_y, h.hi_x, h.hi_y);
       return;
     }
     slot = slot + 1 == p.B ? 0 : slot + 1;
   }
-  stc_set_error(p.st, ERR_PROBE, (uint32_t)(key % p.B));
+  stc_set_error(p.st, ERR_PROBE, (uint32_t)(h.key % p.B));
+}
+
+// Processes the first `n` (<= 32) queued hits, one per lane, so that their
+// random-access probe chains overlap.
+__device__ __forceinline__ void flush_queue(const PipeDev &p, HitRec *q, uint32_t n, uint32_t t) {
+  __syncwarp();
+  uint32_t lane = lane_id();
+  if (lane < n) {
+    HitRec h = q[lane];
+    process_hit(p, h, t);
+  }
+  __syncwarp();
 }
 
 __device__ __forceinline__ float warp_max(float v) {
@@ -127,13 +142,15 @@ struct Counters {
 
 // One 32x32 tile. Rows: own members (own=true) or border units.
 __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtile, uint32_t coltile, uint32_t n,
-                         uint32_t t, Counters &ct) {
+                         uint32_t t, Counters &ct, HitRec *q, uint32_t &qn) {
   const uint32_t lane = lane_id();
   const uint32_t base = p.grid_start[g];
+  const uint32_t lt_mask = (1u << lane) - 1u;
   // column points
   uint32_t j = coltile * 32 + lane;
   bool vc = j < n;
   float4 cp = vc ? p.pts[base + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+  float2 cf = vc ? p.ptf[base + j] : make_float2(0.f, 0.f);
   // row points
   float4 rp;
   float2 rf = make_float2(0.f, 0.f);
@@ -144,6 +161,7 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
   if (own) {
     vr = i < n;
     rp = vr ? p.pts[base + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    rf = vr ? p.ptf[base + i] : make_float2(0.f, 0.f);
     pid1 = __float_as_uint(rp.w);
     rank = pid1;  // own-leaf unit of pid1 is grid_check[pid1] (tracing/filter.cpp:107-109)
   } else {
@@ -156,10 +174,10 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
       pid1 = p.bu_pid[pos];
       rank = (unsigned long long)p.N + pos;  // border units follow the N own units
       const Node *o = &p.sd.nodes[p.sd.gid_node[g]];
-      double2 q = p.xy[pid1];
-      rp = make_float4(__double2float_rn(RN_SUB(q.x, o->lo_x)), __double2float_rn(RN_SUB(q.y, o->lo_y)),
-                       metres_per_deg_lon_f(q.y), 0.f);
-      rf = make_float2(__double2float_rn(q.x), __double2float_rn(q.y));
+      double2 qq = p.xy[pid1];
+      rp = make_float4(__double2float_rn(RN_SUB(qq.x, o->lo_x)), __double2float_rn(RN_SUB(qq.y, o->lo_y)),
+                       metres_per_deg_lon_f(qq.y), 0.f);
+      rf = make_float2(__double2float_rn(qq.x), __double2float_rn(qq.y));
     }
   }
   // tile error margin
@@ -172,43 +190,67 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
   float lo = fmaxf(r - delta, 0.0f);
   float lo2 = lo * lo;
   float hi2 = (r + delta) * (r + delta);
-  bool have_rf = !own;
   uint32_t kmax = n - coltile * 32;
   if (kmax > 32) kmax = 32;
   for (uint32_t k = 0; k < kmax; k++) {
     float cx = __shfl_sync(0xffffffffu, cp.x, k);
     float cy = __shfl_sync(0xffffffffu, cp.y, k);
     uint32_t cpid = __shfl_sync(0xffffffffu, __float_as_uint(cp.w), k);
+    float cfx = __shfl_sync(0xffffffffu, cf.x, k);
+    float cfy = __shfl_sync(0xffffffffu, cf.y, k);
     uint32_t jj = coltile * 32 + k;
-    if (!vr || (own && jj <= i)) continue;  // tracing/refinement.cpp:30
-    float dx = (rp.x - cx) * rp.z;
-    float dy = (rp.y - cy) * STC_SLAT_F;
-    float d2 = dx * dx + dy * dy;
-    ct.tests++;
-    bool hit = d2 <= lo2;
-    if (!hit && d2 < hi2) {
-      ct.exact++;
-      hit = exact_within(p, pid1, cpid, ct.amb);
-    }
-    if (hit) {
-      ct.hits++;
-      if (!have_rf) {
-        rf = p.ptf[base + i];
-        have_rf = true;
+    bool hit = false;
+    if (vr && !(own && jj <= i)) {  // tracing/refinement.cpp:30
+      float dx = (rp.x - cx) * rp.z;
+      float dy = (rp.y - cy) * STC_SLAT_F;
+      float d2 = dx * dx + dy * dy;
+      ct.tests++;
+      hit = d2 <= lo2;
+      if (!hit && d2 < hi2) {
+        ct.exact++;
+        hit = exact_within(p, pid1, cpid, ct.amb);
       }
-      float2 cf = p.ptf[base + jj];
-      hit_a(p, pid1, cpid, (rank << STC_ORDER_SHIFT) | jj, rf, cf, t);
+    }
+    uint32_t hm = __ballot_sync(0xffffffffu, hit);
+    if (hm) {
+      if (hit) {
+        ct.hits++;
+        uint32_t a = pid1 < cpid ? pid1 : cpid, b = pid1 < cpid ? cpid : pid1;
+        HitRec h;
+        h.key = stc_cantor(a, b);
+        h.order = (rank << STC_ORDER_SHIFT) | jj;
+        h.lo_x = fminf(rf.x, cfx);
+        h.lo_y = fminf(rf.y, cfy);
+        h.hi_x = fmaxf(rf.x, cfx);
+        h.hi_y = fmaxf(rf.y, cfy);
+        q[qn + __popc(hm & lt_mask)] = h;
+      }
+      qn += __popc(hm);
+      if (qn >= 32) {
+        flush_queue(p, q, 32, t);
+        uint32_t rest = qn - 32;
+        HitRec mv;
+        if (lane < rest) mv = q[32 + lane];
+        __syncwarp();
+        if (lane < rest) q[lane] = mv;
+        __syncwarp();
+        qn = rest;
+      }
     }
   }
 }
 
 __global__ void __launch_bounds__(REFINE_THREADS) k_refine_a(PipeDev p, uint32_t t) {
+  __shared__ HitRec queues[REFINE_THREADS / 32][QCAP];
+  HitRec *q = queues[threadIdx.x >> 5];
+  uint32_t qn = 0;  // warp-uniform queue length
   const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
   const unsigned long long J = p.st->jobs_total;
   Counters ct = {0, 0, 0, 0};
   for (unsigned long long chunk = warp; chunk * JOB_CHUNK < J; chunk += nwarps) {
-    if (stc_failed(p.st)) break;  // uniform per warp: every lane reads the same flag
+    // one lane reads the flag so that the whole warp leaves together
+    if (__shfl_sync(0xffffffffu, (int)stc_failed(p.st), 0)) break;
     unsigned long long j0 = chunk * JOB_CHUNK;
     unsigned long long j1 = j0 + JOB_CHUNK < J ? j0 + JOB_CHUNK : J;
     // largest g with job_start[g] <= j0
@@ -233,13 +275,14 @@ __global__ void __launch_bounds__(REFINE_THREADS) k_refine_a(PipeDev p, uint32_t
         while (rc > 0 && rc * R - rc * (rc - 1) / 2 > local) rc--;
         while ((rc + 1) * R - (rc + 1) * rc / 2 <= local) rc++;
         uint32_t cc = rc + (local - (rc * R - rc * (rc - 1) / 2));
-        run_tile(p, g, true, rc, cc, n, t, ct);
+        run_tile(p, g, true, rc, cc, n, t, ct, q, qn);
       } else {
         uint32_t b = local - own;
-        run_tile(p, g, false, b / R, b % R, n, t, ct);
+        run_tile(p, g, false, b / R, b % R, n, t, ct, q, qn);
       }
     }
   }
+  if (qn) flush_queue(p, q, qn, t);
   // reduce counters per warp
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {

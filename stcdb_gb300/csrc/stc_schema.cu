@@ -176,6 +176,8 @@ __global__ void k_build_write(const Node *bn, const NodeMeta *bm, uint32_t total
   m.underflow = 0;
   sd.nodes[p] = q;
   sd.meta[p] = m;
+  sd.fbox[p] = make_float4(__double2float_rn(RN_SUB(q.lo_x, sd.ox)), __double2float_rn(RN_SUB(q.lo_y, sd.oy)),
+                           __double2float_rn(RN_SUB(q.hi_x, sd.ox)), __double2float_rn(RN_SUB(q.hi_y, sd.oy)));
 }
 
 __global__ void k_build_finish(const uint32_t *sub_nodes, const uint32_t *sub_leaves, uint32_t S, uint32_t G,
@@ -307,6 +309,8 @@ __device__ bool split_node(SchemaDev sd, uint32_t cur, uint32_t *grid_count, Dev
     c.mid_y = RN_DIV(RN_ADD(c.lo_y, c.hi_y), 2.0);
     c.child[0] = c.child[1] = c.child[2] = c.child[3] = STC_NONE;
     sd.nodes[child] = c;
+    sd.fbox[child] = make_float4(__double2float_rn(RN_SUB(c.lo_x, sd.ox)), __double2float_rn(RN_SUB(c.lo_y, sd.oy)),
+                                 __double2float_rn(RN_SUB(c.hi_x, sd.ox)), __double2float_rn(RN_SUB(c.hi_y, sd.oy)));
     NodeMeta m;
     m.type = NODE_LEAF; m.level = (int16_t)(cm.level + 1); m.overflow = 0; m.underflow = 0;
     m.grid_id = g; m.parent = cur;

@@ -10,6 +10,8 @@ struct SchemaDev {
   uint32_t *schema_stack; // S
   uint32_t *grids_stack;  // G
   uint32_t *gid_node;     // G: leaf grid id -> node index
+  float4 *fbox;           // S: node box in fp32 degrees relative to (ox, oy)
+  double ox, oy;          // map origin for fbox
   uint32_t S, G;
 };
 
