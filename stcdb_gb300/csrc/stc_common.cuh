@@ -31,7 +31,6 @@ enum {
   ERR_SCHEMA = 7,      // schema or grid stack exhausted
   ERR_LOOKUP = 8,      // border lookup stack overflow
   ERR_BUILD = 9,       // initial quadtree build exceeded capacity
-  ERR_PASSB = 10,      // candidate not found after insertion
 };
 
 // One meeting-table slot (32 B; the reference's meeting_unit of
@@ -85,6 +84,7 @@ struct DevState {
   uint32_t work_next;                 // generic persistent-kernel work counter
   uint32_t pad[3];
   unsigned long long border_points;   // points whose lookup starts above their leaf
+  unsigned long long fast_claims;     // new keys walked directly by the refinement
 };
 
 __device__ __forceinline__ void stc_set_error(DevState *st, uint32_t code, uint32_t info) {

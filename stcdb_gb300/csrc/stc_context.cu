@@ -51,7 +51,6 @@ static const char *error_name(uint32_t e) {
     case ERR_SCHEMA: return "quadtree schema or grid stack exhausted";
     case ERR_LOOKUP: return "border lookup stack overflow";
     case ERR_BUILD: return "initial quadtree exceeds schema capacity";
-    case ERR_PASSB: return "inserted meeting not found in pass B";
     default: return "unknown device error";
   }
 }
@@ -199,10 +198,10 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
   p.G = 4 * std::max<uint32_t>(100000u, per);  // tracing/workbench.cpp:38
   p.S = (uint32_t)(1.6 * p.G);                 // tracing/workbench.cpp:41
   p.B = k.num_meeting_buckets;
-  // every candidate ends in a distinct slot (a claimed empty one or its own
-  // live entry), so B bounds the count; half of it covers any table that is
-  // not already more than half full
-  uint64_t cand_cap = k.candidate_capacity ? k.candidate_capacity : std::max<uint64_t>(1024, p.B / 2);
+  // only pairs found twice in one step (two border units targeting each
+  // other's leaves) pass through the candidate set
+  uint64_t cand_cap = k.candidate_capacity ? k.candidate_capacity
+                                           : std::max<uint64_t>(1u << 20, std::min<uint64_t>(p.B / 2, 2ULL * n));
   p.cand_cap = cand_cap;
   p.C = next_pow2(2 * cand_cap);
   p.E = k.emit_capacity ? k.emit_capacity : std::max<uint64_t>(1u << 20, 4ULL * n);
@@ -230,7 +229,7 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
             dalloc(c, &p.lastvalid, n) && dalloc(c, &p.iota, nu) && dalloc(c, &p.sorted_gid, n) &&
             dalloc(c, &p.sorted_pid, n) && dalloc(c, &p.sort_ktmp, nu) && dalloc(c, &p.sort_vtmp, nu) &&
             dalloc(c, &p.sort_hist, radix_hist_words(nu)) && dalloc(c, &p.grid_count, (size_t)p.G + 1) &&
-            dalloc(c, &p.grid_start, (size_t)p.G + 1) && dalloc(c, &p.pts, n) && dalloc(c, &p.ptf, n) &&
+            dalloc(c, &p.grid_start, (size_t)p.G + 1) && dalloc(c, &p.pts, n) && dalloc(c, &p.ptf, n) && dalloc(c, &p.fxy, n) &&
             dalloc(c, &p.bcount, (size_t)n + 1) && dalloc(c, &p.boff, (size_t)n + 1) &&
             dalloc(c, &p.blist, n) && dalloc(c, &p.bres, 4 * (size_t)n) && dalloc(c, &p.sd.fbox, p.S) &&
             dalloc(c, &p.bu_gid, p.U_cap) && dalloc(c, &p.bu_pid, p.U_cap) && dalloc(c, &p.bu_sorted_gid, p.U_cap) &&
@@ -317,7 +316,7 @@ static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copie
   o.pair_tests = h.tests;
   o.exact_tests = h.exact_tests;
   o.hits = h.hits;
-  o.new_candidates = h.cand_count;
+  o.new_candidates = h.cand_count + h.fast_claims;
   o.taken_buckets = h.taken;
   o.emitted = h.step_emitted;
   o.pending = std::min<unsigned long long>(h.emit_count, p.E);

@@ -20,12 +20,14 @@
 //   assignment, which is exactly what inserting the keys one by one in
 //   priority order produces.
 //
-// After the claims settle, pass B writes start/end/MBR of every candidate's
-// final slot, and the sweep turns claims into plain keys, keeps active
-// meetings, emits finished ones whose duration reaches min_meet_time
-// (tracing/meeting.cpp:59, plus the map-box filter of cuda/geometry.cu:667)
-// and clears the rest.
-#include "stc_pipeline.cuh"
+// The ordered walk itself lives in stc_insert.cuh; the refinement runs it for
+// keys found once per step, k_insert_ordered for keys that may occur twice.
+// The sweep turns claims into new meetings (start = end = t, MBR of both
+// objects' current positions -- a new meeting has been seen in this step
+// only), keeps active meetings, emits finished ones whose duration reaches
+// min_meet_time (tracing/meeting.cpp:59, plus the map-box filter of
+// cuda/geometry.cu:667) and clears the rest.
+#include "stc_insert.cuh"
 
 namespace stc {
 
@@ -34,6 +36,7 @@ __global__ void k_step_begin(DevState *st) {
   st->error_info = 0;
   st->border_units = 0;
   st->border_points = 0;
+  st->fast_claims = 0;
   st->jobs_total = 0;
   st->job_next = 0;
   st->cand_count = 0;
@@ -75,120 +78,27 @@ void init_tables(PipeDev &p, cudaStream_t s) {
   STC_KL k_init_cands<<<STC_NUM_SMS * 8, 256, 0, s>>>(p.cset, p.C);
 }
 
-__device__ __forceinline__ U128 load_pair(const Slot *s) {
-  U128 v;
-  v.lo = *(volatile const unsigned long long *)&s->key;
-  v.hi = *(volatile const unsigned long long *)&s->start;
-  return v;
-}
-
-// Ordered insertion (deferred acceptance, see the file comment).
-__global__ void k_insert_ordered(PipeDev p) {
-  const unsigned long long nc = p.st->cand_count < p.cand_cap ? p.st->cand_count : p.cand_cap;
-  const unsigned long long limit = STC_PROBE_LIMIT * 4;
-  for (unsigned long long c = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
-       c += (unsigned long long)gridDim.x * blockDim.x) {
-    const Cand *cd = &p.cset[p.cand_list[c]];
-    unsigned long long key = cd->key, prio = cd->order;
-    unsigned long long slot = key % p.B;
-    unsigned long long steps = 0;
-    bool done = false;
-    if (stc_failed(p.st)) return;
-    while (!done) {
-      if (++steps > limit) {
-        stc_set_error(p.st, ERR_DA, (uint32_t)c);
-        return;
-      }
-      Slot *s = &p.slots[slot];
-      U128 cur = load_pair(s);
-      if (cur.lo == key) break;  // its own live entry: extended in pass B
-      if (cur.lo != STC_EMPTY_KEY && !(cur.lo & STC_CLAIM_BIT)) {
-        slot = slot + 1 == p.B ? 0 : slot + 1;
-        continue;
-      }
-      // contended empty slot
-      while (true) {
-        if (cur.lo == STC_EMPTY_KEY) {
-          U128 want = {key | STC_CLAIM_BIT, prio};
-          U128 old = atomicCAS((U128 *)s, cur, want);
-          if (old.lo == cur.lo && old.hi == cur.hi) {
-            done = true;
-            break;
-          }
-          cur = old;
-          continue;
-        }
-        // claimed by another key
-        unsigned long long other_prio = cur.hi;
-        if (prio < other_prio) {
-          U128 want = {key | STC_CLAIM_BIT, prio};
-          U128 old = atomicCAS((U128 *)s, cur, want);
-          if (old.lo == cur.lo && old.hi == cur.hi) {
-            // carry the evicted key onward
-            key = cur.lo & ~STC_CLAIM_BIT;
-            prio = other_prio;
-            slot = slot + 1 == p.B ? 0 : slot + 1;
-            break;
-          }
-          cur = old;
-          continue;
-        }
-        slot = slot + 1 == p.B ? 0 : slot + 1;  // lost this slot
-        break;
-      }
-    }
-    if (steps > 1) atomicAdd(&p.st->da_iters, steps - 1);
-  }
-}
-
-// Pass B: write the step's state into every candidate's final slot.
-__global__ void k_pass_b(PipeDev p, uint32_t t) {
+// Candidates that may occur twice in a step: walk with their minimum
+// priority once all instances are merged.
+__global__ void k_insert_ordered(PipeDev p, uint32_t t) {
   const unsigned long long nc = p.st->cand_count < p.cand_cap ? p.st->cand_count : p.cand_cap;
   for (unsigned long long c = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
        c += (unsigned long long)gridDim.x * blockDim.x) {
     if (stc_failed(p.st)) return;
     Cand *cp = &p.cset[p.cand_list[c]];
-    Cand cd = *cp;
-    // pass B is the set's last reader this step: reset the entry for the next one
+    unsigned long long key = cp->key, prio = cp->order;
+    // last reader this step: reset the entry for the next one
     Cand x;
     x.key = STC_EMPTY_KEY;
     x.order = ~0ULL;
     x.lo_x = STC_INIT_LO; x.lo_y = STC_INIT_LO; x.hi_x = STC_INIT_HI; x.hi_y = STC_INIT_HI;
     *cp = x;
-    unsigned long long slot = cd.key % p.B;
-    bool found = false;
-    for (unsigned long long probe = 0; probe < STC_PROBE_LIMIT * 4 && probe < p.B; probe++) {
-      Slot *s = &p.slots[slot];
-      unsigned long long k = s->key;
-      if (k == (cd.key | STC_CLAIM_BIT)) {
-        // new meeting: start = end = t, MBR = init then both points (cuda/geometry.cu:480-489)
-        s->start = t;
-        s->end = t;
-        s->lo_x = fminf(STC_INIT_LO, cd.lo_x);
-        s->lo_y = fminf(STC_INIT_LO, cd.lo_y);
-        s->hi_x = fmaxf(STC_INIT_HI, cd.hi_x);
-        s->hi_y = fmaxf(STC_INIT_HI, cd.hi_y);
-        found = true;
-        break;
-      }
-      if (k == cd.key) {  // extended
-        s->end = t;
-        s->lo_x = fminf(s->lo_x, cd.lo_x);
-        s->lo_y = fminf(s->lo_y, cd.lo_y);
-        s->hi_x = fmaxf(s->hi_x, cd.hi_x);
-        s->hi_y = fmaxf(s->hi_y, cd.hi_y);
-        found = true;
-        break;
-      }
-      slot = slot + 1 == p.B ? 0 : slot + 1;
-    }
-    if (!found) stc_set_error(p.st, ERR_PASSB, (uint32_t)c);
+    if (!ordered_walk(p, key, prio, key % p.B, t)) stc_set_error(p.st, ERR_DA, (uint32_t)c);
   }
 }
 
 void step_insert(PipeDev &p, uint32_t t, cudaStream_t s) {
-  STC_KL k_insert_ordered<<<STC_NUM_SMS * 8, 256, 0, s>>>(p);
-  STC_KL k_pass_b<<<STC_NUM_SMS * 8, 256, 0, s>>>(p, t);
+  STC_KL k_insert_ordered<<<STC_NUM_SMS * 4, 256, 0, s>>>(p, t);
 }
 
 // Sweep (tracing/meeting.cpp:32-76, cuda/geometry.cu:595-736).
@@ -207,7 +117,20 @@ __global__ void __launch_bounds__(256) k_sweep(PipeDev p, uint32_t t) {
       s = p.slots[i];
       if (s.key != STC_EMPTY_KEY) {
         if (s.key & STC_CLAIM_BIT) {
-          p.slots[i].key = s.key & ~STC_CLAIM_BIT;  // new meeting of this step
+          // new meeting of this step (cuda/geometry.cu:480-489): start = end = t,
+          // MBR = init, then both objects' positions
+          Slot nm;
+          nm.key = s.key & ~STC_CLAIM_BIT;
+          uint32_t a, b;
+          cantor_decode(nm.key, &a, &b);
+          float2 fa = p.fxy[a], fb = p.fxy[b];
+          nm.start = t;
+          nm.end = t;
+          nm.lo_x = fminf(STC_INIT_LO, fminf(fa.x, fb.x));
+          nm.lo_y = fminf(STC_INIT_LO, fminf(fa.y, fb.y));
+          nm.hi_x = fmaxf(STC_INIT_HI, fmaxf(fa.x, fb.x));
+          nm.hi_y = fmaxf(STC_INIT_HI, fmaxf(fa.y, fb.y));
+          p.slots[i] = nm;
           active++;
         } else if (s.end == t) {
           active++;

@@ -28,8 +28,9 @@ struct PipeDev {
   uint32_t *grid_count, *grid_start;   // G, G+1
   float4 *pts;                          // N sorted: lx, ly, metres/deg lon, pid bits
   float2 *ptf;                          // N sorted: float lon, lat
+  float2 *fxy;                          // N by pid: float lon, lat (MBR of new meetings)
   // border units
-  uint32_t *bcount, *boff;              // N+1
+  uint32_t *bcount, *boff;              // N+1 (border units per pid, exclusive offsets)
   uint32_t *blist;                      // N: pids of border points (any order)
   uint32_t *bres;                       // 4N: first four lookup results per border point
   float border_delta;                   // fp32 band (metres) of the border lookup pre-filter

@@ -30,7 +30,7 @@
 // (end = t, MBR); every other key becomes a candidate for the ordered insert
 // of stc_meetings.cu, keyed with its first position in the reference's
 // sequential processing order: unit rank << 24 | member index.
-#include "stc_pipeline.cuh"
+#include "stc_insert.cuh"
 
 namespace stc {
 
@@ -55,8 +55,9 @@ __device__ bool exact_within(const PipeDev &p, uint32_t pid1, uint32_t pid2, uns
   return d <= p.reach;
 }
 
-__device__ void cand_insert(const PipeDev &p, unsigned long long key, unsigned long long order, float lox, float loy,
-                            float hix, float hiy) {
+// Merges one instance of a key that may occur twice in this step into the
+// candidate set (minimum priority); the candidate pass walks it afterwards.
+__device__ void cand_insert(const PipeDev &p, unsigned long long key, unsigned long long order) {
   unsigned long long h = mix64(key) & (p.C - 1);
   for (unsigned long long probe = 0; probe < STC_PROBE_LIMIT; probe++) {
     Cand *c = &p.cset[h];
@@ -77,10 +78,6 @@ __device__ void cand_insert(const PipeDev &p, unsigned long long key, unsigned l
     }
     if (k == key) {
       atomicMin(&c->order, order);
-      if (lox < c->lo_x) atomic_min_f(&c->lo_x, lox);
-      if (loy < c->lo_y) atomic_min_f(&c->lo_y, loy);
-      if (hix > c->hi_x) atomic_max_f(&c->hi_x, hix);
-      if (hiy > c->hi_y) atomic_max_f(&c->hi_y, hiy);
       return;
     }
     h = (h + 1) & (p.C - 1);
@@ -90,17 +87,18 @@ __device__ void cand_insert(const PipeDev &p, unsigned long long key, unsigned l
 
 // One pair within reach, waiting in its warp's queue.
 struct __align__(16) HitRec {
-  unsigned long long key, order;
+  unsigned long long key, order;  // order bit 63: the pair may occur twice this step
   float lo_x, lo_y, hi_x, hi_y;
 };
 
 static constexpr int QCAP = 64;  // per-warp queue; flushed 32 at a time
+#define DUP_BIT (1ULL << 63)
 
 __device__ void process_hit(const PipeDev &p, const HitRec &h, uint32_t t) {
   unsigned long long slot = h.key % p.B;
   for (unsigned long long probe = 0; probe < STC_PROBE_LIMIT && probe < p.B; probe++) {
     Slot *s = &p.slots[slot];
-    unsigned long long k = s->key;
+    unsigned long long k = *(volatile unsigned long long *)&s->key;
     if (k == h.key) {  // tracing/refinement.cpp:40-42 (+ MBR, cuda/geometry.cu:474-478)
       s->end = t;
       if (h.lo_x < s->lo_x) atomic_min_f(&s->lo_x, h.lo_x);
@@ -109,8 +107,13 @@ __device__ void process_hit(const PipeDev &p, const HitRec &h, uint32_t t) {
       if (h.hi_y > s->hi_y) atomic_max_f(&s->hi_y, h.hi_y);
       return;
     }
-    if (k == STC_EMPTY_KEY) {
-      cand_insert(p, h.key, h.order, h.lo_x, h.lo_y, h.hi_x, h.hi_y);
+    if (k == STC_EMPTY_KEY || (k & STC_CLAIM_BIT)) {  // empty before this step: a new key
+      if (h.order & DUP_BIT) {
+        cand_insert(p, h.key, h.order & ~DUP_BIT);
+      } else {
+        agg_inc(&p.st->fast_claims);
+        if (!ordered_walk(p, h.key, h.order, slot, t)) stc_set_error(p.st, ERR_DA, (uint32_t)(h.key % p.B));
+      }
       return;
     }
     slot = slot + 1 == p.B ? 0 : slot + 1;
@@ -180,6 +183,15 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
       rf = make_float2(__double2float_rn(qq.x), __double2float_rn(qq.y));
     }
   }
+  // A pair of a border row (pid1 outside leaf g) and member cpid occurs twice
+  // in this step iff cpid also has a border unit targeting pid1's leaf.
+  uint32_t row_leaf = (!own && vr) ? p.leaf_gid[pid1] : 0u;
+  uint32_t col_nb = 0, col_off = 0;
+  if (!own && vc) {
+    uint32_t cpid0 = __float_as_uint(cp.w);
+    col_nb = p.bcount[cpid0];
+    col_off = col_nb ? p.boff[cpid0] : 0u;
+  }
   // tile error margin
   float mx = warp_max(fmaxf(fabsf(rp.x), fabsf(cp.x)));
   float my = warp_max(fmaxf(fabsf(rp.y), fabsf(cp.y)));
@@ -198,6 +210,8 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
     uint32_t cpid = __shfl_sync(0xffffffffu, __float_as_uint(cp.w), k);
     float cfx = __shfl_sync(0xffffffffu, cf.x, k);
     float cfy = __shfl_sync(0xffffffffu, cf.y, k);
+    uint32_t cnb = own ? 0u : __shfl_sync(0xffffffffu, col_nb, k);
+    uint32_t coff = own ? 0u : __shfl_sync(0xffffffffu, col_off, k);
     uint32_t jj = coltile * 32 + k;
     bool hit = false;
     if (vr && !(own && jj <= i)) {  // tracing/refinement.cpp:30
@@ -219,6 +233,8 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
         HitRec h;
         h.key = stc_cantor(a, b);
         h.order = (rank << STC_ORDER_SHIFT) | jj;
+        for (uint32_t u2 = 0; u2 < cnb; u2++)
+          if (p.bu_gid[coff + u2] == row_leaf) h.order |= DUP_BIT;
         h.lo_x = fminf(rf.x, cfx);
         h.lo_y = fminf(rf.y, cfy);
         h.hi_x = fmaxf(rf.x, cfx);
