@@ -69,6 +69,7 @@ typedef struct stc_config {
   int32_t mbr_filter;            /* drop meetings whose MBR leaves the map box (cuda/geometry.cu:667-670) */
   uint64_t candidate_capacity;   /* new-meeting candidates per step; 0 = auto */
   uint64_t emit_capacity;        /* emitted meetings held between drains; 0 = auto */
+  uint64_t hit_capacity;         /* pairs buffered between refinement and table update; 0 = auto */
   uint32_t device;               /* CUDA device ordinal */
   uint32_t reserved;
 } stc_config;

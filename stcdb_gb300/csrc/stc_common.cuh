@@ -62,6 +62,13 @@ struct NodeMeta {
   uint32_t parent;
 };
 
+// One pair within reach found by the refinement, waiting to be applied to
+// the meeting table.
+struct __align__(16) HitRec {
+  unsigned long long key, order;  // order bit 63: the pair may occur twice this step
+  float lo_x, lo_y, hi_x, hi_y;
+};
+
 struct __align__(16) U128 {
   unsigned long long lo, hi;
 };
@@ -85,6 +92,7 @@ struct DevState {
   uint32_t pad[3];
   unsigned long long border_points;   // points whose lookup starts above their leaf
   unsigned long long fast_claims;     // new keys walked directly by the refinement
+  unsigned long long hit_count;       // hits appended to the hit buffer this step
 };
 
 __device__ __forceinline__ void stc_set_error(DevState *st, uint32_t code, uint32_t info) {

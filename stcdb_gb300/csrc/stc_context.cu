@@ -205,6 +205,8 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
   p.cand_cap = cand_cap;
   p.C = next_pow2(2 * cand_cap);
   p.E = k.emit_capacity ? k.emit_capacity : std::max<uint64_t>(1u << 20, 4ULL * n);
+  // hits beyond the buffer are applied inside the refinement instead
+  p.hit_cap = k.hit_capacity ? k.hit_capacity : std::max<uint64_t>(1u << 22, 8ULL * n);
   p.U_cap = (uint64_t)k.refine_size * n - n;
   p.reach = k.reach_distance;
   p.x_buffer = k.reach_distance * stc_dpml_ref(mbr[1]);  // tracing/filter.cpp:30
@@ -235,7 +237,7 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
             dalloc(c, &p.bu_gid, p.U_cap) && dalloc(c, &p.bu_pid, p.U_cap) && dalloc(c, &p.bu_sorted_gid, p.U_cap) &&
             dalloc(c, &p.bu_sorted_pos, p.U_cap) && dalloc(c, &p.bu_cnt, (size_t)p.G + 1) &&
             dalloc(c, &p.bu_start, (size_t)p.G + 1) && dalloc(c, &p.job_cnt, (size_t)p.G + 1) &&
-            dalloc(c, &p.job_start, (size_t)p.G + 1) && dalloc(c, &p.slots, p.B) && dalloc(c, &p.cset, p.C) &&
+            dalloc(c, &p.job_start, (size_t)p.G + 1) && dalloc(c, &p.slots, p.B) && dalloc(c, &p.hits, p.hit_cap) && dalloc(c, &p.cset, p.C) &&
             dalloc(c, &p.cand_list, p.cand_cap) && dalloc(c, &p.emit, p.E) && dalloc(c, &p.scan_tmp, scan_words) &&
             dalloc(c, &p.n_dev, 1);
   if (!ok) {

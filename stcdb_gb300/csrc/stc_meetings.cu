@@ -37,6 +37,7 @@ __global__ void k_step_begin(DevState *st) {
   st->border_units = 0;
   st->border_points = 0;
   st->fast_claims = 0;
+  st->hit_count = 0;
   st->jobs_total = 0;
   st->job_next = 0;
   st->cand_count = 0;

@@ -40,6 +40,8 @@ struct PipeDev {
   uint32_t *job_cnt, *job_start;        // G+1
   // meetings
   Slot *slots;                          // B
+  HitRec *hits;                         // hit_cap: hits of the step, applied by k_hits
+  unsigned long long hit_cap;
   Cand *cset;                           // C
   uint32_t *cand_list;                  // cand_cap
   stc_meeting *emit;                    // E

@@ -45,7 +45,7 @@ __device__ __forceinline__ double dpml_fast_r(double lat) {
 }
 
 // Reference distance decision for p1 (whose latitude sets the scale) and p2.
-__device__ bool exact_within(const PipeDev &p, uint32_t pid1, uint32_t pid2, unsigned long long &amb) {
+__device__ bool exact_within(const PipeDev &p, uint32_t pid1, uint32_t pid2, uint32_t &amb) {
   double2 a = p.xy[pid1], b = p.xy[pid2];
   double d = stc_distance_ref(a.x, a.y, b.x, b.y, dpml_fast_r(a.y));
   if (fabs(d - p.reach) > 1e-12 * p.reach) return d <= p.reach;
@@ -85,11 +85,6 @@ __device__ void cand_insert(const PipeDev &p, unsigned long long key, unsigned l
   stc_set_error(p.st, ERR_CAND, 0xFFFFFFFFu);
 }
 
-// One pair within reach, waiting in its warp's queue.
-struct __align__(16) HitRec {
-  unsigned long long key, order;  // order bit 63: the pair may occur twice this step
-  float lo_x, lo_y, hi_x, hi_y;
-};
 
 static constexpr int QCAP = 64;  // per-warp queue; flushed 32 at a time
 #define DUP_BIT (1ULL << 63)
@@ -121,16 +116,31 @@ __device__ void process_hit(const PipeDev &p, const HitRec &h, uint32_t t) {
   stc_set_error(p.st, ERR_PROBE, (uint32_t)(h.key % p.B));
 }
 
-// Processes the first `n` (<= 32) queued hits, one per lane, so that their
-// random-access probe chains overlap.
+// Moves the first `n` (<= 32) queued hits to the step's hit buffer, which
+// k_hits processes with one thread per hit; hits that do not fit are
+// processed here, one per lane.
 __device__ __forceinline__ void flush_queue(const PipeDev &p, HitRec *q, uint32_t n, uint32_t t) {
   __syncwarp();
   uint32_t lane = lane_id();
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(&p.st->hit_count, (unsigned long long)n);
+  base = __shfl_sync(0xffffffffu, base, 0);
   if (lane < n) {
     HitRec h = q[lane];
-    process_hit(p, h, t);
+    unsigned long long pos = base + lane;
+    if (pos < p.hit_cap) p.hits[pos] = h;
+    else process_hit(p, h, t);
   }
   __syncwarp();
+}
+
+__global__ void __launch_bounds__(256) k_hits(PipeDev p, uint32_t t) {
+  const unsigned long long nh = p.st->hit_count < p.hit_cap ? p.st->hit_count : p.hit_cap;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < nh;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    HitRec h = p.hits[i];
+    process_hit(p, h, t);
+  }
 }
 
 __device__ __forceinline__ float warp_max(float v) {
@@ -140,7 +150,7 @@ __device__ __forceinline__ float warp_max(float v) {
 }
 
 struct Counters {
-  unsigned long long tests, exact, hits, amb;
+  uint32_t tests, exact, hits, amb;  // per thread; summed into 64-bit totals per warp
 };
 
 // One 32x32 tile. Rows: own members (own=true) or border units.
@@ -256,7 +266,7 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
   }
 }
 
-__global__ void __launch_bounds__(REFINE_THREADS) k_refine_a(PipeDev p, uint32_t t) {
+__global__ void __launch_bounds__(REFINE_THREADS, 3) k_refine_a(PipeDev p, uint32_t t) {
   __shared__ HitRec queues[REFINE_THREADS / 32][QCAP];
   HitRec *q = queues[threadIdx.x >> 5];
   uint32_t qn = 0;  // warp-uniform queue length
@@ -299,24 +309,26 @@ __global__ void __launch_bounds__(REFINE_THREADS) k_refine_a(PipeDev p, uint32_t
     }
   }
   if (qn) flush_queue(p, q, qn, t);
-  // reduce counters per warp
+  // reduce counters per warp (64-bit sums)
+  unsigned long long tests = ct.tests, exact = ct.exact, hits = ct.hits, amb = ct.amb;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    ct.tests += __shfl_xor_sync(0xffffffffu, ct.tests, o);
-    ct.exact += __shfl_xor_sync(0xffffffffu, ct.exact, o);
-    ct.hits += __shfl_xor_sync(0xffffffffu, ct.hits, o);
-    ct.amb += __shfl_xor_sync(0xffffffffu, ct.amb, o);
+    tests += __shfl_xor_sync(0xffffffffu, tests, o);
+    exact += __shfl_xor_sync(0xffffffffu, exact, o);
+    hits += __shfl_xor_sync(0xffffffffu, hits, o);
+    amb += __shfl_xor_sync(0xffffffffu, amb, o);
   }
   if (lane_id() == 0) {
-    if (ct.tests) atomicAdd(&p.st->tests, ct.tests);
-    if (ct.exact) atomicAdd(&p.st->exact_tests, ct.exact);
-    if (ct.hits) atomicAdd(&p.st->hits, ct.hits);
-    if (ct.amb) atomicAdd(&p.st->ambiguous, ct.amb);
+    if (tests) atomicAdd(&p.st->tests, tests);
+    if (exact) atomicAdd(&p.st->exact_tests, exact);
+    if (hits) atomicAdd(&p.st->hits, hits);
+    if (amb) atomicAdd(&p.st->ambiguous, amb);
   }
 }
 
 void step_refine(PipeDev &p, uint32_t t, cudaStream_t s) {
   STC_KL k_refine_a<<<STC_NUM_SMS * 8, REFINE_THREADS, 0, s>>>(p, t);
+  STC_KL k_hits<<<STC_NUM_SMS * 16, 256, 0, s>>>(p, t);
 }
 
 }  // namespace stc

@@ -42,6 +42,7 @@ class _Config(ctypes.Structure):
         ("mbr_filter", ctypes.c_int32),
         ("candidate_capacity", ctypes.c_uint64),
         ("emit_capacity", ctypes.c_uint64),
+        ("hit_capacity", ctypes.c_uint64),
         ("device", ctypes.c_uint32),
         ("reserved", ctypes.c_uint32),
     ]
@@ -94,6 +95,7 @@ class StcConfig:
     mbr_filter: bool = True
     candidate_capacity: int = 0
     emit_capacity: int = 0
+    hit_capacity: int = 0
     device: int = 0
 
     def resolved(self) -> "StcConfig":
