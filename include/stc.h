@@ -71,8 +71,12 @@ typedef struct stc_config {
   uint64_t emit_capacity;        /* emitted meetings held between drains; 0 = auto */
   uint64_t hit_capacity;         /* pairs buffered between refinement and table update; 0 = auto */
   uint32_t device;               /* CUDA device ordinal */
-  uint32_t reserved;
+  uint32_t flags;                /* STC_FLAG_* (0 for normal operation) */
 } stc_config;
+
+/* Replay quadtree splits/merges on one device thread only (tests compare it
+ * with the default parallel replay). */
+#define STC_FLAG_SERIAL_SCHEMA 1u
 
 /* One finished meeting. pid_lo < pid_hi; start/end are the first and last
  * step in which the pair was within reach; mbr is the float bounding box of
@@ -93,7 +97,7 @@ typedef struct stc_stats {
   uint64_t pair_tests;           /* candidate pairs tested */
   uint64_t exact_tests;          /* tests that needed the fp64 reference arithmetic */
   uint64_t hits;                 /* pairs within reach */
-  uint64_t new_candidates;       /* distinct keys that needed ordered insertion */
+  uint64_t new_candidates;       /* meetings started by the step (ordered insertions) */
   uint64_t taken_buckets;        /* occupied slots after the step */
   uint64_t emitted;              /* meetings emitted by the step */
   uint64_t pending;              /* emitted meetings not yet drained */

@@ -91,7 +91,7 @@ struct DevState {
   uint32_t work_next;                 // generic persistent-kernel work counter
   uint32_t pad[3];
   unsigned long long border_points;   // points whose lookup starts above their leaf
-  unsigned long long fast_claims;     // new keys walked directly by the refinement
+  unsigned long long fast_claims;     // new meetings started this step (claims finalised by the sweep)
   unsigned long long hit_count;       // hits appended to the hit buffer this step
 };
 

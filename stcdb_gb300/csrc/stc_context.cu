@@ -227,7 +227,7 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
             dalloc(c, &p.sw.bsub_leaves, p.S) && dalloc(c, &p.sw.bpre, p.S) && dalloc(c, &p.sw.bleafbase, p.S) &&
             dalloc(c, &p.sw.node_of, n) && dalloc(c, &p.sw.ev_flag, p.S) && dalloc(c, &p.sw.ev_pos, p.S) &&
             dalloc(c, &p.sw.ev_list, p.S) && dalloc(c, &p.sw.old_under, p.S) && dalloc(c, &p.sw.heap, p.S) &&
-            dalloc(c, &p.sw.ev_total, 1) && dalloc(c, &p.sw.queued, p.S) && dalloc(c, &p.leaf_gid, n) &&
+            dalloc(c, &p.sw.ev_total, 2) && dalloc(c, &p.sw.queued, p.S) && dalloc(c, &p.leaf_gid, n) &&
             dalloc(c, &p.lastvalid, n) && dalloc(c, &p.iota, nu) && dalloc(c, &p.sorted_gid, n) &&
             dalloc(c, &p.sorted_pid, n) && dalloc(c, &p.sort_ktmp, nu) && dalloc(c, &p.sort_vtmp, nu) &&
             dalloc(c, &p.sort_hist, radix_hist_words(nu)) && dalloc(c, &p.grid_count, (size_t)p.G + 1) &&
@@ -303,7 +303,8 @@ static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copie
   step_sweep(p, t, s);
   cudaEventRecord(c->ev[PH_SWEEP], s);
   if (c->cfg.dynamic_schema)
-    update_schema(p.sd, p.sw, p.grid_count, p.reach, p.grid_capacity, p.delay, p.st, s);
+    update_schema(p.sd, p.sw, p.grid_count, p.reach, p.grid_capacity, p.delay,
+                  (c->cfg.flags & STC_FLAG_SERIAL_SCHEMA) != 0, p.st, s);
   cudaEventRecord(c->ev[PH_SCHEMA], s);
   stc_status rs = read_state(c, "stc_step");
   if (rs != STC_OK) return rs;
@@ -318,7 +319,7 @@ static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copie
   o.pair_tests = h.tests;
   o.exact_tests = h.exact_tests;
   o.hits = h.hits;
-  o.new_candidates = h.cand_count + h.fast_claims;
+  o.new_candidates = h.fast_claims;  // new meetings started by the step
   o.taken_buckets = h.taken;
   o.emitted = h.step_emitted;
   o.pending = std::min<unsigned long long>(h.emit_count, p.E);

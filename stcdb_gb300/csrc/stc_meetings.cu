@@ -105,7 +105,7 @@ void step_insert(PipeDev &p, uint32_t t, cudaStream_t s) {
 // Sweep (tracing/meeting.cpp:32-76, cuda/geometry.cu:595-736).
 __global__ void __launch_bounds__(256) k_sweep(PipeDev p, uint32_t t) {
   const uint32_t lane = lane_id();
-  unsigned long long active = 0;
+  unsigned long long active = 0, fresh = 0;
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
   const unsigned long long B = p.B;
   // iterate so that whole warps stay converged for the ballot
@@ -133,6 +133,7 @@ __global__ void __launch_bounds__(256) k_sweep(PipeDev p, uint32_t t) {
           nm.hi_y = fmaxf(STC_INIT_HI, fmaxf(fa.y, fb.y));
           p.slots[i] = nm;
           active++;
+          fresh++;
         } else if (s.end == t) {
           active++;
         } else {
@@ -172,8 +173,12 @@ __global__ void __launch_bounds__(256) k_sweep(PipeDev p, uint32_t t) {
     }
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) active += __shfl_xor_sync(0xffffffffu, active, o);
+  for (int o = 16; o > 0; o >>= 1) {
+    active += __shfl_xor_sync(0xffffffffu, active, o);
+    fresh += __shfl_xor_sync(0xffffffffu, fresh, o);
+  }
   if (lane == 0 && active) atomicAdd(&p.st->taken, active);
+  if (lane == 0 && fresh) atomicAdd(&p.st->fast_claims, fresh);
 }
 
 void step_sweep(PipeDev &p, uint32_t t, cudaStream_t s) {

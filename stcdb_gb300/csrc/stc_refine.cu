@@ -106,7 +106,6 @@ __device__ void process_hit(const PipeDev &p, const HitRec &h, uint32_t t) {
       if (h.order & DUP_BIT) {
         cand_insert(p, h.key, h.order & ~DUP_BIT);
       } else {
-        agg_inc(&p.st->fast_claims);
         if (!ordered_walk(p, h.key, h.order, slot, t)) stc_set_error(p.st, ERR_DA, (uint32_t)(h.key % p.B));
       }
       return;
@@ -116,21 +115,36 @@ __device__ void process_hit(const PipeDev &p, const HitRec &h, uint32_t t) {
   stc_set_error(p.st, ERR_PROBE, (uint32_t)(h.key % p.B));
 }
 
+// Per-warp window of the step's hit buffer, reserved HIT_CHUNK entries at a
+// time so that the shared counter sees one atomic per HIT_CHUNK hits.
+static constexpr uint32_t HIT_CHUNK = 256;
+struct HitWindow {
+  unsigned long long next, end;  // warp-uniform
+};
+
 // Moves the first `n` (<= 32) queued hits to the step's hit buffer, which
 // k_hits processes with one thread per hit; hits that do not fit are
 // processed here, one per lane.
-__device__ __forceinline__ void flush_queue(const PipeDev &p, HitRec *q, uint32_t n, uint32_t t) {
+__device__ __forceinline__ void flush_queue(const PipeDev &p, HitRec *q, uint32_t n, uint32_t t, HitWindow &w) {
   __syncwarp();
   uint32_t lane = lane_id();
-  unsigned long long base = 0;
-  if (lane == 0) base = atomicAdd(&p.st->hit_count, (unsigned long long)n);
-  base = __shfl_sync(0xffffffffu, base, 0);
+  if (w.end - w.next < n) {
+    // pad the rest of the old window with empty records, then reserve a new one
+    for (unsigned long long i = w.next + lane; i < w.end; i += 32)
+      if (i < p.hit_cap) p.hits[i].key = STC_EMPTY_KEY;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&p.st->hit_count, (unsigned long long)HIT_CHUNK);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    w.next = base;
+    w.end = base + HIT_CHUNK;
+  }
   if (lane < n) {
     HitRec h = q[lane];
-    unsigned long long pos = base + lane;
+    unsigned long long pos = w.next + lane;
     if (pos < p.hit_cap) p.hits[pos] = h;
     else process_hit(p, h, t);
   }
+  w.next += n;
   __syncwarp();
 }
 
@@ -139,7 +153,7 @@ __global__ void __launch_bounds__(256) k_hits(PipeDev p, uint32_t t) {
   for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < nh;
        i += (unsigned long long)gridDim.x * blockDim.x) {
     HitRec h = p.hits[i];
-    process_hit(p, h, t);
+    if (h.key != STC_EMPTY_KEY) process_hit(p, h, t);
   }
 }
 
@@ -155,7 +169,7 @@ struct Counters {
 
 // One 32x32 tile. Rows: own members (own=true) or border units.
 __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtile, uint32_t coltile, uint32_t n,
-                         uint32_t t, Counters &ct, HitRec *q, uint32_t &qn) {
+                         uint32_t t, Counters &ct, HitRec *q, uint32_t &qn, HitWindow &w) {
   const uint32_t lane = lane_id();
   const uint32_t base = p.grid_start[g];
   const uint32_t lt_mask = (1u << lane) - 1u;
@@ -253,7 +267,7 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
       }
       qn += __popc(hm);
       if (qn >= 32) {
-        flush_queue(p, q, 32, t);
+        flush_queue(p, q, 32, t, w);
         uint32_t rest = qn - 32;
         HitRec mv;
         if (lane < rest) mv = q[32 + lane];
@@ -270,6 +284,7 @@ __global__ void __launch_bounds__(REFINE_THREADS, 3) k_refine_a(PipeDev p, uint3
   __shared__ HitRec queues[REFINE_THREADS / 32][QCAP];
   HitRec *q = queues[threadIdx.x >> 5];
   uint32_t qn = 0;  // warp-uniform queue length
+  HitWindow w = {0, 0};
   const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
   const unsigned long long J = p.st->jobs_total;
@@ -301,14 +316,16 @@ __global__ void __launch_bounds__(REFINE_THREADS, 3) k_refine_a(PipeDev p, uint3
         while (rc > 0 && rc * R - rc * (rc - 1) / 2 > local) rc--;
         while ((rc + 1) * R - (rc + 1) * rc / 2 <= local) rc++;
         uint32_t cc = rc + (local - (rc * R - rc * (rc - 1) / 2));
-        run_tile(p, g, true, rc, cc, n, t, ct, q, qn);
+        run_tile(p, g, true, rc, cc, n, t, ct, q, qn, w);
       } else {
         uint32_t b = local - own;
-        run_tile(p, g, false, b / R, b % R, n, t, ct, q, qn);
+        run_tile(p, g, false, b / R, b % R, n, t, ct, q, qn, w);
       }
     }
   }
-  if (qn) flush_queue(p, q, qn, t);
+  if (qn) flush_queue(p, q, qn, t, w);
+  for (unsigned long long i = w.next + lane_id(); i < w.end; i += 32)
+    if (i < p.hit_cap) p.hits[i].key = STC_EMPTY_KEY;
   // reduce counters per warp (64-bit sums)
   unsigned long long tests = ct.tests, exact = ct.exact, hits = ct.hits, amb = ct.amb;
 #pragma unroll

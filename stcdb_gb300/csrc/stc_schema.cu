@@ -370,10 +370,220 @@ __device__ uint32_t heap_pop(uint32_t *h, uint32_t &n) {
   return top;
 }
 
+
+// Parallel replay of the flagged events for the common case: at most
+// PAR_MAX_EVENTS events and no merge whose parent has a higher index (the
+// only source of a cascade). Without cascades every event's decision is fixed
+// by phase 1, and the sequential replay's only coupling is through the two
+// free stacks: a split pops 4 node slots and, after pushing its own grid id,
+// 4 grid ids (net +4 / +3); a merge pushes its 4 children and their grid ids
+// and pops the last one back (net -4 / -3). Prefix sums give every event its
+// stack positions; a pop reads the most recent earlier push to its position
+// (or the stack's old content); merges are applied before splits because a
+// node or grid id freed by a merge can only be reused by a later split. The
+// per-step grid counts are not reset: nothing reads them before the next
+// step recounts. Sets *done; k_schema_phase2 then does nothing.
+static constexpr int PAR_MAX_EVENTS = 1024;  // keeps the block's static shared memory under 48 KB
+
+__global__ void __launch_bounds__(1024) k_schema_phase2_par(SchemaDev sd, const uint32_t *ev_list,
+                                                            const unsigned long long *ev_total,
+                                                            unsigned int *done, int serial_only, DevState *st) {
+  __shared__ uint32_t ev_node[PAR_MAX_EVENTS];
+  __shared__ uint8_t ev_kind[PAR_MAX_EVENTS];
+  __shared__ int32_t s0[PAR_MAX_EVENTS], g0[PAR_MAX_EVENTS];
+  __shared__ uint32_t spush[PAR_MAX_EVENTS][4], gpush[PAR_MAX_EVENTS][4];
+  __shared__ int cascade;
+  __shared__ uint32_t warp_s[32], warp_g[32];
+  const uint32_t tid = threadIdx.x;
+  uint32_t nev = (uint32_t)*ev_total;
+  if (tid == 0) {
+    *done = 0;
+    cascade = 0;
+  }
+  if (nev > PAR_MAX_EVENTS || serial_only) return;
+  __syncthreads();
+  for (uint32_t e = tid; e < nev; e += blockDim.x) {
+    uint32_t v = ev_list[e];
+    uint32_t node = v >> 2, kind = v & 3u;
+    ev_node[e] = node;
+    ev_kind[e] = (uint8_t)kind;
+    if (kind == EV_MERGE) {
+      uint32_t par = sd.meta[node].parent;
+      if (node != 0 && par != STC_NONE && par > node) cascade = 1;
+    }
+  }
+  __syncthreads();
+  if (cascade) return;
+  // exclusive scan of the stack deltas (each thread owns a contiguous chunk)
+  uint32_t per = (nev + blockDim.x - 1) / blockDim.x;
+  uint32_t e0 = tid * per, e1 = min(nev, e0 + per);
+  int ds = 0, dg = 0;
+  for (uint32_t e = e0; e < e1; e++) {
+    ds += ev_kind[e] == EV_SPLIT ? 4 : -4;
+    dg += ev_kind[e] == EV_SPLIT ? 3 : -3;
+  }
+  // block scan of (ds, dg)
+  uint32_t lane = tid & 31u, warp = tid >> 5;
+  int is = ds, ig = dg;
+  for (int o = 1; o < 32; o <<= 1) {
+    int a = __shfl_up_sync(0xffffffffu, is, o), b = __shfl_up_sync(0xffffffffu, ig, o);
+    if ((int)lane >= o) { is += a; ig += b; }
+  }
+  if (lane == 31) { warp_s[warp] = (uint32_t)is; warp_g[warp] = (uint32_t)ig; }
+  __syncthreads();
+  if (warp == 0) {
+    int a = (int)warp_s[lane], b = (int)warp_g[lane];
+    int ia = a, ib = b;
+    for (int o = 1; o < 32; o <<= 1) {
+      int x = __shfl_up_sync(0xffffffffu, ia, o), y = __shfl_up_sync(0xffffffffu, ib, o);
+      if ((int)lane >= o) { ia += x; ib += y; }
+    }
+    warp_s[lane] = (uint32_t)(ia - a);
+    warp_g[lane] = (uint32_t)(ib - b);
+  }
+  __syncthreads();
+  int bs = (int)st->schema_stack_index + (int)warp_s[warp] + is - ds;
+  int bg = (int)st->grids_stack_index + (int)warp_g[warp] + ig - dg;
+  for (uint32_t e = e0; e < e1; e++) {
+    s0[e] = bs;
+    g0[e] = bg;
+    bs += ev_kind[e] == EV_SPLIT ? 4 : -4;
+    bg += ev_kind[e] == EV_SPLIT ? 3 : -3;
+  }
+  __syncthreads();
+  // merges (tracing/filter.cpp:316-336); record every push
+  for (uint32_t e = tid; e < nev; e += blockDim.x) {
+    uint32_t cur = ev_node[e];
+    if (ev_kind[e] == EV_SPLIT) {
+      gpush[e][0] = sd.meta[cur].grid_id;
+      if (s0[e] + 4 > (int)sd.S || g0[e] < 1 || g0[e] + 3 > (int)sd.G) stc_set_error(st, ERR_SCHEMA, cur);
+      continue;
+    }
+    if (s0[e] < 4 || g0[e] < 4) stc_set_error(st, ERR_SCHEMA, cur);
+    Node q = sd.nodes[cur];
+    uint32_t last_gid = 0;
+    for (int i = 0; i < 4; i++) {
+      uint32_t ch = q.child[i];
+      uint32_t gid = sd.meta[ch].grid_id;
+      sd.meta[ch].type = NODE_INVALID;
+      spush[e][i] = ch;   // schema_stack[s0 - 1 - i]
+      gpush[e][i] = gid;  // grids_stack[g0 - 1 - i]
+      last_gid = gid;
+    }
+    NodeMeta cm = sd.meta[cur];
+    cm.type = NODE_LEAF;
+    cm.grid_id = last_gid;  // the pop returns the last pushed grid id
+    cm.underflow = 0;
+    sd.meta[cur] = cm;
+    sd.gid_node[last_gid] = cur;
+  }
+  __syncthreads();
+  if (!st->error) {
+    // splits (tracing/filter.cpp:338-375)
+    for (uint32_t e = tid; e < nev; e += blockDim.x) {
+      if (ev_kind[e] != EV_SPLIT) continue;
+      uint32_t cur = ev_node[e];
+      uint32_t child[4], gid[4];
+      for (int i = 0; i < 4; i++) {
+        // node slot popped at schema position s0 + i
+        int qs = s0[e] + i;
+        uint32_t v = sd.schema_stack[qs];
+        for (int f = (int)e - 1; f >= 0; f--)
+          if (ev_kind[f] == EV_MERGE && qs >= s0[f] - 4 && qs <= s0[f] - 1) { v = spush[f][s0[f] - 1 - qs]; break; }
+        child[i] = v;
+        // grid id popped at grid position g0 - 1 + i (the first is this split's own push)
+        int qg = g0[e] - 1 + i;
+        uint32_t w = i == 0 ? gpush[e][0] : sd.grids_stack[qg];
+        if (i > 0) {
+          for (int f = (int)e - 1; f >= 0; f--) {
+            if (ev_kind[f] == EV_MERGE && qg >= g0[f] - 4 && qg <= g0[f] - 1) { w = gpush[f][g0[f] - 1 - qg]; break; }
+            if (ev_kind[f] == EV_SPLIT && qg == g0[f] - 1) { w = gpush[f][0]; break; }
+          }
+        }
+        gid[i] = w;
+      }
+      Node q = sd.nodes[cur];
+      NodeMeta cm = sd.meta[cur];
+      double xhalf = RN_SUB(q.mid_x, q.lo_x);
+      double yhalf = RN_SUB(q.mid_y, q.lo_y);
+      for (int i = 0; i < 4; i++) {
+        Node c;
+        c.lo_x = RN_ADD(q.lo_x, (i % 2 == 1) ? xhalf : 0.0);
+        c.lo_y = RN_ADD(q.lo_y, (i / 2 == 1) ? yhalf : 0.0);
+        c.hi_x = RN_ADD(q.mid_x, (i % 2 == 1) ? xhalf : 0.0);
+        c.hi_y = RN_ADD(q.mid_y, (i / 2 == 1) ? yhalf : 0.0);
+        c.mid_x = RN_DIV(RN_ADD(c.lo_x, c.hi_x), 2.0);
+        c.mid_y = RN_DIV(RN_ADD(c.lo_y, c.hi_y), 2.0);
+        c.child[0] = c.child[1] = c.child[2] = c.child[3] = STC_NONE;
+        sd.nodes[child[i]] = c;
+        sd.fbox[child[i]] = make_float4(__double2float_rn(RN_SUB(c.lo_x, sd.ox)), __double2float_rn(RN_SUB(c.lo_y, sd.oy)),
+                                        __double2float_rn(RN_SUB(c.hi_x, sd.ox)), __double2float_rn(RN_SUB(c.hi_y, sd.oy)));
+        NodeMeta m;
+        m.type = NODE_LEAF; m.level = (int16_t)(cm.level + 1); m.overflow = 0; m.underflow = 0;
+        m.grid_id = gid[i]; m.parent = cur;
+        sd.meta[child[i]] = m;
+        sd.gid_node[gid[i]] = child[i];
+        q.child[i] = child[i];
+      }
+      sd.nodes[cur] = q;
+      cm.type = NODE_BRANCH;
+      cm.overflow = 0;
+      sd.meta[cur] = cm;
+    }
+    __syncthreads();
+    // final stack contents: the last push to each position wins
+    for (uint32_t e = tid; e < nev; e += blockDim.x) {
+      if (ev_kind[e] == EV_MERGE) {
+        for (int i = 0; i < 4; i++) {
+          int qs = s0[e] - 1 - i, qg = g0[e] - 1 - i;
+          bool last_s = true, last_g = true;
+          for (uint32_t f = e + 1; f < nev; f++) {
+            if (ev_kind[f] == EV_MERGE) {
+              if (qs >= s0[f] - 4 && qs <= s0[f] - 1) last_s = false;
+              if (qg >= g0[f] - 4 && qg <= g0[f] - 1) last_g = false;
+            } else if (qg == g0[f] - 1) {
+              last_g = false;
+            }
+          }
+          if (last_s) sd.schema_stack[qs] = spush[e][i];
+          if (last_g) sd.grids_stack[qg] = gpush[e][i];
+        }
+      } else {
+        int qg = g0[e] - 1;
+        bool last_g = true;
+        for (uint32_t f = e + 1; f < nev; f++) {
+          if (ev_kind[f] == EV_MERGE) {
+            if (qg >= g0[f] - 4 && qg <= g0[f] - 1) last_g = false;
+          } else if (qg == g0[f] - 1) {
+            last_g = false;
+          }
+        }
+        if (last_g) sd.grids_stack[qg] = gpush[e][0];
+      }
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    uint32_t splits = 0, merges = 0;
+    for (uint32_t e = 0; e < nev; e++) (ev_kind[e] == EV_SPLIT ? splits : merges)++;
+    if (nev) {
+      uint32_t l = nev - 1;
+      st->schema_stack_index = (uint32_t)(s0[l] + (ev_kind[l] == EV_SPLIT ? 4 : -4));
+      st->grids_stack_index = (uint32_t)(g0[l] + (ev_kind[l] == EV_SPLIT ? 3 : -3));
+    }
+    st->splits = splits;
+    st->merges = merges;
+    st->events = nev;
+    *done = 1;
+  }
+}
+
 __global__ void k_schema_phase2(SchemaDev sd, uint32_t *grid_count, const uint32_t *ev_list,
                                 const unsigned long long *ev_total, const int16_t *old_under, uint32_t *heap,
-                                uint8_t *queued, uint32_t cap, uint32_t delay, DevState *st) {
+                                uint8_t *queued, uint32_t cap, uint32_t delay, const unsigned int *done,
+                                DevState *st) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (*done) return;  // handled by k_schema_phase2_par
   uint32_t nev = (uint32_t)*ev_total;
   uint32_t hn = 0, ei = 0;
   uint32_t splits = 0, merges = 0;
@@ -429,14 +639,16 @@ __global__ void k_schema_phase2(SchemaDev sd, uint32_t *grid_count, const uint32
 }
 
 void update_schema(SchemaDev sd, SchemaWork w, uint32_t *grid_count, double reach, uint32_t grid_capacity,
-                   uint32_t delay, DevState *st, cudaStream_t s) {
+                   uint32_t delay, int serial_only, DevState *st, cudaStream_t s) {
   STC_KL k_schema_phase1<<<nblk(sd.S), 256, 0, s>>>(sd, grid_count, reach, grid_capacity, delay, w.ev_flag, w.old_under);
   // ordered compaction of the flagged node indices: ev_pos = exclusive scan of (flag != 0)
   STC_KL k_flags_to_bits<<<nblk(sd.S), 256, 0, s>>>(w.ev_flag, w.ev_pos, sd.S);
   exclusive_scan_u32(w.ev_pos, w.ev_pos, sd.S, w.ev_total, w.scan_tmp, s);
   STC_KL k_schema_compact<<<nblk(sd.S), 256, 0, s>>>(w.ev_flag, w.ev_pos, sd.S, w.ev_list);
+  unsigned int *done = (unsigned int *)(w.ev_total + 1);
+  STC_KL k_schema_phase2_par<<<1, 1024, 0, s>>>(sd, w.ev_list, w.ev_total, done, serial_only, st);
   STC_KL k_schema_phase2<<<1, 32, 0, s>>>(sd, grid_count, w.ev_list, w.ev_total, w.old_under, w.heap, w.queued,
-                                   grid_capacity, delay, st);
+                                   grid_capacity, delay, done, st);
 }
 
 }  // namespace stc

@@ -18,6 +18,8 @@ from ._lib import load_library
 MEETING_DTYPE = np.dtype([("pid_lo", "<u4"), ("pid_hi", "<u4"), ("start", "<u4"), ("end", "<u4"),
                           ("mbr", "<f4", (4,))])
 
+FLAG_SERIAL_SCHEMA = 1
+
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "CUDA", 3: "CAPACITY", 4: "TIMEOUT", 5: "UNSUPPORTED", 6: "STATE"}
 
 
@@ -44,7 +46,7 @@ class _Config(ctypes.Structure):
         ("emit_capacity", ctypes.c_uint64),
         ("hit_capacity", ctypes.c_uint64),
         ("device", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("flags", ctypes.c_uint32),
     ]
 
 
@@ -97,6 +99,7 @@ class StcConfig:
     emit_capacity: int = 0
     hit_capacity: int = 0
     device: int = 0
+    flags: int = 0            # STC_FLAG_* bits of include/stc.h
 
     def resolved(self) -> "StcConfig":
         if self.num_meeting_buckets == 0:

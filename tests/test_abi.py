@@ -1,0 +1,40 @@
+"""The C-ABI library loads and exports every entry point of include/stc.h;
+argument validation happens before any device call."""
+import ctypes
+import os
+import re
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "stc.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(stc_[a-z_]+)\s*\(", text)))
+
+
+def test_exports(built_cuda):
+    from stcdb_gb300._lib import load_library
+    lib = load_library("libstc")
+    names = declared_functions()
+    assert "stc_step" in names and "stc_create" in names
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in include/stc.h but not exported"
+
+
+def test_defaults_and_validation(built_cuda):
+    from stcdb_gb300.pipeline import _Config, _lib
+    lib = _lib()
+    c = _Config()
+    lib.stc_config_default(ctypes.byref(c), 1000)
+    assert c.num_objects == 1000 and c.grid_capacity == 50 and c.num_meeting_buckets == 2000
+    assert abs(c.reach_distance - 2.0) < 1e-12 and c.min_meet_time == 5 and c.refine_size == 4
+    h = ctypes.c_void_p()
+    mbr = np.array([0.0, 0.0, 1.0, 1.0])
+    xy = np.zeros((1000, 2))
+    c.grid_capacity = 0  # invalid: rejected before touching a device
+    st = lib.stc_create(ctypes.byref(c), mbr.ctypes.data, xy.ctypes.data, 1000, ctypes.byref(h))
+    assert st == 1 and not h.value
+    assert b"invalid" in lib.stc_last_error(None)

@@ -38,3 +38,53 @@ def test_hotspot_dense_chain_breaks(built_cuda):
     cfg = StcConfig(num_objects=30000, reach_distance=10.0, min_meet_time=3, grid_capacity=50, grid_amplify=1.2,
                     num_meeting_buckets=1_500_000)
     assert _check(cfg, tc, 15) > 0
+
+
+def test_serial_schema_replay_matches(built_cuda):
+    """The one-thread split/merge replay and the parallel one agree."""
+    from stcdb_gb300.pipeline import FLAG_SERIAL_SCHEMA
+    tc = hotspot_grid(30000, n_hotspots=30, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=12)
+    cfg = StcConfig(num_objects=30000, reach_distance=10.0, min_meet_time=3, grid_capacity=50,
+                    num_meeting_buckets=1_500_000, flags=FLAG_SERIAL_SCHEMA)
+    assert _check(cfg, tc, 12) > 0
+
+
+def test_table_full_reports_capacity(built_cuda):
+    """A meeting table too small for the live pairs returns STC_ERR_CAPACITY
+    (bounded probe walks), never hangs, and the context can be destroyed."""
+    from stcdb_gb300.pipeline import Pipeline, StcError
+    tr, mbr = trace_and_box(hotspot_grid(20000, n_hotspots=20, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=2), 2)
+    cfg = StcConfig(num_objects=20000, reach_distance=10.0, grid_capacity=50, num_meeting_buckets=5000)
+    p = Pipeline(cfg, mbr, tr[0])
+    with pytest.raises(StcError) as e:
+        p.step(tr[0], 0)
+    assert e.value.status in (3, 4)
+    with pytest.raises(StcError) as e2:
+        p.step(tr[1], 1)  # a failed context refuses further steps
+    assert e2.value.status == 6
+    p.close()
+
+
+def test_partial_drain(built_cuda):
+    """Draining in small pieces returns the same meetings as one drain."""
+    import ctypes
+    from stcdb_gb300.pipeline import MEETING_DTYPE, Pipeline
+    tr, mbr = trace_and_box(hotspot_grid(20000, n_hotspots=20, box_m=3000.0, grid_n=16, sigma_m=150.0, seed=5), 9)
+    cfg = StcConfig(num_objects=20000, reach_distance=10.0, min_meet_time=3, grid_capacity=50,
+                    num_meeting_buckets=1 << 20)
+    with Pipeline(cfg, mbr, tr[0]) as a, Pipeline(cfg, mbr, tr[0]) as b:
+        for t in range(9):
+            a.step(tr[t], t)
+            b.step(tr[t], t)
+        whole = a.drain()
+        parts = []
+        while True:
+            buf = np.zeros(37, dtype=MEETING_DTYPE)
+            n = ctypes.c_size_t()
+            assert b._lib.stc_drain_meetings(b._h, buf.ctypes.data, 37, ctypes.byref(n)) == 0
+            parts.append(buf[: n.value])
+            if n.value < 37:
+                break
+        got = np.concatenate(parts)
+        assert len(whole) > 37
+        assert np.array_equal(whole, got)
