@@ -316,7 +316,8 @@ def main():
         "per_step": {"pair_tests": s_last.pair_tests, "exact_tests": s_last.exact_tests, "hits": s_last.hits,
                      "new_candidates": s_last.new_candidates, "live_meetings": s_last.taken_buckets,
                      "emitted": s_last.emitted, "border_units": s_last.border_units, "leaves": s_last.leaves,
-                     "overflow_objects": s_last.overflow_objects, "ambiguous_tests": s_last.ambiguous_tests},
+                     "overflow_objects": s_last.overflow_objects, "ambiguous_tests": s_last.ambiguous_tests,
+                     "splits": s_last.splits, "merges": s_last.merges, "schema_path": s_last.schema_path},
         "wall_s": {"device_steps": r["wall_dev"], "e2e_steps": r["wall_e2e"]},
         "clocks": r["clocks"],
         "cpu_baseline": base,

@@ -103,6 +103,7 @@ typedef struct stc_stats {
   uint64_t pending;              /* emitted meetings not yet drained */
   uint32_t splits, merges;       /* schema updates applied after the step */
   uint32_t kernel_launches;      /* kernels launched by the step */
+  uint32_t schema_path;          /* split/merge replay used: 1 parallel, 0 or 2 one-thread */
   uint32_t ambiguous_tests;      /* distance decisions within a few ulp of reach, where
                                     the last bit of sin() could matter */
   float step_ms;                 /* device time of the step */

@@ -93,6 +93,8 @@ struct DevState {
   unsigned long long border_points;   // points whose lookup starts above their leaf
   unsigned long long fast_claims;     // new meetings started this step (claims finalised by the sweep)
   unsigned long long hit_count;       // hits appended to the hit buffer this step
+  uint32_t schema_path;               // 1 parallel replay, 2 serial (cascade), 0 serial (other)
+  uint32_t pad2;
 };
 
 __device__ __forceinline__ void stc_set_error(DevState *st, uint32_t code, uint32_t info) {

@@ -227,7 +227,7 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
             dalloc(c, &p.sw.bsub_leaves, p.S) && dalloc(c, &p.sw.bpre, p.S) && dalloc(c, &p.sw.bleafbase, p.S) &&
             dalloc(c, &p.sw.node_of, n) && dalloc(c, &p.sw.ev_flag, p.S) && dalloc(c, &p.sw.ev_pos, p.S) &&
             dalloc(c, &p.sw.ev_list, p.S) && dalloc(c, &p.sw.old_under, p.S) && dalloc(c, &p.sw.heap, p.S) &&
-            dalloc(c, &p.sw.ev_total, 2) && dalloc(c, &p.sw.queued, p.S) && dalloc(c, &p.leaf_gid, n) &&
+            dalloc(c, &p.sw.ev_total, 2) && dalloc(c, &p.sw.par_scratch, 10 * 8192) && dalloc(c, &p.sw.queued, p.S) && dalloc(c, &p.leaf_gid, n) &&
             dalloc(c, &p.lastvalid, n) && dalloc(c, &p.iota, nu) && dalloc(c, &p.sorted_gid, n) &&
             dalloc(c, &p.sorted_pid, n) && dalloc(c, &p.sort_ktmp, nu) && dalloc(c, &p.sort_vtmp, nu) &&
             dalloc(c, &p.sort_hist, radix_hist_words(nu)) && dalloc(c, &p.grid_count, (size_t)p.G + 1) &&
@@ -337,6 +337,7 @@ static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copie
   o.phase_ms[7] = 0.f;
   o.ambiguous_tests = (uint32_t)h.ambiguous;
   o.kernel_launches = (uint32_t)(tl_launches - launches0);
+  o.schema_path = h.schema_path;
   float tot = 0;
   cudaEventElapsedTime(&tot, c->ev[PH_START], c->ev[PH_SCHEMA]);
   o.step_ms = tot;

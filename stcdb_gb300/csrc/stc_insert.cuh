@@ -30,11 +30,14 @@
 
 namespace stc {
 
+// (key, claim) pair of a slot in one 16-byte load at L2 (claims change during
+// the walk phase; a torn or stale value only makes a CAS fail and retry).
 __device__ __forceinline__ U128 load_slot_pair(const Slot *s) {
-  U128 v;
-  v.lo = *(volatile const unsigned long long *)&s->key;
-  v.hi = *(volatile const unsigned long long *)&s->start;
-  return v;
+  ulonglong2 v = __ldcg((const ulonglong2 *)s);
+  U128 r;
+  r.lo = v.x;
+  r.hi = v.y;
+  return r;
 }
 
 // Extends an existing meeting found by an ordered walk: end = t and the MBR
@@ -52,14 +55,16 @@ __device__ __forceinline__ void extend_found(const PipeDev &p, Slot *s, unsigned
 }
 
 // Ordered walk of `key` with priority `prio` starting at `slot` (every slot
-// before it in the key's chain holds another S0 key). Returns false if the
-// walk exceeded its bound.
+// before it in the key's chain holds another S0 key). `first`, when given,
+// is a recent read of that slot's (key, claim) pair and saves one round trip
+// (a stale value only makes the first CAS fail and retry). Returns false if
+// the walk exceeded its bound.
 __device__ inline bool ordered_walk(const PipeDev &p, unsigned long long key, unsigned long long prio,
-                             unsigned long long slot, uint32_t t) {
+                                    unsigned long long slot, uint32_t t, const U128 *first = nullptr) {
   const unsigned long long limit = STC_PROBE_LIMIT * 4;
   for (unsigned long long steps = 0; steps < limit; steps++) {
     Slot *s = &p.slots[slot];
-    U128 cur = load_slot_pair(s);
+    U128 cur = (steps == 0 && first) ? *first : load_slot_pair(s);
     if (cur.lo == key) {  // its own live entry
       extend_found(p, s, key, t);
       return true;

@@ -115,7 +115,16 @@ __global__ void __launch_bounds__(256) k_sweep(PipeDev p, uint32_t t) {
     bool emit = false;
     Slot s;
     if (i < B) {
-      s = p.slots[i];
+      // the table streams through once: evict-first loads and stores leave
+      // L2 to the per-object positions read for new meetings
+      {
+        ulonglong2 a = __ldcs((const ulonglong2 *)&p.slots[i]);
+        float4 b = __ldcs((const float4 *)&p.slots[i].lo_x);
+        s.key = a.x;
+        s.start = (uint32_t)a.y;
+        s.end = (uint32_t)(a.y >> 32);
+        s.lo_x = b.x; s.lo_y = b.y; s.hi_x = b.z; s.hi_y = b.w;
+      }
       if (s.key != STC_EMPTY_KEY) {
         if (s.key & STC_CLAIM_BIT) {
           // new meeting of this step (cuda/geometry.cu:480-489): start = end = t,

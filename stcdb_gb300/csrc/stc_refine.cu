@@ -89,30 +89,38 @@ __device__ void cand_insert(const PipeDev &p, unsigned long long key, unsigned l
 static constexpr int QCAP = 64;  // per-warp queue; flushed 32 at a time
 #define DUP_BIT (1ULL << 63)
 
-__device__ void process_hit(const PipeDev &p, const HitRec &h, uint32_t t) {
-  unsigned long long slot = h.key % p.B;
+// Applies one hit to the table. kv/mbr: the slot at key % B, already loaded.
+__device__ void process_hit_at(const PipeDev &p, const HitRec &h, uint32_t t, unsigned long long slot, U128 kv,
+                               float4 mbr) {
   for (unsigned long long probe = 0; probe < STC_PROBE_LIMIT && probe < p.B; probe++) {
     Slot *s = &p.slots[slot];
-    unsigned long long k = *(volatile unsigned long long *)&s->key;
-    if (k == h.key) {  // tracing/refinement.cpp:40-42 (+ MBR, cuda/geometry.cu:474-478)
+    if (kv.lo == h.key) {  // tracing/refinement.cpp:40-42 (+ MBR, cuda/geometry.cu:474-478)
       s->end = t;
-      if (h.lo_x < s->lo_x) atomic_min_f(&s->lo_x, h.lo_x);
-      if (h.lo_y < s->lo_y) atomic_min_f(&s->lo_y, h.lo_y);
-      if (h.hi_x > s->hi_x) atomic_max_f(&s->hi_x, h.hi_x);
-      if (h.hi_y > s->hi_y) atomic_max_f(&s->hi_y, h.hi_y);
+      // the MBR only grows during a step, so a stale read can only cause an extra atomic
+      if (h.lo_x < mbr.x) atomic_min_f(&s->lo_x, h.lo_x);
+      if (h.lo_y < mbr.y) atomic_min_f(&s->lo_y, h.lo_y);
+      if (h.hi_x > mbr.z) atomic_max_f(&s->hi_x, h.hi_x);
+      if (h.hi_y > mbr.w) atomic_max_f(&s->hi_y, h.hi_y);
       return;
     }
-    if (k == STC_EMPTY_KEY || (k & STC_CLAIM_BIT)) {  // empty before this step: a new key
+    if (kv.lo == STC_EMPTY_KEY || (kv.lo & STC_CLAIM_BIT)) {  // empty before this step: a new key
       if (h.order & DUP_BIT) {
         cand_insert(p, h.key, h.order & ~DUP_BIT);
       } else {
-        if (!ordered_walk(p, h.key, h.order, slot, t)) stc_set_error(p.st, ERR_DA, (uint32_t)(h.key % p.B));
+        if (!ordered_walk(p, h.key, h.order, slot, t, &kv)) stc_set_error(p.st, ERR_DA, (uint32_t)(h.key % p.B));
       }
       return;
     }
     slot = slot + 1 == p.B ? 0 : slot + 1;
+    kv = load_slot_pair(&p.slots[slot]);
+    mbr = __ldcg((const float4 *)&p.slots[slot].lo_x);
   }
   stc_set_error(p.st, ERR_PROBE, (uint32_t)(h.key % p.B));
+}
+
+__device__ __forceinline__ void process_hit(const PipeDev &p, const HitRec &h, uint32_t t) {
+  unsigned long long slot = h.key % p.B;
+  process_hit_at(p, h, t, slot, load_slot_pair(&p.slots[slot]), __ldcg((const float4 *)&p.slots[slot].lo_x));
 }
 
 // Per-warp window of the step's hit buffer, reserved HIT_CHUNK entries at a
@@ -148,12 +156,37 @@ __device__ __forceinline__ void flush_queue(const PipeDev &p, HitRec *q, uint32_
   __syncwarp();
 }
 
+__device__ __forceinline__ HitRec load_hit(const HitRec *r) {
+  // streamed once: evict-first loads keep L2 for the table and positions
+  ulonglong2 a = __ldcs((const ulonglong2 *)r);
+  float4 b = __ldcs((const float4 *)&r->lo_x);
+  HitRec h;
+  h.key = a.x; h.order = a.y; h.lo_x = b.x; h.lo_y = b.y; h.hi_x = b.z; h.hi_y = b.w;
+  return h;
+}
+
+// One thread per hit, two hits in flight per thread: both records and both
+// home slots are requested before either is used.
 __global__ void __launch_bounds__(256) k_hits(PipeDev p, uint32_t t) {
   const unsigned long long nh = p.st->hit_count < p.hit_cap ? p.st->hit_count : p.hit_cap;
-  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < nh;
-       i += (unsigned long long)gridDim.x * blockDim.x) {
-    HitRec h = p.hits[i];
-    if (h.key != STC_EMPTY_KEY) process_hit(p, h, t);
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < nh; i += 2 * stride) {
+    unsigned long long i2 = i + stride;
+    HitRec h0 = load_hit(&p.hits[i]);
+    HitRec h1;
+    h1.key = STC_EMPTY_KEY;
+    if (i2 < nh) h1 = load_hit(&p.hits[i2]);
+    unsigned long long s0 = h0.key % p.B, s1 = h1.key % p.B;
+    U128 kv0 = load_slot_pair(&p.slots[s0]);
+    float4 m0 = __ldcg((const float4 *)&p.slots[s0].lo_x);
+    U128 kv1 = {0, 0};
+    float4 m1 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (h1.key != STC_EMPTY_KEY) {
+      kv1 = load_slot_pair(&p.slots[s1]);
+      m1 = __ldcg((const float4 *)&p.slots[s1].lo_x);
+    }
+    if (h0.key != STC_EMPTY_KEY) process_hit_at(p, h0, t, s0, kv0, m0);
+    if (h1.key != STC_EMPTY_KEY) process_hit_at(p, h1, t, s1, kv1, m1);
   }
 }
 

@@ -383,15 +383,29 @@ __device__ uint32_t heap_pop(uint32_t *h, uint32_t &n) {
 // node or grid id freed by a merge can only be reused by a later split. The
 // per-step grid counts are not reset: nothing reads them before the next
 // step recounts. Sets *done; k_schema_phase2 then does nothing.
-static constexpr int PAR_MAX_EVENTS = 1024;  // keeps the block's static shared memory under 48 KB
+static constexpr uint32_t PAR_MAX_EVENTS = 8192;  // bounds the O(E^2) last-push searches
+
+// Per-event scratch of the parallel replay (global memory, 10 words per event).
+struct ParScratch {
+  uint32_t *node;
+  int32_t *s0, *g0;
+  uint32_t *kind, *spush, *gpush;  // spush/gpush: 4 per event
+};
+
+__device__ __forceinline__ ParScratch par_scratch(uint32_t *base, uint32_t cap) {
+  ParScratch ps;
+  ps.node = base;
+  ps.s0 = (int32_t *)(base + cap);
+  ps.g0 = (int32_t *)(base + 2 * (size_t)cap);
+  ps.kind = base + 3 * (size_t)cap;
+  ps.spush = base + 4 * (size_t)cap;
+  ps.gpush = base + 8 * (size_t)cap;
+  return ps;
+}
 
 __global__ void __launch_bounds__(1024) k_schema_phase2_par(SchemaDev sd, const uint32_t *ev_list,
-                                                            const unsigned long long *ev_total,
-                                                            unsigned int *done, int serial_only, DevState *st) {
-  __shared__ uint32_t ev_node[PAR_MAX_EVENTS];
-  __shared__ uint8_t ev_kind[PAR_MAX_EVENTS];
-  __shared__ int32_t s0[PAR_MAX_EVENTS], g0[PAR_MAX_EVENTS];
-  __shared__ uint32_t spush[PAR_MAX_EVENTS][4], gpush[PAR_MAX_EVENTS][4];
+                                                            const unsigned long long *ev_total, unsigned int *done,
+                                                            int serial_only, uint32_t *scratch, DevState *st) {
   __shared__ int cascade;
   __shared__ uint32_t warp_s[32], warp_g[32];
   const uint32_t tid = threadIdx.x;
@@ -399,30 +413,34 @@ __global__ void __launch_bounds__(1024) k_schema_phase2_par(SchemaDev sd, const 
   if (tid == 0) {
     *done = 0;
     cascade = 0;
+    st->schema_path = 0;
   }
   if (nev > PAR_MAX_EVENTS || serial_only) return;
+  ParScratch ps = par_scratch(scratch, PAR_MAX_EVENTS);
   __syncthreads();
   for (uint32_t e = tid; e < nev; e += blockDim.x) {
     uint32_t v = ev_list[e];
     uint32_t node = v >> 2, kind = v & 3u;
-    ev_node[e] = node;
-    ev_kind[e] = (uint8_t)kind;
+    ps.node[e] = node;
+    ps.kind[e] = kind;
     if (kind == EV_MERGE) {
       uint32_t par = sd.meta[node].parent;
       if (node != 0 && par != STC_NONE && par > node) cascade = 1;
     }
   }
   __syncthreads();
-  if (cascade) return;
+  if (cascade) {
+    if (tid == 0) st->schema_path = 2;
+    return;
+  }
   // exclusive scan of the stack deltas (each thread owns a contiguous chunk)
   uint32_t per = (nev + blockDim.x - 1) / blockDim.x;
   uint32_t e0 = tid * per, e1 = min(nev, e0 + per);
   int ds = 0, dg = 0;
   for (uint32_t e = e0; e < e1; e++) {
-    ds += ev_kind[e] == EV_SPLIT ? 4 : -4;
-    dg += ev_kind[e] == EV_SPLIT ? 3 : -3;
+    ds += ps.kind[e] == EV_SPLIT ? 4 : -4;
+    dg += ps.kind[e] == EV_SPLIT ? 3 : -3;
   }
-  // block scan of (ds, dg)
   uint32_t lane = tid & 31u, warp = tid >> 5;
   int is = ds, ig = dg;
   for (int o = 1; o < 32; o <<= 1) {
@@ -445,29 +463,30 @@ __global__ void __launch_bounds__(1024) k_schema_phase2_par(SchemaDev sd, const 
   int bs = (int)st->schema_stack_index + (int)warp_s[warp] + is - ds;
   int bg = (int)st->grids_stack_index + (int)warp_g[warp] + ig - dg;
   for (uint32_t e = e0; e < e1; e++) {
-    s0[e] = bs;
-    g0[e] = bg;
-    bs += ev_kind[e] == EV_SPLIT ? 4 : -4;
-    bg += ev_kind[e] == EV_SPLIT ? 3 : -3;
+    ps.s0[e] = bs;
+    ps.g0[e] = bg;
+    bs += ps.kind[e] == EV_SPLIT ? 4 : -4;
+    bg += ps.kind[e] == EV_SPLIT ? 3 : -3;
   }
   __syncthreads();
   // merges (tracing/filter.cpp:316-336); record every push
   for (uint32_t e = tid; e < nev; e += blockDim.x) {
-    uint32_t cur = ev_node[e];
-    if (ev_kind[e] == EV_SPLIT) {
-      gpush[e][0] = sd.meta[cur].grid_id;
-      if (s0[e] + 4 > (int)sd.S || g0[e] < 1 || g0[e] + 3 > (int)sd.G) stc_set_error(st, ERR_SCHEMA, cur);
+    uint32_t cur = ps.node[e];
+    int s0 = ps.s0[e], g0 = ps.g0[e];
+    if (ps.kind[e] == EV_SPLIT) {
+      ps.gpush[4 * e] = sd.meta[cur].grid_id;
+      if (s0 + 4 > (int)sd.S || g0 < 1 || g0 + 3 > (int)sd.G) stc_set_error(st, ERR_SCHEMA, cur);
       continue;
     }
-    if (s0[e] < 4 || g0[e] < 4) stc_set_error(st, ERR_SCHEMA, cur);
+    if (s0 < 4 || g0 < 4) stc_set_error(st, ERR_SCHEMA, cur);
     Node q = sd.nodes[cur];
     uint32_t last_gid = 0;
     for (int i = 0; i < 4; i++) {
       uint32_t ch = q.child[i];
       uint32_t gid = sd.meta[ch].grid_id;
       sd.meta[ch].type = NODE_INVALID;
-      spush[e][i] = ch;   // schema_stack[s0 - 1 - i]
-      gpush[e][i] = gid;  // grids_stack[g0 - 1 - i]
+      ps.spush[4 * e + i] = ch;   // schema_stack[s0 - 1 - i]
+      ps.gpush[4 * e + i] = gid;  // grids_stack[g0 - 1 - i]
       last_gid = gid;
     }
     NodeMeta cm = sd.meta[cur];
@@ -481,23 +500,33 @@ __global__ void __launch_bounds__(1024) k_schema_phase2_par(SchemaDev sd, const 
   if (!st->error) {
     // splits (tracing/filter.cpp:338-375)
     for (uint32_t e = tid; e < nev; e += blockDim.x) {
-      if (ev_kind[e] != EV_SPLIT) continue;
-      uint32_t cur = ev_node[e];
+      if (ps.kind[e] != EV_SPLIT) continue;
+      uint32_t cur = ps.node[e];
+      int s0 = ps.s0[e], g0 = ps.g0[e];
       uint32_t child[4], gid[4];
       for (int i = 0; i < 4; i++) {
-        // node slot popped at schema position s0 + i
-        int qs = s0[e] + i;
+        // node slot popped at schema position s0 + i: the latest earlier push there, else the old content
+        int qs = s0 + i;
         uint32_t v = sd.schema_stack[qs];
         for (int f = (int)e - 1; f >= 0; f--)
-          if (ev_kind[f] == EV_MERGE && qs >= s0[f] - 4 && qs <= s0[f] - 1) { v = spush[f][s0[f] - 1 - qs]; break; }
+          if (ps.kind[f] == EV_MERGE && qs >= ps.s0[f] - 4 && qs <= ps.s0[f] - 1) {
+            v = ps.spush[4 * f + (ps.s0[f] - 1 - qs)];
+            break;
+          }
         child[i] = v;
         // grid id popped at grid position g0 - 1 + i (the first is this split's own push)
-        int qg = g0[e] - 1 + i;
-        uint32_t w = i == 0 ? gpush[e][0] : sd.grids_stack[qg];
+        int qg = g0 - 1 + i;
+        uint32_t w = i == 0 ? ps.gpush[4 * e] : sd.grids_stack[qg];
         if (i > 0) {
           for (int f = (int)e - 1; f >= 0; f--) {
-            if (ev_kind[f] == EV_MERGE && qg >= g0[f] - 4 && qg <= g0[f] - 1) { w = gpush[f][g0[f] - 1 - qg]; break; }
-            if (ev_kind[f] == EV_SPLIT && qg == g0[f] - 1) { w = gpush[f][0]; break; }
+            if (ps.kind[f] == EV_MERGE && qg >= ps.g0[f] - 4 && qg <= ps.g0[f] - 1) {
+              w = ps.gpush[4 * f + (ps.g0[f] - 1 - qg)];
+              break;
+            }
+            if (ps.kind[f] == EV_SPLIT && qg == ps.g0[f] - 1) {
+              w = ps.gpush[4 * f];
+              break;
+            }
           }
         }
         gid[i] = w;
@@ -533,47 +562,49 @@ __global__ void __launch_bounds__(1024) k_schema_phase2_par(SchemaDev sd, const 
     __syncthreads();
     // final stack contents: the last push to each position wins
     for (uint32_t e = tid; e < nev; e += blockDim.x) {
-      if (ev_kind[e] == EV_MERGE) {
+      int s0 = ps.s0[e], g0 = ps.g0[e];
+      if (ps.kind[e] == EV_MERGE) {
         for (int i = 0; i < 4; i++) {
-          int qs = s0[e] - 1 - i, qg = g0[e] - 1 - i;
+          int qs = s0 - 1 - i, qg = g0 - 1 - i;
           bool last_s = true, last_g = true;
           for (uint32_t f = e + 1; f < nev; f++) {
-            if (ev_kind[f] == EV_MERGE) {
-              if (qs >= s0[f] - 4 && qs <= s0[f] - 1) last_s = false;
-              if (qg >= g0[f] - 4 && qg <= g0[f] - 1) last_g = false;
-            } else if (qg == g0[f] - 1) {
+            if (ps.kind[f] == EV_MERGE) {
+              if (qs >= ps.s0[f] - 4 && qs <= ps.s0[f] - 1) last_s = false;
+              if (qg >= ps.g0[f] - 4 && qg <= ps.g0[f] - 1) last_g = false;
+            } else if (qg == ps.g0[f] - 1) {
               last_g = false;
             }
           }
-          if (last_s) sd.schema_stack[qs] = spush[e][i];
-          if (last_g) sd.grids_stack[qg] = gpush[e][i];
+          if (last_s) sd.schema_stack[qs] = ps.spush[4 * e + i];
+          if (last_g) sd.grids_stack[qg] = ps.gpush[4 * e + i];
         }
       } else {
-        int qg = g0[e] - 1;
+        int qg = g0 - 1;
         bool last_g = true;
         for (uint32_t f = e + 1; f < nev; f++) {
-          if (ev_kind[f] == EV_MERGE) {
-            if (qg >= g0[f] - 4 && qg <= g0[f] - 1) last_g = false;
-          } else if (qg == g0[f] - 1) {
+          if (ps.kind[f] == EV_MERGE) {
+            if (qg >= ps.g0[f] - 4 && qg <= ps.g0[f] - 1) last_g = false;
+          } else if (qg == ps.g0[f] - 1) {
             last_g = false;
           }
         }
-        if (last_g) sd.grids_stack[qg] = gpush[e][0];
+        if (last_g) sd.grids_stack[qg] = ps.gpush[4 * e];
       }
     }
   }
   __syncthreads();
   if (tid == 0) {
     uint32_t splits = 0, merges = 0;
-    for (uint32_t e = 0; e < nev; e++) (ev_kind[e] == EV_SPLIT ? splits : merges)++;
+    for (uint32_t e = 0; e < nev; e++) (ps.kind[e] == EV_SPLIT ? splits : merges)++;
     if (nev) {
       uint32_t l = nev - 1;
-      st->schema_stack_index = (uint32_t)(s0[l] + (ev_kind[l] == EV_SPLIT ? 4 : -4));
-      st->grids_stack_index = (uint32_t)(g0[l] + (ev_kind[l] == EV_SPLIT ? 3 : -3));
+      st->schema_stack_index = (uint32_t)(ps.s0[l] + (ps.kind[l] == EV_SPLIT ? 4 : -4));
+      st->grids_stack_index = (uint32_t)(ps.g0[l] + (ps.kind[l] == EV_SPLIT ? 3 : -3));
     }
     st->splits = splits;
     st->merges = merges;
     st->events = nev;
+    st->schema_path = 1;
     *done = 1;
   }
 }
@@ -646,7 +677,7 @@ void update_schema(SchemaDev sd, SchemaWork w, uint32_t *grid_count, double reac
   exclusive_scan_u32(w.ev_pos, w.ev_pos, sd.S, w.ev_total, w.scan_tmp, s);
   STC_KL k_schema_compact<<<nblk(sd.S), 256, 0, s>>>(w.ev_flag, w.ev_pos, sd.S, w.ev_list);
   unsigned int *done = (unsigned int *)(w.ev_total + 1);
-  STC_KL k_schema_phase2_par<<<1, 1024, 0, s>>>(sd, w.ev_list, w.ev_total, done, serial_only, st);
+  STC_KL k_schema_phase2_par<<<1, 1024, 0, s>>>(sd, w.ev_list, w.ev_total, done, serial_only, w.par_scratch, st);
   STC_KL k_schema_phase2<<<1, 32, 0, s>>>(sd, grid_count, w.ev_list, w.ev_total, w.old_under, w.heap, w.queued,
                                    grid_capacity, delay, done, st);
 }

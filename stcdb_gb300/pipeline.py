@@ -68,6 +68,7 @@ class StcStats(ctypes.Structure):
         ("splits", ctypes.c_uint32),
         ("merges", ctypes.c_uint32),
         ("kernel_launches", ctypes.c_uint32),
+        ("schema_path", ctypes.c_uint32),
         ("ambiguous_tests", ctypes.c_uint32),
         ("step_ms", ctypes.c_float),
         ("phase_ms", ctypes.c_float * 8),

@@ -87,4 +87,5 @@ def test_partial_drain(built_cuda):
                 break
         got = np.concatenate(parts)
         assert len(whole) > 37
-        assert np.array_equal(whole, got)
+        from stcdb_gb300.pipeline import sort_meetings
+        assert np.array_equal(sort_meetings(whole), sort_meetings(got))
