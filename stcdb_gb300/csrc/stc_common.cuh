@@ -142,7 +142,9 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
 // double sqrt, which is exact only while 8z+1 < 2^53).
 __device__ __forceinline__ void cantor_decode(unsigned long long z, uint32_t *a, uint32_t *b) {
   unsigned long long v = 8ULL * z + 1ULL;
-  unsigned long long r = (unsigned long long)sqrt((double)v);
+  // fp32 square root as the first guess (off by at most a few units for
+  // v < 2^60), then exact integer correction
+  unsigned long long r = (unsigned long long)sqrtf((float)v);
   while (r * r > v) r--;
   while ((r + 1) * (r + 1) <= v) r++;
   unsigned long long w = (r - 1) / 2;

@@ -383,7 +383,7 @@ __device__ uint32_t heap_pop(uint32_t *h, uint32_t &n) {
 // node or grid id freed by a merge can only be reused by a later split. The
 // per-step grid counts are not reset: nothing reads them before the next
 // step recounts. Sets *done; k_schema_phase2 then does nothing.
-static constexpr uint32_t PAR_MAX_EVENTS = 8192;  // bounds the O(E^2) last-push searches
+static constexpr uint32_t PAR_MAX_EVENTS = 4096;  // event table in shared memory (36 KB)
 
 // Per-event scratch of the parallel replay (global memory, 10 words per event).
 struct ParScratch {
@@ -408,6 +408,9 @@ __global__ void __launch_bounds__(1024) k_schema_phase2_par(SchemaDev sd, const 
                                                             int serial_only, uint32_t *scratch, DevState *st) {
   __shared__ int cascade;
   __shared__ uint32_t warp_s[32], warp_g[32];
+  // stack positions and kinds of all events, scanned by the last-push searches
+  __shared__ int32_t sh_s0[PAR_MAX_EVENTS], sh_g0[PAR_MAX_EVENTS];
+  __shared__ uint8_t sh_kind[PAR_MAX_EVENTS];
   const uint32_t tid = threadIdx.x;
   uint32_t nev = (uint32_t)*ev_total;
   if (tid == 0) {
@@ -423,6 +426,7 @@ __global__ void __launch_bounds__(1024) k_schema_phase2_par(SchemaDev sd, const 
     uint32_t node = v >> 2, kind = v & 3u;
     ps.node[e] = node;
     ps.kind[e] = kind;
+    sh_kind[e] = (uint8_t)kind;
     if (kind == EV_MERGE) {
       uint32_t par = sd.meta[node].parent;
       if (node != 0 && par != STC_NONE && par > node) cascade = 1;
@@ -438,8 +442,8 @@ __global__ void __launch_bounds__(1024) k_schema_phase2_par(SchemaDev sd, const 
   uint32_t e0 = tid * per, e1 = min(nev, e0 + per);
   int ds = 0, dg = 0;
   for (uint32_t e = e0; e < e1; e++) {
-    ds += ps.kind[e] == EV_SPLIT ? 4 : -4;
-    dg += ps.kind[e] == EV_SPLIT ? 3 : -3;
+    ds += sh_kind[e] == EV_SPLIT ? 4 : -4;
+    dg += sh_kind[e] == EV_SPLIT ? 3 : -3;
   }
   uint32_t lane = tid & 31u, warp = tid >> 5;
   int is = ds, ig = dg;
@@ -465,8 +469,10 @@ __global__ void __launch_bounds__(1024) k_schema_phase2_par(SchemaDev sd, const 
   for (uint32_t e = e0; e < e1; e++) {
     ps.s0[e] = bs;
     ps.g0[e] = bg;
-    bs += ps.kind[e] == EV_SPLIT ? 4 : -4;
-    bg += ps.kind[e] == EV_SPLIT ? 3 : -3;
+    sh_s0[e] = bs;
+    sh_g0[e] = bg;
+    bs += sh_kind[e] == EV_SPLIT ? 4 : -4;
+    bg += sh_kind[e] == EV_SPLIT ? 3 : -3;
   }
   __syncthreads();
   // merges (tracing/filter.cpp:316-336); record every push
@@ -509,8 +515,8 @@ __global__ void __launch_bounds__(1024) k_schema_phase2_par(SchemaDev sd, const 
         int qs = s0 + i;
         uint32_t v = sd.schema_stack[qs];
         for (int f = (int)e - 1; f >= 0; f--)
-          if (ps.kind[f] == EV_MERGE && qs >= ps.s0[f] - 4 && qs <= ps.s0[f] - 1) {
-            v = ps.spush[4 * f + (ps.s0[f] - 1 - qs)];
+          if (sh_kind[f] == EV_MERGE && qs >= sh_s0[f] - 4 && qs <= sh_s0[f] - 1) {
+            v = ps.spush[4 * f + (sh_s0[f] - 1 - qs)];
             break;
           }
         child[i] = v;
@@ -519,11 +525,11 @@ __global__ void __launch_bounds__(1024) k_schema_phase2_par(SchemaDev sd, const 
         uint32_t w = i == 0 ? ps.gpush[4 * e] : sd.grids_stack[qg];
         if (i > 0) {
           for (int f = (int)e - 1; f >= 0; f--) {
-            if (ps.kind[f] == EV_MERGE && qg >= ps.g0[f] - 4 && qg <= ps.g0[f] - 1) {
-              w = ps.gpush[4 * f + (ps.g0[f] - 1 - qg)];
+            if (sh_kind[f] == EV_MERGE && qg >= sh_g0[f] - 4 && qg <= sh_g0[f] - 1) {
+              w = ps.gpush[4 * f + (sh_g0[f] - 1 - qg)];
               break;
             }
-            if (ps.kind[f] == EV_SPLIT && qg == ps.g0[f] - 1) {
+            if (sh_kind[f] == EV_SPLIT && qg == sh_g0[f] - 1) {
               w = ps.gpush[4 * f];
               break;
             }
@@ -568,10 +574,10 @@ __global__ void __launch_bounds__(1024) k_schema_phase2_par(SchemaDev sd, const 
           int qs = s0 - 1 - i, qg = g0 - 1 - i;
           bool last_s = true, last_g = true;
           for (uint32_t f = e + 1; f < nev; f++) {
-            if (ps.kind[f] == EV_MERGE) {
-              if (qs >= ps.s0[f] - 4 && qs <= ps.s0[f] - 1) last_s = false;
-              if (qg >= ps.g0[f] - 4 && qg <= ps.g0[f] - 1) last_g = false;
-            } else if (qg == ps.g0[f] - 1) {
+            if (sh_kind[f] == EV_MERGE) {
+              if (qs >= sh_s0[f] - 4 && qs <= sh_s0[f] - 1) last_s = false;
+              if (qg >= sh_g0[f] - 4 && qg <= sh_g0[f] - 1) last_g = false;
+            } else if (qg == sh_g0[f] - 1) {
               last_g = false;
             }
           }
@@ -582,9 +588,9 @@ __global__ void __launch_bounds__(1024) k_schema_phase2_par(SchemaDev sd, const 
         int qg = g0 - 1;
         bool last_g = true;
         for (uint32_t f = e + 1; f < nev; f++) {
-          if (ps.kind[f] == EV_MERGE) {
-            if (qg >= ps.g0[f] - 4 && qg <= ps.g0[f] - 1) last_g = false;
-          } else if (qg == ps.g0[f] - 1) {
+          if (sh_kind[f] == EV_MERGE) {
+            if (qg >= sh_g0[f] - 4 && qg <= sh_g0[f] - 1) last_g = false;
+          } else if (qg == sh_g0[f] - 1) {
             last_g = false;
           }
         }
