@@ -113,6 +113,16 @@ __device__ __forceinline__ void atomic_max_f(float *a, float v) {
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
+// x % d for a fixed divisor with m = ceil(2^64 / d) (computed on the host):
+// the multiply-high quotient is exact or one too large; 64-bit division
+// would run through the FP64 pipe.
+__device__ __forceinline__ unsigned long long fast_mod(unsigned long long x, unsigned long long d,
+                                                       unsigned long long m) {
+  unsigned long long q = __umul64hi(x, m);
+  unsigned long long r = x - q * d;
+  return (long long)r < 0 ? r + d : r;
+}
+
 __device__ __forceinline__ bool stc_failed(const DevState *st) {
   return *(volatile const uint32_t *)&st->error != 0u;
 }
@@ -139,12 +149,16 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
 }
 
 // Exact integer inverse of the Cantor pairing (util/util.h:72-78 uses a
-// double sqrt, which is exact only while 8z+1 < 2^53).
+// double sqrt, which is exact only while 8z+1 < 2^53). 64-bit integer <->
+// float conversions run on the FP64 pipe, so the first guess comes from the
+// top 32 bits in fp32 (relative error ~2^-22, i.e. a few units for
+// v < 2^62); exact integer steps correct it.
 __device__ __forceinline__ void cantor_decode(unsigned long long z, uint32_t *a, uint32_t *b) {
   unsigned long long v = 8ULL * z + 1ULL;
-  // fp32 square root as the first guess (off by at most a few units for
-  // v < 2^60), then exact integer correction
-  unsigned long long r = (unsigned long long)sqrtf((float)v);
+  int sh = 64 - __clzll(v);
+  sh = sh > 32 ? ((sh - 32 + 1) & ~1) : 0;  // even shift keeps sqrt(v >> sh) * 2^(sh/2)
+  float fv = __uint2float_rn((uint32_t)(v >> sh));
+  unsigned long long r = (unsigned long long)__float2uint_rn(sqrtf(fv)) << (sh / 2);
   while (r * r > v) r--;
   while ((r + 1) * (r + 1) <= v) r++;
   unsigned long long w = (r - 1) / 2;

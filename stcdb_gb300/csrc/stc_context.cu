@@ -166,7 +166,7 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
   const stc_config &k = *cfg;
   double amp_cap = k.grid_amplify * k.grid_capacity;
   if (n == 0 || n != k.num_objects || n >= (1u << 31) || k.grid_capacity == 0 || !(k.reach_distance > 0) ||
-      k.num_meeting_buckets == 0 || k.refine_size == 0 || k.schema_update_delay == 0 || !(amp_cap >= 1.0) ||
+      k.num_meeting_buckets < 2 || k.refine_size == 0 || k.schema_update_delay == 0 || !(amp_cap >= 1.0) ||
       amp_cap >= (double)STC_MAX_LEAF_CAP || !(mbr[2] > mbr[0]) || !(mbr[3] > mbr[1])) {
     g_create_error = "stc_create: invalid configuration";
     return STC_ERR_INVALID_ARG;
@@ -212,6 +212,14 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
   p.x_buffer = k.reach_distance * stc_dpml_ref(mbr[1]);  // tracing/filter.cpp:30
   p.y_buffer = k.reach_distance * stc_dpm_lat();          // tracing/filter.cpp:31
   p.map_lo_x = mbr[0]; p.map_lo_y = mbr[1]; p.map_hi_x = mbr[2]; p.map_hi_y = mbr[3];
+  {
+    // for a float f and double D: f >= D <=> f >= (smallest float >= D), and
+    // f <= D <=> f <= (largest float <= D)
+    auto up = [](double d) { float f = (float)d; return (double)f < d ? nextafterf(f, INFINITY) : f; };
+    auto down = [](double d) { float f = (float)d; return (double)f > d ? nextafterf(f, -INFINITY) : f; };
+    p.fmap_lo_x = up(mbr[0]); p.fmap_lo_y = up(mbr[1]); p.fmap_hi_x = down(mbr[2]); p.fmap_hi_y = down(mbr[3]);
+  }
+  p.B_magic = (unsigned long long)(((unsigned __int128)1 << 64) / p.B + (((unsigned __int128)1 << 64) % p.B != 0));
   p.min_meet_time = k.min_meet_time;
   p.grid_capacity = k.grid_capacity;
   p.delay = k.schema_update_delay;

@@ -94,7 +94,7 @@ __global__ void k_insert_ordered(PipeDev p, uint32_t t) {
     x.order = ~0ULL;
     x.lo_x = STC_INIT_LO; x.lo_y = STC_INIT_LO; x.hi_x = STC_INIT_HI; x.hi_y = STC_INIT_HI;
     *cp = x;
-    if (!ordered_walk(p, key, prio, key % p.B, t)) stc_set_error(p.st, ERR_DA, (uint32_t)c);
+    if (!ordered_walk(p, key, prio, fast_mod(key, p.B, p.B_magic), t)) stc_set_error(p.st, ERR_DA, (uint32_t)c);
   }
 }
 
@@ -147,9 +147,8 @@ __global__ void __launch_bounds__(256) k_sweep(PipeDev p, uint32_t t) {
           active++;
         } else {
           if (t - s.start >= p.min_meet_time + 1) {
-            emit = !p.mbr_filter ||
-                   ((double)s.lo_x >= p.map_lo_x && (double)s.hi_x <= p.map_hi_x &&
-                    (double)s.lo_y >= p.map_lo_y && (double)s.hi_y <= p.map_hi_y);
+            emit = !p.mbr_filter || (s.lo_x >= p.fmap_lo_x && s.hi_x <= p.fmap_hi_x &&
+                                     s.lo_y >= p.fmap_lo_y && s.hi_y <= p.fmap_hi_y);
           }
           Slot e;
           e.key = STC_EMPTY_KEY;

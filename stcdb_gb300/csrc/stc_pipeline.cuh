@@ -9,6 +9,7 @@ struct PipeDev {
   // sizes
   uint32_t N, leaf_cap, G, S;
   unsigned long long B;            // meeting table slots
+  unsigned long long B_magic;      // ceil(2^64 / B) for fast_mod
   unsigned long long C;            // candidate set slots (power of two)
   unsigned long long cand_cap;     // candidate list capacity
   unsigned long long E;            // emit buffer capacity
@@ -16,6 +17,7 @@ struct PipeDev {
   // parameters
   double reach, x_buffer, y_buffer;
   double map_lo_x, map_lo_y, map_hi_x, map_hi_y;
+  float fmap_lo_x, fmap_lo_y, fmap_hi_x, fmap_hi_y;  // float f: f >= map_lo <=> f >= fmap_lo, etc.
   uint32_t min_meet_time, grid_capacity, delay;
   int mbr_filter;
   // state

@@ -107,7 +107,7 @@ __device__ void process_hit_at(const PipeDev &p, const HitRec &h, uint32_t t, un
       if (h.order & DUP_BIT) {
         cand_insert(p, h.key, h.order & ~DUP_BIT);
       } else {
-        if (!ordered_walk(p, h.key, h.order, slot, t, &kv)) stc_set_error(p.st, ERR_DA, (uint32_t)(h.key % p.B));
+        if (!ordered_walk(p, h.key, h.order, slot, t, &kv)) stc_set_error(p.st, ERR_DA, (uint32_t)slot);
       }
       return;
     }
@@ -115,11 +115,11 @@ __device__ void process_hit_at(const PipeDev &p, const HitRec &h, uint32_t t, un
     kv = load_slot_pair(&p.slots[slot]);
     mbr = __ldcg((const float4 *)&p.slots[slot].lo_x);
   }
-  stc_set_error(p.st, ERR_PROBE, (uint32_t)(h.key % p.B));
+  stc_set_error(p.st, ERR_PROBE, (uint32_t)slot);
 }
 
 __device__ __forceinline__ void process_hit(const PipeDev &p, const HitRec &h, uint32_t t) {
-  unsigned long long slot = h.key % p.B;
+  unsigned long long slot = fast_mod(h.key, p.B, p.B_magic);
   process_hit_at(p, h, t, slot, load_slot_pair(&p.slots[slot]), __ldcg((const float4 *)&p.slots[slot].lo_x));
 }
 
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(256) k_hits(PipeDev p, uint32_t t) {
     HitRec h1;
     h1.key = STC_EMPTY_KEY;
     if (i2 < nh) h1 = load_hit(&p.hits[i2]);
-    unsigned long long s0 = h0.key % p.B, s1 = h1.key % p.B;
+    unsigned long long s0 = fast_mod(h0.key, p.B, p.B_magic), s1 = fast_mod(h1.key, p.B, p.B_magic);
     U128 kv0 = load_slot_pair(&p.slots[s0]);
     float4 m0 = __ldcg((const float4 *)&p.slots[s0].lo_x);
     U128 kv1 = {0, 0};
@@ -342,9 +342,9 @@ __global__ void __launch_bounds__(REFINE_THREADS, 3) k_refine_a(PipeDev p, uint3
       uint32_t R = (n + 31) / 32;
       uint32_t own = R * (R + 1) / 2;
       if (local < own) {
-        // row-major upper triangle: row rc has R - rc tiles
-        double b2 = 2.0 * R + 1.0;
-        uint32_t rc = (uint32_t)((b2 - sqrt(b2 * b2 - 8.0 * local)) * 0.5);
+        // row-major upper triangle: row rc has R - rc tiles (fp32 estimate, exact fix-up)
+        float b2 = 2.0f * (float)R + 1.0f;
+        uint32_t rc = (uint32_t)fmaxf((b2 - sqrtf(fmaxf(b2 * b2 - 8.0f * (float)local, 0.0f))) * 0.5f, 0.0f);
         if (rc > R - 1) rc = R - 1;
         while (rc > 0 && rc * R - rc * (rc - 1) / 2 > local) rc--;
         while ((rc + 1) * R - (rc + 1) * rc / 2 <= local) rc++;

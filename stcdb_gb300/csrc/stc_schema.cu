@@ -371,242 +371,177 @@ __device__ uint32_t heap_pop(uint32_t *h, uint32_t &n) {
 }
 
 
-// Parallel replay of the flagged events for the common case: at most
+// Block replay of the flagged events for the common case: at most
 // PAR_MAX_EVENTS events and no merge whose parent has a higher index (the
 // only source of a cascade). Without cascades every event's decision is fixed
 // by phase 1, and the sequential replay's only coupling is through the two
-// free stacks: a split pops 4 node slots and, after pushing its own grid id,
-// 4 grid ids (net +4 / +3); a merge pushes its 4 children and their grid ids
-// and pops the last one back (net -4 / -3). Prefix sums give every event its
-// stack positions; a pop reads the most recent earlier push to its position
-// (or the stack's old content); merges are applied before splits because a
-// node or grid id freed by a merge can only be reused by a later split. The
-// per-step grid counts are not reset: nothing reads them before the next
-// step recounts. Sets *done; k_schema_phase2 then does nothing.
-static constexpr uint32_t PAR_MAX_EVENTS = 4096;  // event table in shared memory (36 KB)
+// free stacks: a split pushes its own grid id, then pops 4 node slots and 4
+// grid ids; a merge pushes its 4 children and their grid ids and pops the last
+// one back. The events touch at most 4 stack positions each side of where the
+// step starts, so one thread replays just the stack operations, in event
+// order, on windows of both stacks held in shared memory; all node and grid
+// bookkeeping is then written in parallel, merges before splits (a node or
+// grid id freed by a merge can only be reused by a later split). The per-step
+// grid counts are not reset: nothing reads them before the next step
+// recounts. Sets *done; k_schema_phase2 then does nothing.
+static constexpr uint32_t PAR_MAX_EVENTS = 4096;
+static constexpr uint32_t PAR_WIN = 4 * PAR_MAX_EVENTS + 8;  // stack positions one step can touch
+static constexpr size_t PAR_SMEM = (size_t)PAR_MAX_EVENTS * 5 + (size_t)2 * PAR_WIN * 4;  // 148 KB
 
-// Per-event scratch of the parallel replay (global memory, 10 words per event).
+// Per-event scratch in global memory: popped / pushed values.
 struct ParScratch {
   uint32_t *node;
-  int32_t *s0, *g0;
-  uint32_t *kind, *spush, *gpush;  // spush/gpush: 4 per event
+  uint32_t *val;  // 8 per event: split -> 4 children, 4 grid ids; merge -> 4 children, 4 grid ids
 };
 
 __device__ __forceinline__ ParScratch par_scratch(uint32_t *base, uint32_t cap) {
   ParScratch ps;
   ps.node = base;
-  ps.s0 = (int32_t *)(base + cap);
-  ps.g0 = (int32_t *)(base + 2 * (size_t)cap);
-  ps.kind = base + 3 * (size_t)cap;
-  ps.spush = base + 4 * (size_t)cap;
-  ps.gpush = base + 8 * (size_t)cap;
+  ps.val = base + cap;
   return ps;
 }
 
 __global__ void __launch_bounds__(1024) k_schema_phase2_par(SchemaDev sd, const uint32_t *ev_list,
                                                             const unsigned long long *ev_total, unsigned int *done,
                                                             int serial_only, uint32_t *scratch, DevState *st) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint32_t *sh_node = (uint32_t *)smem;                              // PAR_MAX_EVENTS
+  uint32_t *swin = sh_node + PAR_MAX_EVENTS;                          // PAR_WIN: schema stack window
+  uint32_t *gwin = swin + PAR_WIN;                                    // PAR_WIN: grid stack window
+  uint8_t *sh_kind = (uint8_t *)(gwin + PAR_WIN);                    // PAR_MAX_EVENTS
   __shared__ int cascade;
-  __shared__ uint32_t warp_s[32], warp_g[32];
-  // stack positions and kinds of all events, scanned by the last-push searches
-  __shared__ int32_t sh_s0[PAR_MAX_EVENTS], sh_g0[PAR_MAX_EVENTS];
-  __shared__ uint8_t sh_kind[PAR_MAX_EVENTS];
+  __shared__ uint32_t n_merges;
   const uint32_t tid = threadIdx.x;
   uint32_t nev = (uint32_t)*ev_total;
   if (tid == 0) {
     *done = 0;
     cascade = 0;
+    n_merges = 0;
     st->schema_path = 0;
   }
   if (nev > PAR_MAX_EVENTS || serial_only) return;
   ParScratch ps = par_scratch(scratch, PAR_MAX_EVENTS);
+  const int ssi0 = (int)st->schema_stack_index, gsi0 = (int)st->grids_stack_index;
   __syncthreads();
   for (uint32_t e = tid; e < nev; e += blockDim.x) {
     uint32_t v = ev_list[e];
     uint32_t node = v >> 2, kind = v & 3u;
-    ps.node[e] = node;
-    ps.kind[e] = kind;
+    sh_node[e] = node;
     sh_kind[e] = (uint8_t)kind;
     if (kind == EV_MERGE) {
+      atomicAdd(&n_merges, 1u);
       uint32_t par = sd.meta[node].parent;
       if (node != 0 && par != STC_NONE && par > node) cascade = 1;
+      Node q = sd.nodes[node];
+      for (int i = 0; i < 4; i++) {
+        ps.val[8 * e + i] = q.child[i];
+        ps.val[8 * e + 4 + i] = sd.meta[q.child[i]].grid_id;
+      }
+    } else {
+      ps.val[8 * e + 4] = sd.meta[node].grid_id;  // the split pushes this first
     }
+  }
+  __syncthreads();
+  // merges move the stack indices down by 4 each, splits up by 4 (schema) and
+  // at most 4 (grid): the window [idx0 - 4 merges - 4, +PAR_WIN) holds every
+  // position the step touches
+  const int sbase = ssi0 - 4 * (int)n_merges - 4, gbase = gsi0 - 4 * (int)n_merges - 4;
+  for (uint32_t k = tid; k < PAR_WIN; k += blockDim.x) {
+    int qs = sbase + (int)k, qg = gbase + (int)k;
+    swin[k] = (qs >= 0 && qs < (int)sd.S) ? sd.schema_stack[qs] : STC_NONE;
+    gwin[k] = (qg >= 0 && qg < (int)sd.G) ? sd.grids_stack[qg] : STC_NONE;
   }
   __syncthreads();
   if (cascade) {
     if (tid == 0) st->schema_path = 2;
     return;
   }
-  // exclusive scan of the stack deltas (each thread owns a contiguous chunk)
-  uint32_t per = (nev + blockDim.x - 1) / blockDim.x;
-  uint32_t e0 = tid * per, e1 = min(nev, e0 + per);
-  int ds = 0, dg = 0;
-  for (uint32_t e = e0; e < e1; e++) {
-    ds += sh_kind[e] == EV_SPLIT ? 4 : -4;
-    dg += sh_kind[e] == EV_SPLIT ? 3 : -3;
-  }
-  uint32_t lane = tid & 31u, warp = tid >> 5;
-  int is = ds, ig = dg;
-  for (int o = 1; o < 32; o <<= 1) {
-    int a = __shfl_up_sync(0xffffffffu, is, o), b = __shfl_up_sync(0xffffffffu, ig, o);
-    if ((int)lane >= o) { is += a; ig += b; }
-  }
-  if (lane == 31) { warp_s[warp] = (uint32_t)is; warp_g[warp] = (uint32_t)ig; }
-  __syncthreads();
-  if (warp == 0) {
-    int a = (int)warp_s[lane], b = (int)warp_g[lane];
-    int ia = a, ib = b;
-    for (int o = 1; o < 32; o <<= 1) {
-      int x = __shfl_up_sync(0xffffffffu, ia, o), y = __shfl_up_sync(0xffffffffu, ib, o);
-      if ((int)lane >= o) { ia += x; ib += y; }
-    }
-    warp_s[lane] = (uint32_t)(ia - a);
-    warp_g[lane] = (uint32_t)(ib - b);
-  }
-  __syncthreads();
-  int bs = (int)st->schema_stack_index + (int)warp_s[warp] + is - ds;
-  int bg = (int)st->grids_stack_index + (int)warp_g[warp] + ig - dg;
-  for (uint32_t e = e0; e < e1; e++) {
-    ps.s0[e] = bs;
-    ps.g0[e] = bg;
-    sh_s0[e] = bs;
-    sh_g0[e] = bg;
-    bs += sh_kind[e] == EV_SPLIT ? 4 : -4;
-    bg += sh_kind[e] == EV_SPLIT ? 3 : -3;
-  }
-  __syncthreads();
-  // merges (tracing/filter.cpp:316-336); record every push
-  for (uint32_t e = tid; e < nev; e += blockDim.x) {
-    uint32_t cur = ps.node[e];
-    int s0 = ps.s0[e], g0 = ps.g0[e];
-    if (ps.kind[e] == EV_SPLIT) {
-      ps.gpush[4 * e] = sd.meta[cur].grid_id;
-      if (s0 + 4 > (int)sd.S || g0 < 1 || g0 + 3 > (int)sd.G) stc_set_error(st, ERR_SCHEMA, cur);
-      continue;
-    }
-    if (s0 < 4 || g0 < 4) stc_set_error(st, ERR_SCHEMA, cur);
-    Node q = sd.nodes[cur];
-    uint32_t last_gid = 0;
-    for (int i = 0; i < 4; i++) {
-      uint32_t ch = q.child[i];
-      uint32_t gid = sd.meta[ch].grid_id;
-      sd.meta[ch].type = NODE_INVALID;
-      ps.spush[4 * e + i] = ch;   // schema_stack[s0 - 1 - i]
-      ps.gpush[4 * e + i] = gid;  // grids_stack[g0 - 1 - i]
-      last_gid = gid;
-    }
-    NodeMeta cm = sd.meta[cur];
-    cm.type = NODE_LEAF;
-    cm.grid_id = last_gid;  // the pop returns the last pushed grid id
-    cm.underflow = 0;
-    sd.meta[cur] = cm;
-    sd.gid_node[last_gid] = cur;
-  }
-  __syncthreads();
-  if (!st->error) {
-    // splits (tracing/filter.cpp:338-375)
-    for (uint32_t e = tid; e < nev; e += blockDim.x) {
-      if (ps.kind[e] != EV_SPLIT) continue;
-      uint32_t cur = ps.node[e];
-      int s0 = ps.s0[e], g0 = ps.g0[e];
-      uint32_t child[4], gid[4];
-      for (int i = 0; i < 4; i++) {
-        // node slot popped at schema position s0 + i: the latest earlier push there, else the old content
-        int qs = s0 + i;
-        uint32_t v = sd.schema_stack[qs];
-        for (int f = (int)e - 1; f >= 0; f--)
-          if (sh_kind[f] == EV_MERGE && qs >= sh_s0[f] - 4 && qs <= sh_s0[f] - 1) {
-            v = ps.spush[4 * f + (sh_s0[f] - 1 - qs)];
-            break;
-          }
-        child[i] = v;
-        // grid id popped at grid position g0 - 1 + i (the first is this split's own push)
-        int qg = g0 - 1 + i;
-        uint32_t w = i == 0 ? ps.gpush[4 * e] : sd.grids_stack[qg];
-        if (i > 0) {
-          for (int f = (int)e - 1; f >= 0; f--) {
-            if (sh_kind[f] == EV_MERGE && qg >= sh_g0[f] - 4 && qg <= sh_g0[f] - 1) {
-              w = ps.gpush[4 * f + (sh_g0[f] - 1 - qg)];
-              break;
-            }
-            if (sh_kind[f] == EV_SPLIT && qg == sh_g0[f] - 1) {
-              w = ps.gpush[4 * f];
-              break;
-            }
-          }
-        }
-        gid[i] = w;
-      }
-      Node q = sd.nodes[cur];
-      NodeMeta cm = sd.meta[cur];
-      double xhalf = RN_SUB(q.mid_x, q.lo_x);
-      double yhalf = RN_SUB(q.mid_y, q.lo_y);
-      for (int i = 0; i < 4; i++) {
-        Node c;
-        c.lo_x = RN_ADD(q.lo_x, (i % 2 == 1) ? xhalf : 0.0);
-        c.lo_y = RN_ADD(q.lo_y, (i / 2 == 1) ? yhalf : 0.0);
-        c.hi_x = RN_ADD(q.mid_x, (i % 2 == 1) ? xhalf : 0.0);
-        c.hi_y = RN_ADD(q.mid_y, (i / 2 == 1) ? yhalf : 0.0);
-        c.mid_x = RN_DIV(RN_ADD(c.lo_x, c.hi_x), 2.0);
-        c.mid_y = RN_DIV(RN_ADD(c.lo_y, c.hi_y), 2.0);
-        c.child[0] = c.child[1] = c.child[2] = c.child[3] = STC_NONE;
-        sd.nodes[child[i]] = c;
-        sd.fbox[child[i]] = make_float4(__double2float_rn(RN_SUB(c.lo_x, sd.ox)), __double2float_rn(RN_SUB(c.lo_y, sd.oy)),
-                                        __double2float_rn(RN_SUB(c.hi_x, sd.ox)), __double2float_rn(RN_SUB(c.hi_y, sd.oy)));
-        NodeMeta m;
-        m.type = NODE_LEAF; m.level = (int16_t)(cm.level + 1); m.overflow = 0; m.underflow = 0;
-        m.grid_id = gid[i]; m.parent = cur;
-        sd.meta[child[i]] = m;
-        sd.gid_node[gid[i]] = child[i];
-        q.child[i] = child[i];
-      }
-      sd.nodes[cur] = q;
-      cm.type = NODE_BRANCH;
-      cm.overflow = 0;
-      sd.meta[cur] = cm;
-    }
-    __syncthreads();
-    // final stack contents: the last push to each position wins
-    for (uint32_t e = tid; e < nev; e += blockDim.x) {
-      int s0 = ps.s0[e], g0 = ps.g0[e];
-      if (ps.kind[e] == EV_MERGE) {
+  if (tid == 0) {
+    // the stack operations of tracing/filter.cpp:316-375, in event order
+    int si = ssi0 - sbase, gi = gsi0 - gbase;
+    bool bad = false;
+    for (uint32_t e = 0; e < nev && !bad; e++) {
+      uint32_t *v = ps.val + 8 * e;
+      if (sh_kind[e] == EV_SPLIT) {
+        if (si + 4 + sbase > (int)sd.S || gi - 1 + gbase < 0 || gi + 3 + gbase > (int)sd.G) { bad = true; break; }
+        gwin[--gi] = v[4];
         for (int i = 0; i < 4; i++) {
-          int qs = s0 - 1 - i, qg = g0 - 1 - i;
-          bool last_s = true, last_g = true;
-          for (uint32_t f = e + 1; f < nev; f++) {
-            if (sh_kind[f] == EV_MERGE) {
-              if (qs >= sh_s0[f] - 4 && qs <= sh_s0[f] - 1) last_s = false;
-              if (qg >= sh_g0[f] - 4 && qg <= sh_g0[f] - 1) last_g = false;
-            } else if (qg == sh_g0[f] - 1) {
-              last_g = false;
-            }
-          }
-          if (last_s) sd.schema_stack[qs] = ps.spush[4 * e + i];
-          if (last_g) sd.grids_stack[qg] = ps.gpush[4 * e + i];
+          v[i] = swin[si++];
+          v[4 + i] = gwin[gi++];
         }
       } else {
-        int qg = g0 - 1;
-        bool last_g = true;
-        for (uint32_t f = e + 1; f < nev; f++) {
-          if (sh_kind[f] == EV_MERGE) {
-            if (qg >= sh_g0[f] - 4 && qg <= sh_g0[f] - 1) last_g = false;
-          } else if (qg == sh_g0[f] - 1) {
-            last_g = false;
-          }
+        if (si - 4 + sbase < 0 || gi - 4 + gbase < 0) { bad = true; break; }
+        for (int i = 0; i < 4; i++) {
+          swin[--si] = v[i];
+          gwin[--gi] = v[4 + i];
         }
-        if (last_g) sd.grids_stack[qg] = ps.gpush[4 * e];
+        gi++;  // pops the last pushed grid id back for the merged node (v[7])
       }
     }
+    if (bad) stc_set_error(st, ERR_SCHEMA, 0u);
+    st->schema_stack_index = (uint32_t)(si + sbase);
+    st->grids_stack_index = (uint32_t)(gi + gbase);
+  }
+  __syncthreads();
+  if (st->error) return;
+  // stack windows back to global memory
+  for (uint32_t k = tid; k < PAR_WIN; k += blockDim.x) {
+    int qs = sbase + (int)k, qg = gbase + (int)k;
+    if (qs >= 0 && qs < (int)sd.S) sd.schema_stack[qs] = swin[k];
+    if (qg >= 0 && qg < (int)sd.G) sd.grids_stack[qg] = gwin[k];
+  }
+  // merges (tracing/filter.cpp:316-336)
+  for (uint32_t e = tid; e < nev; e += blockDim.x) {
+    if (sh_kind[e] != EV_MERGE) continue;
+    uint32_t cur = sh_node[e];
+    const uint32_t *v = ps.val + 8 * e;
+    for (int i = 0; i < 4; i++) sd.meta[v[i]].type = NODE_INVALID;
+    NodeMeta cm = sd.meta[cur];
+    cm.type = NODE_LEAF;
+    cm.grid_id = v[7];  // the pop returns the last pushed grid id
+    cm.underflow = 0;
+    sd.meta[cur] = cm;
+    sd.gid_node[v[7]] = cur;
+  }
+  __syncthreads();
+  // splits (tracing/filter.cpp:338-375)
+  for (uint32_t e = tid; e < nev; e += blockDim.x) {
+    if (sh_kind[e] != EV_SPLIT) continue;
+    uint32_t cur = sh_node[e];
+    const uint32_t *v = ps.val + 8 * e;
+    Node q = sd.nodes[cur];
+    NodeMeta cm = sd.meta[cur];
+    double xhalf = RN_SUB(q.mid_x, q.lo_x);
+    double yhalf = RN_SUB(q.mid_y, q.lo_y);
+    for (int i = 0; i < 4; i++) {
+      uint32_t child = v[i], gid = v[4 + i];
+      Node c;
+      c.lo_x = RN_ADD(q.lo_x, (i % 2 == 1) ? xhalf : 0.0);
+      c.lo_y = RN_ADD(q.lo_y, (i / 2 == 1) ? yhalf : 0.0);
+      c.hi_x = RN_ADD(q.mid_x, (i % 2 == 1) ? xhalf : 0.0);
+      c.hi_y = RN_ADD(q.mid_y, (i / 2 == 1) ? yhalf : 0.0);
+      c.mid_x = RN_DIV(RN_ADD(c.lo_x, c.hi_x), 2.0);
+      c.mid_y = RN_DIV(RN_ADD(c.lo_y, c.hi_y), 2.0);
+      c.child[0] = c.child[1] = c.child[2] = c.child[3] = STC_NONE;
+      sd.nodes[child] = c;
+      sd.fbox[child] = make_float4(__double2float_rn(RN_SUB(c.lo_x, sd.ox)), __double2float_rn(RN_SUB(c.lo_y, sd.oy)),
+                                   __double2float_rn(RN_SUB(c.hi_x, sd.ox)), __double2float_rn(RN_SUB(c.hi_y, sd.oy)));
+      NodeMeta m;
+      m.type = NODE_LEAF; m.level = (int16_t)(cm.level + 1); m.overflow = 0; m.underflow = 0;
+      m.grid_id = gid; m.parent = cur;
+      sd.meta[child] = m;
+      sd.gid_node[gid] = child;
+      q.child[i] = child;
+    }
+    sd.nodes[cur] = q;
+    cm.type = NODE_BRANCH;
+    cm.overflow = 0;
+    sd.meta[cur] = cm;
   }
   __syncthreads();
   if (tid == 0) {
     uint32_t splits = 0, merges = 0;
-    for (uint32_t e = 0; e < nev; e++) (ps.kind[e] == EV_SPLIT ? splits : merges)++;
-    if (nev) {
-      uint32_t l = nev - 1;
-      st->schema_stack_index = (uint32_t)(ps.s0[l] + (ps.kind[l] == EV_SPLIT ? 4 : -4));
-      st->grids_stack_index = (uint32_t)(ps.g0[l] + (ps.kind[l] == EV_SPLIT ? 3 : -3));
-    }
+    for (uint32_t e = 0; e < nev; e++) (sh_kind[e] == EV_SPLIT ? splits : merges)++;
     st->splits = splits;
     st->merges = merges;
     st->events = nev;
@@ -683,7 +618,9 @@ void update_schema(SchemaDev sd, SchemaWork w, uint32_t *grid_count, double reac
   exclusive_scan_u32(w.ev_pos, w.ev_pos, sd.S, w.ev_total, w.scan_tmp, s);
   STC_KL k_schema_compact<<<nblk(sd.S), 256, 0, s>>>(w.ev_flag, w.ev_pos, sd.S, w.ev_list);
   unsigned int *done = (unsigned int *)(w.ev_total + 1);
-  STC_KL k_schema_phase2_par<<<1, 1024, 0, s>>>(sd, w.ev_list, w.ev_total, done, serial_only, w.par_scratch, st);
+  cudaFuncSetAttribute(k_schema_phase2_par, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PAR_SMEM);
+  STC_KL k_schema_phase2_par<<<1, 1024, PAR_SMEM, s>>>(sd, w.ev_list, w.ev_total, done, serial_only, w.par_scratch,
+                                                      st);
   STC_KL k_schema_phase2<<<1, 32, 0, s>>>(sd, grid_count, w.ev_list, w.ev_total, w.old_under, w.heap, w.queued,
                                    grid_capacity, delay, done, st);
 }

@@ -31,7 +31,7 @@ struct SchemaWork {
   unsigned long long *ev_total;
   uint8_t *queued;        // S
   uint32_t *scan_tmp;
-  uint32_t *par_scratch;  // 10 * 8192 words for the parallel replay
+  uint32_t *par_scratch;  // 9 * 4096 words for the block replay
 };
 
 // Builds the schema from step-0 positions (index/QTree.h:157-311 semantics:
