@@ -158,7 +158,9 @@ __device__ __forceinline__ void cantor_decode(unsigned long long z, uint32_t *a,
   int sh = 64 - __clzll(v);
   sh = sh > 32 ? ((sh - 32 + 1) & ~1) : 0;  // even shift keeps sqrt(v >> sh) * 2^(sh/2)
   float fv = __uint2float_rn((uint32_t)(v >> sh));
-  unsigned long long r = (unsigned long long)__float2uint_rn(sqrtf(fv)) << (sh / 2);
+  // scale in fp32 before rounding to an integer (r < 2^30 for v < 2^60)
+  float rf = sqrtf(fv) * __int_as_float((127 + sh / 2) << 23);
+  unsigned long long r = __float2uint_rn(rf);
   while (r * r > v) r--;
   while ((r + 1) * (r + 1) <= v) r++;
   unsigned long long w = (r - 1) / 2;
