@@ -134,11 +134,22 @@ stc_status stc_drain_meetings(stc_ctx *ctx, stc_meeting *out, size_t cap, size_t
 
 stc_status stc_get_stats(stc_ctx *ctx, stc_stats *stats);
 
-/* Last error message of ctx (or of the last failed stc_create when ctx is
- * NULL). Never NULL. */
+/* Last error message of ctx (or, when ctx is NULL, of the last failed
+ * stc_create or context-free call on this thread). Never NULL. */
 const char *stc_last_error(const stc_ctx *ctx);
 
 void stc_destroy(stc_ctx *ctx);
+
+/* Stable LSD radix sort of n (key, value) uint32 pairs on the low key_bits
+ * bits of the key (1..32), on CUDA device `device`. All four pointers are
+ * device memory; outputs must not alias inputs. Scratch (2n words plus
+ * histograms) is allocated and freed inside the call; the call returns when
+ * the sort is done. This is the sort the pipeline uses to group objects by
+ * quadtree leaf in pid order; it replaces thrust::sort_by_key in the
+ * reference's flush (cuda/geometry.cu:1860-1907) for 32-bit keys. Errors:
+ * stc_last_error(NULL). */
+stc_status stc_sort_pairs_u32(const uint32_t *keys, const uint32_t *values, uint32_t *keys_out,
+                              uint32_t *values_out, size_t n, uint32_t key_bits, uint32_t device);
 
 #ifdef __cplusplus
 }

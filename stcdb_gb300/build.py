@@ -31,6 +31,7 @@ CU_SOURCES = [
     "stc_meetings.cu",
     "stc_schema.cu",
     "stc_sort.cu",
+    "stc_util.cu",
 ]
 
 

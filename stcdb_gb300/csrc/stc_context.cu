@@ -24,6 +24,10 @@ enum Phase { PH_START = 0, PH_COPY, PH_PART, PH_BORDER, PH_REFINE, PH_INSERT, PH
 
 }  // namespace
 
+namespace stc {
+void set_thread_error(const std::string &msg) { g_create_error = msg; }
+}  // namespace stc
+
 struct stc_ctx {
   stc_config cfg;
   int device = 0;
