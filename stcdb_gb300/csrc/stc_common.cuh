@@ -192,6 +192,8 @@ extern thread_local unsigned long long tl_launches;
 #define STC_KL ::stc::tl_launches++,
 
 // Primitives implemented in stc_sort.cu.
+#define STC_SCAN_TILE 2048  // items per scan block
+#define STC_RS_TILE 4096    // items per radix-sort block
 namespace stc {
 
 // Exclusive scan of n uint32 values (in place allowed). total (device ptr,

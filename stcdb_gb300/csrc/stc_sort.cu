@@ -11,6 +11,7 @@ thread_local unsigned long long tl_launches = 0;
 static constexpr int SCAN_THREADS = 256;
 static constexpr int SCAN_ITEMS = 8;
 static constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+static_assert(SCAN_TILE == STC_SCAN_TILE, "scan tile");
 
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
   uint32_t lane = threadIdx.x & 31u;
@@ -115,12 +116,13 @@ void exclusive_scan_u32(const uint32_t *in, uint32_t *out, size_t n, unsigned lo
 static constexpr int RS_THREADS = 256;
 static constexpr int RS_ITEMS = 16;
 static constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+static_assert(RS_TILE == STC_RS_TILE, "radix tile");
 static constexpr int RS_WARPS = RS_THREADS / 32;
 
 size_t radix_hist_words(size_t n_max) { return 256 * ((n_max + RS_TILE - 1) / RS_TILE) + 1; }
 
 __global__ void k_rs_hist(const uint32_t *keys, const unsigned long long *n_dev, size_t n_max, int shift,
-                          uint32_t *hist, uint32_t nb) {
+                          uint32_t dmask, uint32_t *hist, uint32_t nb) {
   __shared__ uint32_t h[256];
   h[threadIdx.x] = 0;
   __syncthreads();
@@ -130,7 +132,7 @@ __global__ void k_rs_hist(const uint32_t *keys, const unsigned long long *n_dev,
   if (base < n) {
     for (int i = 0; i < RS_ITEMS; i++) {
       size_t idx = base + (size_t)i * RS_THREADS + threadIdx.x;
-      if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+      if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & dmask], 1u);
     }
   }
   __syncthreads();
@@ -138,8 +140,8 @@ __global__ void k_rs_hist(const uint32_t *keys, const unsigned long long *n_dev,
 }
 
 __global__ void k_rs_scatter(const uint32_t *k_in, const uint32_t *v_in, uint32_t *k_out, uint32_t *v_out,
-                             const unsigned long long *n_dev, size_t n_max, int shift, const uint32_t *hist,
-                             uint32_t nb) {
+                             const unsigned long long *n_dev, size_t n_max, int shift, uint32_t dmask,
+                             const uint32_t *hist, uint32_t nb) {
   __shared__ uint32_t base_off[256];
   __shared__ uint32_t running[256];
   __shared__ uint32_t warp_cnt[RS_WARPS][256];
@@ -158,7 +160,7 @@ __global__ void k_rs_scatter(const uint32_t *k_in, const uint32_t *v_in, uint32_
     bool valid = idx < n;
     uint32_t key = valid ? k_in[idx] : 0u;
     uint32_t val = valid ? v_in[idx] : 0u;
-    uint32_t digit = valid ? ((key >> shift) & 255u) : (256u + lane);
+    uint32_t digit = valid ? ((key >> shift) & dmask) : (256u + lane);
     uint32_t peers = __match_any_sync(0xffffffffu, digit);
     uint32_t rank = __popc(peers & lt_mask);
     if (valid && rank == 0) warp_cnt[warp][digit] = __popc(peers);
@@ -196,9 +198,12 @@ void radix_sort_u32(const uint32_t *k_in, const uint32_t *v_in, uint32_t *k_out,
     bool to_out = ((passes - 1 - p) % 2) == 0;
     uint32_t *ko = to_out ? k_out : k_tmp;
     uint32_t *vo = to_out ? v_out : v_tmp;
-    STC_KL k_rs_hist<<<nb, RS_THREADS, 0, s>>>(ki, n_dev, n_max, 8 * p, hist, nb);
+    // the last digit covers only the key bits that remain
+    int left = bits - 8 * p;
+    uint32_t dmask = left >= 8 ? 255u : (1u << left) - 1u;
+    STC_KL k_rs_hist<<<nb, RS_THREADS, 0, s>>>(ki, n_dev, n_max, 8 * p, dmask, hist, nb);
     exclusive_scan_u32(hist, hist, (size_t)256 * nb, nullptr, scan_tmp, s);
-    STC_KL k_rs_scatter<<<nb, RS_THREADS, 0, s>>>(ki, vi, ko, vo, n_dev, n_max, 8 * p, hist, nb);
+    STC_KL k_rs_scatter<<<nb, RS_THREADS, 0, s>>>(ki, vi, ko, vo, n_dev, n_max, 8 * p, dmask, hist, nb);
     ki = ko;
     vi = vo;
   }
