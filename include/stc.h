@@ -151,6 +151,24 @@ void stc_destroy(stc_ctx *ctx);
 stc_status stc_sort_pairs_u32(const uint32_t *keys, const uint32_t *values, uint32_t *keys_out,
                               uint32_t *values_out, size_t n, uint32_t key_bits, uint32_t device);
 
+/* Same sort and arguments as stc_sort_pairs_u32, for callers that cannot
+ * have device memory allocated on their behalf: code that owns all device
+ * memory through its own allocator or a fixed budget, and code on a
+ * latency-critical path where cudaMalloc/cudaFree (which can take driver
+ * locks and synchronise the device) are not allowed. It allocates nothing:
+ * its scratch is a fixed array inside the library (about 8.7 MB, kept on
+ * every device that uses it until the process exits), so n is limited to
+ * STC_SORT_NOALLOC_MAX_PAIRS; larger n returns STC_ERR_CAPACITY.
+ * The first call on a device looks up the array's device address (a one-time
+ * set-up per device); make that first call before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU (from several
+ * host threads, or launched while another is still running) race and corrupt
+ * each other's results. The call returns when the sort is done.
+ * No counterpart in the reference. Errors: stc_last_error(NULL). */
+#define STC_SORT_NOALLOC_MAX_PAIRS (1u << 20)
+stc_status stc_sort_pairs_u32_noalloc(const uint32_t *keys, const uint32_t *values, uint32_t *keys_out,
+                                      uint32_t *values_out, size_t n, uint32_t key_bits, uint32_t device);
+
 #ifdef __cplusplus
 }
 #endif

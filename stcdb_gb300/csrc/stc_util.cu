@@ -1,4 +1,5 @@
 // Context-free C ABI utilities (include/stc.h).
+#include <mutex>
 #include <string>
 
 #include "stc_common.cuh"
@@ -51,6 +52,86 @@ extern "C" stc_status stc_sort_pairs_u32(const uint32_t *keys, const uint32_t *v
   cudaFree(n_dev);
   if (e != cudaSuccess) {
     set_thread_error(std::string("stc_sort_pairs_u32: ") + cudaGetErrorString(e));
+    return STC_ERR_CUDA;
+  }
+  return STC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// stc_sort_pairs_u32_noalloc: the same sort with its scratch in a fixed
+// device array that belongs to the library, for callers that must not have
+// device memory allocated on their behalf (see include/stc.h).
+
+namespace {
+
+constexpr size_t NA_MAX = STC_SORT_NOALLOC_MAX_PAIRS;
+constexpr size_t NA_HIST = 256 * ((NA_MAX + STC_RS_TILE - 1) / STC_RS_TILE) + 1;  // radix histograms
+constexpr size_t NA_SCAN = (NA_HIST + STC_SCAN_TILE - 1) / STC_SCAN_TILE + 1;       // scan block sums
+constexpr size_t NA_COUNT_AT = (2 * NA_MAX + NA_HIST + NA_SCAN + 1) & ~(size_t)1;  // 8-byte aligned word
+constexpr size_t NA_WORDS = NA_COUNT_AT + 2;
+
+// Every process that loads the library holds this array on every device it
+// touches, until exit (about 8.7 MB).
+__device__ __align__(256) uint32_t g_sort_scratch[NA_WORDS];
+
+constexpr int NA_MAX_DEVICES = 64;
+std::mutex g_na_mutex;
+uint32_t *g_na_addr[NA_MAX_DEVICES] = {};
+
+// Device address of g_sort_scratch on `device` (which must be current). The
+// symbol's name in host code is only a host-side handle, so the address is
+// looked up once per device and cached.
+stc_status sort_scratch(int device, uint32_t **out) {
+  std::lock_guard<std::mutex> lock(g_na_mutex);
+  if (!g_na_addr[device]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
+    if (e != cudaSuccess || !p) {
+      set_thread_error(std::string("stc_sort_pairs_u32_noalloc: cudaGetSymbolAddress failed: ") +
+                       cudaGetErrorString(e));
+      return STC_ERR_CUDA;
+    }
+    g_na_addr[device] = (uint32_t *)p;
+  }
+  *out = g_na_addr[device];
+  return STC_OK;
+}
+
+}  // namespace
+
+extern "C" stc_status stc_sort_pairs_u32_noalloc(const uint32_t *keys, const uint32_t *values, uint32_t *keys_out,
+                                                 uint32_t *values_out, size_t n, uint32_t key_bits,
+                                                 uint32_t device) {
+  stc_status st = sort_args_ok(keys, values, keys_out, values_out, n, key_bits, "stc_sort_pairs_u32_noalloc");
+  if (st != STC_OK) return st;
+  if (n > NA_MAX) {
+    set_thread_error("stc_sort_pairs_u32_noalloc: n = " + std::to_string(n) + " exceeds the " +
+                     std::to_string(NA_MAX) + " pairs its fixed scratch holds");
+    return STC_ERR_CAPACITY;
+  }
+  if (device >= (uint32_t)NA_MAX_DEVICES) {
+    set_thread_error("stc_sort_pairs_u32_noalloc: device ordinal out of range");
+    return STC_ERR_INVALID_ARG;
+  }
+  if (n == 0) return STC_OK;
+  cudaError_t e = cudaSetDevice((int)device);
+  if (e != cudaSuccess) {
+    set_thread_error(std::string("stc_sort_pairs_u32_noalloc: ") + cudaGetErrorString(e));
+    return STC_ERR_CUDA;
+  }
+  uint32_t *scratch = nullptr;
+  st = sort_scratch((int)device, &scratch);
+  if (st != STC_OK) return st;
+  uint32_t *ktmp = scratch, *vtmp = scratch + NA_MAX, *hist = vtmp + NA_MAX, *scan = hist + NA_HIST;
+  unsigned long long *n_dev = (unsigned long long *)(scratch + NA_COUNT_AT);
+  // the count and every histogram word the call reads are written by the
+  // call itself, so nothing left by an earlier call is used
+  STC_KL k_set_count<<<1, 1, 0, 0>>>(n_dev, (unsigned long long)n);
+  radix_sort_u32(keys, values, keys_out, values_out, ktmp, vtmp, n_dev, n, (int)key_bits, hist, scan, 0);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+  if (e != cudaSuccess) {
+    set_thread_error(std::string("stc_sort_pairs_u32_noalloc: ") + cudaGetErrorString(e));
     return STC_ERR_CUDA;
   }
   return STC_OK;
