@@ -72,6 +72,18 @@ typedef struct stc_config {
   uint64_t hit_capacity;         /* pairs buffered between refinement and table update; 0 = auto */
   uint32_t device;               /* CUDA device ordinal */
   uint32_t flags;                /* STC_FLAG_* (0 for normal operation) */
+  /* Memtable and flush into a contact tracing block (CTB) of CTFs, the
+   * reference's GPU flush (cuda/geometry.cu:1752-2138). Off while
+   * kv_restriction is 0. */
+  uint64_t kv_restriction;       /* flush after a step that leaves more directed keys than this
+                                    in the memtable (config.h:55, 80) */
+  uint64_t kv_capacity;          /* memtable size in directed keys; 0 = kv_restriction + 1,000,000
+                                    (config.h:81) */
+  uint32_t ctf_count;            /* CTFs per block, a perfect square <= 3969; 0 = 100 (config.h:59, 83-84) */
+  uint32_t start_time;           /* time of the first step; the first block's key times count from
+                                    start_time + min_meet_time (config.h:28, process.cpp:404) */
+  double area_restriction;       /* an object whose box over all its keys has a larger area (deg^2)
+                                    goes to the oversize buffer (process.cpp:408-411); 0 = 100, no cut */
 } stc_config;
 
 /* Replay quadtree splits/merges on one device thread only (tests compare it
@@ -107,7 +119,10 @@ typedef struct stc_stats {
   uint32_t ambiguous_tests;      /* distance decisions within a few ulp of reach, where
                                     the last bit of sin() could matter */
   float step_ms;                 /* device time of the step */
-  float phase_ms[8];             /* partition, border+jobs, refine, insert, sweep, schema, copy-in, 0 */
+  float phase_ms[8];             /* partition, border+jobs, refine, insert, sweep, schema, copy-in, memtable append */
+  uint64_t memtable_keys;        /* directed keys in the memtable after the step (and any flush) */
+  uint32_t flushes;              /* blocks flushed so far */
+  float flush_ms;                /* device time of the last flush */
 } stc_stats;
 
 /* Fills *cfg with the reference defaults for n objects (util/config.h:29-41,
@@ -133,6 +148,77 @@ stc_status stc_step_device(stc_ctx *ctx, const double *xy_device, uint32_t t);
 stc_status stc_drain_meetings(stc_ctx *ctx, stc_meeting *out, size_t cap, size_t *n);
 
 stc_status stc_get_stats(stc_ctx *ctx, stc_stats *stats);
+
+/* ---- Memtable flush: contact tracing blocks (CTBs) ----------------------
+ *
+ * With kv_restriction > 0 every emitted meeting also enters the memtable as
+ * two directed keys (pid, target, duration = end - start, end - end_time_min)
+ * with its float box, as cuda_identify_meetings does (cuda/geometry.cu:
+ * 701-737). After a step that leaves more than kv_restriction keys, stc_step
+ * flushes the memtable into a block, the reference's flush sequence
+ * (cuda/geometry.cu:1752-2138):
+ *   - objects whose box over all their keys is larger than area_restriction,
+ *     and both objects of a meeting longer than max_meet_time, get sid 1; their
+ *     keys go to the oversize buffer, sorted by key, with a 256 x 256 bitmap of
+ *     their boxes over the map;
+ *   - the other objects are ordered by the midpoint of their box (x, then y
+ *     within ctf_count^(1/2) slabs) and cut into ctf_count sids (2..);
+ *   - their keys, sorted by (sid, pid, target, duration, end), form the CTFs:
+ *     per CTF the box, time limits, bit widths (CTF::get_ctf_bits,
+ *     tracing/step_merge.cpp:140-186), an x_grid * y_grid bitmap of the key
+ *     boxes, and the keys packed into key_bit/8 bytes each (write_key_and_mbr).
+ * The block stays readable until the next flush. end_time_min of the next
+ * block is the flush step (process.cpp:271). */
+
+/* One CTF (an SSTable) of a block: the reference CTF's fields
+ * (tracing/step_merge.h:64-87) plus where its keys are. */
+typedef struct stc_ctf {
+  float mbr[4];                  /* ctf_mbr: box of its key boxes (low x, low y, high x, high y) */
+  uint32_t kv_count;             /* CTF_kv_capacity */
+  uint32_t start_time_min, start_time_max, end_time_min, end_time_max;
+  uint32_t bitmap_bytes;         /* ctf_bitmap_size: (x_grid * y_grid + 7) / 8 */
+  uint16_t key_bit, id_bit, duration_bit, end_bit, low_x_bit, low_y_bit, edge_bit, mbr_bit, x_grid, y_grid;
+  uint32_t pad;
+  uint64_t first_key;            /* index of its first key in the block's sorted keys */
+  uint64_t key_offset;           /* byte offset of its packed keys in the block's key bytes */
+} stc_ctf;
+
+typedef struct stc_ctb_info {
+  uint32_t index;                /* blocks flushed before this one */
+  uint32_t ctf_count;
+  uint32_t flush_time;           /* step after which it was flushed (end_time_max) */
+  uint32_t end_time_min;         /* base of the keys' end field */
+  uint64_t kv_count;             /* directed keys flushed (two per meeting) */
+  uint64_t ctf_kv_count;         /* keys in the CTFs */
+  uint64_t oversize_kv_count;    /* keys in the oversize buffer */
+  uint64_t key_bytes;            /* total bytes of packed CTF keys */
+  uint32_t sid_count;            /* objects with at least one key */
+  uint32_t oversize_oid_count;   /* the reference's counter: oversize objects plus meetings
+                                    longer than max_meet_time */
+  uint32_t o_start_time_min, o_start_time_max, o_end_time_min, o_end_time_max;  /* oversize buffer */
+} stc_ctb_info;
+
+/* Bytes of one bitmap slot: 256 x 256 bits (workbench bit_count,
+ * tracing/filter.cpp:72-73). CTF i's bitmap is slot i; its first
+ * bitmap_bytes bytes are used. */
+#define STC_BITMAP_BYTES 8192u
+
+/* Flushes the memtable now if it holds any key (*flushed = 1) -- the
+ * reference flushes only past kv_restriction; this also ends a run. */
+stc_status stc_flush(stc_ctx *ctx, int *flushed);
+
+/* Describes the last flushed block; STC_ERR_STATE if none yet. */
+stc_status stc_get_ctb(stc_ctx *ctx, stc_ctb_info *info);
+
+/* Copies parts of the last flushed block to host memory; any pointer may be
+ * NULL. Sizes: ctfs[ctf_count]; bitmaps[ctf_count * STC_BITMAP_BYTES];
+ * keys[key_bytes] (CTF i's keys at ctfs[i].key_offset, key_bit/8 bytes each,
+ * little-endian); sids[num_objects] (0 no key, 1 oversize, 2.. CTF + 2);
+ * oversize_keys[2 * oversize_kv_count] (128-bit keys pid:26 | target:26 |
+ * duration:32 | end:32 as (low, high) 64-bit halves, util.h:47-52);
+ * oversize_boxes[4 * oversize_kv_count]; oversize_bitmap[STC_BITMAP_BYTES]. */
+stc_status stc_read_ctb(stc_ctx *ctx, stc_ctf *ctfs, uint8_t *bitmaps, uint8_t *keys, uint16_t *sids,
+                        uint64_t *oversize_keys, float *oversize_boxes, uint8_t *oversize_bitmap);
 
 /* Last error message of ctx (or, when ctx is NULL, of the last failed
  * stc_create or context-free call on this thread). Never NULL. */

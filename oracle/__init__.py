@@ -5,6 +5,8 @@ package, and only as the checker or the timed CPU baseline. The product
 library (stcdb_gb300) never imports it.
 
   Oracle       ctypes wrapper of the C restatement in stc_oracle.c
+  LsmOracle    memtable + flush restatement (stc_lsm.c) and its pinned
+               single routines (ctf_bits, serialize_mbr, pack_key, o_bitmap)
   build()      compiles liboracle.so (and, where the read-only reference
                checkout exists, the reference harness oracle/_ref/ref_driver)
   run_reference_driver()  runs oracle/_ref/ref_driver on a trace (pinning)
@@ -22,17 +24,18 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "liboracle.so")
 REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
+REF_CTF = os.path.join(HERE, "_ref", "ref_ctf")
 
 MEETING_DTYPE = np.dtype([("pid_lo", "<u4"), ("pid_hi", "<u4"), ("start", "<u4"), ("end", "<u4"),
                           ("mbr", "<f4", (4,))])
 
 
 def build(reference: bool = True) -> None:
-    src = os.path.join(HERE, "stc_oracle.c")
-    deps = [src, os.path.join(HERE, "stc_oracle.h"), os.path.join(ROOT, "include", "stc.h")]
+    srcs = [os.path.join(HERE, "stc_oracle.c"), os.path.join(HERE, "stc_lsm.c")]
+    deps = srcs + [os.path.join(HERE, "stc_oracle.h"), os.path.join(ROOT, "include", "stc.h")]
     if not os.path.exists(LIB) or any(os.path.getmtime(d) > os.path.getmtime(LIB) for d in deps):
         subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-Wall",
-                        "-I" + os.path.join(ROOT, "include"), "-o", LIB, src, "-lm"], check=True)
+                        "-I" + os.path.join(ROOT, "include"), "-o", LIB] + srcs + ["-lm"], check=True)
     if reference:
         subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True)
 
@@ -60,6 +63,24 @@ def _lib():
     lib.oracle_grids_stack_index.argtypes = [ctypes.c_void_p]
     lib.oracle_grids_stack_index.restype = ctypes.c_uint32
     lib.oracle_schema_dump.argtypes = [ctypes.c_void_p] * 5
+    lib.lsm_create.restype = ctypes.c_void_p
+    lib.lsm_create.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double,
+                               ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64]
+    lib.lsm_destroy.argtypes = [ctypes.c_void_p]
+    lib.lsm_error.argtypes = [ctypes.c_void_p]
+    lib.lsm_error.restype = ctypes.c_char_p
+    lib.lsm_append.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
+    lib.lsm_kv_count.argtypes = [ctypes.c_void_p]
+    lib.lsm_kv_count.restype = ctypes.c_uint64
+    lib.lsm_flush.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
+    lib.lsm_get_ctb.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.lsm_read_ctb.argtypes = [ctypes.c_void_p] * 8
+    lib.lsm_ctf_bits.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32,
+                                 ctypes.c_void_p]
+    lib.lsm_serialize_mbr.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.lsm_serialize_mbr.restype = ctypes.c_uint64
+    lib.lsm_pack_key.argtypes = [ctypes.c_uint64] * 5 + [ctypes.c_void_p, ctypes.c_void_p]
+    lib.lsm_o_bitmap.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     return lib
 
 
@@ -132,6 +153,85 @@ class Oracle:
 
 def dpml(lat: float) -> float:
     return lib().oracle_dpml(lat)
+
+
+class LsmOracle:
+    """Memtable + flush restatement (stc_lsm.c). Feed each step's emitted
+    meetings with append(); flush(t) builds a block readable with read()."""
+
+    def __init__(self, num_objects: int, max_meet_time: int, ctf_count: int, area_restriction: float,
+                 first_end_time_min: int, mbr, capacity: int):
+        self._lib = lib()
+        self._n = num_objects
+        self._map = np.ascontiguousarray(mbr, dtype=np.float64)
+        self._h = self._lib.lsm_create(num_objects, max_meet_time, ctf_count, area_restriction,
+                                       first_end_time_min, self._map.ctypes.data, capacity)
+        if not self._h:
+            raise MemoryError("lsm_create failed")
+
+    def append(self, meetings: np.ndarray) -> None:
+        m = np.ascontiguousarray(meetings, dtype=MEETING_DTYPE)
+        if self._lib.lsm_append(self._h, m.ctypes.data, len(m)) != 0:
+            raise RuntimeError(self._lib.lsm_error(self._h).decode())
+
+    def kv_count(self) -> int:
+        return int(self._lib.lsm_kv_count(self._h))
+
+    def flush(self, t: int) -> None:
+        if self._lib.lsm_flush(self._h, t) != 0:
+            raise RuntimeError(self._lib.lsm_error(self._h).decode())
+
+    def read(self):
+        from stcdb_gb300.pipeline import StcCtbInfo, ctb_buffers, ctb_trim
+        info = StcCtbInfo()
+        if self._lib.lsm_get_ctb(self._h, ctypes.byref(info)) != 0:
+            raise RuntimeError("no block flushed")
+        b = ctb_buffers(info, self._n)
+        self._lib.lsm_read_ctb(self._h, *[b[k].ctypes.data for k in (
+            "ctfs", "bitmaps", "keys", "sids", "oversize_keys", "oversize_boxes", "oversize_bitmap")])
+        return info, ctb_trim(info, b)
+
+    def close(self):
+        if self._h:
+            self._lib.lsm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def ctf_bits(mbr, map_box, num_objects: int, max_meet_time: int) -> np.ndarray:
+    """lsm_ctf_bits for one CTF box: an stc_ctf record with the bit fields set."""
+    from stcdb_gb300.pipeline import CTF_DTYPE
+    c = np.zeros(1, CTF_DTYPE)
+    c["mbr"][0] = np.asarray(mbr, np.float32)
+    m = np.ascontiguousarray(map_box, np.float64)
+    f = np.ascontiguousarray(np.asarray(mbr, np.float32))
+    lib().lsm_ctf_bits(f.ctypes.data, m.ctypes.data, num_objects, max_meet_time, c.ctypes.data)
+    return c
+
+
+def serialize_mbr(box, ctf: np.ndarray) -> int:
+    b = np.ascontiguousarray(np.asarray(box, np.float32))
+    return int(lib().lsm_serialize_mbr(b.ctypes.data, ctf.ctypes.data))
+
+
+def pack_key(pid_field: int, target: int, duration: int, end: int, value_mbr: int, ctf: np.ndarray) -> bytes:
+    out = np.zeros(16, np.uint8)
+    lib().lsm_pack_key(pid_field, target, duration, end, value_mbr, ctf.ctypes.data, out.ctypes.data)
+    return bytes(out[: int(ctf["key_bit"][0]) // 8])
+
+
+def o_bitmap(boxes: np.ndarray, map_box) -> np.ndarray:
+    bm = np.zeros(8192, np.uint8)
+    m = np.ascontiguousarray(map_box, np.float64)
+    for b in np.ascontiguousarray(boxes, np.float32).reshape(-1, 4):
+        bb = np.ascontiguousarray(b)
+        lib().lsm_o_bitmap(bb.ctypes.data, m.ctypes.data, bm.ctypes.data)
+    return bm
 
 
 # ---------------------------------------------------------------------------

@@ -1,7 +1,8 @@
 #!/usr/bin/env bash
 # Compiles the reference's own CPU co-occurrence path from its unmodified
 # sources (read in place, never copied) plus the harness oracle/ref_driver.cpp
-# into oracle/_ref/ref_driver. The reference is only present on the machine
+# into oracle/_ref/ref_driver, and oracle/ref_ctf.cpp (the reference's host CTF
+# encoding routines) into oracle/_ref/ref_ctf. The reference is only present on the machine
 # that holds the read-only checkout; elsewhere this script exits 0 and does
 # nothing, and the committed fixtures under tests/golden/ stand in for it.
 #
@@ -30,5 +31,11 @@ for s in $SRCS; do
 done
 wait
 g++ -std=c++17 -O2 -ffp-contract=off -w -fopenmp -I"$HERE/ref_stub" -I"$REF/src" -I"$CUDA_INC" \
-  "$HERE/ref_driver.cpp" $OBJS -o "$OUT/ref_driver" -lpthread
-echo "build_ref: built $OUT/ref_driver" >&2
+  "$HERE/ref_driver.cpp" $OBJS -o "$OUT/ref_driver" -lpthread &
+P1=$!
+g++ -std=c++17 -O2 -ffp-contract=off -w -fopenmp -I"$HERE/ref_stub" -I"$REF/src" -I"$CUDA_INC" \
+  "$HERE/ref_ctf.cpp" $OBJS -o "$OUT/ref_ctf" -lpthread &
+P2=$!
+wait "$P1"
+wait "$P2"
+echo "build_ref: built $OUT/ref_driver and $OUT/ref_ctf" >&2

@@ -49,6 +49,29 @@ uint32_t oracle_grids_stack_index(oracle_ctx *c);
  * so tests can compare the device implementation against host libm. */
 double oracle_dpml(double latitude);
 
+/* ---- memtable and flush (oracle/stc_lsm.c) ----------------------------
+ * Feed each step's emitted meetings with lsm_append; flush when
+ * lsm_kv_count exceeds the restriction (or to end a run). Read-out layout is
+ * that of stc_read_ctb. */
+typedef struct lsm_oracle lsm_oracle;
+lsm_oracle *lsm_create(uint32_t n, uint32_t max_meet_time, uint32_t ctf_count, double area_restriction,
+                       uint32_t first_end_time_min, const double map[4], uint64_t capacity);
+void lsm_destroy(lsm_oracle *o);
+const char *lsm_error(const lsm_oracle *o);
+int lsm_append(lsm_oracle *o, const stc_meeting *m, size_t count);
+uint64_t lsm_kv_count(const lsm_oracle *o);
+int lsm_flush(lsm_oracle *o, uint32_t cur_time);
+int lsm_get_ctb(const lsm_oracle *o, stc_ctb_info *info);
+int lsm_read_ctb(const lsm_oracle *o, stc_ctf *ctfs, uint8_t *bitmaps, uint8_t *keys, uint16_t *sids,
+                 uint64_t *okeys, float *oboxes, uint8_t *obitmap);
+/* single routines, pinned against the reference's host code */
+int lsm_ctf_bits(const float mbr[4], const double map[4], uint32_t num_objects, uint32_t max_meet_time,
+                 stc_ctf *c);
+uint64_t lsm_serialize_mbr(const float b[4], const stc_ctf *c);
+void lsm_pack_key(uint64_t pid_field, uint64_t target, uint64_t duration, uint64_t end, uint64_t value_mbr,
+                  const stc_ctf *c, uint8_t *out);
+void lsm_o_bitmap(const float b[4], const double map[4], uint8_t *bitmap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,6 +32,7 @@ CU_SOURCES = [
     "stc_schema.cu",
     "stc_sort.cu",
     "stc_util.cu",
+    "stc_lsm.cu",
 ]
 
 

@@ -31,6 +31,7 @@ enum {
   ERR_SCHEMA = 7,      // schema or grid stack exhausted
   ERR_LOOKUP = 8,      // border lookup stack overflow
   ERR_BUILD = 9,       // initial quadtree build exceeded capacity
+  ERR_MEMTABLE = 10,   // memtable full
 };
 
 // One meeting-table slot (32 B; the reference's meeting_unit of
@@ -95,6 +96,13 @@ struct DevState {
   unsigned long long hit_count;       // hits appended to the hit buffer this step
   uint32_t schema_path;               // 1 parallel replay, 2 serial (cascade), 0 serial (other)
   uint32_t pad2;
+  // memtable (stc_lsm.cu)
+  unsigned long long kv_count;        // directed keys in the memtable
+  unsigned long long lsm_over_keys;   // keys partitioned to the oversize buffer (flush)
+  uint32_t lsm_sid_count;             // objects with at least one key
+  uint32_t lsm_over_count;            // the reference's oversize_oid_count
+  uint32_t lsm_max_dur, lsm_max_end;  // largest duration / end offset (flush sort widths)
+  uint32_t lsm_os_min, lsm_os_max;    // oversize buffer start times (flush)
 };
 
 __device__ __forceinline__ void stc_set_error(DevState *st, uint32_t code, uint32_t info) {

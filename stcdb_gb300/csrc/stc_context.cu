@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include "stc_lsm.cuh"
 #include "stc_pipeline.cuh"
 
 using namespace stc;
@@ -20,7 +21,8 @@ namespace {
 
 thread_local std::string g_create_error = "no error";
 
-enum Phase { PH_START = 0, PH_COPY, PH_PART, PH_BORDER, PH_REFINE, PH_INSERT, PH_SWEEP, PH_SCHEMA, PH_COUNT };
+enum Phase { PH_START = 0, PH_COPY, PH_PART, PH_BORDER, PH_REFINE, PH_INSERT, PH_SWEEP, PH_APPEND, PH_SCHEMA,
+             PH_FLUSH0, PH_FLUSH1, PH_COUNT };
 
 }  // namespace
 
@@ -42,6 +44,9 @@ struct stc_ctx {
   std::vector<void *> allocs;
   stc_stats stats;
   uint32_t last_t = 0;
+  bool lsm_on = false;           // memtable and flush (kv_restriction > 0)
+  LsmDev lsm;
+  LsmHost lsmh;
 };
 
 static const char *error_name(uint32_t e) {
@@ -55,6 +60,7 @@ static const char *error_name(uint32_t e) {
     case ERR_SCHEMA: return "quadtree schema or grid stack exhausted";
     case ERR_LOOKUP: return "border lookup stack overflow";
     case ERR_BUILD: return "initial quadtree exceeds schema capacity";
+    case ERR_MEMTABLE: return "memtable full: raise kv_capacity";
     default: return "unknown device error";
   }
 }
@@ -62,6 +68,7 @@ static const char *error_name(uint32_t e) {
 static stc_status status_of(uint32_t e) {
   switch (e) {
     case ERR_UNITS: case ERR_PROBE: case ERR_CAND: case ERR_EMIT: case ERR_SCHEMA: case ERR_LOOKUP: case ERR_BUILD:
+    case ERR_MEMTABLE:
       return STC_ERR_CAPACITY;
     case ERR_DA: return STC_ERR_TIMEOUT;
     default: return STC_ERR_STATE;
@@ -175,6 +182,16 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
     g_create_error = "stc_create: invalid configuration";
     return STC_ERR_INVALID_ARG;
   }
+  const uint32_t ctf_count = k.ctf_count ? k.ctf_count : 100;  // util/config.h:59
+  const uint32_t split = (uint32_t)std::lround(std::sqrt((double)ctf_count));
+  if (k.kv_restriction &&
+      (split * split != ctf_count || ctf_count > 3969 || n >= (1u << 26) || k.max_meet_time == 0 ||
+       k.area_restriction < 0 || (k.kv_capacity && k.kv_capacity <= k.kv_restriction) ||
+       k.kv_restriction >= (1ull << 31) || k.kv_capacity >= (1ull << 31))) {
+    g_create_error = "stc_create: invalid memtable configuration (ctf_count must be a square <= 3969, "
+                     "num_objects < 2^26, kv_capacity > kv_restriction, both < 2^31)";
+    return STC_ERR_INVALID_ARG;
+  }
   stc_ctx *c = new (std::nothrow) stc_ctx();
   if (!c) {
     g_create_error = "stc_create: out of host memory";
@@ -252,6 +269,33 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
             dalloc(c, &p.job_start, (size_t)p.G + 1) && dalloc(c, &p.slots, p.B) && dalloc(c, &p.hits, p.hit_cap) && dalloc(c, &p.cset, p.C) &&
             dalloc(c, &p.cand_list, p.cand_cap) && dalloc(c, &p.emit, p.E) && dalloc(c, &p.scan_tmp, scan_words) &&
             dalloc(c, &p.n_dev, 1);
+  if (ok && k.kv_restriction) {
+    LsmDev &L = c->lsm;
+    memset(&L, 0, sizeof(L));
+    c->lsm_on = true;
+    L.N = n;
+    L.max_meet = k.max_meet_time;
+    L.F = ctf_count;
+    L.split = split;
+    L.end_time_min = k.start_time + k.min_meet_time;  // tracing/process.cpp:404
+    L.area = k.area_restriction > 0 ? k.area_restriction : 100.0;  // process.cpp:408-411: 100 = no cut
+    L.map[0] = mbr[0]; L.map[1] = mbr[1]; L.map[2] = mbr[2]; L.map[3] = mbr[3];
+    // a step adds at most two keys per emitted meeting, so the default never overflows
+    L.cap = k.kv_capacity ? k.kv_capacity
+                          : std::min<unsigned long long>(k.kv_restriction + 2 * p.E, (1ull << 31) - 1);
+    size_t w = lsm_sort_words(L);
+    size_t hw = radix_hist_words(w);
+    ok = dalloc(c, &L.rec, L.cap) && dalloc(c, &L.box, L.cap) && dalloc(c, &L.brec, L.cap) &&
+         dalloc(c, &L.bbox, L.cap) && dalloc(c, &L.over, L.cap) && dalloc(c, &L.hist, hw) &&
+         dalloc(c, &L.scan, scan_tmp_words(hw)) && dalloc(c, &L.n_dev, 4) && dalloc(c, &L.cnt, n) &&
+         dalloc(c, &L.obox, n) && dalloc(c, &L.sid, n) && dalloc(c, &L.bsid, n) && dalloc(c, &L.mid_lo, n) &&
+         dalloc(c, &L.mid_hi, n) && dalloc(c, &L.ctf_cap, ctf_count) && dalloc(c, &L.ctf_first, ctf_count + 1) &&
+         dalloc(c, &L.ctfs, ctf_count) && dalloc(c, &L.lim_box, ctf_count) && dalloc(c, &L.lim_time, ctf_count) &&
+         dalloc(c, &L.bitmaps, (size_t)ctf_count * (STC_BITMAP_BYTES / 4)) &&
+         dalloc(c, &L.obitmap, STC_BITMAP_BYTES / 4) && dalloc(c, &L.kbytes, 16 * (size_t)L.cap);
+    for (int i = 0; ok && i < 7; i++) ok = dalloc(c, &L.sk[i], w);
+    L.st = p.st;
+  }
   if (!ok) {
     g_create_error = "stc_create: " + c->err;
     destroy_all(c);
@@ -278,6 +322,7 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
   cudaMemcpyAsync(p.n_dev, &nn, sizeof(nn), cudaMemcpyHostToDevice, s);
   iota_u32(p.iota, nu, s);
   init_tables(p, s);
+  if (c->lsm_on) lsm_init(c->lsm, s);
   e = cudaMemcpyAsync(c->xy_own, xy0, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess)
     e = build_schema(c->xy_own, n, mbr, k.reach_distance, k.grid_capacity, p.sd, p.sw, p.st, c->st_host, s);
@@ -293,6 +338,25 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
   c->stats.leaves = c->st_host->grids_stack_index;
   c->stats.schema_nodes = c->st_host->schema_stack_index;
   *out = c;
+  return STC_OK;
+}
+
+static stc_status flush_now(stc_ctx *c, uint32_t t) {
+  cudaEventRecord(c->ev[PH_FLUSH0], c->stream);
+  unsigned long long launches0 = tl_launches;
+  std::string err;
+  stc_status rs = lsm_flush(c->lsm, c->lsmh, t, c->stream, c->st_host, err);
+  if (rs != STC_OK) return fail(c, rs, "stc flush: " + err);
+  if (c->st_host->error) return read_state(c, "stc flush");
+  cudaEventRecord(c->ev[PH_FLUSH1], c->stream);
+  cudaError_t e = cudaEventSynchronize(c->ev[PH_FLUSH1]);
+  if (e != cudaSuccess) return cuda_fail(c, e, "stc flush");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev[PH_FLUSH0], c->ev[PH_FLUSH1]);
+  c->stats.flush_ms = ms;
+  c->stats.flushes = c->lsmh.flushes;
+  c->stats.memtable_keys = c->st_host->kv_count;
+  c->stats.kernel_launches += (uint32_t)(tl_launches - launches0);
   return STC_OK;
 }
 
@@ -314,6 +378,8 @@ static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copie
   cudaEventRecord(c->ev[PH_INSERT], s);
   step_sweep(p, t, s);
   cudaEventRecord(c->ev[PH_SWEEP], s);
+  if (c->lsm_on) lsm_append(p, c->lsm, s);
+  cudaEventRecord(c->ev[PH_APPEND], s);
   if (c->cfg.dynamic_schema)
     update_schema(p.sd, p.sw, p.grid_count, p.reach, p.grid_capacity, p.delay,
                   (c->cfg.flags & STC_FLAG_SERIAL_SCHEMA) != 0, p.st, s);
@@ -338,7 +404,7 @@ static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copie
   o.splits = h.splits;
   o.merges = h.merges;
   float ms[PH_COUNT] = {0};
-  for (int i = PH_COPY; i < PH_COUNT; i++) cudaEventElapsedTime(&ms[i], c->ev[i - 1], c->ev[i]);
+  for (int i = PH_COPY; i <= PH_SCHEMA; i++) cudaEventElapsedTime(&ms[i], c->ev[i - 1], c->ev[i]);
   o.phase_ms[0] = ms[PH_PART];
   o.phase_ms[1] = ms[PH_BORDER];
   o.phase_ms[2] = ms[PH_REFINE];
@@ -346,7 +412,7 @@ static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copie
   o.phase_ms[4] = ms[PH_SWEEP];
   o.phase_ms[5] = ms[PH_SCHEMA];
   o.phase_ms[6] = copied ? ms[PH_COPY] : 0.f;
-  o.phase_ms[7] = 0.f;
+  o.phase_ms[7] = ms[PH_APPEND];
   o.ambiguous_tests = (uint32_t)h.ambiguous;
   o.kernel_launches = (uint32_t)(tl_launches - launches0);
   o.schema_path = h.schema_path;
@@ -355,6 +421,10 @@ static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copie
   o.step_ms = tot;
   c->stepped = true;
   c->last_t = t;
+  o.memtable_keys = h.kv_count;
+  // the reference flushes once a step leaves more keys than kv_restriction
+  // (cuda/geometry.cu:1752)
+  if (c->lsm_on && h.kv_count > c->cfg.kv_restriction) return flush_now(c, t);
   return STC_OK;
 }
 
@@ -408,5 +478,65 @@ extern "C" stc_status stc_drain_meetings(stc_ctx *c, stc_meeting *out, size_t ca
   c->st_host->emit_count = left;
   c->stats.pending = left;
   *n = k;
+  return STC_OK;
+}
+
+extern "C" stc_status stc_flush(stc_ctx *c, int *flushed) {
+  if (!c) return STC_ERR_INVALID_ARG;
+  if (flushed) *flushed = 0;
+  if (c->failed) return STC_ERR_STATE;
+  if (!c->lsm_on) return fail(c, STC_ERR_INVALID_ARG, "stc_flush: the memtable is off (kv_restriction 0)");
+  cudaSetDevice(c->device);
+  if (c->st_host->kv_count == 0) return STC_OK;
+  stc_status rs = flush_now(c, c->last_t);
+  if (rs == STC_OK && flushed) *flushed = 1;
+  return rs;
+}
+
+extern "C" stc_status stc_get_ctb(stc_ctx *c, stc_ctb_info *info) {
+  if (!c || !info) return STC_ERR_INVALID_ARG;
+  if (!c->lsmh.has_block) {
+    c->err = "stc_get_ctb: no block flushed yet";
+    return STC_ERR_STATE;
+  }
+  *info = c->lsmh.info;
+  return STC_OK;
+}
+
+extern "C" stc_status stc_read_ctb(stc_ctx *c, stc_ctf *ctfs, uint8_t *bitmaps, uint8_t *keys, uint16_t *sids,
+                                   uint64_t *oversize_keys, float *oversize_boxes, uint8_t *oversize_bitmap) {
+  if (!c) return STC_ERR_INVALID_ARG;
+  if (!c->lsmh.has_block) {
+    c->err = "stc_read_ctb: no block flushed yet";
+    return STC_ERR_STATE;
+  }
+  cudaSetDevice(c->device);
+  const stc_ctb_info &in = c->lsmh.info;
+  const LsmDev &L = c->lsm;
+  cudaStream_t s = c->stream;
+  cudaError_t e = cudaSuccess;
+  if (ctfs) memcpy(ctfs, c->lsmh.ctfs.data(), in.ctf_count * sizeof(stc_ctf));
+  if (bitmaps)
+    e = cudaMemcpyAsync(bitmaps, L.bitmaps, (size_t)in.ctf_count * STC_BITMAP_BYTES, cudaMemcpyDeviceToHost, s);
+  if (keys && in.key_bytes && e == cudaSuccess)
+    e = cudaMemcpyAsync(keys, L.kbytes, in.key_bytes, cudaMemcpyDeviceToHost, s);
+  if (sids && e == cudaSuccess) e = cudaMemcpyAsync(sids, L.bsid, (size_t)L.N * 2, cudaMemcpyDeviceToHost, s);
+  if (oversize_bitmap && e == cudaSuccess)
+    e = cudaMemcpyAsync(oversize_bitmap, L.obitmap, STC_BITMAP_BYTES, cudaMemcpyDeviceToHost, s);
+  std::vector<uint4> orec;
+  const size_t no = (size_t)in.oversize_kv_count;
+  if (no && oversize_keys && e == cudaSuccess) {
+    orec.resize(no);
+    e = cudaMemcpyAsync(orec.data(), L.brec + in.ctf_kv_count, no * sizeof(uint4), cudaMemcpyDeviceToHost, s);
+  }
+  if (no && oversize_boxes && e == cudaSuccess)
+    e = cudaMemcpyAsync(oversize_boxes, L.bbox + in.ctf_kv_count, no * sizeof(float4), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "stc_read_ctb");
+  // 128-bit oversize keys pid:26 | target:26 | duration:32 | end:32 (util/util.h:47-52)
+  for (size_t i = 0; i < orec.size(); i++) {
+    oversize_keys[2 * i] = ((uint64_t)orec[i].z << 32) | orec[i].w;
+    oversize_keys[2 * i + 1] = ((uint64_t)orec[i].x << 26) | orec[i].y;
+  }
   return STC_OK;
 }

@@ -1,0 +1,79 @@
+// Memtable and flush into contact tracing blocks (the LSM layer).
+//
+// The reference keeps its memtable in the GPU workbench (d_keys / kv_boxs,
+// filled by cuda_identify_meetings, cuda/geometry.cu:701-737) and flushes it
+// in process_with_gpu (cuda/geometry.cu:1752-2138). Here the memtable is a
+// pair of device arrays appended to after every step's sweep, and a flush is
+// a short host-driven sequence of device sorts and per-key kernels:
+//
+//   memtable   rec[i] = (pid, target, duration, end - end_time_min)   uint4
+//              box[i] = float box of the meeting                     float4
+//   per object cnt (keys), obox (uint_box of all its key boxes), sid
+//   block      brec/bbox: CTF keys sorted by (sid, pid, target, duration,
+//              end), then the oversize keys sorted by (pid, target, ...);
+//              kbytes: packed CTF keys; bitmaps; ctfs; bsid.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "stc_pipeline.cuh"
+
+namespace stc {
+
+struct LsmDev {
+  uint32_t N, max_meet, F, split;
+  uint32_t end_time_min;
+  double area;
+  double map[4];
+  unsigned long long cap;          // memtable capacity (directed keys)
+  DevState *st;
+  uint4 *rec;                      // memtable keys
+  float4 *box;                     // memtable boxes
+  uint4 *brec;                     // block: sorted keys
+  float4 *bbox;
+  uint8_t *over;                   // per memtable key: oversize at partition time
+  uint32_t *sk[7];                 // sort scratch, max(cap, N) words each
+  uint32_t *hist, *scan;           // radix-sort histograms and scan blocks
+  unsigned long long *n_dev;       // [4] item counts read by the sorts
+  uint32_t *cnt;                   // per object: keys (same_pid_count)
+  uint4 *obox;                     // per object: low0, low1, high0, high1 (float_to_uint)
+  uint16_t *sid;                   // per object: working sid
+  uint16_t *bsid;                  // per object: sids of the last block
+  uint32_t *mid_lo, *mid_hi;       // per object: STR midpoint (y, x)
+  uint32_t *ctf_cap;               // [F]
+  unsigned long long *ctf_first;   // [F + 1]
+  stc_ctf *ctfs;                   // [F]
+  float4 *lim_box;                 // [F] per-CTF box
+  uint2 *lim_time;                 // [F] per-CTF start min, max
+  uint32_t *bitmaps;               // [F * 2048]
+  uint32_t *obitmap;               // [2048]
+  uint8_t *kbytes;                 // packed CTF keys (16 * cap bytes)
+};
+
+struct LsmHost {
+  bool has_block = false;
+  uint32_t flushes = 0;
+  stc_ctb_info info{};
+  std::vector<stc_ctf> ctfs;
+};
+
+// Words of sort scratch per array and radix histogram words for the flush.
+size_t lsm_sort_words(const LsmDev &L);
+
+// Initial memtable state (empty, object boxes at their initial values).
+void lsm_init(LsmDev &L, cudaStream_t s);
+
+// Appends the step's emitted meetings (the last step_emitted records of the
+// emit buffer) as two directed keys each.
+void lsm_append(const PipeDev &p, const LsmDev &L, cudaStream_t s);
+
+// Flushes the memtable at step t into a block. st_host is a pinned DevState
+// mirror used for read-backs. On failure returns a status and sets err.
+stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState *st_host, std::string &err);
+
+// Host restatement of CTF::get_ctf_bits (tracing/step_merge.cpp:140-186);
+// returns false when the key would exceed 64 box bits or 128 key bits.
+bool ctf_bits(const float mbr[4], const double map[4], uint32_t num_objects, uint32_t max_meet_time,
+              stc_ctf *c);
+
+}  // namespace stc

@@ -47,6 +47,11 @@ class _Config(ctypes.Structure):
         ("hit_capacity", ctypes.c_uint64),
         ("device", ctypes.c_uint32),
         ("flags", ctypes.c_uint32),
+        ("kv_restriction", ctypes.c_uint64),
+        ("kv_capacity", ctypes.c_uint64),
+        ("ctf_count", ctypes.c_uint32),
+        ("start_time", ctypes.c_uint32),
+        ("area_restriction", ctypes.c_double),
     ]
 
 
@@ -72,6 +77,9 @@ class StcStats(ctypes.Structure):
         ("ambiguous_tests", ctypes.c_uint32),
         ("step_ms", ctypes.c_float),
         ("phase_ms", ctypes.c_float * 8),
+        ("memtable_keys", ctypes.c_uint64),
+        ("flushes", ctypes.c_uint32),
+        ("flush_ms", ctypes.c_float),
     ]
 
     def as_dict(self) -> dict:
@@ -80,6 +88,60 @@ class StcStats(ctypes.Structure):
             v = getattr(self, name)
             d[name] = list(v) if name == "phase_ms" else v
         return d
+
+
+class StcCtbInfo(ctypes.Structure):
+    """stc_ctb_info: one flushed contact tracing block."""
+    _fields_ = [
+        ("index", ctypes.c_uint32),
+        ("ctf_count", ctypes.c_uint32),
+        ("flush_time", ctypes.c_uint32),
+        ("end_time_min", ctypes.c_uint32),
+        ("kv_count", ctypes.c_uint64),
+        ("ctf_kv_count", ctypes.c_uint64),
+        ("oversize_kv_count", ctypes.c_uint64),
+        ("key_bytes", ctypes.c_uint64),
+        ("sid_count", ctypes.c_uint32),
+        ("oversize_oid_count", ctypes.c_uint32),
+        ("o_start_time_min", ctypes.c_uint32),
+        ("o_start_time_max", ctypes.c_uint32),
+        ("o_end_time_min", ctypes.c_uint32),
+        ("o_end_time_max", ctypes.c_uint32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+# stc_ctf (include/stc.h), 80 bytes
+CTF_DTYPE = np.dtype([("mbr", "<f4", (4,)), ("kv_count", "<u4"), ("start_time_min", "<u4"),
+                      ("start_time_max", "<u4"), ("end_time_min", "<u4"), ("end_time_max", "<u4"),
+                      ("bitmap_bytes", "<u4"), ("key_bit", "<u2"), ("id_bit", "<u2"), ("duration_bit", "<u2"),
+                      ("end_bit", "<u2"), ("low_x_bit", "<u2"), ("low_y_bit", "<u2"), ("edge_bit", "<u2"),
+                      ("mbr_bit", "<u2"), ("x_grid", "<u2"), ("y_grid", "<u2"), ("pad", "<u4"),
+                      ("first_key", "<u8"), ("key_offset", "<u8")])
+assert CTF_DTYPE.itemsize == 80
+BITMAP_BYTES = 8192  # STC_BITMAP_BYTES
+
+
+def ctb_buffers(info: StcCtbInfo, num_objects: int) -> dict:
+    """Host arrays sized for one block, in the layout of stc_read_ctb."""
+    return dict(ctfs=np.zeros(info.ctf_count, CTF_DTYPE),
+                bitmaps=np.zeros(info.ctf_count * BITMAP_BYTES, np.uint8),
+                keys=np.zeros(max(int(info.key_bytes), 1), np.uint8),
+                sids=np.zeros(num_objects, np.uint16),
+                oversize_keys=np.zeros(2 * max(int(info.oversize_kv_count), 1), np.uint64),
+                oversize_boxes=np.zeros(4 * max(int(info.oversize_kv_count), 1), np.float32),
+                oversize_bitmap=np.zeros(BITMAP_BYTES, np.uint8))
+
+
+def ctb_trim(info: StcCtbInfo, bufs: dict) -> dict:
+    """Cuts the padded buffers of ctb_buffers to the block's sizes."""
+    out = dict(bufs)
+    out["keys"] = bufs["keys"][: int(info.key_bytes)]
+    out["oversize_keys"] = bufs["oversize_keys"][: 2 * int(info.oversize_kv_count)]
+    out["oversize_boxes"] = bufs["oversize_boxes"][: 4 * int(info.oversize_kv_count)]
+    return out
 
 
 @dataclass(frozen=True)
@@ -101,6 +163,11 @@ class StcConfig:
     hit_capacity: int = 0
     device: int = 0
     flags: int = 0            # STC_FLAG_* bits of include/stc.h
+    kv_restriction: int = 0   # memtable flush threshold in directed keys; 0 = no memtable
+    kv_capacity: int = 0      # 0 = kv_restriction + 1,000,000
+    ctf_count: int = 0        # 0 = 100
+    start_time: int = 0
+    area_restriction: float = 0.0  # 0 = 100 (no cut)
 
     def resolved(self) -> "StcConfig":
         if self.num_meeting_buckets == 0:
@@ -136,6 +203,12 @@ def _lib():
         lib.stc_last_error.argtypes = [ctypes.c_void_p]
         lib.stc_last_error.restype = ctypes.c_char_p
         lib.stc_destroy.argtypes = [ctypes.c_void_p]
+        lib.stc_flush.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+        lib.stc_flush.restype = ctypes.c_int
+        lib.stc_get_ctb.argtypes = [ctypes.c_void_p, ctypes.POINTER(StcCtbInfo)]
+        lib.stc_get_ctb.restype = ctypes.c_int
+        lib.stc_read_ctb.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 7
+        lib.stc_read_ctb.restype = ctypes.c_int
         lib._stc_typed = True
     return lib
 
@@ -185,6 +258,25 @@ class Pipeline:
             if n.value < cap or n.value == 0:
                 break
         return np.concatenate(out) if out else np.zeros(0, MEETING_DTYPE)
+
+    def flush(self) -> bool:
+        """Flushes the memtable into a block now; False if it was empty."""
+        f = ctypes.c_int()
+        self._check(self._lib.stc_flush(self._h, ctypes.byref(f)))
+        return bool(f.value)
+
+    def ctb_info(self) -> StcCtbInfo:
+        info = StcCtbInfo()
+        self._check(self._lib.stc_get_ctb(self._h, ctypes.byref(info)))
+        return info
+
+    def read_ctb(self) -> tuple:
+        """(info, dict of host arrays) of the last flushed block."""
+        info = self.ctb_info()
+        b = ctb_buffers(info, self.cfg.num_objects)
+        self._check(self._lib.stc_read_ctb(self._h, *[b[k].ctypes.data for k in (
+            "ctfs", "bitmaps", "keys", "sids", "oversize_keys", "oversize_boxes", "oversize_bitmap")]))
+        return info, ctb_trim(info, b)
 
     def close(self):
         if getattr(self, "_h", None):
