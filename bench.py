@@ -20,6 +20,9 @@ value: position updates per second with positions already resident in HBM
   (stc_step_device), summed device time of K steps (CUDA events on the
   library's stream). Inputs (160 MB per step) and the meeting table exceed
   the 129 MB L2, so no flush is inserted between steps.
+Every step also appends its emitted meetings to the memtable (two directed
+  keys each, as the reference's GPU step does); the JSON's "flush" times one
+  flush of everything gathered over the run into 100 CTFs.
 e2e: the same metric through the public C ABI with host input: every step
   copies that step's positions from pinned host memory (stc_step) and drains
   the emitted meetings back to the host (stc_drain_meetings); wall clock.
@@ -47,11 +50,11 @@ UNIT = "pos-updates/s"
 
 WORKLOADS = {
     "uniform-10M": dict(objects=10_000_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
-                        buckets=1 << 28),
+                        buckets=1 << 28, kv_restriction=1 << 27),
     "hotspot-1M": dict(objects=1_000_000, hot=1000, reach=10.0, min_meet=5, grid_capacity=200, amplify=8.0,
-                       buckets=1 << 28),
+                       buckets=1 << 28, kv_restriction=1 << 27),
     "uniform-100k": dict(objects=100_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
-                         buckets_per_object=8),
+                         buckets_per_object=8, kv_restriction=1 << 22),
 }
 
 
@@ -74,7 +77,7 @@ def make_cfg(w, device=0):
     b = w.get("buckets") or w["buckets_per_object"] * w["objects"]
     return StcConfig(num_objects=w["objects"], reach_distance=w["reach"], min_meet_time=w["min_meet"],
                      grid_capacity=w["grid_capacity"], grid_amplify=w["amplify"], num_meeting_buckets=b,
-                     device=device)
+                     device=device, kv_restriction=w["kv_restriction"])
 
 
 class ClockSampler:
@@ -190,9 +193,17 @@ def run_gpu(args, w, rank, local):
         e2e_stats.append(pipe.stats())
     torch.cuda.synchronize()
     wall_e2e = time.perf_counter() - t1
+    # one flush of everything the memtable gathered (W + 2K steps)
+    keys = pipe.stats().memtable_keys
+    pipe.flush()
+    fs = pipe.stats()
+    info = pipe.ctb_info()
     pipe.close()
+    flush = dict(keys=int(keys), ms=float(fs.flush_ms), ctf_keys=int(info.ctf_kv_count),
+                 oversize_keys=int(info.oversize_kv_count), key_bytes=int(info.key_bytes),
+                 ctfs=int(info.ctf_count), steps=total_steps)
     return dict(stats=stats, dev_ms=dev_ms, wall_dev=wall_dev, wall_e2e=wall_e2e, e2e_stats=e2e_stats,
-                d2h=d2h, clocks=clk.summary())
+                d2h=d2h, clocks=clk.summary(), flush=flush)
 
 
 def barrier(args):
@@ -219,6 +230,17 @@ def kernel_bytes(s, N, B):
     H, Q = s.border_units, s.hits
     return {"partition": 36.0 * N, "refine": 16.0 * N + 16.0 * H + 72.0 * Q,
             "sweep": 32.0 * B + 64.0 * s.emitted}
+
+
+def flush_line(f, peak):
+    """One memtable flush: algorithmic bytes 64 per key (key + box read and
+    written once) plus the packed keys and the bitmap slots written."""
+    if not f["keys"]:
+        return dict(f)
+    ab = 64.0 * f["keys"] + f["key_bytes"] + 8192.0 * (f["ctfs"] + 1)
+    gbs = ab / (f["ms"] / 1e3) / 1e9
+    return dict(f, keys_per_s=f["keys"] / (f["ms"] / 1e3), algorithmic_bytes=ab, achieved_gbs=gbs,
+                frac_of_peak=gbs / peak)
 
 
 def cpu_baseline(w, steps, threads, sample_note):
@@ -263,6 +285,7 @@ def main():
                     "hotspots": w["hot"], "reach_m": w["reach"], "min_meet_steps": w["min_meet"],
                     "leaf_capacity": w["grid_capacity"], "grid_amplify": w["amplify"],
                     "meeting_buckets": make_cfg(w).resolved().num_meeting_buckets,
+                    "memtable": f"on, flush past {w['kv_restriction']} directed keys, 100 CTFs",
                     "l2": "inputs and table larger than L2; no flush", "parallelism": f"replicas x{ws}"}
 
     if args.impl == "reference":
@@ -291,7 +314,7 @@ def main():
     s_last = r["stats"][-1]
     peak, peak_kind = measured_peaks()
     B = make_cfg(w).resolved().num_meeting_buckets
-    phase_names = ["partition", "border", "refine", "insert", "sweep", "schema"]
+    phase_names = ["partition", "border", "refine", "insert", "sweep", "schema", "copy_in", "memtable"]
     phase_ms = {nm: sum(s.phase_ms[i] for s in r["stats"]) / K for i, nm in enumerate(phase_names)}
     kb = {k: sum(kernel_bytes(s, N, B)[k] for s in r["stats"]) / K for k in ("partition", "refine", "sweep")}
     dom = max(("refine", "sweep", "partition"), key=lambda k: phase_ms[k])
@@ -313,6 +336,7 @@ def main():
                      "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
                      "algorithmic_bytes": kb[dom], "launch_ms": phase_ms[dom]},
         "phase_ms": phase_ms,
+        "flush": flush_line(r["flush"], peak),
         "per_step": {"pair_tests": s_last.pair_tests, "exact_tests": s_last.exact_tests, "hits": s_last.hits,
                      "new_candidates": s_last.new_candidates, "live_meetings": s_last.taken_buckets,
                      "emitted": s_last.emitted, "border_units": s_last.border_units, "leaves": s_last.leaves,

@@ -246,12 +246,26 @@ __global__ void k_lsm_gather(LsmDev L, unsigned long long K, const uint32_t *per
   }
 }
 
+constexpr uint32_t LIM_PARTS = 32;  // blocks per CTF in k_lsm_limits
+
+__global__ void k_lsm_limits_init(LsmDev L) {
+  uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= L.F) return;
+  L.lim_box[c] = make_float4(100000.0f, 100000.0f, -100000.0f, -100000.0f);
+  L.lim_time[c] = make_uint2(1u << 30, 0u);
+}
+
 // cuda_get_limit (cuda/geometry.cu:820-891): per CTF the box of its key
 // boxes and the range of its start times, over its key range of the sorted
 // keys (the range can reach into the oversize keys, as in the reference).
+// LIM_PARTS blocks share a CTF; min and max are exact, so combining their
+// results with atomics gives the reference's values in any order.
 __global__ void k_lsm_limits(LsmDev L, unsigned long long K) {
   uint32_t c = blockIdx.x;
-  unsigned long long a = min(L.ctf_first[c], K), b = min(L.ctf_first[c + 1], K);
+  unsigned long long a0 = min(L.ctf_first[c], K), b0 = min(L.ctf_first[c + 1], K);
+  unsigned long long a = a0 + (b0 - a0) * blockIdx.y / LIM_PARTS;
+  unsigned long long b = a0 + (b0 - a0) * (blockIdx.y + 1) / LIM_PARTS;
+  if (a >= b) return;
   float lo0 = 100000.0f, lo1 = 100000.0f, hi0 = -100000.0f, hi1 = -100000.0f;
   uint32_t smin = 1u << 30, smax = 0;
   for (unsigned long long k = a + threadIdx.x; k < b; k += blockDim.x) {
@@ -293,8 +307,12 @@ __global__ void k_lsm_limits(LsmDev L, unsigned long long K) {
       t.x = min(t.x, s_t[i].x);
       t.y = max(t.y, s_t[i].y);
     }
-    L.lim_box[c] = r;
-    L.lim_time[c] = t;
+    atomic_min_f(&L.lim_box[c].x, r.x);
+    atomic_min_f(&L.lim_box[c].y, r.y);
+    atomic_max_f(&L.lim_box[c].z, r.z);
+    atomic_max_f(&L.lim_box[c].w, r.w);
+    atomicMin(&L.lim_time[c].x, t.x);
+    atomicMax(&L.lim_time[c].y, t.y);
   }
 }
 
@@ -556,7 +574,8 @@ stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState
   const unsigned long long slim = K - over_keys;
   const unsigned long long total = std::min<unsigned long long>(first[F], K);
   cudaMemcpyAsync(L.ctf_first, first.data(), (F + 1) * sizeof(unsigned long long), cudaMemcpyHostToDevice, s);
-  STC_KL k_lsm_limits<<<F, 256, 0, s>>>(L, K);
+  STC_KL k_lsm_limits_init<<<nblk(F), 256, 0, s>>>(L);
+  STC_KL k_lsm_limits<<<dim3(F, LIM_PARTS), 256, 0, s>>>(L, K);
   if (K > slim) STC_KL k_lsm_oversize<<<GRID, 256, 0, s>>>(L, slim, K);
   std::vector<float4> lb(F);
   std::vector<uint2> lt(F);

@@ -103,82 +103,135 @@ void step_insert(PipeDev &p, uint32_t t, cudaStream_t s) {
 }
 
 // Sweep (tracing/meeting.cpp:32-76, cuda/geometry.cu:595-736).
-__global__ void __launch_bounds__(256) k_sweep(PipeDev p, uint32_t t) {
+
+// Loads slot i streaming: the table passes through once, so evict-first
+// loads and stores leave L2 to the per-object positions read for new
+// meetings.
+__device__ __forceinline__ Slot load_slot_stream(const Slot *slots, unsigned long long i) {
+  ulonglong2 a = __ldcs((const ulonglong2 *)&slots[i]);
+  float4 b = __ldcs((const float4 *)&slots[i].lo_x);
+  Slot s;
+  s.key = a.x;
+  s.start = (uint32_t)a.y;
+  s.end = (uint32_t)(a.y >> 32);
+  s.lo_x = b.x; s.lo_y = b.y; s.hi_x = b.z; s.hi_y = b.w;
+  return s;
+}
+
+// One slot: finalise a meeting claimed this step, keep an extended one, or
+// clear an ended one; returns whether the ended meeting is emitted.
+__device__ __forceinline__ bool sweep_slot(const PipeDev &p, uint32_t t, unsigned long long i, const Slot &s,
+                                           unsigned long long &active, unsigned long long &fresh) {
+  if (s.key == STC_EMPTY_KEY) return false;
+  if (s.key & STC_CLAIM_BIT) {
+    // new meeting of this step (cuda/geometry.cu:480-489): start = end = t,
+    // MBR = init, then both objects' positions
+    Slot nm;
+    nm.key = s.key & ~STC_CLAIM_BIT;
+    uint32_t a, b;
+    cantor_decode(nm.key, &a, &b);
+    float2 fa = p.fxy[a], fb = p.fxy[b];
+    nm.start = t;
+    nm.end = t;
+    nm.lo_x = fminf(STC_INIT_LO, fminf(fa.x, fb.x));
+    nm.lo_y = fminf(STC_INIT_LO, fminf(fa.y, fb.y));
+    nm.hi_x = fmaxf(STC_INIT_HI, fmaxf(fa.x, fb.x));
+    nm.hi_y = fmaxf(STC_INIT_HI, fmaxf(fa.y, fb.y));
+    p.slots[i] = nm;
+    active++;
+    fresh++;
+    return false;
+  }
+  if (s.end == t) {
+    active++;
+    return false;
+  }
+  bool emit = false;
+  if (t - s.start >= p.min_meet_time + 1) {
+    emit = !p.mbr_filter || (s.lo_x >= p.fmap_lo_x && s.hi_x <= p.fmap_hi_x && s.lo_y >= p.fmap_lo_y &&
+                             s.hi_y <= p.fmap_hi_y);
+  }
+  Slot e;
+  e.key = STC_EMPTY_KEY;
+  e.start = 0xFFFFFFFFu;
+  e.end = 0xFFFFFFFFu;
+  e.lo_x = STC_INIT_LO; e.lo_y = STC_INIT_LO; e.hi_x = STC_INIT_HI; e.hi_y = STC_INIT_HI;
+  p.slots[i] = e;
+  return emit;
+}
+
+static constexpr uint32_t SWEEP_THREADS = 256;
+static constexpr uint32_t SWEEP_WARPS = SWEEP_THREADS / 32;
+static constexpr uint32_t SWEEP_UNROLL = 2;                // slots per lane per pass
+static constexpr uint32_t WARP_TILE = 32 * SWEEP_UNROLL;   // slots per warp pass
+static constexpr uint32_t WARP_STAGE = 96;                 // staged meetings per warp
+
+// Emitted meetings are staged per warp in shared memory and moved to the
+// emit buffer with one reservation per few dozen meetings: one global
+// counter bumped by every emitting warp serialises in L2.
+__device__ __forceinline__ void flush_emits(const PipeDev &p, const stc_meeting *stage, uint32_t n) {
   const uint32_t lane = lane_id();
-  unsigned long long active = 0, fresh = 0;
-  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(&p.st->emit_count, (unsigned long long)n);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  for (uint32_t k = lane; k < n; k += 32) {
+    unsigned long long pos = base + k;
+    if (pos < p.E) {
+      const uint4 *src = (const uint4 *)&stage[k];
+      uint4 *dst = (uint4 *)&p.emit[pos];
+      dst[0] = src[0];
+      dst[1] = src[1];
+    } else {
+      stc_set_error(p.st, ERR_EMIT, (uint32_t)min(pos - p.E, 0xFFFFFFFFull));
+    }
+  }
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(SWEEP_THREADS, 6) k_sweep(PipeDev p, uint32_t t) {
+  __shared__ __align__(16) stc_meeting stage_all[SWEEP_WARPS][WARP_STAGE];
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+  stc_meeting *stage = stage_all[warp];
+  uint32_t n = 0;  // warp-uniform
+  unsigned long long active = 0, fresh = 0, emitted = 0;
   const unsigned long long B = p.B;
-  // iterate so that whole warps stay converged for the ballot
-  for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < B;
-       base += stride) {
-    unsigned long long i = base + lane;
-    bool emit = false;
-    Slot s;
-    if (i < B) {
-      // the table streams through once: evict-first loads and stores leave
-      // L2 to the per-object positions read for new meetings
-      {
-        ulonglong2 a = __ldcs((const ulonglong2 *)&p.slots[i]);
-        float4 b = __ldcs((const float4 *)&p.slots[i].lo_x);
-        s.key = a.x;
-        s.start = (uint32_t)a.y;
-        s.end = (uint32_t)(a.y >> 32);
-        s.lo_x = b.x; s.lo_y = b.y; s.hi_x = b.z; s.hi_y = b.w;
-      }
-      if (s.key != STC_EMPTY_KEY) {
-        if (s.key & STC_CLAIM_BIT) {
-          // new meeting of this step (cuda/geometry.cu:480-489): start = end = t,
-          // MBR = init, then both objects' positions
-          Slot nm;
-          nm.key = s.key & ~STC_CLAIM_BIT;
-          uint32_t a, b;
-          cantor_decode(nm.key, &a, &b);
-          float2 fa = p.fxy[a], fb = p.fxy[b];
-          nm.start = t;
-          nm.end = t;
-          nm.lo_x = fminf(STC_INIT_LO, fminf(fa.x, fb.x));
-          nm.lo_y = fminf(STC_INIT_LO, fminf(fa.y, fb.y));
-          nm.hi_x = fmaxf(STC_INIT_HI, fmaxf(fa.x, fb.x));
-          nm.hi_y = fmaxf(STC_INIT_HI, fmaxf(fa.y, fb.y));
-          p.slots[i] = nm;
-          active++;
-          fresh++;
-        } else if (s.end == t) {
-          active++;
-        } else {
-          if (t - s.start >= p.min_meet_time + 1) {
-            emit = !p.mbr_filter || (s.lo_x >= p.fmap_lo_x && s.hi_x <= p.fmap_hi_x &&
-                                     s.lo_y >= p.fmap_lo_y && s.hi_y <= p.fmap_hi_y);
-          }
-          Slot e;
-          e.key = STC_EMPTY_KEY;
-          e.start = 0xFFFFFFFFu;
-          e.end = 0xFFFFFFFFu;
-          e.lo_x = STC_INIT_LO; e.lo_y = STC_INIT_LO; e.hi_x = STC_INIT_HI; e.hi_y = STC_INIT_HI;
-          p.slots[i] = e;
-        }
-      }
+  const unsigned long long gw = (unsigned long long)blockIdx.x * SWEEP_WARPS + warp;
+  const unsigned long long nw = (unsigned long long)gridDim.x * SWEEP_WARPS;
+  for (unsigned long long bb = gw * WARP_TILE; bb < B; bb += nw * WARP_TILE) {
+    Slot sl[SWEEP_UNROLL];
+    unsigned long long idx[SWEEP_UNROLL];
+#pragma unroll
+    for (uint32_t u = 0; u < SWEEP_UNROLL; u++) {
+      idx[u] = bb + u * 32 + lane;
+      if (idx[u] < B) sl[u] = load_slot_stream(p.slots, idx[u]);
+      else sl[u].key = STC_EMPTY_KEY;
     }
-    uint32_t ball = __ballot_sync(0xffffffffu, emit);
-    if (ball) {
-      unsigned long long basepos = 0;
-      if (lane == 0) basepos = atomicAdd(&p.st->emit_count, (unsigned long long)__popc(ball));
-      basepos = __shfl_sync(0xffffffffu, basepos, 0);
+#pragma unroll
+    for (uint32_t u = 0; u < SWEEP_UNROLL; u++) {
+      bool emit = idx[u] < B && sweep_slot(p, t, idx[u], sl[u], active, fresh);
+      uint32_t ball = __ballot_sync(0xffffffffu, emit);
       if (emit) {
-        unsigned long long pos = basepos + __popc(ball & ((1u << lane) - 1u));
-        if (pos < p.E) {
-          stc_meeting m;
-          cantor_decode(s.key, &m.pid_lo, &m.pid_hi);
-          m.start = s.start;
-          m.end = s.end;
-          m.mbr[0] = s.lo_x; m.mbr[1] = s.lo_y; m.mbr[2] = s.hi_x; m.mbr[3] = s.hi_y;
-          p.emit[pos] = m;
-        } else {
-          stc_set_error(p.st, ERR_EMIT, (uint32_t)(pos - p.E));
-        }
+        stc_meeting m;
+        cantor_decode(sl[u].key, &m.pid_lo, &m.pid_hi);
+        m.start = sl[u].start;
+        m.end = sl[u].end;
+        m.mbr[0] = sl[u].lo_x; m.mbr[1] = sl[u].lo_y; m.mbr[2] = sl[u].hi_x; m.mbr[3] = sl[u].hi_y;
+        stage[n + __popc(ball & ((1u << lane) - 1u))] = m;
       }
-      if (lane == 0) atomicAdd(&p.st->step_emitted, (unsigned long long)__popc(ball));
+      n += __popc(ball);
     }
+    __syncwarp();
+    // room for the next pass (at most WARP_TILE more)
+    if (n > WARP_STAGE - WARP_TILE) {
+      flush_emits(p, stage, n);
+      emitted += n;
+      n = 0;
+    }
+  }
+  __syncwarp();
+  if (n) {
+    flush_emits(p, stage, n);
+    emitted += n;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -187,10 +240,11 @@ __global__ void __launch_bounds__(256) k_sweep(PipeDev p, uint32_t t) {
   }
   if (lane == 0 && active) atomicAdd(&p.st->taken, active);
   if (lane == 0 && fresh) atomicAdd(&p.st->fast_claims, fresh);
+  if (lane == 0 && emitted) atomicAdd(&p.st->step_emitted, emitted);
 }
 
 void step_sweep(PipeDev &p, uint32_t t, cudaStream_t s) {
-  STC_KL k_sweep<<<STC_NUM_SMS * 16, 256, 0, s>>>(p, t);
+  STC_KL k_sweep<<<STC_NUM_SMS * 6, SWEEP_THREADS, 0, s>>>(p, t);
 }
 
 }  // namespace stc
