@@ -84,6 +84,9 @@ typedef struct stc_config {
                                     start_time + min_meet_time (config.h:28, process.cpp:404) */
   double area_restriction;       /* an object whose box over all its keys has a larger area (deg^2)
                                     goes to the oversize buffer (process.cpp:408-411); 0 = 100, no cut */
+  uint32_t ctb_retain;           /* flushed blocks kept on the device for queries; the oldest is
+                                    dropped beyond this; 0 = 8 */
+  uint32_t reserved;
 } stc_config;
 
 /* Replay quadtree splits/merges on one device thread only (tests compare it
@@ -219,6 +222,55 @@ stc_status stc_get_ctb(stc_ctx *ctx, stc_ctb_info *info);
  * oversize_boxes[4 * oversize_kv_count]; oversize_bitmap[STC_BITMAP_BYTES]. */
 stc_status stc_read_ctb(stc_ctx *ctx, stc_ctf *ctfs, uint8_t *bitmaps, uint8_t *keys, uint16_t *sids,
                         uint64_t *oversize_keys, float *oversize_boxes, uint8_t *oversize_bitmap);
+
+/* ---- Queries over the flushed blocks -----------------------------------
+ *
+ * The reference's disk searches (workbench::id_search_in_CTB,
+ * CTF::search_SSTable, oversize_buffer::search_buffer, mbr_search_in_disk;
+ * tracing/workbench.cpp:413-460, 495-572, tracing/step_merge.cpp:65-110,
+ * 518-570) over the blocks this context keeps (ctb_retain), with the time
+ * window applied as the reference's time_query states (a key matches when
+ * its start < t_end and t_start < its end, util/query_context.h:95-105) and
+ * without the fixed test box of CTF::search_SSTable (step_merge.cpp:549).
+ *   object: per block, the object's sid picks the oversize buffer or one CTF,
+ *           a binary search finds its first key, the scan runs while the pid
+ *           matches (keys are directed: pid is the object queried);
+ *   box:    every key whose box intersects the query box (closed intervals,
+ *           geometry/geometry.h:128-133): CTF keys by their decoded box
+ *           (CTF::new_parse_mbr, step_merge.cpp:362-379), oversize keys by
+ *           their float box.
+ * *n receives the number of matches; the first cap are written to out.
+ * Queries read only flushed blocks, so one host thread may query while
+ * another runs stc_step on the same context; queries are serialised among
+ * themselves and run on their own high-priority stream. Their errors are
+ * reported by stc_last_error(NULL) on the calling thread. */
+typedef struct stc_contact {
+  uint32_t pid, target, start, end;
+  double mbr[4];                 /* decoded key box, or the float box of an oversize key */
+  uint32_t block;                /* stc_ctb_info.index of its block */
+  uint32_t ctf;                  /* its CTF, or ctf_count for the oversize buffer */
+} stc_contact;
+
+stc_status stc_query_object(stc_ctx *ctx, uint32_t pid, uint32_t t_start, uint32_t t_end, stc_contact *out,
+                            size_t cap, size_t *n);
+stc_status stc_query_box(stc_ctx *ctx, const double box[4], uint32_t t_start, uint32_t t_end, stc_contact *out,
+                         size_t cap, size_t *n);
+
+/* A batch of queries in one device pass (the serving path: queries that
+ * arrive while a batch runs form the next one). offsets[nq + 1]: the matches
+ * of query i are out[offsets[i] .. offsets[i + 1]) when offsets[nq] <= cap;
+ * otherwise only offsets is filled and out is left untouched. */
+#define STC_QUERY_OBJECT 0u
+#define STC_QUERY_BOX 1u
+typedef struct stc_query {
+  uint32_t kind;                 /* STC_QUERY_OBJECT or STC_QUERY_BOX */
+  uint32_t pid;                  /* object queries */
+  uint32_t t_start, t_end;
+  double box[4];                 /* box queries: low x, low y, high x, high y */
+} stc_query;
+
+stc_status stc_query_batch(stc_ctx *ctx, const stc_query *queries, size_t nq, stc_contact *out, size_t cap,
+                           uint64_t *offsets);
 
 /* Last error message of ctx (or, when ctx is NULL, of the last failed
  * stc_create or context-free call on this thread). Never NULL. */

@@ -81,6 +81,13 @@ def _lib():
     lib.lsm_serialize_mbr.restype = ctypes.c_uint64
     lib.lsm_pack_key.argtypes = [ctypes.c_uint64] * 5 + [ctypes.c_void_p, ctypes.c_void_p]
     lib.lsm_o_bitmap.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.lsm_decode_key.argtypes = [ctypes.c_void_p] * 8
+    lib.lsm_query_object_block.argtypes = [ctypes.c_void_p] * 6 + [ctypes.c_uint32] * 3 + [
+        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t]
+    lib.lsm_query_object_block.restype = ctypes.c_size_t
+    lib.lsm_query_box_block.argtypes = [ctypes.c_void_p] * 6 + [ctypes.c_uint32] * 2 + [
+        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t]
+    lib.lsm_query_box_block.restype = ctypes.c_size_t
     return lib
 
 
@@ -274,3 +281,39 @@ def run_reference_driver(trace: np.ndarray, mbr, cfg, workdir: str):
             str(cfg.refine_size), "1", "1" if cfg.dynamic_schema else "0"]
     subprocess.run(args, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     return read_reference_output(op)
+
+
+def _block_args(info, bufs):
+    return (ctypes.byref(info), bufs["ctfs"].ctypes.data, bufs["keys"].ctypes.data)
+
+
+def query_blocks(blocks, queries) -> list:
+    """The oracle's answers (lsm_query_*_block) over a list of (info, buffers)
+    blocks as stc_read_ctb lays them out; one CONTACT_DTYPE array per query."""
+    from stcdb_gb300.pipeline import CONTACT_DTYPE, QUERY_BOX
+    out = []
+    for q in queries:
+        res = []
+        for info, b in blocks:
+            keys = b["keys"] if len(b["keys"]) else np.zeros(1, np.uint8)
+            okeys = b["oversize_keys"] if len(b["oversize_keys"]) else np.zeros(2, np.uint64)
+            oboxes = b["oversize_boxes"] if len(b["oversize_boxes"]) else np.zeros(4, np.float32)
+            cap = 1 << 12
+            while True:
+                buf = np.zeros(cap, CONTACT_DTYPE)
+                if int(q["kind"]) == QUERY_BOX:
+                    qb = np.ascontiguousarray(q["box"], np.float64)
+                    n = lib().lsm_query_box_block(ctypes.byref(info), b["ctfs"].ctypes.data, keys.ctypes.data,
+                                                  okeys.ctypes.data, oboxes.ctypes.data, qb.ctypes.data,
+                                                  int(q["t_start"]), int(q["t_end"]), buf.ctypes.data, cap, 0)
+                else:
+                    n = lib().lsm_query_object_block(ctypes.byref(info), b["ctfs"].ctypes.data, keys.ctypes.data,
+                                                     b["sids"].ctypes.data, okeys.ctypes.data, oboxes.ctypes.data,
+                                                     int(q["pid"]), int(q["t_start"]), int(q["t_end"]),
+                                                     buf.ctypes.data, cap, 0)
+                if n <= cap:
+                    res.append(buf[:n])
+                    break
+                cap = n
+        out.append(np.concatenate(res) if res else np.zeros(0, CONTACT_DTYPE))
+    return out

@@ -7,7 +7,8 @@
 //   CTF::serial_mbr   (:290-310; the host twin of serialize_mbr,
 //                      cuda/geometry.cu:161-171),
 //   CTF::serial_key   (:284-288),
-//   oversize_buffer::write_o_buffer (:41-63).
+//   oversize_buffer::write_o_buffer (:41-63),
+//   CTF::parse_key, CTF::new_parse_mbr, CTF::ctf_get_key_oid (:329-379).
 //
 // Usage: ref_ctf <in.bin> <out.bin>
 // in.bin:  f64 map[4], u32 num_objects, u32 max_meet_time, u32 n_cases,
@@ -16,7 +17,8 @@
 //          u32 end_time_min, u32 n_boxes, n_boxes x { f32 box[4], u32 duration, u32 end }
 // out.bin: n_cases x { u16 key_bit, id_bit, duration_bit, end_bit, low_x_bit,
 //                      low_y_bit, edge_bit, mbr_bit, x_grid, y_grid; u32 bitmap_size;
-//                      u64 value_mbr; u64 key_lo, key_hi },
+//                      u64 value_mbr; u64 key_lo, key_hi; u32 oid, target, duration,
+//                      end; u64 value_mbr; f64 box[4] (the stored key decoded) },
 //          u8 o_bitmap[8192], u32 o_start_time_min, o_start_time_max
 #include <cstdint>
 #include <cstdio>
@@ -68,6 +70,19 @@ int main(int argc, char **argv) {
     fwrite(&value_mbr, 8, 1, o);
     fwrite(&klo, 8, 1, o);
     fwrite(&khi, 8, 1, o);
+    // decode the key as stored: its low key_bit/8 bytes (CTF::parse_key,
+    // CTF::new_parse_mbr, CTF::ctf_get_key_oid)
+    __uint128_t stored = 0;
+    memcpy(&stored, &key, ctf.key_bit / 8);
+    key_info ki;
+    uint64_t vm2 = 0;
+    ctf.parse_key(stored, ki, vm2);
+    box db = ctf.new_parse_mbr(vm2);
+    uint32_t dec[4] = {ctf.ctf_get_key_oid(stored), ki.target, ki.duration, ki.end};
+    fwrite(dec, 4, 4, o);
+    fwrite(&vm2, 8, 1, o);
+    double dbx[4] = {db.low[0], db.low[1], db.high[0], db.high[1]};
+    fwrite(dbx, 8, 4, o);
   }
   uint32_t end_time_min = 0, nb = 0;
   if (!rd(f, &end_time_min) || !rd(f, &nb)) return 2;

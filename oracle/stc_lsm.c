@@ -478,3 +478,173 @@ int lsm_read_ctb(const lsm_oracle *o, stc_ctf *ctfs, uint8_t *bitmaps, uint8_t *
   if (obitmap) memcpy(obitmap, o->obitmap, sizeof(o->obitmap));
   return 0;
 }
+
+/* ---- queries over a block ------------------------------------------------
+ * The reference's lookups (workbench::id_search_in_CTB, CTF::binary_search,
+ * CTF::search_SSTable, oversize_buffer::search_buffer, mbr_search_in_disk;
+ * tracing/workbench.cpp:413-460, 495-572, tracing/step_merge.cpp:65-110,
+ * 518-570) with the time window applied as its time_query states
+ * (util/query_context.h:95-105: key start < t_end and t_start < key end)
+ * and without the fixed test box of search_SSTable (step_merge.cpp:549). */
+
+static u128 load_key(const uint8_t *p, uint32_t kb) {
+  u128 k = 0;
+  for (uint32_t i = 0; i < kb; i++) k |= (u128)p[i] << (8 * i);
+  return k;
+}
+
+static uint64_t mask64(uint32_t bits) { return bits >= 64 ? ~0ull : (1ull << bits) - 1; }
+
+/* CTF::ctf_get_key_oid, CTF::parse_key and CTF::new_parse_mbr
+ * (tracing/step_merge.cpp:329-379): fields masked to their widths, the box
+ * decoded in double from the CTF box. */
+void lsm_decode_key(const uint8_t *key, const stc_ctf *c, uint32_t *oid, uint32_t *target, uint32_t *duration,
+                    uint32_t *end, uint64_t *value_mbr, double box[4]) {
+  u128 k = load_key(key, c->key_bit / 8u);
+  *oid = (uint32_t)((k >> (c->id_bit + c->duration_bit + c->end_bit + c->mbr_bit)) & mask64(c->id_bit));
+  uint64_t vm = (uint64_t)(k & (u128)mask64(c->mbr_bit));
+  k >>= c->mbr_bit;
+  *end = (uint32_t)(k & mask64(c->end_bit));
+  k >>= c->end_bit;
+  *duration = (uint32_t)(k & mask64(c->duration_bit));
+  k >>= c->duration_bit;
+  *target = (uint32_t)(k & mask64(c->id_bit));
+  *value_mbr = vm;
+  uint64_t me = mask64(c->edge_bit), my = mask64(c->low_y_bit), mx = mask64(c->low_x_bit);
+  uint64_t y = vm & me;
+  vm >>= c->edge_bit;
+  uint64_t x = vm & me;
+  vm >>= c->edge_bit;
+  uint64_t low1 = vm & my;
+  vm >>= c->low_y_bit;
+  uint64_t low0 = vm & mx;
+  float wx = c->mbr[2] - c->mbr[0], wy = c->mbr[3] - c->mbr[1];
+  float longer_edge = wx > wy ? wx : wy;
+  box[0] = c->mbr[0] + (double)low0 / mx * wx;
+  box[1] = c->mbr[1] + (double)low1 / my * wy;
+  box[2] = box[0] + (double)x / me * longer_edge;
+  box[3] = box[1] + (double)y / me * longer_edge;
+}
+
+static int time_ok(uint32_t start, uint32_t end, uint32_t t1, uint32_t t2) { return start < t2 && t1 < end; }
+
+static int box_hits(const double a[4], const double q[4]) {  /* box::intersect (geometry/geometry.h:128-133) */
+  return !(q[0] > a[2] || q[2] < a[0] || q[1] > a[3] || q[3] < a[1]);
+}
+
+static size_t put(stc_contact *out, size_t cap, size_t n, uint32_t pid, uint32_t target, uint32_t start,
+                  uint32_t end, const double box[4], uint32_t block, uint32_t ctf) {
+  if (n < cap) {
+    stc_contact *r = &out[n];
+    r->pid = pid; r->target = target; r->start = start; r->end = end;
+    memcpy(r->mbr, box, sizeof(r->mbr));
+    r->block = block;
+    r->ctf = ctf;
+  }
+  return n + 1;
+}
+
+static void oversize_fields(const uint64_t *ok, uint32_t *pid, uint32_t *target, uint32_t *dur, uint32_t *end) {
+  *pid = (uint32_t)(ok[1] >> 26) & ((1u << 26) - 1);
+  *target = (uint32_t)ok[1] & ((1u << 26) - 1);
+  *dur = (uint32_t)(ok[0] >> 32);
+  *end = (uint32_t)ok[0];
+}
+
+/* Object query on one block: its sid picks the oversize buffer or one CTF,
+ * binary search for the first key of pid, scan while the pid matches.
+ * Returns the number of matches (only the first cap are written). */
+size_t lsm_query_object_block(const stc_ctb_info *in, const stc_ctf *ctfs, const uint8_t *keys,
+                              const uint16_t *sids, const uint64_t *okeys, const float *oboxes, uint32_t pid,
+                              uint32_t t1, uint32_t t2, stc_contact *out, size_t cap, size_t n) {
+  uint16_t sid = sids[pid];
+  if (sid == 0) return n;
+  if (sid == 1) {
+    int64_t low = 0, high = (int64_t)in->oversize_kv_count - 1, find = -1;
+    while (low <= high) {
+      int64_t mid = (low + high) / 2;
+      uint32_t p, tg, d, e;
+      oversize_fields(okeys + 2 * mid, &p, &tg, &d, &e);
+      if (p == pid) { find = mid; high = mid - 1; }
+      else if (p > pid) high = mid - 1;
+      else low = mid + 1;
+    }
+    if (find < 0) return n;
+    for (uint64_t i = (uint64_t)find; i < in->oversize_kv_count; i++) {
+      uint32_t p, tg, d, e;
+      oversize_fields(okeys + 2 * i, &p, &tg, &d, &e);
+      if (p != pid) break;
+      uint32_t end_abs = e + in->o_end_time_min, start = end_abs - d;
+      if (!time_ok(start, end_abs, t1, t2)) continue;
+      double b[4] = {oboxes[4 * i], oboxes[4 * i + 1], oboxes[4 * i + 2], oboxes[4 * i + 3]};
+      n = put(out, cap, n, pid, tg, start, end_abs, b, in->index, in->ctf_count);
+    }
+    return n;
+  }
+  uint32_t c = (uint32_t)sid - 2;
+  if (c >= in->ctf_count) return n;
+  const stc_ctf *t = &ctfs[c];
+  const uint32_t kb = t->key_bit / 8u;
+  const uint8_t *base = keys + t->key_offset;
+  /* CTF::binary_search (tracing/step_merge.cpp:496-521): unsigned bounds */
+  uint32_t low = 0, high = t->kv_count - 1;
+  int64_t find = -1;
+  while (low <= high) {
+    uint64_t mid = low + (uint64_t)(high - low) / 2;
+    if (mid >= t->kv_count) break;
+    uint32_t oid, tg, d, e;
+    uint64_t vm;
+    double b[4];
+    lsm_decode_key(base + mid * kb, t, &oid, &tg, &d, &e, &vm, b);
+    if (oid == pid) {
+      find = (int64_t)mid;
+      if (mid == 0) break;
+      high = (uint32_t)mid - 1;
+    } else if (oid < pid) {
+      low = (uint32_t)mid + 1;
+    } else {
+      if (mid == 0) break;
+      high = (uint32_t)mid - 1;
+    }
+  }
+  if (find < 0) return n;
+  for (uint64_t i = (uint64_t)find; i < t->kv_count; i++) {
+    uint32_t oid, tg, d, e;
+    uint64_t vm;
+    double b[4];
+    lsm_decode_key(base + i * kb, t, &oid, &tg, &d, &e, &vm, b);
+    if (oid != pid) break;
+    uint32_t end_abs = e + t->end_time_min, start = end_abs - d;
+    if (!time_ok(start, end_abs, t1, t2)) continue;
+    n = put(out, cap, n, pid, tg, start, end_abs, b, in->index, c);
+  }
+  return n;
+}
+
+/* Box query on one block: every CTF key whose decoded box intersects q and
+ * every oversize key whose box does, inside the time window. The oracle
+ * scans every key; the GPU prunes CTFs by box, times and bitmap first. */
+size_t lsm_query_box_block(const stc_ctb_info *in, const stc_ctf *ctfs, const uint8_t *keys, const uint64_t *okeys,
+                           const float *oboxes, const double q[4], uint32_t t1, uint32_t t2, stc_contact *out,
+                           size_t cap, size_t n) {
+  for (uint32_t c = 0; c < in->ctf_count; c++) {
+    const stc_ctf *t = &ctfs[c];
+    const uint32_t kb = t->key_bit / 8u;
+    for (uint64_t i = 0; i < t->kv_count; i++) {
+      uint32_t oid, tg, d, e;
+      uint64_t vm;
+      double b[4];
+      lsm_decode_key(keys + t->key_offset + i * kb, t, &oid, &tg, &d, &e, &vm, b);
+      uint32_t end_abs = e + t->end_time_min, start = end_abs - d;
+      if (time_ok(start, end_abs, t1, t2) && box_hits(b, q)) n = put(out, cap, n, oid, tg, start, end_abs, b, in->index, c);
+    }
+  }
+  for (uint64_t i = 0; i < in->oversize_kv_count; i++) {
+    uint32_t p, tg, d, e;
+    oversize_fields(okeys + 2 * i, &p, &tg, &d, &e);
+    uint32_t end_abs = e + in->o_end_time_min, start = end_abs - d;
+    double b[4] = {oboxes[4 * i], oboxes[4 * i + 1], oboxes[4 * i + 2], oboxes[4 * i + 3]};
+    if (time_ok(start, end_abs, t1, t2) && box_hits(b, q)) n = put(out, cap, n, p, tg, start, end_abs, b, in->index, in->ctf_count);
+  }
+  return n;
+}

@@ -71,6 +71,16 @@ uint64_t lsm_serialize_mbr(const float b[4], const stc_ctf *c);
 void lsm_pack_key(uint64_t pid_field, uint64_t target, uint64_t duration, uint64_t end, uint64_t value_mbr,
                   const stc_ctf *c, uint8_t *out);
 void lsm_o_bitmap(const float b[4], const double map[4], uint8_t *bitmap);
+void lsm_decode_key(const uint8_t *key, const stc_ctf *c, uint32_t *oid, uint32_t *target, uint32_t *duration,
+                    uint32_t *end, uint64_t *value_mbr, double box[4]);
+/* queries on one block read out as stc_read_ctb lays it out; n: matches so
+ * far (results go to out[n..cap)); returns the new count */
+size_t lsm_query_object_block(const stc_ctb_info *in, const stc_ctf *ctfs, const uint8_t *keys,
+                              const uint16_t *sids, const uint64_t *okeys, const float *oboxes, uint32_t pid,
+                              uint32_t t1, uint32_t t2, stc_contact *out, size_t cap, size_t n);
+size_t lsm_query_box_block(const stc_ctb_info *in, const stc_ctf *ctfs, const uint8_t *keys, const uint64_t *okeys,
+                           const float *oboxes, const double q[4], uint32_t t1, uint32_t t2, stc_contact *out,
+                           size_t cap, size_t n);
 
 #ifdef __cplusplus
 }

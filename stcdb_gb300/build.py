@@ -33,6 +33,7 @@ CU_SOURCES = [
     "stc_sort.cu",
     "stc_util.cu",
     "stc_lsm.cu",
+    "stc_query.cu",
 ]
 
 

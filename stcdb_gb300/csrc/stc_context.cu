@@ -129,6 +129,7 @@ extern "C" void stc_config_default(stc_config *cfg, uint32_t n) {
 static void destroy_all(stc_ctx *c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  lsm_release(c->lsmh);
   for (void *v : c->allocs) cudaFree(v);
   c->allocs.clear();
   if (c->st_host) cudaFreeHost(c->st_host);
@@ -295,6 +296,15 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
          dalloc(c, &L.obitmap, STC_BITMAP_BYTES / 4) && dalloc(c, &L.kbytes, 16 * (size_t)L.cap);
     for (int i = 0; ok && i < 7; i++) ok = dalloc(c, &L.sk[i], w);
     L.st = p.st;
+    LsmHost &H = c->lsmh;
+    H.retain = k.ctb_retain ? k.ctb_retain : 8;
+    for (int i = 0; i < 4; i++) H.map[i] = mbr[i];
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (ok && cudaStreamCreateWithPriority(&H.qstream, cudaStreamNonBlocking, greatest) != cudaSuccess) {
+      c->err = "query stream creation failed";
+      ok = false;
+    }
   }
   if (!ok) {
     g_create_error = "stc_create: " + c->err;
@@ -348,6 +358,8 @@ static stc_status flush_now(stc_ctx *c, uint32_t t) {
   stc_status rs = lsm_flush(c->lsm, c->lsmh, t, c->stream, c->st_host, err);
   if (rs != STC_OK) return fail(c, rs, "stc flush: " + err);
   if (c->st_host->error) return read_state(c, "stc flush");
+  rs = lsm_store_block(c->lsm, c->lsmh, c->stream, err);
+  if (rs != STC_OK) return fail(c, rs, "stc flush: " + err);
   cudaEventRecord(c->ev[PH_FLUSH1], c->stream);
   cudaError_t e = cudaEventSynchronize(c->ev[PH_FLUSH1]);
   if (e != cudaSuccess) return cuda_fail(c, e, "stc flush");
@@ -539,4 +551,75 @@ extern "C" stc_status stc_read_ctb(stc_ctx *c, stc_ctf *ctfs, uint8_t *bitmaps, 
     oversize_keys[2 * i + 1] = ((uint64_t)orec[i].x << 26) | orec[i].y;
   }
   return STC_OK;
+}
+
+static stc_status query_checks(stc_ctx *c, const char *who) {
+  if (!c) {
+    g_create_error = std::string(who) + ": null context";
+    return STC_ERR_INVALID_ARG;
+  }
+  if (!c->lsm_on) {
+    g_create_error = std::string(who) + ": the memtable is off (kv_restriction 0), nothing to query";
+    return STC_ERR_INVALID_ARG;
+  }
+  cudaSetDevice(c->device);
+  return STC_OK;
+}
+
+extern "C" stc_status stc_query_batch(stc_ctx *c, const stc_query *queries, size_t nq, stc_contact *out,
+                                      size_t cap, uint64_t *offsets) {
+  stc_status st = query_checks(c, "stc_query_batch");
+  if (st != STC_OK) return st;
+  if ((!queries && nq) || !offsets || (!out && cap)) {
+    g_create_error = "stc_query_batch: null argument";
+    return STC_ERR_INVALID_ARG;
+  }
+  for (size_t i = 0; i < nq; i++) {
+    const stc_query &q = queries[i];
+    if ((q.kind != STC_QUERY_OBJECT && q.kind != STC_QUERY_BOX) ||
+        (q.kind == STC_QUERY_OBJECT && q.pid >= c->p.N)) {
+      g_create_error = "stc_query_batch: query " + std::to_string(i) + " has a bad kind or object id";
+      return STC_ERR_INVALID_ARG;
+    }
+  }
+  std::string err;
+  st = lsm_query(c->lsmh, queries, nq, out, cap, offsets, err);
+  if (st != STC_OK) g_create_error = "stc_query_batch: " + err;
+  return st;
+}
+
+static stc_status query_one(stc_ctx *c, const stc_query &q, stc_contact *out, size_t cap, size_t *n,
+                            const char *who) {
+  if (!n || (!out && cap)) {
+    g_create_error = std::string(who) + ": null argument";
+    return STC_ERR_INVALID_ARG;
+  }
+  uint64_t off[2] = {0, 0};
+  stc_status st = stc_query_batch(c, &q, 1, out, cap, off);
+  *n = (size_t)off[1];
+  return st;
+}
+
+extern "C" stc_status stc_query_object(stc_ctx *c, uint32_t pid, uint32_t t_start, uint32_t t_end,
+                                       stc_contact *out, size_t cap, size_t *n) {
+  stc_query q{};
+  q.kind = STC_QUERY_OBJECT;
+  q.pid = pid;
+  q.t_start = t_start;
+  q.t_end = t_end;
+  return query_one(c, q, out, cap, n, "stc_query_object");
+}
+
+extern "C" stc_status stc_query_box(stc_ctx *c, const double box[4], uint32_t t_start, uint32_t t_end,
+                                    stc_contact *out, size_t cap, size_t *n) {
+  if (!box) {
+    g_create_error = "stc_query_box: null box";
+    return STC_ERR_INVALID_ARG;
+  }
+  stc_query q{};
+  q.kind = STC_QUERY_BOX;
+  q.t_start = t_start;
+  q.t_end = t_end;
+  for (int i = 0; i < 4; i++) q.box[i] = box[i];
+  return query_one(c, q, out, cap, n, "stc_query_box");
 }

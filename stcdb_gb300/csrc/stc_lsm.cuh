@@ -13,6 +13,9 @@
 //              end), then the oversize keys sorted by (pid, target, ...);
 //              kbytes: packed CTF keys; bitmaps; ctfs; bsid.
 #pragma once
+#include <deque>
+#include <mutex>
+#include <shared_mutex>
 #include <string>
 #include <vector>
 
@@ -50,11 +53,56 @@ struct LsmDev {
   uint8_t *kbytes;                 // packed CTF keys (16 * cap bytes)
 };
 
+// Device copy of one flushed block, kept for queries.
+struct CtbBlock {
+  stc_ctb_info info{};
+  std::vector<stc_ctf> ctfs;       // host copy
+  uint8_t *keys = nullptr;         // packed CTF keys (+32 bytes of padding for word loads)
+  stc_ctf *d_ctfs = nullptr;
+  uint32_t *bitmaps = nullptr;     // [F * 2048]
+  uint16_t *sids = nullptr;        // [N]
+  uint4 *orec = nullptr;           // oversize keys (pid, target, duration, end offset), sorted
+  float4 *obox = nullptr;
+  uint32_t *obitmap = nullptr;     // [2048]
+};
+
+// A retained block as the query kernels see it.
+struct QBlock {
+  const uint8_t *keys;
+  const stc_ctf *ctfs;
+  const uint16_t *sids;
+  const uint4 *orec;
+  const float4 *obox;
+  const uint32_t *bitmaps;
+  const uint32_t *obitmap;
+  unsigned long long n_over;
+  uint32_t F, index, o_end_time_min, pad;
+};
+
+// One match on the device: the contact and the query it answers.
+struct QueryRec {
+  stc_contact c;
+  uint32_t q, pad;
+};
+
 struct LsmHost {
   bool has_block = false;
   uint32_t flushes = 0;
   stc_ctb_info info{};
   std::vector<stc_ctf> ctfs;
+  // retained blocks (oldest first) and the query state
+  uint32_t retain = 8;
+  std::deque<CtbBlock> blocks;
+  std::shared_mutex blocks_mu;     // exclusive while the list changes
+  std::mutex query_mu;             // one query batch at a time
+  cudaStream_t qstream = nullptr;
+  QBlock *d_qb = nullptr;          // [retain]
+  stc_query *d_q = nullptr;
+  size_t q_cap = 0;
+  QueryRec *d_out = nullptr;
+  size_t out_cap = 0;
+  unsigned long long *d_count = nullptr;
+  double map[4] = {0, 0, 0, 0};
 };
 
 // Words of sort scratch per array and radix histogram words for the flush.
@@ -70,6 +118,18 @@ void lsm_append(const PipeDev &p, const LsmDev &L, cudaStream_t s);
 // Flushes the memtable at step t into a block. st_host is a pinned DevState
 // mirror used for read-backs. On failure returns a status and sets err.
 stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState *st_host, std::string &err);
+
+// Copies the block just flushed into its own allocations and appends it to
+// the retained blocks, dropping the oldest beyond H.retain.
+stc_status lsm_store_block(const LsmDev &L, LsmHost &H, cudaStream_t s, std::string &err);
+
+// Frees the retained blocks and the query buffers.
+void lsm_release(LsmHost &H);
+
+// Runs a batch of queries over the retained blocks on H.qstream (see
+// stc_query_batch in include/stc.h).
+stc_status lsm_query(LsmHost &H, const stc_query *q, size_t nq, stc_contact *out, size_t cap, uint64_t *offsets,
+                     std::string &err);
 
 // Host restatement of CTF::get_ctf_bits (tracing/step_merge.cpp:140-186);
 // returns false when the key would exceed 64 box bits or 128 key bits.

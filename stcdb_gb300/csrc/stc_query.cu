@@ -1,0 +1,441 @@
+// Queries over the retained flushed blocks (the reference's disk searches,
+// with the time window of its time_query; semantics in include/stc.h).
+//
+// A batch of queries is one launch per query kind: object queries get one
+// CTA per (block, query): the object's sid picks the oversize buffer or a
+// CTF, one thread runs the reference's binary search for the first key of
+// the pid and the CTA scans on while the pid matches. Box queries get
+// QBOX_PARTS CTAs per (CTF or oversize buffer, block, query): each first
+// prunes by the CTF box and bitmap (widened so that no key whose decoded box
+// meets the query is lost), then scans its share of the keys. Matches are
+// appended to one device buffer tagged with their query; the host groups
+// them by query.
+#include <algorithm>
+#include <cstring>
+
+#include "stc_lsm.cuh"
+
+namespace stc {
+
+namespace {
+
+constexpr uint32_t QOBJ_THREADS = 128;
+constexpr uint32_t QBOX_THREADS = 128;
+constexpr uint32_t QBOX_PARTS = 8;
+
+struct Key {
+  uint32_t oid, target, duration, end;
+  double box[4];
+};
+
+__device__ __forceinline__ unsigned long long mask64(uint32_t bits) {
+  return bits >= 64 ? ~0ull : (1ull << bits) - 1;
+}
+
+// The low key_bit/8 bytes at p, little-endian, from three aligned words (the
+// key buffers carry 32 bytes of padding).
+__device__ __forceinline__ unsigned __int128 load_key(const uint8_t *p, uint32_t kb) {
+  uintptr_t a = (uintptr_t)p;
+  const unsigned long long *w = (const unsigned long long *)(a & ~(uintptr_t)7);
+  uint32_t sh = (uint32_t)(a & 7) * 8;
+  unsigned __int128 lo = ((unsigned __int128)__ldg(w + 1) << 64) | __ldg(w);
+  unsigned __int128 k = lo >> sh;
+  if (sh) k |= (unsigned __int128)__ldg(w + 2) << (128 - sh);
+  if (kb < 16) k &= (((unsigned __int128)1) << (8 * kb)) - 1;
+  return k;
+}
+
+// CTF::ctf_get_key_oid, CTF::parse_key, CTF::new_parse_mbr
+// (tracing/step_merge.cpp:329-379), the box in double from the CTF box.
+__device__ __forceinline__ uint32_t key_oid(unsigned __int128 k, const stc_ctf &c) {
+  return (uint32_t)((k >> (c.id_bit + c.duration_bit + c.end_bit + c.mbr_bit)) & mask64(c.id_bit));
+}
+
+__device__ void decode_key(unsigned __int128 k, const stc_ctf &c, Key &o) {
+  o.oid = key_oid(k, c);
+  unsigned long long vm = (unsigned long long)(k & (unsigned __int128)mask64(c.mbr_bit));
+  k >>= c.mbr_bit;
+  o.end = (uint32_t)(k & mask64(c.end_bit));
+  k >>= c.end_bit;
+  o.duration = (uint32_t)(k & mask64(c.duration_bit));
+  k >>= c.duration_bit;
+  o.target = (uint32_t)(k & mask64(c.id_bit));
+  unsigned long long me = mask64(c.edge_bit), my = mask64(c.low_y_bit), mx = mask64(c.low_x_bit);
+  unsigned long long y = vm & me;
+  vm >>= c.edge_bit;
+  unsigned long long x = vm & me;
+  vm >>= c.edge_bit;
+  unsigned long long low1 = vm & my;
+  vm >>= c.low_y_bit;
+  unsigned long long low0 = vm & mx;
+  float wx = __fsub_rn(c.mbr[2], c.mbr[0]), wy = __fsub_rn(c.mbr[3], c.mbr[1]);
+  double le = (double)fmaxf(wx, wy);
+  o.box[0] = __dadd_rn((double)c.mbr[0], __dmul_rn(__ddiv_rn(__ull2double_rn(low0), __ull2double_rn(mx)), (double)wx));
+  o.box[1] = __dadd_rn((double)c.mbr[1], __dmul_rn(__ddiv_rn(__ull2double_rn(low1), __ull2double_rn(my)), (double)wy));
+  o.box[2] = __dadd_rn(o.box[0], __dmul_rn(__ddiv_rn(__ull2double_rn(x), __ull2double_rn(me)), le));
+  o.box[3] = __dadd_rn(o.box[1], __dmul_rn(__ddiv_rn(__ull2double_rn(y), __ull2double_rn(me)), le));
+}
+
+__device__ __forceinline__ bool time_ok(uint32_t start, uint32_t end, uint32_t t1, uint32_t t2) {
+  return start < t2 && t1 < end;  // util/query_context.h:100-103
+}
+
+__device__ __forceinline__ bool box_hits(const double *a, const double *q) {  // geometry/geometry.h:128-133
+  return !(q[0] > a[2] || q[2] < a[0] || q[1] > a[3] || q[3] < a[1]);
+}
+
+__device__ __forceinline__ void emit(QueryRec *out, unsigned long long cap, unsigned long long *count, uint32_t q,
+                                     uint32_t pid, uint32_t target, uint32_t start, uint32_t end, const double *b,
+                                     uint32_t block, uint32_t ctf) {
+  unsigned long long i = agg_inc(count);
+  if (i >= cap) return;  // counted; the host re-runs with a larger buffer
+  QueryRec r;
+  r.c.pid = pid;
+  r.c.target = target;
+  r.c.start = start;
+  r.c.end = end;
+  r.c.mbr[0] = b[0]; r.c.mbr[1] = b[1]; r.c.mbr[2] = b[2]; r.c.mbr[3] = b[3];
+  r.c.block = block;
+  r.c.ctf = ctf;
+  r.q = q;
+  r.pad = 0;
+  out[i] = r;
+}
+
+__device__ __forceinline__ void oversize_key(const QBlock &b, unsigned long long i, uint32_t &pid, uint32_t &target,
+                                             uint32_t &start, uint32_t &end) {
+  uint4 r = b.orec[i];
+  pid = r.x;
+  target = r.y;
+  end = r.w + b.o_end_time_min;
+  start = end - r.z;
+}
+
+// ---- object queries ----------------------------------------------------------
+
+__global__ void __launch_bounds__(QOBJ_THREADS) k_query_object(const QBlock *qb, const stc_query *qs,
+                                                              QueryRec *out, unsigned long long cap,
+                                                              unsigned long long *count) {
+  const QBlock &b = qb[blockIdx.x];
+  const stc_query q = qs[blockIdx.y];
+  if (q.kind != STC_QUERY_OBJECT) return;
+  __shared__ long long s_find;
+  __shared__ unsigned long long s_lim, s_bad;
+  __shared__ uint32_t s_ctf;
+  const uint32_t pid = q.pid;
+  if (threadIdx.x == 0) {
+    s_find = -1;
+    s_lim = 0;
+    s_ctf = b.F;
+    uint16_t sid = b.sids[pid];
+    if (sid == 1) {
+      // oversize_buffer::search_buffer (tracing/step_merge.cpp:65-110)
+      long long low = 0, high = (long long)b.n_over - 1;
+      while (low <= high) {
+        long long mid = (low + high) / 2;
+        uint32_t p = b.orec[mid].x;
+        if (p == pid) { s_find = mid; high = mid - 1; }
+        else if (p > pid) high = mid - 1;
+        else low = mid + 1;
+      }
+      s_lim = b.n_over;
+    } else if (sid >= 2 && (uint32_t)sid - 2 < b.F) {
+      // CTF::binary_search (tracing/step_merge.cpp:496-521)
+      const uint32_t c = sid - 2;
+      const stc_ctf &t = b.ctfs[c];
+      const uint32_t kb = t.key_bit / 8u;
+      const uint8_t *base = b.keys + t.key_offset;
+      uint32_t low = 0, high = t.kv_count - 1;
+      while (low <= high) {
+        unsigned long long mid = low + (unsigned long long)(high - low) / 2;
+        if (mid >= t.kv_count) break;
+        uint32_t oid = key_oid(load_key(base + mid * kb, kb), t);
+        if (oid == pid) {
+          s_find = (long long)mid;
+          if (mid == 0) break;
+          high = (uint32_t)mid - 1;
+        } else if (oid < pid) {
+          low = (uint32_t)mid + 1;
+        } else {
+          if (mid == 0) break;
+          high = (uint32_t)mid - 1;
+        }
+      }
+      s_lim = t.kv_count;
+      s_ctf = c;
+    }
+  }
+  __syncthreads();
+  if (s_find < 0) return;
+  const uint32_t c = s_ctf;
+  const unsigned long long lim = s_lim;
+  // scan on while the pid matches (search_SSTable, step_merge.cpp:530-568)
+  for (unsigned long long base = (unsigned long long)s_find;; base += blockDim.x) {
+    if (threadIdx.x == 0) s_bad = ~0ull;
+    __syncthreads();
+    unsigned long long i = base + threadIdx.x;
+    bool match = false;
+    uint32_t target = 0, start = 0, end = 0;
+    double box[4];
+    if (i < lim) {
+      if (c == b.F) {
+        uint32_t p;
+        oversize_key(b, i, p, target, start, end);
+        match = p == pid;
+        float4 fb = b.obox[i];
+        box[0] = fb.x; box[1] = fb.y; box[2] = fb.z; box[3] = fb.w;
+      } else {
+        const stc_ctf &t = b.ctfs[c];
+        Key k;
+        decode_key(load_key(b.keys + t.key_offset + i * (t.key_bit / 8u), t.key_bit / 8u), t, k);
+        match = k.oid == pid;
+        target = k.target;
+        end = k.end + t.end_time_min;
+        start = end - k.duration;
+        box[0] = k.box[0]; box[1] = k.box[1]; box[2] = k.box[2]; box[3] = k.box[3];
+      }
+    }
+    if (!match) atomicMin(&s_bad, i);
+    __syncthreads();
+    const unsigned long long bad = s_bad;
+    if (match && i < bad && time_ok(start, end, q.t_start, q.t_end))
+      emit(out, cap, count, blockIdx.y, pid, target, start, end, box, b.index, c);
+    if (bad != ~0ull) return;
+    __syncthreads();
+  }
+}
+
+// ---- box queries ---------------------------------------------------------------
+
+// Any set bit of a bitmap in cells [i0, i1] x [j0, j1] (bit = i + j * xg,
+// as written by the flush, including its wrap of i = xg into the next row).
+__device__ bool any_bit(const uint32_t *bm, int i0, int i1, int j0, int j1, uint32_t xg) {
+  int found = 0;
+  long long ni = (long long)i1 - i0 + 1, nj = (long long)j1 - j0 + 1;
+  if (ni > 0 && nj > 0) {
+    for (long long k = threadIdx.x; k < ni * nj && !found; k += blockDim.x) {
+      long long bit = (i0 + k % ni) + (j0 + k / ni) * (long long)xg;
+      if (bit >= 0 && bit < 65536 && ((__ldg(&bm[bit >> 5]) >> (bit & 31)) & 1u)) found = 1;
+    }
+  }
+  return __syncthreads_or(found) != 0;
+}
+
+// Cell range [lo, hi] of the interval [a, b] on a grid of n cells over
+// [m0, m1], one cell of slack either side, clamped to [0, n].
+__device__ __forceinline__ void cell_range(double a, double b, double m0, double m1, uint32_t n, int &lo, int &hi) {
+  double w = m1 - m0;
+  double fa = w > 0 ? (a - m0) / w * n : 0.0, fb = w > 0 ? (b - m0) / w * n : (double)n;
+  fa = fmax(fmin(fa, (double)n + 2), -2.0);
+  fb = fmax(fmin(fb, (double)n + 2), -2.0);
+  lo = max((int)floor(fa) - 1, 0);
+  hi = min((int)floor(fb) + 1, (int)n);
+}
+
+__global__ void __launch_bounds__(QBOX_THREADS) k_query_box(const QBlock *qb, uint32_t nb, const stc_query *qs,
+                                                           double m0x, double m0y, double m1x, double m1y,
+                                                           QueryRec *out, unsigned long long cap,
+                                                           unsigned long long *count) {
+  const uint32_t bi = blockIdx.z % nb, qi = blockIdx.z / nb;
+  const QBlock &b = qb[bi];
+  const stc_query q = qs[qi];
+  const uint32_t c = blockIdx.y;
+  if (q.kind != STC_QUERY_BOX || c > b.F) return;
+  const double *qbox = q.box;
+  if (c == b.F) {
+    // oversize buffer: the map bitmap prunes, float boxes decide
+    if (b.n_over == 0) return;
+    int i0, i1, j0, j1;
+    cell_range(qbox[0], qbox[2], m0x, m1x, 256, i0, i1);
+    cell_range(qbox[1], qbox[3], m0y, m1y, 256, j0, j1);
+    if (!any_bit(b.obitmap, i0, i1, j0, j1, 256)) return;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < b.n_over;
+         i += (unsigned long long)QBOX_PARTS * blockDim.x) {
+      float4 fb = b.obox[i];
+      double box[4] = {fb.x, fb.y, fb.z, fb.w};
+      uint32_t pid, target, start, end;
+      oversize_key(b, i, pid, target, start, end);
+      if (time_ok(start, end, q.t_start, q.t_end) && box_hits(box, qbox))
+        emit(out, cap, count, qi, pid, target, start, end, box, b.index, c);
+    }
+    return;
+  }
+  const stc_ctf &t = b.ctfs[c];
+  if (t.kv_count == 0) return;
+  // A decoded box differs from the key's exact box (which set the CTF box
+  // and the bitmap) by less than one corner quantum plus one edge quantum on
+  // either side (float conversions truncate, and may round up first): widen
+  // the query by that much for the box and bitmap tests.
+  const float fwx = __fsub_rn(t.mbr[2], t.mbr[0]), fwy = __fsub_rn(t.mbr[3], t.mbr[1]);
+  const double le = (double)fmaxf(fwx, fwy), me = (double)mask64(t.edge_bit);
+  const double qx = (double)fwx / (double)mask64(t.low_x_bit) + le / me + 1e-9;
+  const double qy = (double)fwy / (double)mask64(t.low_y_bit) + le / me + 1e-9;
+  const double wide[4] = {qbox[0] - qx, qbox[1] - qy, qbox[2] + qx, qbox[3] + qy};
+  const double ctfb[4] = {t.mbr[0], t.mbr[1], t.mbr[2], t.mbr[3]};
+  if (!box_hits(ctfb, wide)) return;
+  int i0, i1, j0, j1;
+  cell_range(wide[0], wide[2], t.mbr[0], t.mbr[2], t.x_grid, i0, i1);
+  cell_range(wide[1], wide[3], t.mbr[1], t.mbr[3], t.y_grid, j0, j1);
+  if (!any_bit(b.bitmaps + (size_t)c * (STC_BITMAP_BYTES / 4), i0, i1, j0, j1, t.x_grid)) return;
+  const uint32_t kb = t.key_bit / 8u;
+  const uint8_t *base = b.keys + t.key_offset;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < t.kv_count;
+       i += (unsigned long long)QBOX_PARTS * blockDim.x) {
+    Key k;
+    decode_key(load_key(base + i * kb, kb), t, k);
+    uint32_t end = k.end + t.end_time_min, start = end - k.duration;
+    if (time_ok(start, end, q.t_start, q.t_end) && box_hits(k.box, qbox))
+      emit(out, cap, count, qi, k.oid, k.target, start, end, k.box, b.index, c);
+  }
+}
+
+template <typename T>
+cudaError_t grow(T **p, size_t *cap, size_t need) {
+  if (*cap >= need) return cudaSuccess;
+  size_t n = std::max<size_t>(need, 2 * *cap);
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  cudaError_t e = cudaMalloc(p, n * sizeof(T));
+  *cap = e == cudaSuccess ? n : 0;
+  return e;
+}
+
+}  // namespace
+
+stc_status lsm_store_block(const LsmDev &L, LsmHost &H, cudaStream_t s, std::string &err) {
+  CtbBlock B;
+  B.info = H.info;
+  B.ctfs = H.ctfs;
+  const size_t F = L.F, no = (size_t)H.info.oversize_kv_count;
+  cudaError_t e = cudaMalloc(&B.keys, H.info.key_bytes + 32);
+  if (e == cudaSuccess) e = cudaMalloc(&B.d_ctfs, F * sizeof(stc_ctf));
+  if (e == cudaSuccess) e = cudaMalloc(&B.bitmaps, F * STC_BITMAP_BYTES);
+  if (e == cudaSuccess) e = cudaMalloc(&B.sids, (size_t)L.N * sizeof(uint16_t));
+  if (e == cudaSuccess) e = cudaMalloc(&B.orec, std::max<size_t>(no, 1) * sizeof(uint4));
+  if (e == cudaSuccess) e = cudaMalloc(&B.obox, std::max<size_t>(no, 1) * sizeof(float4));
+  if (e == cudaSuccess) e = cudaMalloc(&B.obitmap, STC_BITMAP_BYTES);
+  if (e == cudaSuccess) e = cudaMemsetAsync(B.keys + H.info.key_bytes, 0, 32, s);
+  if (e == cudaSuccess && H.info.key_bytes)
+    e = cudaMemcpyAsync(B.keys, L.kbytes, H.info.key_bytes, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_ctfs, L.ctfs, F * sizeof(stc_ctf), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(B.bitmaps, L.bitmaps, F * STC_BITMAP_BYTES, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(B.sids, L.bsid, (size_t)L.N * 2, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess && no)
+    e = cudaMemcpyAsync(B.orec, L.brec + H.info.ctf_kv_count, no * sizeof(uint4), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess && no)
+    e = cudaMemcpyAsync(B.obox, L.bbox + H.info.ctf_kv_count, no * sizeof(float4), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(B.obitmap, L.obitmap, STC_BITMAP_BYTES, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    for (void *v : {(void *)B.keys, (void *)B.d_ctfs, (void *)B.bitmaps, (void *)B.sids, (void *)B.orec,
+                    (void *)B.obox, (void *)B.obitmap})
+      if (v) cudaFree(v);
+    err = std::string("keeping the flushed block for queries: ") + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? STC_ERR_CAPACITY : STC_ERR_CUDA;
+  }
+  std::unique_lock<std::shared_mutex> lock(H.blocks_mu);
+  H.blocks.push_back(std::move(B));
+  while (H.blocks.size() > H.retain) {
+    CtbBlock &o = H.blocks.front();
+    for (void *v : {(void *)o.keys, (void *)o.d_ctfs, (void *)o.bitmaps, (void *)o.sids, (void *)o.orec,
+                    (void *)o.obox, (void *)o.obitmap})
+      cudaFree(v);
+    H.blocks.pop_front();
+  }
+  return STC_OK;
+}
+
+void lsm_release(LsmHost &H) {
+  std::unique_lock<std::shared_mutex> lock(H.blocks_mu);
+  for (CtbBlock &o : H.blocks)
+    for (void *v : {(void *)o.keys, (void *)o.d_ctfs, (void *)o.bitmaps, (void *)o.sids, (void *)o.orec,
+                    (void *)o.obox, (void *)o.obitmap})
+      cudaFree(v);
+  H.blocks.clear();
+  if (H.d_qb) cudaFree(H.d_qb);
+  if (H.d_q) cudaFree(H.d_q);
+  if (H.d_out) cudaFree(H.d_out);
+  if (H.d_count) cudaFree(H.d_count);
+  if (H.qstream) cudaStreamDestroy(H.qstream);
+  H.d_qb = nullptr;
+  H.d_q = nullptr;
+  H.d_out = nullptr;
+  H.d_count = nullptr;
+  H.qstream = nullptr;
+  H.q_cap = H.out_cap = 0;
+}
+
+stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *out, size_t cap, uint64_t *offsets,
+                     std::string &err) {
+  std::lock_guard<std::mutex> qlock(H.query_mu);
+  std::shared_lock<std::shared_mutex> lock(H.blocks_mu);
+  const uint32_t nb = (uint32_t)H.blocks.size();
+  for (size_t i = 0; i <= nq; i++) offsets[i] = 0;
+  if (nq == 0 || nb == 0) return STC_OK;
+  if (nq * nb > 65535) {
+    err = "query batch too large: queries x retained blocks must be <= 65535";
+    return STC_ERR_INVALID_ARG;
+  }
+  cudaStream_t s = H.qstream;
+  cudaError_t e = cudaSuccess;
+  if (!H.d_qb) e = cudaMalloc(&H.d_qb, (size_t)std::max<uint32_t>(H.retain, 1) * sizeof(QBlock));
+  if (e == cudaSuccess && !H.d_count) e = cudaMalloc(&H.d_count, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = grow(&H.d_q, &H.q_cap, nq);
+  if (e == cudaSuccess) e = grow(&H.d_out, &H.out_cap, std::max<size_t>(1 << 16, H.out_cap));
+  if (e != cudaSuccess) {
+    err = std::string("query buffers: ") + cudaGetErrorString(e);
+    return STC_ERR_CUDA;
+  }
+  std::vector<QBlock> qb(nb);
+  uint32_t maxF = 0;
+  for (uint32_t i = 0; i < nb; i++) {
+    const CtbBlock &B = H.blocks[i];
+    qb[i] = QBlock{B.keys, B.d_ctfs, B.sids, B.orec, B.obox, B.bitmaps, B.obitmap,
+                   (unsigned long long)B.info.oversize_kv_count, B.info.ctf_count, B.info.index,
+                   B.info.o_end_time_min, 0};
+    maxF = std::max(maxF, B.info.ctf_count);
+  }
+  bool has_obj = false, has_box = false;
+  for (size_t i = 0; i < nq; i++) (qs[i].kind == STC_QUERY_BOX ? has_box : has_obj) = true;
+  e = cudaMemcpyAsync(H.d_qb, qb.data(), nb * sizeof(QBlock), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(H.d_q, qs, nq * sizeof(stc_query), cudaMemcpyHostToDevice, s);
+  unsigned long long total = 0;
+  for (int attempt = 0; attempt < 2 && e == cudaSuccess; attempt++) {
+    e = cudaMemsetAsync(H.d_count, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) break;
+    if (has_obj)
+      STC_KL k_query_object<<<dim3(nb, (unsigned)nq), QOBJ_THREADS, 0, s>>>(H.d_qb, H.d_q, H.d_out, H.out_cap,
+                                                                           H.d_count);
+    if (has_box)
+      STC_KL k_query_box<<<dim3(QBOX_PARTS, maxF + 1, (unsigned)(nq * nb)), QBOX_THREADS, 0, s>>>(
+          H.d_qb, nb, H.d_q, H.map[0], H.map[1], H.map[2], H.map[3], H.d_out, H.out_cap, H.d_count);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&total, H.d_count, sizeof(total), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess || total <= H.out_cap) break;
+    e = grow(&H.d_out, &H.out_cap, (size_t)total);  // too many matches: once more with room for all
+  }
+  if (e != cudaSuccess) {
+    err = std::string("query: ") + cudaGetErrorString(e);
+    return STC_ERR_CUDA;
+  }
+  std::vector<QueryRec> recs((size_t)total);
+  if (total) {
+    e = cudaMemcpyAsync(recs.data(), H.d_out, total * sizeof(QueryRec), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      err = std::string("query read-back: ") + cudaGetErrorString(e);
+      return STC_ERR_CUDA;
+    }
+  }
+  // group by query (counting sort)
+  for (const QueryRec &r : recs) offsets[r.q + 1]++;
+  for (size_t i = 0; i < nq; i++) offsets[i + 1] += offsets[i];
+  if (total <= cap && out) {
+    std::vector<uint64_t> pos(offsets, offsets + nq);
+    for (const QueryRec &r : recs) out[pos[r.q]++] = r.c;
+  }
+  return STC_OK;
+}
+
+}  // namespace stc

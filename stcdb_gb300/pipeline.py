@@ -52,6 +52,8 @@ class _Config(ctypes.Structure):
         ("ctf_count", ctypes.c_uint32),
         ("start_time", ctypes.c_uint32),
         ("area_restriction", ctypes.c_double),
+        ("ctb_retain", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
     ]
 
 
@@ -123,6 +125,22 @@ CTF_DTYPE = np.dtype([("mbr", "<f4", (4,)), ("kv_count", "<u4"), ("start_time_mi
 assert CTF_DTYPE.itemsize == 80
 BITMAP_BYTES = 8192  # STC_BITMAP_BYTES
 
+# stc_contact and stc_query (include/stc.h)
+CONTACT_DTYPE = np.dtype([("pid", "<u4"), ("target", "<u4"), ("start", "<u4"), ("end", "<u4"),
+                          ("mbr", "<f8", (4,)), ("block", "<u4"), ("ctf", "<u4")])
+assert CONTACT_DTYPE.itemsize == 56
+QUERY_DTYPE = np.dtype([("kind", "<u4"), ("pid", "<u4"), ("t_start", "<u4"), ("t_end", "<u4"),
+                        ("box", "<f8", (4,))])
+assert QUERY_DTYPE.itemsize == 48
+QUERY_OBJECT, QUERY_BOX = 0, 1
+
+
+def sort_contacts(c: np.ndarray) -> np.ndarray:
+    """Canonical order for comparing contact sets."""
+    c = np.ascontiguousarray(c, dtype=CONTACT_DTYPE)
+    order = np.lexsort((c["ctf"], c["block"], c["end"], c["start"], c["target"], c["pid"]))
+    return c[order]
+
 
 def ctb_buffers(info: StcCtbInfo, num_objects: int) -> dict:
     """Host arrays sized for one block, in the layout of stc_read_ctb."""
@@ -168,6 +186,8 @@ class StcConfig:
     ctf_count: int = 0        # 0 = 100
     start_time: int = 0
     area_restriction: float = 0.0  # 0 = 100 (no cut)
+    ctb_retain: int = 0       # flushed blocks kept for queries; 0 = 8
+    reserved: int = 0
 
     def resolved(self) -> "StcConfig":
         if self.num_meeting_buckets == 0:
@@ -209,6 +229,15 @@ def _lib():
         lib.stc_get_ctb.restype = ctypes.c_int
         lib.stc_read_ctb.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 7
         lib.stc_read_ctb.restype = ctypes.c_int
+        lib.stc_query_batch.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                        ctypes.c_size_t, ctypes.c_void_p]
+        lib.stc_query_batch.restype = ctypes.c_int
+        lib.stc_query_object.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                         ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+        lib.stc_query_object.restype = ctypes.c_int
+        lib.stc_query_box.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32,
+                                      ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+        lib.stc_query_box.restype = ctypes.c_int
         lib._stc_typed = True
     return lib
 
@@ -277,6 +306,31 @@ class Pipeline:
         self._check(self._lib.stc_read_ctb(self._h, *[b[k].ctypes.data for k in (
             "ctfs", "bitmaps", "keys", "sids", "oversize_keys", "oversize_boxes", "oversize_bitmap")]))
         return info, ctb_trim(info, b)
+
+    def query_batch(self, queries: np.ndarray):
+        """Runs a batch (QUERY_DTYPE array); returns a list of CONTACT_DTYPE arrays."""
+        q = np.ascontiguousarray(queries, dtype=QUERY_DTYPE)
+        offs = np.zeros(len(q) + 1, np.uint64)
+        cap = 1 << 16
+        while True:
+            out = np.zeros(cap, CONTACT_DTYPE)
+            st = self._lib.stc_query_batch(self._h, q.ctypes.data, len(q), out.ctypes.data, cap, offs.ctypes.data)
+            if st != 0:
+                raise StcError(st, self._lib.stc_last_error(None).decode())
+            if int(offs[-1]) <= cap:
+                return [out[int(offs[i]):int(offs[i + 1])] for i in range(len(q))]
+            cap = int(offs[-1])
+
+    def query_object(self, pid: int, t_start: int = 0, t_end: int = 0xFFFFFFFF) -> np.ndarray:
+        q = np.zeros(1, QUERY_DTYPE)
+        q["kind"], q["pid"], q["t_start"], q["t_end"] = QUERY_OBJECT, pid, t_start, t_end
+        return self.query_batch(q)[0]
+
+    def query_box(self, box, t_start: int = 0, t_end: int = 0xFFFFFFFF) -> np.ndarray:
+        q = np.zeros(1, QUERY_DTYPE)
+        q["kind"], q["t_start"], q["t_end"] = QUERY_BOX, t_start, t_end
+        q["box"][0] = box
+        return self.query_batch(q)[0]
 
     def close(self):
         if getattr(self, "_h", None):

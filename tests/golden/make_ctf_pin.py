@@ -3,9 +3,10 @@ the CTF encoding of a flushed block.
 
 Runs oracle/_ref/ref_ctf (oracle/ref_ctf.cpp linked with the reference's
 unmodified tracing/step_merge.cpp, built by oracle/build_ref.sh), which calls
-CTF::get_ctf_bits, CTF::serial_mbr, CTF::serial_key and
-oversize_buffer::write_o_buffer on seeded random cases, and stores inputs and
-outputs. Only this script needs the reference checkout.
+CTF::get_ctf_bits, CTF::serial_mbr, CTF::serial_key,
+oversize_buffer::write_o_buffer and, on the packed keys, CTF::parse_key,
+CTF::new_parse_mbr and CTF::ctf_get_key_oid on seeded random cases, and
+stores inputs and outputs. Only this script needs the reference checkout.
 
     python tests/golden/make_ctf_pin.py
 """
@@ -106,7 +107,8 @@ def main():
             subprocess.run([ref, ip, op], check=True)
             raw = open(op, "rb").read()
         rec = np.dtype([("bits", "<u2", (10,)), ("bitmap_size", "<u4"), ("value_mbr", "<u8"),
-                        ("key_lo", "<u8"), ("key_hi", "<u8")])
+                        ("key_lo", "<u8"), ("key_hi", "<u8"), ("dec", "<u4", (4,)), ("dec_vm", "<u8"),
+                        ("dec_box", "<f8", (4,))])
         n = CASES_PER_SET * rec.itemsize
         r = np.frombuffer(raw[:n], rec)
         tail = raw[n:]
@@ -118,6 +120,7 @@ def main():
                     p + "dur": dur, p + "end": end, p + "bits": r["bits"].copy(),
                     p + "bitmap_size": r["bitmap_size"].copy(), p + "value_mbr": r["value_mbr"].copy(),
                     p + "key_lo": r["key_lo"].copy(), p + "key_hi": r["key_hi"].copy(),
+                    p + "dec": r["dec"].copy(), p + "dec_vm": r["dec_vm"].copy(), p + "dec_box": r["dec_box"].copy(),
                     p + "oboxes": ob, p + "odur": odur, p + "oend": oend, p + "o_bitmap": obm.copy(),
                     p + "o_times": np.array([osmin, osmax], np.uint32)})
     np.savez_compressed(os.path.join(HERE, "ctf_pin.npz"), **out)

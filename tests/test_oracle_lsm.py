@@ -206,3 +206,86 @@ def test_area_restriction_moves_objects_to_oversize(built):
     assert ia.oversize_kv_count == 0
     assert ib.oversize_kv_count > ia.oversize_kv_count
     assert ib.oversize_oid_count > 0
+
+
+def test_key_decoding_matches_reference_host_code(built):
+    """lsm_decode_key = CTF::ctf_get_key_oid + parse_key + new_parse_mbr on
+    the stored key bytes (fixture made by the reference's own code)."""
+    import ctypes
+    import oracle
+    z = np.load(PIN)
+    lib = oracle.lib()
+    n = 0
+    for s in _sets(z):
+        mp = z[s + "_map"]
+        nobj, mmt, _ = (int(v) for v in z[s + "_meta"])
+        for i in range(len(z[s + "_ctf_mbr"])):
+            c = oracle.ctf_bits(z[s + "_ctf_mbr"][i], mp, nobj, mmt)
+            kb = int(c["key_bit"][0]) // 8
+            key = ((int(z[s + "_key_hi"][i]) << 64) | int(z[s + "_key_lo"][i])) & ((1 << (8 * kb)) - 1)
+            kbytes = np.frombuffer(key.to_bytes(16, "little"), np.uint8).copy()
+            f = (ctypes.c_uint32 * 4)()
+            vm = ctypes.c_uint64()
+            box = np.zeros(4, np.float64)
+            lib.lsm_decode_key(kbytes.ctypes.data, c.ctypes.data, ctypes.byref(f, 0), ctypes.byref(f, 4),
+                               ctypes.byref(f, 8), ctypes.byref(f, 12), ctypes.byref(vm), box.ctypes.data)
+            assert list(f) == [int(v) for v in z[s + "_dec"][i]], (s, i)
+            assert vm.value == int(z[s + "_dec_vm"][i]), (s, i)
+            assert box.tobytes() == z[s + "_dec_box"][i].tobytes(), (s, i)
+            n += 1
+    assert n >= 1000
+
+
+def _truth(m, pid=None, box=None, t1=0, t2=0xFFFFFFFF, etm=5000):
+    """(pid, target, start, end) of every directed key matching the query."""
+    out = set()
+    for r in m:
+        for p, q in ((int(r["pid_lo"]), int(r["pid_hi"])), (int(r["pid_hi"]), int(r["pid_lo"]))):
+            st, en = int(r["start"]), int(r["end"])
+            if not (st < t2 and t1 < en):
+                continue
+            if pid is not None and p != pid:
+                continue
+            out.add((p, q, st, en))
+    return out
+
+
+def test_oracle_queries_match_ground_truth(built):
+    """Object queries over a block without over-long meetings find exactly
+    the directed keys of the object in the window; box queries over the whole
+    map find every key; a box query's matches are those whose decoded box
+    meets the box."""
+    import oracle
+    from stcdb_gb300.pipeline import QUERY_BOX, QUERY_DTYPE, QUERY_OBJECT
+    rng = np.random.default_rng(21)
+    mp = np.array([-87.9412, 41.6437, -87.80, 41.75])
+    m = _meetings(rng, 3000, 8000, 5000, 5900, mp)
+    lo = oracle.LsmOracle(3000, 1000, 16, 100.0, 5000, mp, 1 << 20)
+    lo.append(m)
+    lo.flush(5900)
+    blocks = [lo.read()]
+    qs = np.zeros(40, QUERY_DTYPE)
+    pids = rng.choice(np.concatenate([m["pid_lo"], m["pid_hi"]]), 30)
+    for i in range(30):
+        qs[i]["kind"], qs[i]["pid"] = QUERY_OBJECT, pids[i]
+        a = int(rng.integers(4990, 5900))
+        qs[i]["t_start"], qs[i]["t_end"] = (a, a + int(rng.integers(1, 400))) if i % 3 else (0, 0xFFFFFFFF)
+    for i in range(30, 40):
+        qs[i]["kind"], qs[i]["t_start"], qs[i]["t_end"] = QUERY_BOX, 0, 0xFFFFFFFF
+        if i == 30:
+            qs[i]["box"] = mp
+        else:
+            x, y = mp[0] + rng.random() * (mp[2] - mp[0]), mp[1] + rng.random() * (mp[3] - mp[1])
+            qs[i]["box"] = (x, y, x + 0.005, y + 0.004)
+    res = oracle.query_blocks(blocks, qs)
+    for i in range(30):
+        got = {(int(r["pid"]), int(r["target"]), int(r["start"]), int(r["end"])) for r in res[i]}
+        assert got == _truth(m, pid=int(qs[i]["pid"]), t1=int(qs[i]["t_start"]), t2=int(qs[i]["t_end"])), i
+    assert len(res[30]) == 2 * len(m)
+    for i in range(31, 40):
+        b = qs[i]["box"]
+        for r in res[i]:
+            x0, y0, x1, y1 = r["mbr"]
+            assert not (b[0] > x1 or b[2] < x0 or b[1] > y1 or b[3] < y0)
+        assert set(map(tuple, res[i][["pid", "target", "end"]].tolist())) <= \
+            set(map(tuple, res[30][["pid", "target", "end"]].tolist()))
