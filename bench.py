@@ -26,6 +26,10 @@ Every step also appends its emitted meetings to the memtable (two directed
 e2e: the same metric through the public C ABI with host input: every step
   copies that step's positions from pinned host memory (stc_step) and drains
   the emitted meetings back to the host (stc_drain_meetings); wall clock.
+queries_under_ingest: K more steps (host input) while a serving thread answers
+  a Poisson query stream (default 20,000/s; 60% object, 40% box queries) over
+  the flushed block by continuous batching; queries return match counts, as
+  the reference's searches do; p50/p99 latency from arrival.
 --impl reference: the oracle's C restatement of the reference CPU path with
   all host threads (the reference's own sources are not on the GPU host).
 """
@@ -153,7 +157,7 @@ def run_gpu(args, w, rank, local):
     K, W = args.steps, args.warmup
     gen = TraceGenerator(make_trace_cfg(w, seed=1 + rank))
     mbr = gen.map_box(100.0)
-    total_steps = W + 2 * K
+    total_steps = W + 3 * K
     host = torch.empty((total_steps, N, 2), dtype=torch.float64, pin_memory=True)
     hnp = host.numpy()
     for t in range(total_steps):
@@ -198,12 +202,101 @@ def run_gpu(args, w, rank, local):
     pipe.flush()
     fs = pipe.stats()
     info = pipe.ctb_info()
-    pipe.close()
     flush = dict(keys=int(keys), ms=float(fs.flush_ms), ctf_keys=int(info.ctf_kv_count),
                  oversize_keys=int(info.oversize_kv_count), key_bytes=int(info.key_bytes),
-                 ctfs=int(info.ctf_count), steps=total_steps)
+                 ctfs=int(info.ctf_count), steps=W + 2 * K)
+    # queries under ingest: K more steps while a serving thread answers a
+    # Poisson query stream over the flushed block
+    queries = None
+    if args.query_rate > 0:
+        queries = serve_under_ingest(args, pipe, hnp, W + 2 * K, K, N, mbr)
+    pipe.close()
     return dict(stats=stats, dev_ms=dev_ms, wall_dev=wall_dev, wall_e2e=wall_e2e, e2e_stats=e2e_stats,
-                d2h=d2h, clocks=clk.summary(), flush=flush)
+                d2h=d2h, clocks=clk.summary(), flush=flush, queries=queries)
+
+
+def make_queries(rng, n, N, mbr, t_now):
+    """The query mix of the serving configuration: 60% object queries
+    (uniform object, window log-uniform 10-10,000 steps), 40% box queries
+    (side log-uniform 50 m-5 km at a uniform centre, window 10-3600 steps)."""
+    import math
+    from stcdb_gb300.pipeline import QUERY_BOX, QUERY_DTYPE, QUERY_OBJECT
+    dpm_lat = 360.0 / 40076000.0  # degrees per metre of latitude
+    lat = abs(float((mbr[1] + mbr[3]) / 2))
+    dpm_lon = 360.0 / (math.sin((90 - lat) * math.pi / 180) * 40076000.0)
+    q = np.zeros(n, QUERY_DTYPE)
+    obj = rng.random(n) < 0.6
+    q["kind"] = np.where(obj, QUERY_OBJECT, QUERY_BOX)
+    q["pid"] = rng.integers(0, N, n)
+    win = np.where(obj, 10 ** rng.uniform(1, 4, n), 10 ** rng.uniform(1, np.log10(3600), n)).astype(np.int64)
+    q["t_end"] = t_now + 1
+    q["t_start"] = np.maximum(t_now + 1 - win, 0)
+    side_m = 10 ** rng.uniform(np.log10(50), np.log10(5000), n)
+    cx = mbr[0] + rng.random(n) * (mbr[2] - mbr[0])
+    cy = mbr[1] + rng.random(n) * (mbr[3] - mbr[1])
+    hx, hy = side_m / 2 * dpm_lon, side_m / 2 * dpm_lat
+    q["box"] = np.stack([cx - hx, cy - hy, cx + hx, cy + hy], 1)
+    return q
+
+
+def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr):
+    """Continuous batching: queries arrive as a Poisson stream; whatever has
+    arrived while a batch ran forms the next batch. Latency = answer time -
+    arrival time. The main thread keeps stepping meanwhile (host input)."""
+    rng = np.random.default_rng(12345)
+    rate = float(args.query_rate)
+    lat, sizes, contacts = [], [], [0]
+    cur_t = [t0 - 1]
+    done = threading.Event()
+    errors = []
+
+    def server():
+        start = time.perf_counter()
+        next_arrival = start + rng.exponential(1.0 / rate)
+        while not done.is_set():
+            now = time.perf_counter()
+            arrivals = []
+            while next_arrival <= now:
+                arrivals.append(next_arrival)
+                next_arrival += rng.exponential(1.0 / rate)
+            if not arrivals:
+                time.sleep(min(max(next_arrival - now, 0.0), 0.0005))
+                continue
+            qs = make_queries(rng, len(arrivals), N, mbr, cur_t[0])
+            try:
+                counts = pipe.query_counts(qs)
+            except Exception as e:  # noqa: BLE001 - reported in the JSON line
+                errors.append(str(e))
+                return
+            t_done = time.perf_counter()
+            lat.extend(t_done - a for a in arrivals)
+            sizes.append(len(arrivals))
+            contacts[0] += int(counts.sum())
+
+    th = threading.Thread(target=server, daemon=True)
+    th.start()
+    step_ms = []
+    w0 = time.perf_counter()
+    for t in range(t0, t0 + steps):
+        pipe.step(hnp[t], t)
+        pipe.drain()
+        step_ms.append(pipe.stats().step_ms)
+        cur_t[0] = t
+    wall = time.perf_counter() - w0
+    done.set()
+    th.join()
+    if errors:
+        return {"error": errors[0]}
+    lat_ms = np.array(lat) * 1e3
+    return {"rate_target_per_s": rate, "answered": len(lat), "qps": len(lat) / wall,
+            "p50_ms": float(np.percentile(lat_ms, 50)) if len(lat) else None,
+            "p99_ms": float(np.percentile(lat_ms, 99)) if len(lat) else None,
+            "mean_batch": float(np.mean(sizes)) if sizes else 0.0, "batches": len(sizes),
+            "contacts_per_query": contacts[0] / max(len(lat), 1),
+            "mix": "60% object (window 10-10000 steps), 40% box (50 m-5 km, window 10-3600 steps); "
+                   "match counts, as the reference's searches return",
+            "blocks": 1, "ingest_pos_updates_per_s": N * steps / wall,
+            "ingest_device_ms_per_step": float(np.mean(step_ms))}
 
 
 def barrier(args):
@@ -270,6 +363,8 @@ def main():
     ap.add_argument("--workload", default="uniform-10M", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-steps", type=int, default=2, help="steps timed for the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--query-rate", type=float, default=20000.0,
+                    help="Poisson query arrivals per second during the serving phase (0: skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
@@ -337,6 +432,7 @@ def main():
                      "algorithmic_bytes": kb[dom], "launch_ms": phase_ms[dom]},
         "phase_ms": phase_ms,
         "flush": flush_line(r["flush"], peak),
+        "queries_under_ingest": r["queries"],
         "per_step": {"pair_tests": s_last.pair_tests, "exact_tests": s_last.exact_tests, "hits": s_last.hits,
                      "new_candidates": s_last.new_candidates, "live_meetings": s_last.taken_buckets,
                      "emitted": s_last.emitted, "border_units": s_last.border_units, "leaves": s_last.leaves,

@@ -259,18 +259,22 @@ stc_status stc_query_box(stc_ctx *ctx, const double box[4], uint32_t t_start, ui
 /* A batch of queries in one device pass (the serving path: queries that
  * arrive while a batch runs form the next one). offsets[nq + 1]: the matches
  * of query i are out[offsets[i] .. offsets[i + 1]) when offsets[nq] <= cap;
- * otherwise only offsets is filled and out is left untouched. */
+ * otherwise only offsets is filled and out is left untouched. counts[nq]
+ * (may be NULL): the number of matches of each query. A query whose kind
+ * carries STC_QUERY_COUNT_ONLY is only counted, as the reference's searches
+ * do (search_count): it writes no contacts. */
 #define STC_QUERY_OBJECT 0u
 #define STC_QUERY_BOX 1u
+#define STC_QUERY_COUNT_ONLY 0x100u
 typedef struct stc_query {
-  uint32_t kind;                 /* STC_QUERY_OBJECT or STC_QUERY_BOX */
+  uint32_t kind;                 /* STC_QUERY_OBJECT or STC_QUERY_BOX, optionally | STC_QUERY_COUNT_ONLY */
   uint32_t pid;                  /* object queries */
   uint32_t t_start, t_end;
   double box[4];                 /* box queries: low x, low y, high x, high y */
 } stc_query;
 
 stc_status stc_query_batch(stc_ctx *ctx, const stc_query *queries, size_t nq, stc_contact *out, size_t cap,
-                           uint64_t *offsets);
+                           uint64_t *offsets, uint64_t *counts);
 
 /* Last error message of ctx (or, when ctx is NULL, of the last failed
  * stc_create or context-free call on this thread). Never NULL. */

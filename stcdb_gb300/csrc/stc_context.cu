@@ -293,7 +293,8 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
          dalloc(c, &L.mid_hi, n) && dalloc(c, &L.ctf_cap, ctf_count) && dalloc(c, &L.ctf_first, ctf_count + 1) &&
          dalloc(c, &L.ctfs, ctf_count) && dalloc(c, &L.lim_box, ctf_count) && dalloc(c, &L.lim_time, ctf_count) &&
          dalloc(c, &L.bitmaps, (size_t)ctf_count * (STC_BITMAP_BYTES / 4)) &&
-         dalloc(c, &L.obitmap, STC_BITMAP_BYTES / 4) && dalloc(c, &L.kbytes, 16 * (size_t)L.cap);
+         dalloc(c, &L.obitmap, STC_BITMAP_BYTES / 4) && dalloc(c, &L.kbytes, 16 * (size_t)L.cap) &&
+         dalloc(c, &L.cbase, ctf_count + 1) && dalloc(c, &L.cstart, (size_t)ctf_count * 65537 + 1);
     for (int i = 0; ok && i < 7; i++) ok = dalloc(c, &L.sk[i], w);
     L.st = p.st;
     LsmHost &H = c->lsmh;
@@ -567,7 +568,7 @@ static stc_status query_checks(stc_ctx *c, const char *who) {
 }
 
 extern "C" stc_status stc_query_batch(stc_ctx *c, const stc_query *queries, size_t nq, stc_contact *out,
-                                      size_t cap, uint64_t *offsets) {
+                                      size_t cap, uint64_t *offsets, uint64_t *counts) {
   stc_status st = query_checks(c, "stc_query_batch");
   if (st != STC_OK) return st;
   if ((!queries && nq) || !offsets || (!out && cap)) {
@@ -576,14 +577,14 @@ extern "C" stc_status stc_query_batch(stc_ctx *c, const stc_query *queries, size
   }
   for (size_t i = 0; i < nq; i++) {
     const stc_query &q = queries[i];
-    if ((q.kind != STC_QUERY_OBJECT && q.kind != STC_QUERY_BOX) ||
-        (q.kind == STC_QUERY_OBJECT && q.pid >= c->p.N)) {
+    const uint32_t kind = q.kind & ~STC_QUERY_COUNT_ONLY;
+    if ((kind != STC_QUERY_OBJECT && kind != STC_QUERY_BOX) || (kind == STC_QUERY_OBJECT && q.pid >= c->p.N)) {
       g_create_error = "stc_query_batch: query " + std::to_string(i) + " has a bad kind or object id";
       return STC_ERR_INVALID_ARG;
     }
   }
   std::string err;
-  st = lsm_query(c->lsmh, queries, nq, out, cap, offsets, err);
+  st = lsm_query(c->lsmh, queries, nq, out, cap, offsets, counts, err);
   if (st != STC_OK) g_create_error = "stc_query_batch: " + err;
   return st;
 }
@@ -595,7 +596,7 @@ static stc_status query_one(stc_ctx *c, const stc_query &q, stc_contact *out, si
     return STC_ERR_INVALID_ARG;
   }
   uint64_t off[2] = {0, 0};
-  stc_status st = stc_query_batch(c, &q, 1, out, cap, off);
+  stc_status st = stc_query_batch(c, &q, 1, out, cap, off, nullptr);
   *n = (size_t)off[1];
   return st;
 }

@@ -51,7 +51,13 @@ struct LsmDev {
   uint32_t *bitmaps;               // [F * 2048]
   uint32_t *obitmap;               // [2048]
   uint8_t *kbytes;                 // packed CTF keys (16 * cap bytes)
+  uint32_t *cbase;                 // [F + 1] first dense cell id of each CTF (spatial index)
+  uint32_t *cstart;                // [F * 65537 + 1] first sorted key of each cell
 };
+
+// Keys spanning more than this many bitmap cells in x or y go to their CTF's
+// wide list instead of the cell of their low corner.
+constexpr uint32_t LSM_INDEX_SPAN = 2;
 
 // Device copy of one flushed block, kept for queries.
 struct CtbBlock {
@@ -64,6 +70,11 @@ struct CtbBlock {
   uint4 *orec = nullptr;           // oversize keys (pid, target, duration, end offset), sorted
   float4 *obox = nullptr;
   uint32_t *obitmap = nullptr;     // [2048]
+  // spatial index of the CTF keys: per CTF, dense cells (x_grid + 1) x
+  // (y_grid + 1) of the low corner of each key's box, then one wide slot
+  uint32_t *perm = nullptr;        // block key positions sorted by dense cell id
+  uint32_t *cstart = nullptr;      // [ncells + 1] first position of each cell in perm
+  uint32_t *cbase = nullptr;       // [F + 1] first dense cell id of each CTF
 };
 
 // A retained block as the query kernels see it.
@@ -75,6 +86,9 @@ struct QBlock {
   const float4 *obox;
   const uint32_t *bitmaps;
   const uint32_t *obitmap;
+  const uint32_t *perm;
+  const uint32_t *cstart;
+  const uint32_t *cbase;
   unsigned long long n_over;
   uint32_t F, index, o_end_time_min, pad;
 };
@@ -90,6 +104,8 @@ struct LsmHost {
   uint32_t flushes = 0;
   stc_ctb_info info{};
   std::vector<stc_ctf> ctfs;
+  std::vector<uint32_t> cbase;     // spatial index of the last block (in LsmDev::sk[3], cstart)
+  unsigned long long idx_keys = 0;
   // retained blocks (oldest first) and the query state
   uint32_t retain = 8;
   std::deque<CtbBlock> blocks;
@@ -102,6 +118,8 @@ struct LsmHost {
   QueryRec *d_out = nullptr;
   size_t out_cap = 0;
   unsigned long long *d_count = nullptr;
+  unsigned long long *d_qcounts = nullptr;  // per-query match counts
+  size_t qc_cap = 0;
   double map[4] = {0, 0, 0, 0};
 };
 
@@ -129,7 +147,7 @@ void lsm_release(LsmHost &H);
 // Runs a batch of queries over the retained blocks on H.qstream (see
 // stc_query_batch in include/stc.h).
 stc_status lsm_query(LsmHost &H, const stc_query *q, size_t nq, stc_contact *out, size_t cap, uint64_t *offsets,
-                     std::string &err);
+                     uint64_t *counts, std::string &err);
 
 // Host restatement of CTF::get_ctf_bits (tracing/step_merge.cpp:140-186);
 // returns false when the key would exceed 64 box bits or 128 key bits.

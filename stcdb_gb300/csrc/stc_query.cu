@@ -102,6 +102,16 @@ __device__ __forceinline__ void emit(QueryRec *out, unsigned long long cap, unsi
   out[i] = r;
 }
 
+// Adds the CTA's per-thread match counts to the query's total.
+__device__ __forceinline__ void add_count(unsigned long long *qcounts, uint32_t q, uint32_t mine) {
+  __shared__ unsigned int s_n;
+  if (threadIdx.x == 0) s_n = 0;
+  __syncthreads();
+  if (mine) atomicAdd(&s_n, mine);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_n) atomicAdd(&qcounts[q], (unsigned long long)s_n);
+}
+
 __device__ __forceinline__ void oversize_key(const QBlock &b, unsigned long long i, uint32_t &pid, uint32_t &target,
                                              uint32_t &start, uint32_t &end) {
   uint4 r = b.orec[i];
@@ -115,10 +125,13 @@ __device__ __forceinline__ void oversize_key(const QBlock &b, unsigned long long
 
 __global__ void __launch_bounds__(QOBJ_THREADS) k_query_object(const QBlock *qb, const stc_query *qs,
                                                               QueryRec *out, unsigned long long cap,
-                                                              unsigned long long *count) {
+                                                              unsigned long long *count,
+                                                              unsigned long long *qcounts) {
   const QBlock &b = qb[blockIdx.x];
   const stc_query q = qs[blockIdx.y];
-  if (q.kind != STC_QUERY_OBJECT) return;
+  if ((q.kind & 0xFFu) != STC_QUERY_OBJECT) return;
+  const bool count_only = (q.kind & STC_QUERY_COUNT_ONLY) != 0;
+  uint32_t mine = 0;
   __shared__ long long s_find;
   __shared__ unsigned long long s_lim, s_bad;
   __shared__ uint32_t s_ctf;
@@ -166,7 +179,7 @@ __global__ void __launch_bounds__(QOBJ_THREADS) k_query_object(const QBlock *qb,
     }
   }
   __syncthreads();
-  if (s_find < 0) return;
+  if (s_find < 0) return;  // uniform: no count to add
   const uint32_t c = s_ctf;
   const unsigned long long lim = s_lim;
   // scan on while the pid matches (search_SSTable, step_merge.cpp:530-568)
@@ -198,11 +211,14 @@ __global__ void __launch_bounds__(QOBJ_THREADS) k_query_object(const QBlock *qb,
     if (!match) atomicMin(&s_bad, i);
     __syncthreads();
     const unsigned long long bad = s_bad;
-    if (match && i < bad && time_ok(start, end, q.t_start, q.t_end))
-      emit(out, cap, count, blockIdx.y, pid, target, start, end, box, b.index, c);
-    if (bad != ~0ull) return;
+    if (match && i < bad && time_ok(start, end, q.t_start, q.t_end)) {
+      mine++;
+      if (!count_only) emit(out, cap, count, blockIdx.y, pid, target, start, end, box, b.index, c);
+    }
+    if (bad != ~0ull) break;  // uniform
     __syncthreads();
   }
+  add_count(qcounts, blockIdx.y, mine);
 }
 
 // ---- box queries ---------------------------------------------------------------
@@ -235,12 +251,15 @@ __device__ __forceinline__ void cell_range(double a, double b, double m0, double
 __global__ void __launch_bounds__(QBOX_THREADS) k_query_box(const QBlock *qb, uint32_t nb, const stc_query *qs,
                                                            double m0x, double m0y, double m1x, double m1y,
                                                            QueryRec *out, unsigned long long cap,
-                                                           unsigned long long *count) {
+                                                           unsigned long long *count,
+                                                           unsigned long long *qcounts) {
   const uint32_t bi = blockIdx.z % nb, qi = blockIdx.z / nb;
   const QBlock &b = qb[bi];
   const stc_query q = qs[qi];
   const uint32_t c = blockIdx.y;
-  if (q.kind != STC_QUERY_BOX || c > b.F) return;
+  if ((q.kind & 0xFFu) != STC_QUERY_BOX || c > b.F) return;
+  const bool count_only = (q.kind & STC_QUERY_COUNT_ONLY) != 0;
+  uint32_t mine = 0;
   const double *qbox = q.box;
   if (c == b.F) {
     // oversize buffer: the map bitmap prunes, float boxes decide
@@ -255,9 +274,12 @@ __global__ void __launch_bounds__(QBOX_THREADS) k_query_box(const QBlock *qb, ui
       double box[4] = {fb.x, fb.y, fb.z, fb.w};
       uint32_t pid, target, start, end;
       oversize_key(b, i, pid, target, start, end);
-      if (time_ok(start, end, q.t_start, q.t_end) && box_hits(box, qbox))
-        emit(out, cap, count, qi, pid, target, start, end, box, b.index, c);
+      if (time_ok(start, end, q.t_start, q.t_end) && box_hits(box, qbox)) {
+        mine++;
+        if (!count_only) emit(out, cap, count, qi, pid, target, start, end, box, b.index, c);
+      }
     }
+    add_count(qcounts, qi, mine);
     return;
   }
   const stc_ctf &t = b.ctfs[c];
@@ -273,20 +295,59 @@ __global__ void __launch_bounds__(QBOX_THREADS) k_query_box(const QBlock *qb, ui
   const double wide[4] = {qbox[0] - qx, qbox[1] - qy, qbox[2] + qx, qbox[3] + qy};
   const double ctfb[4] = {t.mbr[0], t.mbr[1], t.mbr[2], t.mbr[3]};
   if (!box_hits(ctfb, wide)) return;
+  if (count_only) {
+    // Every key matches -- count the CTF without decoding it, as the
+    // reference's box search does (workbench.cpp:525-528) -- when the query
+    // holds the CTF box widened by the quantisation, every start is below
+    // t_end, every end above t_start (ends are >= the block's base), and no
+    // time field can have outgrown its bit width (decoded = stored times).
+    const bool inside = qbox[0] <= ctfb[0] - qx && qbox[1] <= ctfb[1] - qy && qbox[2] >= ctfb[2] + qx &&
+                        qbox[3] >= ctfb[3] + qy;
+    const bool times = t.start_time_max < q.t_end && q.t_start < t.end_time_min;
+    const bool fits = (unsigned long long)(t.end_time_max - t.end_time_min) <= mask64(t.end_bit) &&
+                      (unsigned long long)(t.end_time_max - t.start_time_min) <= mask64(t.duration_bit) &&
+                      t.start_time_min <= t.end_time_max && t.end_time_min <= t.end_time_max;
+    if (inside && times && fits) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&qcounts[qi], (unsigned long long)t.kv_count);
+      return;
+    }
+  }
   int i0, i1, j0, j1;
   cell_range(wide[0], wide[2], t.mbr[0], t.mbr[2], t.x_grid, i0, i1);
   cell_range(wide[1], wide[3], t.mbr[1], t.mbr[3], t.y_grid, j0, j1);
   if (!any_bit(b.bitmaps + (size_t)c * (STC_BITMAP_BYTES / 4), i0, i1, j0, j1, t.x_grid)) return;
+  // Spatial index: a key whose exact box meets the widened query has its low
+  // corner at most LSM_INDEX_SPAN cells left of / below the query's first
+  // cell (cell_range already holds one cell of slack), or is in the wide
+  // list. One warp per row segment of low-corner cells.
   const uint32_t kb = t.key_bit / 8u;
   const uint8_t *base = b.keys + t.key_offset;
-  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < t.kv_count;
-       i += (unsigned long long)QBOX_PARTS * blockDim.x) {
-    Key k;
-    decode_key(load_key(base + i * kb, kb), t, k);
-    uint32_t end = k.end + t.end_time_min, start = end - k.duration;
-    if (time_ok(start, end, q.t_start, q.t_end) && box_hits(k.box, qbox))
-      emit(out, cap, count, qi, k.oid, k.target, start, end, k.box, b.index, c);
+  const uint32_t nx = t.x_grid + 1u, ny = t.y_grid + 1u, cb = b.cbase[c];
+  const int li0 = max(i0 - (int)LSM_INDEX_SPAN, 0), lj0 = max(j0 - (int)LSM_INDEX_SPAN, 0);
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, nw = blockDim.x >> 5;
+  const int rows = max(j1 - lj0 + 1, 0);  // the wide list is r == rows
+  for (int r = (int)(blockIdx.x * nw + warp); r <= rows; r += (int)(QBOX_PARTS * nw)) {
+    uint32_t a, e;
+    if (r < rows) {  // row lj0 + r, cells li0..i1
+      const uint32_t row = (uint32_t)(lj0 + r) * nx;
+      a = b.cstart[cb + row + (uint32_t)li0];
+      e = b.cstart[cb + row + (uint32_t)i1 + 1];
+    } else {  // the wide list
+      a = b.cstart[cb + nx * ny];
+      e = b.cstart[cb + nx * ny + 1];
+    }
+    for (uint32_t p = a + lane; p < e; p += 32) {
+      const unsigned long long local = (unsigned long long)b.perm[p] - t.first_key;
+      Key k;
+      decode_key(load_key(base + local * kb, kb), t, k);
+      uint32_t end = k.end + t.end_time_min, start = end - k.duration;
+      if (time_ok(start, end, q.t_start, q.t_end) && box_hits(k.box, qbox)) {
+        mine++;
+        if (!count_only) emit(out, cap, count, qi, k.oid, k.target, start, end, k.box, b.index, c);
+      }
+    }
   }
+  add_count(qcounts, qi, mine);
 }
 
 template <typename T>
@@ -314,6 +375,15 @@ stc_status lsm_store_block(const LsmDev &L, LsmHost &H, cudaStream_t s, std::str
   if (e == cudaSuccess) e = cudaMalloc(&B.orec, std::max<size_t>(no, 1) * sizeof(uint4));
   if (e == cudaSuccess) e = cudaMalloc(&B.obox, std::max<size_t>(no, 1) * sizeof(float4));
   if (e == cudaSuccess) e = cudaMalloc(&B.obitmap, STC_BITMAP_BYTES);
+  const size_t nidx = (size_t)H.idx_keys, ncells = H.cbase.empty() ? 0 : H.cbase.back();
+  if (e == cudaSuccess) e = cudaMalloc(&B.perm, std::max<size_t>(nidx, 1) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&B.cstart, (ncells + 1) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&B.cbase, (F + 1) * sizeof(uint32_t));
+  if (e == cudaSuccess && nidx)
+    e = cudaMemcpyAsync(B.perm, L.sk[3], nidx * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(B.cstart, L.cstart, (ncells + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(B.cbase, L.cbase, (F + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(B.keys + H.info.key_bytes, 0, 32, s);
   if (e == cudaSuccess && H.info.key_bytes)
     e = cudaMemcpyAsync(B.keys, L.kbytes, H.info.key_bytes, cudaMemcpyDeviceToDevice, s);
@@ -328,7 +398,7 @@ stc_status lsm_store_block(const LsmDev &L, LsmHost &H, cudaStream_t s, std::str
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
     for (void *v : {(void *)B.keys, (void *)B.d_ctfs, (void *)B.bitmaps, (void *)B.sids, (void *)B.orec,
-                    (void *)B.obox, (void *)B.obitmap})
+                    (void *)B.obox, (void *)B.obitmap, (void *)B.perm, (void *)B.cstart, (void *)B.cbase})
       if (v) cudaFree(v);
     err = std::string("keeping the flushed block for queries: ") + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? STC_ERR_CAPACITY : STC_ERR_CUDA;
@@ -338,7 +408,7 @@ stc_status lsm_store_block(const LsmDev &L, LsmHost &H, cudaStream_t s, std::str
   while (H.blocks.size() > H.retain) {
     CtbBlock &o = H.blocks.front();
     for (void *v : {(void *)o.keys, (void *)o.d_ctfs, (void *)o.bitmaps, (void *)o.sids, (void *)o.orec,
-                    (void *)o.obox, (void *)o.obitmap})
+                    (void *)o.obox, (void *)o.obitmap, (void *)o.perm, (void *)o.cstart, (void *)o.cbase})
       cudaFree(v);
     H.blocks.pop_front();
   }
@@ -349,13 +419,16 @@ void lsm_release(LsmHost &H) {
   std::unique_lock<std::shared_mutex> lock(H.blocks_mu);
   for (CtbBlock &o : H.blocks)
     for (void *v : {(void *)o.keys, (void *)o.d_ctfs, (void *)o.bitmaps, (void *)o.sids, (void *)o.orec,
-                    (void *)o.obox, (void *)o.obitmap})
+                    (void *)o.obox, (void *)o.obitmap, (void *)o.perm, (void *)o.cstart, (void *)o.cbase})
       cudaFree(v);
   H.blocks.clear();
   if (H.d_qb) cudaFree(H.d_qb);
   if (H.d_q) cudaFree(H.d_q);
   if (H.d_out) cudaFree(H.d_out);
   if (H.d_count) cudaFree(H.d_count);
+  if (H.d_qcounts) cudaFree(H.d_qcounts);
+  H.d_qcounts = nullptr;
+  H.qc_cap = 0;
   if (H.qstream) cudaStreamDestroy(H.qstream);
   H.d_qb = nullptr;
   H.d_q = nullptr;
@@ -366,11 +439,13 @@ void lsm_release(LsmHost &H) {
 }
 
 stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *out, size_t cap, uint64_t *offsets,
-                     std::string &err) {
+                     uint64_t *counts, std::string &err) {
   std::lock_guard<std::mutex> qlock(H.query_mu);
   std::shared_lock<std::shared_mutex> lock(H.blocks_mu);
   const uint32_t nb = (uint32_t)H.blocks.size();
   for (size_t i = 0; i <= nq; i++) offsets[i] = 0;
+  if (counts)
+    for (size_t i = 0; i < nq; i++) counts[i] = 0;
   if (nq == 0 || nb == 0) return STC_OK;
   if (nq * nb > 65535) {
     err = "query batch too large: queries x retained blocks must be <= 65535";
@@ -381,6 +456,7 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
   if (!H.d_qb) e = cudaMalloc(&H.d_qb, (size_t)std::max<uint32_t>(H.retain, 1) * sizeof(QBlock));
   if (e == cudaSuccess && !H.d_count) e = cudaMalloc(&H.d_count, sizeof(unsigned long long));
   if (e == cudaSuccess) e = grow(&H.d_q, &H.q_cap, nq);
+  if (e == cudaSuccess) e = grow(&H.d_qcounts, &H.qc_cap, nq);
   if (e == cudaSuccess) e = grow(&H.d_out, &H.out_cap, std::max<size_t>(1 << 16, H.out_cap));
   if (e != cudaSuccess) {
     err = std::string("query buffers: ") + cudaGetErrorString(e);
@@ -390,27 +466,31 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
   uint32_t maxF = 0;
   for (uint32_t i = 0; i < nb; i++) {
     const CtbBlock &B = H.blocks[i];
-    qb[i] = QBlock{B.keys, B.d_ctfs, B.sids, B.orec, B.obox, B.bitmaps, B.obitmap,
+    qb[i] = QBlock{B.keys, B.d_ctfs, B.sids, B.orec, B.obox, B.bitmaps, B.obitmap, B.perm, B.cstart, B.cbase,
                    (unsigned long long)B.info.oversize_kv_count, B.info.ctf_count, B.info.index,
                    B.info.o_end_time_min, 0};
     maxF = std::max(maxF, B.info.ctf_count);
   }
   bool has_obj = false, has_box = false;
-  for (size_t i = 0; i < nq; i++) (qs[i].kind == STC_QUERY_BOX ? has_box : has_obj) = true;
+  for (size_t i = 0; i < nq; i++) ((qs[i].kind & 0xFFu) == STC_QUERY_BOX ? has_box : has_obj) = true;
   e = cudaMemcpyAsync(H.d_qb, qb.data(), nb * sizeof(QBlock), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(H.d_q, qs, nq * sizeof(stc_query), cudaMemcpyHostToDevice, s);
   unsigned long long total = 0;
   for (int attempt = 0; attempt < 2 && e == cudaSuccess; attempt++) {
     e = cudaMemsetAsync(H.d_count, 0, sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(H.d_qcounts, 0, nq * sizeof(unsigned long long), s);
     if (e != cudaSuccess) break;
     if (has_obj)
       STC_KL k_query_object<<<dim3(nb, (unsigned)nq), QOBJ_THREADS, 0, s>>>(H.d_qb, H.d_q, H.d_out, H.out_cap,
-                                                                           H.d_count);
+                                                                           H.d_count, H.d_qcounts);
     if (has_box)
       STC_KL k_query_box<<<dim3(QBOX_PARTS, maxF + 1, (unsigned)(nq * nb)), QBOX_THREADS, 0, s>>>(
-          H.d_qb, nb, H.d_q, H.map[0], H.map[1], H.map[2], H.map[3], H.d_out, H.out_cap, H.d_count);
+          H.d_qb, nb, H.d_q, H.map[0], H.map[1], H.map[2], H.map[3], H.d_out, H.out_cap, H.d_count,
+          H.d_qcounts);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(&total, H.d_count, sizeof(total), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && counts)
+      e = cudaMemcpyAsync(counts, H.d_qcounts, nq * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess || total <= H.out_cap) break;
     e = grow(&H.d_out, &H.out_cap, (size_t)total);  // too many matches: once more with room for all

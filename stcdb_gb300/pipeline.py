@@ -132,7 +132,7 @@ assert CONTACT_DTYPE.itemsize == 56
 QUERY_DTYPE = np.dtype([("kind", "<u4"), ("pid", "<u4"), ("t_start", "<u4"), ("t_end", "<u4"),
                         ("box", "<f8", (4,))])
 assert QUERY_DTYPE.itemsize == 48
-QUERY_OBJECT, QUERY_BOX = 0, 1
+QUERY_OBJECT, QUERY_BOX, QUERY_COUNT_ONLY = 0, 1, 0x100
 
 
 def sort_contacts(c: np.ndarray) -> np.ndarray:
@@ -230,7 +230,7 @@ def _lib():
         lib.stc_read_ctb.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 7
         lib.stc_read_ctb.restype = ctypes.c_int
         lib.stc_query_batch.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
-                                        ctypes.c_size_t, ctypes.c_void_p]
+                                        ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
         lib.stc_query_batch.restype = ctypes.c_int
         lib.stc_query_object.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                          ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
@@ -307,19 +307,29 @@ class Pipeline:
             "ctfs", "bitmaps", "keys", "sids", "oversize_keys", "oversize_boxes", "oversize_bitmap")]))
         return info, ctb_trim(info, b)
 
-    def query_batch(self, queries: np.ndarray):
-        """Runs a batch (QUERY_DTYPE array); returns a list of CONTACT_DTYPE arrays."""
+    def query_batch(self, queries: np.ndarray, with_counts: bool = False):
+        """Runs a batch (QUERY_DTYPE array); returns a list of CONTACT_DTYPE
+        arrays (and the per-query match counts when with_counts)."""
         q = np.ascontiguousarray(queries, dtype=QUERY_DTYPE)
         offs = np.zeros(len(q) + 1, np.uint64)
+        counts = np.zeros(max(len(q), 1), np.uint64)
         cap = 1 << 16
         while True:
             out = np.zeros(cap, CONTACT_DTYPE)
-            st = self._lib.stc_query_batch(self._h, q.ctypes.data, len(q), out.ctypes.data, cap, offs.ctypes.data)
+            st = self._lib.stc_query_batch(self._h, q.ctypes.data, len(q), out.ctypes.data, cap, offs.ctypes.data,
+                                           counts.ctypes.data)
             if st != 0:
                 raise StcError(st, self._lib.stc_last_error(None).decode())
             if int(offs[-1]) <= cap:
-                return [out[int(offs[i]):int(offs[i + 1])] for i in range(len(q))]
+                res = [out[int(offs[i]):int(offs[i + 1])] for i in range(len(q))]
+                return (res, counts[:len(q)]) if with_counts else res
             cap = int(offs[-1])
+
+    def query_counts(self, queries: np.ndarray) -> np.ndarray:
+        """Match counts only (STC_QUERY_COUNT_ONLY on every query)."""
+        q = np.array(queries, dtype=QUERY_DTYPE, copy=True)
+        q["kind"] |= QUERY_COUNT_ONLY
+        return self.query_batch(q, with_counts=True)[1]
 
     def query_object(self, pid: int, t_start: int = 0, t_end: int = 0xFFFFFFFF) -> np.ndarray:
         q = np.zeros(1, QUERY_DTYPE)

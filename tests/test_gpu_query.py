@@ -76,13 +76,15 @@ def _queries(rng, blocks, mbr, n_obj, n_box):
 
 def _compare(pipe, blocks, qs):
     import oracle as orc
-    got = pipe.query_batch(qs)
+    got, counts = pipe.query_batch(qs, with_counts=True)
     want = orc.query_blocks(blocks, qs)
+    only = pipe.query_counts(qs)  # count-only, with the contained-CTF shortcut
     total = 0
     for i in range(len(qs)):
         g, w = sort_contacts(got[i]), sort_contacts(want[i])
         assert len(g) == len(w) and g.tobytes() == w.tobytes(), \
             f"query {i} ({qs[i]}): GPU {len(g)} contacts, oracle {len(w)}"
+        assert int(counts[i]) == len(w) and int(only[i]) == len(w), f"query {i}: counts {counts[i]}, {only[i]}"
         total += len(w)
     return total
 
