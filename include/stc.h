@@ -276,6 +276,25 @@ typedef struct stc_query {
 stc_status stc_query_batch(stc_ctx *ctx, const stc_query *queries, size_t nq, stc_contact *out, size_t cap,
                            uint64_t *offsets, uint64_t *counts);
 
+/* ---- Block files ---------------------------------------------------------
+ *
+ * stc_write_ctb writes retained block `index` (stc_ctb_info.index) as the
+ * reference's files (straight_dump, tracing/process.cpp:254-348) in dir:
+ *   <prefix>_SSTable_<index>-<c>  packed keys of CTF c,
+ *   <prefix>_STcL<index>-<c>      the CTF object (80 bytes) and its bitmap
+ *                                 (CTF::dump_meta, step_merge.cpp:644-650),
+ *   <prefix>_CTB<index>           the CTB object (128 bytes), sids, oversize keys
+ *                                 (128-bit), boxes, map bitmap (dump_CTB_meta,
+ *                                 workbench.cpp:597-614),
+ * objects in the reference's LP64 byte layout with pointers and padding 0, so
+ * the reference's loaders (workbench::load_CTB_meta, load_CTF_keys) read them.
+ * stc_load_ctb reads such files (written here or by the reference; its key
+ * files must be gathered into dir) into a retained block for queries, as
+ * block `index`. Like stc_step, neither may run concurrently with stc_step on
+ * the same context. Errors: stc_last_error(ctx). */
+stc_status stc_write_ctb(stc_ctx *ctx, uint32_t index, const char *dir, const char *prefix);
+stc_status stc_load_ctb(stc_ctx *ctx, uint32_t index, const char *dir, const char *prefix);
+
 /* Last error message of ctx (or, when ctx is NULL, of the last failed
  * stc_create or context-free call on this thread). Never NULL. */
 const char *stc_last_error(const stc_ctx *ctx);

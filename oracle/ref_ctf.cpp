@@ -11,6 +11,7 @@
 //   CTF::parse_key, CTF::new_parse_mbr, CTF::ctf_get_key_oid (:329-379).
 //
 // Usage: ref_ctf <in.bin> <out.bin>
+//        ref_ctf layout      (offsets and sizes of CTF, CTB, oversize_buffer)
 // in.bin:  f64 map[4], u32 num_objects, u32 max_meet_time, u32 n_cases,
 //          n_cases x { f32 ctf_mbr[4], f32 box[4], u64 pid_field, u32 target,
 //                      u32 duration, u32 end },
@@ -20,6 +21,7 @@
 //                      u64 value_mbr; u64 key_lo, key_hi; u32 oid, target, duration,
 //                      end; u64 value_mbr; f64 box[4] (the stored key decoded) },
 //          u8 o_bitmap[8192], u32 o_start_time_min, o_start_time_max
+#include <cstddef>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -30,7 +32,31 @@
 template <typename T>
 static bool rd(FILE *f, T *v, size_t n = 1) { return fread(v, sizeof(T), n, f) == n; }
 
+// Byte layout of the reference's on-disk structs (CTF::dump_meta and
+// workbench::dump_CTB_meta write them raw): "name offset size" lines.
+#define FIELD(T, f) printf("%s.%s %zu %zu\n", #T, #f, offsetof(T, f), sizeof(((T *)nullptr)->f))
+static int print_layout() {
+  printf("CTF %zu %zu\n", sizeof(CTF), alignof(CTF));
+  FIELD(CTF, ctf_mbr); FIELD(CTF, keys); FIELD(CTF, bitmap); FIELD(CTF, CTF_kv_capacity);
+  FIELD(CTF, start_time_min); FIELD(CTF, start_time_max); FIELD(CTF, end_time_min); FIELD(CTF, end_time_max);
+  FIELD(CTF, ctf_bitmap_size); FIELD(CTF, key_bit); FIELD(CTF, id_bit); FIELD(CTF, duration_bit);
+  FIELD(CTF, end_bit); FIELD(CTF, low_x_bit); FIELD(CTF, low_y_bit); FIELD(CTF, edge_bit); FIELD(CTF, mbr_bit);
+  FIELD(CTF, x_grid); FIELD(CTF, y_grid);
+  printf("CTB %zu %zu\n", sizeof(CTB), alignof(CTB));
+  FIELD(CTB, ctfs); FIELD(CTB, CTF_count); FIELD(CTB, start_time_min); FIELD(CTB, start_time_max);
+  FIELD(CTB, end_time_min); FIELD(CTB, end_time_max); FIELD(CTB, first_widpid); FIELD(CTB, sids);
+  FIELD(CTB, bitmaps); FIELD(CTB, bitmap_mbrs); FIELD(CTB, CTF_capacity); FIELD(CTB, o_buffer);
+  FIELD(CTB, box_rtree);
+  printf("oversize_buffer %zu %zu\n", sizeof(oversize_buffer), alignof(oversize_buffer));
+  FIELD(oversize_buffer, oversize_kv_count); FIELD(oversize_buffer, keys); FIELD(oversize_buffer, boxes);
+  FIELD(oversize_buffer, o_bitmaps); FIELD(oversize_buffer, start_time_min); FIELD(oversize_buffer, start_time_max);
+  FIELD(oversize_buffer, end_time_min); FIELD(oversize_buffer, end_time_max);
+  printf("f_box %zu %zu\n", sizeof(f_box), alignof(f_box));
+  return 0;
+}
+
 int main(int argc, char **argv) {
+  if (argc == 2 && strcmp(argv[1], "layout") == 0) return print_layout();
   if (argc < 3) {
     fprintf(stderr, "usage: %s in.bin out.bin\n", argv[0]);
     return 2;

@@ -293,8 +293,7 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
          dalloc(c, &L.mid_hi, n) && dalloc(c, &L.ctf_cap, ctf_count) && dalloc(c, &L.ctf_first, ctf_count + 1) &&
          dalloc(c, &L.ctfs, ctf_count) && dalloc(c, &L.lim_box, ctf_count) && dalloc(c, &L.lim_time, ctf_count) &&
          dalloc(c, &L.bitmaps, (size_t)ctf_count * (STC_BITMAP_BYTES / 4)) &&
-         dalloc(c, &L.obitmap, STC_BITMAP_BYTES / 4) && dalloc(c, &L.kbytes, 16 * (size_t)L.cap) &&
-         dalloc(c, &L.cbase, ctf_count + 1) && dalloc(c, &L.cstart, (size_t)ctf_count * 65537 + 1);
+         dalloc(c, &L.obitmap, STC_BITMAP_BYTES / 4) && dalloc(c, &L.kbytes, 16 * (size_t)L.cap);
     for (int i = 0; ok && i < 7; i++) ok = dalloc(c, &L.sk[i], w);
     L.st = p.st;
     LsmHost &H = c->lsmh;
@@ -623,4 +622,27 @@ extern "C" stc_status stc_query_box(stc_ctx *c, const double box[4], uint32_t t_
   q.t_end = t_end;
   for (int i = 0; i < 4; i++) q.box[i] = box[i];
   return query_one(c, q, out, cap, n, "stc_query_box");
+}
+
+extern "C" stc_status stc_write_ctb(stc_ctx *c, uint32_t index, const char *dir, const char *prefix) {
+  if (!c) return STC_ERR_INVALID_ARG;
+  if (!dir || !prefix) return fail(c, STC_ERR_INVALID_ARG, "stc_write_ctb: null path");
+  if (!c->lsm_on) return fail(c, STC_ERR_INVALID_ARG, "stc_write_ctb: the memtable is off (kv_restriction 0)");
+  cudaSetDevice(c->device);
+  std::string err;
+  stc_status st = lsm_write_block(c->lsmh, index, c->p.N, dir, prefix, err);
+  if (st != STC_OK) c->err = "stc_write_ctb: " + err;
+  return st;
+}
+
+extern "C" stc_status stc_load_ctb(stc_ctx *c, uint32_t index, const char *dir, const char *prefix) {
+  if (!c) return STC_ERR_INVALID_ARG;
+  if (!dir || !prefix) return fail(c, STC_ERR_INVALID_ARG, "stc_load_ctb: null path");
+  if (!c->lsm_on) return fail(c, STC_ERR_INVALID_ARG, "stc_load_ctb: the memtable is off (kv_restriction 0)");
+  if (c->failed) return STC_ERR_STATE;
+  cudaSetDevice(c->device);
+  std::string err;
+  stc_status st = lsm_load_block(c->lsm, c->lsmh, index, dir, prefix, c->stream, err);
+  if (st != STC_OK) c->err = "stc_load_ctb: " + err;
+  return st;
 }

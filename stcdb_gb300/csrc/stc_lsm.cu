@@ -421,54 +421,6 @@ __global__ void k_lsm_encode(LsmDev L, unsigned long long total, unsigned long l
   }
 }
 
-// Spatial index of the CTF keys for box queries: the dense cell id of the
-// low corner of each key's box in its CTF's bitmap grid (same float cell
-// arithmetic as the bitmap), or the CTF's wide slot when the box spans more
-// than LSM_INDEX_SPAN cells.
-__global__ void k_lsm_cell_keys(LsmDev L, unsigned long long total, uint32_t *keys, uint32_t *vals) {
-  __shared__ unsigned long long s_first[MAX_CTF + 1];
-  for (uint32_t c = threadIdx.x; c <= L.F; c += blockDim.x) s_first[c] = L.ctf_first[c];
-  __syncthreads();
-  for (unsigned long long kid = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; kid < total;
-       kid += (unsigned long long)gridDim.x * blockDim.x) {
-    uint32_t lo = 0, hi = L.F - 1;
-    while (lo < hi) {
-      uint32_t mid = (lo + hi + 1) >> 1;
-      if (s_first[mid] <= kid) lo = mid;
-      else hi = mid - 1;
-    }
-    const uint32_t c = lo;
-    const stc_ctf &t = L.ctfs[c];
-    float4 b = L.bbox[kid];
-    float wx = __fsub_rn(t.mbr[2], t.mbr[0]), wy = __fsub_rn(t.mbr[3], t.mbr[1]);
-    float gx = (float)t.x_grid, gy = (float)t.y_grid;
-    uint32_t l0 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.x, t.mbr[0]), wx), gx));
-    uint32_t l1 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.y, t.mbr[1]), wy), gy));
-    uint32_t h0 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.z, t.mbr[0]), wx), gx));
-    uint32_t h1 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.w, t.mbr[1]), wy), gy));
-    const uint32_t nx = t.x_grid + 1u, ny = t.y_grid + 1u;
-    bool narrow = l0 < nx && l1 < ny && h0 >= l0 && h1 >= l1 && h0 - l0 <= LSM_INDEX_SPAN &&
-                  h1 - l1 <= LSM_INDEX_SPAN;
-    keys[kid] = L.cbase[c] + (narrow ? l1 * nx + l0 : nx * ny);
-    vals[kid] = (uint32_t)kid;
-  }
-}
-
-// cstart[k] = first position of the sorted cell ids holding an id >= k.
-__global__ void k_lsm_cell_starts(const uint32_t *sorted, unsigned long long total, uint32_t ncells,
-                                  uint32_t *cstart) {
-  for (unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; k <= ncells;
-       k += (unsigned long long)gridDim.x * blockDim.x) {
-    unsigned long long lo = 0, hi = total;
-    while (lo < hi) {
-      unsigned long long mid = (lo + hi) >> 1;
-      if (sorted[mid] < k) lo = mid + 1;
-      else hi = mid;
-    }
-    cstart[k] = (uint32_t)lo;
-  }
-}
-
 stc_status cuda_err(cudaError_t e, const char *where, std::string &err) {
   err = std::string(where) + ": " + cudaGetErrorString(e);
   return STC_ERR_CUDA;
@@ -659,20 +611,6 @@ stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState
   cudaMemcpyAsync(L.ctfs, H.ctfs.data(), F * sizeof(stc_ctf), cudaMemcpyHostToDevice, s);
   // 7. bitmaps and packed keys
   if (total) STC_KL k_lsm_encode<<<GRID, 256, 0, s>>>(L, total, slim);
-  // 7b. spatial index of the CTF keys for box queries (not part of the
-  // reference's block): keys sorted by the dense cell of their low corner
-  H.cbase.assign(F + 1, 0);
-  for (uint32_t c = 0; c < F; c++)
-    H.cbase[c + 1] = H.cbase[c] + ((uint32_t)H.ctfs[c].x_grid + 1) * ((uint32_t)H.ctfs[c].y_grid + 1) + 1;
-  const uint32_t ncells = H.cbase[F];
-  H.idx_keys = total;
-  cudaMemcpyAsync(L.cbase, H.cbase.data(), (F + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
-  if (total) {
-    STC_KL k_lsm_set_counts<<<1, 1, 0, s>>>(L.n_dev, N, 0, total);
-    STC_KL k_lsm_cell_keys<<<GRID, 256, 0, s>>>(L, total, sk[0], sk[1]);
-    sort_words(L, sk[0], sk[1], sk[2], sk[3], sk[4], sk[5], 2, (size_t)total, bits_for(ncells), s);
-  }
-  STC_KL k_lsm_cell_starts<<<GRID, 256, 0, s>>>(sk[2], total, ncells, L.cstart);  // sk[3]: positions by cell
   // 8. keep the sids of the block; empty the memtable
   cudaMemcpyAsync(L.bsid, L.sid, (size_t)N * sizeof(uint16_t), cudaMemcpyDeviceToDevice, s);
   stc_ctb_info in{};

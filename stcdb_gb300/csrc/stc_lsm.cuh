@@ -51,8 +51,6 @@ struct LsmDev {
   uint32_t *bitmaps;               // [F * 2048]
   uint32_t *obitmap;               // [2048]
   uint8_t *kbytes;                 // packed CTF keys (16 * cap bytes)
-  uint32_t *cbase;                 // [F + 1] first dense cell id of each CTF (spatial index)
-  uint32_t *cstart;                // [F * 65537 + 1] first sorted key of each cell
 };
 
 // Keys spanning more than this many bitmap cells in x or y go to their CTF's
@@ -104,8 +102,6 @@ struct LsmHost {
   uint32_t flushes = 0;
   stc_ctb_info info{};
   std::vector<stc_ctf> ctfs;
-  std::vector<uint32_t> cbase;     // spatial index of the last block (in LsmDev::sk[3], cstart)
-  unsigned long long idx_keys = 0;
   // retained blocks (oldest first) and the query state
   uint32_t retain = 8;
   std::deque<CtbBlock> blocks;
@@ -137,9 +133,17 @@ void lsm_append(const PipeDev &p, const LsmDev &L, cudaStream_t s);
 // mirror used for read-backs. On failure returns a status and sets err.
 stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState *st_host, std::string &err);
 
-// Copies the block just flushed into its own allocations and appends it to
-// the retained blocks, dropping the oldest beyond H.retain.
+// Copies the block just flushed into its own allocations, builds its cell
+// index and appends it to the retained blocks, dropping the oldest beyond
+// H.retain. L's sort scratch is used for the index.
 stc_status lsm_store_block(const LsmDev &L, LsmHost &H, cudaStream_t s, std::string &err);
+
+// Writes retained block `index` as the reference's files, and reads such
+// files back into a retained block (stc_write_ctb / stc_load_ctb).
+stc_status lsm_write_block(LsmHost &H, uint32_t index, uint32_t num_objects, const std::string &dir,
+                           const std::string &prefix, std::string &err);
+stc_status lsm_load_block(const LsmDev &L, LsmHost &H, uint32_t index, const std::string &dir,
+                          const std::string &prefix, cudaStream_t s, std::string &err);
 
 // Frees the retained blocks and the query buffers.
 void lsm_release(LsmHost &H);

@@ -11,7 +11,10 @@
 // appended to one device buffer tagged with their query; the host groups
 // them by query.
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
+#include <string>
+#include <vector>
 
 #include "stc_lsm.cuh"
 
@@ -237,16 +240,84 @@ __device__ bool any_bit(const uint32_t *bm, int i0, int i1, int j0, int j1, uint
   return __syncthreads_or(found) != 0;
 }
 
+// Position of v on a grid of n cells over [m0, m1], in cells (monotone in v;
+// the cell index and the query windows both use it).
+__device__ __forceinline__ double grid_coord(double v, double m0, double m1, uint32_t n) {
+  double w = __dsub_rn(m1, m0);
+  return __dmul_rn(__ddiv_rn(__dsub_rn(v, m0), w), (double)n);
+}
+
 // Cell range [lo, hi] of the interval [a, b] on a grid of n cells over
 // [m0, m1], one cell of slack either side, clamped to [0, n].
 __device__ __forceinline__ void cell_range(double a, double b, double m0, double m1, uint32_t n, int &lo, int &hi) {
-  double w = m1 - m0;
-  double fa = w > 0 ? (a - m0) / w * n : 0.0, fb = w > 0 ? (b - m0) / w * n : (double)n;
+  const bool ok = m1 > m0;
+  double fa = ok ? grid_coord(a, m0, m1, n) : 0.0, fb = ok ? grid_coord(b, m0, m1, n) : (double)n;
   fa = fmax(fmin(fa, (double)n + 2), -2.0);
   fb = fmax(fmin(fb, (double)n + 2), -2.0);
   lo = max((int)floor(fa) - 1, 0);
   hi = min((int)floor(fb) + 1, (int)n);
 }
+
+// ---- cell index of a block ------------------------------------------------------
+
+constexpr uint32_t MAX_CTF = 3969;
+
+// Dense cell id of each CTF key: the cell of the low corner of its decoded
+// box in its CTF's bitmap grid, or the CTF's wide slot when the box spans
+// more than LSM_INDEX_SPAN cells. A decoded box meeting a query box then has
+// its low-corner cell inside the query's cell window extended by the span.
+__global__ void k_index_cells(const uint8_t *keys, const stc_ctf *ctfs, uint32_t F, const uint32_t *cbase,
+                              unsigned long long total, uint32_t *cells, uint32_t *pos) {
+  __shared__ unsigned long long s_first[MAX_CTF + 1];
+  for (uint32_t c = threadIdx.x; c < F; c += blockDim.x) s_first[c] = ctfs[c].first_key;
+  __syncthreads();
+  for (unsigned long long kid = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; kid < total;
+       kid += (unsigned long long)gridDim.x * blockDim.x) {
+    uint32_t lo = 0, hi = F - 1;
+    while (lo < hi) {
+      uint32_t mid = (lo + hi + 1) >> 1;
+      if (s_first[mid] <= kid) lo = mid;
+      else hi = mid - 1;
+    }
+    const stc_ctf &t = ctfs[lo];
+    const uint32_t kb = t.key_bit / 8u;
+    Key k;
+    decode_key(load_key(keys + t.key_offset + (kid - s_first[lo]) * kb, kb), t, k);
+    const uint32_t nx = t.x_grid + 1u, ny = t.y_grid + 1u;
+    bool narrow = false;
+    uint32_t cell = nx * ny;
+    if (t.mbr[2] > t.mbr[0] && t.mbr[3] > t.mbr[1]) {
+      double fx0 = grid_coord(k.box[0], t.mbr[0], t.mbr[2], t.x_grid);
+      double fx1 = grid_coord(k.box[2], t.mbr[0], t.mbr[2], t.x_grid);
+      double fy0 = grid_coord(k.box[1], t.mbr[1], t.mbr[3], t.y_grid);
+      double fy1 = grid_coord(k.box[3], t.mbr[1], t.mbr[3], t.y_grid);
+      if (fx0 >= 0 && fy0 >= 0 && fx0 < nx && fy0 < ny && fx1 >= fx0 && fy1 >= fy0) {
+        uint32_t l0 = (uint32_t)floor(fx0), l1 = (uint32_t)floor(fy0);
+        double h0 = floor(fx1), h1 = floor(fy1);
+        narrow = h0 - l0 <= LSM_INDEX_SPAN && h1 - l1 <= LSM_INDEX_SPAN;
+        if (narrow) cell = l1 * nx + l0;
+      }
+    }
+    cells[kid] = cbase[lo] + cell;
+    pos[kid] = (uint32_t)kid;
+  }
+}
+
+// cstart[k] = first position of the sorted cell ids holding an id >= k.
+__global__ void k_cell_starts(const uint32_t *sorted, unsigned long long total, uint32_t ncells, uint32_t *cstart) {
+  for (unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; k <= ncells;
+       k += (unsigned long long)gridDim.x * blockDim.x) {
+    unsigned long long lo = 0, hi = total;
+    while (lo < hi) {
+      unsigned long long mid = (lo + hi) >> 1;
+      if (sorted[mid] < k) lo = mid + 1;
+      else hi = mid;
+    }
+    cstart[k] = (uint32_t)lo;
+  }
+}
+
+__global__ void k_set_one(unsigned long long *p, unsigned long long v) { *p = v; }
 
 __global__ void __launch_bounds__(QBOX_THREADS) k_query_box(const QBlock *qb, uint32_t nb, const stc_query *qs,
                                                            double m0x, double m0y, double m1x, double m1y,
@@ -363,6 +434,54 @@ cudaError_t grow(T **p, size_t *cap, size_t need) {
 
 }  // namespace
 
+static void free_block(CtbBlock &B) {
+  for (void *v : {(void *)B.keys, (void *)B.d_ctfs, (void *)B.bitmaps, (void *)B.sids, (void *)B.orec,
+                  (void *)B.obox, (void *)B.obitmap, (void *)B.perm, (void *)B.cstart, (void *)B.cbase})
+    if (v) cudaFree(v);
+  B.keys = nullptr;
+  B.d_ctfs = nullptr;
+  B.bitmaps = nullptr;
+  B.sids = nullptr;
+  B.orec = nullptr;
+  B.obox = nullptr;
+  B.obitmap = nullptr;
+  B.perm = nullptr;
+  B.cstart = nullptr;
+  B.cbase = nullptr;
+}
+
+static void retain_block(LsmHost &H, CtbBlock &&B);
+
+// Cell index of block B (its keys, device CTF records and host CTF copies
+// must be in place), sorted with L's radix-sort scratch.
+static cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
+  const uint32_t F = (uint32_t)B.ctfs.size();
+  std::vector<uint32_t> cbase(F + 1, 0);
+  unsigned long long total = 0;
+  for (uint32_t c = 0; c < F; c++) {
+    cbase[c + 1] = cbase[c] + ((uint32_t)B.ctfs[c].x_grid + 1) * ((uint32_t)B.ctfs[c].y_grid + 1) + 1;
+    total = std::max<unsigned long long>(total, B.ctfs[c].first_key + B.ctfs[c].kv_count);
+  }
+  const uint32_t ncells = cbase[F];
+  if (total > lsm_sort_words(L)) return cudaErrorInvalidValue;  // more keys than the sort scratch holds
+  cudaError_t e = cudaMalloc(&B.perm, std::max<unsigned long long>(total, 1) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&B.cstart, ((size_t)ncells + 1) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&B.cbase, (F + 1) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(B.cbase, cbase.data(), (F + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return e;
+  uint32_t *const *sk = L.sk;
+  if (total) {
+    int bits = 1;
+    while (bits < 32 && ((unsigned long long)ncells >> bits)) bits++;
+    STC_KL k_set_one<<<1, 1, 0, s>>>(L.n_dev + 3, total);
+    STC_KL k_index_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(B.keys, B.d_ctfs, F, B.cbase, total, sk[0], sk[1]);
+    radix_sort_u32(sk[0], sk[1], sk[2], B.perm, sk[4], sk[5], L.n_dev + 3, (size_t)total, bits, L.hist, L.scan, s);
+  }
+  STC_KL k_cell_starts<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[2], total, ncells, B.cstart);
+  e = cudaStreamSynchronize(s);  // the copy of cbase reads this stack frame
+  return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
 stc_status lsm_store_block(const LsmDev &L, LsmHost &H, cudaStream_t s, std::string &err) {
   CtbBlock B;
   B.info = H.info;
@@ -375,15 +494,6 @@ stc_status lsm_store_block(const LsmDev &L, LsmHost &H, cudaStream_t s, std::str
   if (e == cudaSuccess) e = cudaMalloc(&B.orec, std::max<size_t>(no, 1) * sizeof(uint4));
   if (e == cudaSuccess) e = cudaMalloc(&B.obox, std::max<size_t>(no, 1) * sizeof(float4));
   if (e == cudaSuccess) e = cudaMalloc(&B.obitmap, STC_BITMAP_BYTES);
-  const size_t nidx = (size_t)H.idx_keys, ncells = H.cbase.empty() ? 0 : H.cbase.back();
-  if (e == cudaSuccess) e = cudaMalloc(&B.perm, std::max<size_t>(nidx, 1) * sizeof(uint32_t));
-  if (e == cudaSuccess) e = cudaMalloc(&B.cstart, (ncells + 1) * sizeof(uint32_t));
-  if (e == cudaSuccess) e = cudaMalloc(&B.cbase, (F + 1) * sizeof(uint32_t));
-  if (e == cudaSuccess && nidx)
-    e = cudaMemcpyAsync(B.perm, L.sk[3], nidx * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(B.cstart, L.cstart, (ncells + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(B.cbase, L.cbase, (F + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(B.keys + H.info.key_bytes, 0, 32, s);
   if (e == cudaSuccess && H.info.key_bytes)
     e = cudaMemcpyAsync(B.keys, L.kbytes, H.info.key_bytes, cudaMemcpyDeviceToDevice, s);
@@ -395,32 +505,29 @@ stc_status lsm_store_block(const LsmDev &L, LsmHost &H, cudaStream_t s, std::str
   if (e == cudaSuccess && no)
     e = cudaMemcpyAsync(B.obox, L.bbox + H.info.ctf_kv_count, no * sizeof(float4), cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(B.obitmap, L.obitmap, STC_BITMAP_BYTES, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = build_index(L, B, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
-    for (void *v : {(void *)B.keys, (void *)B.d_ctfs, (void *)B.bitmaps, (void *)B.sids, (void *)B.orec,
-                    (void *)B.obox, (void *)B.obitmap, (void *)B.perm, (void *)B.cstart, (void *)B.cbase})
-      if (v) cudaFree(v);
+    free_block(B);
     err = std::string("keeping the flushed block for queries: ") + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? STC_ERR_CAPACITY : STC_ERR_CUDA;
   }
+  retain_block(H, std::move(B));
+  return STC_OK;
+}
+
+static void retain_block(LsmHost &H, CtbBlock &&B) {
   std::unique_lock<std::shared_mutex> lock(H.blocks_mu);
   H.blocks.push_back(std::move(B));
   while (H.blocks.size() > H.retain) {
-    CtbBlock &o = H.blocks.front();
-    for (void *v : {(void *)o.keys, (void *)o.d_ctfs, (void *)o.bitmaps, (void *)o.sids, (void *)o.orec,
-                    (void *)o.obox, (void *)o.obitmap, (void *)o.perm, (void *)o.cstart, (void *)o.cbase})
-      cudaFree(v);
+    free_block(H.blocks.front());
     H.blocks.pop_front();
   }
-  return STC_OK;
 }
 
 void lsm_release(LsmHost &H) {
   std::unique_lock<std::shared_mutex> lock(H.blocks_mu);
-  for (CtbBlock &o : H.blocks)
-    for (void *v : {(void *)o.keys, (void *)o.d_ctfs, (void *)o.bitmaps, (void *)o.sids, (void *)o.orec,
-                    (void *)o.obox, (void *)o.obitmap, (void *)o.perm, (void *)o.cstart, (void *)o.cbase})
-      cudaFree(v);
+  for (CtbBlock &o : H.blocks) free_block(o);
   H.blocks.clear();
   if (H.d_qb) cudaFree(H.d_qb);
   if (H.d_q) cudaFree(H.d_q);
@@ -515,6 +622,260 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
     std::vector<uint64_t> pos(offsets, offsets + nq);
     for (const QueryRec &r : recs) out[pos[r.q]++] = r.c;
   }
+  return STC_OK;
+}
+
+
+// ---- the reference's block files --------------------------------------------------
+//
+// straight_dump (tracing/process.cpp:254-348) writes a block as
+//   <prefix>_SSTable_<ctb>-<ctf>  the packed keys of each CTF,
+//   <prefix>_CTB<ctb>             the CTB object, sids, oversize keys (128-bit),
+//                                 boxes (f_box) and map bitmap (workbench::dump_CTB_meta),
+//   <prefix>_STcL<ctb>-<ctf>      the CTF object and its bitmap (CTF::dump_meta),
+// with the objects written raw. Their byte layout on LP64 (little-endian):
+//   CTF (80 B): ctf_mbr f32[4] @0, keys ptr @16, bitmap ptr @24, CTF_kv_capacity @32,
+//     start_time_min/max @36/40, end_time_min/max @44/48, ctf_bitmap_size @52,
+//     key_bit, id_bit, duration_bit, end_bit, low_x_bit, low_y_bit, edge_bit, mbr_bit,
+//     x_grid, y_grid u16 @56..74 (tracing/step_merge.h:64-87);
+//   CTB (128 B): ctfs ptr @0, CTF_count @8, start/end times @12..24, pointers @32..64,
+//     o_buffer @72 { oversize_kv_count @+0, pointers @+8..+24, start_time_min/max @+32/36,
+//     end_time_min/max @+40/44 }, box_rtree ptr @120 (step_merge.h:33-61, 111-131).
+// Pointers and padding are written as 0 (the reference's loaders replace the
+// pointers, workbench.cpp:639-694). straight_dump leaves CTF_count and the CTB's
+// own times at 0; so does this writer. The reference spreads the key files over
+// two RAID directories by CTF parity; here they all go to one directory.
+
+namespace {
+
+constexpr size_t REF_CTF_BYTES = 80, REF_CTB_BYTES = 128, REF_OBUF = 72;
+
+inline void put32(uint8_t *b, size_t off, uint32_t v) { memcpy(b + off, &v, 4); }
+inline void put16(uint8_t *b, size_t off, uint16_t v) { memcpy(b + off, &v, 2); }
+inline uint32_t get32(const uint8_t *b, size_t off) { uint32_t v; memcpy(&v, b + off, 4); return v; }
+inline uint16_t get16(const uint8_t *b, size_t off) { uint16_t v; memcpy(&v, b + off, 2); return v; }
+
+std::string ctb_path(const std::string &dir, const std::string &prefix, const char *kind, uint32_t ctb, long ctf) {
+  std::string p = dir + "/" + prefix + kind + std::to_string(ctb);
+  if (ctf >= 0) p += "-" + std::to_string(ctf);
+  return p;
+}
+
+bool write_file(const std::string &path, const void *a, size_t na, const void *b, size_t nb) {
+  FILE *f = fopen(path.c_str(), "wb");
+  if (!f) return false;
+  bool ok = (na == 0 || fwrite(a, 1, na, f) == na) && (nb == 0 || fwrite(b, 1, nb, f) == nb);
+  return fclose(f) == 0 && ok;
+}
+
+bool read_file(const std::string &path, std::vector<uint8_t> &out) {
+  FILE *f = fopen(path.c_str(), "rb");
+  if (!f) return false;
+  out.clear();
+  uint8_t buf[1 << 16];
+  size_t n;
+  while ((n = fread(buf, 1, sizeof(buf), f)) > 0) out.insert(out.end(), buf, buf + n);
+  bool ok = !ferror(f);
+  fclose(f);
+  return ok;
+}
+
+void ctf_to_bytes(const stc_ctf &c, uint8_t *b) {
+  memset(b, 0, REF_CTF_BYTES);
+  memcpy(b, c.mbr, 16);
+  put32(b, 32, c.kv_count);
+  put32(b, 36, c.start_time_min);
+  put32(b, 40, c.start_time_max);
+  put32(b, 44, c.end_time_min);
+  put32(b, 48, c.end_time_max);
+  put32(b, 52, c.bitmap_bytes);
+  const uint16_t f[10] = {c.key_bit, c.id_bit, c.duration_bit, c.end_bit, c.low_x_bit,
+                          c.low_y_bit, c.edge_bit, c.mbr_bit, c.x_grid, c.y_grid};
+  for (int i = 0; i < 10; i++) put16(b, 56 + 2 * i, f[i]);
+}
+
+void ctf_from_bytes(const uint8_t *b, stc_ctf &c) {
+  memset(&c, 0, sizeof(c));
+  memcpy(c.mbr, b, 16);
+  c.kv_count = get32(b, 32);
+  c.start_time_min = get32(b, 36);
+  c.start_time_max = get32(b, 40);
+  c.end_time_min = get32(b, 44);
+  c.end_time_max = get32(b, 48);
+  c.bitmap_bytes = get32(b, 52);
+  uint16_t *f[10] = {&c.key_bit, &c.id_bit, &c.duration_bit, &c.end_bit, &c.low_x_bit,
+                     &c.low_y_bit, &c.edge_bit, &c.mbr_bit, &c.x_grid, &c.y_grid};
+  for (int i = 0; i < 10; i++) *f[i] = get16(b, 56 + 2 * i);
+}
+
+}  // namespace
+
+stc_status lsm_write_block(LsmHost &H, uint32_t index, uint32_t N, const std::string &dir, const std::string &prefix,
+                           std::string &err) {
+  std::shared_lock<std::shared_mutex> lock(H.blocks_mu);
+  const CtbBlock *B = nullptr;
+  for (const CtbBlock &b : H.blocks)
+    if (b.info.index == index) B = &b;
+  if (!B) {
+    err = "block " + std::to_string(index) + " is not retained";
+    return STC_ERR_INVALID_ARG;
+  }
+  const stc_ctb_info &in = B->info;
+  const uint32_t F = in.ctf_count;
+  const size_t no = (size_t)in.oversize_kv_count;
+  std::vector<uint8_t> keys(in.key_bytes), bitmaps((size_t)F * STC_BITMAP_BYTES), obitmap(STC_BITMAP_BYTES);
+  std::vector<uint16_t> sids(N);
+  std::vector<uint4> orec(no);
+  std::vector<float4> obox(no);
+  cudaError_t e = cudaSuccess;
+  if (in.key_bytes) e = cudaMemcpy(keys.data(), B->keys, in.key_bytes, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(bitmaps.data(), B->bitmaps, bitmaps.size(), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(sids.data(), B->sids, (size_t)N * 2, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && no) e = cudaMemcpy(orec.data(), B->orec, no * sizeof(uint4), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && no) e = cudaMemcpy(obox.data(), B->obox, no * sizeof(float4), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(obitmap.data(), B->obitmap, STC_BITMAP_BYTES, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    err = std::string("reading the block: ") + cudaGetErrorString(e);
+    return STC_ERR_CUDA;
+  }
+  for (uint32_t c = 0; c < F; c++) {
+    const stc_ctf &t = B->ctfs[c];
+    uint8_t hdr[REF_CTF_BYTES];
+    ctf_to_bytes(t, hdr);
+    const size_t kb = t.key_bit / 8u, nbytes = (size_t)t.kv_count * kb;
+    std::string pm = ctb_path(dir, prefix, "_STcL", index, c), pk = ctb_path(dir, prefix, "_SSTable_", index, c);
+    if (!write_file(pm, hdr, REF_CTF_BYTES, bitmaps.data() + (size_t)c * STC_BITMAP_BYTES, t.bitmap_bytes) ||
+        !write_file(pk, keys.data() + t.key_offset, nbytes, nullptr, 0)) {
+      err = "cannot write " + pm + " or " + pk;
+      return STC_ERR_INVALID_ARG;
+    }
+  }
+  std::vector<uint8_t> ctb(REF_CTB_BYTES + (size_t)N * 2 + no * 32 + STC_BITMAP_BYTES, 0);
+  uint8_t *h = ctb.data();
+  put32(h, REF_OBUF + 0, (uint32_t)no);
+  put32(h, REF_OBUF + 32, in.o_start_time_min);
+  put32(h, REF_OBUF + 36, in.o_start_time_max);
+  put32(h, REF_OBUF + 40, in.o_end_time_min);
+  put32(h, REF_OBUF + 44, in.o_end_time_max);
+  size_t off = REF_CTB_BYTES;
+  memcpy(h + off, sids.data(), (size_t)N * 2);
+  off += (size_t)N * 2;
+  for (size_t i = 0; i < no; i++) {  // 128-bit keys pid:26 | target:26 | duration:32 | end:32 (util/util.h:47-52)
+    uint64_t lo = ((uint64_t)orec[i].z << 32) | orec[i].w, hi = ((uint64_t)orec[i].x << 26) | orec[i].y;
+    memcpy(h + off + 16 * i, &lo, 8);
+    memcpy(h + off + 16 * i + 8, &hi, 8);
+  }
+  off += no * 16;
+  memcpy(h + off, obox.data(), no * 16);
+  off += no * 16;
+  memcpy(h + off, obitmap.data(), STC_BITMAP_BYTES);
+  std::string pc = ctb_path(dir, prefix, "_CTB", index, -1);
+  if (!write_file(pc, ctb.data(), ctb.size(), nullptr, 0)) {
+    err = "cannot write " + pc;
+    return STC_ERR_INVALID_ARG;
+  }
+  return STC_OK;
+}
+
+stc_status lsm_load_block(const LsmDev &L, LsmHost &H, uint32_t index, const std::string &dir,
+                          const std::string &prefix, cudaStream_t s, std::string &err) {
+  const uint32_t F = L.F, N = L.N;
+  std::vector<uint8_t> ctb;
+  std::string pc = ctb_path(dir, prefix, "_CTB", index, -1);
+  if (!read_file(pc, ctb) || ctb.size() < REF_CTB_BYTES) {
+    err = "cannot read " + pc;
+    return STC_ERR_INVALID_ARG;
+  }
+  const size_t no = get32(ctb.data(), REF_OBUF);
+  if (ctb.size() != REF_CTB_BYTES + (size_t)N * 2 + no * 32 + STC_BITMAP_BYTES) {
+    err = pc + ": size does not match " + std::to_string(N) + " objects and " + std::to_string(no) +
+          " oversize keys";
+    return STC_ERR_INVALID_ARG;
+  }
+  CtbBlock B;
+  B.ctfs.resize(F);
+  std::vector<uint8_t> keys, bitmaps((size_t)F * STC_BITMAP_BYTES, 0), meta, part;
+  unsigned long long first = 0;
+  for (uint32_t c = 0; c < F; c++) {
+    std::string pm = ctb_path(dir, prefix, "_STcL", index, c), pk = ctb_path(dir, prefix, "_SSTable_", index, c);
+    if (!read_file(pm, meta) || meta.size() < REF_CTF_BYTES) {
+      err = "cannot read " + pm;
+      return STC_ERR_INVALID_ARG;
+    }
+    stc_ctf &t = B.ctfs[c];
+    ctf_from_bytes(meta.data(), t);
+    if (t.key_bit % 8 || t.key_bit > 128 || t.bitmap_bytes > STC_BITMAP_BYTES ||
+        meta.size() != REF_CTF_BYTES + t.bitmap_bytes) {
+      err = pm + ": not a CTF meta file of this layout";
+      return STC_ERR_INVALID_ARG;
+    }
+    memcpy(bitmaps.data() + (size_t)c * STC_BITMAP_BYTES, meta.data() + REF_CTF_BYTES, t.bitmap_bytes);
+    if (!read_file(pk, part) || part.size() != (size_t)t.kv_count * (t.key_bit / 8u)) {
+      err = "cannot read " + std::to_string((size_t)t.kv_count * (t.key_bit / 8u)) + " key bytes from " + pk;
+      return STC_ERR_INVALID_ARG;
+    }
+    t.first_key = first;
+    t.key_offset = keys.size();
+    first += t.kv_count;
+    keys.insert(keys.end(), part.begin(), part.end());
+  }
+  if (first > lsm_sort_words(L)) {
+    err = "the block holds " + std::to_string(first) + " CTF keys, more than this context's sort scratch (" +
+          std::to_string(lsm_sort_words(L)) + "); raise kv_capacity";
+    return STC_ERR_CAPACITY;
+  }
+  const uint8_t *h = ctb.data();
+  std::vector<uint16_t> sids(N);
+  memcpy(sids.data(), h + REF_CTB_BYTES, (size_t)N * 2);
+  std::vector<uint4> orec(no);
+  std::vector<float4> obox(no);
+  const uint8_t *ok = h + REF_CTB_BYTES + (size_t)N * 2;
+  for (size_t i = 0; i < no; i++) {
+    uint64_t lo, hi;
+    memcpy(&lo, ok + 16 * i, 8);
+    memcpy(&hi, ok + 16 * i + 8, 8);
+    orec[i] = make_uint4((uint32_t)(hi >> 26) & ((1u << 26) - 1), (uint32_t)hi & ((1u << 26) - 1),
+                         (uint32_t)(lo >> 32), (uint32_t)lo);
+  }
+  memcpy(obox.data(), ok + no * 16, no * 16);
+  const uint8_t *obm = ok + no * 32;
+  stc_ctb_info &in = B.info;
+  in.index = index;
+  in.ctf_count = F;
+  in.flush_time = F ? B.ctfs[0].end_time_max : 0;
+  in.end_time_min = F ? B.ctfs[0].end_time_min : 0;
+  in.ctf_kv_count = first;
+  in.oversize_kv_count = no;
+  in.kv_count = first + no;
+  in.key_bytes = keys.size();
+  for (uint16_t v : sids) in.sid_count += v != 0;
+  in.o_start_time_min = get32(h, REF_OBUF + 32);
+  in.o_start_time_max = get32(h, REF_OBUF + 36);
+  in.o_end_time_min = get32(h, REF_OBUF + 40);
+  in.o_end_time_max = get32(h, REF_OBUF + 44);
+  cudaError_t e = cudaMalloc(&B.keys, keys.size() + 32);
+  if (e == cudaSuccess) e = cudaMalloc(&B.d_ctfs, F * sizeof(stc_ctf));
+  if (e == cudaSuccess) e = cudaMalloc(&B.bitmaps, bitmaps.size());
+  if (e == cudaSuccess) e = cudaMalloc(&B.sids, (size_t)N * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&B.orec, std::max<size_t>(no, 1) * sizeof(uint4));
+  if (e == cudaSuccess) e = cudaMalloc(&B.obox, std::max<size_t>(no, 1) * sizeof(float4));
+  if (e == cudaSuccess) e = cudaMalloc(&B.obitmap, STC_BITMAP_BYTES);
+  if (e == cudaSuccess) e = cudaMemsetAsync(B.keys + keys.size(), 0, 32, s);
+  if (e == cudaSuccess && !keys.empty()) e = cudaMemcpyAsync(B.keys, keys.data(), keys.size(), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_ctfs, B.ctfs.data(), F * sizeof(stc_ctf), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(B.bitmaps, bitmaps.data(), bitmaps.size(), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(B.sids, sids.data(), (size_t)N * 2, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && no) e = cudaMemcpyAsync(B.orec, orec.data(), no * sizeof(uint4), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && no) e = cudaMemcpyAsync(B.obox, obox.data(), no * sizeof(float4), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(B.obitmap, obm, STC_BITMAP_BYTES, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = build_index(L, B, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    free_block(B);
+    err = std::string("loading the block: ") + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? STC_ERR_CAPACITY : STC_ERR_CUDA;
+  }
+  retain_block(H, std::move(B));
   return STC_OK;
 }
 

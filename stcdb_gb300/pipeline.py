@@ -232,6 +232,9 @@ def _lib():
         lib.stc_query_batch.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                         ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
         lib.stc_query_batch.restype = ctypes.c_int
+        for fn in ("stc_write_ctb", "stc_load_ctb"):
+            getattr(lib, fn).argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_char_p]
+            getattr(lib, fn).restype = ctypes.c_int
         lib.stc_query_object.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                          ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
         lib.stc_query_object.restype = ctypes.c_int
@@ -330,6 +333,14 @@ class Pipeline:
         q = np.array(queries, dtype=QUERY_DTYPE, copy=True)
         q["kind"] |= QUERY_COUNT_ONLY
         return self.query_batch(q, with_counts=True)[1]
+
+    def write_ctb(self, index: int, directory: str, prefix: str) -> None:
+        """Writes retained block `index` as the reference's block files."""
+        self._check(self._lib.stc_write_ctb(self._h, index, directory.encode(), prefix.encode()))
+
+    def load_ctb(self, index: int, directory: str, prefix: str) -> None:
+        """Reads block files into a retained block (queried like a flushed one)."""
+        self._check(self._lib.stc_load_ctb(self._h, index, directory.encode(), prefix.encode()))
 
     def query_object(self, pid: int, t_start: int = 0, t_end: int = 0xFFFFFFFF) -> np.ndarray:
         q = np.zeros(1, QUERY_DTYPE)

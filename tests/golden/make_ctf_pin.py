@@ -6,7 +6,9 @@ unmodified tracing/step_merge.cpp, built by oracle/build_ref.sh), which calls
 CTF::get_ctf_bits, CTF::serial_mbr, CTF::serial_key,
 oversize_buffer::write_o_buffer and, on the packed keys, CTF::parse_key,
 CTF::new_parse_mbr and CTF::ctf_get_key_oid on seeded random cases, and
-stores inputs and outputs. Only this script needs the reference checkout.
+stores inputs and outputs; and the byte layout of the reference's CTF, CTB
+and oversize_buffer objects (ref_layout.txt), which its block files hold raw.
+Only this script needs the reference checkout.
 
     python tests/golden/make_ctf_pin.py
 """
@@ -125,6 +127,11 @@ def main():
                     p + "o_times": np.array([osmin, osmax], np.uint32)})
     np.savez_compressed(os.path.join(HERE, "ctf_pin.npz"), **out)
     print("wrote ctf_pin.npz with", len(SETS), "sets")
+    # byte layout of the reference's CTF / CTB / oversize_buffer objects
+    layout = subprocess.run([ref, "layout"], check=True, capture_output=True, text=True).stdout
+    with open(os.path.join(HERE, "ref_layout.txt"), "w") as f:
+        f.write(layout)
+    print("wrote ref_layout.txt")
 
 
 if __name__ == "__main__":

@@ -289,3 +289,15 @@ def test_oracle_queries_match_ground_truth(built):
             assert not (b[0] > x1 or b[2] < x0 or b[1] > y1 or b[3] < y0)
         assert set(map(tuple, res[i][["pid", "target", "end"]].tolist())) <= \
             set(map(tuple, res[30][["pid", "target", "end"]].tolist()))
+
+
+def test_reference_layout_fixture():
+    """The struct layout the block files use (printed by the reference's own
+    headers): CTF 80 bytes, CTB 128 with the oversize buffer at 72."""
+    lay = {}
+    for line in open(os.path.join(HERE, "golden", "ref_layout.txt")):
+        name, a, b = line.split()
+        lay[name] = (int(a), int(b))
+    assert lay["CTF"][0] == 80 and lay["CTB"][0] == 128 and lay["oversize_buffer"][0] == 48
+    assert lay["CTF.key_bit"][0] == 56 and lay["CTF.y_grid"][0] == 74 and lay["CTF.ctf_bitmap_size"][0] == 52
+    assert lay["CTB.o_buffer"][0] == 72 and lay["oversize_buffer.start_time_min"][0] == 32
