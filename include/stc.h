@@ -295,6 +295,24 @@ stc_status stc_query_batch(stc_ctx *ctx, const stc_query *queries, size_t nq, st
 stc_status stc_write_ctb(stc_ctx *ctx, uint32_t index, const char *dir, const char *prefix);
 stc_status stc_load_ctb(stc_ctx *ctx, uint32_t index, const char *dir, const char *prefix);
 
+/* ---- Checkpoint / restore ------------------------------------------------
+ *
+ * stc_checkpoint writes everything a context carries from one step to the
+ * next -- configuration, quadtree schema, meeting table, undrained emitted
+ * meetings, memtable, counters -- to one versioned file (a replacement for
+ * the reference's raw workbench dumps, tracing/workbench.cpp:574-694);
+ * stc_restore creates a context on `device` from it, and the next stc_step
+ * continues as the checkpointed context would have. Retained flushed blocks
+ * are not in the file (write them with stc_write_ctb); after a restore
+ * stc_get_ctb reports none until the next flush, and block indices continue.
+ * The file is tied to this library version (struct sizes are checked) and
+ * carries a checksum. Call between steps. Errors: stc_last_error(ctx), or
+ * stc_last_error(NULL) for stc_restore. */
+stc_status stc_checkpoint(stc_ctx *ctx, const char *path);
+/* The configuration a context runs with (a restored one's comes from its file). */
+stc_status stc_get_config(const stc_ctx *ctx, stc_config *cfg);
+stc_status stc_restore(const char *path, uint32_t device, stc_ctx **out);
+
 /* Last error message of ctx (or, when ctx is NULL, of the last failed
  * stc_create or context-free call on this thread). Never NULL. */
 const char *stc_last_error(const stc_ctx *ctx);

@@ -44,6 +44,7 @@ struct stc_ctx {
   std::vector<void *> allocs;
   stc_stats stats;
   uint32_t last_t = 0;
+  double map[4] = {0, 0, 0, 0};  // map box given at creation
   bool lsm_on = false;           // memtable and flush (kv_restriction > 0)
   LsmDev lsm;
   LsmHost lsmh;
@@ -168,10 +169,25 @@ static stc_status read_state(stc_ctx *c, const char *where) {
   return STC_OK;
 }
 
+// Creates a context; builds the quadtree from xy0 unless xy0 is null (a
+// restore fills the schema from a checkpoint instead).
+static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const double *xy0, uint32_t n,
+                             stc_ctx **out);
+
 extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], const double *xy0, uint32_t n,
                                  stc_ctx **out) {
   if (out) *out = nullptr;
-  if (!cfg || !mbr || !xy0 || !out) {
+  if (!xy0) {
+    g_create_error = "stc_create: null argument";
+    return STC_ERR_INVALID_ARG;
+  }
+  return create_ctx(cfg, mbr, xy0, n, out);
+}
+
+static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const double *xy0, uint32_t n,
+                             stc_ctx **out) {
+  if (out) *out = nullptr;
+  if (!cfg || !mbr || !out) {
     g_create_error = "stc_create: null argument";
     return STC_ERR_INVALID_ARG;
   }
@@ -200,6 +216,7 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
   }
   c->cfg = k;
   c->device = (int)k.device;
+  for (int i = 0; i < 4; i++) c->map[i] = mbr[i];
   memset(&c->stats, 0, sizeof(c->stats));
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
@@ -333,9 +350,12 @@ extern "C" stc_status stc_create(const stc_config *cfg, const double mbr[4], con
   iota_u32(p.iota, nu, s);
   init_tables(p, s);
   if (c->lsm_on) lsm_init(c->lsm, s);
-  e = cudaMemcpyAsync(c->xy_own, xy0, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess)
-    e = build_schema(c->xy_own, n, mbr, k.reach_distance, k.grid_capacity, p.sd, p.sw, p.st, c->st_host, s);
+  e = cudaSuccess;
+  if (xy0) {
+    e = cudaMemcpyAsync(c->xy_own, xy0, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = build_schema(c->xy_own, n, mbr, k.reach_distance, k.grid_capacity, p.sd, p.sw, p.st, c->st_host, s);
+  }
   stc_status rs = STC_OK;
   if (e != cudaSuccess) rs = cuda_fail(c, e, "stc_create");
   else rs = read_state(c, "stc_create");
@@ -645,4 +665,219 @@ extern "C" stc_status stc_load_ctb(stc_ctx *c, uint32_t index, const char *dir, 
   stc_status st = lsm_load_block(c->lsm, c->lsmh, index, dir, prefix, c->stream, err);
   if (st != STC_OK) c->err = "stc_load_ctb: " + err;
   return st;
+}
+
+// ---- Checkpoint / restore ------------------------------------------------------
+//
+// A versioned replacement for the reference's raw workbench dumps
+// (tracing/workbench.cpp:574-694): a header (magic, version, the sizes of the
+// structs it embeds, configuration, map box, counters) then length-prefixed
+// sections holding every piece of device state that lives from one step to
+// the next, and a 64-bit checksum of the section bytes.
+
+namespace {
+
+const char CKPT_MAGIC[8] = {'S', 'T', 'C', 'C', 'K', 'P', 'T', '1'};
+constexpr uint32_t CKPT_VERSION = 1;
+constexpr size_t CKPT_CHUNK = 64u << 20;
+
+struct CkptHeader {
+  char magic[8];
+  uint32_t version, header_bytes;
+  uint32_t config_bytes, stats_bytes, state_bytes, node_bytes, meta_bytes, pad0;
+  stc_config cfg;
+  double map[4];
+  uint32_t N, S, G, F;
+  unsigned long long B, E, lsm_cap;
+  uint32_t last_t, stepped, lsm_on, lsm_end_time_min, lsm_flushes, pad1;
+  stc_stats stats;
+  DevState st;
+};
+
+struct Section {
+  void *dev;
+  unsigned long long bytes;
+};
+
+unsigned long long mix_words(unsigned long long h, const uint8_t *p, size_t n) {
+  size_t i = 0;
+  for (; i + 8 <= n; i += 8) {
+    unsigned long long w;
+    memcpy(&w, p + i, 8);
+    h = (h ^ w) * 0x100000001B3ull;
+  }
+  for (; i < n; i++) h = (h ^ p[i]) * 0x100000001B3ull;
+  return h;
+}
+
+std::vector<Section> sections(stc_ctx *c, const DevState &st) {
+  PipeDev &p = c->p;
+  std::vector<Section> v = {
+      {p.sd.nodes, (unsigned long long)p.S * sizeof(Node)},
+      {p.sd.meta, (unsigned long long)p.S * sizeof(NodeMeta)},
+      {p.sd.schema_stack, (unsigned long long)p.S * 4},
+      {p.sd.grids_stack, (unsigned long long)p.G * 4},
+      {p.sd.gid_node, (unsigned long long)p.G * 4},
+      {p.sd.fbox, (unsigned long long)p.S * sizeof(float4)},
+      {p.sw.queued, (unsigned long long)p.S},
+      {p.slots, p.B * sizeof(Slot)},
+      {p.emit, std::min<unsigned long long>(st.emit_count, p.E) * sizeof(stc_meeting)},
+  };
+  if (c->lsm_on) {
+    LsmDev &L = c->lsm;
+    unsigned long long kv = std::min<unsigned long long>(st.kv_count, L.cap);
+    v.push_back({L.rec, kv * sizeof(uint4)});
+    v.push_back({L.box, kv * sizeof(float4)});
+    v.push_back({L.cnt, (unsigned long long)L.N * 4});
+    v.push_back({L.obox, (unsigned long long)L.N * sizeof(uint4)});
+    v.push_back({L.sid, (unsigned long long)L.N * 2});
+  }
+  return v;
+}
+
+}  // namespace
+
+extern "C" stc_status stc_checkpoint(stc_ctx *c, const char *path) {
+  if (!c) return STC_ERR_INVALID_ARG;
+  if (!path) return fail(c, STC_ERR_INVALID_ARG, "stc_checkpoint: null path");
+  if (c->failed) return STC_ERR_STATE;
+  cudaSetDevice(c->device);
+  stc_status rs = read_state(c, "stc_checkpoint");
+  if (rs != STC_OK) return rs;
+  CkptHeader h;
+  memset(&h, 0, sizeof(h));
+  memcpy(h.magic, CKPT_MAGIC, 8);
+  h.version = CKPT_VERSION;
+  h.header_bytes = sizeof(CkptHeader);
+  h.config_bytes = sizeof(stc_config);
+  h.stats_bytes = sizeof(stc_stats);
+  h.state_bytes = sizeof(DevState);
+  h.node_bytes = sizeof(Node);
+  h.meta_bytes = sizeof(NodeMeta);
+  h.cfg = c->cfg;
+  for (int i = 0; i < 4; i++) h.map[i] = c->map[i];
+  h.N = c->p.N;
+  h.S = c->p.S;
+  h.G = c->p.G;
+  h.F = c->lsm_on ? c->lsm.F : 0;
+  h.B = c->p.B;
+  h.E = c->p.E;
+  h.lsm_cap = c->lsm_on ? c->lsm.cap : 0;
+  h.last_t = c->last_t;
+  h.stepped = c->stepped;
+  h.lsm_on = c->lsm_on;
+  h.lsm_end_time_min = c->lsm_on ? c->lsm.end_time_min : 0;
+  h.lsm_flushes = c->lsmh.flushes;
+  h.stats = c->stats;
+  h.st = *c->st_host;
+  FILE *f = fopen(path, "wb");
+  if (!f) return fail(c, STC_ERR_INVALID_ARG, std::string("stc_checkpoint: cannot create ") + path);
+  uint8_t *stage = nullptr;
+  cudaError_t e = cudaMallocHost(&stage, CKPT_CHUNK);
+  bool io = e == cudaSuccess && fwrite(&h, sizeof(h), 1, f) == 1;
+  unsigned long long hash = 0xcbf29ce484222325ull;
+  for (const Section &sec : sections(c, h.st)) {
+    io = io && fwrite(&sec.bytes, 8, 1, f) == 1;
+    for (unsigned long long off = 0; io && off < sec.bytes; off += CKPT_CHUNK) {
+      size_t n = (size_t)std::min<unsigned long long>(CKPT_CHUNK, sec.bytes - off);
+      e = cudaMemcpy(stage, (const uint8_t *)sec.dev + off, n, cudaMemcpyDeviceToHost);
+      io = e == cudaSuccess && fwrite(stage, 1, n, f) == n;
+      if (io) hash = mix_words(hash, stage, n);
+    }
+  }
+  io = io && fwrite(&hash, 8, 1, f) == 1;
+  if (stage) cudaFreeHost(stage);
+  io = (fclose(f) == 0) && io;
+  if (e != cudaSuccess) return cuda_fail(c, e, "stc_checkpoint");
+  if (!io) return fail(c, STC_ERR_INVALID_ARG, std::string("stc_checkpoint: writing ") + path + " failed");
+  return STC_OK;
+}
+
+extern "C" stc_status stc_restore(const char *path, uint32_t device, stc_ctx **out) {
+  if (out) *out = nullptr;
+  if (!path || !out) {
+    g_create_error = "stc_restore: null argument";
+    return STC_ERR_INVALID_ARG;
+  }
+  FILE *f = fopen(path, "rb");
+  if (!f) {
+    g_create_error = std::string("stc_restore: cannot open ") + path;
+    return STC_ERR_INVALID_ARG;
+  }
+  CkptHeader h;
+  if (fread(&h, sizeof(h), 1, f) != 1 || memcmp(h.magic, CKPT_MAGIC, 8) != 0 || h.version != CKPT_VERSION ||
+      h.header_bytes != sizeof(CkptHeader) || h.config_bytes != sizeof(stc_config) ||
+      h.stats_bytes != sizeof(stc_stats) || h.state_bytes != sizeof(DevState) || h.node_bytes != sizeof(Node) ||
+      h.meta_bytes != sizeof(NodeMeta)) {
+    fclose(f);
+    g_create_error = std::string("stc_restore: ") + path + " is not a checkpoint of this library version";
+    return STC_ERR_INVALID_ARG;
+  }
+  stc_config cfg = h.cfg;
+  cfg.device = device;
+  stc_ctx *c = nullptr;
+  stc_status rs = create_ctx(&cfg, h.map, nullptr, h.N, &c);
+  if (rs != STC_OK) {
+    fclose(f);
+    return rs;
+  }
+  auto bail = [&](stc_status st, const std::string &msg) {
+    fclose(f);
+    g_create_error = "stc_restore: " + msg;
+    stc_destroy(c);
+    return st;
+  };
+  if (c->p.S != h.S || c->p.G != h.G || c->p.B != h.B || c->p.E != h.E || (c->lsm_on ? 1u : 0u) != h.lsm_on ||
+      (c->lsm_on && (c->lsm.cap != h.lsm_cap || c->lsm.F != h.F)))
+    return bail(STC_ERR_INVALID_ARG, "the checkpoint's sizes do not match its configuration");
+  uint8_t *stage = nullptr;
+  cudaError_t e = cudaMallocHost(&stage, CKPT_CHUNK);
+  if (e != cudaSuccess) return bail(STC_ERR_CUDA, cudaGetErrorString(e));
+  unsigned long long hash = 0xcbf29ce484222325ull;
+  std::string bad;
+  for (const Section &sec : sections(c, h.st)) {
+    unsigned long long bytes = 0;
+    if (fread(&bytes, 8, 1, f) != 1 || bytes != sec.bytes) {
+      bad = "a section's size does not match";
+      break;
+    }
+    for (unsigned long long off = 0; off < bytes && bad.empty(); off += CKPT_CHUNK) {
+      size_t n = (size_t)std::min<unsigned long long>(CKPT_CHUNK, bytes - off);
+      if (fread(stage, 1, n, f) != n) {
+        bad = "the file is truncated";
+        break;
+      }
+      hash = mix_words(hash, stage, n);
+      e = cudaMemcpy((uint8_t *)sec.dev + off, stage, n, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) bad = cudaGetErrorString(e);
+    }
+    if (!bad.empty()) break;
+  }
+  unsigned long long want = 0;
+  if (bad.empty() && (fread(&want, 8, 1, f) != 1 || want != hash)) bad = "checksum mismatch";
+  cudaFreeHost(stage);
+  if (!bad.empty()) return bail(STC_ERR_INVALID_ARG, bad);
+  fclose(f);
+  e = cudaMemcpy(c->p.st, &h.st, sizeof(DevState), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    g_create_error = std::string("stc_restore: ") + cudaGetErrorString(e);
+    stc_destroy(c);
+    return STC_ERR_CUDA;
+  }
+  *c->st_host = h.st;
+  c->stats = h.stats;
+  c->last_t = h.last_t;
+  c->stepped = h.stepped != 0;
+  if (c->lsm_on) {
+    c->lsm.end_time_min = h.lsm_end_time_min;
+    c->lsmh.flushes = h.lsm_flushes;
+  }
+  *out = c;
+  return STC_OK;
+}
+
+extern "C" stc_status stc_get_config(const stc_ctx *c, stc_config *cfg) {
+  if (!c || !cfg) return STC_ERR_INVALID_ARG;
+  *cfg = c->cfg;
+  return STC_OK;
 }

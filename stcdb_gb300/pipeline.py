@@ -232,6 +232,12 @@ def _lib():
         lib.stc_query_batch.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                         ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
         lib.stc_query_batch.restype = ctypes.c_int
+        lib.stc_get_config.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Config)]
+        lib.stc_get_config.restype = ctypes.c_int
+        lib.stc_checkpoint.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+        lib.stc_checkpoint.restype = ctypes.c_int
+        lib.stc_restore.argtypes = [ctypes.c_char_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p)]
+        lib.stc_restore.restype = ctypes.c_int
         for fn in ("stc_write_ctb", "stc_load_ctb"):
             getattr(lib, fn).argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_char_p]
             getattr(lib, fn).restype = ctypes.c_int
@@ -333,6 +339,25 @@ class Pipeline:
         q = np.array(queries, dtype=QUERY_DTYPE, copy=True)
         q["kind"] |= QUERY_COUNT_ONLY
         return self.query_batch(q, with_counts=True)[1]
+
+    def checkpoint(self, path: str) -> None:
+        """Writes the context's step-to-step state to one file (stc_checkpoint)."""
+        self._check(self._lib.stc_checkpoint(self._h, path.encode()))
+
+    @classmethod
+    def restore(cls, path: str, device: int = 0) -> "Pipeline":
+        """A pipeline continuing from a checkpoint file (stc_restore)."""
+        lib = _lib()
+        h = ctypes.c_void_p()
+        st = lib.stc_restore(path.encode(), device, ctypes.byref(h))
+        if st != 0:
+            raise StcError(st, lib.stc_last_error(None).decode())
+        c = _Config()
+        lib.stc_get_config(h, ctypes.byref(c))
+        p = cls.__new__(cls)
+        p._lib, p._h, p._c = lib, h, c
+        p.cfg = StcConfig(**{f.name: getattr(c, f.name) for f in fields(StcConfig)})
+        return p
 
     def write_ctb(self, index: int, directory: str, prefix: str) -> None:
         """Writes retained block `index` as the reference's block files."""
