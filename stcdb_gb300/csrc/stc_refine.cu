@@ -201,8 +201,18 @@ struct Counters {
 };
 
 // One 32x32 tile. Rows: own members (own=true) or border units.
+// A tile's 32 column points, staged per warp in shared memory: the test loop
+// reads one broadcast (x, y) per column; the rest is read on a hit only.
+struct ColTile {
+  float2 xy[32];     // leaf-relative fp32 offsets
+  float2 f[32];      // fp32 lon / lat (meeting MBR)
+  uint32_t pid[32];
+  uint32_t nb[32];   // border units of the column object (border tiles)
+  uint32_t off[32];
+};
+
 __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtile, uint32_t coltile, uint32_t n,
-                         uint32_t t, Counters &ct, HitRec *q, uint32_t &qn, HitWindow &w) {
+                         uint32_t t, Counters &ct, HitRec *q, uint32_t &qn, HitWindow &w, ColTile &col) {
   const uint32_t lane = lane_id();
   const uint32_t base = p.grid_start[g];
   const uint32_t lt_mask = (1u << lane) - 1u;
@@ -261,41 +271,51 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
   float hi2 = (r + delta) * (r + delta);
   uint32_t kmax = n - coltile * 32;
   if (kmax > 32) kmax = 32;
+  // stage the columns (the previous tile's reads are over)
+  __syncwarp();
+  col.xy[lane] = make_float2(cp.x, cp.y);
+  col.f[lane] = cf;
+  col.pid[lane] = __float_as_uint(cp.w);
+  col.nb[lane] = col_nb;
+  col.off[lane] = col_off;
+  __syncwarp();
+  // this lane tests columns k in [kstart, kmax): an own-leaf unit pairs pid1
+  // only with later members (tracing/refinement.cpp:30)
+  int kstart = !vr ? 64 : (own ? (int)i - (int)(coltile * 32) + 1 : 0);
+  if (kstart < 0) kstart = 0;
+  if (kstart < (int)kmax) ct.tests += kmax - (uint32_t)kstart;
+#pragma unroll 1
   for (uint32_t k = 0; k < kmax; k++) {
-    float cx = __shfl_sync(0xffffffffu, cp.x, k);
-    float cy = __shfl_sync(0xffffffffu, cp.y, k);
-    uint32_t cpid = __shfl_sync(0xffffffffu, __float_as_uint(cp.w), k);
-    float cfx = __shfl_sync(0xffffffffu, cf.x, k);
-    float cfy = __shfl_sync(0xffffffffu, cf.y, k);
-    uint32_t cnb = own ? 0u : __shfl_sync(0xffffffffu, col_nb, k);
-    uint32_t coff = own ? 0u : __shfl_sync(0xffffffffu, col_off, k);
-    uint32_t jj = coltile * 32 + k;
-    bool hit = false;
-    if (vr && !(own && jj <= i)) {  // tracing/refinement.cpp:30
-      float dx = (rp.x - cx) * rp.z;
-      float dy = (rp.y - cy) * STC_SLAT_F;
-      float d2 = dx * dx + dy * dy;
-      ct.tests++;
-      hit = d2 <= lo2;
-      if (!hit && d2 < hi2) {
-        ct.exact++;
-        hit = exact_within(p, pid1, cpid, ct.amb);
-      }
+    const float2 c = col.xy[k];
+    float dx = (rp.x - c.x) * rp.z;
+    float dy = (rp.y - c.y) * STC_SLAT_F;
+    float d2 = dx * dx + dy * dy;
+    const bool valid = (int)k >= kstart;
+    bool hit = valid && d2 <= lo2;
+    if (valid && !hit && d2 < hi2) {
+      ct.exact++;
+      hit = exact_within(p, pid1, col.pid[k], ct.amb);
     }
     uint32_t hm = __ballot_sync(0xffffffffu, hit);
     if (hm) {
+      const uint32_t jj = coltile * 32 + k;
       if (hit) {
         ct.hits++;
+        const uint32_t cpid = col.pid[k];
+        const float2 cfk = col.f[k];
         uint32_t a = pid1 < cpid ? pid1 : cpid, b = pid1 < cpid ? cpid : pid1;
         HitRec h;
         h.key = stc_cantor(a, b);
         h.order = (rank << STC_ORDER_SHIFT) | jj;
-        for (uint32_t u2 = 0; u2 < cnb; u2++)
-          if (p.bu_gid[coff + u2] == row_leaf) h.order |= DUP_BIT;
-        h.lo_x = fminf(rf.x, cfx);
-        h.lo_y = fminf(rf.y, cfy);
-        h.hi_x = fmaxf(rf.x, cfx);
-        h.hi_y = fmaxf(rf.y, cfy);
+        if (!own) {
+          const uint32_t cnb = col.nb[k], coff = col.off[k];
+          for (uint32_t u2 = 0; u2 < cnb; u2++)
+            if (p.bu_gid[coff + u2] == row_leaf) h.order |= DUP_BIT;
+        }
+        h.lo_x = fminf(rf.x, cfk.x);
+        h.lo_y = fminf(rf.y, cfk.y);
+        h.hi_x = fmaxf(rf.x, cfk.x);
+        h.hi_y = fmaxf(rf.y, cfk.y);
         q[qn + __popc(hm & lt_mask)] = h;
       }
       qn += __popc(hm);
@@ -313,9 +333,11 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
   }
 }
 
-__global__ void __launch_bounds__(REFINE_THREADS, 3) k_refine_a(PipeDev p, uint32_t t) {
+__global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint32_t t) {
   __shared__ HitRec queues[REFINE_THREADS / 32][QCAP];
+  __shared__ ColTile cols[REFINE_THREADS / 32];
   HitRec *q = queues[threadIdx.x >> 5];
+  ColTile &col = cols[threadIdx.x >> 5];
   uint32_t qn = 0;  // warp-uniform queue length
   HitWindow w = {0, 0};
   const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -349,10 +371,10 @@ __global__ void __launch_bounds__(REFINE_THREADS, 3) k_refine_a(PipeDev p, uint3
         while (rc > 0 && rc * R - rc * (rc - 1) / 2 > local) rc--;
         while ((rc + 1) * R - (rc + 1) * rc / 2 <= local) rc++;
         uint32_t cc = rc + (local - (rc * R - rc * (rc - 1) / 2));
-        run_tile(p, g, true, rc, cc, n, t, ct, q, qn, w);
+        run_tile(p, g, true, rc, cc, n, t, ct, q, qn, w, col);
       } else {
         uint32_t b = local - own;
-        run_tile(p, g, false, b / R, b % R, n, t, ct, q, qn, w);
+        run_tile(p, g, false, b / R, b % R, n, t, ct, q, qn, w, col);
       }
     }
   }
