@@ -64,10 +64,12 @@ struct NodeMeta {
 };
 
 // One pair within reach found by the refinement, waiting to be applied to
-// the meeting table.
+// the meeting table: the pair (a < b; a = STC_NONE marks an unused record)
+// and its priority. The key is cantor(a, b) and the MBR contribution the two
+// objects' float positions of the step (fxy), both rebuilt when applied.
 struct __align__(16) HitRec {
-  unsigned long long key, order;  // order bit 63: the pair may occur twice this step
-  float lo_x, lo_y, hi_x, hi_y;
+  uint32_t a, b;
+  unsigned long long order;  // bit 63: the pair may occur twice this step
 };
 
 struct __align__(16) U128 {

@@ -68,7 +68,6 @@ __global__ void k_gather(PipeDev p) {
   float ly = __double2float_rn(RN_SUB(q.y, o->lo_y));
   float2 f = make_float2(__double2float_rn(q.x), __double2float_rn(q.y));
   p.pts[i] = make_float4(lx, ly, metres_per_deg_lon_f(q.y), __uint_as_float(pid));
-  p.ptf[i] = f;
   p.fxy[pid] = f;
 }
 

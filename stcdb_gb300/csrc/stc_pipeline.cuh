@@ -29,7 +29,6 @@ struct PipeDev {
   uint32_t *leaf_gid, *lastvalid, *iota, *sorted_gid, *sorted_pid, *sort_ktmp, *sort_vtmp, *sort_hist;
   uint32_t *grid_count, *grid_start;   // G, G+1
   float4 *pts;                          // N sorted: lx, ly, metres/deg lon, pid bits
-  float2 *ptf;                          // N sorted: float lon, lat
   float2 *fxy;                          // N by pid: float lon, lat (MBR of new meetings)
   // border units
   uint32_t *bcount, *boff;              // N+1 (border units per pid, exclusive offsets)

@@ -89,25 +89,29 @@ __device__ void cand_insert(const PipeDev &p, unsigned long long key, unsigned l
 static constexpr int QCAP = 64;  // per-warp queue; flushed 32 at a time
 #define DUP_BIT (1ULL << 63)
 
-// Applies one hit to the table. kv/mbr: the slot at key % B, already loaded.
-__device__ void process_hit_at(const PipeDev &p, const HitRec &h, uint32_t t, unsigned long long slot, U128 kv,
-                               float4 mbr) {
+// Applies one hit (key = cantor(h.a, h.b)) to the table. kv/mbr: the slot
+// at key % B, already loaded.
+__device__ void process_hit_at(const PipeDev &p, const HitRec &h, unsigned long long key, uint32_t t,
+                               unsigned long long slot, U128 kv, float4 mbr) {
   for (unsigned long long probe = 0; probe < STC_PROBE_LIMIT && probe < p.B; probe++) {
     Slot *s = &p.slots[slot];
-    if (kv.lo == h.key) {  // tracing/refinement.cpp:40-42 (+ MBR, cuda/geometry.cu:474-478)
+    if (kv.lo == key) {  // tracing/refinement.cpp:40-42 (+ MBR, cuda/geometry.cu:474-478)
       s->end = t;
-      // the MBR only grows during a step, so a stale read can only cause an extra atomic
-      if (h.lo_x < mbr.x) atomic_min_f(&s->lo_x, h.lo_x);
-      if (h.lo_y < mbr.y) atomic_min_f(&s->lo_y, h.lo_y);
-      if (h.hi_x > mbr.z) atomic_max_f(&s->hi_x, h.hi_x);
-      if (h.hi_y > mbr.w) atomic_max_f(&s->hi_y, h.hi_y);
+      // both objects' float positions this step; the MBR only grows during a
+      // step, so a stale read can only cause an extra atomic
+      const float2 fa = p.fxy[h.a], fb = p.fxy[h.b];
+      const float lx = fminf(fa.x, fb.x), ly = fminf(fa.y, fb.y), hx = fmaxf(fa.x, fb.x), hy = fmaxf(fa.y, fb.y);
+      if (lx < mbr.x) atomic_min_f(&s->lo_x, lx);
+      if (ly < mbr.y) atomic_min_f(&s->lo_y, ly);
+      if (hx > mbr.z) atomic_max_f(&s->hi_x, hx);
+      if (hy > mbr.w) atomic_max_f(&s->hi_y, hy);
       return;
     }
     if (kv.lo == STC_EMPTY_KEY || (kv.lo & STC_CLAIM_BIT)) {  // empty before this step: a new key
       if (h.order & DUP_BIT) {
-        cand_insert(p, h.key, h.order & ~DUP_BIT);
+        cand_insert(p, key, h.order & ~DUP_BIT);
       } else {
-        if (!ordered_walk(p, h.key, h.order, slot, t, &kv)) stc_set_error(p.st, ERR_DA, (uint32_t)slot);
+        if (!ordered_walk(p, key, h.order, slot, t, &kv)) stc_set_error(p.st, ERR_DA, (uint32_t)slot);
       }
       return;
     }
@@ -119,8 +123,9 @@ __device__ void process_hit_at(const PipeDev &p, const HitRec &h, uint32_t t, un
 }
 
 __device__ __forceinline__ void process_hit(const PipeDev &p, const HitRec &h, uint32_t t) {
-  unsigned long long slot = fast_mod(h.key, p.B, p.B_magic);
-  process_hit_at(p, h, t, slot, load_slot_pair(&p.slots[slot]), __ldcg((const float4 *)&p.slots[slot].lo_x));
+  const unsigned long long key = stc_cantor(h.a, h.b);
+  unsigned long long slot = fast_mod(key, p.B, p.B_magic);
+  process_hit_at(p, h, key, t, slot, load_slot_pair(&p.slots[slot]), __ldcg((const float4 *)&p.slots[slot].lo_x));
 }
 
 // Per-warp window of the step's hit buffer, reserved HIT_CHUNK entries at a
@@ -139,7 +144,7 @@ __device__ __forceinline__ void flush_queue(const PipeDev &p, HitRec *q, uint32_
   if (w.end - w.next < n) {
     // pad the rest of the old window with empty records, then reserve a new one
     for (unsigned long long i = w.next + lane; i < w.end; i += 32)
-      if (i < p.hit_cap) p.hits[i].key = STC_EMPTY_KEY;
+      if (i < p.hit_cap) p.hits[i].a = STC_NONE;
     unsigned long long base = 0;
     if (lane == 0) base = atomicAdd(&p.st->hit_count, (unsigned long long)HIT_CHUNK);
     base = __shfl_sync(0xffffffffu, base, 0);
@@ -158,10 +163,11 @@ __device__ __forceinline__ void flush_queue(const PipeDev &p, HitRec *q, uint32_
 
 __device__ __forceinline__ HitRec load_hit(const HitRec *r) {
   // streamed once: evict-first loads keep L2 for the table and positions
-  ulonglong2 a = __ldcs((const ulonglong2 *)r);
-  float4 b = __ldcs((const float4 *)&r->lo_x);
+  ulonglong2 v = __ldcs((const ulonglong2 *)r);
   HitRec h;
-  h.key = a.x; h.order = a.y; h.lo_x = b.x; h.lo_y = b.y; h.hi_x = b.z; h.hi_y = b.w;
+  h.a = (uint32_t)v.x;
+  h.b = (uint32_t)(v.x >> 32);
+  h.order = v.y;
   return h;
 }
 
@@ -174,19 +180,23 @@ __global__ void __launch_bounds__(256) k_hits(PipeDev p, uint32_t t) {
     unsigned long long i2 = i + stride;
     HitRec h0 = load_hit(&p.hits[i]);
     HitRec h1;
-    h1.key = STC_EMPTY_KEY;
+    h1.a = STC_NONE;
     if (i2 < nh) h1 = load_hit(&p.hits[i2]);
-    unsigned long long s0 = fast_mod(h0.key, p.B, p.B_magic), s1 = fast_mod(h1.key, p.B, p.B_magic);
-    U128 kv0 = load_slot_pair(&p.slots[s0]);
-    float4 m0 = __ldcg((const float4 *)&p.slots[s0].lo_x);
-    U128 kv1 = {0, 0};
-    float4 m1 = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (h1.key != STC_EMPTY_KEY) {
+    const bool v0 = h0.a != STC_NONE, v1 = h1.a != STC_NONE;
+    const unsigned long long k0 = v0 ? stc_cantor(h0.a, h0.b) : 0, k1 = v1 ? stc_cantor(h1.a, h1.b) : 0;
+    unsigned long long s0 = fast_mod(k0, p.B, p.B_magic), s1 = fast_mod(k1, p.B, p.B_magic);
+    U128 kv0 = {0, 0}, kv1 = {0, 0};
+    float4 m0 = make_float4(0.f, 0.f, 0.f, 0.f), m1 = m0;
+    if (v0) {
+      kv0 = load_slot_pair(&p.slots[s0]);
+      m0 = __ldcg((const float4 *)&p.slots[s0].lo_x);
+    }
+    if (v1) {
       kv1 = load_slot_pair(&p.slots[s1]);
       m1 = __ldcg((const float4 *)&p.slots[s1].lo_x);
     }
-    if (h0.key != STC_EMPTY_KEY) process_hit_at(p, h0, t, s0, kv0, m0);
-    if (h1.key != STC_EMPTY_KEY) process_hit_at(p, h1, t, s1, kv1, m1);
+    if (v0) process_hit_at(p, h0, k0, t, s0, kv0, m0);
+    if (v1) process_hit_at(p, h1, k1, t, s1, kv1, m1);
   }
 }
 
@@ -202,10 +212,9 @@ struct Counters {
 
 // One 32x32 tile. Rows: own members (own=true) or border units.
 // A tile's 32 column points, staged per warp in shared memory: the test loop
-// reads one broadcast (x, y) per column; the rest is read on a hit only.
+// reads one broadcast (x, y) per column; pid and border data on a hit only.
 struct ColTile {
   float2 xy[32];     // leaf-relative fp32 offsets
-  float2 f[32];      // fp32 lon / lat (meeting MBR)
   uint32_t pid[32];
   uint32_t nb[32];   // border units of the column object (border tiles)
   uint32_t off[32];
@@ -220,10 +229,8 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
   uint32_t j = coltile * 32 + lane;
   bool vc = j < n;
   float4 cp = vc ? p.pts[base + j] : make_float4(0.f, 0.f, 0.f, 0.f);
-  float2 cf = vc ? p.ptf[base + j] : make_float2(0.f, 0.f);
   // row points
   float4 rp;
-  float2 rf = make_float2(0.f, 0.f);
   uint32_t pid1 = 0;
   unsigned long long rank = 0;
   uint32_t i = rowtile * 32 + lane;
@@ -231,7 +238,6 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
   if (own) {
     vr = i < n;
     rp = vr ? p.pts[base + i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    rf = vr ? p.ptf[base + i] : make_float2(0.f, 0.f);
     pid1 = __float_as_uint(rp.w);
     rank = pid1;  // own-leaf unit of pid1 is grid_check[pid1] (tracing/filter.cpp:107-109)
   } else {
@@ -247,7 +253,6 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
       double2 qq = p.xy[pid1];
       rp = make_float4(__double2float_rn(RN_SUB(qq.x, o->lo_x)), __double2float_rn(RN_SUB(qq.y, o->lo_y)),
                        metres_per_deg_lon_f(qq.y), 0.f);
-      rf = make_float2(__double2float_rn(qq.x), __double2float_rn(qq.y));
     }
   }
   // A pair of a border row (pid1 outside leaf g) and member cpid occurs twice
@@ -274,7 +279,6 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
   // stage the columns (the previous tile's reads are over)
   __syncwarp();
   col.xy[lane] = make_float2(cp.x, cp.y);
-  col.f[lane] = cf;
   col.pid[lane] = __float_as_uint(cp.w);
   col.nb[lane] = col_nb;
   col.off[lane] = col_off;
@@ -302,20 +306,15 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
       if (hit) {
         ct.hits++;
         const uint32_t cpid = col.pid[k];
-        const float2 cfk = col.f[k];
-        uint32_t a = pid1 < cpid ? pid1 : cpid, b = pid1 < cpid ? cpid : pid1;
         HitRec h;
-        h.key = stc_cantor(a, b);
+        h.a = pid1 < cpid ? pid1 : cpid;
+        h.b = pid1 < cpid ? cpid : pid1;
         h.order = (rank << STC_ORDER_SHIFT) | jj;
         if (!own) {
           const uint32_t cnb = col.nb[k], coff = col.off[k];
           for (uint32_t u2 = 0; u2 < cnb; u2++)
             if (p.bu_gid[coff + u2] == row_leaf) h.order |= DUP_BIT;
         }
-        h.lo_x = fminf(rf.x, cfk.x);
-        h.lo_y = fminf(rf.y, cfk.y);
-        h.hi_x = fmaxf(rf.x, cfk.x);
-        h.hi_y = fmaxf(rf.y, cfk.y);
         q[qn + __popc(hm & lt_mask)] = h;
       }
       qn += __popc(hm);
@@ -380,7 +379,7 @@ __global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint3
   }
   if (qn) flush_queue(p, q, qn, t, w);
   for (unsigned long long i = w.next + lane_id(); i < w.end; i += 32)
-    if (i < p.hit_cap) p.hits[i].key = STC_EMPTY_KEY;
+    if (i < p.hit_cap) p.hits[i].a = STC_NONE;
   // reduce counters per warp (64-bit sums)
   unsigned long long tests = ct.tests, exact = ct.exact, hits = ct.hits, amb = ct.amb;
 #pragma unroll
