@@ -99,7 +99,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -147,26 +147,47 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+class HostSteps:
+    """Host position steps first..first+len-1, indexed by step number."""
+
+    def __init__(self, arr, first):
+        self.arr, self.first = arr, first
+
+    def __getitem__(self, t):
+        return self.arr[t - self.first]
+
+
 def run_gpu(args, w, rank, local):
     import torch
     from stcdb_gb300.pipeline import Pipeline
-    from stcdb_gb300.tracegen import TraceGenerator
+    from stcdb_gb300.tracegen import DeviceTraceGenerator
 
     torch.cuda.set_device(local)
     N = w["objects"]
     K, W = args.steps, args.warmup
-    gen = TraceGenerator(make_trace_cfg(w, seed=1 + rank))
+    # positions come from the device trace generator (bit-identical to the
+    # host generator): steps 0..W+K-1 stay in HBM for the device-resident
+    # run, steps W+K..W+3K-1 go to pinned host memory for the end-to-end and
+    # serving runs
+    gen = DeviceTraceGenerator(make_trace_cfg(w, seed=1 + rank), local)
     mbr = gen.map_box(100.0)
-    total_steps = W + 3 * K
-    host = torch.empty((total_steps, N, 2), dtype=torch.float64, pin_memory=True)
-    hnp = host.numpy()
-    for t in range(total_steps):
-        gen.next(hnp[t])
     dev = torch.empty((W + K, N, 2), dtype=torch.float64, device=f"cuda:{local}")
-    dev.copy_(host[: W + K])
+    gen.next_into(dev.data_ptr(), W + K)
+    gen_ms = gen.last_ms
+    host = torch.empty((2 * K, N, 2), dtype=torch.float64, pin_memory=True)
+    stage = torch.empty((K, N, 2), dtype=torch.float64, device=f"cuda:{local}")
+    for half in range(2):
+        gen.next_into(stage.data_ptr(), K)
+        host[half * K:(half + 1) * K].copy_(stage)
+    gen.close()
+    del stage
+    hnp = HostSteps(host.numpy(), W + K)
     torch.cuda.synchronize()
+    trace_gen = {"steps": W + K, "ms": gen_ms, "ms_per_step": gen_ms / (W + K),
+                 "positions_per_s": N * (W + K) / (gen_ms / 1e3),
+                 "written_gb_s": 16.0 * N * (W + K) / (gen_ms / 1e3) / 1e9}
     cfg = make_cfg(w, device=local)
-    pipe = Pipeline(cfg, mbr, hnp[0])
+    pipe = Pipeline(cfg, mbr, dev[0].cpu().numpy())
     # warm-up steps (device-resident input)
     for t in range(W):
         pipe.step_device(dev[t].data_ptr(), t)
@@ -212,7 +233,7 @@ def run_gpu(args, w, rank, local):
         queries = serve_under_ingest(args, pipe, hnp, W + 2 * K, K, N, mbr)
     pipe.close()
     return dict(stats=stats, dev_ms=dev_ms, wall_dev=wall_dev, wall_e2e=wall_e2e, e2e_stats=e2e_stats,
-                d2h=d2h, clocks=clk.summary(), flush=flush, queries=queries)
+                d2h=d2h, clocks=clk.summary(), flush=flush, queries=queries, trace_gen=trace_gen)
 
 
 def make_queries(rng, n, N, mbr, t_now):
@@ -357,7 +378,7 @@ def cpu_baseline(w, steps, threads, sample_note):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="uniform-10M", choices=sorted(WORKLOADS))
@@ -433,6 +454,7 @@ def main():
         "phase_ms": phase_ms,
         "flush": flush_line(r["flush"], peak),
         "queries_under_ingest": r["queries"],
+        "trace_gen": r["trace_gen"],
         "per_step": {"pair_tests": s_last.pair_tests, "exact_tests": s_last.exact_tests, "hits": s_last.hits,
                      "new_candidates": s_last.new_candidates, "live_meetings": s_last.taken_buckets,
                      "emitted": s_last.emitted, "border_units": s_last.border_units, "leaves": s_last.leaves,

@@ -1,6 +1,7 @@
 """Builds the native libraries in-tree (no pip install, no cmake).
 
-  lib/libstctrace.so  host C: seeded synthetic trace generator
+  lib/libstctrace.so  host C: seeded synthetic trace generator (the device
+                      generator in libstc.so shares its per-object code)
   lib/libstc.so       CUDA sm_103a kernels + C++ host runtime behind the C ABI
                       declared in include/stc.h
 
@@ -34,6 +35,7 @@ CU_SOURCES = [
     "stc_util.cu",
     "stc_lsm.cu",
     "stc_query.cu",
+    "stc_tracegen.cu",
 ]
 
 
@@ -63,9 +65,11 @@ def build_tracegen() -> str:
     os.makedirs(LIB_DIR, exist_ok=True)
     out = os.path.join(LIB_DIR, "libstctrace.so")
     src = os.path.join(CSRC, "tracegen.c")
-    if _stale(out, [src, os.path.join(CSRC, "tracegen.h")]):
+    deps = [src, os.path.join(CSRC, "tracegen.h"), os.path.join(CSRC, "tracegen_walk.h"),
+            os.path.join(INCLUDE, "stc_trace.h"), os.path.join(INCLUDE, "stc.h")]
+    if _stale(out, deps):
         _run(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-Wall",
-              "-o", out, src, "-lm"])
+              "-I" + INCLUDE, "-I" + CSRC, "-o", out, src, "-lm"])
     return out
 
 

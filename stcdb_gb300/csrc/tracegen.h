@@ -2,22 +2,12 @@
 #ifndef STC_TRACEGEN_H
 #define STC_TRACEGEN_H
 #include <stdint.h>
+
+#include "stc_trace.h" /* stc_trace_config */
+
 #ifdef __cplusplus
 extern "C" {
 #endif
-
-typedef struct stc_trace_config {
-  uint32_t num_objects;
-  int32_t grid_n;       /* street nodes per side */
-  double box_m;         /* side of the square box, metres */
-  double jitter_m;      /* node jitter, +- metres */
-  double speed_lo, speed_hi;  /* m/s, uniform */
-  int32_t n_hotspots;   /* 0: all objects start uniformly on edges */
-  double hot_frac;      /* fraction of objects drawn from hotspots */
-  double sigma_m;       /* hotspot Gaussian sigma, metres */
-  double zipf_s;        /* hotspot weight exponent */
-  uint64_t seed;
-} stc_trace_config;
 
 typedef struct stc_tracegen stc_tracegen;
 

@@ -115,3 +115,76 @@ class TraceGenerator:
             self.close()
         except Exception:
             pass
+
+
+def _dev_lib():
+    lib = load_library("libstc")
+    if not getattr(lib, "_stc_trace_typed", False):
+        lib.stc_trace_dev_create.restype = ctypes.c_int
+        lib.stc_trace_dev_create.argtypes = [ctypes.POINTER(_Cfg), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+        lib.stc_trace_dev_next.restype = ctypes.c_int
+        lib.stc_trace_dev_next.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32]
+        lib.stc_trace_dev_step.restype = ctypes.c_uint32
+        lib.stc_trace_dev_step.argtypes = [ctypes.c_void_p]
+        lib.stc_trace_dev_map_box.restype = ctypes.c_int
+        lib.stc_trace_dev_map_box.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p]
+        lib.stc_trace_dev_last_ms.restype = ctypes.c_float
+        lib.stc_trace_dev_last_ms.argtypes = [ctypes.c_void_p]
+        lib.stc_trace_dev_destroy.argtypes = [ctypes.c_void_p]
+        lib._stc_trace_typed = True
+    return lib
+
+
+class DeviceTraceGenerator:
+    """The same walker with its state in GPU memory (stc_trace_dev_* in
+    libstc): writes steps straight into a device buffer, bit-identical to
+    TraceGenerator's output for the same configuration."""
+
+    def __init__(self, cfg: TraceConfig, device: int = 0):
+        self.cfg = cfg
+        c = _Cfg(cfg.num_objects, cfg.grid_n, cfg.box_m, cfg.jitter_m, cfg.speed_lo, cfg.speed_hi,
+                 cfg.n_hotspots, cfg.hot_frac, cfg.sigma_m, cfg.zipf_s, cfg.seed)
+        self._lib = _dev_lib()
+        h = ctypes.c_void_p()
+        st = self._lib.stc_trace_dev_create(ctypes.byref(c), device, ctypes.byref(h))
+        if st != 0:
+            raise ValueError(f"stc_trace_dev_create failed with status {st} for {cfg}")
+        self._h = h.value
+
+    def map_box(self, pad_m: float = 100.0) -> np.ndarray:
+        out = np.zeros(4, dtype=np.float64)
+        self._lib.stc_trace_dev_map_box(self._h, pad_m, out.ctypes.data)
+        return out
+
+    def next_into(self, xy_device_ptr: int, steps: int = 1) -> None:
+        """Writes `steps` steps of (N, 2) f64 positions at the device address
+        (16-byte aligned), step k at offset 16 * N * k bytes."""
+        st = self._lib.stc_trace_dev_next(self._h, ctypes.c_void_p(xy_device_ptr), steps)
+        if st != 0:
+            raise RuntimeError(f"stc_trace_dev_next failed with status {st}")
+
+    @property
+    def step(self) -> int:
+        return int(self._lib.stc_trace_dev_step(self._h))
+
+    @property
+    def last_ms(self) -> float:
+        """Device time of the last next_into call."""
+        return float(self._lib.stc_trace_dev_last_ms(self._h))
+
+    def close(self):
+        if self._h:
+            self._lib.stc_trace_dev_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -22,3 +22,23 @@ def test_inside_map_and_speed(built):
     dpm_lat = 360.0 / 40076000.0
     d = np.hypot(np.diff(tr[..., 0], axis=0) / dpml0, np.diff(tr[..., 1], axis=0) / dpm_lat)
     assert d.max() <= 15.0 + 1e-6
+
+
+# sha256 of 30 steps, recorded from the generator before its per-object
+# arithmetic moved into tracegen_walk.h (shared with the device generator):
+# the walk of a given configuration never changes.
+PINNED = [
+    (dict(num_objects=20000, n_hotspots=40, hot_frac=0.7, seed=21, grid_n=25, box_m=2500.0, sigma_m=80.0),
+     "e56308539854a8e84f4aa769fb99d4a7df57bfd1ffce7fd7e2e5ca461ae3aacd"),
+    (dict(num_objects=3000, grid_n=4, box_m=60.0, jitter_m=5.0, speed_lo=20.0, speed_hi=90.0, n_hotspots=3,
+          hot_frac=0.5, sigma_m=10.0, seed=77),
+     "34caceee78c82e238872270b378ee7a8571e5b970e4ca0aee621963fb180f2eb"),
+]
+
+
+def test_walk_is_pinned(built):
+    import hashlib
+    from stcdb_gb300.tracegen import TraceConfig
+    for kw, digest in PINNED:
+        tr = TraceGenerator(TraceConfig(**kw)).steps(30)
+        assert hashlib.sha256(tr.tobytes()).hexdigest() == digest, kw
