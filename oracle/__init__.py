@@ -17,6 +17,7 @@ import ctypes
 import os
 import struct
 import subprocess
+import tempfile
 
 import numpy as np
 
@@ -25,6 +26,7 @@ ROOT = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "liboracle.so")
 REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
 REF_CTF = os.path.join(HERE, "_ref", "ref_ctf")
+REF_COMPACT = os.path.join(HERE, "_ref", "ref_compact")
 
 MEETING_DTYPE = np.dtype([("pid_lo", "<u4"), ("pid_hi", "<u4"), ("start", "<u4"), ("end", "<u4"),
                           ("mbr", "<f4", (4,))])
@@ -32,10 +34,16 @@ MEETING_DTYPE = np.dtype([("pid_lo", "<u4"), ("pid_hi", "<u4"), ("start", "<u4")
 
 def build(reference: bool = True) -> None:
     srcs = [os.path.join(HERE, "stc_oracle.c"), os.path.join(HERE, "stc_lsm.c")]
-    deps = srcs + [os.path.join(HERE, "stc_oracle.h"), os.path.join(ROOT, "include", "stc.h")]
+    cpp = os.path.join(HERE, "stc_compact.cpp")
+    deps = srcs + [cpp, os.path.join(HERE, "stc_oracle.h"), os.path.join(ROOT, "include", "stc.h")]
     if not os.path.exists(LIB) or any(os.path.getmtime(d) > os.path.getmtime(LIB) for d in deps):
-        subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-Wall",
-                        "-I" + os.path.join(ROOT, "include"), "-o", LIB] + srcs + ["-lm"], check=True)
+        inc = ["-I" + os.path.join(ROOT, "include"), "-I" + HERE]
+        with tempfile.TemporaryDirectory() as tmp:
+            obj = os.path.join(tmp, "stc_compact.o")
+            subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-Wall", "-c", cpp, "-o", obj]
+                           + inc, check=True)
+            subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-Wall"] + inc
+                           + ["-o", LIB] + srcs + [obj, "-lstdc++", "-lm"], check=True)
     if reference:
         subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True)
 
@@ -63,6 +71,12 @@ def _lib():
     lib.oracle_grids_stack_index.argtypes = [ctypes.c_void_p]
     lib.oracle_grids_stack_index.restype = ctypes.c_uint32
     lib.oracle_schema_dump.argtypes = [ctypes.c_void_p] * 5
+    lib.cmp_compact.restype = ctypes.c_void_p
+    lib.cmp_compact.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]
+    lib.cmp_get.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.cmp_read.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 7
+    lib.cmp_free.argtypes = [ctypes.c_void_p]
     lib.lsm_create.restype = ctypes.c_void_p
     lib.lsm_create.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double,
                                ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64]
@@ -317,3 +331,52 @@ def query_blocks(blocks, queries) -> list:
                 cap = n
         out.append(np.concatenate(res) if res else np.zeros(0, CONTACT_DTYPE))
     return out
+
+
+def _cmp_block_type():
+    """cmp_block (stc_oracle.h)."""
+    from stcdb_gb300.pipeline import StcCtbInfo
+
+    class CmpBlock(ctypes.Structure):
+        _fields_ = [("info", StcCtbInfo), ("ctfs", ctypes.c_void_p), ("keys", ctypes.c_void_p),
+                    ("sids", ctypes.c_void_p), ("okeys", ctypes.c_void_p), ("oboxes", ctypes.c_void_p),
+                    ("obitmap", ctypes.c_void_p)]
+    return CmpBlock
+
+
+def compact(blocks, num_objects: int, split: int, max_meet_time: int, map_box, new_index: int,
+            reference_mode: bool = False):
+    """cmp_compact over a list of (info, buffers) blocks as stc_read_ctb lays
+    them out; returns (info, buffers) of the merged block."""
+    from stcdb_gb300.pipeline import StcCtbInfo, ctb_buffers, ctb_trim
+    keep = []
+    arr = (_cmp_block_type() * len(blocks))()
+    for i, (info, b) in enumerate(blocks):
+        bufs = {k: np.ascontiguousarray(b[k]) for k in ("ctfs", "keys", "sids", "oversize_keys", "oversize_boxes",
+                                                        "oversize_bitmap")}
+        for k, dt, n in (("keys", np.uint8, 16), ("oversize_keys", np.uint64, 2), ("oversize_boxes", np.float32, 4)):
+            if len(bufs[k]) == 0:
+                bufs[k] = np.zeros(n, dt)
+        keep.append(bufs)
+        arr[i].info = info
+        arr[i].ctfs = bufs["ctfs"].ctypes.data
+        arr[i].keys = bufs["keys"].ctypes.data
+        arr[i].sids = bufs["sids"].ctypes.data
+        arr[i].okeys = bufs["oversize_keys"].ctypes.data
+        arr[i].oboxes = bufs["oversize_boxes"].ctypes.data
+        arr[i].obitmap = bufs["oversize_bitmap"].ctypes.data
+    m = np.ascontiguousarray(map_box, np.float64)
+    err = ctypes.create_string_buffer(256)
+    h = lib().cmp_compact(ctypes.byref(arr), len(blocks), num_objects, split, max_meet_time, m.ctypes.data,
+                          new_index, int(bool(reference_mode)), err, 256)
+    if not h:
+        raise RuntimeError("cmp_compact: " + err.value.decode())
+    try:
+        info = StcCtbInfo()
+        lib().cmp_get(h, ctypes.byref(info))
+        out = ctb_buffers(info, num_objects)
+        lib().cmp_read(h, *[out[k].ctypes.data for k in (
+            "ctfs", "bitmaps", "keys", "sids", "oversize_keys", "oversize_boxes", "oversize_bitmap")])
+    finally:
+        lib().cmp_free(h)
+    return info, ctb_trim(info, out)

@@ -1,8 +1,9 @@
 #!/usr/bin/env bash
 # Compiles the reference's own CPU co-occurrence path from its unmodified
 # sources (read in place, never copied) plus the harness oracle/ref_driver.cpp
-# into oracle/_ref/ref_driver, and oracle/ref_ctf.cpp (the reference's host CTF
-# encoding routines) into oracle/_ref/ref_ctf. The reference is only present on the machine
+# into oracle/_ref/ref_driver, oracle/ref_ctf.cpp (the reference's host CTF
+# encoding routines) into oracle/_ref/ref_ctf, and oracle/ref_compact.cpp (the
+# reference's compaction, tools/compaction.cpp) into oracle/_ref/ref_compact. The reference is only present on the machine
 # that holds the read-only checkout; elsewhere this script exits 0 and does
 # nothing, and the committed fixtures under tests/golden/ stand in for it.
 #
@@ -30,6 +31,16 @@ for s in $SRCS; do
   OBJS="$OBJS $o"
 done
 wait
+# tools/compaction.cpp holds the experiment driver's main(); it is renamed so
+# the harness supplies its own (the driver is never called).
+CO="$OUT/compaction.o"
+if [ ! -f "$CO" ] || [ "$REF/src/tools/compaction.cpp" -nt "$CO" ]; then
+  g++ -std=c++17 -O2 -ffp-contract=off -w -fopenmp -I"$HERE/ref_stub" -I"$REF/src" -I"$CUDA_INC" \
+    -Dmain=reference_compaction_driver_main -c "$REF/src/tools/compaction.cpp" -o "$CO"
+fi
+g++ -std=c++17 -O2 -ffp-contract=off -w -fopenmp -I"$HERE/ref_stub" -I"$REF/src" -I"$CUDA_INC" \
+  "$HERE/ref_compact.cpp" "$CO" $OBJS -o "$OUT/ref_compact" -lpthread &
+P3=$!
 g++ -std=c++17 -O2 -ffp-contract=off -w -fopenmp -I"$HERE/ref_stub" -I"$REF/src" -I"$CUDA_INC" \
   "$HERE/ref_driver.cpp" $OBJS -o "$OUT/ref_driver" -lpthread &
 P1=$!
@@ -38,4 +49,5 @@ g++ -std=c++17 -O2 -ffp-contract=off -w -fopenmp -I"$HERE/ref_stub" -I"$REF/src"
 P2=$!
 wait "$P1"
 wait "$P2"
-echo "build_ref: built $OUT/ref_driver and $OUT/ref_ctf" >&2
+wait "$P3"
+echo "build_ref: built $OUT/ref_driver, $OUT/ref_ctf and $OUT/ref_compact" >&2

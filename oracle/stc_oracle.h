@@ -82,6 +82,28 @@ size_t lsm_query_box_block(const stc_ctb_info *in, const stc_ctf *ctfs, const ui
                            const float *oboxes, const double q[4], uint32_t t1, uint32_t t2, stc_contact *out,
                            size_t cap, size_t n);
 
+/* Compaction (stc_compact.cpp): merges m blocks, each read out as
+ * stc_read_ctb lays it out, into one block of split x split CTFs. */
+typedef struct cmp_block {
+  stc_ctb_info info;
+  const stc_ctf *ctfs;
+  const uint8_t *keys;
+  const uint16_t *sids;
+  const uint64_t *okeys;
+  const float *oboxes;
+  const uint8_t *obitmap;
+} cmp_block;
+typedef struct cmp_result cmp_result;
+/* reference_mode: follow merge_dump literally where its output is pinned
+ * (see stc_compact.cpp). NULL on error (message in err). */
+cmp_result *cmp_compact(const cmp_block *blocks, uint32_t m, uint32_t num_objects, uint32_t split,
+                        uint32_t max_meet_time, const double map[4], uint32_t new_index, int reference_mode,
+                        char *err, size_t errlen);
+int cmp_get(const cmp_result *r, stc_ctb_info *info);
+int cmp_read(const cmp_result *r, stc_ctf *ctfs, uint8_t *bitmaps, uint8_t *keys, uint16_t *sids, uint64_t *okeys,
+             float *oboxes, uint8_t *obitmap);
+void cmp_free(cmp_result *r);
+
 #ifdef __cplusplus
 }
 #endif

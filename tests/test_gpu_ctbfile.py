@@ -12,51 +12,10 @@ import pytest
 from stcdb_gb300.pipeline import (QUERY_BOX, QUERY_DTYPE, QUERY_OBJECT, Pipeline, StcConfig, sort_contacts)
 from stcdb_gb300.tracegen import hotspot_grid
 
+from blockfiles import ctb_file, ctf_file, layout
 from parity import trace_and_box
 
 pytestmark = pytest.mark.gpu
-
-HERE = os.path.dirname(os.path.abspath(__file__))
-
-
-def _layout():
-    lay = {}
-    for line in open(os.path.join(HERE, "golden", "ref_layout.txt")):
-        name, off, size = line.split()
-        lay[name] = (int(off), int(size))
-    return lay
-
-
-def _put(buf, off, value, dtype):
-    a = np.asarray(value, dtype=dtype).tobytes()
-    buf[off:off + len(a)] = a
-
-
-def _ctf_file(ctf, bitmap, lay):
-    """CTF::dump_meta: the CTF object (pointers 0) then its bitmap."""
-    size = lay["CTF"][0]
-    b = bytearray(size)
-    _put(b, lay["CTF.ctf_mbr"][0], ctf["mbr"], "<f4")
-    for f in ("kv_count", "start_time_min", "start_time_max", "end_time_min", "end_time_max"):
-        name = "CTF_kv_capacity" if f == "kv_count" else f
-        _put(b, lay["CTF." + name][0], ctf[f], "<u4")
-    _put(b, lay["CTF.ctf_bitmap_size"][0], ctf["bitmap_bytes"], "<u4")
-    for f in ("key_bit", "id_bit", "duration_bit", "end_bit", "low_x_bit", "low_y_bit", "edge_bit", "mbr_bit",
-              "x_grid", "y_grid"):
-        _put(b, lay["CTF." + f][0], ctf[f], "<u2")
-    return bytes(b) + bitmap[: int(ctf["bitmap_bytes"])].tobytes()
-
-
-def _ctb_file(info, blk, lay):
-    """workbench::dump_CTB_meta after straight_dump: the CTB object (pointers,
-    CTF_count and its own times 0), sids, oversize keys, boxes, map bitmap."""
-    b = bytearray(lay["CTB"][0])
-    ob = lay["CTB.o_buffer"][0]
-    _put(b, ob + lay["oversize_buffer.oversize_kv_count"][0], info.oversize_kv_count, "<u4")
-    for f in ("start_time_min", "start_time_max", "end_time_min", "end_time_max"):
-        _put(b, ob + lay["oversize_buffer." + f][0], getattr(info, "o_" + f), "<u4")
-    return (bytes(b) + blk["sids"].astype("<u2").tobytes() + blk["oversize_keys"].astype("<u8").tobytes() +
-            blk["oversize_boxes"].astype("<f4").tobytes() + blk["oversize_bitmap"].tobytes())
 
 
 def _run(tmp_path):
@@ -86,7 +45,7 @@ def test_block_files_are_the_references_bytes_and_load_back(built_cuda, tmp_path
     cfg, mbr, pipe, blocks, xy0 = _run(tmp_path)
     try:
         assert len(blocks) >= 2
-        lay = _layout()
+        lay = layout()
         info, blk = blocks[-1]
         idx = int(info.index)
         d = str(tmp_path)
@@ -94,13 +53,13 @@ def test_block_files_are_the_references_bytes_and_load_back(built_cuda, tmp_path
         for c in range(int(info.ctf_count)):
             ctf = blk["ctfs"][c]
             meta = open(os.path.join(d, f"6oversize_3600_STcL{idx}-{c}"), "rb").read()
-            assert meta == _ctf_file(ctf, blk["bitmaps"][c * 8192:(c + 1) * 8192], lay), f"CTF {c} meta"
+            assert meta == ctf_file(ctf, blk["bitmaps"][c * 8192:(c + 1) * 8192], lay), f"CTF {c} meta"
             kb = int(ctf["key_bit"]) // 8
             o, n = int(ctf["key_offset"]), int(ctf["kv_count"]) * kb
             keys = open(os.path.join(d, f"6oversize_3600_SSTable_{idx}-{c}"), "rb").read()
             assert keys == blk["keys"][o:o + n].tobytes(), f"CTF {c} keys"
         ctb = open(os.path.join(d, f"6oversize_3600_CTB{idx}"), "rb").read()
-        assert ctb == _ctb_file(info, blk, lay)
+        assert ctb == ctb_file(info, blk, lay)
 
         # a fresh context loads the files and answers as the flushing one
         rng = np.random.default_rng(4)
