@@ -187,7 +187,8 @@ typedef struct stc_ctf {
 } stc_ctf;
 
 typedef struct stc_ctb_info {
-  uint32_t index;                /* blocks flushed before this one */
+  uint32_t index;                /* block number: flushes and compactions number their
+                                    blocks 0, 1, 2, ... in the order they make them */
   uint32_t ctf_count;
   uint32_t flush_time;           /* step after which it was flushed (end_time_max) */
   uint32_t end_time_min;         /* base of the keys' end field */
@@ -290,10 +291,47 @@ stc_status stc_query_batch(stc_ctx *ctx, const stc_query *queries, size_t nq, st
  * the reference's loaders (workbench::load_CTB_meta, load_CTF_keys) read them.
  * stc_load_ctb reads such files (written here or by the reference; its key
  * files must be gathered into dir) into a retained block for queries, as
- * block `index`. Like stc_step, neither may run concurrently with stc_step on
+ * block `index`; the block has as many CTFs as consecutive <prefix>_STcL
+ * files exist from CTF 0 (a compacted block may have more or fewer than
+ * ctf_count). Like stc_step, neither may run concurrently with stc_step on
  * the same context. Errors: stc_last_error(ctx). */
 stc_status stc_write_ctb(stc_ctx *ctx, uint32_t index, const char *dir, const char *prefix);
 stc_status stc_load_ctb(stc_ctx *ctx, uint32_t index, const char *dir, const char *prefix);
+
+/* ---- Any retained block --------------------------------------------------
+ *
+ * stc_get_block / stc_read_block: stc_get_ctb / stc_read_ctb for retained
+ * block `index` (a flushed, loaded or compacted one), same layout. */
+stc_status stc_get_block(stc_ctx *ctx, uint32_t index, stc_ctb_info *info);
+stc_status stc_read_block(stc_ctx *ctx, uint32_t index, stc_ctf *ctfs, uint8_t *bitmaps, uint8_t *keys,
+                          uint16_t *sids, uint64_t *oversize_keys, float *oversize_boxes, uint8_t *oversize_bitmap);
+
+/* ---- Compaction ------------------------------------------------------------
+ *
+ * Merges retained block first_index and the count - 1 blocks retained after it
+ * (oldest first) into one block of split * split CTFs (1 <= split <= 63),
+ * which replaces them in the retained list under a new index (*new_index);
+ * queries then search the merged block. This is the reference's merge_dump
+ * (tools/compaction.cpp:729-1206): every CTF key is decoded (CTF::parse_key,
+ * CTF::new_parse_mbr_f_box), each object's keys are sorted by target, the
+ * objects are re-partitioned by STR over the midpoints of their key boxes
+ * into split x split sids, every CTF gets its box, time limits, bit widths
+ * (CTF::get_ctf_bits), bitmap and re-packed keys, and the oversize buffers are
+ * merged in key order with one map bitmap. Where merge_dump loses or corrupts
+ * keys this does not: every key of the inputs is in the result (the STR
+ * object merge_dump leaves without a CTF, :931-942, gets one; no CTF is padded
+ * with object 0's keys, :925-929; decoded oids are masked to id_bit, as
+ * CTF::ctf_get_key_oid does), an object oversize in any input stays oversize,
+ * CTF end times are the merged blocks' with key ends stored relative to
+ * end_time_min (end_bit grows when the merged span needs it), and oversize
+ * ends are re-based to the merged buffer's end_time_min. Objects with equal
+ * midpoints are ordered by pid and one object's keys by (target, duration,
+ * end), orders merge_dump leaves unspecified. The merge allocates its own
+ * scratch (about 100 bytes per merged key). *device_ms (may be NULL): device
+ * time of the merge. Call between steps; queries may run meanwhile on other
+ * threads. Errors: stc_last_error(ctx). */
+stc_status stc_compact(stc_ctx *ctx, uint32_t first_index, uint32_t count, uint32_t split, uint32_t *new_index,
+                       float *device_ms);
 
 /* ---- Checkpoint / restore ------------------------------------------------
  *

@@ -36,6 +36,7 @@ CU_SOURCES = [
     "stc_lsm.cu",
     "stc_query.cu",
     "stc_tracegen.cu",
+    "stc_compact.cu",
 ]
 
 

@@ -655,6 +655,47 @@ extern "C" stc_status stc_write_ctb(stc_ctx *c, uint32_t index, const char *dir,
   return st;
 }
 
+extern "C" stc_status stc_get_block(stc_ctx *c, uint32_t index, stc_ctb_info *info) {
+  if (!c) return STC_ERR_INVALID_ARG;
+  if (!info) return fail(c, STC_ERR_INVALID_ARG, "stc_get_block: null info");
+  std::string err;
+  stc_status st = lsm_block_info(c->lsmh, index, info, err);
+  if (st != STC_OK) c->err = "stc_get_block: " + err;
+  return st;
+}
+
+extern "C" stc_status stc_read_block(stc_ctx *c, uint32_t index, stc_ctf *ctfs, uint8_t *bitmaps, uint8_t *keys,
+                                     uint16_t *sids, uint64_t *oversize_keys, float *oversize_boxes,
+                                     uint8_t *oversize_bitmap) {
+  if (!c) return STC_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  std::string err;
+  stc_status st = lsm_read_block(c->lsmh, index, c->p.N, ctfs, bitmaps, keys, sids, oversize_keys, oversize_boxes,
+                                 oversize_bitmap, err);
+  if (st != STC_OK) c->err = "stc_read_block: " + err;
+  return st;
+}
+
+extern "C" stc_status stc_compact(stc_ctx *c, uint32_t first_index, uint32_t count, uint32_t split,
+                                  uint32_t *new_index, float *device_ms) {
+  if (!c) return STC_ERR_INVALID_ARG;
+  if (!c->lsm_on) return fail(c, STC_ERR_INVALID_ARG, "stc_compact: the memtable is off (kv_restriction 0)");
+  if (c->failed) return STC_ERR_STATE;
+  cudaSetDevice(c->device);
+  std::string err;
+  float ms = 0.0f;
+  const uint32_t idx = c->lsmh.next_index;
+  stc_status st = lsm_compact(c->lsm, c->lsmh, first_index, count, split, idx, c->stream, &ms, err);
+  if (st != STC_OK) {
+    c->err = "stc_compact: " + err;
+    return st;
+  }
+  c->lsmh.next_index++;
+  if (new_index) *new_index = idx;
+  if (device_ms) *device_ms = ms;
+  return STC_OK;
+}
+
 extern "C" stc_status stc_load_ctb(stc_ctx *c, uint32_t index, const char *dir, const char *prefix) {
   if (!c) return STC_ERR_INVALID_ARG;
   if (!dir || !prefix) return fail(c, STC_ERR_INVALID_ARG, "stc_load_ctb: null path");
@@ -689,7 +730,7 @@ struct CkptHeader {
   double map[4];
   uint32_t N, S, G, F;
   unsigned long long B, E, lsm_cap;
-  uint32_t last_t, stepped, lsm_on, lsm_end_time_min, lsm_flushes, pad1;
+  uint32_t last_t, stepped, lsm_on, lsm_end_time_min, lsm_flushes, lsm_next_index;
   stc_stats stats;
   DevState st;
 };
@@ -768,6 +809,7 @@ extern "C" stc_status stc_checkpoint(stc_ctx *c, const char *path) {
   h.lsm_on = c->lsm_on;
   h.lsm_end_time_min = c->lsm_on ? c->lsm.end_time_min : 0;
   h.lsm_flushes = c->lsmh.flushes;
+  h.lsm_next_index = c->lsmh.next_index;
   h.stats = c->stats;
   h.st = *c->st_host;
   FILE *f = fopen(path, "wb");
@@ -871,6 +913,7 @@ extern "C" stc_status stc_restore(const char *path, uint32_t device, stc_ctx **o
   if (c->lsm_on) {
     c->lsm.end_time_min = h.lsm_end_time_min;
     c->lsmh.flushes = h.lsm_flushes;
+    c->lsmh.next_index = std::max(h.lsm_flushes, h.lsm_next_index);
   }
   *out = c;
   return STC_OK;

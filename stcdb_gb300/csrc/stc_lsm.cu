@@ -8,37 +8,11 @@
 #include <cmath>
 #include <cstring>
 
-#include "stc_lsm.cuh"
+#include "stc_lsm_kernels.cuh"
 
 namespace stc {
 
-namespace {
-
-inline unsigned nblk(size_t n, unsigned t = 256) { return (unsigned)std::max<size_t>((n + t - 1) / t, 1); }
-
-// Smallest b >= 1 with v < 2^b.
-inline uint32_t bits_for(unsigned long long v) {
-  uint32_t b = 1;
-  while (b < 64 && (v >> b)) b++;
-  return b;
-}
-
-constexpr unsigned GRID = STC_NUM_SMS * 8;  // grid-stride kernels over keys
-constexpr uint32_t OBOX_INIT = 100000000u;  // uint_box initial low (geometry/geometry.h:320-324)
-
-// float_to_uint / uint_to_float (cuda/cuda_util.cuh:116-125)
-__device__ __forceinline__ uint32_t f2u_ref(float xy) {
-  return __float2uint_rz(__fmul_rn(__fadd_rn(xy, 180.0f), 100000.0f));
-}
-__device__ __forceinline__ float u2f_ref(uint32_t f) {
-  return __fsub_rn(__fdiv_rn(__uint2float_rn(f), 100000.0f), 180.0f);
-}
-
-__device__ __forceinline__ uint32_t warp_max_u32(uint32_t v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
+namespace lsmk {
 
 // ---- memtable --------------------------------------------------------------
 
@@ -213,8 +187,6 @@ __global__ void k_make_sid(LsmDev L, const uint32_t *oids, const uint32_t *jv, u
 // duration, end): the CTF keys by their 128-bit key sid:12 | pid:26 |
 // target:26 | duration:32 | end:32 (cuda/geometry.cu:724-726, 799-806),
 // then the oversize keys by theirs (sid 0).
-enum WordKind : int { W_END_DUR, W_END, W_DUR, W_TARGET, W_SID_PID, W_PID, W_SID, W_OVER };
-
 __global__ void k_lsm_word(LsmDev L, unsigned long long K, const uint32_t *perm, uint32_t *keys, uint32_t *vals,
                            int kind, uint32_t shift) {
   for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < K;
@@ -245,8 +217,6 @@ __global__ void k_lsm_gather(LsmDev L, unsigned long long K, const uint32_t *per
     L.bbox[i] = L.box[src];
   }
 }
-
-constexpr uint32_t LIM_PARTS = 32;  // blocks per CTF in k_lsm_limits
 
 __global__ void k_lsm_limits_init(LsmDev L) {
   uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -316,10 +286,6 @@ __global__ void k_lsm_limits(LsmDev L, unsigned long long K) {
   }
 }
 
-__device__ __forceinline__ uint32_t d2u_cell(double v) {
-  return __double2uint_rz(v);
-}
-
 // get_o_limit and cuda_write_o_bitmap (cuda/geometry.cu:935-1010): start
 // times of the oversize keys and the 256 x 256 map bitmap of their boxes (in
 // double, relative to the map box). Cells past the bitmap are skipped.
@@ -355,21 +321,6 @@ __global__ void k_lsm_oversize(LsmDev L, unsigned long long a, unsigned long lon
     atomicMax(&L.st->lsm_os_max, smax);
   }
 }
-
-// serialize_mbr (cuda/geometry.cu:161-171)
-__device__ __forceinline__ unsigned long long serialize_mbr_dev(float4 b, const stc_ctf &c) {
-  float wx = __fsub_rn(c.mbr[2], c.mbr[0]), wy = __fsub_rn(c.mbr[3], c.mbr[1]);
-  float le = fmaxf(wx, wy);
-  float fx = __ull2float_rn((1ull << c.low_x_bit) - 1), fy = __ull2float_rn((1ull << c.low_y_bit) - 1);
-  float fe = __ull2float_rn((1ull << c.edge_bit) - 1);
-  unsigned long long low0 = __float2ull_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.x, c.mbr[0]), wx), fx));
-  unsigned long long low1 = __float2ull_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.y, c.mbr[1]), wy), fy));
-  unsigned long long x = __float2ull_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.z, b.x), le), fe));
-  unsigned long long y = __float2ull_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.w, b.y), le), fe));
-  return (low0 << (c.low_y_bit + 2 * c.edge_bit)) + (low1 << (2 * c.edge_bit)) + (x << c.edge_bit) + y;
-}
-
-constexpr uint32_t MAX_CTF = 3969;  // 63^2: sids 2..3970 fit the 12-bit sid field
 
 // cuda_write_bitmap (cuda/geometry.cu:957-987) and write_key_and_mbr
 // (:1062-1098) per key of the CTF ranges. The pid field keeps the sid above
@@ -421,12 +372,14 @@ __global__ void k_lsm_encode(LsmDev L, unsigned long long total, unsigned long l
   }
 }
 
-stc_status cuda_err(cudaError_t e, const char *where, std::string &err) {
+}  // namespace lsmk
+
+using namespace lsmk;
+
+static stc_status cuda_err(cudaError_t e, const char *where, std::string &err) {
   err = std::string(where) + ": " + cudaGetErrorString(e);
   return STC_ERR_CUDA;
 }
-
-}  // namespace
 
 // ---- host ------------------------------------------------------------------
 
@@ -493,8 +446,8 @@ void lsm_append(const PipeDev &p, const LsmDev &L, cudaStream_t s) {
 }
 
 // Stable sort of n (key, value) words; returns the buffers holding the result.
-static void sort_words(const LsmDev &L, const uint32_t *k, const uint32_t *v, uint32_t *ko, uint32_t *vo,
-                       uint32_t *kt, uint32_t *vt, int count_slot, size_t n, uint32_t bits, cudaStream_t s) {
+void lsmk::sort_words(const LsmDev &L, const uint32_t *k, const uint32_t *v, uint32_t *ko, uint32_t *vo,
+                      uint32_t *kt, uint32_t *vt, int count_slot, size_t n, uint32_t bits, cudaStream_t s) {
   radix_sort_u32(k, v, ko, vo, kt, vt, L.n_dev + count_slot, n, (int)bits, L.hist, L.scan, s);
 }
 
@@ -614,7 +567,7 @@ stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState
   // 8. keep the sids of the block; empty the memtable
   cudaMemcpyAsync(L.bsid, L.sid, (size_t)N * sizeof(uint16_t), cudaMemcpyDeviceToDevice, s);
   stc_ctb_info in{};
-  in.index = H.flushes;
+  in.index = H.next_index;
   in.ctf_count = F;
   in.flush_time = t;
   in.end_time_min = L.end_time_min;
@@ -633,6 +586,7 @@ stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState
   H.info = in;
   H.has_block = true;
   H.flushes++;
+  H.next_index++;
   L.end_time_min = t;  // straight_dump: the next block starts at the flush step (process.cpp:271)
   return STC_OK;
 }

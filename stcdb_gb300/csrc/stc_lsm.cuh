@@ -100,6 +100,7 @@ struct QueryRec {
 struct LsmHost {
   bool has_block = false;
   uint32_t flushes = 0;
+  uint32_t next_index = 0;         // index of the next block a flush or compaction makes
   stc_ctb_info info{};
   std::vector<stc_ctf> ctfs;
   // retained blocks (oldest first) and the query state
@@ -145,8 +146,30 @@ stc_status lsm_write_block(LsmHost &H, uint32_t index, uint32_t num_objects, con
 stc_status lsm_load_block(const LsmDev &L, LsmHost &H, uint32_t index, const std::string &dir,
                           const std::string &prefix, cudaStream_t s, std::string &err);
 
+// Retained block `index`: its description, and copies of its arrays in the
+// layout of stc_read_ctb (any pointer may be null).
+stc_status lsm_block_info(LsmHost &H, uint32_t index, stc_ctb_info *info, std::string &err);
+stc_status lsm_read_block(LsmHost &H, uint32_t index, uint32_t num_objects, stc_ctf *ctfs, uint8_t *bitmaps,
+                          uint8_t *keys, uint16_t *sids, uint64_t *okeys, float *oboxes, uint8_t *obitmap,
+                          std::string &err);
+
 // Frees the retained blocks and the query buffers.
 void lsm_release(LsmHost &H);
+
+// Frees the device arrays of one block.
+void free_block(CtbBlock &B);
+
+// Builds the cell index of block B (its keys, device CTF records and host CTF
+// copies must be in place), sorting with L's radix-sort scratch.
+cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s);
+
+// Merges the retained block `first_index` and the count - 1 blocks retained
+// after it into one block of split x split CTFs (the reference's merge_dump,
+// tools/compaction.cpp:729-1206), which takes their place in the retained
+// list under index new_index. L supplies the configuration (objects,
+// max_meet_time, map); the merge allocates its own scratch. ms: device time.
+stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32_t count, uint32_t split,
+                       uint32_t new_index, cudaStream_t s, float *ms, std::string &err);
 
 // Runs a batch of queries over the retained blocks on H.qstream (see
 // stc_query_batch in include/stc.h).

@@ -434,7 +434,7 @@ cudaError_t grow(T **p, size_t *cap, size_t need) {
 
 }  // namespace
 
-static void free_block(CtbBlock &B) {
+void free_block(CtbBlock &B) {
   for (void *v : {(void *)B.keys, (void *)B.d_ctfs, (void *)B.bitmaps, (void *)B.sids, (void *)B.orec,
                   (void *)B.obox, (void *)B.obitmap, (void *)B.perm, (void *)B.cstart, (void *)B.cbase})
     if (v) cudaFree(v);
@@ -452,9 +452,7 @@ static void free_block(CtbBlock &B) {
 
 static void retain_block(LsmHost &H, CtbBlock &&B);
 
-// Cell index of block B (its keys, device CTF records and host CTF copies
-// must be in place), sorted with L's radix-sort scratch.
-static cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
+cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
   const uint32_t F = (uint32_t)B.ctfs.size();
   std::vector<uint32_t> cbase(F + 1, 0);
   unsigned long long total = 0;
@@ -777,9 +775,66 @@ stc_status lsm_write_block(LsmHost &H, uint32_t index, uint32_t N, const std::st
   return STC_OK;
 }
 
+stc_status lsm_block_info(LsmHost &H, uint32_t index, stc_ctb_info *info, std::string &err) {
+  std::shared_lock<std::shared_mutex> lock(H.blocks_mu);
+  for (const CtbBlock &b : H.blocks)
+    if (b.info.index == index) {
+      *info = b.info;
+      return STC_OK;
+    }
+  err = "block " + std::to_string(index) + " is not retained";
+  return STC_ERR_INVALID_ARG;
+}
+
+stc_status lsm_read_block(LsmHost &H, uint32_t index, uint32_t N, stc_ctf *ctfs, uint8_t *bitmaps, uint8_t *keys,
+                          uint16_t *sids, uint64_t *okeys, float *oboxes, uint8_t *obitmap, std::string &err) {
+  std::shared_lock<std::shared_mutex> lock(H.blocks_mu);
+  const CtbBlock *B = nullptr;
+  for (const CtbBlock &b : H.blocks)
+    if (b.info.index == index) B = &b;
+  if (!B) {
+    err = "block " + std::to_string(index) + " is not retained";
+    return STC_ERR_INVALID_ARG;
+  }
+  const stc_ctb_info &in = B->info;
+  const size_t no = (size_t)in.oversize_kv_count;
+  if (ctfs) memcpy(ctfs, B->ctfs.data(), B->ctfs.size() * sizeof(stc_ctf));
+  cudaError_t e = cudaSuccess;
+  if (bitmaps) e = cudaMemcpy(bitmaps, B->bitmaps, (size_t)in.ctf_count * STC_BITMAP_BYTES, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && keys && in.key_bytes) e = cudaMemcpy(keys, B->keys, in.key_bytes, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && sids) e = cudaMemcpy(sids, B->sids, (size_t)N * 2, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && obitmap) e = cudaMemcpy(obitmap, B->obitmap, STC_BITMAP_BYTES, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && oboxes && no) e = cudaMemcpy(oboxes, B->obox, no * sizeof(float4), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && okeys && no) {
+    std::vector<uint4> orec(no);
+    e = cudaMemcpy(orec.data(), B->orec, no * sizeof(uint4), cudaMemcpyDeviceToHost);
+    for (size_t i = 0; e == cudaSuccess && i < no; i++) {
+      okeys[2 * i] = ((uint64_t)orec[i].z << 32) | orec[i].w;
+      okeys[2 * i + 1] = ((uint64_t)orec[i].x << 26) | orec[i].y;
+    }
+  }
+  if (e != cudaSuccess) {
+    err = std::string("reading the block: ") + cudaGetErrorString(e);
+    return STC_ERR_CUDA;
+  }
+  return STC_OK;
+}
+
 stc_status lsm_load_block(const LsmDev &L, LsmHost &H, uint32_t index, const std::string &dir,
                           const std::string &prefix, cudaStream_t s, std::string &err) {
-  const uint32_t F = L.F, N = L.N;
+  const uint32_t N = L.N;
+  // the block's CTFs: the consecutive CTF meta files from CTF 0
+  uint32_t F = 0;
+  while (F < 3969u) {
+    FILE *f = fopen(ctb_path(dir, prefix, "_STcL", index, F).c_str(), "rb");
+    if (!f) break;
+    fclose(f);
+    F++;
+  }
+  if (F == 0) {
+    err = "no CTF files " + ctb_path(dir, prefix, "_STcL", index, 0);
+    return STC_ERR_INVALID_ARG;
+  }
   std::vector<uint8_t> ctb;
   std::string pc = ctb_path(dir, prefix, "_CTB", index, -1);
   if (!read_file(pc, ctb) || ctb.size() < REF_CTB_BYTES) {
@@ -876,6 +931,7 @@ stc_status lsm_load_block(const LsmDev &L, LsmHost &H, uint32_t index, const std
     return e == cudaErrorMemoryAllocation ? STC_ERR_CAPACITY : STC_ERR_CUDA;
   }
   retain_block(H, std::move(B));
+  H.next_index = std::max(H.next_index, index + 1);
   return STC_OK;
 }
 

@@ -229,6 +229,13 @@ def _lib():
         lib.stc_get_ctb.restype = ctypes.c_int
         lib.stc_read_ctb.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 7
         lib.stc_read_ctb.restype = ctypes.c_int
+        lib.stc_get_block.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(StcCtbInfo)]
+        lib.stc_get_block.restype = ctypes.c_int
+        lib.stc_read_block.argtypes = [ctypes.c_void_p, ctypes.c_uint32] + [ctypes.c_void_p] * 7
+        lib.stc_read_block.restype = ctypes.c_int
+        lib.stc_compact.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                    ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_float)]
+        lib.stc_compact.restype = ctypes.c_int
         lib.stc_query_batch.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                         ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
         lib.stc_query_batch.restype = ctypes.c_int
@@ -315,6 +322,28 @@ class Pipeline:
         self._check(self._lib.stc_read_ctb(self._h, *[b[k].ctypes.data for k in (
             "ctfs", "bitmaps", "keys", "sids", "oversize_keys", "oversize_boxes", "oversize_bitmap")]))
         return info, ctb_trim(info, b)
+
+    def block_info(self, index: int) -> StcCtbInfo:
+        """Description of retained block `index`."""
+        info = StcCtbInfo()
+        self._check(self._lib.stc_get_block(self._h, index, ctypes.byref(info)))
+        return info
+
+    def read_block(self, index: int) -> tuple:
+        """(info, dict of host arrays) of retained block `index`."""
+        info = self.block_info(index)
+        b = ctb_buffers(info, self.cfg.num_objects)
+        self._check(self._lib.stc_read_block(self._h, index, *[b[k].ctypes.data for k in (
+            "ctfs", "bitmaps", "keys", "sids", "oversize_keys", "oversize_boxes", "oversize_bitmap")]))
+        return info, ctb_trim(info, b)
+
+    def compact(self, first_index: int, count: int, split: int) -> tuple:
+        """Merges retained block first_index and the count - 1 after it into
+        one block of split * split CTFs; returns (its index, device ms)."""
+        idx = ctypes.c_uint32()
+        ms = ctypes.c_float()
+        self._check(self._lib.stc_compact(self._h, first_index, count, split, ctypes.byref(idx), ctypes.byref(ms)))
+        return int(idx.value), float(ms.value)
 
     def query_batch(self, queries: np.ndarray, with_counts: bool = False):
         """Runs a batch (QUERY_DTYPE array); returns a list of CONTACT_DTYPE
