@@ -32,7 +32,7 @@ enum {
   ERR_LOOKUP = 8,      // border lookup stack overflow
   ERR_BUILD = 9,       // initial quadtree build exceeded capacity
   ERR_MEMTABLE = 10,   // memtable full
-  ERR_COMPACT = 11,    // a key to compact names an object outside the configuration
+  ERR_COMPACT = 11,    // a key to compact lies outside its CTF or names an unknown object
 };
 
 // One meeting-table slot (32 B; the reference's meeting_unit of

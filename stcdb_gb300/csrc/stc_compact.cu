@@ -109,6 +109,10 @@ __global__ void k_cmp_decode(const InCtf *ic, uint32_t nc, unsigned long long nk
     }
     const stc_ctf &t = ic[lo].ctf;
     const uint32_t kb = t.key_bit / 8u;
+    if (kid - ic[lo].first >= t.kv_count) {  // outside every CTF: never read past its keys
+      stc_set_error(st, ERR_COMPACT, lo);
+      continue;
+    }
     unsigned __int128 k = load_packed(ic[lo].keys + (kid - ic[lo].first) * kb, kb);
     unsigned long long vm = (unsigned long long)(k & (unsigned __int128)mask64(t.mbr_bit));
     k >>= t.mbr_bit;
@@ -323,7 +327,10 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
   unsigned long long nk = 0, no = 0;
   uint32_t etm = 0xFFFFFFFFu, etmax = 0, o_etm = 0xFFFFFFFFu, o_etmax = 0, flush_max = 0, nc = 0;
   for (const CtbBlock *b : in) {
-    nk += b->info.ctf_kv_count;
+    // the keys of the CTF files: the flush's CTF ranges can differ from its
+    // count of CTF keys (they reach into the oversize keys, as the
+    // reference's do), and merge_dump reads each CTF's kv_count keys (:796)
+    for (const stc_ctf &t : b->ctfs) nk += t.kv_count;
     no += b->info.oversize_kv_count;
     etm = std::min(etm, b->info.end_time_min);
     etmax = std::max(etmax, b->info.flush_time);
@@ -423,7 +430,7 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
     return STC_ERR_CUDA;
   }
   if (st.error) {
-    err = "compact: a decoded key names an object outside the configuration";
+    err = "compact: a key to merge is outside its CTF or names an object outside the configuration";
     return STC_ERR_INVALID_ARG;
   }
   const uint32_t n_str = st.work_next;
