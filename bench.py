@@ -231,9 +231,20 @@ def run_gpu(args, w, rank, local):
     queries = None
     if args.query_rate > 0:
         queries = serve_under_ingest(args, pipe, hnp, W + 2 * K, K, N, mbr)
+    # compaction: the serving steps' keys become a second block; both merge
+    # into one block of split x split CTFs (100 CTFs, as a flush makes)
+    compaction = None
+    if pipe.flush():
+        b0, b1 = pipe.block_info(info.index), pipe.ctb_info()
+        keys_in = int(b0.kv_count) + int(b1.kv_count)
+        new, cms = pipe.compact(int(info.index), 2, 10)
+        out = pipe.block_info(new)
+        compaction = dict(blocks=2, keys=keys_in, split=10, ms=cms, keys_per_s=keys_in / (cms / 1e3),
+                          out_ctf_keys=int(out.ctf_kv_count), out_oversize_keys=int(out.oversize_kv_count))
     pipe.close()
     return dict(stats=stats, dev_ms=dev_ms, wall_dev=wall_dev, wall_e2e=wall_e2e, e2e_stats=e2e_stats,
-                d2h=d2h, clocks=clk.summary(), flush=flush, queries=queries, trace_gen=trace_gen)
+                d2h=d2h, clocks=clk.summary(), flush=flush, queries=queries, trace_gen=trace_gen,
+                compaction=compaction)
 
 
 def make_queries(rng, n, N, mbr, t_now):
@@ -357,6 +368,18 @@ def flush_line(f, peak):
                 frac_of_peak=gbs / peak)
 
 
+def compaction_line(c, peak):
+    """Merge throughput; algorithmic bytes 2 x 32 per merged key (read and
+    write each key and its box once)."""
+    if not c:
+        return None
+    b = 64.0 * c["keys"]
+    c = dict(c)
+    c.update(algorithmic_bytes=b, achieved_gbs=b / (c["ms"] / 1e3) / 1e9,
+             frac_of_peak=b / (c["ms"] / 1e3) / 1e9 / peak)
+    return c
+
+
 def cpu_baseline(w, steps, threads, sample_note):
     import oracle
     from stcdb_gb300.tracegen import TraceGenerator
@@ -455,6 +478,7 @@ def main():
         "flush": flush_line(r["flush"], peak),
         "queries_under_ingest": r["queries"],
         "trace_gen": r["trace_gen"],
+        "compaction": compaction_line(r["compaction"], peak),
         "per_step": {"pair_tests": s_last.pair_tests, "exact_tests": s_last.exact_tests, "hits": s_last.hits,
                      "new_candidates": s_last.new_candidates, "live_meetings": s_last.taken_buckets,
                      "emitted": s_last.emitted, "border_units": s_last.border_units, "leaves": s_last.leaves,
