@@ -53,9 +53,17 @@ struct LsmDev {
   uint8_t *kbytes;                 // packed CTF keys (16 * cap bytes)
 };
 
-// Keys spanning more than this many bitmap cells in x or y go to their CTF's
-// wide list instead of the cell of their low corner.
-constexpr uint32_t LSM_INDEX_SPAN = 2;
+// Spatial index of a block's CTF keys (query pruning; not part of the
+// reference's format). Each CTF gets its own grid of g x g cells over its box,
+// g = sqrt(keys / LSM_INDEX_KEYS_PER_CELL) clamped to [LSM_INDEX_MIN_GRID,
+// LSM_INDEX_MAX_GRID]; a key is filed under the cell of the low corner of its
+// decoded box, or in the CTF's wide list when the box spans more than
+// LSM_INDEX_SPAN cells in x or y. The largest span of the filed keys is kept
+// per CTF, so a query widens its window by exactly that much.
+constexpr uint32_t LSM_INDEX_SPAN = 16;
+constexpr uint32_t LSM_INDEX_KEYS_PER_CELL = 8;
+constexpr uint32_t LSM_INDEX_MIN_GRID = 16;
+constexpr uint32_t LSM_INDEX_MAX_GRID = 256;
 
 // Device copy of one flushed block, kept for queries.
 struct CtbBlock {
@@ -68,11 +76,14 @@ struct CtbBlock {
   uint4 *orec = nullptr;           // oversize keys (pid, target, duration, end offset), sorted
   float4 *obox = nullptr;
   uint32_t *obitmap = nullptr;     // [2048]
-  // spatial index of the CTF keys: per CTF, dense cells (x_grid + 1) x
-  // (y_grid + 1) of the low corner of each key's box, then one wide slot
+  // spatial index of the CTF keys: per CTF, dense cells (gx + 1) x (gy + 1)
+  // of the low corner of each key's box, then one wide slot
   uint32_t *perm = nullptr;        // block key positions sorted by dense cell id
   uint32_t *cstart = nullptr;      // [ncells + 1] first position of each cell in perm
   uint32_t *cbase = nullptr;       // [F + 1] first dense cell id of each CTF
+  uint4 *ixg = nullptr;            // [F] (gx, gy, largest x span, largest y span) in cells
+  uint16_t *pend = nullptr;        // [keys] end offset of the key at each perm position, saturated at
+                                   // 65535; within a cell the keys go by increasing end
 };
 
 // A retained block as the query kernels see it.
@@ -87,6 +98,8 @@ struct QBlock {
   const uint32_t *perm;
   const uint32_t *cstart;
   const uint32_t *cbase;
+  const uint4 *ixg;
+  const uint16_t *pend;
   unsigned long long n_over;
   uint32_t F, index, o_end_time_min, pad;
 };

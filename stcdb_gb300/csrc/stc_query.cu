@@ -24,7 +24,7 @@ namespace {
 
 constexpr uint32_t QOBJ_THREADS = 128;
 constexpr uint32_t QBOX_THREADS = 128;
-constexpr uint32_t QBOX_PARTS = 8;
+constexpr uint32_t QBOX_PARTS = 2;
 
 struct Key {
   uint32_t oid, target, duration, end;
@@ -263,11 +263,13 @@ __device__ __forceinline__ void cell_range(double a, double b, double m0, double
 constexpr uint32_t MAX_CTF = 3969;
 
 // Dense cell id of each CTF key: the cell of the low corner of its decoded
-// box in its CTF's bitmap grid, or the CTF's wide slot when the box spans
-// more than LSM_INDEX_SPAN cells. A decoded box meeting a query box then has
-// its low-corner cell inside the query's cell window extended by the span.
+// box in its CTF's index grid, or the CTF's wide slot when the box spans more
+// than LSM_INDEX_SPAN cells; the largest span of the filed keys goes to
+// ixg[c].z / .w. A decoded box meeting a query box then has its low-corner
+// cell inside the query's cell window extended by that span.
 __global__ void k_index_cells(const uint8_t *keys, const stc_ctf *ctfs, uint32_t F, const uint32_t *cbase,
-                              unsigned long long total, uint32_t *cells, uint32_t *pos) {
+                              uint4 *ixg, unsigned long long total, uint32_t *cells, uint32_t *pos,
+                              uint32_t *endo) {
   __shared__ unsigned long long s_first[MAX_CTF + 1];
   for (uint32_t c = threadIdx.x; c < F; c += blockDim.x) s_first[c] = ctfs[c].first_key;
   __syncthreads();
@@ -283,24 +285,40 @@ __global__ void k_index_cells(const uint8_t *keys, const stc_ctf *ctfs, uint32_t
     const uint32_t kb = t.key_bit / 8u;
     Key k;
     decode_key(load_key(keys + t.key_offset + (kid - s_first[lo]) * kb, kb), t, k);
-    const uint32_t nx = t.x_grid + 1u, ny = t.y_grid + 1u;
-    bool narrow = false;
+    const uint32_t gx = ixg[lo].x, gy = ixg[lo].y, nx = gx + 1u, ny = gy + 1u;
     uint32_t cell = nx * ny;
     if (t.mbr[2] > t.mbr[0] && t.mbr[3] > t.mbr[1]) {
-      double fx0 = grid_coord(k.box[0], t.mbr[0], t.mbr[2], t.x_grid);
-      double fx1 = grid_coord(k.box[2], t.mbr[0], t.mbr[2], t.x_grid);
-      double fy0 = grid_coord(k.box[1], t.mbr[1], t.mbr[3], t.y_grid);
-      double fy1 = grid_coord(k.box[3], t.mbr[1], t.mbr[3], t.y_grid);
+      double fx0 = grid_coord(k.box[0], t.mbr[0], t.mbr[2], gx);
+      double fx1 = grid_coord(k.box[2], t.mbr[0], t.mbr[2], gx);
+      double fy0 = grid_coord(k.box[1], t.mbr[1], t.mbr[3], gy);
+      double fy1 = grid_coord(k.box[3], t.mbr[1], t.mbr[3], gy);
       if (fx0 >= 0 && fy0 >= 0 && fx0 < nx && fy0 < ny && fx1 >= fx0 && fy1 >= fy0) {
         uint32_t l0 = (uint32_t)floor(fx0), l1 = (uint32_t)floor(fy0);
-        double h0 = floor(fx1), h1 = floor(fy1);
-        narrow = h0 - l0 <= LSM_INDEX_SPAN && h1 - l1 <= LSM_INDEX_SPAN;
-        if (narrow) cell = l1 * nx + l0;
+        double ex = floor(fx1) - l0, ey = floor(fy1) - l1;
+        if (ex <= LSM_INDEX_SPAN && ey <= LSM_INDEX_SPAN) {
+          cell = l1 * nx + l0;
+          const uint32_t sx = (uint32_t)ex, sy = (uint32_t)ey;
+          if (sx > __ldcg(&ixg[lo].z)) atomicMax(&ixg[lo].z, sx);
+          if (sy > __ldcg(&ixg[lo].w)) atomicMax(&ixg[lo].w, sy);
+        }
       }
     }
     cells[kid] = cbase[lo] + cell;
     pos[kid] = (uint32_t)kid;
+    endo[kid] = min(k.end, 65535u);
   }
+}
+
+__global__ void k_gather_cells(const uint32_t *src, const uint32_t *idx, uint32_t *dst, unsigned long long n) {
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x)
+    dst[i] = src[idx[i]];
+}
+
+__global__ void k_gather_ends(const uint32_t *endo, const uint32_t *perm, uint16_t *pend, unsigned long long n) {
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x)
+    pend[i] = (uint16_t)endo[perm[i]];
 }
 
 // cstart[k] = first position of the sorted cell ids holding an id >= k.
@@ -366,55 +384,110 @@ __global__ void __launch_bounds__(QBOX_THREADS) k_query_box(const QBlock *qb, ui
   const double wide[4] = {qbox[0] - qx, qbox[1] - qy, qbox[2] + qx, qbox[3] + qy};
   const double ctfb[4] = {t.mbr[0], t.mbr[1], t.mbr[2], t.mbr[3]};
   if (!box_hits(ctfb, wide)) return;
-  if (count_only) {
+  // Time conditions that hold for every key of the CTF: no time field can
+  // have outgrown its bit width (decoded = stored times), and then every
+  // start is below t_end, or every end above t_start (ends are >= the
+  // block's base).
+  const bool fits = (unsigned long long)(t.end_time_max - t.end_time_min) <= mask64(t.end_bit) &&
+                    (unsigned long long)(t.end_time_max - t.start_time_min) <= mask64(t.duration_bit) &&
+                    t.start_time_min <= t.end_time_max && t.end_time_min <= t.end_time_max;
+  const bool all_starts = fits && t.start_time_max < q.t_end;
+  const bool all_ends = fits && q.t_start < t.end_time_min;
+  // end offsets above ts pass t_start < end (ts < 65535: the saturated
+  // offsets of the index order them exactly)
+  const uint32_t ts = all_ends ? 0u : q.t_start - t.end_time_min;
+  if (count_only && all_starts && all_ends) {
     // Every key matches -- count the CTF without decoding it, as the
     // reference's box search does (workbench.cpp:525-528) -- when the query
-    // holds the CTF box widened by the quantisation, every start is below
-    // t_end, every end above t_start (ends are >= the block's base), and no
-    // time field can have outgrown its bit width (decoded = stored times).
+    // also holds the CTF box widened by the quantisation.
     const bool inside = qbox[0] <= ctfb[0] - qx && qbox[1] <= ctfb[1] - qy && qbox[2] >= ctfb[2] + qx &&
                         qbox[3] >= ctfb[3] + qy;
-    const bool times = t.start_time_max < q.t_end && q.t_start < t.end_time_min;
-    const bool fits = (unsigned long long)(t.end_time_max - t.end_time_min) <= mask64(t.end_bit) &&
-                      (unsigned long long)(t.end_time_max - t.start_time_min) <= mask64(t.duration_bit) &&
-                      t.start_time_min <= t.end_time_max && t.end_time_min <= t.end_time_max;
-    if (inside && times && fits) {
+    if (inside) {
       if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&qcounts[qi], (unsigned long long)t.kv_count);
       return;
     }
   }
+  {
+    int bi0, bi1, bj0, bj1;  // the bitmap's cells
+    cell_range(wide[0], wide[2], t.mbr[0], t.mbr[2], t.x_grid, bi0, bi1);
+    cell_range(wide[1], wide[3], t.mbr[1], t.mbr[3], t.y_grid, bj0, bj1);
+    if (!any_bit(b.bitmaps + (size_t)c * (STC_BITMAP_BYTES / 4), bi0, bi1, bj0, bj1, t.x_grid)) return;
+  }
+  const uint4 g = b.ixg[c];  // the index grid and the largest span of its filed keys
   int i0, i1, j0, j1;
-  cell_range(wide[0], wide[2], t.mbr[0], t.mbr[2], t.x_grid, i0, i1);
-  cell_range(wide[1], wide[3], t.mbr[1], t.mbr[3], t.y_grid, j0, j1);
-  if (!any_bit(b.bitmaps + (size_t)c * (STC_BITMAP_BYTES / 4), i0, i1, j0, j1, t.x_grid)) return;
+  cell_range(wide[0], wide[2], t.mbr[0], t.mbr[2], g.x, i0, i1);
+  cell_range(wide[1], wide[3], t.mbr[1], t.mbr[3], g.y, j0, j1);
+  // Interior cells (counting only, every start passing): cells whose every
+  // decoded low corner lies in the query box. A key's box meets the query
+  // when its low corner is inside it; grid_coord is monotone, so a corner in
+  // cell i (gc in [i, i + 1)) lies in [q_lo, q_hi] when i > gc(q_lo) and
+  // i + 1 <= gc(q_hi). Their keys are counted from the cell index: all of
+  // them when every end passes, else those past a binary search on the ends.
+  int ii0 = 1, ii1 = 0, jj0 = 1, jj1 = 0;  // empty
+  if (count_only && all_starts && (all_ends || ts < 65535u) && t.mbr[2] > t.mbr[0] && t.mbr[3] > t.mbr[1]) {
+    auto interior = [](double g0, double g1, uint32_t n, int &lo, int &hi) {
+      g0 = fmax(fmin(g0, (double)n + 2), -2.0);
+      g1 = fmax(fmin(g1, (double)n + 2), -2.0);
+      lo = max((int)floor(g0) + 1, 0);
+      hi = min((int)floor(g1) - 1, (int)n);
+    };
+    interior(grid_coord(qbox[0], t.mbr[0], t.mbr[2], g.x), grid_coord(qbox[2], t.mbr[0], t.mbr[2], g.x), g.x, ii0,
+             ii1);
+    interior(grid_coord(qbox[1], t.mbr[1], t.mbr[3], g.y), grid_coord(qbox[3], t.mbr[1], t.mbr[3], g.y), g.y, jj0,
+             jj1);
+  }
   // Spatial index: a key whose exact box meets the widened query has its low
-  // corner at most LSM_INDEX_SPAN cells left of / below the query's first
+  // corner at most the CTF's largest span left of / below the query's first
   // cell (cell_range already holds one cell of slack), or is in the wide
   // list. One warp per row segment of low-corner cells.
   const uint32_t kb = t.key_bit / 8u;
   const uint8_t *base = b.keys + t.key_offset;
-  const uint32_t nx = t.x_grid + 1u, ny = t.y_grid + 1u, cb = b.cbase[c];
-  const int li0 = max(i0 - (int)LSM_INDEX_SPAN, 0), lj0 = max(j0 - (int)LSM_INDEX_SPAN, 0);
+  const uint32_t nx = g.x + 1u, ny = g.y + 1u, cb = b.cbase[c];
+  const int li0 = max(i0 - (int)g.z, 0), lj0 = max(j0 - (int)g.w, 0);
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, nw = blockDim.x >> 5;
   const int rows = max(j1 - lj0 + 1, 0);  // the wide list is r == rows
   for (int r = (int)(blockIdx.x * nw + warp); r <= rows; r += (int)(QBOX_PARTS * nw)) {
-    uint32_t a, e;
+    uint32_t a, e, ma, me2;  // scan [a, ma) and [me2, e); [ma, me2) is counted
     if (r < rows) {  // row lj0 + r, cells li0..i1
-      const uint32_t row = (uint32_t)(lj0 + r) * nx;
+      const int jr = lj0 + r;
+      const uint32_t row = (uint32_t)jr * nx;
       a = b.cstart[cb + row + (uint32_t)li0];
       e = b.cstart[cb + row + (uint32_t)i1 + 1];
+      ma = me2 = a;
+      const int lo = max(ii0, li0), hi = min(ii1, i1);
+      if (jr >= jj0 && jr <= jj1 && lo <= hi) {
+        ma = b.cstart[cb + row + (uint32_t)lo];
+        me2 = b.cstart[cb + row + (uint32_t)hi + 1];
+        if (all_ends) {
+          if (lane == 0) mine += me2 - ma;
+        } else {
+          for (int ci = lo + (int)lane; ci <= hi; ci += 32) {
+            uint32_t x = b.cstart[cb + row + (uint32_t)ci], y = b.cstart[cb + row + (uint32_t)ci + 1];
+            const uint32_t n = y;
+            while (x < y) {  // first key of the cell with end offset > ts
+              uint32_t mid = (x + y) >> 1;
+              if (__ldg(&b.pend[mid]) <= ts) x = mid + 1;
+              else y = mid;
+            }
+            mine += n - x;
+          }
+        }
+      }
     } else {  // the wide list
       a = b.cstart[cb + nx * ny];
       e = b.cstart[cb + nx * ny + 1];
+      ma = me2 = a;
     }
-    for (uint32_t p = a + lane; p < e; p += 32) {
-      const unsigned long long local = (unsigned long long)b.perm[p] - t.first_key;
-      Key k;
-      decode_key(load_key(base + local * kb, kb), t, k);
-      uint32_t end = k.end + t.end_time_min, start = end - k.duration;
-      if (time_ok(start, end, q.t_start, q.t_end) && box_hits(k.box, qbox)) {
-        mine++;
-        if (!count_only) emit(out, cap, count, qi, k.oid, k.target, start, end, k.box, b.index, c);
+    for (int seg = 0; seg < 2; seg++) {
+      for (uint32_t p = (seg ? me2 : a) + lane, pe = seg ? e : ma; p < pe; p += 32) {
+        const unsigned long long local = (unsigned long long)b.perm[p] - t.first_key;
+        Key k;
+        decode_key(load_key(base + local * kb, kb), t, k);
+        uint32_t end = k.end + t.end_time_min, start = end - k.duration;
+        if (time_ok(start, end, q.t_start, q.t_end) && box_hits(k.box, qbox)) {
+          mine++;
+          if (!count_only) emit(out, cap, count, qi, k.oid, k.target, start, end, k.box, b.index, c);
+        }
       }
     }
   }
@@ -436,8 +509,11 @@ cudaError_t grow(T **p, size_t *cap, size_t need) {
 
 void free_block(CtbBlock &B) {
   for (void *v : {(void *)B.keys, (void *)B.d_ctfs, (void *)B.bitmaps, (void *)B.sids, (void *)B.orec,
-                  (void *)B.obox, (void *)B.obitmap, (void *)B.perm, (void *)B.cstart, (void *)B.cbase})
+                  (void *)B.obox, (void *)B.obitmap, (void *)B.perm, (void *)B.cstart, (void *)B.cbase,
+                  (void *)B.ixg, (void *)B.pend})
     if (v) cudaFree(v);
+  B.ixg = nullptr;
+  B.pend = nullptr;
   B.keys = nullptr;
   B.d_ctfs = nullptr;
   B.bitmaps = nullptr;
@@ -455,28 +531,42 @@ static void retain_block(LsmHost &H, CtbBlock &&B);
 cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
   const uint32_t F = (uint32_t)B.ctfs.size();
   std::vector<uint32_t> cbase(F + 1, 0);
+  std::vector<uint4> ixg(F);
   unsigned long long total = 0;
   for (uint32_t c = 0; c < F; c++) {
-    cbase[c + 1] = cbase[c] + ((uint32_t)B.ctfs[c].x_grid + 1) * ((uint32_t)B.ctfs[c].y_grid + 1) + 1;
-    total = std::max<unsigned long long>(total, B.ctfs[c].first_key + B.ctfs[c].kv_count);
+    const stc_ctf &t = B.ctfs[c];
+    uint32_t g = (uint32_t)std::ceil(std::sqrt((double)t.kv_count / LSM_INDEX_KEYS_PER_CELL));
+    g = std::min(std::max(g, LSM_INDEX_MIN_GRID), LSM_INDEX_MAX_GRID);
+    ixg[c] = make_uint4(g, g, 0u, 0u);
+    cbase[c + 1] = cbase[c] + (g + 1) * (g + 1) + 1;
+    total = std::max<unsigned long long>(total, t.first_key + t.kv_count);
   }
   const uint32_t ncells = cbase[F];
   if (total > lsm_sort_words(L)) return cudaErrorInvalidValue;  // more keys than the sort scratch holds
   cudaError_t e = cudaMalloc(&B.perm, std::max<unsigned long long>(total, 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&B.cstart, ((size_t)ncells + 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&B.cbase, (F + 1) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&B.ixg, std::max<size_t>(F, 1) * sizeof(uint4));
   if (e == cudaSuccess) e = cudaMemcpyAsync(B.cbase, cbase.data(), (F + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(B.ixg, ixg.data(), F * sizeof(uint4), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return e;
+  if (e == cudaSuccess) e = cudaMalloc(&B.pend, std::max<unsigned long long>(total, 1) * sizeof(uint16_t));
   if (e != cudaSuccess) return e;
   uint32_t *const *sk = L.sk;
   if (total) {
     int bits = 1;
     while (bits < 32 && ((unsigned long long)ncells >> bits)) bits++;
+    // keys by (cell, end offset): stable sorts by end, then by cell
     STC_KL k_set_one<<<1, 1, 0, s>>>(L.n_dev + 3, total);
-    STC_KL k_index_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(B.keys, B.d_ctfs, F, B.cbase, total, sk[0], sk[1]);
-    radix_sort_u32(sk[0], sk[1], sk[2], B.perm, sk[4], sk[5], L.n_dev + 3, (size_t)total, bits, L.hist, L.scan, s);
+    STC_KL k_index_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(B.keys, B.d_ctfs, F, B.cbase, B.ixg, total, sk[0], sk[1],
+                                                         sk[6]);
+    radix_sort_u32(sk[6], sk[1], sk[2], sk[3], sk[4], sk[5], L.n_dev + 3, (size_t)total, 16, L.hist, L.scan, s);
+    STC_KL k_gather_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[0], sk[3], sk[4], total);
+    radix_sort_u32(sk[4], sk[3], sk[2], B.perm, sk[0], sk[5], L.n_dev + 3, (size_t)total, bits, L.hist, L.scan, s);
+    STC_KL k_gather_ends<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[6], B.perm, B.pend, total);
   }
   STC_KL k_cell_starts<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[2], total, ncells, B.cstart);
-  e = cudaStreamSynchronize(s);  // the copy of cbase reads this stack frame
+  e = cudaStreamSynchronize(s);  // the copies of cbase and ixg read this stack frame
   return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
@@ -571,7 +661,8 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
   uint32_t maxF = 0;
   for (uint32_t i = 0; i < nb; i++) {
     const CtbBlock &B = H.blocks[i];
-    qb[i] = QBlock{B.keys, B.d_ctfs, B.sids, B.orec, B.obox, B.bitmaps, B.obitmap, B.perm, B.cstart, B.cbase,
+    qb[i] = QBlock{B.keys, B.d_ctfs, B.sids, B.orec, B.obox, B.bitmaps, B.obitmap, B.perm, B.cstart, B.cbase, B.ixg,
+                   B.pend,
                    (unsigned long long)B.info.oversize_kv_count, B.info.ctf_count, B.info.index,
                    B.info.o_end_time_min, 0};
     maxF = std::max(maxF, B.info.ctf_count);

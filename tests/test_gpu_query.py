@@ -63,7 +63,9 @@ def _queries(rng, blocks, mbr, n_obj, n_box):
         if j == 0:
             qs[i]["box"] = mbr
         else:
-            side = 10 ** rng.uniform(-4.3, -1.6)  # about 5 m to 2.5 km
+            # about 5 m to 2.5 km; every fifth one 250 m to 5 km, so that some
+            # counted queries cover whole cells of the index
+            side = 10 ** (rng.uniform(-2.5, -1.3) if j % 5 == 4 else rng.uniform(-4.3, -1.6))
             x, y = mbr[0] + rng.random() * (W - side), mbr[1] + rng.random() * (H - side)
             qs[i]["box"] = (x, y, x + side, y + side * 0.8)
         if j % 2:
