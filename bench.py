@@ -76,12 +76,12 @@ def make_trace_cfg(w, seed):
     return uniform_grid(w["objects"], seed=seed)
 
 
-def make_cfg(w, device=0):
+def make_cfg(w, device=0, step_slices=0):
     from stcdb_gb300.pipeline import StcConfig
     b = w.get("buckets") or w["buckets_per_object"] * w["objects"]
     return StcConfig(num_objects=w["objects"], reach_distance=w["reach"], min_meet_time=w["min_meet"],
                      grid_capacity=w["grid_capacity"], grid_amplify=w["amplify"], num_meeting_buckets=b,
-                     device=device, kv_restriction=w["kv_restriction"])
+                     device=device, kv_restriction=w["kv_restriction"], step_slices=step_slices)
 
 
 class ClockSampler:
@@ -186,7 +186,7 @@ def run_gpu(args, w, rank, local):
     trace_gen = {"steps": W + K, "ms": gen_ms, "ms_per_step": gen_ms / (W + K),
                  "positions_per_s": N * (W + K) / (gen_ms / 1e3),
                  "written_gb_s": 16.0 * N * (W + K) / (gen_ms / 1e3) / 1e9}
-    cfg = make_cfg(w, device=local)
+    cfg = make_cfg(w, device=local, step_slices=args.step_slices)
     pipe = Pipeline(cfg, mbr, dev[0].cpu().numpy())
     # warm-up steps (device-resident input)
     for t in range(W):
@@ -409,6 +409,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--query-rate", type=float, default=20000.0,
                     help="Poisson query arrivals per second during the serving phase (0: skip)")
+    ap.add_argument("--step-slices", type=int, default=0,
+                    help="launches per long step kernel (stc_config.step_slices; 0 = 1)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()

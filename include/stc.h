@@ -86,7 +86,9 @@ typedef struct stc_config {
                                     goes to the oversize buffer (process.cpp:408-411); 0 = 100, no cut */
   uint32_t ctb_retain;           /* flushed blocks kept on the device for queries; the oldest is
                                     dropped beyond this; 0 = 8 */
-  uint32_t reserved;
+  uint32_t step_slices;          /* launches each long step kernel (pair tests, table update,
+                                    sweep) is cut into, so that queries running on another thread
+                                    get the GPU between them; results do not change; 0 = 1 */
 } stc_config;
 
 /* Replay quadtree splits/merges on one device thread only (tests compare it

@@ -263,6 +263,7 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
   p.grid_capacity = k.grid_capacity;
   p.delay = k.schema_update_delay;
   p.mbr_filter = k.mbr_filter;
+  p.slices = std::min<uint32_t>(std::max<uint32_t>(k.step_slices, 1u), 64u);
 
   size_t nu = std::max<size_t>(n, p.U_cap);
   size_t scan_words = scan_tmp_words(std::max<size_t>({(size_t)n, (size_t)p.G + 1, (size_t)p.S,

@@ -54,16 +54,22 @@ struct LsmDev {
 };
 
 // Spatial index of a block's CTF keys (query pruning; not part of the
-// reference's format). Each CTF gets its own grid of g x g cells over its box,
-// g = sqrt(keys / LSM_INDEX_KEYS_PER_CELL) clamped to [LSM_INDEX_MIN_GRID,
-// LSM_INDEX_MAX_GRID]; a key is filed under the cell of the low corner of its
-// decoded box, or in the CTF's wide list when the box spans more than
-// LSM_INDEX_SPAN cells in x or y. The largest span of the filed keys is kept
-// per CTF, so a query widens its window by exactly that much.
-constexpr uint32_t LSM_INDEX_SPAN = 16;
+// reference's format). Each CTF gets a loose multi-level grid over its box:
+// level 0 has g x g cells, g a power of two near sqrt(keys /
+// LSM_INDEX_KEYS_PER_CELL) in [LSM_INDEX_MIN_GRID, LSM_INDEX_MAX_GRID], and
+// level k has cells 2^k times larger. A key is filed at the first level
+// whose cells are at least as large as its decoded box's extent in level-0
+// cells, under the cell of the box's low corner; so at its level the box
+// ends at most one cell right of / above that cell, and a query widens its
+// window by one cell per level. Keys whose corner falls outside the grid go
+// to the CTF's wide list. Within a cell keys go by end time.
 constexpr uint32_t LSM_INDEX_KEYS_PER_CELL = 8;
 constexpr uint32_t LSM_INDEX_MIN_GRID = 16;
 constexpr uint32_t LSM_INDEX_MAX_GRID = 256;
+
+// Cells of one level of the index: (g >> k) + 1 per side (the last holds
+// corners exactly on the CTF box's high edge).
+__host__ __device__ inline uint32_t index_level_side(uint32_t g, uint32_t k) { return (g >> k) + 1u; }
 
 // Device copy of one flushed block, kept for queries.
 struct CtbBlock {
@@ -81,7 +87,7 @@ struct CtbBlock {
   uint32_t *perm = nullptr;        // block key positions sorted by dense cell id
   uint32_t *cstart = nullptr;      // [ncells + 1] first position of each cell in perm
   uint32_t *cbase = nullptr;       // [F + 1] first dense cell id of each CTF
-  uint4 *ixg = nullptr;            // [F] (gx, gy, largest x span, largest y span) in cells
+  uint4 *ixg = nullptr;            // [F] (g, levels, 0, 0) of each CTF's index
   uint16_t *pend = nullptr;        // [keys] end offset of the key at each perm position, saturated at
                                    // 65535; within a cell the keys go by increasing end
 };

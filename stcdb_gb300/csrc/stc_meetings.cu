@@ -188,16 +188,17 @@ __device__ __forceinline__ void flush_emits(const PipeDev &p, const stc_meeting 
   __syncwarp();
 }
 
-__global__ void __launch_bounds__(SWEEP_THREADS, 6) k_sweep(PipeDev p, uint32_t t) {
+// Slice `part` of `parts` sweeps slots [B * part / parts, B * (part + 1) / parts).
+__global__ void __launch_bounds__(SWEEP_THREADS, 6) k_sweep(PipeDev p, uint32_t t, uint32_t part, uint32_t parts) {
   __shared__ __align__(16) stc_meeting stage_all[SWEEP_WARPS][WARP_STAGE];
   const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
   stc_meeting *stage = stage_all[warp];
   uint32_t n = 0;  // warp-uniform
   unsigned long long active = 0, fresh = 0, emitted = 0;
-  const unsigned long long B = p.B;
+  const unsigned long long B0 = p.B * part / parts, B = p.B * (part + 1) / parts;
   const unsigned long long gw = (unsigned long long)blockIdx.x * SWEEP_WARPS + warp;
   const unsigned long long nw = (unsigned long long)gridDim.x * SWEEP_WARPS;
-  for (unsigned long long bb = gw * WARP_TILE; bb < B; bb += nw * WARP_TILE) {
+  for (unsigned long long bb = B0 + gw * WARP_TILE; bb < B; bb += nw * WARP_TILE) {
     Slot sl[SWEEP_UNROLL];
     unsigned long long idx[SWEEP_UNROLL];
 #pragma unroll
@@ -244,7 +245,8 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 6) k_sweep(PipeDev p, uint32_t 
 }
 
 void step_sweep(PipeDev &p, uint32_t t, cudaStream_t s) {
-  STC_KL k_sweep<<<STC_NUM_SMS * 6, SWEEP_THREADS, 0, s>>>(p, t);
+  for (uint32_t part = 0; part < p.slices; part++)
+    STC_KL k_sweep<<<STC_NUM_SMS * 6, SWEEP_THREADS, 0, s>>>(p, t, part, p.slices);
 }
 
 }  // namespace stc

@@ -20,6 +20,7 @@ struct PipeDev {
   float fmap_lo_x, fmap_lo_y, fmap_hi_x, fmap_hi_y;  // float f: f >= map_lo <=> f >= fmap_lo, etc.
   uint32_t min_meet_time, grid_capacity, delay;
   int mbr_filter;
+  uint32_t slices;                 // launches per long step kernel (stc_config.step_slices)
   // state
   DevState *st;
   SchemaDev sd;

@@ -24,7 +24,7 @@ namespace {
 
 constexpr uint32_t QOBJ_THREADS = 128;
 constexpr uint32_t QBOX_THREADS = 128;
-constexpr uint32_t QBOX_PARTS = 2;
+constexpr uint32_t QBOX_PARTS = 4;
 
 struct Key {
   uint32_t oid, target, duration, end;
@@ -262,13 +262,11 @@ __device__ __forceinline__ void cell_range(double a, double b, double m0, double
 
 constexpr uint32_t MAX_CTF = 3969;
 
-// Dense cell id of each CTF key: the cell of the low corner of its decoded
-// box in its CTF's index grid, or the CTF's wide slot when the box spans more
-// than LSM_INDEX_SPAN cells; the largest span of the filed keys goes to
-// ixg[c].z / .w. A decoded box meeting a query box then has its low-corner
-// cell inside the query's cell window extended by that span.
+// Dense cell id of each CTF key in its CTF's loose grid (stc_lsm.cuh): the
+// level whose cells cover the extent of its decoded box, the cell of the box's
+// low corner there; or the CTF's wide slot.
 __global__ void k_index_cells(const uint8_t *keys, const stc_ctf *ctfs, uint32_t F, const uint32_t *cbase,
-                              uint4 *ixg, unsigned long long total, uint32_t *cells, uint32_t *pos,
+                              const uint4 *ixg, unsigned long long total, uint32_t *cells, uint32_t *pos,
                               uint32_t *endo) {
   __shared__ unsigned long long s_first[MAX_CTF + 1];
   for (uint32_t c = threadIdx.x; c < F; c += blockDim.x) s_first[c] = ctfs[c].first_key;
@@ -285,24 +283,26 @@ __global__ void k_index_cells(const uint8_t *keys, const stc_ctf *ctfs, uint32_t
     const uint32_t kb = t.key_bit / 8u;
     Key k;
     decode_key(load_key(keys + t.key_offset + (kid - s_first[lo]) * kb, kb), t, k);
-    const uint32_t gx = ixg[lo].x, gy = ixg[lo].y, nx = gx + 1u, ny = gy + 1u;
-    uint32_t cell = nx * ny;
+    const uint32_t g = ixg[lo].x, levels = ixg[lo].y;
+    uint32_t cell = 0xFFFFFFFFu;  // the wide slot, after every level
     if (t.mbr[2] > t.mbr[0] && t.mbr[3] > t.mbr[1]) {
-      double fx0 = grid_coord(k.box[0], t.mbr[0], t.mbr[2], gx);
-      double fx1 = grid_coord(k.box[2], t.mbr[0], t.mbr[2], gx);
-      double fy0 = grid_coord(k.box[1], t.mbr[1], t.mbr[3], gy);
-      double fy1 = grid_coord(k.box[3], t.mbr[1], t.mbr[3], gy);
-      if (fx0 >= 0 && fy0 >= 0 && fx0 < nx && fy0 < ny && fx1 >= fx0 && fy1 >= fy0) {
+      double fx0 = grid_coord(k.box[0], t.mbr[0], t.mbr[2], g);
+      double fx1 = grid_coord(k.box[2], t.mbr[0], t.mbr[2], g);
+      double fy0 = grid_coord(k.box[1], t.mbr[1], t.mbr[3], g);
+      double fy1 = grid_coord(k.box[3], t.mbr[1], t.mbr[3], g);
+      if (fx0 >= 0 && fy0 >= 0 && fx0 < g + 1 && fy0 < g + 1 && fx1 >= fx0 && fy1 >= fy0) {
         uint32_t l0 = (uint32_t)floor(fx0), l1 = (uint32_t)floor(fy0);
-        double ex = floor(fx1) - l0, ey = floor(fy1) - l1;
-        if (ex <= LSM_INDEX_SPAN && ey <= LSM_INDEX_SPAN) {
-          cell = l1 * nx + l0;
-          const uint32_t sx = (uint32_t)ex, sy = (uint32_t)ey;
-          if (sx > __ldcg(&ixg[lo].z)) atomicMax(&ixg[lo].z, sx);
-          if (sy > __ldcg(&ixg[lo].w)) atomicMax(&ixg[lo].w, sy);
+        double ext = fmax(floor(fx1) - l0, floor(fy1) - l1);
+        uint32_t lv = 0, off = 0;
+        while (lv + 1 < levels && ext > (double)(1u << lv)) {
+          uint32_t side = index_level_side(g, lv);
+          off += side * side;
+          lv++;
         }
+        if (ext <= (double)(1u << lv)) cell = off + (l1 >> lv) * index_level_side(g, lv) + (l0 >> lv);
       }
     }
+    if (cell == 0xFFFFFFFFu) cell = cbase[lo + 1] - cbase[lo] - 1;
     cells[kid] = cbase[lo] + cell;
     pos[kid] = (uint32_t)kid;
     endo[kid] = min(k.end, 65535u);
@@ -413,15 +413,17 @@ __global__ void __launch_bounds__(QBOX_THREADS) k_query_box(const QBlock *qb, ui
     cell_range(wide[1], wide[3], t.mbr[1], t.mbr[3], t.y_grid, bj0, bj1);
     if (!any_bit(b.bitmaps + (size_t)c * (STC_BITMAP_BYTES / 4), bi0, bi1, bj0, bj1, t.x_grid)) return;
   }
-  const uint4 g = b.ixg[c];  // the index grid and the largest span of its filed keys
+  const uint32_t g = b.ixg[c].x, levels = b.ixg[c].y;
+  // the query window in level-0 cells, one cell of slack either side
   int i0, i1, j0, j1;
-  cell_range(wide[0], wide[2], t.mbr[0], t.mbr[2], g.x, i0, i1);
-  cell_range(wide[1], wide[3], t.mbr[1], t.mbr[3], g.y, j0, j1);
-  // Interior cells (counting only, every start passing): cells whose every
-  // decoded low corner lies in the query box. A key's box meets the query
-  // when its low corner is inside it; grid_coord is monotone, so a corner in
-  // cell i (gc in [i, i + 1)) lies in [q_lo, q_hi] when i > gc(q_lo) and
-  // i + 1 <= gc(q_hi). Their keys are counted from the cell index: all of
+  cell_range(wide[0], wide[2], t.mbr[0], t.mbr[2], g, i0, i1);
+  cell_range(wide[1], wide[3], t.mbr[1], t.mbr[3], g, j0, j1);
+  // Interior cells (counting only, every start passing): level-0 cells whose
+  // every decoded low corner lies in the query box. A key's box meets the
+  // query when its low corner is inside it; grid_coord is monotone, so a
+  // corner in cell i (gc in [i, i + 1)) lies in [q_lo, q_hi] when
+  // i > gc(q_lo) and i + 1 <= gc(q_hi). A cell of level k is interior when
+  // all its level-0 cells are. Their keys are counted from the index: all of
   // them when every end passes, else those past a binary search on the ends.
   int ii0 = 1, ii1 = 0, jj0 = 1, jj1 = 0;  // empty
   if (count_only && all_starts && (all_ends || ts < 65535u) && t.mbr[2] > t.mbr[0] && t.mbr[3] > t.mbr[1]) {
@@ -431,52 +433,77 @@ __global__ void __launch_bounds__(QBOX_THREADS) k_query_box(const QBlock *qb, ui
       lo = max((int)floor(g0) + 1, 0);
       hi = min((int)floor(g1) - 1, (int)n);
     };
-    interior(grid_coord(qbox[0], t.mbr[0], t.mbr[2], g.x), grid_coord(qbox[2], t.mbr[0], t.mbr[2], g.x), g.x, ii0,
-             ii1);
-    interior(grid_coord(qbox[1], t.mbr[1], t.mbr[3], g.y), grid_coord(qbox[3], t.mbr[1], t.mbr[3], g.y), g.y, jj0,
-             jj1);
+    interior(grid_coord(qbox[0], t.mbr[0], t.mbr[2], g), grid_coord(qbox[2], t.mbr[0], t.mbr[2], g), g, ii0, ii1);
+    interior(grid_coord(qbox[1], t.mbr[1], t.mbr[3], g), grid_coord(qbox[3], t.mbr[1], t.mbr[3], g), g, jj0, jj1);
   }
-  // Spatial index: a key whose exact box meets the widened query has its low
-  // corner at most the CTF's largest span left of / below the query's first
-  // cell (cell_range already holds one cell of slack), or is in the wide
-  // list. One warp per row segment of low-corner cells.
+  // A key filed at level k under cell (cx, cy) whose box meets the widened
+  // query has cx in [(i0 >> k) - 1, i1 >> k] (its box ends at most one cell
+  // right of cx) and likewise cy: one warp per row segment of each level,
+  // then the wide list.
   const uint32_t kb = t.key_bit / 8u;
   const uint8_t *base = b.keys + t.key_offset;
-  const uint32_t nx = g.x + 1u, ny = g.y + 1u, cb = b.cbase[c];
-  const int li0 = max(i0 - (int)g.z, 0), lj0 = max(j0 - (int)g.w, 0);
+  const uint32_t cb = b.cbase[c], wide_slot = b.cbase[c + 1] - 1u;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, nw = blockDim.x >> 5;
-  const int rows = max(j1 - lj0 + 1, 0);  // the wide list is r == rows
+  int rows = 0;
+  for (uint32_t lv = 0; lv < levels; lv++) {
+    const int side = (int)index_level_side(g, lv);
+    rows += max(min(j1 >> lv, side - 1) - max((j0 >> lv) - 1, 0) + 1, 0);
+  }
   for (int r = (int)(blockIdx.x * nw + warp); r <= rows; r += (int)(QBOX_PARTS * nw)) {
     uint32_t a, e, ma, me2;  // scan [a, ma) and [me2, e); [ma, me2) is counted
-    if (r < rows) {  // row lj0 + r, cells li0..i1
-      const int jr = lj0 + r;
-      const uint32_t row = (uint32_t)jr * nx;
-      a = b.cstart[cb + row + (uint32_t)li0];
-      e = b.cstart[cb + row + (uint32_t)i1 + 1];
+    int clo = 1, chi = 0;    // counted cells of this row (level lv)
+    uint32_t row_base = 0;
+    if (r < rows) {
+      // level and row of work item r
+      uint32_t lv = 0, off = 0;
+      int rr = r, side = 0, cj0 = 0;
+      for (;; lv++) {
+        side = (int)index_level_side(g, lv);
+        cj0 = max((j0 >> lv) - 1, 0);
+        const int n = max(min(j1 >> lv, side - 1) - cj0 + 1, 0);
+        if (rr < n) break;
+        rr -= n;
+        off += (uint32_t)(side * side);
+      }
+      const int jr = cj0 + rr;
+      const int ci0 = max((i0 >> lv) - 1, 0), ci1 = min(i1 >> lv, side - 1);
+      row_base = cb + off + (uint32_t)(jr * side);
+      a = b.cstart[row_base + (uint32_t)ci0];
+      e = b.cstart[row_base + (uint32_t)ci1 + 1];
       ma = me2 = a;
-      const int lo = max(ii0, li0), hi = min(ii1, i1);
-      if (jr >= jj0 && jr <= jj1 && lo <= hi) {
-        ma = b.cstart[cb + row + (uint32_t)lo];
-        me2 = b.cstart[cb + row + (uint32_t)hi + 1];
-        if (all_ends) {
-          if (lane == 0) mine += me2 - ma;
-        } else {
-          for (int ci = lo + (int)lane; ci <= hi; ci += 32) {
-            uint32_t x = b.cstart[cb + row + (uint32_t)ci], y = b.cstart[cb + row + (uint32_t)ci + 1];
-            const uint32_t n = y;
-            while (x < y) {  // first key of the cell with end offset > ts
-              uint32_t mid = (x + y) >> 1;
-              if (__ldg(&b.pend[mid]) <= ts) x = mid + 1;
-              else y = mid;
-            }
-            mine += n - x;
-          }
-        }
+      // interior at this level: cell C covers level-0 cells [C 2^lv, (C + 1) 2^lv - 1]
+      const int s2 = 1 << lv;
+      const int ilo = (ii0 + s2 - 1) >> lv, ihi = ((ii1 + 1) >> lv) - 1;
+      const bool row_in = ii0 <= ii1 && jj0 <= jj1 && jr * s2 >= jj0 && (jr + 1) * s2 - 1 <= jj1;
+      clo = max(ilo, ci0);
+      chi = min(ihi, ci1);
+      if (row_in && clo <= chi) {
+        ma = b.cstart[row_base + (uint32_t)clo];
+        me2 = b.cstart[row_base + (uint32_t)chi + 1];
+      } else {
+        clo = 1;
+        chi = 0;
       }
     } else {  // the wide list
-      a = b.cstart[cb + nx * ny];
-      e = b.cstart[cb + nx * ny + 1];
+      a = b.cstart[wide_slot];
+      e = b.cstart[wide_slot + 1];
       ma = me2 = a;
+    }
+    if (clo <= chi) {
+      if (all_ends) {
+        if (lane == 0) mine += me2 - ma;
+      } else {
+        for (int ci = clo + (int)lane; ci <= chi; ci += 32) {
+          uint32_t x = b.cstart[row_base + (uint32_t)ci], y = b.cstart[row_base + (uint32_t)ci + 1];
+          const uint32_t n = y;
+          while (x < y) {  // first key of the cell with end offset > ts
+            uint32_t mid = (x + y) >> 1;
+            if (__ldg(&b.pend[mid]) <= ts) x = mid + 1;
+            else y = mid;
+          }
+          mine += n - x;
+        }
+      }
     }
     for (int seg = 0; seg < 2; seg++) {
       for (uint32_t p = (seg ? me2 : a) + lane, pe = seg ? e : ma; p < pe; p += 32) {
@@ -535,10 +562,13 @@ cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
   unsigned long long total = 0;
   for (uint32_t c = 0; c < F; c++) {
     const stc_ctf &t = B.ctfs[c];
-    uint32_t g = (uint32_t)std::ceil(std::sqrt((double)t.kv_count / LSM_INDEX_KEYS_PER_CELL));
-    g = std::min(std::max(g, LSM_INDEX_MIN_GRID), LSM_INDEX_MAX_GRID);
-    ixg[c] = make_uint4(g, g, 0u, 0u);
-    cbase[c + 1] = cbase[c] + (g + 1) * (g + 1) + 1;
+    const double want = std::sqrt((double)t.kv_count / LSM_INDEX_KEYS_PER_CELL);
+    uint32_t g = LSM_INDEX_MIN_GRID, levels = 1, cells = 1;  // the wide slot
+    while (g < LSM_INDEX_MAX_GRID && g < want) g *= 2;
+    while ((1u << (levels - 1)) < g) levels++;  // down to one cell of the whole box
+    for (uint32_t lv = 0; lv < levels; lv++) cells += index_level_side(g, lv) * index_level_side(g, lv);
+    ixg[c] = make_uint4(g, levels, 0u, 0u);
+    cbase[c + 1] = cbase[c] + cells;
     total = std::max<unsigned long long>(total, t.first_key + t.kv_count);
   }
   const uint32_t ncells = cbase[F];
@@ -559,7 +589,7 @@ cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
     // keys by (cell, end offset): stable sorts by end, then by cell
     STC_KL k_set_one<<<1, 1, 0, s>>>(L.n_dev + 3, total);
     STC_KL k_index_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(B.keys, B.d_ctfs, F, B.cbase, B.ixg, total, sk[0], sk[1],
-                                                         sk[6]);
+                                                         sk[6]);  // ixg copied above on this stream
     radix_sort_u32(sk[6], sk[1], sk[2], sk[3], sk[4], sk[5], L.n_dev + 3, (size_t)total, 16, L.hist, L.scan, s);
     STC_KL k_gather_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[0], sk[3], sk[4], total);
     radix_sort_u32(sk[4], sk[3], sk[2], B.perm, sk[0], sk[5], L.n_dev + 3, (size_t)total, bits, L.hist, L.scan, s);

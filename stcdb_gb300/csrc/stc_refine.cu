@@ -173,10 +173,13 @@ __device__ __forceinline__ HitRec load_hit(const HitRec *r) {
 
 // One thread per hit, two hits in flight per thread: both records and both
 // home slots are requested before either is used.
-__global__ void __launch_bounds__(256) k_hits(PipeDev p, uint32_t t) {
-  const unsigned long long nh = p.st->hit_count < p.hit_cap ? p.st->hit_count : p.hit_cap;
+// Slice `part` of `parts` covers hits [nh * part / parts, nh * (part + 1) / parts).
+__global__ void __launch_bounds__(256) k_hits(PipeDev p, uint32_t t, uint32_t part, uint32_t parts) {
+  const unsigned long long nt = p.st->hit_count < p.hit_cap ? p.st->hit_count : p.hit_cap;
+  const unsigned long long h0i = nt * part / parts, nh = nt * (part + 1) / parts;
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < nh; i += 2 * stride) {
+  for (unsigned long long i = h0i + (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < nh;
+       i += 2 * stride) {
     unsigned long long i2 = i + stride;
     HitRec h0 = load_hit(&p.hits[i]);
     HitRec h1;
@@ -332,7 +335,10 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
   }
 }
 
-__global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint32_t t) {
+// Slice `part` of `parts` runs job chunks [C * part / parts, C * (part + 1) / parts)
+// of the C = ceil(jobs / JOB_CHUNK) chunks.
+__global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint32_t t, uint32_t part,
+                                                                 uint32_t parts) {
   __shared__ HitRec queues[REFINE_THREADS / 32][QCAP];
   __shared__ ColTile cols[REFINE_THREADS / 32];
   HitRec *q = queues[threadIdx.x >> 5];
@@ -342,8 +348,10 @@ __global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint3
   const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
   const unsigned long long J = p.st->jobs_total;
+  const unsigned long long nchunks = (J + JOB_CHUNK - 1) / JOB_CHUNK;
+  const unsigned long long c0 = nchunks * part / parts, c1 = nchunks * (part + 1) / parts;
   Counters ct = {0, 0, 0, 0};
-  for (unsigned long long chunk = warp; chunk * JOB_CHUNK < J; chunk += nwarps) {
+  for (unsigned long long chunk = c0 + warp; chunk < c1; chunk += nwarps) {
     // one lane reads the flag so that the whole warp leaves together
     if (__shfl_sync(0xffffffffu, (int)stc_failed(p.st), 0)) break;
     unsigned long long j0 = chunk * JOB_CHUNK;
@@ -398,8 +406,9 @@ __global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint3
 }
 
 void step_refine(PipeDev &p, uint32_t t, cudaStream_t s) {
-  STC_KL k_refine_a<<<STC_NUM_SMS * 8, REFINE_THREADS, 0, s>>>(p, t);
-  STC_KL k_hits<<<STC_NUM_SMS * 16, 256, 0, s>>>(p, t);
+  for (uint32_t part = 0; part < p.slices; part++)
+    STC_KL k_refine_a<<<STC_NUM_SMS * 8, REFINE_THREADS, 0, s>>>(p, t, part, p.slices);
+  for (uint32_t part = 0; part < p.slices; part++) STC_KL k_hits<<<STC_NUM_SMS * 16, 256, 0, s>>>(p, t, part, p.slices);
 }
 
 }  // namespace stc

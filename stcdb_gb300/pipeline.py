@@ -53,7 +53,7 @@ class _Config(ctypes.Structure):
         ("start_time", ctypes.c_uint32),
         ("area_restriction", ctypes.c_double),
         ("ctb_retain", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("step_slices", ctypes.c_uint32),
     ]
 
 
@@ -187,7 +187,7 @@ class StcConfig:
     start_time: int = 0
     area_restriction: float = 0.0  # 0 = 100 (no cut)
     ctb_retain: int = 0       # flushed blocks kept for queries; 0 = 8
-    reserved: int = 0
+    step_slices: int = 0      # launches per long step kernel (query latency under ingest); 0 = 1
 
     def resolved(self) -> "StcConfig":
         if self.num_meeting_buckets == 0:

@@ -13,15 +13,16 @@ pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-@pytest.mark.parametrize("name,flags", [("c1_uniform_100k", 0), ("uniform_20k_small", 0), ("hotspot_30k", 0),
-                                        ("hotspot_30k", FLAG_SERIAL_SCHEMA)])
-def test_gpu_matches_reference(built_cuda, name, flags):
+@pytest.mark.parametrize("name,flags,slices", [("c1_uniform_100k", 0, 0), ("uniform_20k_small", 0, 0),
+                                               ("hotspot_30k", 0, 0), ("hotspot_30k", FLAG_SERIAL_SCHEMA, 0),
+                                               ("hotspot_30k", 0, 5)])
+def test_gpu_matches_reference(built_cuda, name, flags, slices):
     from dataclasses import replace
     case = CASES[name]
     fx = dict(np.load(os.path.join(HERE, "golden", name + ".npz")))
     trace, mbr = make_trace(case)
     assert trace_digest(trace) == str(fx["trace_sha256"]), "trace generator differs on this host"
-    cfg = replace(stc_config(case), flags=flags)
+    cfg = replace(stc_config(case), flags=flags, step_slices=slices)
     with Pipeline(cfg, mbr, trace[0]) as p:
         for t in range(case["steps"]):
             p.step(trace[t], t)
