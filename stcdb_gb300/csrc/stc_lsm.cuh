@@ -136,6 +136,10 @@ struct LsmHost {
   unsigned long long *d_count = nullptr;
   unsigned long long *d_qcounts = nullptr;  // per-query match counts
   size_t qc_cap = 0;
+  uint32_t *d_items = nullptr;     // box-query plan: work items per (query, block, CTF), then their scan
+  size_t items_cap = 0;
+  uint32_t *d_iscan = nullptr;     // scan scratch
+  size_t iscan_cap = 0;
   double map[4] = {0, 0, 0, 0};
 };
 

@@ -1,13 +1,11 @@
 // Queries over the retained flushed blocks (the reference's disk searches,
 // with the time window of its time_query; semantics in include/stc.h).
 //
-// A batch of queries is one launch per query kind: object queries get one
-// CTA per (block, query): the object's sid picks the oversize buffer or a
-// CTF, one thread runs the reference's binary search for the first key of
-// the pid and the CTA scans on while the pid matches. Box queries get
-// QBOX_PARTS CTAs per (CTF or oversize buffer, block, query): each first
-// prunes by the CTF box and bitmap (widened so that no key whose decoded box
-// meets the query is lost), then scans its share of the keys. Matches are
+// Object queries get one CTA per (block, query): the object's sid picks the
+// oversize buffer or a CTF, one thread runs the reference's binary search for
+// the first key of the pid and the CTA scans on while the pid matches. Box
+// queries are planned per (query, block, CTF) and run as rows of the blocks'
+// cell indexes, one warp per row (k_box_plan, k_box_rows). Matches are
 // appended to one device buffer tagged with their query; the host groups
 // them by query.
 #include <algorithm>
@@ -24,7 +22,6 @@ namespace {
 
 constexpr uint32_t QOBJ_THREADS = 128;
 constexpr uint32_t QBOX_THREADS = 128;
-constexpr uint32_t QBOX_PARTS = 4;
 
 struct Key {
   uint32_t oid, target, duration, end;
@@ -54,15 +51,8 @@ __device__ __forceinline__ uint32_t key_oid(unsigned __int128 k, const stc_ctf &
   return (uint32_t)((k >> (c.id_bit + c.duration_bit + c.end_bit + c.mbr_bit)) & mask64(c.id_bit));
 }
 
-__device__ void decode_key(unsigned __int128 k, const stc_ctf &c, Key &o) {
-  o.oid = key_oid(k, c);
-  unsigned long long vm = (unsigned long long)(k & (unsigned __int128)mask64(c.mbr_bit));
-  k >>= c.mbr_bit;
-  o.end = (uint32_t)(k & mask64(c.end_bit));
-  k >>= c.end_bit;
-  o.duration = (uint32_t)(k & mask64(c.duration_bit));
-  k >>= c.duration_bit;
-  o.target = (uint32_t)(k & mask64(c.id_bit));
+// The packed box fields of value_mbr in CTF c, decoded (CTF::new_parse_mbr).
+__device__ void exact_box(unsigned long long vm, const stc_ctf &c, double box[4]) {
   unsigned long long me = mask64(c.edge_bit), my = mask64(c.low_y_bit), mx = mask64(c.low_x_bit);
   unsigned long long y = vm & me;
   vm >>= c.edge_bit;
@@ -73,10 +63,67 @@ __device__ void decode_key(unsigned __int128 k, const stc_ctf &c, Key &o) {
   unsigned long long low0 = vm & mx;
   float wx = __fsub_rn(c.mbr[2], c.mbr[0]), wy = __fsub_rn(c.mbr[3], c.mbr[1]);
   double le = (double)fmaxf(wx, wy);
-  o.box[0] = __dadd_rn((double)c.mbr[0], __dmul_rn(__ddiv_rn(__ull2double_rn(low0), __ull2double_rn(mx)), (double)wx));
-  o.box[1] = __dadd_rn((double)c.mbr[1], __dmul_rn(__ddiv_rn(__ull2double_rn(low1), __ull2double_rn(my)), (double)wy));
-  o.box[2] = __dadd_rn(o.box[0], __dmul_rn(__ddiv_rn(__ull2double_rn(x), __ull2double_rn(me)), le));
-  o.box[3] = __dadd_rn(o.box[1], __dmul_rn(__ddiv_rn(__ull2double_rn(y), __ull2double_rn(me)), le));
+  box[0] = __dadd_rn((double)c.mbr[0], __dmul_rn(__ddiv_rn(__ull2double_rn(low0), __ull2double_rn(mx)), (double)wx));
+  box[1] = __dadd_rn((double)c.mbr[1], __dmul_rn(__ddiv_rn(__ull2double_rn(low1), __ull2double_rn(my)), (double)wy));
+  box[2] = __dadd_rn(box[0], __dmul_rn(__ddiv_rn(__ull2double_rn(x), __ull2double_rn(me)), le));
+  box[3] = __dadd_rn(box[1], __dmul_rn(__ddiv_rn(__ull2double_rn(y), __ull2double_rn(me)), le));
+}
+
+// The integer fields of a packed key (CTF::parse_key with the oid masked).
+__device__ __forceinline__ unsigned long long key_fields(unsigned __int128 k, const stc_ctf &c, Key &o) {
+  o.oid = key_oid(k, c);
+  unsigned long long vm = (unsigned long long)(k & (unsigned __int128)mask64(c.mbr_bit));
+  k >>= c.mbr_bit;
+  o.end = (uint32_t)(k & mask64(c.end_bit));
+  k >>= c.end_bit;
+  o.duration = (uint32_t)(k & mask64(c.duration_bit));
+  k >>= c.duration_bit;
+  o.target = (uint32_t)(k & mask64(c.id_bit));
+  return vm;
+}
+
+// Screening of the box test without decode_key's four correctly rounded
+// divisions: the decoded corners computed with reciprocals differ from the
+// exact ones by a few ulp of coordinates below 2^8 degrees (< 1e-12), so a
+// key whose approximate box clears every query edge by BOX_EPS is decided;
+// box_screen returns 1 (meets the query), 0 (misses it) or -1 (decode it).
+constexpr double BOX_EPS = 1e-10;
+struct BoxRecip {
+  double m0, m1, wx, wy, le, rx, ry, re;
+};
+
+__device__ __forceinline__ BoxRecip box_recip(const stc_ctf &c) {
+  BoxRecip r;
+  const float wx = __fsub_rn(c.mbr[2], c.mbr[0]), wy = __fsub_rn(c.mbr[3], c.mbr[1]);
+  r.m0 = c.mbr[0];
+  r.m1 = c.mbr[1];
+  r.wx = wx;
+  r.wy = wy;
+  r.le = (double)fmaxf(wx, wy);
+  r.rx = 1.0 / (double)mask64(c.low_x_bit);
+  r.ry = 1.0 / (double)mask64(c.low_y_bit);
+  r.re = 1.0 / (double)mask64(c.edge_bit);
+  return r;
+}
+
+__device__ __forceinline__ int box_screen(unsigned long long vm, const stc_ctf &c, const BoxRecip &r, const double *q) {
+  const unsigned long long y = vm & mask64(c.edge_bit);
+  vm >>= c.edge_bit;
+  const unsigned long long x = vm & mask64(c.edge_bit);
+  vm >>= c.edge_bit;
+  const unsigned long long low1 = vm & mask64(c.low_y_bit);
+  vm >>= c.low_y_bit;
+  const unsigned long long low0 = vm & mask64(c.low_x_bit);
+  const double b0 = r.m0 + (double)low0 * r.rx * r.wx, b1 = r.m1 + (double)low1 * r.ry * r.wy;
+  const double b2 = b0 + (double)x * r.re * r.le, b3 = b1 + (double)y * r.re * r.le;
+  // box::intersect (geometry/geometry.h:128-133) on closed intervals
+  if (b0 > q[2] + BOX_EPS || b2 < q[0] - BOX_EPS || b1 > q[3] + BOX_EPS || b3 < q[1] - BOX_EPS) return 0;
+  if (b0 < q[2] - BOX_EPS && b2 > q[0] + BOX_EPS && b1 < q[3] - BOX_EPS && b3 > q[1] + BOX_EPS) return 1;
+  return -1;
+}
+
+__device__ void decode_key(unsigned __int128 k, const stc_ctf &c, Key &o) {
+  exact_box(key_fields(k, c, o), c, o.box);
 }
 
 __device__ __forceinline__ bool time_ok(uint32_t start, uint32_t end, uint32_t t1, uint32_t t2) {
@@ -226,20 +273,6 @@ __global__ void __launch_bounds__(QOBJ_THREADS) k_query_object(const QBlock *qb,
 
 // ---- box queries ---------------------------------------------------------------
 
-// Any set bit of a bitmap in cells [i0, i1] x [j0, j1] (bit = i + j * xg,
-// as written by the flush, including its wrap of i = xg into the next row).
-__device__ bool any_bit(const uint32_t *bm, int i0, int i1, int j0, int j1, uint32_t xg) {
-  int found = 0;
-  long long ni = (long long)i1 - i0 + 1, nj = (long long)j1 - j0 + 1;
-  if (ni > 0 && nj > 0) {
-    for (long long k = threadIdx.x; k < ni * nj && !found; k += blockDim.x) {
-      long long bit = (i0 + k % ni) + (j0 + k / ni) * (long long)xg;
-      if (bit >= 0 && bit < 65536 && ((__ldg(&bm[bit >> 5]) >> (bit & 31)) & 1u)) found = 1;
-    }
-  }
-  return __syncthreads_or(found) != 0;
-}
-
 // Position of v on a grid of n cells over [m0, m1], in cells (monotone in v;
 // the cell index and the query windows both use it).
 __device__ __forceinline__ double grid_coord(double v, double m0, double m1, uint32_t n) {
@@ -337,53 +370,62 @@ __global__ void k_cell_starts(const uint32_t *sorted, unsigned long long total, 
 
 __global__ void k_set_one(unsigned long long *p, unsigned long long v) { *p = v; }
 
-__global__ void __launch_bounds__(QBOX_THREADS) k_query_box(const QBlock *qb, uint32_t nb, const stc_query *qs,
-                                                           double m0x, double m0y, double m1x, double m1y,
-                                                           QueryRec *out, unsigned long long cap,
-                                                           unsigned long long *count,
-                                                           unsigned long long *qcounts) {
-  const uint32_t bi = blockIdx.z % nb, qi = blockIdx.z / nb;
-  const QBlock &b = qb[bi];
-  const stc_query q = qs[qi];
-  const uint32_t c = blockIdx.y;
-  if ((q.kind & 0xFFu) != STC_QUERY_BOX || c > b.F) return;
-  const bool count_only = (q.kind & STC_QUERY_COUNT_ONLY) != 0;
-  uint32_t mine = 0;
-  const double *qbox = q.box;
-  if (c == b.F) {
-    // oversize buffer: the map bitmap prunes, float boxes decide
-    if (b.n_over == 0) return;
-    int i0, i1, j0, j1;
-    cell_range(qbox[0], qbox[2], m0x, m1x, 256, i0, i1);
-    cell_range(qbox[1], qbox[3], m0y, m1y, 256, j0, j1);
-    if (!any_bit(b.obitmap, i0, i1, j0, j1, 256)) return;
-    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < b.n_over;
-         i += (unsigned long long)QBOX_PARTS * blockDim.x) {
-      float4 fb = b.obox[i];
-      double box[4] = {fb.x, fb.y, fb.z, fb.w};
-      uint32_t pid, target, start, end;
-      oversize_key(b, i, pid, target, start, end);
-      if (time_ok(start, end, q.t_start, q.t_end) && box_hits(box, qbox)) {
-        mine++;
-        if (!count_only) emit(out, cap, count, qi, pid, target, start, end, box, b.index, c);
-      }
+// ---- box queries: plan, then rows --------------------------------------------
+//
+// A batch's box queries run in three launches. k_box_plan gives every
+// (query, block, CTF or oversize buffer) pair one thread: it prunes by the CTF
+// box and bitmap (widened so that no key whose decoded box meets the query is
+// lost), counts whole CTFs a counting query holds, and writes how many work
+// items the pair needs: one per row of every index level plus the wide list
+// (CTFs), or one per OV_CHUNK oversize keys. An exclusive scan turns the
+// counts into the items' first numbers, and k_box_rows gives each work item
+// one warp, so that big and small queries alike spread over the whole GPU.
+
+constexpr uint32_t OV_CHUNK = 2048;       // oversize keys per work item
+constexpr uint32_t SEQ_BITMAP_CELLS = 1024;  // larger windows skip the per-thread bitmap test
+
+// Any set bit in cells [i0, i1] x [j0, j1] (one thread); windows of more than
+// SEQ_BITMAP_CELLS cells are taken as hit (the bitmap only prunes).
+__device__ bool any_bit_seq(const uint32_t *bm, int i0, int i1, int j0, int j1, uint32_t xg) {
+  long long ni = (long long)i1 - i0 + 1, nj = (long long)j1 - j0 + 1;
+  if (ni <= 0 || nj <= 0) return false;
+  if (ni * nj > SEQ_BITMAP_CELLS) return true;
+  for (long long j = j0; j <= j1; j++)
+    for (long long i = i0; i <= i1; i++) {
+      long long bit = i + j * (long long)xg;
+      if (bit >= 0 && bit < 65536 && ((__ldg(&bm[bit >> 5]) >> (bit & 31)) & 1u)) return true;
     }
-    add_count(qcounts, qi, mine);
-    return;
-  }
-  const stc_ctf &t = b.ctfs[c];
-  if (t.kv_count == 0) return;
+  return false;
+}
+
+// What a box query needs to know about one CTF.
+struct BoxCtx {
+  double wide[4];
+  double qx, qy;
+  bool all_starts, all_ends;
+  uint32_t ts;                 // end offsets above ts pass t_start < end
+  uint32_t g, levels;          // the CTF's index
+  int i0, i1, j0, j1;          // query window in level-0 cells, one cell of slack
+  int ii0, ii1, jj0, jj1;      // interior level-0 cells (counting queries), empty if ii0 > ii1
+};
+
+// Fills x for CTF t and query q; false when the CTF box misses the widened query.
+__device__ bool box_ctx(const stc_ctf &t, const uint4 &ix, const stc_query &q, BoxCtx &x) {
   // A decoded box differs from the key's exact box (which set the CTF box
   // and the bitmap) by less than one corner quantum plus one edge quantum on
   // either side (float conversions truncate, and may round up first): widen
   // the query by that much for the box and bitmap tests.
+  const double *qbox = q.box;
   const float fwx = __fsub_rn(t.mbr[2], t.mbr[0]), fwy = __fsub_rn(t.mbr[3], t.mbr[1]);
   const double le = (double)fmaxf(fwx, fwy), me = (double)mask64(t.edge_bit);
-  const double qx = (double)fwx / (double)mask64(t.low_x_bit) + le / me + 1e-9;
-  const double qy = (double)fwy / (double)mask64(t.low_y_bit) + le / me + 1e-9;
-  const double wide[4] = {qbox[0] - qx, qbox[1] - qy, qbox[2] + qx, qbox[3] + qy};
+  x.qx = (double)fwx / (double)mask64(t.low_x_bit) + le / me + 1e-9;
+  x.qy = (double)fwy / (double)mask64(t.low_y_bit) + le / me + 1e-9;
+  x.wide[0] = qbox[0] - x.qx;
+  x.wide[1] = qbox[1] - x.qy;
+  x.wide[2] = qbox[2] + x.qx;
+  x.wide[3] = qbox[3] + x.qy;
   const double ctfb[4] = {t.mbr[0], t.mbr[1], t.mbr[2], t.mbr[3]};
-  if (!box_hits(ctfb, wide)) return;
+  if (!box_hits(ctfb, x.wide)) return false;
   // Time conditions that hold for every key of the CTF: no time field can
   // have outgrown its bit width (decoded = stored times), and then every
   // start is below t_end, or every end above t_start (ends are >= the
@@ -391,134 +433,201 @@ __global__ void __launch_bounds__(QBOX_THREADS) k_query_box(const QBlock *qb, ui
   const bool fits = (unsigned long long)(t.end_time_max - t.end_time_min) <= mask64(t.end_bit) &&
                     (unsigned long long)(t.end_time_max - t.start_time_min) <= mask64(t.duration_bit) &&
                     t.start_time_min <= t.end_time_max && t.end_time_min <= t.end_time_max;
-  const bool all_starts = fits && t.start_time_max < q.t_end;
-  const bool all_ends = fits && q.t_start < t.end_time_min;
-  // end offsets above ts pass t_start < end (ts < 65535: the saturated
-  // offsets of the index order them exactly)
-  const uint32_t ts = all_ends ? 0u : q.t_start - t.end_time_min;
-  if (count_only && all_starts && all_ends) {
-    // Every key matches -- count the CTF without decoding it, as the
-    // reference's box search does (workbench.cpp:525-528) -- when the query
-    // also holds the CTF box widened by the quantisation.
-    const bool inside = qbox[0] <= ctfb[0] - qx && qbox[1] <= ctfb[1] - qy && qbox[2] >= ctfb[2] + qx &&
-                        qbox[3] >= ctfb[3] + qy;
-    if (inside) {
-      if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&qcounts[qi], (unsigned long long)t.kv_count);
-      return;
-    }
-  }
-  {
-    int bi0, bi1, bj0, bj1;  // the bitmap's cells
-    cell_range(wide[0], wide[2], t.mbr[0], t.mbr[2], t.x_grid, bi0, bi1);
-    cell_range(wide[1], wide[3], t.mbr[1], t.mbr[3], t.y_grid, bj0, bj1);
-    if (!any_bit(b.bitmaps + (size_t)c * (STC_BITMAP_BYTES / 4), bi0, bi1, bj0, bj1, t.x_grid)) return;
-  }
-  const uint32_t g = b.ixg[c].x, levels = b.ixg[c].y;
-  // the query window in level-0 cells, one cell of slack either side
-  int i0, i1, j0, j1;
-  cell_range(wide[0], wide[2], t.mbr[0], t.mbr[2], g, i0, i1);
-  cell_range(wide[1], wide[3], t.mbr[1], t.mbr[3], g, j0, j1);
+  x.all_starts = fits && t.start_time_max < q.t_end;
+  x.all_ends = fits && q.t_start < t.end_time_min;
+  // the saturated end offsets of the index order them exactly below 65535
+  x.ts = x.all_ends ? 0u : q.t_start - t.end_time_min;
+  x.g = ix.x;
+  x.levels = ix.y;
+  cell_range(x.wide[0], x.wide[2], t.mbr[0], t.mbr[2], x.g, x.i0, x.i1);
+  cell_range(x.wide[1], x.wide[3], t.mbr[1], t.mbr[3], x.g, x.j0, x.j1);
   // Interior cells (counting only, every start passing): level-0 cells whose
   // every decoded low corner lies in the query box. A key's box meets the
   // query when its low corner is inside it; grid_coord is monotone, so a
   // corner in cell i (gc in [i, i + 1)) lies in [q_lo, q_hi] when
-  // i > gc(q_lo) and i + 1 <= gc(q_hi). A cell of level k is interior when
-  // all its level-0 cells are. Their keys are counted from the index: all of
-  // them when every end passes, else those past a binary search on the ends.
-  int ii0 = 1, ii1 = 0, jj0 = 1, jj1 = 0;  // empty
-  if (count_only && all_starts && (all_ends || ts < 65535u) && t.mbr[2] > t.mbr[0] && t.mbr[3] > t.mbr[1]) {
+  // i > gc(q_lo) and i + 1 <= gc(q_hi).
+  x.ii0 = x.jj0 = 1;
+  x.ii1 = x.jj1 = 0;
+  const bool count_only = (q.kind & STC_QUERY_COUNT_ONLY) != 0;
+  if (count_only && x.all_starts && (x.all_ends || x.ts < 65535u) && t.mbr[2] > t.mbr[0] && t.mbr[3] > t.mbr[1]) {
     auto interior = [](double g0, double g1, uint32_t n, int &lo, int &hi) {
       g0 = fmax(fmin(g0, (double)n + 2), -2.0);
       g1 = fmax(fmin(g1, (double)n + 2), -2.0);
       lo = max((int)floor(g0) + 1, 0);
       hi = min((int)floor(g1) - 1, (int)n);
     };
-    interior(grid_coord(qbox[0], t.mbr[0], t.mbr[2], g), grid_coord(qbox[2], t.mbr[0], t.mbr[2], g), g, ii0, ii1);
-    interior(grid_coord(qbox[1], t.mbr[1], t.mbr[3], g), grid_coord(qbox[3], t.mbr[1], t.mbr[3], g), g, jj0, jj1);
+    interior(grid_coord(qbox[0], t.mbr[0], t.mbr[2], x.g), grid_coord(qbox[2], t.mbr[0], t.mbr[2], x.g), x.g, x.ii0,
+             x.ii1);
+    interior(grid_coord(qbox[1], t.mbr[1], t.mbr[3], x.g), grid_coord(qbox[3], t.mbr[1], t.mbr[3], x.g), x.g, x.jj0,
+             x.jj1);
   }
-  // A key filed at level k under cell (cx, cy) whose box meets the widened
-  // query has cx in [(i0 >> k) - 1, i1 >> k] (its box ends at most one cell
-  // right of cx) and likewise cy: one warp per row segment of each level,
-  // then the wide list.
-  const uint32_t kb = t.key_bit / 8u;
-  const uint8_t *base = b.keys + t.key_offset;
-  const uint32_t cb = b.cbase[c], wide_slot = b.cbase[c + 1] - 1u;
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, nw = blockDim.x >> 5;
-  int rows = 0;
-  for (uint32_t lv = 0; lv < levels; lv++) {
-    const int side = (int)index_level_side(g, lv);
-    rows += max(min(j1 >> lv, side - 1) - max((j0 >> lv) - 1, 0) + 1, 0);
-  }
-  for (int r = (int)(blockIdx.x * nw + warp); r <= rows; r += (int)(QBOX_PARTS * nw)) {
-    uint32_t a, e, ma, me2;  // scan [a, ma) and [me2, e); [ma, me2) is counted
-    int clo = 1, chi = 0;    // counted cells of this row (level lv)
-    uint32_t row_base = 0;
-    if (r < rows) {
-      // level and row of work item r
-      uint32_t lv = 0, off = 0;
-      int rr = r, side = 0, cj0 = 0;
-      for (;; lv++) {
-        side = (int)index_level_side(g, lv);
-        cj0 = max((j0 >> lv) - 1, 0);
-        const int n = max(min(j1 >> lv, side - 1) - cj0 + 1, 0);
-        if (rr < n) break;
-        rr -= n;
-        off += (uint32_t)(side * side);
-      }
-      const int jr = cj0 + rr;
-      const int ci0 = max((i0 >> lv) - 1, 0), ci1 = min(i1 >> lv, side - 1);
-      row_base = cb + off + (uint32_t)(jr * side);
-      a = b.cstart[row_base + (uint32_t)ci0];
-      e = b.cstart[row_base + (uint32_t)ci1 + 1];
-      ma = me2 = a;
-      // interior at this level: cell C covers level-0 cells [C 2^lv, (C + 1) 2^lv - 1]
-      const int s2 = 1 << lv;
-      const int ilo = (ii0 + s2 - 1) >> lv, ihi = ((ii1 + 1) >> lv) - 1;
-      const bool row_in = ii0 <= ii1 && jj0 <= jj1 && jr * s2 >= jj0 && (jr + 1) * s2 - 1 <= jj1;
-      clo = max(ilo, ci0);
-      chi = min(ihi, ci1);
-      if (row_in && clo <= chi) {
-        ma = b.cstart[row_base + (uint32_t)clo];
-        me2 = b.cstart[row_base + (uint32_t)chi + 1];
+  return true;
+}
+
+// Rows of level lv in the window: a key filed at level lv under cell
+// (cx, cy) whose box meets the widened query has cy in
+// [(j0 >> lv) - 1, j1 >> lv] (its box ends at most one cell above cy), and
+// likewise cx.
+__device__ __forceinline__ int level_rows(const BoxCtx &x, uint32_t lv, int &cj0) {
+  const int side = (int)index_level_side(x.g, lv);
+  cj0 = max((x.j0 >> lv) - 1, 0);
+  return max(min(x.j1 >> lv, side - 1) - cj0 + 1, 0);
+}
+
+__global__ void k_box_plan(const QBlock *qb, uint32_t nb, const stc_query *qs, uint32_t nq, uint32_t F1,
+                           double m0x, double m0y, double m1x, double m1y, uint32_t *items,
+                           unsigned long long *qcounts) {
+  const uint32_t P = nq * nb * F1;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+    const uint32_t c = p % F1, bi = (p / F1) % nb, qi = p / F1 / nb;
+    const stc_query &q = qs[qi];
+    const QBlock &b = qb[bi];
+    uint32_t n = 0;
+    if ((q.kind & 0xFFu) == STC_QUERY_BOX && c <= b.F) {
+      if (c == b.F) {  // oversize buffer: the map bitmap prunes
+        if (b.n_over) {
+          int i0, i1, j0, j1;
+          cell_range(q.box[0], q.box[2], m0x, m1x, 256, i0, i1);
+          cell_range(q.box[1], q.box[3], m0y, m1y, 256, j0, j1);
+          if (any_bit_seq(b.obitmap, i0, i1, j0, j1, 256)) n = (uint32_t)((b.n_over + OV_CHUNK - 1) / OV_CHUNK);
+        }
       } else {
-        clo = 1;
-        chi = 0;
-      }
-    } else {  // the wide list
-      a = b.cstart[wide_slot];
-      e = b.cstart[wide_slot + 1];
-      ma = me2 = a;
-    }
-    if (clo <= chi) {
-      if (all_ends) {
-        if (lane == 0) mine += me2 - ma;
-      } else {
-        for (int ci = clo + (int)lane; ci <= chi; ci += 32) {
-          uint32_t x = b.cstart[row_base + (uint32_t)ci], y = b.cstart[row_base + (uint32_t)ci + 1];
-          const uint32_t n = y;
-          while (x < y) {  // first key of the cell with end offset > ts
-            uint32_t mid = (x + y) >> 1;
-            if (__ldg(&b.pend[mid]) <= ts) x = mid + 1;
-            else y = mid;
+        const stc_ctf &t = b.ctfs[c];
+        BoxCtx x;
+        if (t.kv_count && box_ctx(t, b.ixg[c], q, x)) {
+          const double *qbox = q.box;
+          const bool count_only = (q.kind & STC_QUERY_COUNT_ONLY) != 0;
+          if (count_only && x.all_starts && x.all_ends && qbox[0] <= t.mbr[0] - x.qx && qbox[1] <= t.mbr[1] - x.qy &&
+              qbox[2] >= t.mbr[2] + x.qx && qbox[3] >= t.mbr[3] + x.qy) {
+            // Every key matches -- count the CTF without decoding it, as the
+            // reference's box search does (workbench.cpp:525-528).
+            atomicAdd(&qcounts[qi], (unsigned long long)t.kv_count);
+          } else {
+            int bi0, bi1, bj0, bj1;  // the bitmap's cells
+            cell_range(x.wide[0], x.wide[2], t.mbr[0], t.mbr[2], t.x_grid, bi0, bi1);
+            cell_range(x.wide[1], x.wide[3], t.mbr[1], t.mbr[3], t.y_grid, bj0, bj1);
+            if (any_bit_seq(b.bitmaps + (size_t)c * (STC_BITMAP_BYTES / 4), bi0, bi1, bj0, bj1, t.x_grid)) {
+              n = 1;  // the wide list
+              for (uint32_t lv = 0; lv < x.levels; lv++) {
+                int cj0;
+                n += (uint32_t)level_rows(x, lv, cj0);
+              }
+            }
           }
-          mine += n - x;
         }
       }
     }
-    for (int seg = 0; seg < 2; seg++) {
-      for (uint32_t p = (seg ? me2 : a) + lane, pe = seg ? e : ma; p < pe; p += 32) {
-        const unsigned long long local = (unsigned long long)b.perm[p] - t.first_key;
-        Key k;
-        decode_key(load_key(base + local * kb, kb), t, k);
-        uint32_t end = k.end + t.end_time_min, start = end - k.duration;
-        if (time_ok(start, end, q.t_start, q.t_end) && box_hits(k.box, qbox)) {
-          mine++;
-          if (!count_only) emit(out, cap, count, qi, k.oid, k.target, start, end, k.box, b.index, c);
-        }
-      }
-    }
+    items[p] = n;
   }
-  add_count(qcounts, qi, mine);
+}
+
+// One warp per work item; item numbers come from the exclusive scan of the
+// plan's counts (items[P] = all items).
+__global__ void __launch_bounds__(QBOX_THREADS) k_box_rows(const QBlock *qb, uint32_t nb, const stc_query *qs,
+                                                          uint32_t nq, uint32_t F1, const uint32_t *first,
+                                                          QueryRec *out, unsigned long long cap,
+                                                          unsigned long long *count, unsigned long long *qcounts) {
+  const uint32_t P = nq * nb * F1;
+  const uint32_t total = first[P];
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t item = gw; item < total; item += nw) {
+    uint32_t lo = 0, hi = P - 1;  // the pair: largest p with first[p] <= item
+    while (lo < hi) {
+      uint32_t mid = (lo + hi + 1) >> 1;
+      if (__ldg(&first[mid]) <= item) lo = mid;
+      else hi = mid - 1;
+    }
+    const uint32_t p = lo, r = item - first[p];
+    const uint32_t c = p % F1, bi = (p / F1) % nb, qi = p / F1 / nb;
+    const stc_query q = qs[qi];
+    const QBlock &b = qb[bi];
+    const bool count_only = (q.kind & STC_QUERY_COUNT_ONLY) != 0;
+    const double *qbox = q.box;
+    uint32_t mine = 0;
+    if (c == b.F) {  // oversize keys [r * OV_CHUNK, ...): float boxes decide
+      const unsigned long long k1 = min((unsigned long long)(r + 1) * OV_CHUNK, b.n_over);
+      for (unsigned long long i = (unsigned long long)r * OV_CHUNK + lane; i < k1; i += 32) {
+        float4 fb = b.obox[i];
+        double box[4] = {fb.x, fb.y, fb.z, fb.w};
+        uint32_t pid, target, start, end;
+        oversize_key(b, i, pid, target, start, end);
+        if (time_ok(start, end, q.t_start, q.t_end) && box_hits(box, qbox)) {
+          mine++;
+          if (!count_only) emit(out, cap, count, qi, pid, target, start, end, box, b.index, c);
+        }
+      }
+    } else {
+      const stc_ctf &t = b.ctfs[c];
+      BoxCtx x;
+      box_ctx(t, b.ixg[c], q, x);  // the plan saw it pass
+      const uint32_t cb = b.cbase[c], wide_slot = b.cbase[c + 1] - 1u;
+      uint32_t a, e, ma, me2;  // scan [a, ma) and [me2, e); [ma, me2) is counted
+      int clo = 1, chi = 0;    // counted cells of this row
+      uint32_t row_base = 0;
+      uint32_t rr = r, lv = 0, off = 0;
+      int cj0 = 0, n = 0;
+      for (; lv < x.levels; lv++) {
+        n = level_rows(x, lv, cj0);
+        if (rr < (uint32_t)n) break;
+        rr -= (uint32_t)n;
+        const uint32_t side = index_level_side(x.g, lv);
+        off += side * side;
+      }
+      if (lv < x.levels) {  // row cj0 + rr of level lv
+        const int side = (int)index_level_side(x.g, lv);
+        const int jr = cj0 + (int)rr;
+        const int ci0 = max((x.i0 >> lv) - 1, 0), ci1 = min(x.i1 >> lv, side - 1);
+        row_base = cb + off + (uint32_t)(jr * side);
+        a = b.cstart[row_base + (uint32_t)ci0];
+        e = ci1 >= ci0 ? b.cstart[row_base + (uint32_t)ci1 + 1] : a;
+        ma = me2 = a;
+        // interior at this level: cell C covers level-0 cells [C 2^lv, (C + 1) 2^lv - 1]
+        const int s2 = 1 << lv;
+        const bool row_in = x.ii0 <= x.ii1 && x.jj0 <= x.jj1 && jr * s2 >= x.jj0 && (jr + 1) * s2 - 1 <= x.jj1;
+        if (row_in) {
+          clo = max((x.ii0 + s2 - 1) >> lv, ci0);
+          chi = min(((x.ii1 + 1) >> lv) - 1, ci1);
+        }
+        if (clo <= chi) {
+          ma = b.cstart[row_base + (uint32_t)clo];
+          me2 = b.cstart[row_base + (uint32_t)chi + 1];
+          if (x.all_ends) {
+            if (lane == 0) mine += me2 - ma;
+          } else {
+            // the counted cells' end offsets lie side by side: one coalesced pass
+            for (uint32_t pp = ma + lane; pp < me2; pp += 32) mine += __ldg(&b.pend[pp]) > x.ts;
+          }
+        }
+      } else {  // the wide list
+        a = b.cstart[wide_slot];
+        e = b.cstart[wide_slot + 1];
+        ma = me2 = a;
+      }
+      const uint32_t kb = t.key_bit / 8u;
+      const uint8_t *base = b.keys + t.key_offset;
+      const BoxRecip rc = box_recip(t);
+      for (int seg = 0; seg < 2; seg++) {
+        for (uint32_t pp = (seg ? me2 : a) + lane, pe = seg ? e : ma; pp < pe; pp += 32) {
+          const unsigned long long local = (unsigned long long)b.perm[pp] - t.first_key;
+          Key k;
+          const unsigned long long vm = key_fields(load_key(base + local * kb, kb), t, k);
+          uint32_t end = k.end + t.end_time_min, start = end - k.duration;
+          if (!time_ok(start, end, q.t_start, q.t_end)) continue;
+          const int sc = box_screen(vm, t, rc, qbox);
+          if (sc == 0) continue;
+          if (sc < 0 || !count_only) exact_box(vm, t, k.box);
+          if (sc > 0 || box_hits(k.box, qbox)) {
+            mine++;
+            if (!count_only) emit(out, cap, count, qi, k.oid, k.target, start, end, k.box, b.index, c);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
+    if (lane == 0 && mine) atomicAdd(&qcounts[qi], (unsigned long long)mine);
+  }
 }
 
 template <typename T>
@@ -654,6 +763,10 @@ void lsm_release(LsmHost &H) {
   if (H.d_qcounts) cudaFree(H.d_qcounts);
   H.d_qcounts = nullptr;
   H.qc_cap = 0;
+  if (H.d_items) cudaFree(H.d_items);
+  if (H.d_iscan) cudaFree(H.d_iscan);
+  H.d_items = H.d_iscan = nullptr;
+  H.items_cap = H.iscan_cap = 0;
   if (H.qstream) cudaStreamDestroy(H.qstream);
   H.d_qb = nullptr;
   H.d_q = nullptr;
@@ -683,19 +796,27 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
   if (e == cudaSuccess) e = grow(&H.d_q, &H.q_cap, nq);
   if (e == cudaSuccess) e = grow(&H.d_qcounts, &H.qc_cap, nq);
   if (e == cudaSuccess) e = grow(&H.d_out, &H.out_cap, std::max<size_t>(1 << 16, H.out_cap));
+  uint32_t maxF = 0;
+  for (uint32_t i = 0; i < nb; i++) maxF = std::max(maxF, H.blocks[i].info.ctf_count);
+  // box-query plan: one count per (query, block, CTF or oversize buffer), then their exclusive scan
+  const size_t npairs = nq * nb * ((size_t)maxF + 1) + 1;
+  if (npairs > 0xFFFFFFFFull) {
+    err = "query batch too large for the box-query plan";
+    return STC_ERR_INVALID_ARG;
+  }
+  if (e == cudaSuccess) e = grow(&H.d_items, &H.items_cap, npairs);
+  if (e == cudaSuccess) e = grow(&H.d_iscan, &H.iscan_cap, scan_tmp_words(npairs));
   if (e != cudaSuccess) {
     err = std::string("query buffers: ") + cudaGetErrorString(e);
     return STC_ERR_CUDA;
   }
   std::vector<QBlock> qb(nb);
-  uint32_t maxF = 0;
   for (uint32_t i = 0; i < nb; i++) {
     const CtbBlock &B = H.blocks[i];
     qb[i] = QBlock{B.keys, B.d_ctfs, B.sids, B.orec, B.obox, B.bitmaps, B.obitmap, B.perm, B.cstart, B.cbase, B.ixg,
                    B.pend,
                    (unsigned long long)B.info.oversize_kv_count, B.info.ctf_count, B.info.index,
                    B.info.o_end_time_min, 0};
-    maxF = std::max(maxF, B.info.ctf_count);
   }
   bool has_obj = false, has_box = false;
   for (size_t i = 0; i < nq; i++) ((qs[i].kind & 0xFFu) == STC_QUERY_BOX ? has_box : has_obj) = true;
@@ -709,10 +830,14 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
     if (has_obj)
       STC_KL k_query_object<<<dim3(nb, (unsigned)nq), QOBJ_THREADS, 0, s>>>(H.d_qb, H.d_q, H.d_out, H.out_cap,
                                                                            H.d_count, H.d_qcounts);
-    if (has_box)
-      STC_KL k_query_box<<<dim3(QBOX_PARTS, maxF + 1, (unsigned)(nq * nb)), QBOX_THREADS, 0, s>>>(
-          H.d_qb, nb, H.d_q, H.map[0], H.map[1], H.map[2], H.map[3], H.d_out, H.out_cap, H.d_count,
-          H.d_qcounts);
+    if (has_box) {
+      const uint32_t F1 = maxF + 1, P = (uint32_t)nq * nb * F1;
+      STC_KL k_box_plan<<<(P + 255) / 256, 256, 0, s>>>(H.d_qb, nb, H.d_q, (uint32_t)nq, F1, H.map[0], H.map[1],
+                                                        H.map[2], H.map[3], H.d_items, H.d_qcounts);
+      exclusive_scan_u32(H.d_items, H.d_items, (size_t)P + 1, nullptr, H.d_iscan, s);
+      STC_KL k_box_rows<<<STC_NUM_SMS * 16, QBOX_THREADS, 0, s>>>(H.d_qb, nb, H.d_q, (uint32_t)nq, F1, H.d_items,
+                                                                  H.d_out, H.out_cap, H.d_count, H.d_qcounts);
+    }
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(&total, H.d_count, sizeof(total), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess && counts)
