@@ -306,6 +306,7 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr):
             contacts[0] += int(counts.sum())
 
     th = threading.Thread(target=server, daemon=True)
+    pipe.set_step_slices(args.serve_slices)  # query kernels get the GPU between slices
     th.start()
     step_ms = []
     w0 = time.perf_counter()
@@ -317,6 +318,7 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr):
     wall = time.perf_counter() - w0
     done.set()
     th.join()
+    pipe.set_step_slices(args.step_slices)
     if errors:
         return {"error": errors[0]}
     lat_ms = np.array(lat) * 1e3
@@ -327,7 +329,7 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr):
             "contacts_per_query": contacts[0] / max(len(lat), 1),
             "mix": "60% object (window 10-10000 steps), 40% box (50 m-5 km, window 10-3600 steps); "
                    "match counts, as the reference's searches return",
-            "blocks": 1, "ingest_pos_updates_per_s": N * steps / wall,
+            "blocks": 1, "step_slices": args.serve_slices, "ingest_pos_updates_per_s": N * steps / wall,
             "ingest_device_ms_per_step": float(np.mean(step_ms))}
 
 
@@ -411,6 +413,8 @@ def main():
                     help="Poisson query arrivals per second during the serving phase (0: skip)")
     ap.add_argument("--step-slices", type=int, default=0,
                     help="launches per long step kernel (stc_config.step_slices; 0 = 1)")
+    ap.add_argument("--serve-slices", type=int, default=4,
+                    help="step slices while the serving phase answers queries (stc_set_step_slices)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()

@@ -353,6 +353,11 @@ stc_status stc_checkpoint(stc_ctx *ctx, const char *path);
 stc_status stc_get_config(const stc_ctx *ctx, stc_config *cfg);
 stc_status stc_restore(const char *path, uint32_t device, stc_ctx **out);
 
+/* Changes stc_config.step_slices of a running context (between steps): a
+ * server slices its steps while it answers queries, so that query kernels
+ * start between the slices, and runs whole steps otherwise. */
+stc_status stc_set_step_slices(stc_ctx *ctx, uint32_t slices);
+
 /* Last error message of ctx (or, when ctx is NULL, of the last failed
  * stc_create or context-free call on this thread). Never NULL. */
 const char *stc_last_error(const stc_ctx *ctx);

@@ -30,6 +30,8 @@ namespace stc {
 void set_thread_error(const std::string &msg) { g_create_error = msg; }
 }  // namespace stc
 
+static constexpr size_t DRAIN_CHUNK = (size_t)8 << 20;  // bytes per pinned staging chunk of a drain
+
 struct stc_ctx {
   stc_config cfg;
   int device = 0;
@@ -40,6 +42,11 @@ struct stc_ctx {
   bool stepped = false;
   PipeDev p;
   DevState *st_host = nullptr;   // pinned mirror
+  // pinned staging of drained meetings: copies from pinned memory are plain
+  // DMA, while copies into the caller's pageable memory go through the
+  // driver's staging path, which other threads' copies (queries) wait on
+  uint8_t *drain_stage[2] = {nullptr, nullptr};
+  cudaEvent_t drain_ev[2] = {nullptr, nullptr};
   double2 *xy_own = nullptr;     // device copy target for host input
   std::vector<void *> allocs;
   stc_stats stats;
@@ -134,6 +141,10 @@ static void destroy_all(stc_ctx *c) {
   for (void *v : c->allocs) cudaFree(v);
   c->allocs.clear();
   if (c->st_host) cudaFreeHost(c->st_host);
+  for (int i = 0; i < 2; i++) {
+    if (c->drain_stage[i]) cudaFreeHost(c->drain_stage[i]);
+    if (c->drain_ev[i]) cudaEventDestroy(c->drain_ev[i]);
+  }
   for (int i = 0; i < PH_COUNT; i++)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -222,6 +233,10 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   for (int i = 0; i < PH_COUNT && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
   if (e == cudaSuccess) e = cudaMallocHost(&c->st_host, sizeof(DevState));
+  for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+    e = cudaMallocHost(&c->drain_stage[i], DRAIN_CHUNK);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->drain_ev[i], cudaEventDisableTiming);
+  }
   if (e != cudaSuccess) {
     g_create_error = std::string("stc_create: ") + cudaGetErrorString(e);
     destroy_all(c);
@@ -321,6 +336,12 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
     cudaDeviceGetStreamPriorityRange(&least, &greatest);
     if (ok && cudaStreamCreateWithPriority(&H.qstream, cudaStreamNonBlocking, greatest) != cudaSuccess) {
       c->err = "query stream creation failed";
+      ok = false;
+    }
+    // query buffers now: allocating them later would wait for a step in flight
+    std::string qerr;
+    if (ok && lsm_query_reserve(H, 4096, ctf_count, qerr) != STC_OK) {
+      c->err = qerr;
       ok = false;
     }
   }
@@ -497,7 +518,21 @@ extern "C" stc_status stc_drain_meetings(stc_ctx *c, stc_meeting *out, size_t ca
   size_t k = (size_t)std::min<unsigned long long>(pending, cap);
   cudaStream_t s = c->stream;
   cudaError_t e = cudaSuccess;
-  if (k) e = cudaMemcpyAsync(out, p.emit, k * sizeof(stc_meeting), cudaMemcpyDeviceToHost, s);
+  // the k records through the two pinned chunks: the copy of chunk i + 1
+  // runs while chunk i is moved to out
+  const size_t bytes = k * sizeof(stc_meeting), nch = (bytes + DRAIN_CHUNK - 1) / DRAIN_CHUNK;
+  for (size_t i = 0; e == cudaSuccess && i <= nch; i++) {
+    if (i < nch) {
+      const size_t off = i * DRAIN_CHUNK, len = std::min(DRAIN_CHUNK, bytes - off);
+      e = cudaMemcpyAsync(c->drain_stage[i & 1], (const uint8_t *)p.emit + off, len, cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaEventRecord(c->drain_ev[i & 1], s);
+    }
+    if (e == cudaSuccess && i > 0) {
+      const size_t j = i - 1, off = j * DRAIN_CHUNK, len = std::min(DRAIN_CHUNK, bytes - off);
+      e = cudaEventSynchronize(c->drain_ev[j & 1]);
+      if (e == cudaSuccess) memcpy((uint8_t *)out + off, c->drain_stage[j & 1], len);
+    }
+  }
   // shift the rest down in non-overlapping chunks of k records
   for (size_t src = k; e == cudaSuccess && k && src < pending; src += k) {
     size_t len = std::min<size_t>(k, pending - src);
@@ -505,7 +540,8 @@ extern "C" stc_status stc_drain_meetings(stc_ctx *c, stc_meeting *out, size_t ca
   }
   unsigned long long left = pending - k;
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(&p.st->emit_count, &left, sizeof(left), cudaMemcpyHostToDevice, s);
+    e = cudaMemcpyAsync(&p.st->emit_count, &(c->st_host->emit_count = left), sizeof(left), cudaMemcpyHostToDevice,
+                        s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(c, e, "stc_drain_meetings");
   c->st_host->emit_count = left;
@@ -675,6 +711,13 @@ extern "C" stc_status stc_read_block(stc_ctx *c, uint32_t index, stc_ctf *ctfs, 
                                  oversize_bitmap, err);
   if (st != STC_OK) c->err = "stc_read_block: " + err;
   return st;
+}
+
+extern "C" stc_status stc_set_step_slices(stc_ctx *c, uint32_t slices) {
+  if (!c) return STC_ERR_INVALID_ARG;
+  c->cfg.step_slices = slices;
+  c->p.slices = std::min<uint32_t>(std::max<uint32_t>(slices, 1u), 64u);
+  return STC_OK;
 }
 
 extern "C" stc_status stc_compact(stc_ctx *c, uint32_t first_index, uint32_t count, uint32_t split,

@@ -140,6 +140,14 @@ struct LsmHost {
   size_t items_cap = 0;
   uint32_t *d_iscan = nullptr;     // scan scratch
   size_t iscan_cap = 0;
+  // pinned host staging of a batch's copies (pageable copies would wait on
+  // the driver's staging path, which a stepping thread's copies hold)
+  QBlock *h_qb = nullptr;          // [retain]
+  stc_query *h_q = nullptr;
+  size_t hq_cap = 0;
+  unsigned long long *h_counts = nullptr;  // [hq_cap + 1]: per-query counts, then the match total
+  QueryRec *h_recs = nullptr;
+  size_t hrecs_cap = 0;
   double map[4] = {0, 0, 0, 0};
 };
 
@@ -193,6 +201,10 @@ cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s);
 // max_meet_time, map); the merge allocates its own scratch. ms: device time.
 stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32_t count, uint32_t split,
                        uint32_t new_index, cudaStream_t s, float *ms, std::string &err);
+
+// Allocates the query buffers for batches of up to nq queries over blocks of
+// up to F CTFs (later batches then allocate nothing unless they need more).
+stc_status lsm_query_reserve(LsmHost &H, size_t nq, uint32_t F, std::string &err);
 
 // Runs a batch of queries over the retained blocks on H.qstream (see
 // stc_query_batch in include/stc.h).

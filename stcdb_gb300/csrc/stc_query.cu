@@ -630,6 +630,18 @@ __global__ void __launch_bounds__(QBOX_THREADS) k_box_rows(const QBlock *qb, uin
   }
 }
 
+// Pinned host buffer of at least `need` elements (contents not kept).
+template <typename T>
+cudaError_t grow_pinned(T **p, size_t *cap, size_t need) {
+  if (*cap >= need) return cudaSuccess;
+  size_t n = std::max<size_t>(need, 2 * *cap);
+  if (*p) cudaFreeHost(*p);
+  *p = nullptr;
+  cudaError_t e = cudaMallocHost((void **)p, n * sizeof(T));
+  *cap = e == cudaSuccess ? n : 0;
+  return e;
+}
+
 template <typename T>
 cudaError_t grow(T **p, size_t *cap, size_t need) {
   if (*cap >= need) return cudaSuccess;
@@ -767,6 +779,13 @@ void lsm_release(LsmHost &H) {
   if (H.d_iscan) cudaFree(H.d_iscan);
   H.d_items = H.d_iscan = nullptr;
   H.items_cap = H.iscan_cap = 0;
+  for (void *v : {(void *)H.h_qb, (void *)H.h_q, (void *)H.h_counts, (void *)H.h_recs})
+    if (v) cudaFreeHost(v);
+  H.h_qb = nullptr;
+  H.h_q = nullptr;
+  H.h_counts = nullptr;
+  H.h_recs = nullptr;
+  H.hq_cap = H.hrecs_cap = 0;
   if (H.qstream) cudaStreamDestroy(H.qstream);
   H.d_qb = nullptr;
   H.d_q = nullptr;
@@ -774,6 +793,55 @@ void lsm_release(LsmHost &H) {
   H.d_count = nullptr;
   H.qstream = nullptr;
   H.q_cap = H.out_cap = 0;
+}
+
+// Device and pinned buffers of a batch of up to nq queries over H.retain
+// blocks of up to F CTFs. Allocations synchronise with the device (a step in
+// flight), so they are made once, before any step runs; batches that need
+// more grow them.
+cudaError_t query_buffers(LsmHost &H, size_t nq, uint32_t F) {
+  cudaError_t e = cudaSuccess;
+  if (!H.d_qb) e = cudaMalloc(&H.d_qb, (size_t)std::max<uint32_t>(H.retain, 1) * sizeof(QBlock));
+  if (e == cudaSuccess && !H.h_qb)
+    e = cudaMallocHost((void **)&H.h_qb, (size_t)std::max<uint32_t>(H.retain, 1) * sizeof(QBlock));
+  if (e == cudaSuccess && !H.d_count) e = cudaMalloc(&H.d_count, sizeof(unsigned long long));
+  if (e == cudaSuccess && H.hq_cap < nq) {
+    size_t cap_q = H.hq_cap;
+    e = grow_pinned(&H.h_q, &H.hq_cap, nq);
+    if (e == cudaSuccess) e = grow_pinned(&H.h_counts, &cap_q, H.hq_cap + 1);
+  }
+  if (e == cudaSuccess) e = grow(&H.d_q, &H.q_cap, nq);
+  if (e == cudaSuccess) e = grow(&H.d_qcounts, &H.qc_cap, nq);
+  if (e == cudaSuccess) e = grow(&H.d_out, &H.out_cap, std::max<size_t>(1 << 16, H.out_cap));
+  const size_t npairs = nq * (size_t)H.blocks.size() * ((size_t)F + 1) + 1;
+  if (e == cudaSuccess) e = grow(&H.d_items, &H.items_cap, npairs);
+  if (e == cudaSuccess) e = grow(&H.d_iscan, &H.iscan_cap, scan_tmp_words(npairs));
+  return e;
+}
+
+stc_status lsm_query_reserve(LsmHost &H, size_t nq, uint32_t F, std::string &err) {
+  std::lock_guard<std::mutex> qlock(H.query_mu);
+  const size_t nb = H.blocks.size();
+  cudaError_t e = cudaSuccess;
+  {
+    // size the plan for the retained-block limit, not today's count
+    const size_t npairs = nq * (size_t)std::max<uint32_t>(H.retain, 1) * ((size_t)F + 1) + 1;
+    e = grow(&H.d_items, &H.items_cap, npairs);
+    if (e == cudaSuccess) e = grow(&H.d_iscan, &H.iscan_cap, scan_tmp_words(npairs));
+  }
+  if (e == cudaSuccess) e = query_buffers(H, nq, F);
+  if (e == cudaSuccess) e = grow_pinned(&H.h_recs, &H.hrecs_cap, 1 << 16);
+  (void)nb;
+  // load the query kernels now: with lazy module loading their first launch
+  // would load them then, which waits for a step in flight
+  cudaFuncAttributes fa;
+  for (const void *k : {(const void *)k_query_object, (const void *)k_box_plan, (const void *)k_box_rows})
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k);
+  if (e != cudaSuccess) {
+    err = std::string("query buffers: ") + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? STC_ERR_CAPACITY : STC_ERR_CUDA;
+  }
+  return STC_OK;
 }
 
 stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *out, size_t cap, uint64_t *offsets,
@@ -790,27 +858,19 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
     return STC_ERR_INVALID_ARG;
   }
   cudaStream_t s = H.qstream;
-  cudaError_t e = cudaSuccess;
-  if (!H.d_qb) e = cudaMalloc(&H.d_qb, (size_t)std::max<uint32_t>(H.retain, 1) * sizeof(QBlock));
-  if (e == cudaSuccess && !H.d_count) e = cudaMalloc(&H.d_count, sizeof(unsigned long long));
-  if (e == cudaSuccess) e = grow(&H.d_q, &H.q_cap, nq);
-  if (e == cudaSuccess) e = grow(&H.d_qcounts, &H.qc_cap, nq);
-  if (e == cudaSuccess) e = grow(&H.d_out, &H.out_cap, std::max<size_t>(1 << 16, H.out_cap));
   uint32_t maxF = 0;
   for (uint32_t i = 0; i < nb; i++) maxF = std::max(maxF, H.blocks[i].info.ctf_count);
   // box-query plan: one count per (query, block, CTF or oversize buffer), then their exclusive scan
-  const size_t npairs = nq * nb * ((size_t)maxF + 1) + 1;
-  if (npairs > 0xFFFFFFFFull) {
+  if (nq * nb * ((size_t)maxF + 1) + 1 > 0xFFFFFFFFull) {
     err = "query batch too large for the box-query plan";
     return STC_ERR_INVALID_ARG;
   }
-  if (e == cudaSuccess) e = grow(&H.d_items, &H.items_cap, npairs);
-  if (e == cudaSuccess) e = grow(&H.d_iscan, &H.iscan_cap, scan_tmp_words(npairs));
+  cudaError_t e = query_buffers(H, nq, maxF);
   if (e != cudaSuccess) {
     err = std::string("query buffers: ") + cudaGetErrorString(e);
     return STC_ERR_CUDA;
   }
-  std::vector<QBlock> qb(nb);
+  QBlock *qb = H.h_qb;
   for (uint32_t i = 0; i < nb; i++) {
     const CtbBlock &B = H.blocks[i];
     qb[i] = QBlock{B.keys, B.d_ctfs, B.sids, B.orec, B.obox, B.bitmaps, B.obitmap, B.perm, B.cstart, B.cbase, B.ixg,
@@ -820,8 +880,9 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
   }
   bool has_obj = false, has_box = false;
   for (size_t i = 0; i < nq; i++) ((qs[i].kind & 0xFFu) == STC_QUERY_BOX ? has_box : has_obj) = true;
-  e = cudaMemcpyAsync(H.d_qb, qb.data(), nb * sizeof(QBlock), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(H.d_q, qs, nq * sizeof(stc_query), cudaMemcpyHostToDevice, s);
+  memcpy(H.h_q, qs, nq * sizeof(stc_query));
+  e = cudaMemcpyAsync(H.d_qb, qb, nb * sizeof(QBlock), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(H.d_q, H.h_q, nq * sizeof(stc_query), cudaMemcpyHostToDevice, s);
   unsigned long long total = 0;
   for (int attempt = 0; attempt < 2 && e == cudaSuccess; attempt++) {
     e = cudaMemsetAsync(H.d_count, 0, sizeof(unsigned long long), s);
@@ -839,10 +900,12 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
                                                                   H.d_out, H.out_cap, H.d_count, H.d_qcounts);
     }
     e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&total, H.d_count, sizeof(total), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(H.h_counts + nq, H.d_count, sizeof(total), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess && counts)
-      e = cudaMemcpyAsync(counts, H.d_qcounts, nq * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+      e = cudaMemcpyAsync(H.h_counts, H.d_qcounts, nq * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    total = H.h_counts[nq];
+    if (e == cudaSuccess && counts) memcpy(counts, H.h_counts, nq * sizeof(unsigned long long));
     if (e != cudaSuccess || total <= H.out_cap) break;
     e = grow(&H.d_out, &H.out_cap, (size_t)total);  // too many matches: once more with room for all
   }
@@ -850,9 +913,9 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
     err = std::string("query: ") + cudaGetErrorString(e);
     return STC_ERR_CUDA;
   }
-  std::vector<QueryRec> recs((size_t)total);
   if (total) {
-    e = cudaMemcpyAsync(recs.data(), H.d_out, total * sizeof(QueryRec), cudaMemcpyDeviceToHost, s);
+    e = grow_pinned(&H.h_recs, &H.hrecs_cap, (size_t)total);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(H.h_recs, H.d_out, total * sizeof(QueryRec), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
       err = std::string("query read-back: ") + cudaGetErrorString(e);
@@ -860,11 +923,12 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
     }
   }
   // group by query (counting sort)
-  for (const QueryRec &r : recs) offsets[r.q + 1]++;
+  const QueryRec *recs = H.h_recs;
+  for (unsigned long long i = 0; i < total; i++) offsets[recs[i].q + 1]++;
   for (size_t i = 0; i < nq; i++) offsets[i + 1] += offsets[i];
   if (total <= cap && out) {
     std::vector<uint64_t> pos(offsets, offsets + nq);
-    for (const QueryRec &r : recs) out[pos[r.q]++] = r.c;
+    for (unsigned long long i = 0; i < total; i++) out[pos[recs[i].q]++] = recs[i].c;
   }
   return STC_OK;
 }

@@ -236,6 +236,8 @@ def _lib():
         lib.stc_compact.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                     ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_float)]
         lib.stc_compact.restype = ctypes.c_int
+        lib.stc_set_step_slices.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
+        lib.stc_set_step_slices.restype = ctypes.c_int
         lib.stc_query_batch.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                         ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
         lib.stc_query_batch.restype = ctypes.c_int
@@ -292,17 +294,20 @@ class Pipeline:
         return s
 
     def drain(self) -> np.ndarray:
+        """The meetings emitted since the last drain (stc_drain_meetings).
+        One buffer sized to the pending count receives them; the copy runs
+        in the library without the interpreter lock, so threads that query
+        meanwhile are not held up."""
         out = []
         while True:
-            pend = self.stats().pending
-            cap = max(int(pend), 1)
-            buf = np.zeros(cap, dtype=MEETING_DTYPE)
+            cap = max(int(self.stats().pending), 1)
+            buf = np.empty(cap, dtype=MEETING_DTYPE)
             n = ctypes.c_size_t()
             self._check(self._lib.stc_drain_meetings(self._h, buf.ctypes.data, cap, ctypes.byref(n)))
             out.append(buf[: n.value])
-            if n.value < cap or n.value == 0:
+            if n.value < cap or n.value == 0 or self.stats().pending == 0:
                 break
-        return np.concatenate(out) if out else np.zeros(0, MEETING_DTYPE)
+        return out[0] if len(out) == 1 else np.concatenate(out)
 
     def flush(self) -> bool:
         """Flushes the memtable into a block now; False if it was empty."""
@@ -336,6 +341,10 @@ class Pipeline:
         self._check(self._lib.stc_read_block(self._h, index, *[b[k].ctypes.data for k in (
             "ctfs", "bitmaps", "keys", "sids", "oversize_keys", "oversize_boxes", "oversize_bitmap")]))
         return info, ctb_trim(info, b)
+
+    def set_step_slices(self, slices: int) -> None:
+        """Launches per long step kernel from the next step on (stc_set_step_slices)."""
+        self._check(self._lib.stc_set_step_slices(self._h, slices))
 
     def compact(self, first_index: int, count: int, split: int) -> tuple:
         """Merges retained block first_index and the count - 1 after it into
