@@ -205,7 +205,11 @@ def run_gpu(args, w, rank, local):
     wall_dev = time.perf_counter() - t0
     barrier(args)
     dev_ms = sum(s.step_ms for s in stats)
-    # end to end: host positions in, meetings out, through the C ABI
+    # end to end: host positions in, meetings out, through the C ABI; the
+    # meetings land in a reused page-locked buffer, as a server would keep one
+    from stcdb_gb300.pipeline import MEETING_DTYPE
+    mbuf = torch.empty(8 * N * MEETING_DTYPE.itemsize // 10, dtype=torch.uint8, pin_memory=True)
+    mnp = mbuf.numpy().view(MEETING_DTYPE)
     e2e_stats = []
     d2h = 0
     barrier(args)
@@ -213,7 +217,7 @@ def run_gpu(args, w, rank, local):
     t1 = time.perf_counter()
     for t in range(W + K, W + 2 * K):
         pipe.step(hnp[t], t)
-        m = pipe.drain()
+        m = pipe.drain(mnp)
         d2h += m.nbytes + 128
         e2e_stats.append(pipe.stats())
     torch.cuda.synchronize()
@@ -230,7 +234,7 @@ def run_gpu(args, w, rank, local):
     # Poisson query stream over the flushed block
     queries = None
     if args.query_rate > 0:
-        queries = serve_under_ingest(args, pipe, hnp, W + 2 * K, K, N, mbr)
+        queries = serve_under_ingest(args, pipe, hnp, W + 2 * K, K, N, mbr, mnp)
     # compaction: the serving steps' keys become a second block; both merge
     # into one block of split x split CTFs (100 CTFs, as a flush makes)
     compaction = None
@@ -271,7 +275,7 @@ def make_queries(rng, n, N, mbr, t_now):
     return q
 
 
-def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr):
+def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
     """Continuous batching: queries arrive as a Poisson stream; whatever has
     arrived while a batch ran forms the next batch. Latency = answer time -
     arrival time. The main thread keeps stepping meanwhile (host input)."""
@@ -312,7 +316,7 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr):
     w0 = time.perf_counter()
     for t in range(t0, t0 + steps):
         pipe.step(hnp[t], t)
-        pipe.drain()
+        pipe.drain(mout)
         step_ms.append(pipe.stats().step_ms)
         cur_t[0] = t
     wall = time.perf_counter() - w0
@@ -413,7 +417,7 @@ def main():
                     help="Poisson query arrivals per second during the serving phase (0: skip)")
     ap.add_argument("--step-slices", type=int, default=0,
                     help="launches per long step kernel (stc_config.step_slices; 0 = 1)")
-    ap.add_argument("--serve-slices", type=int, default=4,
+    ap.add_argument("--serve-slices", type=int, default=8,
                     help="step slices while the serving phase answers queries (stc_set_step_slices)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

@@ -518,10 +518,16 @@ extern "C" stc_status stc_drain_meetings(stc_ctx *c, stc_meeting *out, size_t ca
   size_t k = (size_t)std::min<unsigned long long>(pending, cap);
   cudaStream_t s = c->stream;
   cudaError_t e = cudaSuccess;
-  // the k records through the two pinned chunks: the copy of chunk i + 1
-  // runs while chunk i is moved to out
-  const size_t bytes = k * sizeof(stc_meeting), nch = (bytes + DRAIN_CHUNK - 1) / DRAIN_CHUNK;
-  for (size_t i = 0; e == cudaSuccess && i <= nch; i++) {
+  // pinned (page-locked) output takes one direct copy; other memory gets the
+  // k records through the two pinned chunks, the copy of chunk i + 1 running
+  // while chunk i is moved to out
+  const size_t bytes = k * sizeof(stc_meeting);
+  cudaPointerAttributes pa;
+  const bool pinned_out = k && cudaPointerGetAttributes(&pa, out) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+  cudaGetLastError();  // pageable memory is not an error
+  if (pinned_out) e = cudaMemcpyAsync(out, p.emit, bytes, cudaMemcpyDeviceToHost, s);
+  const size_t nch = pinned_out ? 0 : (bytes + DRAIN_CHUNK - 1) / DRAIN_CHUNK;
+  for (size_t i = 0; e == cudaSuccess && nch && i <= nch; i++) {
     if (i < nch) {
       const size_t off = i * DRAIN_CHUNK, len = std::min(DRAIN_CHUNK, bytes - off);
       e = cudaMemcpyAsync(c->drain_stage[i & 1], (const uint8_t *)p.emit + off, len, cudaMemcpyDeviceToHost, s);

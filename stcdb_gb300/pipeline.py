@@ -293,11 +293,19 @@ class Pipeline:
         self._check(self._lib.stc_get_stats(self._h, ctypes.byref(s)))
         return s
 
-    def drain(self) -> np.ndarray:
+    def drain(self, out: np.ndarray | None = None) -> np.ndarray:
         """The meetings emitted since the last drain (stc_drain_meetings).
         One buffer sized to the pending count receives them; the copy runs
         in the library without the interpreter lock, so threads that query
-        meanwhile are not held up."""
+        meanwhile are not held up. `out`, a MEETING_DTYPE array (best in
+        page-locked memory, which the library fills by direct DMA), is
+        reused when it can hold them all; the result is then a view of it."""
+        if out is not None:
+            assert out.dtype == MEETING_DTYPE and out.flags.c_contiguous
+            if int(self.stats().pending) <= len(out):
+                n = ctypes.c_size_t()
+                self._check(self._lib.stc_drain_meetings(self._h, out.ctypes.data, len(out), ctypes.byref(n)))
+                return out[: n.value]
         out = []
         while True:
             cap = max(int(self.stats().pending), 1)
