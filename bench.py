@@ -36,6 +36,7 @@ queries_under_ingest: K more steps (host input) while a serving thread answers
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -174,11 +175,13 @@ def run_gpu(args, w, rank, local):
     dev = torch.empty((W + K, N, 2), dtype=torch.float64, device=f"cuda:{local}")
     gen.next_into(dev.data_ptr(), W + K)
     gen_ms = gen.last_ms
-    host = torch.empty((2 * K, N, 2), dtype=torch.float64, pin_memory=True)
+    S = args.serve_steps if args.serve_steps > 0 else 2 * K
+    host = torch.empty((K + S, N, 2), dtype=torch.float64, pin_memory=True)
     stage = torch.empty((K, N, 2), dtype=torch.float64, device=f"cuda:{local}")
-    for half in range(2):
-        gen.next_into(stage.data_ptr(), K)
-        host[half * K:(half + 1) * K].copy_(stage)
+    for lo in range(0, K + S, K):
+        n = min(K, K + S - lo)
+        gen.next_into(stage.data_ptr(), n)
+        host[lo:lo + n].copy_(stage[:n])
     gen.close()
     del stage
     hnp = HostSteps(host.numpy(), W + K)
@@ -234,7 +237,7 @@ def run_gpu(args, w, rank, local):
     # Poisson query stream over the flushed block
     queries = None
     if args.query_rate > 0:
-        queries = serve_under_ingest(args, pipe, hnp, W + 2 * K, K, N, mbr, mnp)
+        queries = serve_under_ingest(args, pipe, hnp, W + 2 * K, S, N, mbr, mnp)
     # compaction: the serving steps' keys become a second block; both merge
     # into one block of split x split CTFs (100 CTFs, as a flush makes)
     compaction = None
@@ -311,6 +314,8 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
 
     th = threading.Thread(target=server, daemon=True)
     pipe.set_step_slices(args.serve_slices)  # query kernels get the GPU between slices
+    gc.collect()
+    gc.disable()  # no collector pause holds the interpreter lock while serving
     th.start()
     step_ms = []
     w0 = time.perf_counter()
@@ -322,6 +327,7 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
     wall = time.perf_counter() - w0
     done.set()
     th.join()
+    gc.enable()
     pipe.set_step_slices(args.step_slices)
     if errors:
         return {"error": errors[0]}
@@ -329,6 +335,8 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
     return {"rate_target_per_s": rate, "answered": len(lat), "qps": len(lat) / wall,
             "p50_ms": float(np.percentile(lat_ms, 50)) if len(lat) else None,
             "p99_ms": float(np.percentile(lat_ms, 99)) if len(lat) else None,
+            "p999_ms": float(np.percentile(lat_ms, 99.9)) if len(lat) else None,
+            "max_ms": float(lat_ms.max()) if len(lat) else None,
             "mean_batch": float(np.mean(sizes)) if sizes else 0.0, "batches": len(sizes),
             "contacts_per_query": contacts[0] / max(len(lat), 1),
             "mix": "60% object (window 10-10000 steps), 40% box (50 m-5 km, window 10-3600 steps); "
@@ -417,6 +425,8 @@ def main():
                     help="Poisson query arrivals per second during the serving phase (0: skip)")
     ap.add_argument("--step-slices", type=int, default=0,
                     help="launches per long step kernel (stc_config.step_slices; 0 = 1)")
+    ap.add_argument("--serve-steps", type=int, default=0,
+                    help="ingest steps of the serving phase (0 = twice --steps)")
     ap.add_argument("--serve-slices", type=int, default=8,
                     help="step slices while the serving phase answers queries (stc_set_step_slices)")
     args = ap.parse_args()

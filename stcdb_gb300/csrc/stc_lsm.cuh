@@ -88,6 +88,7 @@ struct CtbBlock {
   uint32_t *cstart = nullptr;      // [ncells + 1] first position of each cell in perm
   uint32_t *cbase = nullptr;       // [F + 1] first dense cell id of each CTF
   uint4 *ixg = nullptr;            // [F] (g, levels, 0, 0) of each CTF's index
+  double2 *ixs = nullptr;          // [F] level-0 cells per degree in x and y (g / CTF box side)
   uint16_t *pend = nullptr;        // [keys] end offset of the key at each perm position, saturated at
                                    // 65535; within a cell the keys go by increasing end
 };
@@ -105,6 +106,7 @@ struct QBlock {
   const uint32_t *cstart;
   const uint32_t *cbase;
   const uint4 *ixg;
+  const double2 *ixs;
   const uint16_t *pend;
   unsigned long long n_over;
   uint32_t F, index, o_end_time_min, pad;

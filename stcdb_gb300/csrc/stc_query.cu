@@ -291,6 +291,25 @@ __device__ __forceinline__ void cell_range(double a, double b, double m0, double
   hi = min((int)floor(fb) + 1, (int)n);
 }
 
+// Position of v in level-0 cells of a CTF's index: (v - m0) times the CTF's
+// stored cells per degree. Monotone in v, and the same function files keys
+// and bounds queries, which is all the index's exactness needs.
+__device__ __forceinline__ double index_coord(double v, double m0, double scale) {
+  return __dmul_rn(__dsub_rn(v, m0), scale);
+}
+
+// cell_range on the index grid: [lo, hi] of [a, b], one cell of slack either
+// side, clamped to [0, n]; scale 0 (a degenerate CTF box) takes every cell.
+__device__ __forceinline__ void index_range(double a, double b, double m0, double scale, uint32_t n, int &lo,
+                                            int &hi) {
+  const bool ok = scale > 0.0;
+  double fa = ok ? index_coord(a, m0, scale) : 0.0, fb = ok ? index_coord(b, m0, scale) : (double)n;
+  fa = fmax(fmin(fa, (double)n + 2), -2.0);
+  fb = fmax(fmin(fb, (double)n + 2), -2.0);
+  lo = max((int)floor(fa) - 1, 0);
+  hi = min((int)floor(fb) + 1, (int)n);
+}
+
 // ---- cell index of a block ------------------------------------------------------
 
 constexpr uint32_t MAX_CTF = 3969;
@@ -299,8 +318,8 @@ constexpr uint32_t MAX_CTF = 3969;
 // level whose cells cover the extent of its decoded box, the cell of the box's
 // low corner there; or the CTF's wide slot.
 __global__ void k_index_cells(const uint8_t *keys, const stc_ctf *ctfs, uint32_t F, const uint32_t *cbase,
-                              const uint4 *ixg, unsigned long long total, uint32_t *cells, uint32_t *pos,
-                              uint32_t *endo) {
+                              const uint4 *ixg, const double2 *ixs, unsigned long long total, uint32_t *cells,
+                              uint32_t *pos, uint32_t *endo) {
   __shared__ unsigned long long s_first[MAX_CTF + 1];
   for (uint32_t c = threadIdx.x; c < F; c += blockDim.x) s_first[c] = ctfs[c].first_key;
   __syncthreads();
@@ -317,12 +336,13 @@ __global__ void k_index_cells(const uint8_t *keys, const stc_ctf *ctfs, uint32_t
     Key k;
     decode_key(load_key(keys + t.key_offset + (kid - s_first[lo]) * kb, kb), t, k);
     const uint32_t g = ixg[lo].x, levels = ixg[lo].y;
+    const double2 sc = ixs[lo];
     uint32_t cell = 0xFFFFFFFFu;  // the wide slot, after every level
-    if (t.mbr[2] > t.mbr[0] && t.mbr[3] > t.mbr[1]) {
-      double fx0 = grid_coord(k.box[0], t.mbr[0], t.mbr[2], g);
-      double fx1 = grid_coord(k.box[2], t.mbr[0], t.mbr[2], g);
-      double fy0 = grid_coord(k.box[1], t.mbr[1], t.mbr[3], g);
-      double fy1 = grid_coord(k.box[3], t.mbr[1], t.mbr[3], g);
+    if (sc.x > 0.0 && sc.y > 0.0) {
+      double fx0 = index_coord(k.box[0], t.mbr[0], sc.x);
+      double fx1 = index_coord(k.box[2], t.mbr[0], sc.x);
+      double fy0 = index_coord(k.box[1], t.mbr[1], sc.y);
+      double fy1 = index_coord(k.box[3], t.mbr[1], sc.y);
       if (fx0 >= 0 && fy0 >= 0 && fx0 < g + 1 && fy0 < g + 1 && fx1 >= fx0 && fy1 >= fy0) {
         uint32_t l0 = (uint32_t)floor(fx0), l1 = (uint32_t)floor(fy0);
         double ext = fmax(floor(fx1) - l0, floor(fy1) - l1);
@@ -410,7 +430,7 @@ struct BoxCtx {
 };
 
 // Fills x for CTF t and query q; false when the CTF box misses the widened query.
-__device__ bool box_ctx(const stc_ctf &t, const uint4 &ix, const stc_query &q, BoxCtx &x) {
+__device__ bool box_ctx(const stc_ctf &t, const uint4 &ix, const double2 &sc, const stc_query &q, BoxCtx &x) {
   // A decoded box differs from the key's exact box (which set the CTF box
   // and the bitmap) by less than one corner quantum plus one edge quantum on
   // either side (float conversions truncate, and may round up first): widen
@@ -439,27 +459,25 @@ __device__ bool box_ctx(const stc_ctf &t, const uint4 &ix, const stc_query &q, B
   x.ts = x.all_ends ? 0u : q.t_start - t.end_time_min;
   x.g = ix.x;
   x.levels = ix.y;
-  cell_range(x.wide[0], x.wide[2], t.mbr[0], t.mbr[2], x.g, x.i0, x.i1);
-  cell_range(x.wide[1], x.wide[3], t.mbr[1], t.mbr[3], x.g, x.j0, x.j1);
+  index_range(x.wide[0], x.wide[2], t.mbr[0], sc.x, x.g, x.i0, x.i1);
+  index_range(x.wide[1], x.wide[3], t.mbr[1], sc.y, x.g, x.j0, x.j1);
   // Interior cells (counting only, every start passing): level-0 cells whose
   // every decoded low corner lies in the query box. A key's box meets the
-  // query when its low corner is inside it; grid_coord is monotone, so a
+  // query when its low corner is inside it; index_coord is monotone, so a
   // corner in cell i (gc in [i, i + 1)) lies in [q_lo, q_hi] when
   // i > gc(q_lo) and i + 1 <= gc(q_hi).
   x.ii0 = x.jj0 = 1;
   x.ii1 = x.jj1 = 0;
   const bool count_only = (q.kind & STC_QUERY_COUNT_ONLY) != 0;
-  if (count_only && x.all_starts && (x.all_ends || x.ts < 65535u) && t.mbr[2] > t.mbr[0] && t.mbr[3] > t.mbr[1]) {
+  if (count_only && x.all_starts && (x.all_ends || x.ts < 65535u) && sc.x > 0.0 && sc.y > 0.0) {
     auto interior = [](double g0, double g1, uint32_t n, int &lo, int &hi) {
       g0 = fmax(fmin(g0, (double)n + 2), -2.0);
       g1 = fmax(fmin(g1, (double)n + 2), -2.0);
       lo = max((int)floor(g0) + 1, 0);
       hi = min((int)floor(g1) - 1, (int)n);
     };
-    interior(grid_coord(qbox[0], t.mbr[0], t.mbr[2], x.g), grid_coord(qbox[2], t.mbr[0], t.mbr[2], x.g), x.g, x.ii0,
-             x.ii1);
-    interior(grid_coord(qbox[1], t.mbr[1], t.mbr[3], x.g), grid_coord(qbox[3], t.mbr[1], t.mbr[3], x.g), x.g, x.jj0,
-             x.jj1);
+    interior(index_coord(qbox[0], t.mbr[0], sc.x), index_coord(qbox[2], t.mbr[0], sc.x), x.g, x.ii0, x.ii1);
+    interior(index_coord(qbox[1], t.mbr[1], sc.y), index_coord(qbox[3], t.mbr[1], sc.y), x.g, x.jj0, x.jj1);
   }
   return true;
 }
@@ -494,7 +512,7 @@ __global__ void k_box_plan(const QBlock *qb, uint32_t nb, const stc_query *qs, u
       } else {
         const stc_ctf &t = b.ctfs[c];
         BoxCtx x;
-        if (t.kv_count && box_ctx(t, b.ixg[c], q, x)) {
+        if (t.kv_count && box_ctx(t, b.ixg[c], b.ixs[c], q, x)) {
           const double *qbox = q.box;
           const bool count_only = (q.kind & STC_QUERY_COUNT_ONLY) != 0;
           if (count_only && x.all_starts && x.all_ends && qbox[0] <= t.mbr[0] - x.qx && qbox[1] <= t.mbr[1] - x.qy &&
@@ -560,7 +578,7 @@ __global__ void __launch_bounds__(QBOX_THREADS) k_box_rows(const QBlock *qb, uin
     } else {
       const stc_ctf &t = b.ctfs[c];
       BoxCtx x;
-      box_ctx(t, b.ixg[c], q, x);  // the plan saw it pass
+      box_ctx(t, b.ixg[c], b.ixs[c], q, x);  // the plan saw it pass
       const uint32_t cb = b.cbase[c], wide_slot = b.cbase[c + 1] - 1u;
       uint32_t a, e, ma, me2;  // scan [a, ma) and [me2, e); [ma, me2) is counted
       int clo = 1, chi = 0;    // counted cells of this row
@@ -658,9 +676,10 @@ cudaError_t grow(T **p, size_t *cap, size_t need) {
 void free_block(CtbBlock &B) {
   for (void *v : {(void *)B.keys, (void *)B.d_ctfs, (void *)B.bitmaps, (void *)B.sids, (void *)B.orec,
                   (void *)B.obox, (void *)B.obitmap, (void *)B.perm, (void *)B.cstart, (void *)B.cbase,
-                  (void *)B.ixg, (void *)B.pend})
+                  (void *)B.ixg, (void *)B.ixs, (void *)B.pend})
     if (v) cudaFree(v);
   B.ixg = nullptr;
+  B.ixs = nullptr;
   B.pend = nullptr;
   B.keys = nullptr;
   B.d_ctfs = nullptr;
@@ -680,6 +699,7 @@ cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
   const uint32_t F = (uint32_t)B.ctfs.size();
   std::vector<uint32_t> cbase(F + 1, 0);
   std::vector<uint4> ixg(F);
+  std::vector<double2> ixs(F);
   unsigned long long total = 0;
   for (uint32_t c = 0; c < F; c++) {
     const stc_ctf &t = B.ctfs[c];
@@ -689,6 +709,9 @@ cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
     while ((1u << (levels - 1)) < g) levels++;  // down to one cell of the whole box
     for (uint32_t lv = 0; lv < levels; lv++) cells += index_level_side(g, lv) * index_level_side(g, lv);
     ixg[c] = make_uint4(g, levels, 0u, 0u);
+    const double wx = (double)t.mbr[2] - (double)t.mbr[0], wy = (double)t.mbr[3] - (double)t.mbr[1];
+    ixs[c] = make_double2(t.mbr[2] > t.mbr[0] && t.mbr[3] > t.mbr[1] ? (double)g / wx : 0.0,
+                          t.mbr[2] > t.mbr[0] && t.mbr[3] > t.mbr[1] ? (double)g / wy : 0.0);
     cbase[c + 1] = cbase[c] + cells;
     total = std::max<unsigned long long>(total, t.first_key + t.kv_count);
   }
@@ -698,6 +721,8 @@ cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
   if (e == cudaSuccess) e = cudaMalloc(&B.cstart, ((size_t)ncells + 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&B.cbase, (F + 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&B.ixg, std::max<size_t>(F, 1) * sizeof(uint4));
+  if (e == cudaSuccess) e = cudaMalloc(&B.ixs, std::max<size_t>(F, 1) * sizeof(double2));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(B.ixs, ixs.data(), F * sizeof(double2), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(B.cbase, cbase.data(), (F + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(B.ixg, ixg.data(), F * sizeof(uint4), cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return e;
@@ -709,15 +734,15 @@ cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
     while (bits < 32 && ((unsigned long long)ncells >> bits)) bits++;
     // keys by (cell, end offset): stable sorts by end, then by cell
     STC_KL k_set_one<<<1, 1, 0, s>>>(L.n_dev + 3, total);
-    STC_KL k_index_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(B.keys, B.d_ctfs, F, B.cbase, B.ixg, total, sk[0], sk[1],
-                                                         sk[6]);  // ixg copied above on this stream
+    STC_KL k_index_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(B.keys, B.d_ctfs, F, B.cbase, B.ixg, B.ixs, total, sk[0],
+                                                         sk[1], sk[6]);  // ixg, ixs copied above on this stream
     radix_sort_u32(sk[6], sk[1], sk[2], sk[3], sk[4], sk[5], L.n_dev + 3, (size_t)total, 16, L.hist, L.scan, s);
     STC_KL k_gather_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[0], sk[3], sk[4], total);
     radix_sort_u32(sk[4], sk[3], sk[2], B.perm, sk[0], sk[5], L.n_dev + 3, (size_t)total, bits, L.hist, L.scan, s);
     STC_KL k_gather_ends<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[6], B.perm, B.pend, total);
   }
   STC_KL k_cell_starts<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[2], total, ncells, B.cstart);
-  e = cudaStreamSynchronize(s);  // the copies of cbase and ixg read this stack frame
+  e = cudaStreamSynchronize(s);  // the copies of cbase, ixg and ixs read this stack frame
   return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
@@ -874,7 +899,7 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
   for (uint32_t i = 0; i < nb; i++) {
     const CtbBlock &B = H.blocks[i];
     qb[i] = QBlock{B.keys, B.d_ctfs, B.sids, B.orec, B.obox, B.bitmaps, B.obitmap, B.perm, B.cstart, B.cbase, B.ixg,
-                   B.pend,
+                   B.ixs, B.pend,
                    (unsigned long long)B.info.oversize_kv_count, B.info.ctf_count, B.info.index,
                    B.info.o_end_time_min, 0};
   }

@@ -139,49 +139,82 @@ __global__ void k_rs_hist(const uint32_t *keys, const unsigned long long *n_dev,
   hist[(size_t)threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
 }
 
-__global__ void k_rs_scatter(const uint32_t *k_in, const uint32_t *v_in, uint32_t *k_out, uint32_t *v_out,
-                             const unsigned long long *n_dev, size_t n_max, int shift, uint32_t dmask,
-                             const uint32_t *hist, uint32_t nb) {
-  __shared__ uint32_t base_off[256];
+// One tile of RS_TILE items: each item's stable rank among the tile's items
+// of its digit (as k_rs_hist counted them) places it in a shared-memory copy
+// of the tile ordered by digit; the tile is then written out one digit run
+// after another, so that neighbouring threads write neighbouring addresses.
+// hist holds the exclusive scan of the counts laid out [digit][tile].
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t *k_in, const uint32_t *v_in,
+                                                           uint32_t *k_out, uint32_t *v_out,
+                                                           const unsigned long long *n_dev, size_t n_max, int shift,
+                                                           uint32_t dmask, const uint32_t *hist, uint32_t nb) {
+  __shared__ uint32_t s_key[RS_TILE];
+  __shared__ uint32_t s_val[RS_TILE];
+  __shared__ uint32_t base_off[256];  // global position of the tile's first item of each digit
+  __shared__ uint32_t loc[256];       // the same in the tile's digit order
   __shared__ uint32_t running[256];
   __shared__ uint32_t warp_cnt[RS_WARPS][256];
+  __shared__ uint32_t scan_tmp[RS_WARPS];
   size_t n = (size_t)*n_dev;
   if (n > n_max) n = n_max;
   size_t tile = (size_t)blockIdx.x * RS_TILE;
   if (tile >= n) return;
-  base_off[threadIdx.x] = hist[(size_t)threadIdx.x * nb + blockIdx.x];
-  running[threadIdx.x] = 0;
-  uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  uint32_t lt_mask = (1u << lane) - 1u;
+  const uint32_t d0 = threadIdx.x, lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  {
+    const size_t idx = (size_t)d0 * nb + blockIdx.x;
+    const uint32_t b = hist[idx];
+    const uint32_t next = idx + 1 < (size_t)256 * nb ? hist[idx + 1] : (uint32_t)n;
+    base_off[d0] = b;
+    // exclusive scan of this tile's digit counts over the 256 digits
+    uint32_t cnt = next - b, incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += v;
+    }
+    if (lane == 31) scan_tmp[warp] = incl;
+    __syncthreads();
+    uint32_t before = 0;
+    for (uint32_t w = 0; w < warp; w++) before += scan_tmp[w];
+    loc[d0] = before + incl - cnt;
+    running[d0] = 0;
+  }
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const uint32_t in_tile = (uint32_t)min((size_t)RS_TILE, n - tile);
   for (int it = 0; it < RS_ITEMS; it++) {
     for (int w = 0; w < RS_WARPS; w++) warp_cnt[w][threadIdx.x] = 0;
     __syncthreads();
-    size_t idx = tile + (size_t)it * RS_THREADS + threadIdx.x;
-    bool valid = idx < n;
-    uint32_t key = valid ? k_in[idx] : 0u;
-    uint32_t val = valid ? v_in[idx] : 0u;
-    uint32_t digit = valid ? ((key >> shift) & dmask) : (256u + lane);
-    uint32_t peers = __match_any_sync(0xffffffffu, digit);
-    uint32_t rank = __popc(peers & lt_mask);
+    const uint32_t li = (uint32_t)it * RS_THREADS + threadIdx.x;
+    const bool valid = li < in_tile;
+    const uint32_t key = valid ? k_in[tile + li] : 0u;
+    const uint32_t val = valid ? v_in[tile + li] : 0u;
+    const uint32_t digit = valid ? ((key >> shift) & dmask) : (256u + lane);
+    const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+    const uint32_t rank = __popc(peers & lt_mask);
     if (valid && rank == 0) warp_cnt[warp][digit] = __popc(peers);
     __syncthreads();
     {
-      uint32_t d = threadIdx.x;
-      uint32_t acc = running[d];
+      uint32_t acc = running[d0];
       for (int w = 0; w < RS_WARPS; w++) {
-        uint32_t c = warp_cnt[w][d];
-        warp_cnt[w][d] = acc;
+        uint32_t c = warp_cnt[w][d0];
+        warp_cnt[w][d0] = acc;
         acc += c;
       }
-      running[d] = acc;
+      running[d0] = acc;
     }
     __syncthreads();
     if (valid) {
-      uint32_t pos = base_off[digit] + warp_cnt[warp][digit] + rank;
-      k_out[pos] = key;
-      v_out[pos] = val;
+      const uint32_t pos = loc[digit] + warp_cnt[warp][digit] + rank;
+      s_key[pos] = key;
+      s_val[pos] = val;
     }
-    __syncthreads();
+    __syncthreads();  // warp_cnt is cleared for the next items
+  }
+  for (uint32_t i = threadIdx.x; i < in_tile; i += RS_THREADS) {
+    const uint32_t key = s_key[i], digit = (key >> shift) & dmask;
+    const uint32_t pos = base_off[digit] + (i - loc[digit]);
+    k_out[pos] = key;
+    v_out[pos] = s_val[i];
   }
 }
 
