@@ -382,6 +382,36 @@ def flush_line(f, peak):
                 frac_of_peak=gbs / peak)
 
 
+def sort_line(device, peak, n=100_000_000, reps=5):
+    """The library's stable LSD radix sort (stc_sort_pairs_u32) on n random
+    32-bit (key, value) pairs in HBM: 4 passes of 8 bits, each reading and
+    writing every key and value once, 16 * 4 = 64 algorithmic bytes per pair.
+    Device time of the passes only (the call's scratch allocation excluded)."""
+    import ctypes
+    import torch
+    from stcdb_gb300._lib import load_library
+    lib = load_library("libstc")
+    lib.stc_sort_pairs_u32.restype = ctypes.c_int
+    lib.stc_sort_pairs_u32.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_size_t, ctypes.c_uint32, ctypes.c_uint32]
+    lib.stc_last_sort_ms.restype = ctypes.c_float
+    g = torch.Generator(device=f"cuda:{device}").manual_seed(3)
+    k = torch.randint(0, 2 ** 31 - 1, (n,), dtype=torch.int32, device=f"cuda:{device}", generator=g)
+    v = torch.arange(n, dtype=torch.int32, device=f"cuda:{device}")
+    ko, vo = torch.empty_like(k), torch.empty_like(v)
+    times = []
+    for r in range(reps + 2):
+        if lib.stc_sort_pairs_u32(k.data_ptr(), v.data_ptr(), ko.data_ptr(), vo.data_ptr(), n, 32, device) != 0:
+            return {"error": "stc_sort_pairs_u32 failed"}
+        if r >= 2:
+            times.append(float(lib.stc_last_sort_ms()))
+    ms = statistics.median(times)
+    ok = bool(torch.all(ko[1:] >= ko[:-1]).item())
+    b = 64.0 * n
+    del k, v, ko, vo
+    return {"pairs": n, "key_bits": 32, "ms": ms, "pairs_per_s": n / (ms / 1e3), "algorithmic_bytes": b,
+            "achieved_gbs": b / (ms / 1e3) / 1e9, "frac_of_peak": b / (ms / 1e3) / 1e9 / peak, "sorted": ok}
+
+
 def compaction_line(c, peak):
     """Merge throughput; algorithmic bytes 2 x 32 per merged key (read and
     write each key and its box once)."""
@@ -499,6 +529,7 @@ def main():
         "queries_under_ingest": r["queries"],
         "trace_gen": r["trace_gen"],
         "compaction": compaction_line(r["compaction"], peak),
+        "sort": sort_line(local, peak),
         "per_step": {"pair_tests": s_last.pair_tests, "exact_tests": s_last.exact_tests, "hits": s_last.hits,
                      "new_candidates": s_last.new_candidates, "live_meetings": s_last.taken_buckets,
                      "emitted": s_last.emitted, "border_units": s_last.border_units, "leaves": s_last.leaves,

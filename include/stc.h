@@ -390,6 +390,10 @@ stc_status stc_sort_pairs_u32(const uint32_t *keys, const uint32_t *values, uint
  * each other's results. The call returns when the sort is done.
  * No counterpart in the reference. Errors: stc_last_error(NULL). */
 #define STC_SORT_NOALLOC_MAX_PAIRS (1u << 20)
+
+/* Device time in milliseconds of the sort passes of the last successful
+ * stc_sort_pairs_u32 call on this thread (scratch allocation excluded). */
+float stc_last_sort_ms(void);
 stc_status stc_sort_pairs_u32_noalloc(const uint32_t *keys, const uint32_t *values, uint32_t *keys_out,
                                       uint32_t *values_out, size_t n, uint32_t key_bits, uint32_t device);
 

@@ -130,20 +130,33 @@ __global__ void k_rs_hist(const uint32_t *keys, const unsigned long long *n_dev,
   if (n > n_max) n = n_max;
   size_t base = (size_t)blockIdx.x * RS_TILE;
   if (base < n) {
+    // all of the thread's items are requested before any is counted
+    uint32_t kr[RS_ITEMS];
+#pragma unroll
     for (int i = 0; i < RS_ITEMS; i++) {
       size_t idx = base + (size_t)i * RS_THREADS + threadIdx.x;
-      if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & dmask], 1u);
+      kr[i] = idx < n ? keys[idx] : 0u;  // kept in L2 for the scatter that follows
+    }
+#pragma unroll
+    for (int i = 0; i < RS_ITEMS; i++) {
+      size_t idx = base + (size_t)i * RS_THREADS + threadIdx.x;
+      if (idx < n) atomicAdd(&h[(kr[i] >> shift) & dmask], 1u);
     }
   }
   __syncthreads();
   hist[(size_t)threadIdx.x * nb + blockIdx.x] = h[threadIdx.x];
 }
 
-// One tile of RS_TILE items: each item's stable rank among the tile's items
-// of its digit (as k_rs_hist counted them) places it in a shared-memory copy
-// of the tile ordered by digit; the tile is then written out one digit run
-// after another, so that neighbouring threads write neighbouring addresses.
-// hist holds the exclusive scan of the counts laid out [digit][tile].
+// One tile of RS_TILE items, stable. Warp w takes the tile's items
+// [w * 512, (w + 1) * 512) in order, 32 at a time, and ranks each among the
+// warp's earlier items of its digit with a warp-private histogram; one scan
+// over (digit, warp) then places every item in a shared-memory copy of the
+// tile ordered by digit, which is written out one digit run after another,
+// so that neighbouring threads write neighbouring addresses. hist holds the
+// exclusive scan of the counts laid out [digit][tile].
+static constexpr int RS_WARP_ITEMS = RS_TILE / RS_WARPS;  // 512
+static_assert(RS_WARP_ITEMS == 32 * RS_ITEMS, "warp share");
+
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t *k_in, const uint32_t *v_in,
                                                            uint32_t *k_out, uint32_t *v_out,
                                                            const unsigned long long *n_dev, size_t n_max, int shift,
@@ -152,21 +165,55 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t *k_in,
   __shared__ uint32_t s_val[RS_TILE];
   __shared__ uint32_t base_off[256];  // global position of the tile's first item of each digit
   __shared__ uint32_t loc[256];       // the same in the tile's digit order
-  __shared__ uint32_t running[256];
-  __shared__ uint32_t warp_cnt[RS_WARPS][256];
+  __shared__ uint32_t whist[RS_WARPS][256];
   __shared__ uint32_t scan_tmp[RS_WARPS];
   size_t n = (size_t)*n_dev;
   if (n > n_max) n = n_max;
   size_t tile = (size_t)blockIdx.x * RS_TILE;
   if (tile >= n) return;
-  const uint32_t d0 = threadIdx.x, lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const uint32_t in_tile = (uint32_t)min((size_t)RS_TILE, n - tile);
+  base_off[threadIdx.x] = hist[(size_t)threadIdx.x * nb + blockIdx.x];
+  for (int w = 0; w < RS_WARPS; w++) whist[w][threadIdx.x] = 0;
+  // all of the thread's items are requested before the ranking starts
+  uint32_t kr[RS_ITEMS], vr[RS_ITEMS], pr[RS_ITEMS];
+#pragma unroll
+  for (int it = 0; it < RS_ITEMS; it++) {
+    const uint32_t li = warp * RS_WARP_ITEMS + (uint32_t)it * 32u + lane;
+    kr[it] = li < in_tile ? __ldcs(&k_in[tile + li]) : 0u;
+    vr[it] = li < in_tile ? __ldcs(&v_in[tile + li]) : 0u;
+  }
+  __syncthreads();
+  uint32_t *wh = whist[warp];
+#pragma unroll
+  for (int it = 0; it < RS_ITEMS; it++) {
+    const uint32_t li = warp * RS_WARP_ITEMS + (uint32_t)it * 32u + lane;
+    const bool valid = li < in_tile;
+    const uint32_t digit = valid ? ((kr[it] >> shift) & dmask) : (256u + lane);
+    const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+    const uint32_t rank = __popc(peers & lt_mask);
+    const uint32_t leader = __ffs(peers) - 1u;
+    uint32_t before = 0;
+    if (valid && rank == 0) {
+      before = wh[digit];
+      wh[digit] = before + __popc(peers);
+    }
+    before = __shfl_sync(0xffffffffu, before, leader);
+    pr[it] = before + rank;  // position among the warp's items of this digit
+    __syncwarp();
+  }
+  __syncthreads();
   {
-    const size_t idx = (size_t)d0 * nb + blockIdx.x;
-    const uint32_t b = hist[idx];
-    const uint32_t next = idx + 1 < (size_t)256 * nb ? hist[idx + 1] : (uint32_t)n;
-    base_off[d0] = b;
-    // exclusive scan of this tile's digit counts over the 256 digits
-    uint32_t cnt = next - b, incl = cnt;
+    // per digit: the tile's exclusive offset, and each warp's offset within it
+    const uint32_t d = threadIdx.x;
+    uint32_t cnt = 0;
+    for (int w = 0; w < RS_WARPS; w++) {
+      const uint32_t c = whist[w][d];
+      whist[w][d] = cnt;
+      cnt += c;
+    }
+    uint32_t incl = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
@@ -176,40 +223,20 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t *k_in,
     __syncthreads();
     uint32_t before = 0;
     for (uint32_t w = 0; w < warp; w++) before += scan_tmp[w];
-    loc[d0] = before + incl - cnt;
-    running[d0] = 0;
+    loc[d] = before + incl - cnt;
   }
-  const uint32_t lt_mask = (1u << lane) - 1u;
-  const uint32_t in_tile = (uint32_t)min((size_t)RS_TILE, n - tile);
+  __syncthreads();
+#pragma unroll
   for (int it = 0; it < RS_ITEMS; it++) {
-    for (int w = 0; w < RS_WARPS; w++) warp_cnt[w][threadIdx.x] = 0;
-    __syncthreads();
-    const uint32_t li = (uint32_t)it * RS_THREADS + threadIdx.x;
-    const bool valid = li < in_tile;
-    const uint32_t key = valid ? k_in[tile + li] : 0u;
-    const uint32_t val = valid ? v_in[tile + li] : 0u;
-    const uint32_t digit = valid ? ((key >> shift) & dmask) : (256u + lane);
-    const uint32_t peers = __match_any_sync(0xffffffffu, digit);
-    const uint32_t rank = __popc(peers & lt_mask);
-    if (valid && rank == 0) warp_cnt[warp][digit] = __popc(peers);
-    __syncthreads();
-    {
-      uint32_t acc = running[d0];
-      for (int w = 0; w < RS_WARPS; w++) {
-        uint32_t c = warp_cnt[w][d0];
-        warp_cnt[w][d0] = acc;
-        acc += c;
-      }
-      running[d0] = acc;
+    const uint32_t li = warp * RS_WARP_ITEMS + (uint32_t)it * 32u + lane;
+    if (li < in_tile) {
+      const uint32_t digit = (kr[it] >> shift) & dmask;
+      const uint32_t pos = loc[digit] + whist[warp][digit] + pr[it];
+      s_key[pos] = kr[it];
+      s_val[pos] = vr[it];
     }
-    __syncthreads();
-    if (valid) {
-      const uint32_t pos = loc[digit] + warp_cnt[warp][digit] + rank;
-      s_key[pos] = key;
-      s_val[pos] = val;
-    }
-    __syncthreads();  // warp_cnt is cleared for the next items
   }
+  __syncthreads();
   for (uint32_t i = threadIdx.x; i < in_tile; i += RS_THREADS) {
     const uint32_t key = s_key[i], digit = (key >> shift) & dmask;
     const uint32_t pos = base_off[digit] + (i - loc[digit]);

@@ -14,6 +14,28 @@ namespace {
 
 __global__ void k_set_count(unsigned long long *dst, unsigned long long v) { *dst = v; }
 
+thread_local float t_last_sort_ms = 0.0f;
+
+// Device time of the sort kernels (events around them on stream 0).
+struct SortTimer {
+  cudaEvent_t a = nullptr, b = nullptr;
+  SortTimer() {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+  }
+  ~SortTimer() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+  void start() { cudaEventRecord(a, 0); }
+  void stop() { cudaEventRecord(b, 0); }
+  void read() {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, a, b) == cudaSuccess) t_last_sort_ms = ms;
+    cudaGetLastError();
+  }
+};
+
 stc_status sort_args_ok(const uint32_t *keys, const uint32_t *values, uint32_t *keys_out, uint32_t *values_out,
                         size_t n, uint32_t key_bits, const char *who) {
   if (key_bits < 1 || key_bits > 32 || n > (size_t)1 << 31 ||
@@ -40,10 +62,14 @@ extern "C" stc_status stc_sort_pairs_u32(const uint32_t *keys, const uint32_t *v
   if (e == cudaSuccess) e = cudaMalloc(&scan, scan_tmp_words(hw) * 4);
   if (e == cudaSuccess) e = cudaMalloc(&n_dev, sizeof(unsigned long long));
   if (e == cudaSuccess) {
+    SortTimer tm;
     STC_KL k_set_count<<<1, 1, 0, 0>>>(n_dev, (unsigned long long)n);
+    tm.start();
     radix_sort_u32(keys, values, keys_out, values_out, ktmp, vtmp, n_dev, n, (int)key_bits, hist, scan, 0);
+    tm.stop();
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+    if (e == cudaSuccess) tm.read();
   }
   cudaFree(ktmp);
   cudaFree(vtmp);
@@ -136,3 +162,5 @@ extern "C" stc_status stc_sort_pairs_u32_noalloc(const uint32_t *keys, const uin
   }
   return STC_OK;
 }
+
+extern "C" float stc_last_sort_ms(void) { return t_last_sort_ms; }
