@@ -190,8 +190,16 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t *k_in,
   for (int it = 0; it < RS_ITEMS; it++) {
     const uint32_t li = warp * RS_WARP_ITEMS + (uint32_t)it * 32u + lane;
     const bool valid = li < in_tile;
-    const uint32_t digit = valid ? ((kr[it] >> shift) & dmask) : (256u + lane);
-    const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+    const uint32_t digit = (kr[it] >> shift) & dmask;
+    // lanes with the same digit: one vote per digit bit (valid lanes only)
+    uint32_t peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+    for (int b = 0; b < 8; b++) {
+      const bool bit = (digit >> b) & 1u;
+      const uint32_t m = __ballot_sync(0xffffffffu, bit);
+      peers &= bit ? m : ~m;
+    }
+    if (!valid) peers = 1u << lane;
     const uint32_t rank = __popc(peers & lt_mask);
     const uint32_t leader = __ffs(peers) - 1u;
     uint32_t before = 0;
