@@ -353,11 +353,22 @@ __global__ void k_lsm_encode(LsmDev L, unsigned long long total, unsigned long l
     // 8 KB slot are skipped, so the loops stop where every bit would be
     h0 = min(h0, 65535u);
     h1 = min(h1, 65535u / max(1u, (uint32_t)t.x_grid));
+    // bits i + j * x_grid for i in [l0, h0], j in [l1, h1], below 65536: per
+    // row one contiguous run, set a word at a time, and only where a bit of
+    // the run is still clear
     uint32_t *bm = L.bitmaps + (size_t)c * (STC_BITMAP_BYTES / 4);
-    for (uint32_t i = l0; i <= h0; i++)
+    if (t.x_grid == 0) h1 = min(h1, l1);  // every row is the same run
+    if (l0 <= h0)
       for (uint32_t j = l1; j <= h1; j++) {
-        unsigned long long bit = (unsigned long long)i + (unsigned long long)j * t.x_grid;
-        if (bit < 65536ull) atomicOr(&bm[bit >> 5], 1u << (bit & 31u));
+        const unsigned long long a = (unsigned long long)l0 + (unsigned long long)j * t.x_grid;
+        if (a > 65535ull) break;  // later rows start no lower
+        const uint32_t lo = (uint32_t)a;
+        const uint32_t hi = (uint32_t)min((unsigned long long)h0 + (unsigned long long)j * t.x_grid, 65535ull);
+        for (uint32_t w = lo >> 5; w <= (hi >> 5); w++) {
+          const uint32_t b0 = max(lo, w << 5) & 31u, b1 = min(hi, (w << 5) + 31u) & 31u;
+          const uint32_t mask = (0xFFFFFFFFu >> (31u - b1)) & (0xFFFFFFFFu << b0);
+          if ((__ldcg(&bm[w]) & mask) != mask) atomicOr(&bm[w], mask);
+        }
       }
     unsigned long long pid_field = kid >= slim ? r.x : (((unsigned long long)L.sid[r.x] << 26) | r.x);
     unsigned long long vm = serialize_mbr_dev(b, t);

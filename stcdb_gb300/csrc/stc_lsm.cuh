@@ -89,7 +89,9 @@ struct CtbBlock {
   uint32_t *cbase = nullptr;       // [F + 1] first dense cell id of each CTF
   uint4 *ixg = nullptr;            // [F] (g, levels, 0, 0) of each CTF's index
   double2 *ixs = nullptr;          // [F] level-0 cells per degree in x and y (g / CTF box side)
-  uint16_t *pend = nullptr;        // [keys] end offset of the key at each perm position, saturated at
+  float4 *ixf = nullptr;           // [2F] float filing of keys: per axis (cells per low unit, cells per
+                                   // edge unit, error margin, 1 if usable)
+  uint16_t *pend = nullptr;       // [keys] end offset of the key at each perm position, saturated at
                                    // 65535; within a cell the keys go by increasing end
 };
 

@@ -28,7 +28,7 @@ struct Key {
   double box[4];
 };
 
-__device__ __forceinline__ unsigned long long mask64(uint32_t bits) {
+__host__ __device__ __forceinline__ unsigned long long mask64(uint32_t bits) {
   return bits >= 64 ? ~0ull : (1ull << bits) - 1;
 }
 
@@ -317,9 +317,75 @@ constexpr uint32_t MAX_CTF = 3969;
 // Dense cell id of each CTF key in its CTF's loose grid (stc_lsm.cuh): the
 // level whose cells cover the extent of its decoded box, the cell of the box's
 // low corner there; or the CTF's wide slot.
+//
+// The cell depends on the decoded box only through floor() of its four corner
+// coordinates in level-0 cells. These are first computed in float from the
+// key's integer fields (cells per field unit, ixf); a corner whose float value
+// lies within its error margin of an integer could floor the other way, and
+// only keys with such a corner take the exact decode (four correctly rounded
+// FP64 divisions, which the key's filing must agree with).
+struct IndexFile {
+  uint32_t l0, l1;  // floor of the low corner, level-0 cells
+  float ext;        // extent in level-0 cells: max over x, y of floor(high) - floor(low)
+  bool inside;      // low corner in [0, g + 1) on both axes
+};
+
+__device__ __forceinline__ uint32_t index_cell_of(const IndexFile &f, uint32_t g, uint32_t levels) {
+  if (!f.inside) return 0xFFFFFFFFu;
+  uint32_t lv = 0, off = 0;
+  while (lv + 1 < levels && f.ext > (float)(1u << lv)) {
+    uint32_t side = index_level_side(g, lv);
+    off += side * side;
+    lv++;
+  }
+  if (f.ext > (float)(1u << lv)) return 0xFFFFFFFFu;
+  return off + (f.l1 >> lv) * index_level_side(g, lv) + (f.l0 >> lv);
+}
+
+// floor(v) when every value within d of v has the same floor; else false.
+__device__ __forceinline__ bool sure_floor(float v, float d, float &fl) {
+  fl = floorf(v - d);
+  return fl == floorf(v + d);
+}
+
+__device__ __forceinline__ bool index_file_fast(unsigned long long vm, const stc_ctf &c, const float4 &ax,
+                                                const float4 &ay, uint32_t g, IndexFile &f) {
+  if (ax.w == 0.0f || ay.w == 0.0f) return false;
+  const unsigned long long y = vm & mask64(c.edge_bit);
+  vm >>= c.edge_bit;
+  const unsigned long long x = vm & mask64(c.edge_bit);
+  vm >>= c.edge_bit;
+  const unsigned long long low1 = vm & mask64(c.low_y_bit);
+  vm >>= c.low_y_bit;
+  const unsigned long long low0 = vm & mask64(c.low_x_bit);
+  const float fx0 = __ull2float_rn(low0) * ax.x, fy0 = __ull2float_rn(low1) * ay.x;
+  const float fx1 = fx0 + __ull2float_rn(x) * ax.y, fy1 = fy0 + __ull2float_rn(y) * ay.y;
+  float a, b, p, q;
+  if (!sure_floor(fx0, fmaf(fx0, 1e-6f, ax.z), a) || !sure_floor(fy0, fmaf(fy0, 1e-6f, ay.z), b) ||
+      !sure_floor(fx1, fmaf(fx1, 1e-6f, ax.z), p) || !sure_floor(fy1, fmaf(fy1, 1e-6f, ay.z), q))
+    return false;
+  f.inside = a >= 0.0f && b >= 0.0f && a <= (float)g && b <= (float)g;
+  f.l0 = f.inside ? (uint32_t)a : 0u;
+  f.l1 = f.inside ? (uint32_t)b : 0u;
+  f.ext = fmaxf(p - a, q - b);
+  return true;
+}
+
+__device__ __forceinline__ void index_file_exact(unsigned long long vm, const stc_ctf &c, const double2 sc,
+                                                 uint32_t g, IndexFile &f) {
+  double box[4];
+  exact_box(vm, c, box);
+  const double fx0 = index_coord(box[0], c.mbr[0], sc.x), fx1 = index_coord(box[2], c.mbr[0], sc.x);
+  const double fy0 = index_coord(box[1], c.mbr[1], sc.y), fy1 = index_coord(box[3], c.mbr[1], sc.y);
+  f.inside = fx0 >= 0 && fy0 >= 0 && fx0 < g + 1 && fy0 < g + 1 && fx1 >= fx0 && fy1 >= fy0;
+  f.l0 = f.inside ? (uint32_t)floor(fx0) : 0u;
+  f.l1 = f.inside ? (uint32_t)floor(fy0) : 0u;
+  f.ext = f.inside ? (float)fmax(floor(fx1) - f.l0, floor(fy1) - f.l1) : 0.0f;
+}
+
 __global__ void k_index_cells(const uint8_t *keys, const stc_ctf *ctfs, uint32_t F, const uint32_t *cbase,
-                              const uint4 *ixg, const double2 *ixs, unsigned long long total, uint32_t *cells,
-                              uint32_t *pos, uint32_t *endo) {
+                              const uint4 *ixg, const double2 *ixs, const float4 *ixf, unsigned long long total,
+                              uint32_t *cells, uint32_t *pos, uint32_t *endo) {
   __shared__ unsigned long long s_first[MAX_CTF + 1];
   for (uint32_t c = threadIdx.x; c < F; c += blockDim.x) s_first[c] = ctfs[c].first_key;
   __syncthreads();
@@ -334,26 +400,14 @@ __global__ void k_index_cells(const uint8_t *keys, const stc_ctf *ctfs, uint32_t
     const stc_ctf &t = ctfs[lo];
     const uint32_t kb = t.key_bit / 8u;
     Key k;
-    decode_key(load_key(keys + t.key_offset + (kid - s_first[lo]) * kb, kb), t, k);
+    const unsigned long long vm = key_fields(load_key(keys + t.key_offset + (kid - s_first[lo]) * kb, kb), t, k);
     const uint32_t g = ixg[lo].x, levels = ixg[lo].y;
     const double2 sc = ixs[lo];
     uint32_t cell = 0xFFFFFFFFu;  // the wide slot, after every level
     if (sc.x > 0.0 && sc.y > 0.0) {
-      double fx0 = index_coord(k.box[0], t.mbr[0], sc.x);
-      double fx1 = index_coord(k.box[2], t.mbr[0], sc.x);
-      double fy0 = index_coord(k.box[1], t.mbr[1], sc.y);
-      double fy1 = index_coord(k.box[3], t.mbr[1], sc.y);
-      if (fx0 >= 0 && fy0 >= 0 && fx0 < g + 1 && fy0 < g + 1 && fx1 >= fx0 && fy1 >= fy0) {
-        uint32_t l0 = (uint32_t)floor(fx0), l1 = (uint32_t)floor(fy0);
-        double ext = fmax(floor(fx1) - l0, floor(fy1) - l1);
-        uint32_t lv = 0, off = 0;
-        while (lv + 1 < levels && ext > (double)(1u << lv)) {
-          uint32_t side = index_level_side(g, lv);
-          off += side * side;
-          lv++;
-        }
-        if (ext <= (double)(1u << lv)) cell = off + (l1 >> lv) * index_level_side(g, lv) + (l0 >> lv);
-      }
+      IndexFile f;
+      if (!index_file_fast(vm, t, ixf[2 * lo], ixf[2 * lo + 1], g, f)) index_file_exact(vm, t, sc, g, f);
+      cell = index_cell_of(f, g, levels);
     }
     if (cell == 0xFFFFFFFFu) cell = cbase[lo + 1] - cbase[lo] - 1;
     cells[kid] = cbase[lo] + cell;
@@ -676,8 +730,9 @@ cudaError_t grow(T **p, size_t *cap, size_t need) {
 void free_block(CtbBlock &B) {
   for (void *v : {(void *)B.keys, (void *)B.d_ctfs, (void *)B.bitmaps, (void *)B.sids, (void *)B.orec,
                   (void *)B.obox, (void *)B.obitmap, (void *)B.perm, (void *)B.cstart, (void *)B.cbase,
-                  (void *)B.ixg, (void *)B.ixs, (void *)B.pend})
+                  (void *)B.ixg, (void *)B.ixs, (void *)B.ixf, (void *)B.pend})
     if (v) cudaFree(v);
+  B.ixf = nullptr;
   B.ixg = nullptr;
   B.ixs = nullptr;
   B.pend = nullptr;
@@ -695,11 +750,31 @@ void free_block(CtbBlock &B) {
 
 static void retain_block(LsmHost &H, CtbBlock &&B);
 
+// Float filing coefficients of one axis of CTF t (k_index_cells): level-0
+// cells per unit of the low field and of the edge field, the absolute error
+// margin of the exact filing in cells, and 1 when the float filing applies.
+// The exact corner differs from its real value by a few units of 2^-52 of the
+// largest coordinate (one division, one product, two sums and a difference,
+// each correctly rounded); the margin is 2^6 times that.
+static float4 index_file_coeffs(const stc_ctf &t, double scale, bool x_axis) {
+  const float wx = t.mbr[2] - t.mbr[0], wy = t.mbr[3] - t.mbr[1];
+  const double w = x_axis ? wx : wy, le = std::max(wx, wy);
+  const double lowmax = (double)mask64(x_axis ? t.low_x_bit : t.low_y_bit), edgemax = (double)mask64(t.edge_bit);
+  double m = 0.0;
+  for (int i = 0; i < 4; i++) m = std::max(m, std::fabs((double)t.mbr[i]));
+  m += le + 1.0;
+  const double a = scale * w / lowmax, b = scale * le / edgemax, d = scale * m * std::ldexp(1.0, -46);
+  const bool ok = scale > 0.0 && w > 0.0 && le > 0.0 && lowmax > 0.0 && edgemax > 0.0 && std::isfinite(a) &&
+                  std::isfinite(b) && std::isfinite(d) && a < 1e30 && b < 1e30 && d < 1e30;
+  return ok ? make_float4((float)a, (float)b, (float)d + 1e-9f, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
 cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
   const uint32_t F = (uint32_t)B.ctfs.size();
   std::vector<uint32_t> cbase(F + 1, 0);
   std::vector<uint4> ixg(F);
   std::vector<double2> ixs(F);
+  std::vector<float4> ixf(2 * (size_t)F);
   unsigned long long total = 0;
   for (uint32_t c = 0; c < F; c++) {
     const stc_ctf &t = B.ctfs[c];
@@ -712,6 +787,8 @@ cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
     const double wx = (double)t.mbr[2] - (double)t.mbr[0], wy = (double)t.mbr[3] - (double)t.mbr[1];
     ixs[c] = make_double2(t.mbr[2] > t.mbr[0] && t.mbr[3] > t.mbr[1] ? (double)g / wx : 0.0,
                           t.mbr[2] > t.mbr[0] && t.mbr[3] > t.mbr[1] ? (double)g / wy : 0.0);
+    ixf[2 * c] = index_file_coeffs(t, ixs[c].x, true);
+    ixf[2 * c + 1] = index_file_coeffs(t, ixs[c].y, false);
     cbase[c + 1] = cbase[c] + cells;
     total = std::max<unsigned long long>(total, t.first_key + t.kv_count);
   }
@@ -722,7 +799,9 @@ cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
   if (e == cudaSuccess) e = cudaMalloc(&B.cbase, (F + 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&B.ixg, std::max<size_t>(F, 1) * sizeof(uint4));
   if (e == cudaSuccess) e = cudaMalloc(&B.ixs, std::max<size_t>(F, 1) * sizeof(double2));
+  if (e == cudaSuccess) e = cudaMalloc(&B.ixf, std::max<size_t>(2 * (size_t)F, 1) * sizeof(float4));
   if (e == cudaSuccess) e = cudaMemcpyAsync(B.ixs, ixs.data(), F * sizeof(double2), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(B.ixf, ixf.data(), 2 * (size_t)F * sizeof(float4), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(B.cbase, cbase.data(), (F + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(B.ixg, ixg.data(), F * sizeof(uint4), cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return e;
@@ -734,8 +813,8 @@ cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
     while (bits < 32 && ((unsigned long long)ncells >> bits)) bits++;
     // keys by (cell, end offset): stable sorts by end, then by cell
     STC_KL k_set_one<<<1, 1, 0, s>>>(L.n_dev + 3, total);
-    STC_KL k_index_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(B.keys, B.d_ctfs, F, B.cbase, B.ixg, B.ixs, total, sk[0],
-                                                         sk[1], sk[6]);  // ixg, ixs copied above on this stream
+    STC_KL k_index_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(B.keys, B.d_ctfs, F, B.cbase, B.ixg, B.ixs, B.ixf, total,
+                                                         sk[0], sk[1], sk[6]);  // tables copied above on this stream
     radix_sort_u32(sk[6], sk[1], sk[2], sk[3], sk[4], sk[5], L.n_dev + 3, (size_t)total, 16, L.hist, L.scan, s);
     STC_KL k_gather_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[0], sk[3], sk[4], total);
     radix_sort_u32(sk[4], sk[3], sk[2], B.perm, sk[0], sk[5], L.n_dev + 3, (size_t)total, bits, L.hist, L.scan, s);
