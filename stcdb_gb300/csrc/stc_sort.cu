@@ -161,8 +161,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t *k_in,
                                                            uint32_t *k_out, uint32_t *v_out,
                                                            const unsigned long long *n_dev, size_t n_max, int shift,
                                                            uint32_t dmask, const uint32_t *hist, uint32_t nb) {
-  __shared__ uint32_t s_key[RS_TILE];
-  __shared__ uint32_t s_val[RS_TILE];
+  __shared__ uint2 s_kv[RS_TILE];     // the tile in digit order
   __shared__ uint32_t base_off[256];  // global position of the tile's first item of each digit
   __shared__ uint32_t loc[256];       // the same in the tile's digit order
   __shared__ uint32_t whist[RS_WARPS][256];
@@ -232,6 +231,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t *k_in,
     uint32_t before = 0;
     for (uint32_t w = 0; w < warp; w++) before += scan_tmp[w];
     loc[d] = before + incl - cnt;
+    base_off[d] -= before + incl - cnt;  // now: output position of tile position i of digit d, less i
   }
   __syncthreads();
 #pragma unroll
@@ -240,16 +240,15 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t *k_in,
     if (li < in_tile) {
       const uint32_t digit = (kr[it] >> shift) & dmask;
       const uint32_t pos = loc[digit] + whist[warp][digit] + pr[it];
-      s_key[pos] = kr[it];
-      s_val[pos] = vr[it];
+      s_kv[pos] = make_uint2(kr[it], vr[it]);
     }
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < in_tile; i += RS_THREADS) {
-    const uint32_t key = s_key[i], digit = (key >> shift) & dmask;
-    const uint32_t pos = base_off[digit] + (i - loc[digit]);
-    k_out[pos] = key;
-    v_out[pos] = s_val[i];
+    const uint2 kv = s_kv[i];
+    const uint32_t pos = base_off[(kv.x >> shift) & dmask] + i;
+    k_out[pos] = kv.x;
+    v_out[pos] = kv.y;
   }
 }
 
