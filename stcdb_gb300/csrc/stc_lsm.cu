@@ -326,60 +326,147 @@ __global__ void k_lsm_oversize(LsmDev L, unsigned long long a, unsigned long lon
 // (:1062-1098) per key of the CTF ranges. The pid field keeps the sid above
 // it for CTF keys (extract_fields does not mask it, cuda/cuda_util.cuh:164-169);
 // oversize keys reached by a range carry none.
-__global__ void k_lsm_encode(LsmDev L, unsigned long long total, unsigned long long slim) {
-  __shared__ unsigned long long s_first[MAX_CTF + 1];
-  for (uint32_t c = threadIdx.x; c <= L.F; c += blockDim.x) s_first[c] = L.ctf_first[c];
-  __syncthreads();
-  for (unsigned long long kid = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; kid < total;
-       kid += (unsigned long long)gridDim.x * blockDim.x) {
-    // largest c with first[c] <= kid (empty CTFs share their start)
-    uint32_t lo = 0, hi = L.F - 1;
-    while (lo < hi) {
-      uint32_t mid = (lo + hi + 1) >> 1;
-      if (s_first[mid] <= kid) lo = mid;
-      else hi = mid - 1;
+//
+// Each block takes one contiguous run of keys, which the CTF ranges split
+// into one or a few pieces. Per group of 256 keys, those of the CTF the group
+// starts in (the block's current CTF) set their bitmap bits in a shared copy
+// of that CTF's bitmap, merged into the global one when the block moves to
+// the next CTF, and their packed bytes are staged in shared memory and written
+// out as whole 32-bit words; the group's other keys (past a CTF boundary) go
+// to global memory directly.
+
+// Bits i + j * x_grid for i in [l0, h0], j in [l1, h1], below 65536: per
+// row one contiguous run, set a word at a time. In global memory a word is
+// only updated when a bit of the run is still clear.
+template <bool SHARED>
+__device__ __forceinline__ void set_bitmap_runs(uint32_t *bm, uint32_t l0, uint32_t h0, uint32_t l1, uint32_t h1,
+                                                uint32_t x_grid) {
+  if (x_grid == 0) h1 = min(h1, l1);  // every row is the same run
+  if (l0 > h0) return;
+  for (uint32_t j = l1; j <= h1; j++) {
+    const unsigned long long a = (unsigned long long)l0 + (unsigned long long)j * x_grid;
+    if (a > 65535ull) break;  // later rows start no lower
+    const uint32_t lo = (uint32_t)a;
+    const uint32_t hi = (uint32_t)min((unsigned long long)h0 + (unsigned long long)j * x_grid, 65535ull);
+    for (uint32_t w = lo >> 5; w <= (hi >> 5); w++) {
+      const uint32_t b0 = max(lo, w << 5) & 31u, b1 = min(hi, (w << 5) + 31u) & 31u;
+      const uint32_t mask = (0xFFFFFFFFu >> (31u - b1)) & (0xFFFFFFFFu << b0);
+      if (SHARED) atomicOr(&bm[w], mask);
+      else if ((__ldcg(&bm[w]) & mask) != mask) atomicOr(&bm[w], mask);
     }
-    const uint32_t c = lo;
-    const stc_ctf &t = L.ctfs[c];
-    float4 b = L.bbox[kid];
-    uint4 r = L.brec[kid];
-    float wx = __fsub_rn(t.mbr[2], t.mbr[0]), wy = __fsub_rn(t.mbr[3], t.mbr[1]);
-    float gx = (float)t.x_grid, gy = (float)t.y_grid;
-    uint32_t l0 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.x, t.mbr[0]), wx), gx));
-    uint32_t l1 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.y, t.mbr[1]), wy), gy));
-    uint32_t h0 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.z, t.mbr[0]), wx), gx));
-    uint32_t h1 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.w, t.mbr[1]), wy), gy));
-    // a box inside the CTF box gives cells <= the grid size; cells past the
-    // 8 KB slot are skipped, so the loops stop where every bit would be
-    h0 = min(h0, 65535u);
-    h1 = min(h1, 65535u / max(1u, (uint32_t)t.x_grid));
-    // bits i + j * x_grid for i in [l0, h0], j in [l1, h1], below 65536: per
-    // row one contiguous run, set a word at a time, and only where a bit of
-    // the run is still clear
-    uint32_t *bm = L.bitmaps + (size_t)c * (STC_BITMAP_BYTES / 4);
-    if (t.x_grid == 0) h1 = min(h1, l1);  // every row is the same run
-    if (l0 <= h0)
-      for (uint32_t j = l1; j <= h1; j++) {
-        const unsigned long long a = (unsigned long long)l0 + (unsigned long long)j * t.x_grid;
-        if (a > 65535ull) break;  // later rows start no lower
-        const uint32_t lo = (uint32_t)a;
-        const uint32_t hi = (uint32_t)min((unsigned long long)h0 + (unsigned long long)j * t.x_grid, 65535ull);
-        for (uint32_t w = lo >> 5; w <= (hi >> 5); w++) {
-          const uint32_t b0 = max(lo, w << 5) & 31u, b1 = min(hi, (w << 5) + 31u) & 31u;
-          const uint32_t mask = (0xFFFFFFFFu >> (31u - b1)) & (0xFFFFFFFFu << b0);
-          if ((__ldcg(&bm[w]) & mask) != mask) atomicOr(&bm[w], mask);
+  }
+}
+
+__device__ __forceinline__ uint32_t ctf_of(const unsigned long long *first, uint32_t F, unsigned long long kid,
+                                           uint32_t from) {
+  // largest c >= from with first[c] <= kid (empty CTFs share their start)
+  uint32_t lo = from, hi = F - 1;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi + 1) >> 1;
+    if (first[mid] <= kid) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+constexpr uint32_t ENC_GROUP = 256;  // keys per group = threads per block
+constexpr uint32_t ENC_STAGE_WORDS = ENC_GROUP * 16 / 4 + 2;
+
+__global__ void __launch_bounds__(ENC_GROUP) k_lsm_encode(LsmDev L, unsigned long long total,
+                                                          unsigned long long slim) {
+  __shared__ unsigned long long s_first[MAX_CTF + 1];
+  __shared__ uint32_t s_bm[STC_BITMAP_BYTES / 4];
+  __shared__ uint32_t s_stage[ENC_STAGE_WORDS];
+  __shared__ uint32_t s_c0;
+  for (uint32_t c = threadIdx.x; c <= L.F; c += blockDim.x) s_first[c] = L.ctf_first[c];
+  for (uint32_t w = threadIdx.x; w < STC_BITMAP_BYTES / 4; w += blockDim.x) s_bm[w] = 0;
+  const unsigned long long per = (total + gridDim.x - 1) / gridDim.x;
+  const unsigned long long k0 = min(total, per * blockIdx.x), k1 = min(total, k0 + per);
+  uint32_t cur = 0xFFFFFFFFu;  // CTF whose bits s_bm holds
+  uint8_t *const stage = (uint8_t *)s_stage;
+  for (unsigned long long base = k0; base < k1; base += ENC_GROUP) {
+    __syncthreads();  // s_first and s_bm ready; the previous group's staging copied out
+    if (threadIdx.x == 0) s_c0 = ctf_of(s_first, L.F, base, 0);
+    __syncthreads();
+    const uint32_t c0 = s_c0;
+    if (c0 != cur) {
+      if (cur != 0xFFFFFFFFu) {
+        uint32_t *gbm = L.bitmaps + (size_t)cur * (STC_BITMAP_BYTES / 4);
+        for (uint32_t w = threadIdx.x; w < STC_BITMAP_BYTES / 4; w += blockDim.x) {
+          const uint32_t v = s_bm[w];
+          if (v && (__ldcg(&gbm[w]) & v) != v) atomicOr(&gbm[w], v);
+          s_bm[w] = 0;
         }
       }
-    unsigned long long pid_field = kid >= slim ? r.x : (((unsigned long long)L.sid[r.x] << 26) | r.x);
-    unsigned long long vm = serialize_mbr_dev(b, t);
-    uint32_t s_end = t.mbr_bit, s_dur = t.end_bit + t.mbr_bit, s_tgt = t.duration_bit + t.end_bit + t.mbr_bit;
-    uint32_t s_pid = t.id_bit + s_tgt;
-    unsigned __int128 k = ((unsigned __int128)pid_field << s_pid) + ((unsigned __int128)r.y << s_tgt) +
-                          ((unsigned __int128)r.z << s_dur) + ((unsigned __int128)r.w << s_end) +
-                          (unsigned __int128)vm;
-    uint32_t kb = t.key_bit / 8u;
-    uint8_t *dst = L.kbytes + t.key_offset + (kid - s_first[c]) * kb;
-    for (uint32_t i = 0; i < kb; i++) dst[i] = (uint8_t)(k >> (8 * i));
+      cur = c0;
+      __syncthreads();
+    }
+    // the group's keys of CTF c0 are [base, g1)
+    const unsigned long long g1 = min(min(base + ENC_GROUP, k1), s_first[c0 + 1] > base ? s_first[c0 + 1] : k1);
+    const stc_ctf &t0 = L.ctfs[c0];
+    const uint32_t kb0 = t0.key_bit / 8u;
+    const unsigned long long g_start = t0.key_offset + (base - s_first[c0]) * kb0;  // byte of the group's first key
+    const uint32_t lead = (uint32_t)(g_start & 3ull);
+    const unsigned long long kid = base + threadIdx.x;
+    if (kid < k1) {
+      const uint32_t c = kid < g1 ? c0 : ctf_of(s_first, L.F, kid, c0);
+      const stc_ctf &t = L.ctfs[c];
+      float4 b = L.bbox[kid];
+      uint4 r = L.brec[kid];
+      float wx = __fsub_rn(t.mbr[2], t.mbr[0]), wy = __fsub_rn(t.mbr[3], t.mbr[1]);
+      float gx = (float)t.x_grid, gy = (float)t.y_grid;
+      uint32_t l0 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.x, t.mbr[0]), wx), gx));
+      uint32_t l1 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.y, t.mbr[1]), wy), gy));
+      uint32_t h0 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.z, t.mbr[0]), wx), gx));
+      uint32_t h1 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.w, t.mbr[1]), wy), gy));
+      // a box inside the CTF box gives cells <= the grid size; cells past the
+      // 8 KB slot are skipped, so the loops stop where every bit would be
+      h0 = min(h0, 65535u);
+      h1 = min(h1, 65535u / max(1u, (uint32_t)t.x_grid));
+      if (c == c0) set_bitmap_runs<true>(s_bm, l0, h0, l1, h1, t.x_grid);
+      else set_bitmap_runs<false>(L.bitmaps + (size_t)c * (STC_BITMAP_BYTES / 4), l0, h0, l1, h1, t.x_grid);
+      unsigned long long pid_field = kid >= slim ? r.x : (((unsigned long long)L.sid[r.x] << 26) | r.x);
+      unsigned long long vm = serialize_mbr_dev(b, t);
+      uint32_t s_end = t.mbr_bit, s_dur = t.end_bit + t.mbr_bit, s_tgt = t.duration_bit + t.end_bit + t.mbr_bit;
+      uint32_t s_pid = t.id_bit + s_tgt;
+      unsigned __int128 k = ((unsigned __int128)pid_field << s_pid) + ((unsigned __int128)r.y << s_tgt) +
+                            ((unsigned __int128)r.z << s_dur) + ((unsigned __int128)r.w << s_end) +
+                            (unsigned __int128)vm;
+      const unsigned long long lo = (unsigned long long)k, hi = (unsigned long long)(k >> 64);
+      const uint32_t kb = t.key_bit / 8u;
+      if (c == c0) {
+        uint8_t *dst = stage + lead + threadIdx.x * kb0;
+#pragma unroll
+        for (uint32_t i = 0; i < 16; i++)
+          if (i < kb) dst[i] = (uint8_t)(i < 8 ? lo >> (8 * i) : hi >> (8 * (i - 8)));
+      } else {
+        uint8_t *dst = L.kbytes + t.key_offset + (kid - s_first[c]) * kb;
+#pragma unroll
+        for (uint32_t i = 0; i < 16; i++)
+          if (i < kb) dst[i] = (uint8_t)(i < 8 ? lo >> (8 * i) : hi >> (8 * (i - 8)));
+      }
+    }
+    __syncthreads();
+    // the staged bytes [lead, lead + len) go to [g_start, g_start + len):
+    // whole words where all four bytes are the group's, bytes at the ends
+    const uint32_t len = (uint32_t)(g1 - base) * kb0, end = lead + len;
+    uint32_t *gw = (uint32_t *)(L.kbytes + (g_start - lead));
+    for (uint32_t w = threadIdx.x; w < (end + 3) / 4; w += blockDim.x) {
+      const uint32_t b0 = 4 * w, b1 = b0 + 4;
+      if (b0 >= lead && b1 <= end) {
+        gw[w] = s_stage[w];
+      } else {
+        for (uint32_t x = max(b0, lead); x < min(b1, end); x++) L.kbytes[g_start - lead + x] = stage[x];
+      }
+    }
+  }
+  __syncthreads();
+  if (cur != 0xFFFFFFFFu) {
+    uint32_t *gbm = L.bitmaps + (size_t)cur * (STC_BITMAP_BYTES / 4);
+    for (uint32_t w = threadIdx.x; w < STC_BITMAP_BYTES / 4; w += blockDim.x) {
+      const uint32_t v = s_bm[w];
+      if (v && (__ldcg(&gbm[w]) & v) != v) atomicOr(&gbm[w], v);
+    }
   }
 }
 

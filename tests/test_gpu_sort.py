@@ -15,13 +15,26 @@ def _sort_fn(lib):
     return f
 
 
-@pytest.mark.parametrize("n,bits", [(1, 8), (1000, 20), (300_001, 19), (2_000_000, 32)])
-def test_sort_pairs_matches_stable_numpy(built_cuda, n, bits):
+# (n, bits, keys): tile-edge sizes (4096 items a tile), partial last digits,
+# and key sets whose digits all fall in one or two buckets, so that every
+# tile's look-back runs through the same digit.
+@pytest.mark.parametrize("n,bits,dist", [(1, 8, "uniform"), (1000, 20, "uniform"), (300_001, 19, "uniform"),
+                                         (2_000_000, 32, "uniform"), (4096, 12, "uniform"),
+                                         (4097, 1, "uniform"), (1_000_003, 32, "equal"),
+                                         (1_000_003, 17, "two"), (3_000_000, 32, "small"),
+                                         (12_000_000, 25, "uniform")])
+def test_sort_pairs_matches_stable_numpy(built_cuda, n, bits, dist):
     import torch
     from stcdb_gb300._lib import load_library
     f = _sort_fn(load_library("libstc"))
     rng = np.random.default_rng(n)
     keys = rng.integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+    if dist == "equal":
+        keys[:] = np.uint32(0x5A5A5A5A)
+    elif dist == "two":
+        keys = np.where(keys & 1, np.uint32(0x1FFFF), np.uint32(0x10000)).astype(np.uint32)
+    elif dist == "small":
+        keys &= np.uint32(15)
     vals = np.arange(n, dtype=np.uint32)
     dk = torch.from_numpy(keys.view(np.int32)).cuda()
     dv = torch.from_numpy(vals.view(np.int32)).cuda()
