@@ -446,28 +446,7 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
     STC_KL k_make_sid<<<STC_NUM_SMS, 512, F2 * sizeof(uint32_t), s>>>(C, sk[6], sk[2], 0, n_str, xcap, ycap);
   }
   // 3. all records by (oversize, sid, oid, target, duration, end), stable
-  struct Word { int kind; uint32_t shift, bits; };
-  Word words[8];
-  int nw = 0;
-  uint32_t eb = bits_for(st.lsm_max_end), db = bits_for(st.lsm_max_dur), ib = bits_for(N > 1 ? N - 1 : 1);
-  uint32_t sb = bits_for(F2 + 1);
-  if (eb + db <= 32) words[nw++] = {W_END_DUR, eb, eb + db};
-  else { words[nw++] = {W_END, 0, eb}; words[nw++] = {W_DUR, 0, db}; }
-  words[nw++] = {W_TARGET, 0, ib};
-  if (ib + sb <= 32) words[nw++] = {W_SID_PID, ib, ib + sb};
-  else { words[nw++] = {W_PID, 0, ib}; words[nw++] = {W_SID, 0, sb}; }
-  words[nw++] = {W_OVER, 0, 1};
-  if (T) {
-    const uint32_t *perm = nullptr;
-    uint32_t *vbuf[2] = {sk[1], sk[3]};
-    for (int w = 0; w < nw; w++) {
-      uint32_t *vin = vbuf[w & 1], *vout = vbuf[(w + 1) & 1];
-      STC_KL k_lsm_word<<<GRID, 256, 0, s>>>(C, T, perm, sk[0], perm ? nullptr : vin, words[w].kind, words[w].shift);
-      sort_words(C, sk[0], perm ? perm : vin, sk[2], vout, sk[4], sk[5], 2, T, words[w].bits, s);
-      perm = vout;
-    }
-    STC_KL k_lsm_gather<<<GRID, 256, 0, s>>>(C, T, perm);
-  }
+  sort_keys(C, T, N, st.lsm_max_end, st.lsm_max_dur, bits_for(F2 + 1), s);
   // 4. CTF ranges and limits (:944-1004), oversize times and bitmap
   std::vector<uint32_t> cap(F2);
   e = cudaMemcpyAsync(cap.data(), C.ctf_cap, F2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);

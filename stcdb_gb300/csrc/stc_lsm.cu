@@ -186,27 +186,51 @@ __global__ void k_make_sid(LsmDev L, const uint32_t *oids, const uint32_t *jv, u
 // One 32-bit word of the key sort. The order is (over, sid, pid, target,
 // duration, end): the CTF keys by their 128-bit key sid:12 | pid:26 |
 // target:26 | duration:32 | end:32 (cuda/geometry.cu:724-726, 799-806),
-// then the oversize keys by theirs (sid 0).
+// then the oversize keys by theirs (sid 0). W_LOW and W_HIGH split the order
+// in two words: the low target bits, duration and end; then the over flag,
+// the object's rank in (sid, pid) order (its pid for an oversize key, whose
+// sid counts as 0) and the high target bits.
 __global__ void k_lsm_word(LsmDev L, unsigned long long K, const uint32_t *perm, uint32_t *keys, uint32_t *vals,
-                           int kind, uint32_t shift) {
+                           WordSpec ws, const uint32_t *rank) {
   for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < K;
        i += (unsigned long long)gridDim.x * blockDim.x) {
     uint32_t src = perm ? perm[i] : (uint32_t)i;
     if (!perm) vals[i] = (uint32_t)i;
     uint4 r = L.rec[src];
     uint32_t w;
-    switch (kind) {
-      case W_END_DUR: w = r.w | (r.z << shift); break;
+    switch (ws.kind) {
+      case W_END_DUR: w = r.w | (r.z << ws.a); break;
       case W_END: w = r.w; break;
       case W_DUR: w = r.z; break;
       case W_TARGET: w = r.y; break;
-      case W_SID_PID: w = r.x | ((L.over[src] ? 0u : (uint32_t)L.sid[r.x]) << shift); break;
+      case W_SID_PID: w = r.x | ((L.over[src] ? 0u : (uint32_t)L.sid[r.x]) << ws.a); break;
       case W_PID: w = r.x; break;
       case W_SID: w = L.over[src] ? 0u : (uint32_t)L.sid[r.x]; break;
+      case W_LOW: w = r.w | (r.z << ws.a) | (r.y << ws.b); break;  // a = end bits, b = end + duration bits < 32
+      case W_HIGH: {  // a = high target bits, b = low target bits, c = pid bits
+        const bool over = L.over[src] != 0;
+        const uint32_t major = over ? r.x : rank[r.x];
+        w = (over ? 1u << (ws.c + ws.a) : 0u) | (major << ws.a) | (ws.a ? r.y >> ws.b : 0u);
+        break;
+      }
       default: w = L.over[src]; break;
     }
     keys[i] = w;
   }
+}
+
+// Objects by sid (stable): keys sid, values pid.
+__global__ void k_sid_keys(const uint16_t *sid, uint32_t N, uint32_t *keys, uint32_t *vals) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) {
+    keys[i] = sid[i];
+    vals[i] = i;
+  }
+}
+
+__global__ void k_rank_of(const uint32_t *order, uint32_t N, uint32_t *rank) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) rank[order[i]] = i;
 }
 
 __global__ void k_lsm_gather(LsmDev L, unsigned long long K, const uint32_t *perm) {
@@ -543,6 +567,43 @@ void lsm_append(const PipeDev &p, const LsmDev &L, cudaStream_t s) {
   STC_KL k_lsm_append<<<GRID, 256, 0, s>>>(p.emit, p.E, L);
 }
 
+void lsmk::sort_keys(const LsmDev &L, unsigned long long K, uint32_t N, uint32_t max_end, uint32_t max_dur,
+                     uint32_t sid_bits, cudaStream_t s) {
+  if (!K) return;
+  uint32_t *const *sk = L.sk;
+  WordSpec words[8];
+  int nw = 0;
+  const uint32_t eb = bits_for(max_end), db = bits_for(max_dur), ib = bits_for(N > 1 ? N - 1 : 1);
+  const uint32_t low_t = eb + db < 32 ? 32 - eb - db : 0, th = ib > low_t ? ib - low_t : 0;
+  const uint32_t *rank = nullptr;
+  if (eb + db < 32 && 1 + ib + th <= 32) {
+    // two words; the rank of each object in (sid, pid) order in sk[6]
+    STC_KL k_sid_keys<<<nblk(N), 256, 0, s>>>(L.sid, N, sk[0], sk[1]);
+    sort_words(L, sk[0], sk[1], sk[2], sk[3], sk[4], sk[5], 0, N, sid_bits, s);
+    STC_KL k_rank_of<<<nblk(N), 256, 0, s>>>(sk[3], N, sk[6]);
+    rank = sk[6];
+    words[nw++] = {W_LOW, eb, eb + db, 0u, std::min(32u, eb + db + ib)};
+    words[nw++] = {W_HIGH, th, low_t, ib, 1 + ib + th};
+  } else {
+    const uint32_t sb = sid_bits;
+    if (eb + db <= 32) words[nw++] = {W_END_DUR, eb, 0u, 0u, eb + db};
+    else { words[nw++] = {W_END, 0u, 0u, 0u, eb}; words[nw++] = {W_DUR, 0u, 0u, 0u, db}; }
+    words[nw++] = {W_TARGET, 0u, 0u, 0u, ib};
+    if (ib + sb <= 32) words[nw++] = {W_SID_PID, ib, 0u, 0u, ib + sb};
+    else { words[nw++] = {W_PID, 0u, 0u, 0u, ib}; words[nw++] = {W_SID, 0u, 0u, 0u, sb}; }
+    words[nw++] = {W_OVER, 0u, 0u, 0u, 1u};
+  }
+  const uint32_t *perm = nullptr;
+  uint32_t *vbuf[2] = {sk[1], sk[3]};
+  for (int w = 0; w < nw; w++) {
+    uint32_t *vin = vbuf[w & 1], *vout = vbuf[(w + 1) & 1];
+    STC_KL k_lsm_word<<<GRID, 256, 0, s>>>(L, K, perm, sk[0], perm ? nullptr : vin, words[w], rank);
+    sort_words(L, sk[0], perm ? perm : vin, sk[2], vout, sk[4], sk[5], 2, K, words[w].bits, s);
+    perm = vout;
+  }
+  STC_KL k_lsm_gather<<<GRID, 256, 0, s>>>(L, K, perm);
+}
+
 // Stable sort of n (key, value) words; returns the buffers holding the result.
 void lsmk::sort_words(const LsmDev &L, const uint32_t *k, const uint32_t *v, uint32_t *ko, uint32_t *vo,
                       uint32_t *kt, uint32_t *vt, int count_slot, size_t n, uint32_t bits, cudaStream_t s) {
@@ -590,31 +651,8 @@ stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState
     sort_words(L, sk[0], sk[5], sk[1], sk[2], sk[3], sk[4], 1, R, bits_for(S - 1), s);
     STC_KL k_make_sid<<<STC_NUM_SMS, 512, F * sizeof(uint32_t), s>>>(L, sk[6], sk[2], z, R, xcap, ycap);
   }
-  // 4. sort the keys: (over, sid, pid, target, duration, end), least
-  // significant word first
-  struct Word { int kind; uint32_t shift, bits; };
-  Word words[8];
-  int nw = 0;
-  uint32_t eb = bits_for(max_end), db = bits_for(max_dur), ib = bits_for(N > 1 ? N - 1 : 1);
-  uint32_t sb = bits_for(S * S + 1);
-  if (eb + db <= 32) words[nw++] = {W_END_DUR, eb, eb + db};
-  else { words[nw++] = {W_END, 0, eb}; words[nw++] = {W_DUR, 0, db}; }
-  words[nw++] = {W_TARGET, 0, ib};
-  if (ib + sb <= 32) words[nw++] = {W_SID_PID, ib, ib + sb};
-  else { words[nw++] = {W_PID, 0, ib}; words[nw++] = {W_SID, 0, sb}; }
-  words[nw++] = {W_OVER, 0, 1};
-  if (K) {
-    const uint32_t *perm = nullptr;
-    uint32_t *vbuf[2] = {sk[1], sk[3]};
-    for (int w = 0; w < nw; w++) {
-      uint32_t *vin = vbuf[w & 1], *vout = vbuf[(w + 1) & 1];
-      STC_KL k_lsm_word<<<GRID, 256, 0, s>>>(L, K, perm, sk[0], perm ? nullptr : vin, words[w].kind,
-                                              words[w].shift);
-      sort_words(L, sk[0], perm ? perm : vin, sk[2], vout, sk[4], sk[5], 2, K, words[w].bits, s);
-      perm = vout;
-    }
-    STC_KL k_lsm_gather<<<GRID, 256, 0, s>>>(L, K, perm);
-  }
+  // 4. sort the keys: (over, sid, pid, target, duration, end)
+  sort_keys(L, K, N, max_end, max_dur, bits_for(S * S + 1), s);
   // 5. CTF key ranges
   std::vector<uint32_t> cap(F);
   e = cudaMemcpyAsync(cap.data(), L.ctf_cap, (size_t)F * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);

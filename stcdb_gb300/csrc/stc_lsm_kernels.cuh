@@ -55,7 +55,14 @@ __device__ __forceinline__ unsigned long long serialize_mbr_dev(float4 b, const 
 // duration, end): the CTF keys by their 128-bit key sid:12 | pid:26 |
 // target:26 | duration:32 | end:32 (cuda/geometry.cu:724-726, 799-806),
 // then the oversize keys by theirs (sid 0).
-enum WordKind : int { W_END_DUR, W_END, W_DUR, W_TARGET, W_SID_PID, W_PID, W_SID, W_OVER };
+enum WordKind : int { W_END_DUR, W_END, W_DUR, W_TARGET, W_SID_PID, W_PID, W_SID, W_OVER, W_LOW, W_HIGH };
+
+// One word of the key sort: its kind, the field shifts it needs and its
+// significant bits.
+struct WordSpec {
+  int kind;
+  uint32_t a, b, c, bits;
+};
 
 __global__ void k_lsm_set_counts(unsigned long long *n_dev, unsigned long long a, unsigned long long b,
                                  unsigned long long c);
@@ -66,7 +73,7 @@ __global__ void k_slab_of(const uint32_t *jv, uint32_t R, uint32_t xcap, uint32_
 __global__ void k_make_sid(LsmDev L, const uint32_t *oids, const uint32_t *jv, uint32_t z, uint32_t R,
                            uint32_t xcap, uint32_t ycap);
 __global__ void k_lsm_word(LsmDev L, unsigned long long K, const uint32_t *perm, uint32_t *keys, uint32_t *vals,
-                           int kind, uint32_t shift);
+                           WordSpec w, const uint32_t *rank);
 __global__ void k_lsm_gather(LsmDev L, unsigned long long K, const uint32_t *perm);
 __global__ void k_lsm_limits(LsmDev L, unsigned long long K);
 __global__ void k_lsm_oversize(LsmDev L, unsigned long long a, unsigned long long b);
@@ -75,6 +82,13 @@ __global__ void k_lsm_oversize(LsmDev L, unsigned long long a, unsigned long lon
 // count is read from L.n_dev[count_slot].
 void sort_words(const LsmDev &L, const uint32_t *k, const uint32_t *v, uint32_t *ko, uint32_t *vo, uint32_t *kt,
                 uint32_t *vt, int count_slot, size_t n, uint32_t bits, cudaStream_t s);
+
+// The K records (L.rec, L.box) into (L.brec, L.bbox), stably ordered by
+// (over, sid, pid, target, duration, end). L.sid holds each object's sid
+// (below 2^sid_bits); L.n_dev[0] = N and L.n_dev[2] = K; L.sk[0..6] are
+// scratch (sk[6] free on entry).
+void sort_keys(const LsmDev &L, unsigned long long K, uint32_t N, uint32_t max_end, uint32_t max_dur,
+               uint32_t sid_bits, cudaStream_t s);
 
 }  // namespace lsmk
 }  // namespace stc
