@@ -33,6 +33,7 @@
 // the new one (<= 16) plus the 32-byte record and box once each way for the
 // sort gather: 2 * 32 per key, as for the flush.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -49,9 +50,25 @@ struct InCtf {
   unsigned long long first;  // first key of this CTF among all decoded CTF keys
   const uint8_t *keys;       // its packed keys (block buffer padded by 32 bytes)
   stc_ctf ctf;
+  double rx, ry, re;         // 1 / the largest low-x, low-y and edge field
+  double dx, dy, de;         // bounds on the reciprocal decode's error (parse_coord)
 };
 
-__device__ __forceinline__ unsigned long long mask64(uint32_t bits) {
+// One box coordinate as CTF::new_parse_mbr_f_box computes it: the float
+// nearest to base + (q / qmax) * w evaluated in double. The correctly rounded
+// division costs many FP64 instructions, so q * (1 / qmax) is tried first: it
+// differs from the exact double by at most d, and when both ends of
+// [v - d, v + d] round to the same float that float is the result.
+__device__ __forceinline__ float parse_coord(double base, unsigned long long q, unsigned long long qmax, double rq,
+                                            double w, double d) {
+  const double qd = __ull2double_rn(q);
+  const double v = base + qd * rq * w;
+  const float lo = __double2float_rn(v - d), hi = __double2float_rn(v + d);
+  if (lo == hi) return lo;
+  return __double2float_rn(__dadd_rn(base, __dmul_rn(__ddiv_rn(qd, __ull2double_rn(qmax)), w)));
+}
+
+__host__ __device__ __forceinline__ unsigned long long mask64(uint32_t bits) {
   return bits >= 64 ? ~0ull : ((1ull << bits) - 1ull);
 }
 
@@ -129,6 +146,7 @@ __global__ void k_cmp_decode(const InCtf *ic, uint32_t nc, unsigned long long nk
     }
     const uint32_t real_end = end + t.end_time_min;
     // CTF::new_parse_mbr_f_box: double arithmetic, stored as float
+    const InCtf &x = ic[lo];
     unsigned long long me_ = mask64(t.edge_bit), my = mask64(t.low_y_bit), mx = mask64(t.low_x_bit);
     unsigned long long ey = vm & me_;
     vm >>= t.edge_bit;
@@ -140,14 +158,10 @@ __global__ void k_cmp_decode(const InCtf *ic, uint32_t nc, unsigned long long nk
     float wx = __fsub_rn(t.mbr[2], t.mbr[0]), wy = __fsub_rn(t.mbr[3], t.mbr[1]);
     float le = fmaxf(wx, wy);
     float4 b;
-    b.x = __double2float_rn(__dadd_rn((double)t.mbr[0], __dmul_rn(__ddiv_rn(__ull2double_rn(low0), __ull2double_rn(mx)),
-                                                                  (double)wx)));
-    b.y = __double2float_rn(__dadd_rn((double)t.mbr[1], __dmul_rn(__ddiv_rn(__ull2double_rn(low1), __ull2double_rn(my)),
-                                                                  (double)wy)));
-    b.z = __double2float_rn(__dadd_rn((double)b.x, __dmul_rn(__ddiv_rn(__ull2double_rn(ex), __ull2double_rn(me_)),
-                                                             (double)le)));
-    b.w = __double2float_rn(__dadd_rn((double)b.y, __dmul_rn(__ddiv_rn(__ull2double_rn(ey), __ull2double_rn(me_)),
-                                                             (double)le)));
+    b.x = parse_coord((double)t.mbr[0], low0, mx, x.rx, (double)wx, x.dx);
+    b.y = parse_coord((double)t.mbr[1], low1, my, x.ry, (double)wy, x.dy);
+    b.z = parse_coord((double)b.x, ex, me_, x.re, (double)le, x.de);
+    b.w = parse_coord((double)b.y, ey, me_, x.re, (double)le, x.de);
     const bool ov = o.csid[oid] == 1;
     const uint32_t off = real_end - (ov ? o_etm : etm);
     rec[base + kid] = make_uint4(oid, target, dur, off);
@@ -229,52 +243,6 @@ __global__ void k_cmp_limits_init(float4 *lim_box, uint2 *lim_time, uint32_t F) 
 __global__ void k_cmp_or_bitmap(const uint32_t *in, uint32_t *out) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < STC_BITMAP_BYTES / 4) out[i] |= in[i];
-}
-
-// Bitmaps (:1015-1035: cells clamped to the grid on each axis) and packed keys
-// (:1048-1060: oid, target, duration, end offset, box; fields added).
-__global__ void k_cmp_encode(const uint4 *brec, const float4 *bbox, const stc_ctf *ctfs,
-                             const unsigned long long *ctf_first, uint32_t F, unsigned long long total,
-                             uint32_t *bitmaps, uint8_t *kbytes) {
-  __shared__ unsigned long long s_first[MAX_CTF + 1];
-  for (uint32_t c = threadIdx.x; c <= F; c += blockDim.x) s_first[c] = ctf_first[c];
-  __syncthreads();
-  for (unsigned long long kid = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; kid < total;
-       kid += (unsigned long long)gridDim.x * blockDim.x) {
-    uint32_t lo = 0, hi = F - 1;
-    while (lo < hi) {
-      uint32_t mid = (lo + hi + 1) >> 1;
-      if (s_first[mid] <= kid) lo = mid;
-      else hi = mid - 1;
-    }
-    const uint32_t c = lo;
-    const stc_ctf &t = ctfs[c];
-    float4 b = bbox[kid];
-    uint4 r = brec[kid];
-    float wx = __fsub_rn(t.mbr[2], t.mbr[0]), wy = __fsub_rn(t.mbr[3], t.mbr[1]);
-    float gx = (float)t.x_grid, gy = (float)t.y_grid;
-    uint32_t l0 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.x, t.mbr[0]), wx), gx));
-    uint32_t l1 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.y, t.mbr[1]), wy), gy));
-    uint32_t h0 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.z, t.mbr[0]), wx), gx));
-    uint32_t h1 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.w, t.mbr[1]), wy), gy));
-    h0 = min(h0, (uint32_t)t.x_grid - 1u);
-    h1 = min(h1, (uint32_t)t.y_grid - 1u);
-    uint32_t *bm = bitmaps + (size_t)c * (STC_BITMAP_BYTES / 4);
-    for (uint32_t i = l0; i <= h0; i++)
-      for (uint32_t j = l1; j <= h1; j++) {
-        uint32_t bit = i + j * (uint32_t)t.x_grid;
-        atomicOr(&bm[bit >> 5], 1u << (bit & 31u));
-      }
-    unsigned long long vm = serialize_mbr_dev(b, t);
-    uint32_t s_end = t.mbr_bit, s_dur = t.end_bit + t.mbr_bit, s_tgt = t.duration_bit + t.end_bit + t.mbr_bit;
-    uint32_t s_pid = t.id_bit + s_tgt;
-    unsigned __int128 k = ((unsigned __int128)r.x << s_pid) + ((unsigned __int128)r.y << s_tgt) +
-                          ((unsigned __int128)r.z << s_dur) + ((unsigned __int128)r.w << s_end) +
-                          (unsigned __int128)vm;
-    uint32_t kb = t.key_bit / 8u;
-    uint8_t *dst = kbytes + t.key_offset + (kid - s_first[c]) * kb;
-    for (uint32_t i = 0; i < kb; i++) dst[i] = (uint8_t)(k >> (8 * i));
-  }
 }
 
 __global__ void k_cmp_state_init(DevState *st) {
@@ -392,6 +360,21 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
       x.first = first;
       x.keys = b->keys + t.key_offset;
       x.ctf = t;
+      // each of the exact decode's five roundings (and the reciprocal
+      // decode's) is within 2^-53 of a value below |base| + 2|w| in size; the
+      // bound used is 2^7 times their sum
+      const double mx = (double)mask64(t.low_x_bit), my = (double)mask64(t.low_y_bit), me = (double)mask64(t.edge_bit);
+      const float wx = t.mbr[2] - t.mbr[0], wy = t.mbr[3] - t.mbr[1], le = std::max(wx, wy);
+      double m = 0.0;
+      for (int i = 0; i < 4; i++) m = std::max(m, std::fabs((double)t.mbr[i]));
+      const bool ok = mx > 0 && my > 0 && me > 0 && std::isfinite(m) && std::isfinite((double)le);
+      x.rx = ok ? 1.0 / mx : 0.0;
+      x.ry = ok ? 1.0 / my : 0.0;
+      x.re = ok ? 1.0 / me : 0.0;
+      const double u = std::ldexp(1.0, -46);
+      x.dx = ok ? (std::fabs((double)t.mbr[0]) + 2.0 * std::fabs((double)wx) + 1.0) * u : INFINITY;
+      x.dy = ok ? (std::fabs((double)t.mbr[1]) + 2.0 * std::fabs((double)wy) + 1.0) * u : INFINITY;
+      x.de = ok ? (m + std::fabs((double)wx) + std::fabs((double)wy) + 2.0 * std::fabs((double)le) + 1.0) * u : INFINITY;
       ic.push_back(x);
       first += t.kv_count;
     }
@@ -554,7 +537,10 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
   if (e == cudaSuccess && no_out)
     e = cudaMemcpyAsync(B.obox, C.bbox + slim, no_out * sizeof(float4), cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess && slim)
-    STC_KL k_cmp_encode<<<GRID, 256, 0, s>>>(C.brec, C.bbox, B.d_ctfs, C.ctf_first, F2, slim, B.bitmaps, B.keys);
+    // bitmaps (:1015-1035: cells clamped to the grid on each axis) and packed
+    // keys (:1048-1060: oid, target, duration, end offset, box; fields added)
+    STC_KL k_encode_keys<<<GRID, ENC_GROUP, 0, s>>>(
+        EncodeArgs{C.brec, C.bbox, B.d_ctfs, C.ctf_first, nullptr, B.bitmaps, B.keys, slim, slim, F2, true});
   if (e == cudaSuccess) e = build_index(C, B, s);
   if (e == cudaSuccess) e = cudaEventRecord(ev1, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

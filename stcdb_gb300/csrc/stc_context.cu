@@ -32,6 +32,17 @@ void set_thread_error(const std::string &msg) { g_create_error = msg; }
 
 static constexpr size_t DRAIN_CHUNK = (size_t)8 << 20;  // bytes per pinned staging chunk of a drain
 
+// A large host<->device copy of a step or drain as pieces of COPY_PIECE
+// bytes: the copy engine takes them one by one, so that the small copies of
+// a query batch on the query stream wait for one piece, not the whole copy.
+static constexpr size_t COPY_PIECE = (size_t)16 << 20;
+static cudaError_t copy_in_pieces(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  for (size_t off = 0; off < bytes && e == cudaSuccess; off += COPY_PIECE)
+    e = cudaMemcpyAsync((uint8_t *)dst + off, (const uint8_t *)src + off, std::min(COPY_PIECE, bytes - off), kind, s);
+  return e;
+}
+
 struct stc_ctx {
   stc_config cfg;
   int device = 0;
@@ -488,8 +499,8 @@ extern "C" stc_status stc_step(stc_ctx *c, const double *xy, uint32_t t) {
   if (c->failed) return STC_ERR_STATE;
   cudaSetDevice(c->device);
   cudaEventRecord(c->ev[PH_START], c->stream);
-  cudaError_t e = cudaMemcpyAsync(c->xy_own, xy, (size_t)c->p.N * sizeof(double2), cudaMemcpyHostToDevice,
-                                  c->stream);
+  cudaError_t e =
+      copy_in_pieces(c->xy_own, xy, (size_t)c->p.N * sizeof(double2), cudaMemcpyHostToDevice, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "stc_step copy-in");
   return run_step(c, c->xy_own, t, true);
 }
@@ -525,7 +536,7 @@ extern "C" stc_status stc_drain_meetings(stc_ctx *c, stc_meeting *out, size_t ca
   cudaPointerAttributes pa;
   const bool pinned_out = k && cudaPointerGetAttributes(&pa, out) == cudaSuccess && pa.type == cudaMemoryTypeHost;
   cudaGetLastError();  // pageable memory is not an error
-  if (pinned_out) e = cudaMemcpyAsync(out, p.emit, bytes, cudaMemcpyDeviceToHost, s);
+  if (pinned_out) e = copy_in_pieces(out, p.emit, bytes, cudaMemcpyDeviceToHost, s);
   const size_t nch = pinned_out ? 0 : (bytes + DRAIN_CHUNK - 1) / DRAIN_CHUNK;
   for (size_t i = 0; e == cudaSuccess && nch && i <= nch; i++) {
     if (i < nch) {

@@ -349,7 +349,8 @@ __global__ void k_lsm_oversize(LsmDev L, unsigned long long a, unsigned long lon
 // cuda_write_bitmap (cuda/geometry.cu:957-987) and write_key_and_mbr
 // (:1062-1098) per key of the CTF ranges. The pid field keeps the sid above
 // it for CTF keys (extract_fields does not mask it, cuda/cuda_util.cuh:164-169);
-// oversize keys reached by a range carry none.
+// oversize keys reached by a range carry none. In compaction mode the cells
+// are clamped to the grid and the pid field is the object id alone.
 //
 // Each block takes one contiguous run of keys, which the CTF ranges split
 // into one or a few pieces. Per group of 256 keys, those of the CTF the group
@@ -393,15 +394,14 @@ __device__ __forceinline__ uint32_t ctf_of(const unsigned long long *first, uint
   return lo;
 }
 
-constexpr uint32_t ENC_GROUP = 256;  // keys per group = threads per block
 constexpr uint32_t ENC_STAGE_WORDS = ENC_GROUP * 16 / 4 + 2;
 
-__global__ void __launch_bounds__(ENC_GROUP) k_lsm_encode(LsmDev L, unsigned long long total,
-                                                          unsigned long long slim) {
+__global__ void __launch_bounds__(ENC_GROUP) k_encode_keys(EncodeArgs L) {
   __shared__ unsigned long long s_first[MAX_CTF + 1];
   __shared__ uint32_t s_bm[STC_BITMAP_BYTES / 4];
   __shared__ uint32_t s_stage[ENC_STAGE_WORDS];
   __shared__ uint32_t s_c0;
+  const unsigned long long total = L.total, slim = L.slim;
   for (uint32_t c = threadIdx.x; c <= L.F; c += blockDim.x) s_first[c] = L.ctf_first[c];
   for (uint32_t w = threadIdx.x; w < STC_BITMAP_BYTES / 4; w += blockDim.x) s_bm[w] = 0;
   const unsigned long long per = (total + gridDim.x - 1) / gridDim.x;
@@ -443,13 +443,20 @@ __global__ void __launch_bounds__(ENC_GROUP) k_lsm_encode(LsmDev L, unsigned lon
       uint32_t l1 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.y, t.mbr[1]), wy), gy));
       uint32_t h0 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.z, t.mbr[0]), wx), gx));
       uint32_t h1 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.w, t.mbr[1]), wy), gy));
-      // a box inside the CTF box gives cells <= the grid size; cells past the
-      // 8 KB slot are skipped, so the loops stop where every bit would be
-      h0 = min(h0, 65535u);
-      h1 = min(h1, 65535u / max(1u, (uint32_t)t.x_grid));
+      if (L.compact) {
+        // cells clamped to the grid (the merged block's rule)
+        h0 = min(h0, (uint32_t)t.x_grid - 1u);
+        h1 = min(h1, (uint32_t)t.y_grid - 1u);
+      } else {
+        // a box inside the CTF box gives cells <= the grid size; cells past
+        // the 8 KB slot are skipped, so the loops stop where every bit would be
+        h0 = min(h0, 65535u);
+        h1 = min(h1, 65535u / max(1u, (uint32_t)t.x_grid));
+      }
       if (c == c0) set_bitmap_runs<true>(s_bm, l0, h0, l1, h1, t.x_grid);
       else set_bitmap_runs<false>(L.bitmaps + (size_t)c * (STC_BITMAP_BYTES / 4), l0, h0, l1, h1, t.x_grid);
-      unsigned long long pid_field = kid >= slim ? r.x : (((unsigned long long)L.sid[r.x] << 26) | r.x);
+      unsigned long long pid_field =
+          L.compact || kid >= slim ? r.x : (((unsigned long long)L.sid[r.x] << 26) | r.x);
       unsigned long long vm = serialize_mbr_dev(b, t);
       uint32_t s_end = t.mbr_bit, s_dur = t.end_bit + t.mbr_bit, s_tgt = t.duration_bit + t.end_bit + t.mbr_bit;
       uint32_t s_pid = t.id_bit + s_tgt;
@@ -699,7 +706,9 @@ stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState
   }
   cudaMemcpyAsync(L.ctfs, H.ctfs.data(), F * sizeof(stc_ctf), cudaMemcpyHostToDevice, s);
   // 7. bitmaps and packed keys
-  if (total) STC_KL k_lsm_encode<<<GRID, 256, 0, s>>>(L, total, slim);
+  if (total)
+    STC_KL k_encode_keys<<<GRID, ENC_GROUP, 0, s>>>(
+        EncodeArgs{L.brec, L.bbox, L.ctfs, L.ctf_first, L.sid, L.bitmaps, L.kbytes, total, slim, L.F, false});
   // 8. keep the sids of the block; empty the memtable
   cudaMemcpyAsync(L.bsid, L.sid, (size_t)N * sizeof(uint16_t), cudaMemcpyDeviceToDevice, s);
   stc_ctb_info in{};

@@ -75,6 +75,23 @@ __global__ void k_make_sid(LsmDev L, const uint32_t *oids, const uint32_t *jv, u
 __global__ void k_lsm_word(LsmDev L, unsigned long long K, const uint32_t *perm, uint32_t *keys, uint32_t *vals,
                            WordSpec w, const uint32_t *rank);
 __global__ void k_lsm_gather(LsmDev L, unsigned long long K, const uint32_t *perm);
+
+// Bitmaps and packed keys of the sorted keys [0, total) over CTF ranges
+// ctf_first[0..F] (k_encode_keys, launched with ENC_GROUP threads a block).
+struct EncodeArgs {
+  const uint4 *brec;
+  const float4 *bbox;
+  const stc_ctf *ctfs;
+  const unsigned long long *ctf_first;
+  const uint16_t *sid;
+  uint32_t *bitmaps;
+  uint8_t *kbytes;
+  unsigned long long total, slim;
+  uint32_t F;
+  bool compact;
+};
+constexpr uint32_t ENC_GROUP = 256;
+__global__ void k_encode_keys(EncodeArgs a);
 __global__ void k_lsm_limits(LsmDev L, unsigned long long K);
 __global__ void k_lsm_oversize(LsmDev L, unsigned long long a, unsigned long long b);
 
