@@ -14,7 +14,9 @@ configuration (1M-20M objects, 0-90% hotspot) at the headline 10M objects.
 The 10M-object hotspot configuration (70% in 1000 Zipf hotspots, sigma
 300 m) does not fit one GPU: its live pairs grow with N^2 (measured 3.5e7
 at 1M objects, so ~3.5e9 at 10M), beyond any 32-byte-slot meeting table
-that fits in HBM. "hotspot-1M" runs that model at 1M objects.
+that fits in HBM. "hotspot-1M" runs that model at 1M objects; "uniform-3M"
+is the default workload at 3M objects (a few GB on the device, the case the
+kernel profiles are captured on).
 
 value: position updates per second with positions already resident in HBM
   (stc_step_device), summed device time of K steps (CUDA events on the
@@ -58,6 +60,8 @@ WORKLOADS = {
                         buckets=1 << 28, kv_restriction=1 << 27),
     "hotspot-1M": dict(objects=1_000_000, hot=1000, reach=10.0, min_meet=5, grid_capacity=200, amplify=8.0,
                        buckets=1 << 28, kv_restriction=1 << 27),
+    "uniform-3M": dict(objects=3_000_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
+                       buckets=1 << 26, kv_restriction=1 << 25),
     "uniform-100k": dict(objects=100_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
                          buckets_per_object=8, kv_restriction=1 << 22),
 }
