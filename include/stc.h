@@ -16,6 +16,9 @@
  *                          tracing/process.cpp:375) and its CPU twin in
  *                          tracer::process (tracing/process.cpp:452-459, 608-612):
  *                          filter + reachability + update_meetings + update_schema
+ *   stc_step_window     <- the per-step loop of tracer::process
+ *                          (tracing/process.cpp:401-612) over a window of
+ *                          steps, with the step replayed from a CUDA graph
  *   stc_drain_meetings  <- reading h_meetings_ps[0..kv_count) after
  *                          update_meetings (tracing/meeting.cpp:11-24)
  *   stc_get_stats       <- workbench counters grid_check_counter,
@@ -147,6 +150,19 @@ stc_status stc_create(const stc_config *cfg, const double mbr[4], const double *
  * [oid], in host memory (copied in) or device memory (stc_step_device). */
 stc_status stc_step(stc_ctx *ctx, const double *xy, uint32_t t);
 stc_status stc_step_device(stc_ctx *ctx, const double *xy_device, uint32_t t);
+
+/* Processes a window of `steps` consecutive steps t0, t0 + 1, ...: xy holds
+ * steps x num_objects (lon, lat) f64 pairs, layout [step][oid], in host
+ * memory (on_device 0) or device memory (on_device 1). The step runs as a
+ * CUDA graph captured once and replayed (captured again after a flush or a
+ * change of the slice count), so a step costs one launch instead of one per
+ * kernel; results equal those of stc_step called step by step, flushes
+ * included (each step's state is still read back for the flush rule). When
+ * out is given, each step's meetings are drained into out[*n_out..cap) and
+ * *n_out counts them; STC_ERR_CAPACITY when they do not fit. Phase times of
+ * the window's steps are not recorded (stc_stats.step_ms is). */
+stc_status stc_step_window(stc_ctx *ctx, const double *xy, int on_device, uint32_t steps, uint32_t t0,
+                           stc_meeting *out, size_t cap, size_t *n_out);
 
 /* Copies up to cap emitted meetings (in emission order) into out, removes
  * them from the context and stores how many were copied in *n. */

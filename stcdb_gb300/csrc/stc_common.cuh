@@ -93,7 +93,8 @@ struct DevState {
   uint32_t splits, merges, events, overflow_objects;
   uint32_t build_nodes, build_leaves, build_active, build_level;
   uint32_t work_next;                 // generic persistent-kernel work counter
-  uint32_t pad[3];
+  uint32_t step_t;                    // time of the step in flight (set at its start)
+  uint32_t pad[2];
   unsigned long long border_points;   // points whose lookup starts above their leaf
   unsigned long long fast_claims;     // new meetings started this step (claims finalised by the sweep)
   unsigned long long hit_count;       // hits appended to the hit buffer this step

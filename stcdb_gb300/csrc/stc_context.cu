@@ -58,7 +58,14 @@ struct stc_ctx {
   // driver's staging path, which other threads' copies (queries) wait on
   uint8_t *drain_stage[2] = {nullptr, nullptr};
   cudaEvent_t drain_ev[2] = {nullptr, nullptr};
-  double2 *xy_own = nullptr;     // device copy target for host input
+  double2 *xy_own = nullptr;     // device copy target for host input (and every step of a window)
+  uint32_t *t_pinned = nullptr;  // page-locked time of the step being issued (step_begin copies it)
+  // the step captured as a CUDA graph, replayed by stc_step_window; it holds
+  // the pipeline's and the memtable's arguments by value, so anything that
+  // changes them (a flush, the slice count) invalidates it
+  cudaGraphExec_t graph = nullptr;
+  bool graph_valid = false;
+  uint32_t graph_kernels = 0;
   std::vector<void *> allocs;
   stc_stats stats;
   uint32_t last_t = 0;
@@ -152,6 +159,8 @@ static void destroy_all(stc_ctx *c) {
   for (void *v : c->allocs) cudaFree(v);
   c->allocs.clear();
   if (c->st_host) cudaFreeHost(c->st_host);
+  if (c->t_pinned) cudaFreeHost(c->t_pinned);
+  if (c->graph) cudaGraphExecDestroy(c->graph);
   for (int i = 0; i < 2; i++) {
     if (c->drain_stage[i]) cudaFreeHost(c->drain_stage[i]);
     if (c->drain_ev[i]) cudaEventDestroy(c->drain_ev[i]);
@@ -244,6 +253,8 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   for (int i = 0; i < PH_COUNT && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
   if (e == cudaSuccess) e = cudaMallocHost(&c->st_host, sizeof(DevState));
+  if (e == cudaSuccess) e = cudaMallocHost(&c->t_pinned, sizeof(uint32_t));
+  if (e == cudaSuccess) e = schema_prepare();
   for (int i = 0; i < 2 && e == cudaSuccess; i++) {
     e = cudaMallocHost(&c->drain_stage[i], DRAIN_CHUNK);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->drain_ev[i], cudaEventDisableTiming);
@@ -405,6 +416,7 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
 }
 
 static stc_status flush_now(stc_ctx *c, uint32_t t) {
+  c->graph_valid = false;  // the memtable's arguments change
   cudaEventRecord(c->ev[PH_FLUSH0], c->stream);
   unsigned long long launches0 = tl_launches;
   std::string err;
@@ -425,29 +437,77 @@ static stc_status flush_now(stc_ctx *c, uint32_t t) {
   return STC_OK;
 }
 
-static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copied) {
+// The step's device work, in stream order (phase events only when not being
+// captured into a graph).
+static void issue_step(stc_ctx *c, bool events) {
   PipeDev &p = c->p;
   cudaStream_t s = c->stream;
-  p.xy = xy;
-  unsigned long long launches0 = tl_launches;
-  step_begin(p, s);
-  cudaEventRecord(c->ev[PH_COPY], s);
+  step_begin(p, c->t_pinned, s);
+  if (events) cudaEventRecord(c->ev[PH_COPY], s);
   step_partition(p, s);
-  cudaEventRecord(c->ev[PH_PART], s);
+  if (events) cudaEventRecord(c->ev[PH_PART], s);
   step_border(p, s);
   step_jobs(p, s);
-  cudaEventRecord(c->ev[PH_BORDER], s);
-  step_refine(p, t, s);
-  cudaEventRecord(c->ev[PH_REFINE], s);
-  step_insert(p, t, s);
-  cudaEventRecord(c->ev[PH_INSERT], s);
-  step_sweep(p, t, s);
-  cudaEventRecord(c->ev[PH_SWEEP], s);
+  if (events) cudaEventRecord(c->ev[PH_BORDER], s);
+  step_refine(p, s);
+  if (events) cudaEventRecord(c->ev[PH_REFINE], s);
+  step_insert(p, s);
+  if (events) cudaEventRecord(c->ev[PH_INSERT], s);
+  step_sweep(p, s);
+  if (events) cudaEventRecord(c->ev[PH_SWEEP], s);
   if (c->lsm_on) lsm_append(p, c->lsm, s);
-  cudaEventRecord(c->ev[PH_APPEND], s);
+  if (events) cudaEventRecord(c->ev[PH_APPEND], s);
   if (c->cfg.dynamic_schema)
     update_schema(p.sd, p.sw, p.grid_count, p.reach, p.grid_capacity, p.delay,
                   (c->cfg.flags & STC_FLAG_SERIAL_SCHEMA) != 0, p.st, s);
+}
+
+// Captures the step (positions in xy_own) as a CUDA graph. Only this
+// thread's work on the context's stream is captured: a serving thread's
+// queries on other streams go on meanwhile.
+static stc_status capture_step(stc_ctx *c) {
+  if (c->graph) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
+  c->graph_valid = false;
+  c->p.xy = c->xy_own;
+  const unsigned long long l0 = tl_launches;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    issue_step(c, false);
+    e = cudaStreamEndCapture(c->stream, &g);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&c->graph, g, 0);
+  if (g) cudaGraphDestroy(g);
+  c->graph_kernels = (uint32_t)(tl_launches - l0);
+  tl_launches = l0;  // counted when replayed
+  if (e != cudaSuccess) {
+    c->graph = nullptr;
+    return cuda_fail(c, e, "capturing the step graph");
+  }
+  c->graph_valid = true;
+  return STC_OK;
+}
+
+static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copied, bool graph = false) {
+  PipeDev &p = c->p;
+  cudaStream_t s = c->stream;
+  p.xy = xy;
+  *c->t_pinned = t;  // the previous step has been waited for: nothing reads it now
+  unsigned long long launches0 = tl_launches;
+  if (graph) {
+    if (!c->graph_valid) {
+      stc_status gs = capture_step(c);
+      if (gs != STC_OK) return gs;
+    }
+    cudaError_t e = cudaGraphLaunch(c->graph, s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window");
+    tl_launches += c->graph_kernels;
+  } else {
+    issue_step(c, true);
+  }
   cudaEventRecord(c->ev[PH_SCHEMA], s);
   stc_status rs = read_state(c, "stc_step");
   if (rs != STC_OK) return rs;
@@ -469,7 +529,8 @@ static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copie
   o.splits = h.splits;
   o.merges = h.merges;
   float ms[PH_COUNT] = {0};
-  for (int i = PH_COPY; i <= PH_SCHEMA; i++) cudaEventElapsedTime(&ms[i], c->ev[i - 1], c->ev[i]);
+  if (!graph)  // a replayed graph records no phase events
+    for (int i = PH_COPY; i <= PH_SCHEMA; i++) cudaEventElapsedTime(&ms[i], c->ev[i - 1], c->ev[i]);
   o.phase_ms[0] = ms[PH_PART];
   o.phase_ms[1] = ms[PH_BORDER];
   o.phase_ms[2] = ms[PH_REFINE];
@@ -512,6 +573,36 @@ extern "C" stc_status stc_step_device(stc_ctx *c, const double *xy_device, uint3
   cudaSetDevice(c->device);
   cudaEventRecord(c->ev[PH_START], c->stream);
   return run_step(c, (const double2 *)xy_device, t, false);
+}
+
+extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_device, uint32_t steps, uint32_t t0,
+                                      stc_meeting *out, size_t cap, size_t *n_out) {
+  if (!c) return STC_ERR_INVALID_ARG;
+  if (n_out) *n_out = 0;
+  if (steps && !xy) return fail(c, STC_ERR_INVALID_ARG, "stc_step_window: null positions");
+  if (out && !n_out) return fail(c, STC_ERR_INVALID_ARG, "stc_step_window: output without a count");
+  if (c->failed) return STC_ERR_STATE;
+  cudaSetDevice(c->device);
+  const size_t step_bytes = (size_t)c->p.N * sizeof(double2);
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  size_t n = 0;
+  for (uint32_t i = 0; i < steps; i++) {
+    cudaEventRecord(c->ev[PH_START], c->stream);
+    cudaError_t e = copy_in_pieces(c->xy_own, (const uint8_t *)xy + (size_t)i * step_bytes, step_bytes, kind,
+                                   c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window copy-in");
+    stc_status rs = run_step(c, c->xy_own, t0 + i, true, true);
+    if (rs != STC_OK) return rs;
+    if (out) {
+      size_t k = 0;
+      rs = stc_drain_meetings(c, out + n, cap - n, &k);
+      if (rs != STC_OK) return rs;
+      n += k;
+      *n_out = n;
+      if (c->st_host->emit_count) return fail(c, STC_ERR_CAPACITY, "stc_step_window: the output buffer is full");
+    }
+  }
+  return STC_OK;
 }
 
 extern "C" stc_status stc_get_stats(stc_ctx *c, stc_stats *out) {
@@ -734,6 +825,7 @@ extern "C" stc_status stc_set_step_slices(stc_ctx *c, uint32_t slices) {
   if (!c) return STC_ERR_INVALID_ARG;
   c->cfg.step_slices = slices;
   c->p.slices = std::min<uint32_t>(std::max<uint32_t>(slices, 1u), 64u);
+  c->graph_valid = false;
   return STC_OK;
 }
 
@@ -763,6 +855,7 @@ extern "C" stc_status stc_load_ctb(stc_ctx *c, uint32_t index, const char *dir, 
   if (!c->lsm_on) return fail(c, STC_ERR_INVALID_ARG, "stc_load_ctb: the memtable is off (kv_restriction 0)");
   if (c->failed) return STC_ERR_STATE;
   cudaSetDevice(c->device);
+  c->graph_valid = false;
   std::string err;
   stc_status st = lsm_load_block(c->lsm, c->lsmh, index, dir, prefix, c->stream, err);
   if (st != STC_OK) c->err = "stc_load_ctb: " + err;

@@ -49,7 +49,13 @@ __global__ void k_step_begin(DevState *st) {
   st->overflow_objects = 0;
 }
 
-void step_begin(PipeDev &p, cudaStream_t s) { STC_KL k_step_begin<<<1, 1, 0, s>>>(p.st); }
+// The step's time goes to the device from a page-locked word that the host
+// sets before the step is issued (also when the step is replayed from a
+// captured graph); the step's kernels read it from DevState::step_t.
+void step_begin(PipeDev &p, const uint32_t *t_pinned, cudaStream_t s) {
+  cudaMemcpyAsync(&p.st->step_t, t_pinned, sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+  STC_KL k_step_begin<<<1, 1, 0, s>>>(p.st);
+}
 
 __global__ void k_init_slots(Slot *slots, unsigned long long B) {
   for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < B;
@@ -81,7 +87,8 @@ void init_tables(PipeDev &p, cudaStream_t s) {
 
 // Candidates that may occur twice in a step: walk with their minimum
 // priority once all instances are merged.
-__global__ void k_insert_ordered(PipeDev p, uint32_t t) {
+__global__ void k_insert_ordered(PipeDev p) {
+  const uint32_t t = p.st->step_t;
   const unsigned long long nc = p.st->cand_count < p.cand_cap ? p.st->cand_count : p.cand_cap;
   for (unsigned long long c = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
        c += (unsigned long long)gridDim.x * blockDim.x) {
@@ -98,9 +105,7 @@ __global__ void k_insert_ordered(PipeDev p, uint32_t t) {
   }
 }
 
-void step_insert(PipeDev &p, uint32_t t, cudaStream_t s) {
-  STC_KL k_insert_ordered<<<STC_NUM_SMS * 4, 256, 0, s>>>(p, t);
-}
+void step_insert(PipeDev &p, cudaStream_t s) { STC_KL k_insert_ordered<<<STC_NUM_SMS * 4, 256, 0, s>>>(p); }
 
 // Sweep (tracing/meeting.cpp:32-76, cuda/geometry.cu:595-736).
 
@@ -189,7 +194,8 @@ __device__ __forceinline__ void flush_emits(const PipeDev &p, const stc_meeting 
 }
 
 // Slice `part` of `parts` sweeps slots [B * part / parts, B * (part + 1) / parts).
-__global__ void __launch_bounds__(SWEEP_THREADS, 6) k_sweep(PipeDev p, uint32_t t, uint32_t part, uint32_t parts) {
+__global__ void __launch_bounds__(SWEEP_THREADS, 6) k_sweep(PipeDev p, uint32_t part, uint32_t parts) {
+  const uint32_t t = p.st->step_t;
   __shared__ __align__(16) stc_meeting stage_all[SWEEP_WARPS][WARP_STAGE];
   const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
   stc_meeting *stage = stage_all[warp];
@@ -244,9 +250,9 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 6) k_sweep(PipeDev p, uint32_t 
   if (lane == 0 && emitted) atomicAdd(&p.st->step_emitted, emitted);
 }
 
-void step_sweep(PipeDev &p, uint32_t t, cudaStream_t s) {
+void step_sweep(PipeDev &p, cudaStream_t s) {
   for (uint32_t part = 0; part < p.slices; part++)
-    STC_KL k_sweep<<<STC_NUM_SMS * 6, SWEEP_THREADS, 0, s>>>(p, t, part, p.slices);
+    STC_KL k_sweep<<<STC_NUM_SMS * 6, SWEEP_THREADS, 0, s>>>(p, part, p.slices);
 }
 
 }  // namespace stc

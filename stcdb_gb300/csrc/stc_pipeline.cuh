@@ -56,11 +56,11 @@ void step_partition(PipeDev &p, cudaStream_t s);
 void step_border(PipeDev &p, cudaStream_t s);
 void step_jobs(PipeDev &p, cudaStream_t s);
 // stc_refine.cu
-void step_refine(PipeDev &p, uint32_t t, cudaStream_t s);
+void step_refine(PipeDev &p, cudaStream_t s);
 // stc_meetings.cu
-void step_insert(PipeDev &p, uint32_t t, cudaStream_t s);
-void step_sweep(PipeDev &p, uint32_t t, cudaStream_t s);
+void step_insert(PipeDev &p, cudaStream_t s);
+void step_sweep(PipeDev &p, cudaStream_t s);
 void init_tables(PipeDev &p, cudaStream_t s);
-void step_begin(PipeDev &p, cudaStream_t s);
+void step_begin(PipeDev &p, const uint32_t *t_pinned, cudaStream_t s);
 
 }  // namespace stc

@@ -610,6 +610,10 @@ __global__ void k_schema_phase2(SchemaDev sd, uint32_t *grid_count, const uint32
   st->events = nev;
 }
 
+cudaError_t schema_prepare() {
+  return cudaFuncSetAttribute(k_schema_phase2_par, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PAR_SMEM);
+}
+
 void update_schema(SchemaDev sd, SchemaWork w, uint32_t *grid_count, double reach, uint32_t grid_capacity,
                    uint32_t delay, int serial_only, DevState *st, cudaStream_t s) {
   STC_KL k_schema_phase1<<<nblk(sd.S), 256, 0, s>>>(sd, grid_count, reach, grid_capacity, delay, w.ev_flag, w.old_under);
@@ -618,7 +622,6 @@ void update_schema(SchemaDev sd, SchemaWork w, uint32_t *grid_count, double reac
   exclusive_scan_u32(w.ev_pos, w.ev_pos, sd.S, w.ev_total, w.scan_tmp, s);
   STC_KL k_schema_compact<<<nblk(sd.S), 256, 0, s>>>(w.ev_flag, w.ev_pos, sd.S, w.ev_list);
   unsigned int *done = (unsigned int *)(w.ev_total + 1);
-  cudaFuncSetAttribute(k_schema_phase2_par, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PAR_SMEM);
   STC_KL k_schema_phase2_par<<<1, 1024, PAR_SMEM, s>>>(sd, w.ev_list, w.ev_total, done, serial_only, w.par_scratch,
                                                       st);
   STC_KL k_schema_phase2<<<1, 32, 0, s>>>(sd, grid_count, w.ev_list, w.ev_total, w.old_under, w.heap, w.queued,

@@ -44,6 +44,9 @@ cudaError_t build_schema(const double2 *xy, uint32_t n, const double mbr[4], dou
 
 // Dynamic update after a step (tracing/filter.cpp:377-449).
 // serial_only forces the one-thread replay (the parallel one is used when it applies).
+// Kernel attributes the schema update needs, set once per device before any
+// step is issued (outside a stream capture).
+cudaError_t schema_prepare();
 void update_schema(SchemaDev sd, SchemaWork w, uint32_t *grid_count, double reach, uint32_t grid_capacity,
                    uint32_t delay, int serial_only, DevState *st, cudaStream_t s);
 

@@ -215,6 +215,10 @@ def _lib():
         lib.stc_step.restype = ctypes.c_int
         lib.stc_step_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32]
         lib.stc_step_device.restype = ctypes.c_int
+        lib.stc_step_window.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32,
+                                        ctypes.c_uint32, ctypes.c_void_p, ctypes.c_size_t,
+                                        ctypes.POINTER(ctypes.c_size_t)]
+        lib.stc_step_window.restype = ctypes.c_int
         lib.stc_drain_meetings.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                            ctypes.POINTER(ctypes.c_size_t)]
         lib.stc_drain_meetings.restype = ctypes.c_int
@@ -287,6 +291,24 @@ class Pipeline:
 
     def step_device(self, xy_device_ptr: int, t: int) -> None:
         self._check(self._lib.stc_step_device(self._h, ctypes.c_void_p(xy_device_ptr), t))
+
+    def step_window(self, xy, t0: int, out: np.ndarray | None = None) -> np.ndarray | None:
+        """Steps t0 .. t0 + len(xy) - 1 replayed from a captured CUDA graph
+        (stc_step_window). xy: a (steps, num_objects, 2) float64 numpy array
+        in host memory, or (device pointer, steps) of that layout in device
+        memory. With `out` (a MEETING_DTYPE array) each step's meetings are
+        drained into it and the filled part is returned."""
+        n = ctypes.c_size_t(0)
+        optr, cap = (out.ctypes.data, len(out)) if out is not None else (None, 0)
+        if isinstance(xy, tuple):
+            ptr, steps = xy
+            st = self._lib.stc_step_window(self._h, ctypes.c_void_p(ptr), 1, steps, t0, optr, cap, ctypes.byref(n))
+        else:
+            xy = np.ascontiguousarray(xy, dtype=np.float64)
+            assert xy.ndim == 3 and xy.shape[1:] == (self.cfg.num_objects, 2)
+            st = self._lib.stc_step_window(self._h, xy.ctypes.data, 0, xy.shape[0], t0, optr, cap, ctypes.byref(n))
+        self._check(st)
+        return out[:n.value] if out is not None else None
 
     def stats(self) -> StcStats:
         s = StcStats()

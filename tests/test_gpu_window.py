@@ -1,0 +1,95 @@
+"""stc_step_window (each step replayed from a captured CUDA graph) against the
+plain step-by-step pipeline: uneven windows, host and device input, flushes
+inside windows (the graph is captured again after each), a change of the
+slice count between windows. Meetings, statistics and every flushed block
+must be identical."""
+import numpy as np
+import pytest
+
+from stcdb_gb300.pipeline import MEETING_DTYPE, Pipeline, StcConfig
+from stcdb_gb300.tracegen import hotspot_grid
+
+from parity import trace_and_box
+
+pytestmark = pytest.mark.gpu
+
+
+def _rows(meetings):
+    a = np.ascontiguousarray(meetings).view(np.uint32).reshape(-1, MEETING_DTYPE.itemsize // 4)
+    return a[np.lexsort(a.T[::-1])] if len(a) else a
+
+
+def _blocks(p):
+    n = p.stats().flushes
+    out = []
+    for i in range(max(0, n - 8), n):  # the context keeps the last 8 blocks
+        info, arrays = p.read_block(i)
+        out.append((info.as_dict(), {k: v.view(np.uint8).tobytes() for k, v in arrays.items()}))
+    return out
+
+
+def test_windows_match_plain_steps(built_cuda):
+    import torch
+    steps = 24
+    tc = hotspot_grid(30000, n_hotspots=30, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=11)
+    cfg = StcConfig(num_objects=30000, reach_distance=10.0, min_meet_time=3, max_meet_time=6, grid_capacity=50,
+                    grid_amplify=1.2, num_meeting_buckets=1_500_000, kv_restriction=60_000, ctf_count=16)
+    tr, mbr = trace_and_box(tc, steps)
+    tr = np.ascontiguousarray(tr, dtype=np.float64)
+
+    plain = Pipeline(cfg, mbr, tr[0])
+    try:
+        got_plain = []
+        for t in range(steps):
+            plain.step(tr[t], t)
+            got_plain.append(plain.drain())
+        ps = plain.stats()
+        plain_blocks = _blocks(plain)
+    finally:
+        plain.close()
+
+    win = Pipeline(cfg, mbr, tr[0])
+    dev = torch.from_numpy(tr).cuda()
+    try:
+        got_win = []
+        t0 = 0
+        # (steps, slices, device input)
+        for w, slices, on_device in [(1, 1, False), (4, 1, True), (7, 3, False), (2, 3, True), (6, 1, False),
+                                     (4, 2, True)]:
+            win.set_step_slices(slices)
+            out = np.empty(2_000_000, MEETING_DTYPE)
+            if on_device:
+                got = win.step_window((dev[t0].data_ptr(), w), t0, out)
+            else:
+                got = win.step_window(tr[t0:t0 + w], t0, out)
+            got_win.append(got.copy())
+            t0 += w
+        assert t0 == steps
+        ws = win.stats()
+        win_blocks = _blocks(win)
+    finally:
+        win.close()
+
+    a, b = _rows(np.concatenate(got_plain)), _rows(np.concatenate(got_win))
+    assert len(a) > 0 and a.shape == b.shape and np.array_equal(a, b)
+    assert ps.flushes >= 2 and ws.flushes == ps.flushes
+    assert ws.memtable_keys == ps.memtable_keys and ws.hits == ps.hits and ws.leaves == ps.leaves
+    assert len(win_blocks) == len(plain_blocks)
+    for (gi, ga), (pi, pa) in zip(win_blocks, plain_blocks):
+        assert gi == pi
+        for k in pa:
+            assert ga[k] == pa[k], f"block array {k} differs"
+
+
+def test_window_output_too_small_reports_capacity(built_cuda):
+    from stcdb_gb300.pipeline import StcError
+    tr, mbr = trace_and_box(hotspot_grid(20000, n_hotspots=20, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=4), 12)
+    cfg = StcConfig(num_objects=20000, reach_distance=10.0, min_meet_time=3, grid_capacity=50,
+                    num_meeting_buckets=1_000_000)
+    p = Pipeline(cfg, mbr, tr[0])
+    try:
+        with pytest.raises(StcError) as e:
+            p.step_window(np.ascontiguousarray(tr, dtype=np.float64), 0, np.empty(1, MEETING_DTYPE))
+        assert e.value.status == 3  # STC_ERR_CAPACITY
+    finally:
+        p.close()
