@@ -32,6 +32,11 @@ queries_under_ingest: K more steps (host input) while a serving thread answers
   a Poisson query stream (default 20,000/s; 60% object, 40% box queries) over
   the flushed block by continuous batching; queries return match counts, as
   the reference's searches do; p50/p99 latency from arrival.
+batched: uneven ingest windows (1M-3M objects, 0/30% hotspot, reach 5/10 m,
+  10-30 steps) run as plain steps and as graph-replayed windows
+  (stc_step_window) from fresh contexts: both rates, the speed-up and whether
+  the two emitted the same meetings (--no-batched skips it).
+sort: the library's radix sort on 100M random 32-bit pairs.
 --impl reference: the oracle's C restatement of the reference CPU path with
   all host threads (the reference's own sources are not on the GPU host).
 """
@@ -416,6 +421,66 @@ def sort_line(device, peak, n=100_000_000, reps=5):
             "achieved_gbs": b / (ms / 1e3) / 1e9, "frac_of_peak": b / (ms / 1e3) / 1e9 / peak, "sorted": ok}
 
 
+def batched_line(device, windows=4, seed=7):
+    """Uneven ingest windows: each window (seeded object count 1M-3M, 0 or
+    30% of objects in hotspots, reach 5 or 10 m, 10-30 steps) runs twice from
+    fresh contexts, as plain steps (stc_step_device: one launch per kernel)
+    and as one stc_step_window call (each step replayed from a captured CUDA
+    graph), positions resident in HBM and meetings drained into a page-locked
+    buffer every step in both. Both runs must emit the same meetings (sorted
+    sets compared); times are wall-clock from the first step to the last
+    drain."""
+    import numpy as np
+    import torch
+    from stcdb_gb300.pipeline import MEETING_DTYPE, Pipeline, StcConfig
+    from stcdb_gb300.tracegen import DeviceTraceGenerator, hotspot_grid, uniform_grid
+    rng = np.random.default_rng(seed)
+    cap = 16_000_000
+    pinned = torch.empty(cap * MEETING_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
+    buf = pinned.numpy().view(MEETING_DTYPE)
+    per, same, pos, secs = [], True, 0, {"plain": 0.0, "window": 0.0}
+    for w in range(windows):
+        n = int(round(10 ** rng.uniform(6.0, np.log10(3e6))))
+        hot = 0.3 if w % 2 else 0.0
+        reach = float(rng.choice([5.0, 10.0]))
+        steps = int(rng.integers(10, 31))
+        tcfg = hotspot_grid(n, hot_frac=hot, seed=seed + w) if hot else uniform_grid(n, seed=seed + w)
+        gen = DeviceTraceGenerator(tcfg, device)
+        mbr = gen.map_box(100.0)
+        xy = torch.empty((steps, n, 2), dtype=torch.float64, device=f"cuda:{device}")
+        gen.next_into(xy.data_ptr(), steps)
+        gen.close()
+        cfg = StcConfig(num_objects=n, reach_distance=reach, min_meet_time=5, grid_capacity=200, grid_amplify=4.0,
+                        num_meeting_buckets=1 << 28, device=device)
+        x0 = xy[0].cpu().numpy()
+        rows, rate = {}, {}
+        for mode in ("plain", "window"):
+            p = Pipeline(cfg, mbr, x0)
+            torch.cuda.synchronize(device)
+            t0 = time.perf_counter()
+            if mode == "plain":
+                k = 0
+                for t in range(steps):
+                    p.step_device(xy[t].data_ptr(), t)
+                    k += len(p.drain(out=buf[k:]))
+            else:
+                k = len(p.step_window((xy.data_ptr(), steps), 0, buf))
+            dt = time.perf_counter() - t0
+            p.close()
+            a = np.ascontiguousarray(buf[:k]).view(np.uint32).reshape(-1, 8)
+            rows[mode] = a[np.lexsort(a.T[::-1])] if k else a
+            rate[mode] = n * steps / dt
+            secs[mode] += dt
+        same &= np.array_equal(rows["plain"], rows["window"])
+        pos += n * steps
+        per.append({"objects": n, "hot_frac": hot, "reach_m": reach, "steps": steps, "meetings": len(rows["plain"]),
+                    "plain_pos_per_s": rate["plain"], "window_pos_per_s": rate["window"]})
+        del xy
+    return {"windows": per, "plain_pos_per_s": pos / secs["plain"], "window_pos_per_s": pos / secs["window"],
+            "speedup": secs["plain"] / secs["window"], "same_meetings": bool(same),
+            "unit": "pos-updates/s"}
+
+
 def compaction_line(c, peak):
     """Merge throughput; algorithmic bytes 2 x 32 per merged key (read and
     write each key and its box once)."""
@@ -455,6 +520,7 @@ def main():
     ap.add_argument("--workload", default="uniform-10M", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-steps", type=int, default=2, help="steps timed for the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the plain-versus-graph window comparison")
     ap.add_argument("--query-rate", type=float, default=20000.0,
                     help="Poisson query arrivals per second during the serving phase (0: skip)")
     ap.add_argument("--step-slices", type=int, default=0,
@@ -534,6 +600,7 @@ def main():
         "trace_gen": r["trace_gen"],
         "compaction": compaction_line(r["compaction"], peak),
         "sort": sort_line(local, peak),
+        "batched": None if args.no_batched else batched_line(local),
         "per_step": {"pair_tests": s_last.pair_tests, "exact_tests": s_last.exact_tests, "hits": s_last.hits,
                      "new_candidates": s_last.new_candidates, "live_meetings": s_last.taken_buckets,
                      "emitted": s_last.emitted, "border_units": s_last.border_units, "leaves": s_last.leaves,
