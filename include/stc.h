@@ -19,6 +19,8 @@
  *   stc_step_window     <- the per-step loop of tracer::process
  *                          (tracing/process.cpp:401-612) over a window of
  *                          steps, with the step replayed from a CUDA graph
+ *   stc_autotune        (no reference counterpart: the reference takes
+ *                          grid_capacity from its command line, config.h:29)
  *   stc_drain_meetings  <- reading h_meetings_ps[0..kv_count) after
  *                          update_meetings (tracing/meeting.cpp:11-24)
  *   stc_get_stats       <- workbench counters grid_check_counter,
@@ -92,6 +94,13 @@ typedef struct stc_config {
   uint32_t step_slices;          /* launches each long step kernel (pair tests, table update,
                                     sweep) is cut into, so that queries running on another thread
                                     get the GPU between them; results do not change; 0 = 1 */
+  /* Launch shape of the refinement (stc_autotune picks it; results do not
+   * depend on it: new meetings take their slots by priority, not by
+   * arrival). */
+  uint32_t job_chunk;            /* 32x32 pair tiles a warp takes at a time; 0 = 8, at most 64 */
+  uint32_t refine_blocks_per_sm; /* pair-test blocks launched per SM; 0 = 8, at most 32 */
+  uint32_t hits_blocks_per_sm;   /* table-update blocks launched per SM; 0 = 16, at most 64 */
+  uint32_t reserved;             /* 0 */
 } stc_config;
 
 /* Replay quadtree splits/merges on one device thread only (tests compare it
@@ -150,6 +159,30 @@ stc_status stc_create(const stc_config *cfg, const double mbr[4], const double *
  * [oid], in host memory (copied in) or device memory (stc_step_device). */
 stc_status stc_step(stc_ctx *ctx, const double *xy, uint32_t t);
 stc_status stc_step_device(stc_ctx *ctx, const double *xy_device, uint32_t t);
+
+/* Result of stc_autotune. */
+typedef struct stc_tune_result {
+  stc_config config;             /* the configuration given, with the chosen grid_capacity,
+                                    job_chunk, refine_blocks_per_sm and hits_blocks_per_sm */
+  float base_step_ms;            /* device time per timed step of the configuration given */
+  float best_step_ms;            /* the same for the chosen one */
+  uint32_t trials;               /* candidate settings run */
+  uint32_t reserved;
+} stc_tune_result;
+
+/* Autotuner: picks the quadtree leaf capacity and the refinement's launch
+ * shape for positions like those given (steps x n (lon, lat) f64 pairs in
+ * host memory, layout [step][oid], steps >= 3). Every candidate runs the same
+ * steps from a fresh context (memtable off) and is scored by the device time
+ * of its steps after the first two; the leaf capacity is chosen first among
+ * `capacities` (n_capacities values; null = {grid_capacity / 2,
+ * grid_capacity, 2 * grid_capacity}), then job_chunk, refine_blocks_per_sm and
+ * hits_blocks_per_sm one after the other. The launch shape never changes
+ * results; the leaf capacity is part of the reference's configuration (it
+ * orders the reference's table inserts), so a run with the chosen capacity
+ * matches the reference run with that capacity. */
+stc_status stc_autotune(const stc_config *cfg, const double mbr[4], const double *xy, uint32_t n, uint32_t steps,
+                        const uint32_t *capacities, uint32_t n_capacities, stc_tune_result *out);
 
 /* Processes a window of `steps` consecutive steps t0, t0 + 1, ...: xy holds
  * steps x num_objects (lon, lat) f64 pairs, layout [step][oid], in host

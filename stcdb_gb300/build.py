@@ -37,6 +37,7 @@ CU_SOURCES = [
     "stc_query.cu",
     "stc_tracegen.cu",
     "stc_compact.cu",
+    "stc_tune.cu",
 ]
 
 

@@ -301,6 +301,9 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
   p.delay = k.schema_update_delay;
   p.mbr_filter = k.mbr_filter;
   p.slices = std::min<uint32_t>(std::max<uint32_t>(k.step_slices, 1u), 64u);
+  p.job_chunk = k.job_chunk ? std::min<uint32_t>(k.job_chunk, 64u) : 8u;
+  p.refine_bps = k.refine_blocks_per_sm ? std::min<uint32_t>(k.refine_blocks_per_sm, 32u) : 8u;
+  p.hits_bps = k.hits_blocks_per_sm ? std::min<uint32_t>(k.hits_blocks_per_sm, 64u) : 16u;
 
   size_t nu = std::max<size_t>(n, p.U_cap);
   size_t scan_words = scan_tmp_words(std::max<size_t>({(size_t)n, (size_t)p.G + 1, (size_t)p.S,

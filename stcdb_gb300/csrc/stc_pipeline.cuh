@@ -21,6 +21,8 @@ struct PipeDev {
   uint32_t min_meet_time, grid_capacity, delay;
   int mbr_filter;
   uint32_t slices;                 // launches per long step kernel (stc_config.step_slices)
+  uint32_t job_chunk;              // refinement jobs a warp takes at a time (stc_config.job_chunk)
+  uint32_t refine_bps, hits_bps;   // blocks per SM of the pair tests and of the table update
   // state
   DevState *st;
   SchemaDev sd;

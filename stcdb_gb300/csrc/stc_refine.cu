@@ -35,7 +35,6 @@
 namespace stc {
 
 static constexpr int REFINE_THREADS = 256;
-static constexpr unsigned long long JOB_CHUNK = 8;
 
 __device__ __forceinline__ double dpml_fast_r(double lat) {
   double absla = fabs(lat);
@@ -344,7 +343,7 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
 }
 
 // Slice `part` of `parts` runs job chunks [C * part / parts, C * (part + 1) / parts)
-// of the C = ceil(jobs / JOB_CHUNK) chunks.
+// of the C = ceil(jobs / p.job_chunk) chunks.
 __global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint32_t part, uint32_t parts) {
   const uint32_t t = p.st->step_t;
   __shared__ HitRec queues[REFINE_THREADS / 32][QCAP];
@@ -356,14 +355,15 @@ __global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint3
   const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
   const unsigned long long J = p.st->jobs_total;
-  const unsigned long long nchunks = (J + JOB_CHUNK - 1) / JOB_CHUNK;
+  const unsigned long long jc = p.job_chunk;
+  const unsigned long long nchunks = (J + jc - 1) / jc;
   const unsigned long long c0 = nchunks * part / parts, c1 = nchunks * (part + 1) / parts;
   Counters ct = {0, 0, 0, 0};
   for (unsigned long long chunk = c0 + warp; chunk < c1; chunk += nwarps) {
     // one lane reads the flag so that the whole warp leaves together
     if (__shfl_sync(0xffffffffu, (int)stc_failed(p.st), 0)) break;
-    unsigned long long j0 = chunk * JOB_CHUNK;
-    unsigned long long j1 = j0 + JOB_CHUNK < J ? j0 + JOB_CHUNK : J;
+    unsigned long long j0 = chunk * jc;
+    unsigned long long j1 = j0 + jc < J ? j0 + jc : J;
     // largest g with job_start[g] <= j0
     uint32_t lo = 0, hi = p.G;
     while (hi - lo > 1) {
@@ -415,8 +415,9 @@ __global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint3
 
 void step_refine(PipeDev &p, cudaStream_t s) {
   for (uint32_t part = 0; part < p.slices; part++)
-    STC_KL k_refine_a<<<STC_NUM_SMS * 8, REFINE_THREADS, 0, s>>>(p, part, p.slices);
-  for (uint32_t part = 0; part < p.slices; part++) STC_KL k_hits<<<STC_NUM_SMS * 16, 256, 0, s>>>(p, part, p.slices);
+    STC_KL k_refine_a<<<STC_NUM_SMS * p.refine_bps, REFINE_THREADS, 0, s>>>(p, part, p.slices);
+  for (uint32_t part = 0; part < p.slices; part++)
+    STC_KL k_hits<<<STC_NUM_SMS * p.hits_bps, 256, 0, s>>>(p, part, p.slices);
 }
 
 }  // namespace stc

@@ -54,7 +54,16 @@ class _Config(ctypes.Structure):
         ("area_restriction", ctypes.c_double),
         ("ctb_retain", ctypes.c_uint32),
         ("step_slices", ctypes.c_uint32),
+        ("job_chunk", ctypes.c_uint32),
+        ("refine_blocks_per_sm", ctypes.c_uint32),
+        ("hits_blocks_per_sm", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
     ]
+
+
+class _TuneResult(ctypes.Structure):
+    _fields_ = [("config", _Config), ("base_step_ms", ctypes.c_float), ("best_step_ms", ctypes.c_float),
+                ("trials", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class StcStats(ctypes.Structure):
@@ -188,6 +197,9 @@ class StcConfig:
     area_restriction: float = 0.0  # 0 = 100 (no cut)
     ctb_retain: int = 0       # flushed blocks kept for queries; 0 = 8
     step_slices: int = 0      # launches per long step kernel (query latency under ingest); 0 = 1
+    job_chunk: int = 0        # refinement launch shape (results do not depend on it); 0 = 8
+    refine_blocks_per_sm: int = 0  # 0 = 8
+    hits_blocks_per_sm: int = 0    # 0 = 16
 
     def resolved(self) -> "StcConfig":
         if self.num_meeting_buckets == 0:
@@ -202,6 +214,28 @@ def config_struct(cfg: StcConfig) -> _Config:
         setattr(c, f.name, int(getattr(cfg, f.name)) if not isinstance(getattr(cfg, f.name), float)
                 else getattr(cfg, f.name))
     return c
+
+
+def autotune(cfg: StcConfig, mbr, xy_steps: np.ndarray, capacities=None) -> tuple:
+    """stc_autotune: (the configuration with the chosen leaf capacity and
+    refinement launch shape, {"base_step_ms", "best_step_ms", "trials"}).
+    xy_steps: (steps >= 3, num_objects, 2) float64 positions in host memory."""
+    lib = _lib()
+    c = config_struct(cfg)
+    mbr = np.ascontiguousarray(mbr, dtype=np.float64)
+    xy = np.ascontiguousarray(xy_steps, dtype=np.float64)
+    assert xy.ndim == 3 and xy.shape[1:] == (cfg.num_objects, 2)
+    caps = np.ascontiguousarray(capacities if capacities is not None else [], dtype=np.uint32)
+    r = _TuneResult()
+    st = lib.stc_autotune(ctypes.byref(c), mbr.ctypes.data, xy.ctypes.data, cfg.num_objects, xy.shape[0],
+                          caps.ctypes.data if len(caps) else None, len(caps), ctypes.byref(r))
+    if st != 0:
+        raise StcError(st, lib.stc_last_error(None).decode())
+    chosen = replace(cfg, grid_capacity=int(r.config.grid_capacity), job_chunk=int(r.config.job_chunk),
+                     refine_blocks_per_sm=int(r.config.refine_blocks_per_sm),
+                     hits_blocks_per_sm=int(r.config.hits_blocks_per_sm))
+    return chosen, {"base_step_ms": float(r.base_step_ms), "best_step_ms": float(r.best_step_ms),
+                    "trials": int(r.trials)}
 
 
 def _lib():
@@ -219,6 +253,10 @@ def _lib():
                                         ctypes.c_uint32, ctypes.c_void_p, ctypes.c_size_t,
                                         ctypes.POINTER(ctypes.c_size_t)]
         lib.stc_step_window.restype = ctypes.c_int
+        lib.stc_autotune.argtypes = [ctypes.POINTER(_Config), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                     ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32,
+                                     ctypes.POINTER(_TuneResult)]
+        lib.stc_autotune.restype = ctypes.c_int
         lib.stc_drain_meetings.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                            ctypes.POINTER(ctypes.c_size_t)]
         lib.stc_drain_meetings.restype = ctypes.c_int
