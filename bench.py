@@ -35,7 +35,9 @@ queries_under_ingest: K more steps (host input) while a serving thread answers
 batched: uneven ingest windows (1M-3M objects, 0/30% hotspot, reach 5/10 m,
   10-30 steps) run as plain steps and as graph-replayed windows
   (stc_step_window) from fresh contexts: both rates, the speed-up and whether
-  the two emitted the same meetings (--no-batched skips it).
+  the two emitted the same meetings (--no-batched skips it and autotune).
+autotune: stc_autotune on the hotspot-1M model: the leaf capacity and launch
+  shape it picks and the device time per step before and after.
 sort: the library's radix sort on 100M random 32-bit pairs.
 --impl reference: the oracle's C restatement of the reference CPU path with
   all host threads (the reference's own sources are not on the GPU host).
@@ -481,6 +483,27 @@ def batched_line(device, windows=4, seed=7):
             "unit": "pos-updates/s"}
 
 
+def tune_line(device, steps=8):
+    """stc_autotune on the hotspot-1M model (1M objects, 70% in 1000 Zipf
+    hotspots): leaf capacity among 50/100/200 (the workload's own 200 is the
+    base) and the refinement launch shape, scored on device time per step."""
+    import numpy as np
+    from stcdb_gb300.pipeline import autotune
+    from stcdb_gb300.tracegen import TraceGenerator
+    w = WORKLOADS["hotspot-1M"]
+    g = TraceGenerator(make_trace_cfg(w, seed=5))
+    mbr = g.map_box(100.0)
+    xy = np.stack([g.next() for _ in range(steps)])
+    g.close()
+    cfg = make_cfg(w, device=device)
+    chosen, rep = autotune(cfg, mbr, xy, capacities=[50, 100, 200])
+    return {"workload": "hotspot-1M", "steps": steps, "base_grid_capacity": cfg.grid_capacity,
+            "grid_capacity": chosen.grid_capacity, "job_chunk": chosen.job_chunk,
+            "refine_blocks_per_sm": chosen.refine_blocks_per_sm, "hits_blocks_per_sm": chosen.hits_blocks_per_sm,
+            "base_step_ms": rep["base_step_ms"], "best_step_ms": rep["best_step_ms"],
+            "speedup": rep["base_step_ms"] / rep["best_step_ms"], "trials": rep["trials"]}
+
+
 def compaction_line(c, peak):
     """Merge throughput; algorithmic bytes 2 x 32 per merged key (read and
     write each key and its box once)."""
@@ -601,6 +624,7 @@ def main():
         "compaction": compaction_line(r["compaction"], peak),
         "sort": sort_line(local, peak),
         "batched": None if args.no_batched else batched_line(local),
+        "autotune": None if args.no_batched else tune_line(local),
         "per_step": {"pair_tests": s_last.pair_tests, "exact_tests": s_last.exact_tests, "hits": s_last.hits,
                      "new_candidates": s_last.new_candidates, "live_meetings": s_last.taken_buckets,
                      "emitted": s_last.emitted, "border_units": s_last.border_units, "leaves": s_last.leaves,
