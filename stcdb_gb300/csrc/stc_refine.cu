@@ -170,43 +170,36 @@ __device__ __forceinline__ HitRec load_hit(const HitRec *r) {
   return h;
 }
 
-// One thread per hit, HITS_IN_FLIGHT hits in flight per thread: every
-// record and every home slot is requested before any is used.
+// One thread per hit, two hits in flight per thread: both records and both
+// home slots are requested before either is used.
 // Slice `part` of `parts` covers hits [nh * part / parts, nh * (part + 1) / parts).
-static constexpr int HITS_IN_FLIGHT = 2;
-static constexpr int HITS_MIN_BLOCKS = 4;
-__global__ void __launch_bounds__(256, HITS_MIN_BLOCKS) k_hits(PipeDev p, uint32_t part, uint32_t parts) {
+__global__ void __launch_bounds__(256) k_hits(PipeDev p, uint32_t part, uint32_t parts) {
   const uint32_t t = p.st->step_t;
   const unsigned long long nt = p.st->hit_count < p.hit_cap ? p.st->hit_count : p.hit_cap;
   const unsigned long long h0i = nt * part / parts, nh = nt * (part + 1) / parts;
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
   for (unsigned long long i = h0i + (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < nh;
-       i += HITS_IN_FLIGHT * stride) {
-    HitRec h[HITS_IN_FLIGHT];
-    unsigned long long k[HITS_IN_FLIGHT], sl[HITS_IN_FLIGHT];
-    U128 kv[HITS_IN_FLIGHT];
-    float4 m[HITS_IN_FLIGHT];
-#pragma unroll
-    for (int j = 0; j < HITS_IN_FLIGHT; j++) {
-      const unsigned long long ij = i + j * stride;
-      h[j].a = STC_NONE;
-      if (ij < nh) h[j] = load_hit(&p.hits[ij]);
+       i += 2 * stride) {
+    unsigned long long i2 = i + stride;
+    HitRec h0 = load_hit(&p.hits[i]);
+    HitRec h1;
+    h1.a = STC_NONE;
+    if (i2 < nh) h1 = load_hit(&p.hits[i2]);
+    const bool v0 = h0.a != STC_NONE, v1 = h1.a != STC_NONE;
+    const unsigned long long k0 = v0 ? stc_cantor(h0.a, h0.b) : 0, k1 = v1 ? stc_cantor(h1.a, h1.b) : 0;
+    unsigned long long s0 = fast_mod(k0, p.B, p.B_magic), s1 = fast_mod(k1, p.B, p.B_magic);
+    U128 kv0 = {0, 0}, kv1 = {0, 0};
+    float4 m0 = make_float4(0.f, 0.f, 0.f, 0.f), m1 = m0;
+    if (v0) {
+      kv0 = load_slot_pair(&p.slots[s0]);
+      m0 = __ldcg((const float4 *)&p.slots[s0].lo_x);
     }
-#pragma unroll
-    for (int j = 0; j < HITS_IN_FLIGHT; j++) {
-      const bool v = h[j].a != STC_NONE;
-      k[j] = v ? stc_cantor(h[j].a, h[j].b) : 0;
-      sl[j] = fast_mod(k[j], p.B, p.B_magic);
-      kv[j] = {0, 0};
-      m[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (v) {
-        kv[j] = load_slot_pair(&p.slots[sl[j]]);
-        m[j] = __ldcg((const float4 *)&p.slots[sl[j]].lo_x);
-      }
+    if (v1) {
+      kv1 = load_slot_pair(&p.slots[s1]);
+      m1 = __ldcg((const float4 *)&p.slots[s1].lo_x);
     }
-#pragma unroll
-    for (int j = 0; j < HITS_IN_FLIGHT; j++)
-      if (h[j].a != STC_NONE) process_hit_at(p, h[j], k[j], t, sl[j], kv[j], m[j]);
+    if (v0) process_hit_at(p, h0, k0, t, s0, kv0, m0);
+    if (v1) process_hit_at(p, h1, k1, t, s1, kv1, m1);
   }
 }
 
