@@ -291,6 +291,10 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
   int kstart = !vr ? 64 : (own ? (int)i - (int)(coltile * 32) + 1 : 0);
   if (kstart < 0) kstart = 0;
   if (kstart < (int)kmax) ct.tests += kmax - (uint32_t)kstart;
+  // the column loop only marks hits (one bit per column); records are made
+  // afterwards, one per lane per round, so that the loop carries no warp vote
+  // or branch for them
+  uint32_t hitmask = 0;
 #pragma unroll 1
   for (uint32_t k = 0; k < kmax; k++) {
     const float2 c = col.xy[k];
@@ -303,34 +307,37 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
       ct.exact++;
       hit = exact_within(p, pid1, col.pid[k], ct.amb);
     }
-    uint32_t hm = __ballot_sync(0xffffffffu, hit);
-    if (hm) {
-      const uint32_t jj = coltile * 32 + k;
-      if (hit) {
-        ct.hits++;
-        const uint32_t cpid = col.pid[k];
-        HitRec h;
-        h.a = pid1 < cpid ? pid1 : cpid;
-        h.b = pid1 < cpid ? cpid : pid1;
-        h.order = (rank << STC_ORDER_SHIFT) | jj;
-        if (!own) {
-          const uint32_t cnb = col.nb[k], coff = col.off[k];
-          for (uint32_t u2 = 0; u2 < cnb; u2++)
-            if (p.bu_gid[coff + u2] == row_leaf) h.order |= DUP_BIT;
-        }
-        q[qn + __popc(hm & lt_mask)] = h;
+    hitmask |= (uint32_t)hit << k;
+  }
+  ct.hits += __popc(hitmask);
+  while (__any_sync(0xffffffffu, hitmask != 0)) {
+    const bool has = hitmask != 0;
+    const uint32_t k = has ? (uint32_t)(__ffs(hitmask) - 1) : 0u;
+    hitmask &= hitmask - 1u;
+    const uint32_t hm = __ballot_sync(0xffffffffu, has);
+    if (has) {
+      const uint32_t cpid = col.pid[k];
+      HitRec h;
+      h.a = pid1 < cpid ? pid1 : cpid;
+      h.b = pid1 < cpid ? cpid : pid1;
+      h.order = (rank << STC_ORDER_SHIFT) | (coltile * 32 + k);
+      if (!own) {
+        const uint32_t cnb = col.nb[k], coff = col.off[k];
+        for (uint32_t u2 = 0; u2 < cnb; u2++)
+          if (p.bu_gid[coff + u2] == row_leaf) h.order |= DUP_BIT;
       }
-      qn += __popc(hm);
-      if (qn >= 32) {
-        flush_queue(p, q, 32, t, w);
-        uint32_t rest = qn - 32;
-        HitRec mv;
-        if (lane < rest) mv = q[32 + lane];
-        __syncwarp();
-        if (lane < rest) q[lane] = mv;
-        __syncwarp();
-        qn = rest;
-      }
+      q[qn + __popc(hm & lt_mask)] = h;
+    }
+    qn += __popc(hm);
+    if (qn >= 32) {
+      flush_queue(p, q, 32, t, w);
+      uint32_t rest = qn - 32;
+      HitRec mv;
+      if (lane < rest) mv = q[32 + lane];
+      __syncwarp();
+      if (lane < rest) q[lane] = mv;
+      __syncwarp();
+      qn = rest;
     }
   }
 }
