@@ -47,6 +47,8 @@ struct stc_ctx {
   stc_config cfg;
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;   // the schema update, beside the table update and sweep
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   cudaEvent_t ev[PH_COUNT] = {};
   std::string err;
   bool failed = false;
@@ -167,6 +169,9 @@ static void destroy_all(stc_ctx *c) {
   }
   for (int i = 0; i < PH_COUNT; i++)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+  if (c->join_ev) cudaEventDestroy(c->join_ev);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -251,6 +256,9 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
   memset(&c->stats, 0, sizeof(c->stats));
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming);
   for (int i = 0; i < PH_COUNT && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
   if (e == cudaSuccess) e = cudaMallocHost(&c->st_host, sizeof(DevState));
   if (e == cudaSuccess) e = cudaMallocHost(&c->t_pinned, sizeof(uint32_t));
@@ -452,7 +460,21 @@ static void issue_step(stc_ctx *c, bool events) {
   step_border(p, s);
   step_jobs(p, s);
   if (events) cudaEventRecord(c->ev[PH_BORDER], s);
-  step_refine(p, s);
+  step_pairs(p, s);
+  // The schema update reads this step's leaf counts and rewrites quadtree
+  // nodes, which only the pair tests read: it runs on the side stream while
+  // the table update, insert, sweep and memtable append run here (none of
+  // them touches the schema or its scan scratch), and the step ends when both
+  // have.
+  const bool schema = c->cfg.dynamic_schema != 0;
+  if (schema) {
+    cudaEventRecord(c->fork_ev, s);
+    cudaStreamWaitEvent(c->side, c->fork_ev, 0);
+    update_schema(p.sd, p.sw, p.grid_count, p.reach, p.grid_capacity, p.delay,
+                  (c->cfg.flags & STC_FLAG_SERIAL_SCHEMA) != 0, p.st, c->side);
+    cudaEventRecord(c->join_ev, c->side);
+  }
+  step_hits(p, s);
   if (events) cudaEventRecord(c->ev[PH_REFINE], s);
   step_insert(p, s);
   if (events) cudaEventRecord(c->ev[PH_INSERT], s);
@@ -460,9 +482,7 @@ static void issue_step(stc_ctx *c, bool events) {
   if (events) cudaEventRecord(c->ev[PH_SWEEP], s);
   if (c->lsm_on) lsm_append(p, c->lsm, s);
   if (events) cudaEventRecord(c->ev[PH_APPEND], s);
-  if (c->cfg.dynamic_schema)
-    update_schema(p.sd, p.sw, p.grid_count, p.reach, p.grid_capacity, p.delay,
-                  (c->cfg.flags & STC_FLAG_SERIAL_SCHEMA) != 0, p.st, s);
+  if (schema) cudaStreamWaitEvent(s, c->join_ev, 0);
 }
 
 // Captures the step (positions in xy_own) as a CUDA graph. Only this

@@ -58,7 +58,10 @@ void step_partition(PipeDev &p, cudaStream_t s);
 void step_border(PipeDev &p, cudaStream_t s);
 void step_jobs(PipeDev &p, cudaStream_t s);
 // stc_refine.cu
-void step_refine(PipeDev &p, cudaStream_t s);
+// refinement in two parts: the pair tests (which read the leaves' node
+// boxes) and the table update of their hits
+void step_pairs(PipeDev &p, cudaStream_t s);
+void step_hits(PipeDev &p, cudaStream_t s);
 // stc_meetings.cu
 void step_insert(PipeDev &p, cudaStream_t s);
 void step_sweep(PipeDev &p, cudaStream_t s);

@@ -413,9 +413,12 @@ __global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint3
   }
 }
 
-void step_refine(PipeDev &p, cudaStream_t s) {
+void step_pairs(PipeDev &p, cudaStream_t s) {
   for (uint32_t part = 0; part < p.slices; part++)
     STC_KL k_refine_a<<<STC_NUM_SMS * p.refine_bps, REFINE_THREADS, 0, s>>>(p, part, p.slices);
+}
+
+void step_hits(PipeDev &p, cudaStream_t s) {
   for (uint32_t part = 0; part < p.slices; part++)
     STC_KL k_hits<<<STC_NUM_SMS * p.hits_bps, 256, 0, s>>>(p, part, p.slices);
 }
