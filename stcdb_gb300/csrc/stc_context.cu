@@ -48,7 +48,7 @@ struct stc_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;   // the schema update, beside the table update and sweep
-  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr, fork2_ev = nullptr, join2_ev = nullptr;
   cudaEvent_t ev[PH_COUNT] = {};
   std::string err;
   bool failed = false;
@@ -170,6 +170,8 @@ static void destroy_all(stc_ctx *c) {
   for (int i = 0; i < PH_COUNT; i++)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+  if (c->fork2_ev) cudaEventDestroy(c->fork2_ev);
+  if (c->join2_ev) cudaEventDestroy(c->join2_ev);
   if (c->join_ev) cudaEventDestroy(c->join_ev);
   if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -259,6 +261,8 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork2_ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join2_ev, cudaEventDisableTiming);
   for (int i = 0; i < PH_COUNT && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
   if (e == cudaSuccess) e = cudaMallocHost(&c->st_host, sizeof(DevState));
   if (e == cudaSuccess) e = cudaMallocHost(&c->t_pinned, sizeof(uint32_t));
@@ -327,6 +331,8 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
             dalloc(c, &p.lastvalid, n) && dalloc(c, &p.iota, nu) && dalloc(c, &p.sorted_gid, n) &&
             dalloc(c, &p.sorted_pid, n) && dalloc(c, &p.sort_ktmp, nu) && dalloc(c, &p.sort_vtmp, nu) &&
             dalloc(c, &p.sort_hist, radix_hist_words(nu)) && dalloc(c, &p.grid_count, (size_t)p.G + 1) &&
+            dalloc(c, &p.sort_ktmp2, nu) && dalloc(c, &p.sort_vtmp2, nu) &&
+            dalloc(c, &p.sort_hist2, radix_hist_words(nu)) && dalloc(c, &p.scan_tmp2, scan_words) &&
             dalloc(c, &p.grid_start, (size_t)p.G + 1) && dalloc(c, &p.pts, n) && dalloc(c, &p.fxy, n) &&
             dalloc(c, &p.bcount, (size_t)n + 1) && dalloc(c, &p.boff, (size_t)n + 1) &&
             dalloc(c, &p.blist, n) && dalloc(c, &p.bres, 4 * (size_t)n) && dalloc(c, &p.sd.fbox, p.S) &&
@@ -455,9 +461,17 @@ static void issue_step(stc_ctx *c, bool events) {
   cudaStream_t s = c->stream;
   step_begin(p, c->t_pinned, s);
   if (events) cudaEventRecord(c->ev[PH_COPY], s);
-  step_partition(p, s);
+  step_descend(p, s);
+  // the border units (lookups, scan, sort by leaf) need the descent only:
+  // they run on the side stream, with their own scratch, beside the
+  // leaf-order sort and gather
+  cudaEventRecord(c->fork2_ev, s);
+  cudaStreamWaitEvent(c->side, c->fork2_ev, 0);
+  step_border(p, c->side);
+  cudaEventRecord(c->join2_ev, c->side);
+  step_leaf_order(p, s);
   if (events) cudaEventRecord(c->ev[PH_PART], s);
-  step_border(p, s);
+  cudaStreamWaitEvent(s, c->join2_ev, 0);
   step_jobs(p, s);
   if (events) cudaEventRecord(c->ev[PH_BORDER], s);
   step_pairs(p, s);

@@ -220,10 +220,13 @@ __global__ void k_jobs(PipeDev p) {
   p.job_cnt[g] = jobs;
 }
 
-void step_partition(PipeDev &p, cudaStream_t s) {
+void step_descend(PipeDev &p, cudaStream_t s) {
   cudaMemsetAsync(p.grid_count, 0, (size_t)(p.G + 1) * sizeof(uint32_t), s);
   cudaMemsetAsync(p.bcount, 0, (size_t)p.N * sizeof(uint32_t), s);
   STC_KL k_descend<<<nblk(p.N), 256, 0, s>>>(p);
+}
+
+void step_leaf_order(PipeDev &p, cudaStream_t s) {
   int bits = 1;
   while ((1u << bits) < p.G && bits < 32) bits++;
   radix_sort_u32(p.leaf_gid, p.iota, p.sorted_gid, p.sorted_pid, p.sort_ktmp, p.sort_vtmp, p.n_dev, p.N, bits,
@@ -235,14 +238,14 @@ void step_partition(PipeDev &p, cudaStream_t s) {
 void step_border(PipeDev &p, cudaStream_t s) {
   cudaMemsetAsync(p.bu_cnt, 0, (size_t)(p.G + 1) * sizeof(uint32_t), s);
   STC_KL k_border_count<<<STC_NUM_SMS * 16, 128, 0, s>>>(p);
-  exclusive_scan_u32(p.bcount, p.boff, p.N, &p.st->border_units, p.scan_tmp, s);
+  exclusive_scan_u32(p.bcount, p.boff, p.N, &p.st->border_units, p.scan_tmp2, s);
   STC_KL k_check_units<<<1, 1, 0, s>>>(p);
   STC_KL k_border_fill<<<STC_NUM_SMS * 16, 128, 0, s>>>(p);
   int bits = 1;
   while ((1u << bits) < p.G && bits < 32) bits++;
-  radix_sort_u32(p.bu_gid, p.iota, p.bu_sorted_gid, p.bu_sorted_pos, p.sort_ktmp, p.sort_vtmp,
-                 &p.st->border_units, p.U_cap, bits, p.sort_hist, p.scan_tmp, s);
-  exclusive_scan_u32(p.bu_cnt, p.bu_start, (size_t)p.G + 1, nullptr, p.scan_tmp, s);
+  radix_sort_u32(p.bu_gid, p.iota, p.bu_sorted_gid, p.bu_sorted_pos, p.sort_ktmp2, p.sort_vtmp2,
+                 &p.st->border_units, p.U_cap, bits, p.sort_hist2, p.scan_tmp2, s);
+  exclusive_scan_u32(p.bu_cnt, p.bu_start, (size_t)p.G + 1, nullptr, p.scan_tmp2, s);
 }
 
 void step_jobs(PipeDev &p, cudaStream_t s) {

@@ -50,11 +50,17 @@ struct PipeDev {
   uint32_t *cand_list;                  // cand_cap
   stc_meeting *emit;                    // E
   uint32_t *scan_tmp;
+  // scratch of the border units' scan and sort, which run on the side
+  // stream beside the leaf-order sort
+  uint32_t *scan_tmp2, *sort_ktmp2, *sort_vtmp2, *sort_hist2;
   unsigned long long *n_dev;            // device copy of N (for radix sort)
 };
 
 // stc_partition.cu
-void step_partition(PipeDev &p, cudaStream_t s);
+// partition in two parts: the descent (leaf of every object, border
+// candidates), then the leaf-order sort, leaf starts and gathered points
+void step_descend(PipeDev &p, cudaStream_t s);
+void step_leaf_order(PipeDev &p, cudaStream_t s);
 void step_border(PipeDev &p, cudaStream_t s);
 void step_jobs(PipeDev &p, cudaStream_t s);
 // stc_refine.cu
