@@ -118,6 +118,9 @@ static constexpr int RS_ITEMS = 16;
 static constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 static_assert(RS_TILE == STC_RS_TILE, "radix tile");
 static constexpr int RS_WARPS = RS_THREADS / 32;
+// the histogram, scan and scatter kernels give each of the 256 digits its
+// own thread (per-digit shared arrays and histogram rows are indexed by it)
+static_assert(RS_THREADS == 256, "one thread per 8-bit digit");
 
 size_t radix_hist_words(size_t n_max) { return 256 * ((n_max + RS_TILE - 1) / RS_TILE) + 1; }
 
