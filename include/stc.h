@@ -19,6 +19,9 @@
  *   stc_step_window     <- the per-step loop of tracer::process
  *                          (tracing/process.cpp:401-612) over a window of
  *                          steps, with the step replayed from a CUDA graph
+ *   stc_server_*        (no reference counterpart: the reference answers
+ *                          one query at a time from its experiment loops,
+ *                          tools/load_search.cpp)
  *   stc_autotune        (no reference counterpart: the reference takes
  *                          grid_capacity from its command line, config.h:29)
  *   stc_drain_meetings  <- reading h_meetings_ps[0..kv_count) after
@@ -327,6 +330,58 @@ typedef struct stc_query {
 
 stc_status stc_query_batch(stc_ctx *ctx, const stc_query *queries, size_t nq, stc_contact *out, size_t cap,
                            uint64_t *offsets, uint64_t *counts);
+
+/* ---- Serving: a request loop over stc_query_batch --------------------------
+ *
+ * A server owns a thread that answers submitted queries by continuous
+ * batching: whatever has arrived while a batch runs forms the next batch, in
+ * arrival order, admitted while the batch's device footprint stays within
+ * hbm_budget: every query takes its record and counters, and a query that
+ * returns contacts (no STC_QUERY_COUNT_ONLY) also reserves result_cap
+ * contacts of device output. The first query of a batch is always admitted.
+ * A query whose contacts exceed its reservation is answered with its count,
+ * no contacts and STC_ERR_CAPACITY. The context keeps stepping meanwhile on
+ * other threads (stc_query_batch may run beside stc_step). */
+typedef struct stc_server_config {
+  uint32_t max_batch;            /* queries per batch; 0 = 4096 */
+  uint32_t result_cap;           /* contacts reserved per non-counting query; 0 = 1024 */
+  uint64_t hbm_budget;           /* device bytes of one batch's queries and output; 0 = 64 MB */
+} stc_server_config;
+
+typedef struct stc_answer {
+  uint64_t ticket;               /* from stc_server_submit */
+  uint64_t count;                /* matches of the query */
+  uint64_t contact_offset;       /* its contacts in the poll's contacts array */
+  uint32_t stored;               /* contacts written there */
+  uint32_t status;               /* STC_OK, or the error of its batch / STC_ERR_CAPACITY */
+  double latency_ms;             /* from its arrival time to its answer */
+  uint32_t batch;                /* sequence number of the batch that answered it */
+  uint32_t batch_size;           /* queries in that batch */
+} stc_answer;
+
+typedef struct stc_server_stats {
+  uint64_t submitted, answered, batches;
+  uint64_t max_batch_queries;    /* largest batch */
+  uint64_t max_batch_bytes;      /* largest admitted footprint */
+  uint64_t budget_cuts;          /* batches closed by the budget before max_batch */
+} stc_server_stats;
+
+typedef struct stc_server stc_server;
+
+stc_status stc_server_start(stc_ctx *ctx, const stc_server_config *cfg, stc_server **out);
+/* Queues nq queries that arrived at arrival_s (seconds on the host's
+ * monotonic clock, as CLOCK_MONOTONIC; <= 0: now); *first_ticket receives the
+ * ticket of the first, the others follow in order. */
+stc_status stc_server_submit(stc_server *srv, const stc_query *queries, size_t nq, double arrival_s,
+                             uint64_t *first_ticket);
+/* Moves up to cap answers (and their contacts, up to contacts_cap) completed
+ * since the last poll into out / contacts; waits up to wait_ms for the first
+ * when none is ready. */
+stc_status stc_server_poll(stc_server *srv, stc_answer *out, size_t cap, stc_contact *contacts,
+                           size_t contacts_cap, size_t *n, int wait_ms);
+stc_status stc_server_get_stats(const stc_server *srv, stc_server_stats *out);
+/* Answers everything queued, stops the thread and frees the server. */
+stc_status stc_server_stop(stc_server *srv);
 
 /* ---- Block files ---------------------------------------------------------
  *

@@ -38,6 +38,7 @@ CU_SOURCES = [
     "stc_tracegen.cu",
     "stc_compact.cu",
     "stc_tune.cu",
+    "stc_serve.cu",
 ]
 
 
@@ -95,7 +96,7 @@ def build_cuda(verbose_ptxas: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(_run, jobs))
     if jobs or _stale(out, objs):
-        _run([NVCC, GENCODE, "-shared", "-o", out] + objs + ["-lcudart"])
+        _run([NVCC, GENCODE, "-shared", "-o", out] + objs + ["-lcudart", "-lpthread"])
     return out
 
 

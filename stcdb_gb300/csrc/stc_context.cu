@@ -768,8 +768,20 @@ static stc_status query_checks(stc_ctx *c, const char *who) {
   return STC_OK;
 }
 
+namespace stc {
+// stc_query_batch with a bound on the match records held on the device (the
+// serving loop's admission); 0 = none.
+stc_status query_batch_limited(stc_ctx *c, const stc_query *queries, size_t nq, stc_contact *out, size_t cap,
+                               uint64_t *offsets, uint64_t *counts, size_t device_limit);
+}
+
 extern "C" stc_status stc_query_batch(stc_ctx *c, const stc_query *queries, size_t nq, stc_contact *out,
                                       size_t cap, uint64_t *offsets, uint64_t *counts) {
+  return stc::query_batch_limited(c, queries, nq, out, cap, offsets, counts, 0);
+}
+
+stc_status stc::query_batch_limited(stc_ctx *c, const stc_query *queries, size_t nq, stc_contact *out, size_t cap,
+                                    uint64_t *offsets, uint64_t *counts, size_t device_limit) {
   stc_status st = query_checks(c, "stc_query_batch");
   if (st != STC_OK) return st;
   if ((!queries && nq) || !offsets || (!out && cap)) {
@@ -785,7 +797,7 @@ extern "C" stc_status stc_query_batch(stc_ctx *c, const stc_query *queries, size
     }
   }
   std::string err;
-  st = lsm_query(c->lsmh, queries, nq, out, cap, offsets, counts, err);
+  st = lsm_query(c->lsmh, queries, nq, out, cap, offsets, counts, err, device_limit);
   if (st != STC_OK) g_create_error = "stc_query_batch: " + err;
   return st;
 }

@@ -211,9 +211,11 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
 stc_status lsm_query_reserve(LsmHost &H, size_t nq, uint32_t F, std::string &err);
 
 // Runs a batch of queries over the retained blocks on H.qstream (see
-// stc_query_batch in include/stc.h).
+// stc_query_batch in include/stc.h). device_limit (0 = none) bounds the match
+// records the device output may hold: a batch with more matches is only
+// counted (offsets and counts filled, out untouched).
 stc_status lsm_query(LsmHost &H, const stc_query *q, size_t nq, stc_contact *out, size_t cap, uint64_t *offsets,
-                     uint64_t *counts, std::string &err);
+                     uint64_t *counts, std::string &err, size_t device_limit = 0);
 
 // Host restatement of CTF::get_ctf_bits (tracing/step_merge.cpp:140-186);
 // returns false when the key would exceed 64 box bits or 128 key bits.

@@ -949,7 +949,7 @@ stc_status lsm_query_reserve(LsmHost &H, size_t nq, uint32_t F, std::string &err
 }
 
 stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *out, size_t cap, uint64_t *offsets,
-                     uint64_t *counts, std::string &err) {
+                     uint64_t *counts, std::string &err, size_t device_limit) {
   std::lock_guard<std::mutex> qlock(H.query_mu);
   std::shared_lock<std::shared_mutex> lock(H.blocks_mu);
   const uint32_t nb = (uint32_t)H.blocks.size();
@@ -988,6 +988,7 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
   e = cudaMemcpyAsync(H.d_qb, qb, nb * sizeof(QBlock), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(H.d_q, H.h_q, nq * sizeof(stc_query), cudaMemcpyHostToDevice, s);
   unsigned long long total = 0;
+  bool over = false;  // more matches than device_limit: counted only
   for (int attempt = 0; attempt < 2 && e == cudaSuccess; attempt++) {
     e = cudaMemsetAsync(H.d_count, 0, sizeof(unsigned long long), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(H.d_qcounts, 0, nq * sizeof(unsigned long long), s);
@@ -1005,17 +1006,25 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
     }
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(H.h_counts + nq, H.d_count, sizeof(total), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess && counts)
+    if (e == cudaSuccess && (counts || device_limit))
       e = cudaMemcpyAsync(H.h_counts, H.d_qcounts, nq * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     total = H.h_counts[nq];
     if (e == cudaSuccess && counts) memcpy(counts, H.h_counts, nq * sizeof(unsigned long long));
     if (e != cudaSuccess || total <= H.out_cap) break;
+    if (device_limit && total > device_limit) {
+      over = true;
+      break;
+    }
     e = grow(&H.d_out, &H.out_cap, (size_t)total);  // too many matches: once more with room for all
   }
   if (e != cudaSuccess) {
     err = std::string("query: ") + cudaGetErrorString(e);
     return STC_ERR_CUDA;
+  }
+  if (over) {
+    for (size_t i = 0; i < nq; i++) offsets[i + 1] = offsets[i] + H.h_counts[i];
+    return STC_OK;
   }
   if (total) {
     e = grow_pinned(&H.h_recs, &H.hrecs_cap, (size_t)total);

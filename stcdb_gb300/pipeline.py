@@ -142,6 +142,22 @@ QUERY_DTYPE = np.dtype([("kind", "<u4"), ("pid", "<u4"), ("t_start", "<u4"), ("t
                         ("box", "<f8", (4,))])
 assert QUERY_DTYPE.itemsize == 48
 QUERY_OBJECT, QUERY_BOX, QUERY_COUNT_ONLY = 0, 1, 0x100
+ANSWER_DTYPE = np.dtype([("ticket", "<u8"), ("count", "<u8"), ("contact_offset", "<u8"), ("stored", "<u4"),
+                         ("status", "<u4"), ("latency_ms", "<f8"), ("batch", "<u4"), ("batch_size", "<u4")])
+assert ANSWER_DTYPE.itemsize == 48
+
+
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("max_batch", ctypes.c_uint32), ("result_cap", ctypes.c_uint32), ("hbm_budget", ctypes.c_uint64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("answered", ctypes.c_uint64), ("batches", ctypes.c_uint64),
+                ("max_batch_queries", ctypes.c_uint64), ("max_batch_bytes", ctypes.c_uint64),
+                ("budget_cuts", ctypes.c_uint64)]
+
+    def as_dict(self) -> dict:
+        return {name: int(getattr(self, name)) for name, _ in self._fields_}
 
 
 def sort_contacts(c: np.ndarray) -> np.ndarray:
@@ -257,6 +273,18 @@ def _lib():
                                      ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32,
                                      ctypes.POINTER(_TuneResult)]
         lib.stc_autotune.restype = ctypes.c_int
+        lib.stc_server_start.argtypes = [ctypes.c_void_p, ctypes.POINTER(_ServerConfig), ctypes.POINTER(ctypes.c_void_p)]
+        lib.stc_server_start.restype = ctypes.c_int
+        lib.stc_server_submit.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_double,
+                                          ctypes.POINTER(ctypes.c_uint64)]
+        lib.stc_server_submit.restype = ctypes.c_int
+        lib.stc_server_poll.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                        ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t), ctypes.c_int]
+        lib.stc_server_poll.restype = ctypes.c_int
+        lib.stc_server_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ServerStats)]
+        lib.stc_server_get_stats.restype = ctypes.c_int
+        lib.stc_server_stop.argtypes = [ctypes.c_void_p]
+        lib.stc_server_stop.restype = ctypes.c_int
         lib.stc_drain_meetings.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                            ctypes.POINTER(ctypes.c_size_t)]
         lib.stc_drain_meetings.restype = ctypes.c_int
@@ -446,6 +474,10 @@ class Pipeline:
         q["kind"] |= QUERY_COUNT_ONLY
         return self.query_batch(q, with_counts=True)[1]
 
+    def server(self, max_batch: int = 0, result_cap: int = 0, hbm_budget: int = 0) -> "Server":
+        """A request loop answering queries by continuous batching (stc_server_start)."""
+        return Server(self, max_batch, result_cap, hbm_budget)
+
     def checkpoint(self, path: str) -> None:
         """Writes the context's step-to-step state to one file (stc_checkpoint)."""
         self._check(self._lib.stc_checkpoint(self._h, path.encode()))
@@ -513,3 +545,54 @@ def meetings_digest(m: np.ndarray) -> str:
     import hashlib
     s = sort_meetings(np.ascontiguousarray(m, dtype=MEETING_DTYPE))
     return hashlib.sha256(s.tobytes()).hexdigest()
+
+
+class Server:
+    """stc_server_*: queries submitted from any thread are answered by the
+    library's serving thread in batches admitted by device footprint; answers
+    carry the latency from each query's arrival (seconds on the monotonic
+    clock, as time.perf_counter on Linux)."""
+
+    def __init__(self, pipe: "Pipeline", max_batch: int = 0, result_cap: int = 0, hbm_budget: int = 0):
+        self._lib = pipe._lib
+        self._pipe = pipe
+        cfg = _ServerConfig(max_batch, result_cap, hbm_budget)
+        h = ctypes.c_void_p()
+        st = self._lib.stc_server_start(pipe._h, ctypes.byref(cfg), ctypes.byref(h))
+        if st != 0:
+            raise StcError(st, self._lib.stc_last_error(None).decode())
+        self._h = h
+
+    def submit(self, queries: np.ndarray, arrival: float = 0.0) -> int:
+        """Queues the queries (QUERY_DTYPE); returns the first ticket."""
+        q = np.ascontiguousarray(queries, dtype=QUERY_DTYPE)
+        first = ctypes.c_uint64()
+        st = self._lib.stc_server_submit(self._h, q.ctypes.data, len(q), float(arrival), ctypes.byref(first))
+        if st != 0:
+            raise StcError(st, "stc_server_submit")
+        return int(first.value)
+
+    def poll(self, cap: int = 65536, contacts_cap: int = 0, wait_ms: int = 0) -> tuple:
+        """(answers, contacts) completed since the last poll."""
+        ans = np.empty(cap, ANSWER_DTYPE)
+        con = np.empty(max(contacts_cap, 1), CONTACT_DTYPE)
+        n = ctypes.c_size_t(0)
+        st = self._lib.stc_server_poll(self._h, ans.ctypes.data, cap, con.ctypes.data, contacts_cap,
+                                       ctypes.byref(n), int(wait_ms))
+        if st != 0:
+            raise StcError(st, "stc_server_poll")
+        a = ans[: n.value]
+        used = int((a["contact_offset"] + a["stored"]).max()) if len(a) else 0
+        return a, con[:used]
+
+    def stats(self) -> ServerStats:
+        s = ServerStats()
+        self._lib.stc_server_get_stats(self._h, ctypes.byref(s))
+        return s
+
+    def stop(self) -> None:
+        """Answers everything queued and stops the serving thread."""
+        if self._h:
+            self._lib.stc_server_stop(self._h)
+            self._h = None
+
