@@ -290,19 +290,22 @@ def make_queries(rng, n, N, mbr, t_now):
 
 
 def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
-    """Continuous batching: queries arrive as a Poisson stream; whatever has
-    arrived while a batch ran forms the next batch. Latency = answer time -
-    arrival time. The main thread keeps stepping meanwhile (host input)."""
+    """Queries arrive as a Poisson stream and go to the library's request loop
+    (stc_server_*), which answers them by continuous batching (whatever has
+    arrived while a batch ran forms the next batch, admitted by device
+    footprint). Latency = answer time - arrival time, both on the monotonic
+    clock. The main thread keeps stepping meanwhile (host input)."""
+    from stcdb_gb300.pipeline import QUERY_COUNT_ONLY
     rng = np.random.default_rng(12345)
     rate = float(args.query_rate)
-    lat, sizes, contacts = [], [], [0]
+    answers = []
     cur_t = [t0 - 1]
     done = threading.Event()
     errors = []
+    srv = pipe.server(max_batch=4096, result_cap=1024, hbm_budget=64 << 20)
 
     def server():
-        start = time.perf_counter()
-        next_arrival = start + rng.exponential(1.0 / rate)
+        next_arrival = time.perf_counter() + rng.exponential(1.0 / rate)
         while not done.is_set():
             now = time.perf_counter()
             arrivals = []
@@ -310,18 +313,19 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
                 arrivals.append(next_arrival)
                 next_arrival += rng.exponential(1.0 / rate)
             if not arrivals:
-                time.sleep(min(max(next_arrival - now, 0.0), 0.0005))
+                a, _ = srv.poll(cap=8192, wait_ms=0)
+                if len(a):
+                    answers.append(a)
+                time.sleep(min(max(next_arrival - time.perf_counter(), 0.0), 0.0005))
                 continue
             qs = make_queries(rng, len(arrivals), N, mbr, cur_t[0])
+            qs["kind"] |= QUERY_COUNT_ONLY
             try:
-                counts = pipe.query_counts(qs)
+                for q, t_arr in zip(qs, arrivals):
+                    srv.submit(q[None], arrival=t_arr)
             except Exception as e:  # noqa: BLE001 - reported in the JSON line
                 errors.append(str(e))
                 return
-            t_done = time.perf_counter()
-            lat.extend(t_done - a for a in arrivals)
-            sizes.append(len(arrivals))
-            contacts[0] += int(counts.sum())
 
     th = threading.Thread(target=server, daemon=True)
     pipe.set_step_slices(args.serve_slices)  # query kernels get the GPU between slices
@@ -338,18 +342,33 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
     wall = time.perf_counter() - w0
     done.set()
     th.join()
+    # the rest of what was submitted, then the loop's statistics
+    deadline = time.perf_counter() + 30.0
+    while sum(len(a) for a in answers) < srv.stats().submitted and time.perf_counter() < deadline:
+        a, _ = srv.poll(cap=65536, wait_ms=100)
+        if len(a):
+            answers.append(a)
+    sst = srv.stats()
+    srv.stop()
     gc.enable()
     pipe.set_step_slices(args.step_slices)
     if errors:
         return {"error": errors[0]}
-    lat_ms = np.array(lat) * 1e3
-    return {"rate_target_per_s": rate, "answered": len(lat), "qps": len(lat) / wall,
-            "p50_ms": float(np.percentile(lat_ms, 50)) if len(lat) else None,
-            "p99_ms": float(np.percentile(lat_ms, 99)) if len(lat) else None,
-            "p999_ms": float(np.percentile(lat_ms, 99.9)) if len(lat) else None,
-            "max_ms": float(lat_ms.max()) if len(lat) else None,
-            "mean_batch": float(np.mean(sizes)) if sizes else 0.0, "batches": len(sizes),
-            "contacts_per_query": contacts[0] / max(len(lat), 1),
+    ans = np.concatenate(answers) if answers else np.zeros(0)
+    if len(ans) and (ans["status"] != 0).any():
+        return {"error": f"{int((ans['status'] != 0).sum())} queries failed"}
+    lat_ms = ans["latency_ms"] if len(ans) else np.zeros(0)
+    sizes = np.bincount(ans["batch"]) if len(ans) else np.zeros(0)
+    return {"rate_target_per_s": rate, "answered": len(ans), "qps": len(ans) / wall,
+            "p50_ms": float(np.percentile(lat_ms, 50)) if len(ans) else None,
+            "p99_ms": float(np.percentile(lat_ms, 99)) if len(ans) else None,
+            "p999_ms": float(np.percentile(lat_ms, 99.9)) if len(ans) else None,
+            "max_ms": float(lat_ms.max()) if len(ans) else None,
+            "mean_batch": float(sizes[sizes > 0].mean()) if len(ans) else 0.0, "batches": int(sst.batches),
+            "contacts_per_query": float(ans["count"].mean()) if len(ans) else 0.0,
+            "server": {"loop": "stc_server (library thread, continuous batching)", "max_batch": 4096,
+                       "hbm_budget_bytes": 64 << 20, "max_batch_queries": int(sst.max_batch_queries),
+                       "max_batch_bytes": int(sst.max_batch_bytes), "budget_cuts": int(sst.budget_cuts)},
             "mix": "60% object (window 10-10000 steps), 40% box (50 m-5 km, window 10-3600 steps); "
                    "match counts, as the reference's searches return",
             "blocks": 1, "step_slices": args.serve_slices, "ingest_pos_updates_per_s": N * steps / wall,
