@@ -391,6 +391,14 @@ def max_over_ranks(args, v):
     return float(t.item())
 
 
+# DRAM bytes (read + write) of the refinement phase (k_refine_a + k_hits)
+# per hit, from one ncu capture of both kernels on the 3M-object workload:
+# 1.414 GB for 6.09M hits. The traffic grows with the hits (records written
+# and read, one table slot and two positions per hit), so the 10M line scales
+# it by its own hit count.
+REFINE_DRAM_BYTES_PER_HIT = 1.414e9 / 6.085e6
+
+
 def kernel_bytes(s, N, B):
     """Algorithmic bytes per launch of the step's kernels.
     partition: 36 N (read positions, write leaf-ordered points, id map)
@@ -634,7 +642,10 @@ def main():
                 "d2h_bytes_per_step": int(r["d2h"] / K)},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
-                     "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": (REFINE_DRAM_BYTES_PER_HIT * sum(s.hits for s in r["stats"]) / K
+                                 if dom == "refine" else None),
+                     "traffic_source": "ncu capture of k_refine_a + k_hits at 3M objects, scaled by hits",
                      "algorithmic_bytes": kb[dom], "launch_ms": phase_ms[dom]},
         "phase_ms": phase_ms,
         "flush": flush_line(r["flush"], peak),
