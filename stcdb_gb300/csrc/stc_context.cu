@@ -31,6 +31,7 @@ void set_thread_error(const std::string &msg) { g_create_error = msg; }
 }  // namespace stc
 
 static constexpr size_t DRAIN_CHUNK = (size_t)8 << 20;  // bytes per pinned staging chunk of a drain
+static constexpr uint32_t PAIR_PARTS = 4;                // parts of the pair tests (more while serving)
 
 // A large host<->device copy of a step or drain as pieces of COPY_PIECE
 // bytes: the copy engine takes them one by one, so that the small copies of
@@ -47,8 +48,10 @@ struct stc_ctx {
   stc_config cfg;
   int device = 0;
   cudaStream_t stream = nullptr;
-  cudaStream_t side = nullptr;   // the schema update, beside the table update and sweep
-  cudaEvent_t fork_ev = nullptr, join_ev = nullptr, fork2_ev = nullptr, join2_ev = nullptr;
+  cudaStream_t side = nullptr;   // border units; the table update beside the pair tests
+  cudaStream_t side2 = nullptr;  // the schema update, beside the table update and sweep
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr, fork2_ev = nullptr, join2_ev = nullptr, hits_ev = nullptr;
+  cudaEvent_t part_ev[STC_MAX_PARTS] = {};  // end of each part of the pair tests
   cudaEvent_t ev[PH_COUNT] = {};
   std::string err;
   bool failed = false;
@@ -171,9 +174,13 @@ static void destroy_all(stc_ctx *c) {
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->fork_ev) cudaEventDestroy(c->fork_ev);
   if (c->fork2_ev) cudaEventDestroy(c->fork2_ev);
+  if (c->hits_ev) cudaEventDestroy(c->hits_ev);
+  for (cudaEvent_t ev : c->part_ev)
+    if (ev) cudaEventDestroy(ev);
   if (c->join2_ev) cudaEventDestroy(c->join2_ev);
   if (c->join_ev) cudaEventDestroy(c->join_ev);
   if (c->side) cudaStreamDestroy(c->side);
+  if (c->side2) cudaStreamDestroy(c->side2);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -259,10 +266,14 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork2_ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join2_ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->hits_ev, cudaEventDisableTiming);
+  for (uint32_t i = 0; i < STC_MAX_PARTS && e == cudaSuccess; i++)
+    e = cudaEventCreateWithFlags(&c->part_ev[i], cudaEventDisableTiming);
   for (int i = 0; i < PH_COUNT && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
   if (e == cudaSuccess) e = cudaMallocHost(&c->st_host, sizeof(DevState));
   if (e == cudaSuccess) e = cudaMallocHost(&c->t_pinned, sizeof(uint32_t));
@@ -332,6 +343,7 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
             dalloc(c, &p.sorted_pid, n) && dalloc(c, &p.sort_ktmp, nu) && dalloc(c, &p.sort_vtmp, nu) &&
             dalloc(c, &p.sort_hist, radix_hist_words(nu)) && dalloc(c, &p.grid_count, (size_t)p.G + 1) &&
             dalloc(c, &p.sort_ktmp2, nu) && dalloc(c, &p.sort_vtmp2, nu) &&
+            dalloc(c, &p.hit_bounds, STC_MAX_PARTS + 1) &&
             dalloc(c, &p.sort_hist2, radix_hist_words(nu)) && dalloc(c, &p.scan_tmp2, scan_words) &&
             dalloc(c, &p.grid_start, (size_t)p.G + 1) && dalloc(c, &p.pts, n) && dalloc(c, &p.fxy, n) &&
             dalloc(c, &p.bcount, (size_t)n + 1) && dalloc(c, &p.boff, (size_t)n + 1) &&
@@ -474,21 +486,31 @@ static void issue_step(stc_ctx *c, bool events) {
   cudaStreamWaitEvent(s, c->join2_ev, 0);
   step_jobs(p, s);
   if (events) cudaEventRecord(c->ev[PH_BORDER], s);
-  step_pairs(p, s);
+  // The pair tests run in parts; each part's hits are applied to the table
+  // on the side stream while the next part's pairs are tested (the two
+  // kernels are bound by different units; concurrent table updates are safe,
+  // new meetings take their slots by priority).
+  const uint32_t parts = std::min<uint32_t>(std::max<uint32_t>(p.slices, PAIR_PARTS), STC_MAX_PARTS);
+  for (uint32_t part = 0; part < parts; part++) {
+    step_pairs_part(p, part, parts, s);
+    cudaEventRecord(c->part_ev[part], s);
+    cudaStreamWaitEvent(c->side, c->part_ev[part], 0);
+    step_hits_part(p, part, parts, c->side);
+  }
+  cudaEventRecord(c->hits_ev, c->side);
   // The schema update reads this step's leaf counts and rewrites quadtree
-  // nodes, which only the pair tests read: it runs on the side stream while
-  // the table update, insert, sweep and memtable append run here (none of
-  // them touches the schema or its scan scratch), and the step ends when both
-  // have.
+  // nodes, which only the pair tests read: once they are done it runs on a
+  // third stream while the table update, insert, sweep and memtable append
+  // run (none of them touches the schema or its scan scratch), and the step
+  // ends when all have.
   const bool schema = c->cfg.dynamic_schema != 0;
   if (schema) {
-    cudaEventRecord(c->fork_ev, s);
-    cudaStreamWaitEvent(c->side, c->fork_ev, 0);
+    cudaStreamWaitEvent(c->side2, c->part_ev[parts - 1], 0);
     update_schema(p.sd, p.sw, p.grid_count, p.reach, p.grid_capacity, p.delay,
-                  (c->cfg.flags & STC_FLAG_SERIAL_SCHEMA) != 0, p.st, c->side);
-    cudaEventRecord(c->join_ev, c->side);
+                  (c->cfg.flags & STC_FLAG_SERIAL_SCHEMA) != 0, p.st, c->side2);
+    cudaEventRecord(c->join_ev, c->side2);
   }
-  step_hits(p, s);
+  cudaStreamWaitEvent(s, c->hits_ev, 0);
   if (events) cudaEventRecord(c->ev[PH_REFINE], s);
   step_insert(p, s);
   if (events) cudaEventRecord(c->ev[PH_INSERT], s);

@@ -46,6 +46,7 @@ struct PipeDev {
   Slot *slots;                          // B
   HitRec *hits;                         // hit_cap: hits of the step, applied by k_hits
   unsigned long long hit_cap;
+  unsigned long long *hit_bounds;       // [MAX_PARTS + 1]: hit buffer end after each part of the pair tests
   Cand *cset;                           // C
   uint32_t *cand_list;                  // cand_cap
   stc_meeting *emit;                    // E
@@ -66,8 +67,11 @@ void step_jobs(PipeDev &p, cudaStream_t s);
 // stc_refine.cu
 // refinement in two parts: the pair tests (which read the leaves' node
 // boxes) and the table update of their hits
-void step_pairs(PipeDev &p, cudaStream_t s);
-void step_hits(PipeDev &p, cudaStream_t s);
+// Part `part` of `parts` of the pair tests, then the mark of its hit range;
+// the table update of that range (k_hits) may run beside the next part.
+constexpr uint32_t STC_MAX_PARTS = 64;
+void step_pairs_part(PipeDev &p, uint32_t part, uint32_t parts, cudaStream_t s);
+void step_hits_part(PipeDev &p, uint32_t part, uint32_t parts, cudaStream_t s);
 // stc_meetings.cu
 void step_insert(PipeDev &p, cudaStream_t s);
 void step_sweep(PipeDev &p, cudaStream_t s);

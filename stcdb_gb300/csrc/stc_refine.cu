@@ -173,10 +173,12 @@ __device__ __forceinline__ HitRec load_hit(const HitRec *r) {
 // One thread per hit, two hits in flight per thread: both records and both
 // home slots are requested before either is used.
 // Slice `part` of `parts` covers hits [nh * part / parts, nh * (part + 1) / parts).
+// Part `part` applies the hits the pair tests' part `part` appended:
+// [hit_bounds[part], hit_bounds[part + 1]).
 __global__ void __launch_bounds__(256) k_hits(PipeDev p, uint32_t part, uint32_t parts) {
   const uint32_t t = p.st->step_t;
-  const unsigned long long nt = p.st->hit_count < p.hit_cap ? p.st->hit_count : p.hit_cap;
-  const unsigned long long h0i = nt * part / parts, nh = nt * (part + 1) / parts;
+  (void)parts;
+  const unsigned long long h0i = p.hit_bounds[part], nh = p.hit_bounds[part + 1];
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
   for (unsigned long long i = h0i + (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < nh;
        i += 2 * stride) {
@@ -413,14 +415,21 @@ __global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint3
   }
 }
 
-void step_pairs(PipeDev &p, cudaStream_t s) {
-  for (uint32_t part = 0; part < p.slices; part++)
-    STC_KL k_refine_a<<<STC_NUM_SMS * p.refine_bps, REFINE_THREADS, 0, s>>>(p, part, p.slices);
+// hit_bounds[part + 1] = the hit buffer's end after part `part` (its hits
+// are [hit_bounds[part], hit_bounds[part + 1]): parts run in stream order)
+__global__ void k_hit_mark(PipeDev p, uint32_t part) {
+  const unsigned long long n = p.st->hit_count;
+  p.hit_bounds[part + 1] = n < p.hit_cap ? n : p.hit_cap;
+  if (part == 0) p.hit_bounds[0] = 0;
 }
 
-void step_hits(PipeDev &p, cudaStream_t s) {
-  for (uint32_t part = 0; part < p.slices; part++)
-    STC_KL k_hits<<<STC_NUM_SMS * p.hits_bps, 256, 0, s>>>(p, part, p.slices);
+void step_pairs_part(PipeDev &p, uint32_t part, uint32_t parts, cudaStream_t s) {
+  STC_KL k_refine_a<<<STC_NUM_SMS * p.refine_bps, REFINE_THREADS, 0, s>>>(p, part, parts);
+  STC_KL k_hit_mark<<<1, 1, 0, s>>>(p, part);
+}
+
+void step_hits_part(PipeDev &p, uint32_t part, uint32_t parts, cudaStream_t s) {
+  STC_KL k_hits<<<STC_NUM_SMS * p.hits_bps, 256, 0, s>>>(p, part, parts);
 }
 
 }  // namespace stc
