@@ -160,48 +160,27 @@ __global__ void k_rs_hist(const uint32_t *keys, const unsigned long long *n_dev,
 static constexpr int RS_WARP_ITEMS = RS_TILE / RS_WARPS;  // 512
 static_assert(RS_WARP_ITEMS == 32 * RS_ITEMS, "warp share");
 
-__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t *k_in, const uint32_t *v_in,
-                                                           uint32_t *k_out, uint32_t *v_out,
-                                                           const unsigned long long *n_dev, size_t n_max, int shift,
-                                                           uint32_t dmask, const uint32_t *hist, uint32_t nb) {
-  __shared__ uint2 s_kv[RS_TILE];     // the tile in digit order
-  __shared__ uint32_t base_off[256];  // global position of the tile's first item of each digit
-  __shared__ uint32_t loc[256];       // the same in the tile's digit order
-  __shared__ uint32_t whist[RS_WARPS][256];
-  __shared__ uint32_t scan_tmp[RS_WARPS];
-  size_t n = (size_t)*n_dev;
-  if (n > n_max) n = n_max;
-  size_t tile = (size_t)blockIdx.x * RS_TILE;
-  if (tile >= n) return;
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+// Ranks the thread's RS_ITEMS items among the warp's earlier items of their
+// digit (pr) and counts the warp's items per digit (wh). FULL: every item of
+// the tile is valid (all tiles but the last), so no lane needs masking.
+template <bool FULL>
+__device__ __forceinline__ void rank_items(const uint32_t *kr, uint32_t *pr, uint32_t *wh, uint32_t warp,
+                                           uint32_t lane, uint32_t in_tile, int shift, uint32_t dmask) {
   const uint32_t lt_mask = (1u << lane) - 1u;
-  const uint32_t in_tile = (uint32_t)min((size_t)RS_TILE, n - tile);
-  base_off[threadIdx.x] = hist[(size_t)threadIdx.x * nb + blockIdx.x];
-  for (int w = 0; w < RS_WARPS; w++) whist[w][threadIdx.x] = 0;
-  // all of the thread's items are requested before the ranking starts
-  uint32_t kr[RS_ITEMS], vr[RS_ITEMS], pr[RS_ITEMS];
 #pragma unroll
   for (int it = 0; it < RS_ITEMS; it++) {
     const uint32_t li = warp * RS_WARP_ITEMS + (uint32_t)it * 32u + lane;
-    kr[it] = li < in_tile ? __ldcs(&k_in[tile + li]) : 0u;
-    vr[it] = li < in_tile ? __ldcs(&v_in[tile + li]) : 0u;
-  }
-  __syncthreads();
-  uint32_t *wh = whist[warp];
-#pragma unroll
-  for (int it = 0; it < RS_ITEMS; it++) {
-    const uint32_t li = warp * RS_WARP_ITEMS + (uint32_t)it * 32u + lane;
-    const bool valid = li < in_tile;
+    const bool valid = FULL || li < in_tile;
     const uint32_t digit = (kr[it] >> shift) & dmask;
     // lanes with the same digit: one vote per digit bit (valid lanes only)
-    uint32_t peers = __ballot_sync(0xffffffffu, valid);
+    uint32_t peers = FULL ? 0xffffffffu : __ballot_sync(0xffffffffu, valid);
 #pragma unroll
     for (int b = 0; b < 8; b++) {
       const bool bit = (digit >> b) & 1u;
       const uint32_t m = __ballot_sync(0xffffffffu, bit);
       peers &= bit ? m : ~m;
     }
-    if (!valid) peers = 1u << lane;
+    if (!FULL && !valid) peers = 1u << lane;
     const uint32_t rank = __popc(peers & lt_mask);
     const uint32_t leader = __ffs(peers) - 1u;
     uint32_t before = 0;
@@ -213,15 +192,47 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t *k_in,
     pr[it] = before + rank;  // position among the warp's items of this digit
     __syncwarp();
   }
+}
+
+__global__ void __launch_bounds__(RS_THREADS, 3) k_rs_scatter(const uint32_t *k_in, const uint32_t *v_in,
+                                                           uint32_t *k_out, uint32_t *v_out,
+                                                           const unsigned long long *n_dev, size_t n_max, int shift,
+                                                           uint32_t dmask, const uint32_t *hist, uint32_t nb) {
+  __shared__ uint2 s_kv[RS_TILE];     // the tile in digit order
+  __shared__ uint32_t base_off[256];  // output position of tile position i of digit d, less i
+  // per warp and digit: counts, then the tile position of the warp's first item of the digit
+  __shared__ uint32_t whist[RS_WARPS][256];
+  __shared__ uint32_t scan_tmp[RS_WARPS];
+  size_t n = (size_t)*n_dev;
+  if (n > n_max) n = n_max;
+  size_t tile = (size_t)blockIdx.x * RS_TILE;
+  if (tile >= n) return;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t in_tile = (uint32_t)min((size_t)RS_TILE, n - tile);
+  const bool full = in_tile == RS_TILE;
+  base_off[threadIdx.x] = hist[(size_t)threadIdx.x * nb + blockIdx.x];
+  for (int w = 0; w < RS_WARPS; w++) whist[w][threadIdx.x] = 0;
+  // all of the thread's items are requested before the ranking starts
+  uint32_t kr[RS_ITEMS], vr[RS_ITEMS], pr[RS_ITEMS];
+#pragma unroll
+  for (int it = 0; it < RS_ITEMS; it++) {
+    const uint32_t li = warp * RS_WARP_ITEMS + (uint32_t)it * 32u + lane;
+    kr[it] = li < in_tile ? __ldcs(&k_in[tile + li]) : 0u;
+    vr[it] = li < in_tile ? __ldcs(&v_in[tile + li]) : 0u;
+  }
+  __syncthreads();
+  if (full) rank_items<true>(kr, pr, whist[warp], warp, lane, in_tile, shift, dmask);
+  else rank_items<false>(kr, pr, whist[warp], warp, lane, in_tile, shift, dmask);
   __syncthreads();
   {
-    // per digit: the tile's exclusive offset, and each warp's offset within it
+    // per digit: the tile's exclusive offset (block scan over digits), then
+    // each warp's first tile position of the digit
     const uint32_t d = threadIdx.x;
-    uint32_t cnt = 0;
+    uint32_t c[RS_WARPS], cnt = 0;
+#pragma unroll
     for (int w = 0; w < RS_WARPS; w++) {
-      const uint32_t c = whist[w][d];
-      whist[w][d] = cnt;
-      cnt += c;
+      c[w] = whist[w][d];
+      cnt += c[w];
     }
     uint32_t incl = cnt;
 #pragma unroll
@@ -233,17 +244,21 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t *k_in,
     __syncthreads();
     uint32_t before = 0;
     for (uint32_t w = 0; w < warp; w++) before += scan_tmp[w];
-    loc[d] = before + incl - cnt;
-    base_off[d] -= before + incl - cnt;  // now: output position of tile position i of digit d, less i
+    uint32_t start = before + incl - cnt;
+    base_off[d] -= start;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; w++) {
+      whist[w][d] = start;
+      start += c[w];
+    }
   }
   __syncthreads();
 #pragma unroll
   for (int it = 0; it < RS_ITEMS; it++) {
     const uint32_t li = warp * RS_WARP_ITEMS + (uint32_t)it * 32u + lane;
-    if (li < in_tile) {
+    if (full || li < in_tile) {
       const uint32_t digit = (kr[it] >> shift) & dmask;
-      const uint32_t pos = loc[digit] + whist[warp][digit] + pr[it];
-      s_kv[pos] = make_uint2(kr[it], vr[it]);
+      s_kv[whist[warp][digit] + pr[it]] = make_uint2(kr[it], vr[it]);
     }
   }
   __syncthreads();
