@@ -25,9 +25,10 @@ value: position updates per second with positions already resident in HBM
 Every step also appends its emitted meetings to the memtable (two directed
   keys each, as the reference's GPU step does); the JSON's "flush" times one
   flush of everything gathered over the run into 100 CTFs.
-e2e: the same metric through the public C ABI with host input: every step
-  copies that step's positions from pinned host memory (stc_step) and drains
-  the emitted meetings back to the host (stc_drain_meetings); wall clock.
+e2e: the same metric through the public C ABI with host input: windows of
+  10 steps (stc_step_window), every step's positions copied from pinned host
+  memory (the next step's while the current one runs) and its emitted
+  meetings drained back to the host after it; wall clock.
 queries_under_ingest: K more steps (host input) while a serving thread answers
   a Poisson query stream (default 20,000/s; 60% object, 40% box queries) over
   the flushed block by continuous batching; queries return match counts, as
@@ -159,6 +160,9 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+E2E_WINDOW = 10  # steps per stc_step_window call of the end-to-end run
+
+
 class HostSteps:
     """Host position steps first..first+len-1, indexed by step number."""
 
@@ -202,10 +206,15 @@ def run_gpu(args, w, rank, local):
                  "written_gb_s": 16.0 * N * (W + K) / (gen_ms / 1e3) / 1e9}
     cfg = make_cfg(w, device=local, step_slices=args.step_slices)
     pipe = Pipeline(cfg, mbr, dev[0].cpu().numpy())
-    # warm-up steps (device-resident input)
-    for t in range(W):
-        pipe.step_device(dev[t].data_ptr(), t)
+    # warm-up steps (device-resident input), as one window: it also captures
+    # the step graphs of both input buffers that the end-to-end windows replay
+    if W >= 2:
+        pipe.step_window((dev.data_ptr(), W), 0)
         pipe.drain()
+    else:
+        for t in range(W):
+            pipe.step_device(dev[t].data_ptr(), t)
+            pipe.drain()
     stats = []
     barrier(args)
     torch.cuda.synchronize()
@@ -219,20 +228,26 @@ def run_gpu(args, w, rank, local):
     wall_dev = time.perf_counter() - t0
     barrier(args)
     dev_ms = sum(s.step_ms for s in stats)
-    # end to end: host positions in, meetings out, through the C ABI; the
-    # meetings land in a reused page-locked buffer, as a server would keep one
+    # end to end: host positions in, meetings out, through the C ABI, in
+    # windows of up to E2E_WINDOW steps (stc_step_window: each step's
+    # positions copied from page-locked host memory while the step before
+    # runs, its meetings drained after it); the meetings land in a reused
+    # page-locked buffer, as a server would keep one
     from stcdb_gb300.pipeline import MEETING_DTYPE
-    mbuf = torch.empty(8 * N * MEETING_DTYPE.itemsize // 10, dtype=torch.uint8, pin_memory=True)
+    per_step = max(max(s.emitted for s in stats), 1)
+    win = min(K, E2E_WINDOW)
+    cap = max(int(per_step * win * 1.5) + 4096, 8 * N // 10)
+    mbuf = torch.empty(cap * MEETING_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
     mnp = mbuf.numpy().view(MEETING_DTYPE)
     e2e_stats = []
     d2h = 0
     barrier(args)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    for t in range(W + K, W + 2 * K):
-        pipe.step(hnp[t], t)
-        m = pipe.drain(mnp)
-        d2h += m.nbytes + 128
+    for c0 in range(0, K, win):
+        n = min(win, K - c0)
+        m = pipe.step_window(hnp.arr[c0:c0 + n], W + K + c0, out=mnp)
+        d2h += m.nbytes + 128 * n
         e2e_stats.append(pipe.stats())
     torch.cuda.synchronize()
     wall_e2e = time.perf_counter() - t1

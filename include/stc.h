@@ -103,7 +103,10 @@ typedef struct stc_config {
   uint32_t job_chunk;            /* 32x32 pair tiles a warp takes at a time; 0 = 8, at most 64 */
   uint32_t refine_blocks_per_sm; /* pair-test blocks launched per SM; 0 = 8, at most 32 */
   uint32_t hits_blocks_per_sm;   /* table-update blocks launched per SM; 0 = 16, at most 64 */
-  uint32_t reserved;             /* 0 */
+  uint32_t window_graphs;        /* stc_step_window replays each step from a captured CUDA graph:
+                                    0 = when num_objects <= 2^21 (where per-kernel launch costs
+                                    show; a replayed graph ran a 10M-object step 10% slower than
+                                    direct launches), 1 = always, 2 = never */
 } stc_config;
 
 /* Replay quadtree splits/merges on one device thread only (tests compare it
@@ -189,11 +192,13 @@ stc_status stc_autotune(const stc_config *cfg, const double mbr[4], const double
 
 /* Processes a window of `steps` consecutive steps t0, t0 + 1, ...: xy holds
  * steps x num_objects (lon, lat) f64 pairs, layout [step][oid], in host
- * memory (on_device 0) or device memory (on_device 1). The step runs as a
- * CUDA graph captured once and replayed (captured again after a flush or a
- * change of the slice count), so a step costs one launch instead of one per
- * kernel; results equal those of stc_step called step by step, flushes
- * included (each step's state is still read back for the flush rule). When
+ * memory (on_device 0) or device memory (on_device 1). Each step's positions
+ * are copied in while the step before runs. The step runs as a CUDA graph
+ * captured once and replayed (stc_config.window_graphs; captured again after
+ * a flush or a change of the slice count), so a step costs one launch instead
+ * of one per kernel; results equal those of stc_step called step by step,
+ * flushes included (each step's state is still read back for the flush
+ * rule). When
  * out is given, each step's meetings are drained into out[*n_out..cap) and
  * *n_out counts them; STC_ERR_CAPACITY when they do not fit. Phase times of
  * the window's steps are not recorded (stc_stats.step_ms is). */

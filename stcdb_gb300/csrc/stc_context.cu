@@ -68,9 +68,14 @@ struct stc_ctx {
   // the step captured as a CUDA graph, replayed by stc_step_window; it holds
   // the pipeline's and the memtable's arguments by value, so anything that
   // changes them (a flush, the slice count) invalidates it
-  cudaGraphExec_t graph = nullptr;
-  bool graph_valid = false;
+  // one graph per input buffer: a window with host input fills the other
+  // buffer (copy stream) while a step runs
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  bool graph_valid[2] = {false, false};
   uint32_t graph_kernels = 0;
+  double2 *xy_alt = nullptr;     // second input buffer of a window (allocated on first use)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_ev[2] = {nullptr, nullptr};
   std::vector<void *> allocs;
   stc_stats stats;
   uint32_t last_t = 0;
@@ -165,7 +170,11 @@ static void destroy_all(stc_ctx *c) {
   c->allocs.clear();
   if (c->st_host) cudaFreeHost(c->st_host);
   if (c->t_pinned) cudaFreeHost(c->t_pinned);
-  if (c->graph) cudaGraphExecDestroy(c->graph);
+  for (int i = 0; i < 2; i++) {
+    if (c->graph[i]) cudaGraphExecDestroy(c->graph[i]);
+    if (c->copy_ev[i]) cudaEventDestroy(c->copy_ev[i]);
+  }
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   for (int i = 0; i < 2; i++) {
     if (c->drain_stage[i]) cudaFreeHost(c->drain_stage[i]);
     if (c->drain_ev[i]) cudaEventDestroy(c->drain_ev[i]);
@@ -445,7 +454,7 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
 }
 
 static stc_status flush_now(stc_ctx *c, uint32_t t) {
-  c->graph_valid = false;  // the memtable's arguments change
+  c->graph_valid[0] = c->graph_valid[1] = false;  // the memtable's arguments change
   cudaEventRecord(c->ev[PH_FLUSH0], c->stream);
   unsigned long long launches0 = tl_launches;
   std::string err;
@@ -521,16 +530,16 @@ static void issue_step(stc_ctx *c, bool events) {
   if (schema) cudaStreamWaitEvent(s, c->join_ev, 0);
 }
 
-// Captures the step (positions in xy_own) as a CUDA graph. Only this
-// thread's work on the context's stream is captured: a serving thread's
-// queries on other streams go on meanwhile.
-static stc_status capture_step(stc_ctx *c) {
-  if (c->graph) {
-    cudaGraphExecDestroy(c->graph);
-    c->graph = nullptr;
+// Captures the step with positions in input buffer b (xy_own, xy_alt) as a
+// CUDA graph. Only this thread's work on the context's streams is captured:
+// a serving thread's queries on other streams go on meanwhile.
+static stc_status capture_step(stc_ctx *c, int b) {
+  if (c->graph[b]) {
+    cudaGraphExecDestroy(c->graph[b]);
+    c->graph[b] = nullptr;
   }
-  c->graph_valid = false;
-  c->p.xy = c->xy_own;
+  c->graph_valid[b] = false;
+  c->p.xy = b ? c->xy_alt : c->xy_own;
   const unsigned long long l0 = tl_launches;
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
@@ -538,30 +547,30 @@ static stc_status capture_step(stc_ctx *c) {
     issue_step(c, false);
     e = cudaStreamEndCapture(c->stream, &g);
   }
-  if (e == cudaSuccess) e = cudaGraphInstantiate(&c->graph, g, 0);
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&c->graph[b], g, 0);
   if (g) cudaGraphDestroy(g);
   c->graph_kernels = (uint32_t)(tl_launches - l0);
   tl_launches = l0;  // counted when replayed
   if (e != cudaSuccess) {
-    c->graph = nullptr;
+    c->graph[b] = nullptr;
     return cuda_fail(c, e, "capturing the step graph");
   }
-  c->graph_valid = true;
+  c->graph_valid[b] = true;
   return STC_OK;
 }
 
-static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copied, bool graph = false) {
+static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copied, bool graph = false, int gb = 0) {
   PipeDev &p = c->p;
   cudaStream_t s = c->stream;
   p.xy = xy;
   *c->t_pinned = t;  // the previous step has been waited for: nothing reads it now
   unsigned long long launches0 = tl_launches;
   if (graph) {
-    if (!c->graph_valid) {
-      stc_status gs = capture_step(c);
+    if (!c->graph_valid[gb]) {
+      stc_status gs = capture_step(c, gb);
       if (gs != STC_OK) return gs;
     }
-    cudaError_t e = cudaGraphLaunch(c->graph, s);
+    cudaError_t e = cudaGraphLaunch(c->graph[gb], s);
     if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window");
     tl_launches += c->graph_kernels;
   } else {
@@ -644,13 +653,36 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   cudaSetDevice(c->device);
   const size_t step_bytes = (size_t)c->p.N * sizeof(double2);
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  // Two input buffers: while step i runs from one, the copy stream fills the
+  // other with step i + 1 (that buffer was last read by step i - 1, whose
+  // state has been read back, so it is done with it).
+  if (steps && (!c->xy_alt || !c->copy_stream)) {
+    cudaError_t e = cudaSuccess;
+    if (!c->xy_alt) e = cudaMalloc(&c->xy_alt, step_bytes);
+    if (e == cudaSuccess && !c->copy_stream) e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+    for (int b = 0; b < 2 && e == cudaSuccess; b++)
+      if (!c->copy_ev[b]) e = cudaEventCreateWithFlags(&c->copy_ev[b], cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window buffers");
+    c->allocs.push_back(c->xy_alt);
+  }
+  double2 *const buf[2] = {c->xy_own, c->xy_alt};
+  const bool graphs = c->cfg.window_graphs == 1 || (c->cfg.window_graphs == 0 && c->p.N <= (1u << 21));
+  auto fetch = [&](uint32_t i) -> cudaError_t {
+    cudaError_t e = copy_in_pieces(buf[i & 1], (const uint8_t *)xy + (size_t)i * step_bytes, step_bytes, kind,
+                                   c->copy_stream);
+    return e == cudaSuccess ? cudaEventRecord(c->copy_ev[i & 1], c->copy_stream) : e;
+  };
   size_t n = 0;
+  if (steps) {
+    cudaError_t e = fetch(0);
+    if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window copy-in");
+  }
   for (uint32_t i = 0; i < steps; i++) {
     cudaEventRecord(c->ev[PH_START], c->stream);
-    cudaError_t e = copy_in_pieces(c->xy_own, (const uint8_t *)xy + (size_t)i * step_bytes, step_bytes, kind,
-                                   c->stream);
+    cudaError_t e = cudaStreamWaitEvent(c->stream, c->copy_ev[i & 1], 0);
+    if (e == cudaSuccess && i + 1 < steps) e = fetch(i + 1);
     if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window copy-in");
-    stc_status rs = run_step(c, c->xy_own, t0 + i, true, true);
+    stc_status rs = run_step(c, buf[i & 1], t0 + i, true, graphs, (int)(i & 1));
     if (rs != STC_OK) return rs;
     if (out) {
       size_t k = 0;
@@ -661,6 +693,7 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
       if (c->st_host->emit_count) return fail(c, STC_ERR_CAPACITY, "stc_step_window: the output buffer is full");
     }
   }
+  if (steps) cudaStreamSynchronize(c->copy_stream);
   return STC_OK;
 }
 
@@ -896,7 +929,7 @@ extern "C" stc_status stc_set_step_slices(stc_ctx *c, uint32_t slices) {
   if (!c) return STC_ERR_INVALID_ARG;
   c->cfg.step_slices = slices;
   c->p.slices = std::min<uint32_t>(std::max<uint32_t>(slices, 1u), 64u);
-  c->graph_valid = false;
+  c->graph_valid[0] = c->graph_valid[1] = false;
   return STC_OK;
 }
 
@@ -926,7 +959,7 @@ extern "C" stc_status stc_load_ctb(stc_ctx *c, uint32_t index, const char *dir, 
   if (!c->lsm_on) return fail(c, STC_ERR_INVALID_ARG, "stc_load_ctb: the memtable is off (kv_restriction 0)");
   if (c->failed) return STC_ERR_STATE;
   cudaSetDevice(c->device);
-  c->graph_valid = false;
+  c->graph_valid[0] = c->graph_valid[1] = false;
   std::string err;
   stc_status st = lsm_load_block(c->lsm, c->lsmh, index, dir, prefix, c->stream, err);
   if (st != STC_OK) c->err = "stc_load_ctb: " + err;

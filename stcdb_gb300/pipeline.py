@@ -57,7 +57,7 @@ class _Config(ctypes.Structure):
         ("job_chunk", ctypes.c_uint32),
         ("refine_blocks_per_sm", ctypes.c_uint32),
         ("hits_blocks_per_sm", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("window_graphs", ctypes.c_uint32),
     ]
 
 
@@ -216,6 +216,7 @@ class StcConfig:
     job_chunk: int = 0        # refinement launch shape (results do not depend on it); 0 = 8
     refine_blocks_per_sm: int = 0  # 0 = 8
     hits_blocks_per_sm: int = 0    # 0 = 16
+    window_graphs: int = 0    # step_window replays a captured graph: 0 = up to 2^21 objects, 1 = always, 2 = never
 
     def resolved(self) -> "StcConfig":
         if self.num_meeting_buckets == 0:

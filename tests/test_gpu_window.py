@@ -28,7 +28,8 @@ def _blocks(p):
     return out
 
 
-def test_windows_match_plain_steps(built_cuda):
+@pytest.mark.parametrize("graphs", [1, 2])  # replayed graphs, direct launches
+def test_windows_match_plain_steps(built_cuda, graphs):
     import torch
     steps = 24
     tc = hotspot_grid(30000, n_hotspots=30, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=11)
@@ -48,7 +49,8 @@ def test_windows_match_plain_steps(built_cuda):
     finally:
         plain.close()
 
-    win = Pipeline(cfg, mbr, tr[0])
+    from dataclasses import replace
+    win = Pipeline(replace(cfg, window_graphs=graphs), mbr, tr[0])
     dev = torch.from_numpy(tr).cuda()
     try:
         got_win = []
