@@ -64,8 +64,11 @@ METRIC = "pos-updates/s at 10M objs (bit-exact meetings); query p50/p99 under in
 UNIT = "pos-updates/s"
 
 WORKLOADS = {
+    # launch shape chosen by stc_autotune on 8 steps of this workload (4
+    # pair-test and 32 table-update blocks per SM: 15.12 -> 14.80 ms a step);
+    # it does not change results
     "uniform-10M": dict(objects=10_000_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
-                        buckets=1 << 28, kv_restriction=1 << 27),
+                        buckets=1 << 28, kv_restriction=1 << 27, refine_bps=4, hits_bps=32),
     "hotspot-1M": dict(objects=1_000_000, hot=1000, reach=10.0, min_meet=5, grid_capacity=200, amplify=8.0,
                        buckets=1 << 28, kv_restriction=1 << 27),
     "uniform-3M": dict(objects=3_000_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
@@ -94,7 +97,8 @@ def make_cfg(w, device=0, step_slices=0):
     b = w.get("buckets") or w["buckets_per_object"] * w["objects"]
     return StcConfig(num_objects=w["objects"], reach_distance=w["reach"], min_meet_time=w["min_meet"],
                      grid_capacity=w["grid_capacity"], grid_amplify=w["amplify"], num_meeting_buckets=b,
-                     device=device, kv_restriction=w["kv_restriction"], step_slices=step_slices)
+                     device=device, kv_restriction=w["kv_restriction"], step_slices=step_slices,
+                     refine_blocks_per_sm=w.get("refine_bps", 0), hits_blocks_per_sm=w.get("hits_bps", 0))
 
 
 class ClockSampler:
@@ -608,6 +612,8 @@ def main():
                     "street_grid": "200x200 over 40 km, jitter 20 m", "speed_mps": [1, 15],
                     "hotspots": w["hot"], "reach_m": w["reach"], "min_meet_steps": w["min_meet"],
                     "leaf_capacity": w["grid_capacity"], "grid_amplify": w["amplify"],
+                    "launch_shape": {"refine_blocks_per_sm": w.get("refine_bps", 8),
+                                     "hits_blocks_per_sm": w.get("hits_bps", 16)},
                     "meeting_buckets": make_cfg(w).resolved().num_meeting_buckets,
                     "memtable": f"on, flush past {w['kv_restriction']} directed keys, 100 CTFs",
                     "l2": "inputs and table larger than L2; no flush", "parallelism": f"replicas x{ws}"}
