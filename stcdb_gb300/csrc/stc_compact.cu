@@ -332,7 +332,7 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
   const size_t hw = radix_hist_words(W);
   C.hist = sc.get<uint32_t>(hw);
   C.scan = sc.get<uint32_t>(scan_tmp_words(hw));
-  C.n_dev = sc.get<unsigned long long>(4);
+  C.n_dev = sc.get<unsigned long long>(6);
   C.cnt = sc.get<uint32_t>(N);
   C.sid = sc.get<uint16_t>(N);
   C.mid_lo = sc.get<uint32_t>(N);

@@ -381,7 +381,7 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
     size_t hw = radix_hist_words(w);
     ok = dalloc(c, &L.rec, L.cap) && dalloc(c, &L.box, L.cap) && dalloc(c, &L.brec, L.cap) &&
          dalloc(c, &L.bbox, L.cap) && dalloc(c, &L.over, L.cap) && dalloc(c, &L.hist, hw) &&
-         dalloc(c, &L.scan, scan_tmp_words(hw)) && dalloc(c, &L.n_dev, 4) && dalloc(c, &L.cnt, n) &&
+         dalloc(c, &L.scan, scan_tmp_words(hw)) && dalloc(c, &L.n_dev, 6) && dalloc(c, &L.cnt, n) &&
          dalloc(c, &L.obox, n) && dalloc(c, &L.sid, n) && dalloc(c, &L.bsid, n) && dalloc(c, &L.mid_lo, n) &&
          dalloc(c, &L.mid_hi, n) && dalloc(c, &L.ctf_cap, ctf_count) && dalloc(c, &L.ctf_first, ctf_count + 1) &&
          dalloc(c, &L.ctfs, ctf_count) && dalloc(c, &L.lim_box, ctf_count) && dalloc(c, &L.lim_time, ctf_count) &&

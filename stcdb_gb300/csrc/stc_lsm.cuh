@@ -37,7 +37,7 @@ struct LsmDev {
   uint8_t *over;                   // per memtable key: oversize at partition time
   uint32_t *sk[7];                 // sort scratch, max(cap, N) words each
   uint32_t *hist, *scan;           // radix-sort histograms and scan blocks
-  unsigned long long *n_dev;       // [4] item counts read by the sorts
+  unsigned long long *n_dev;       // [6] item counts read by the sorts; [4] the index's largest end offset
   uint32_t *cnt;                   // per object: keys (same_pid_count)
   uint4 *obox;                     // per object: low0, low1, high0, high1 (float_to_uint)
   uint16_t *sid;                   // per object: working sid

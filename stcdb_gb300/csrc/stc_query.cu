@@ -385,8 +385,11 @@ __device__ __forceinline__ void index_file_exact(unsigned long long vm, const st
 
 __global__ void k_index_cells(const uint8_t *keys, const stc_ctf *ctfs, uint32_t F, const uint32_t *cbase,
                               const uint4 *ixg, const double2 *ixs, const float4 *ixf, unsigned long long total,
-                              uint32_t *cells, uint32_t *pos, uint32_t *endo) {
+                              uint32_t *cells, uint32_t *pos, uint32_t *endo, unsigned long long *max_end) {
   __shared__ unsigned long long s_first[MAX_CTF + 1];
+  __shared__ uint32_t s_max;
+  if (threadIdx.x == 0) s_max = 0;
+  uint32_t my_max = 0;
   for (uint32_t c = threadIdx.x; c < F; c += blockDim.x) s_first[c] = ctfs[c].first_key;
   __syncthreads();
   for (unsigned long long kid = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; kid < total;
@@ -413,7 +416,27 @@ __global__ void k_index_cells(const uint8_t *keys, const stc_ctf *ctfs, uint32_t
     cells[kid] = cbase[lo] + cell;
     pos[kid] = (uint32_t)kid;
     endo[kid] = min(k.end, 65535u);
+    my_max = max(my_max, min(k.end, 65535u));
   }
+  __syncthreads();
+  atomicMax(&s_max, my_max);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_max) atomicMax(max_end, (unsigned long long)s_max);
+}
+
+// Sort keys of the one-pass index order: cell above the end offset.
+__global__ void k_index_keys(const uint32_t *cells, const uint32_t *endo, uint32_t eb, unsigned long long n,
+                             uint32_t *keys) {
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x)
+    keys[i] = (cells[i] << eb) | endo[i];
+}
+
+__global__ void k_index_ends(const uint32_t *sorted, uint32_t eb, unsigned long long n, uint16_t *pend) {
+  const uint32_t mask = (1u << eb) - 1u;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x)
+    pend[i] = (uint16_t)(sorted[i] & mask);
 }
 
 __global__ void k_gather_cells(const uint32_t *src, const uint32_t *idx, uint32_t *dst, unsigned long long n) {
@@ -428,14 +451,16 @@ __global__ void k_gather_ends(const uint32_t *endo, const uint32_t *perm, uint16
     pend[i] = (uint16_t)endo[perm[i]];
 }
 
-// cstart[k] = first position of the sorted cell ids holding an id >= k.
-__global__ void k_cell_starts(const uint32_t *sorted, unsigned long long total, uint32_t ncells, uint32_t *cstart) {
+// cstart[k] = first position of the sorted cell ids (sorted >> shift)
+// holding an id >= k.
+__global__ void k_cell_starts(const uint32_t *sorted, uint32_t shift, unsigned long long total, uint32_t ncells,
+                              uint32_t *cstart) {
   for (unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; k <= ncells;
        k += (unsigned long long)gridDim.x * blockDim.x) {
     unsigned long long lo = 0, hi = total;
     while (lo < hi) {
       unsigned long long mid = (lo + hi) >> 1;
-      if (sorted[mid] < k) lo = mid + 1;
+      if ((sorted[mid] >> shift) < k) lo = mid + 1;
       else hi = mid;
     }
     cstart[k] = (uint32_t)lo;
@@ -808,19 +833,39 @@ cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
   if (e == cudaSuccess) e = cudaMalloc(&B.pend, std::max<unsigned long long>(total, 1) * sizeof(uint16_t));
   if (e != cudaSuccess) return e;
   uint32_t *const *sk = L.sk;
+  uint32_t shift = 0;  // of the cell ids in the sorted keys (sk[2])
   if (total) {
     int bits = 1;
     while (bits < 32 && ((unsigned long long)ncells >> bits)) bits++;
-    // keys by (cell, end offset): stable sorts by end, then by cell
+    // keys by (cell, end offset)
     STC_KL k_set_one<<<1, 1, 0, s>>>(L.n_dev + 3, total);
+    e = cudaMemsetAsync(L.n_dev + 4, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
     STC_KL k_index_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(B.keys, B.d_ctfs, F, B.cbase, B.ixg, B.ixs, B.ixf, total,
-                                                         sk[0], sk[1], sk[6]);  // tables copied above on this stream
-    radix_sort_u32(sk[6], sk[1], sk[2], sk[3], sk[4], sk[5], L.n_dev + 3, (size_t)total, 16, L.hist, L.scan, s);
-    STC_KL k_gather_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[0], sk[3], sk[4], total);
-    radix_sort_u32(sk[4], sk[3], sk[2], B.perm, sk[0], sk[5], L.n_dev + 3, (size_t)total, bits, L.hist, L.scan, s);
-    STC_KL k_gather_ends<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[6], B.perm, B.pend, total);
+                                                         sk[0], sk[1], sk[6], L.n_dev + 4);  // tables copied above
+    unsigned long long max_end = 65535;
+    e = cudaMemcpyAsync(&max_end, L.n_dev + 4, sizeof(max_end), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    int eb = 1;
+    while (eb < 16 && (max_end >> eb)) eb++;
+    if (bits + eb <= 32) {
+      // one sort of (cell << eb | end offset); the end offsets are the sorted keys' low bits
+      STC_KL k_index_keys<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[0], sk[6], (uint32_t)eb, total, sk[4]);
+      radix_sort_u32(sk[4], sk[1], sk[2], B.perm, sk[0], sk[5], L.n_dev + 3, (size_t)total, bits + eb, L.hist,
+                     L.scan, s);
+      STC_KL k_index_ends<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[2], (uint32_t)eb, total, B.pend);
+      shift = (uint32_t)eb;
+    } else {
+      // stable sorts by end, then by cell
+      radix_sort_u32(sk[6], sk[1], sk[2], sk[3], sk[4], sk[5], L.n_dev + 3, (size_t)total, 16, L.hist, L.scan, s);
+      STC_KL k_gather_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[0], sk[3], sk[4], total);
+      radix_sort_u32(sk[4], sk[3], sk[2], B.perm, sk[0], sk[5], L.n_dev + 3, (size_t)total, bits, L.hist, L.scan,
+                     s);
+      STC_KL k_gather_ends<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[6], B.perm, B.pend, total);
+    }
   }
-  STC_KL k_cell_starts<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[2], total, ncells, B.cstart);
+  STC_KL k_cell_starts<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[2], shift, total, ncells, B.cstart);
   e = cudaStreamSynchronize(s);  // the copies of cbase, ixg and ixs read this stack frame
   return e == cudaSuccess ? cudaGetLastError() : e;
 }
