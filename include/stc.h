@@ -385,7 +385,8 @@ stc_status stc_server_submit(stc_server *srv, const stc_query *queries, size_t n
 stc_status stc_server_poll(stc_server *srv, stc_answer *out, size_t cap, stc_contact *contacts,
                            size_t contacts_cap, size_t *n, int wait_ms);
 stc_status stc_server_get_stats(const stc_server *srv, stc_server_stats *out);
-/* Answers everything queued, stops the thread and frees the server. */
+/* Answers everything queued, stops the thread and frees the server. A
+ * server must be stopped before its context is destroyed. */
 stc_status stc_server_stop(stc_server *srv);
 
 /* ---- Block files ---------------------------------------------------------

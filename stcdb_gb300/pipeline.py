@@ -477,7 +477,11 @@ class Pipeline:
 
     def server(self, max_batch: int = 0, result_cap: int = 0, hbm_budget: int = 0) -> "Server":
         """A request loop answering queries by continuous batching (stc_server_start)."""
-        return Server(self, max_batch, result_cap, hbm_budget)
+        srv = Server(self, max_batch, result_cap, hbm_budget)
+        if not hasattr(self, "_servers"):
+            self._servers = []
+        self._servers.append(srv)
+        return srv
 
     def checkpoint(self, path: str) -> None:
         """Writes the context's step-to-step state to one file (stc_checkpoint)."""
@@ -518,6 +522,8 @@ class Pipeline:
         return self.query_batch(q)[0]
 
     def close(self):
+        for srv in list(getattr(self, "_servers", [])):
+            srv.stop()  # a server must not outlive its context
         if getattr(self, "_h", None):
             self._lib.stc_destroy(self._h)
             self._h = None
@@ -596,4 +602,7 @@ class Server:
         if self._h:
             self._lib.stc_server_stop(self._h)
             self._h = None
+            servers = getattr(self._pipe, "_servers", [])
+            if self in servers:
+                servers.remove(self)
 
