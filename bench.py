@@ -318,6 +318,7 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
     rng = np.random.default_rng(12345)
     rate = float(args.query_rate)
     answers = []
+    lags = []  # submit time - arrival time per query (the submitting thread's delay)
     cur_t = [t0 - 1]
     done = threading.Event()
     errors = []
@@ -342,6 +343,7 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
             try:
                 for q, t_arr in zip(qs, arrivals):
                     srv.submit(q[None], arrival=t_arr)
+                    lags.append(time.perf_counter() - t_arr)
             except Exception as e:  # noqa: BLE001 - reported in the JSON line
                 errors.append(str(e))
                 return
@@ -378,12 +380,24 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
         return {"error": f"{int((ans['status'] != 0).sum())} queries failed"}
     lat_ms = ans["latency_ms"] if len(ans) else np.zeros(0)
     sizes = np.bincount(ans["batch"]) if len(ans) else np.zeros(0)
+    # where the slowest answers come from: their batch (size, latency spread:
+    # a small minimum means its queries waited before the batch started)
+    worst = {}
+    if len(ans):
+        wb = int(ans["batch"][int(np.argmax(lat_ms))])
+        wl = lat_ms[ans["batch"] == wb]
+        worst = {"batch_queries": int(len(wl)), "min_latency_ms": float(wl.min()),
+                 "max_latency_ms": float(wl.max())}
+    lag_ms = np.asarray(lags) * 1e3
     return {"rate_target_per_s": rate, "answered": len(ans), "qps": len(ans) / wall,
             "p50_ms": float(np.percentile(lat_ms, 50)) if len(ans) else None,
             "p99_ms": float(np.percentile(lat_ms, 99)) if len(ans) else None,
             "p999_ms": float(np.percentile(lat_ms, 99.9)) if len(ans) else None,
             "max_ms": float(lat_ms.max()) if len(ans) else None,
             "mean_batch": float(sizes[sizes > 0].mean()) if len(ans) else 0.0, "batches": int(sst.batches),
+            "slowest_batch": worst,
+            "submit_lag_ms": {"p99": float(np.percentile(lag_ms, 99)) if len(lag_ms) else None,
+                              "max": float(lag_ms.max()) if len(lag_ms) else None},
             "contacts_per_query": float(ans["count"].mean()) if len(ans) else 0.0,
             "server": {"loop": "stc_server (library thread, continuous batching)", "max_batch": 4096,
                        "hbm_budget_bytes": 64 << 20, "max_batch_queries": int(sst.max_batch_queries),
