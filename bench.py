@@ -319,6 +319,7 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
     rate = float(args.query_rate)
     answers = []
     lags = []  # submit time - arrival time per query (the submitting thread's delay)
+    arrived = {}  # ticket -> arrival time
     cur_t = [t0 - 1]
     done = threading.Event()
     errors = []
@@ -342,7 +343,7 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
             qs["kind"] |= QUERY_COUNT_ONLY
             try:
                 for q, t_arr in zip(qs, arrivals):
-                    srv.submit(q[None], arrival=t_arr)
+                    arrived[srv.submit(q[None], arrival=t_arr)] = t_arr
                     lags.append(time.perf_counter() - t_arr)
             except Exception as e:  # noqa: BLE001 - reported in the JSON line
                 errors.append(str(e))
@@ -382,12 +383,23 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
     sizes = np.bincount(ans["batch"]) if len(ans) else np.zeros(0)
     # where the slowest answers come from: their batch (size, latency spread:
     # a small minimum means its queries waited before the batch started)
+    # and the batch before it: its completion time (arrival + latency, one
+    # clock) and its own latency spread; a batch runs at most its minimum
+    # latency, so a long gap with a short run means the queries queued behind
+    # the previous batch
     worst = {}
     if len(ans):
         wb = int(ans["batch"][int(np.argmax(lat_ms))])
         wl = lat_ms[ans["batch"] == wb]
         worst = {"batch_queries": int(len(wl)), "min_latency_ms": float(wl.min()),
                  "max_latency_ms": float(wl.max())}
+        done_at = np.array([arrived.get(int(tk), np.nan) for tk in ans["ticket"]]) + lat_ms * 1e-3
+        prev = ans["batch"] == wb - 1
+        if prev.any():
+            worst["since_previous_batch_ms"] = float((np.nanmax(done_at[ans["batch"] == wb]) -
+                                                      np.nanmax(done_at[prev])) * 1e3)
+            worst["previous_batch_queries"] = int(prev.sum())
+            worst["previous_min_latency_ms"] = float(lat_ms[prev].min())
     lag_ms = np.asarray(lags) * 1e3
     return {"rate_target_per_s": rate, "answered": len(ans), "qps": len(ans) / wall,
             "p50_ms": float(np.percentile(lat_ms, 50)) if len(ans) else None,

@@ -190,6 +190,15 @@ __global__ void k_make_sid(LsmDev L, const uint32_t *oids, const uint32_t *jv, u
 // in two words: the low target bits, duration and end; then the over flag,
 // the object's rank in (sid, pid) order (its pid for an oversize key, whose
 // sid counts as 0) and the high target bits.
+__device__ __forceinline__ uint32_t low_word(const uint4 &r, const WordSpec &ws) {
+  return r.w | (r.z << ws.a) | (r.y << ws.b);  // a = end bits, b = end + duration bits < 32
+}
+__device__ __forceinline__ uint32_t high_word(const uint4 &r, bool over, const uint32_t *rank, const WordSpec &ws) {
+  // a = high target bits, b = low target bits, c = pid bits
+  const uint32_t major = over ? r.x : rank[r.x];
+  return (over ? 1u << (ws.c + ws.a) : 0u) | (major << ws.a) | (ws.a ? r.y >> ws.b : 0u);
+}
+
 __global__ void k_lsm_word(LsmDev L, unsigned long long K, const uint32_t *perm, uint32_t *keys, uint32_t *vals,
                            WordSpec ws, const uint32_t *rank) {
   for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < K;
@@ -206,16 +215,26 @@ __global__ void k_lsm_word(LsmDev L, unsigned long long K, const uint32_t *perm,
       case W_SID_PID: w = r.x | ((L.over[src] ? 0u : (uint32_t)L.sid[r.x]) << ws.a); break;
       case W_PID: w = r.x; break;
       case W_SID: w = L.over[src] ? 0u : (uint32_t)L.sid[r.x]; break;
-      case W_LOW: w = r.w | (r.z << ws.a) | (r.y << ws.b); break;  // a = end bits, b = end + duration bits < 32
-      case W_HIGH: {  // a = high target bits, b = low target bits, c = pid bits
-        const bool over = L.over[src] != 0;
-        const uint32_t major = over ? r.x : rank[r.x];
-        w = (over ? 1u << (ws.c + ws.a) : 0u) | (major << ws.a) | (ws.a ? r.y >> ws.b : 0u);
-        break;
-      }
+      case W_LOW: w = low_word(r, ws); break;
+      case W_HIGH: w = high_word(r, L.over[src] != 0, rank, ws); break;
       default: w = L.over[src]; break;
     }
     keys[i] = w;
+  }
+}
+
+// First pass of the two-word order, in memtable order: the low word as the
+// sort key (value = the key's index) and the high word into `hi`, so that
+// the second pass gathers one word a key instead of its record, over flag
+// and object rank.
+__global__ void k_lsm_low_high(LsmDev L, unsigned long long K, uint32_t *keys, uint32_t *vals, uint32_t *hi,
+                               WordSpec lo, WordSpec hs, const uint32_t *rank) {
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < K;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const uint4 r = L.rec[i];
+    vals[i] = (uint32_t)i;
+    keys[i] = low_word(r, lo);
+    hi[i] = high_word(r, L.over[i] != 0, rank, hs);
   }
 }
 
@@ -601,12 +620,23 @@ void lsmk::sort_keys(const LsmDev &L, unsigned long long K, uint32_t N, uint32_t
     words[nw++] = {W_OVER, 0u, 0u, 0u, 1u};
   }
   const uint32_t *perm = nullptr;
-  uint32_t *vbuf[2] = {sk[1], sk[3]};
-  for (int w = 0; w < nw; w++) {
-    uint32_t *vin = vbuf[w & 1], *vout = vbuf[(w + 1) & 1];
-    STC_KL k_lsm_word<<<GRID, 256, 0, s>>>(L, K, perm, sk[0], perm ? nullptr : vin, words[w], rank);
-    sort_words(L, sk[0], perm ? perm : vin, sk[2], vout, sk[4], sk[5], 2, K, words[w].bits, s);
-    perm = vout;
+  if (rank) {
+    // the sorted records' buffer is free until the final gather: it holds
+    // the high words meanwhile
+    uint32_t *hi = reinterpret_cast<uint32_t *>(L.brec);
+    STC_KL k_lsm_low_high<<<GRID, 256, 0, s>>>(L, K, sk[0], sk[1], hi, words[0], words[1], rank);
+    sort_words(L, sk[0], sk[1], sk[2], sk[3], sk[4], sk[5], 2, K, words[0].bits, s);
+    STC_KL k_gather_u32<<<nblk(K), 256, 0, s>>>(hi, sk[3], sk[0], (uint32_t)K);
+    sort_words(L, sk[0], sk[3], sk[2], sk[1], sk[4], sk[5], 2, K, words[1].bits, s);
+    perm = sk[1];
+  } else {
+    uint32_t *vbuf[2] = {sk[1], sk[3]};
+    for (int w = 0; w < nw; w++) {
+      uint32_t *vin = vbuf[w & 1], *vout = vbuf[(w + 1) & 1];
+      STC_KL k_lsm_word<<<GRID, 256, 0, s>>>(L, K, perm, sk[0], perm ? nullptr : vin, words[w], rank);
+      sort_words(L, sk[0], perm ? perm : vin, sk[2], vout, sk[4], sk[5], 2, K, words[w].bits, s);
+      perm = vout;
+    }
   }
   STC_KL k_lsm_gather<<<GRID, 256, 0, s>>>(L, K, perm);
 }
