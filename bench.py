@@ -394,8 +394,8 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
         worst = {"batch_queries": int(len(wl)), "min_latency_ms": float(wl.min()),
                  "max_latency_ms": float(wl.max())}
         done_at = np.array([arrived.get(int(tk), np.nan) for tk in ans["ticket"]]) + lat_ms * 1e-3
-        prev = ans["batch"] == wb - 1
-        if prev.any():
+        prev = ans["batch"] == (wb - 1 if wb > 0 else wb)
+        if wb > 0 and prev.any():
             worst["since_previous_batch_ms"] = float((np.nanmax(done_at[ans["batch"] == wb]) -
                                                       np.nanmax(done_at[prev])) * 1e3)
             worst["previous_batch_queries"] = int(prev.sum())
