@@ -200,7 +200,7 @@ __device__ __forceinline__ uint32_t high_word(const uint4 &r, bool over, const u
 }
 
 __global__ void k_lsm_word(LsmDev L, unsigned long long K, const uint32_t *perm, uint32_t *keys, uint32_t *vals,
-                           WordSpec ws, const uint32_t *rank) {
+                           WordSpec ws) {
   for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < K;
        i += (unsigned long long)gridDim.x * blockDim.x) {
     uint32_t src = perm ? perm[i] : (uint32_t)i;
@@ -215,9 +215,7 @@ __global__ void k_lsm_word(LsmDev L, unsigned long long K, const uint32_t *perm,
       case W_SID_PID: w = r.x | ((L.over[src] ? 0u : (uint32_t)L.sid[r.x]) << ws.a); break;
       case W_PID: w = r.x; break;
       case W_SID: w = L.over[src] ? 0u : (uint32_t)L.sid[r.x]; break;
-      case W_LOW: w = low_word(r, ws); break;
-      case W_HIGH: w = high_word(r, L.over[src] != 0, rank, ws); break;
-      default: w = L.over[src]; break;
+      default: w = L.over[src]; break;  // W_OVER (W_LOW / W_HIGH go through k_lsm_low_high)
     }
     keys[i] = w;
   }
@@ -633,7 +631,7 @@ void lsmk::sort_keys(const LsmDev &L, unsigned long long K, uint32_t N, uint32_t
     uint32_t *vbuf[2] = {sk[1], sk[3]};
     for (int w = 0; w < nw; w++) {
       uint32_t *vin = vbuf[w & 1], *vout = vbuf[(w + 1) & 1];
-      STC_KL k_lsm_word<<<GRID, 256, 0, s>>>(L, K, perm, sk[0], perm ? nullptr : vin, words[w], rank);
+      STC_KL k_lsm_word<<<GRID, 256, 0, s>>>(L, K, perm, sk[0], perm ? nullptr : vin, words[w]);
       sort_words(L, sk[0], perm ? perm : vin, sk[2], vout, sk[4], sk[5], 2, K, words[w].bits, s);
       perm = vout;
     }

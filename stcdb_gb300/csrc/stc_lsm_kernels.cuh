@@ -73,7 +73,9 @@ __global__ void k_slab_of(const uint32_t *jv, uint32_t R, uint32_t xcap, uint32_
 __global__ void k_make_sid(LsmDev L, const uint32_t *oids, const uint32_t *jv, uint32_t z, uint32_t R,
                            uint32_t xcap, uint32_t ycap);
 __global__ void k_lsm_word(LsmDev L, unsigned long long K, const uint32_t *perm, uint32_t *keys, uint32_t *vals,
-                           WordSpec w, const uint32_t *rank);
+                           WordSpec w);
+__global__ void k_lsm_low_high(LsmDev L, unsigned long long K, uint32_t *keys, uint32_t *vals, uint32_t *hi,
+                               WordSpec lo, WordSpec hs, const uint32_t *rank);
 __global__ void k_lsm_gather(LsmDev L, unsigned long long K, const uint32_t *perm);
 
 // Bitmaps and packed keys of the sorted keys [0, total) over CTF ranges
