@@ -212,13 +212,14 @@ def run_gpu(args, w, rank, local):
     pipe = Pipeline(cfg, mbr, dev[0].cpu().numpy())
     # warm-up steps (device-resident input), as one window: it also captures
     # the step graphs of both input buffers that the end-to-end windows replay
+    checked = []  # every meeting drained from the device-resident steps, for the bit-exact check
     if W >= 2:
         pipe.step_window((dev.data_ptr(), W), 0)
-        pipe.drain()
+        checked.append(pipe.drain())
     else:
         for t in range(W):
             pipe.step_device(dev[t].data_ptr(), t)
-            pipe.drain()
+            checked.append(pipe.drain())
     stats = []
     barrier(args)
     torch.cuda.synchronize()
@@ -227,9 +228,11 @@ def run_gpu(args, w, rank, local):
         for t in range(W, W + K):
             pipe.step_device(dev[t].data_ptr(), t)
             stats.append(pipe.stats())
-            pipe.drain()
+            checked.append(pipe.drain())
         torch.cuda.synchronize()
     wall_dev = time.perf_counter() - t0
+    checked = np.concatenate([meeting_rows(m) for m in checked])
+    units = {W + i: int(s.checking_units) for i, s in enumerate(stats)}
     barrier(args)
     dev_ms = sum(s.step_ms for s in stats)
     # end to end: host positions in, meetings out, through the C ABI, in
@@ -281,7 +284,50 @@ def run_gpu(args, w, rank, local):
     pipe.close()
     return dict(stats=stats, dev_ms=dev_ms, wall_dev=wall_dev, wall_e2e=wall_e2e, e2e_stats=e2e_stats,
                 d2h=d2h, clocks=clk.summary(), flush=flush, queries=queries, trace_gen=trace_gen,
-                compaction=compaction)
+                compaction=compaction, bit_exact=bit_exact_check(args.workload, rank, checked, units, W + K))
+
+
+def meeting_rows(m):
+    """(pid_lo, pid_hi, start, end) rows of drained meetings."""
+    if not len(m):
+        return np.zeros((0, 4), np.uint32)
+    return np.stack([m["pid_lo"], m["pid_hi"], m["start"], m["end"]], 1).astype(np.uint32)
+
+
+# fixtures made by the reference's own single-threaded CPU path on the
+# workloads' first steps (tests/golden/make_golden_scale.py)
+SCALE_FIXTURES = {"uniform-10M": "scale_uniform_10m.npz", "hotspot-1M": "scale_hotspot_1m.npz"}
+
+
+def bit_exact_check(workload, rank, rows, units, steps_run):
+    """Compares the meetings the run emitted in its first steps with the
+    reference's: per step the SHA-256 of the sorted tuples, their count and
+    the checking units (known for the individually timed steps). A meeting
+    is emitted at the first step after its end, so the drained rows split
+    into steps by end + 1."""
+    import hashlib
+    name = SCALE_FIXTURES.get(workload)
+    path = os.path.join(ROOT, "tests", "golden", name) if name else None
+    if rank != 0 or not path or not os.path.exists(path):
+        return None
+    fx = np.load(path)
+    n = min(len(fx["counts"]), steps_run)
+    step_of = rows[:, 3].astype(np.int64) + 1
+    mismatched = []
+    for t in range(n):
+        r = rows[step_of == t]
+        r = r[np.lexsort((r[:, 3], r[:, 2], r[:, 1], r[:, 0]))] if len(r) else r
+        ok = len(r) == int(fx["counts"][t]) and \
+            hashlib.sha256(np.ascontiguousarray(r).astype("<u4").tobytes()).hexdigest() == str(fx["digests"][t])
+        if t in units and units[t] != int(fx["units"][t]):
+            ok = False
+        if not ok:
+            mismatched.append(t)
+    return {"bit_exact": not mismatched, "steps_compared": n, "mismatched_steps": mismatched,
+            "meetings_compared": int(np.asarray(fx["counts"][:n]).sum()), "units_compared": sorted(t for t in units if t < n),
+            "fixture": "tests/golden/" + name,
+            "reference": "the reference's own CPU path (tracing/filter.cpp, refinement.cpp, meeting.cpp), "
+                         "single thread, same seeded positions"}
 
 
 def make_queries(rng, n, N, mbr, t_now):
@@ -702,6 +748,8 @@ def main():
         "sort": sort_line(local, peak),
         "batched": None if args.no_batched else batched_line(local),
         "autotune": None if args.no_batched else tune_line(local),
+        "bit_exact": r["bit_exact"]["bit_exact"] if r["bit_exact"] else None,
+        "bit_exact_check": r["bit_exact"],
         "per_step": {"pair_tests": s_last.pair_tests, "exact_tests": s_last.exact_tests, "hits": s_last.hits,
                      "new_candidates": s_last.new_candidates, "live_meetings": s_last.taken_buckets,
                      "emitted": s_last.emitted, "border_units": s_last.border_units, "leaves": s_last.leaves,

@@ -193,15 +193,22 @@ stc_status stc_autotune(const stc_config *cfg, const double mbr[4], const double
 /* Processes a window of `steps` consecutive steps t0, t0 + 1, ...: xy holds
  * steps x num_objects (lon, lat) f64 pairs, layout [step][oid], in host
  * memory (on_device 0) or device memory (on_device 1). Each step's positions
- * are copied in while the step before runs. The step runs as a CUDA graph
- * captured once and replayed (stc_config.window_graphs; captured again after
- * a flush or a change of the slice count), so a step costs one launch instead
- * of one per kernel; results equal those of stc_step called step by step,
- * flushes included (each step's state is still read back for the flush
- * rule). When
- * out is given, each step's meetings are drained into out[*n_out..cap) and
- * *n_out counts them; STC_ERR_CAPACITY when they do not fit. Phase times of
- * the window's steps are not recorded (stc_stats.step_ms is). */
+ * are copied in while the step before runs, and the window is pipelined one
+ * step deep: step i + 1 is queued on the GPU before the host reads step i's
+ * state, so the GPU does not wait for the host between steps. The memtable
+ * append of step i + 1 is queued only after step i's flush decision (a flush
+ * runs behind the next step's core, which never touches the memtable), so
+ * results equal those of stc_step called step by step, flushes included.
+ * Small windows replay each step's core from a CUDA graph captured once
+ * (stc_config.window_graphs; captured again after a flush or a change of the
+ * slice count), so such a step costs one launch instead of one per kernel.
+ * When out is given, each step's meetings are drained into out[*n_out..cap)
+ * beside the next step and *n_out counts them. When they do not fit the call
+ * returns STC_ERR_CAPACITY (the context stays usable): at most one step
+ * beyond the one that filled out has run, stc_stats.step names the last step
+ * that ran, and the meetings that did not fit stay pending for
+ * stc_drain_meetings. Phase times of the window's steps are not recorded
+ * (stc_stats.step_ms is). */
 stc_status stc_step_window(stc_ctx *ctx, const double *xy, int on_device, uint32_t steps, uint32_t t0,
                            stc_meeting *out, size_t cap, size_t *n_out);
 
@@ -319,10 +326,13 @@ stc_status stc_query_box(stc_ctx *ctx, const double box[4], uint32_t t_start, ui
 /* A batch of queries in one device pass (the serving path: queries that
  * arrive while a batch runs form the next one). offsets[nq + 1]: the matches
  * of query i are out[offsets[i] .. offsets[i + 1]) when offsets[nq] <= cap;
- * otherwise only offsets is filled and out is left untouched. counts[nq]
- * (may be NULL): the number of matches of each query. A query whose kind
- * carries STC_QUERY_COUNT_ONLY is only counted, as the reference's searches
- * do (search_count): it writes no contacts. */
+ * otherwise only offsets and counts are meaningful and out's contents are
+ * unspecified. counts[nq] (may be NULL): the number of matches of each
+ * query. A query whose kind carries STC_QUERY_COUNT_ONLY is only counted, as
+ * the reference's searches do (search_count): it writes no contacts. Up to
+ * two batches (from different threads) run on the GPU at the same time, each
+ * on its own stream and buffers; a batch larger than 65535 / ctb_retain
+ * queries runs as several device passes. */
 #define STC_QUERY_OBJECT 0u
 #define STC_QUERY_BOX 1u
 #define STC_QUERY_COUNT_ONLY 0x100u
@@ -338,15 +348,20 @@ stc_status stc_query_batch(stc_ctx *ctx, const stc_query *queries, size_t nq, st
 
 /* ---- Serving: a request loop over stc_query_batch --------------------------
  *
- * A server owns a thread that answers submitted queries by continuous
- * batching: whatever has arrived while a batch runs forms the next batch, in
- * arrival order, admitted while the batch's device footprint stays within
- * hbm_budget: every query takes its record and counters, and a query that
- * returns contacts (no STC_QUERY_COUNT_ONLY) also reserves result_cap
- * contacts of device output. The first query of a batch is always admitted.
- * A query whose contacts exceed its reservation is answered with its count,
- * no contacts and STC_ERR_CAPACITY. The context keeps stepping meanwhile on
- * other threads (stc_query_batch may run beside stc_step). */
+ * A server owns two worker threads that answer submitted queries by
+ * continuous batching: an idle worker takes what has arrived, in arrival
+ * order, as its batch and runs it on its own query stream, so queries that
+ * arrive while a batch is on the GPU start at once beside it instead of
+ * waiting for it to end. Admission is by device footprint: every query takes
+ * its record and counters, a query that returns contacts (no
+ * STC_QUERY_COUNT_ONLY) also reserves result_cap contacts of device output,
+ * and a batch is admitted while the footprint of all batches in flight stays
+ * within hbm_budget (a batch's first query is always admitted when nothing
+ * else is in flight; otherwise it waits until memory frees). A query with
+ * more than result_cap contacts is answered with its count, no contacts and
+ * STC_ERR_CAPACITY, whatever else its batch holds. The context keeps
+ * stepping meanwhile on other threads (stc_query_batch may run beside
+ * stc_step). */
 typedef struct stc_server_config {
   uint32_t max_batch;            /* queries per batch; 0 = 4096 */
   uint32_t result_cap;           /* contacts reserved per non-counting query; 0 = 1024 */
@@ -369,6 +384,7 @@ typedef struct stc_server_stats {
   uint64_t max_batch_queries;    /* largest batch */
   uint64_t max_batch_bytes;      /* largest admitted footprint */
   uint64_t budget_cuts;          /* batches closed by the budget before max_batch */
+  uint64_t overlapped_batches;   /* batches that started while another batch was on the GPU */
 } stc_server_stats;
 
 typedef struct stc_server stc_server;
@@ -381,7 +397,9 @@ stc_status stc_server_submit(stc_server *srv, const stc_query *queries, size_t n
                              uint64_t *first_ticket);
 /* Moves up to cap answers (and their contacts, up to contacts_cap) completed
  * since the last poll into out / contacts; waits up to wait_ms for the first
- * when none is ready. */
+ * when none is ready. An answer holds at most result_cap contacts; when the
+ * first ready answer alone does not fit contacts_cap, the poll returns
+ * STC_ERR_CAPACITY with *n = 0 and the answer stays queued. */
 stc_status stc_server_poll(stc_server *srv, stc_answer *out, size_t cap, stc_contact *contacts,
                            size_t contacts_cap, size_t *n, int wait_ms);
 stc_status stc_server_get_stats(const stc_server *srv, stc_server_stats *out);
@@ -497,15 +515,19 @@ stc_status stc_sort_pairs_u32(const uint32_t *keys, const uint32_t *values, uint
  * set-up per device); make that first call before any stream capture.
  * All calls share the one array: calls that overlap on the GPU (from several
  * host threads, or launched while another is still running) race and corrupt
- * each other's results. The call returns when the sort is done.
+ * each other's results. The array's device address is kept per device for
+ * the life of the process, so a device reset (cudaDeviceReset) while the
+ * library is loaded is not supported by this call. The call returns when the
+ * sort is done.
  * No counterpart in the reference. Errors: stc_last_error(NULL). */
 #define STC_SORT_NOALLOC_MAX_PAIRS (1u << 20)
-
-/* Device time in milliseconds of the sort passes of the last successful
- * stc_sort_pairs_u32 call on this thread (scratch allocation excluded). */
-float stc_last_sort_ms(void);
 stc_status stc_sort_pairs_u32_noalloc(const uint32_t *keys, const uint32_t *values, uint32_t *keys_out,
                                       uint32_t *values_out, size_t n, uint32_t key_bits, uint32_t device);
+
+/* Device time in milliseconds of the sort passes of the last successful
+ * stc_sort_pairs_u32 call on this thread (scratch allocation excluded). Only
+ * stc_sort_pairs_u32 sets it; stc_sort_pairs_u32_noalloc leaves it as it is. */
+float stc_last_sort_ms(void);
 
 #ifdef __cplusplus
 }

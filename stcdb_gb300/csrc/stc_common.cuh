@@ -14,7 +14,6 @@
 #define STC_ORDER_SHIFT 24          // order = unit_rank << 24 | member index
 #define STC_MAX_LEAF_CAP (1u << 16)    // leaf list capacity bound (tile counts fit in 32 bits)
 #define STC_MAX_DEPTH 96            // descent / lookup depth bound
-#define STC_NUM_SMS 152
 #define STC_PROBE_LIMIT (1ULL << 16)  // longest probe walk before the table counts as full
 
 enum { NODE_INVALID = 0, NODE_BRANCH = 1, NODE_LEAF = 2 };  // index/QTree.h:43-47
@@ -197,6 +196,11 @@ namespace stc {
 
 // Kernel launches issued by this thread (counted per step in stc_stats).
 extern thread_local unsigned long long tl_launches;
+
+// Streaming multiprocessors of the current device
+// (cudaDevAttrMultiProcessorCount, looked up once per device): grid-stride
+// launches are sized in multiples of it.
+int num_sms();
 
 }  // namespace stc
 

@@ -393,12 +393,12 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
   for (const CtbBlock *b : in) {
     const unsigned long long n = b->info.oversize_kv_count;
     if (n)
-      STC_KL k_cmp_copy_over<<<GRID, 256, 0, s>>>(b->orec, b->obox, n, at, b->info.o_end_time_min - o_etm, C.rec,
+      STC_KL k_cmp_copy_over<<<lsm_grid(), 256, 0, s>>>(b->orec, b->obox, n, at, b->info.o_end_time_min - o_etm, C.rec,
                                                   C.box, C.over, C.st);
     at += n;
   }
   if (nk)
-    STC_KL k_cmp_decode<<<GRID, 256, 0, s>>>(d_ic, nc, nk, no, N, etm, o_etm, ob, C.rec, C.box, C.over, C.st);
+    STC_KL k_cmp_decode<<<lsm_grid(), 256, 0, s>>>(d_ic, nc, nk, no, N, etm, o_etm, ob, C.rec, C.box, C.over, C.st);
   // 2. STR: objects by x midpoint, x slabs by y midpoint (:843-942)
   uint32_t **sk = C.sk;
   STC_KL k_cmp_mid<<<nblk(N), 256, 0, s>>>(ob, N, sk[5], C.mid_lo, sk[0], C.st);
@@ -426,7 +426,7 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
     sort_words(C, sk[0], sk[2], sk[1], sk[5], sk[3], sk[4], 1, n_str, 32, s);
     STC_KL k_slab_of<<<nblk(n_str), 256, 0, s>>>(sk[5], n_str, xcap, S, sk[0]);
     sort_words(C, sk[0], sk[5], sk[1], sk[2], sk[3], sk[4], 1, n_str, bits_for(S - 1), s);
-    STC_KL k_make_sid<<<STC_NUM_SMS, 512, F2 * sizeof(uint32_t), s>>>(C, sk[6], sk[2], 0, n_str, xcap, ycap);
+    STC_KL k_make_sid<<<num_sms(), 512, F2 * sizeof(uint32_t), s>>>(C, sk[6], sk[2], 0, n_str, xcap, ycap);
   }
   // 3. all records by (oversize, sid, oid, target, duration, end), stable
   sort_keys(C, T, N, st.lsm_max_end, st.lsm_max_dur, bits_for(F2 + 1), s);
@@ -463,7 +463,7 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
     LsmDev O = C;
     O.end_time_min = o_etm;
     O.obitmap = B.obitmap;
-    STC_KL k_lsm_oversize<<<GRID, 256, 0, s>>>(O, slim, T);
+    STC_KL k_lsm_oversize<<<lsm_grid(), 256, 0, s>>>(O, slim, T);
   }
   std::vector<float4> lb(F2);
   std::vector<uint2> lt(F2);
@@ -539,7 +539,7 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
   if (e == cudaSuccess && slim)
     // bitmaps (:1015-1035: cells clamped to the grid on each axis) and packed
     // keys (:1048-1060: oid, target, duration, end offset, box; fields added)
-    STC_KL k_encode_keys<<<GRID, ENC_GROUP, 0, s>>>(
+    STC_KL k_encode_keys<<<lsm_grid(), ENC_GROUP, 0, s>>>(
         EncodeArgs{C.brec, C.bbox, B.d_ctfs, C.ctf_first, nullptr, B.bitmaps, B.keys, slim, slim, F2, true});
   if (e == cudaSuccess) e = build_index(C, B, s);
   if (e == cudaSuccess) e = cudaEventRecord(ev1, s);

@@ -64,7 +64,17 @@ struct stc_ctx {
   uint8_t *drain_stage[2] = {nullptr, nullptr};
   cudaEvent_t drain_ev[2] = {nullptr, nullptr};
   double2 *xy_own = nullptr;     // device copy target for host input (and every step of a window)
-  uint32_t *t_pinned = nullptr;  // page-locked time of the step being issued (step_begin copies it)
+  // page-locked times of the steps being issued, one word per input buffer
+  // (step_begin copies it): a window issues step i + 1 before step i has run
+  uint32_t *t_pinned = nullptr;
+  // pipelined windows (stc_step_window): per input buffer b, the state read
+  // back after that step's memtable append, and the step's events
+  DevState *st_slot[2] = {nullptr, nullptr};
+  cudaEvent_t st_ev[2] = {nullptr, nullptr};      // the state copy of the step in buffer b has landed
+  cudaEvent_t core_ev[2] = {nullptr, nullptr};    // end of the step's core: its input buffer is free
+  cudaEvent_t wev[2][3] = {};                     // start of the core, start and end of the append
+  cudaStream_t drain_stream = nullptr;            // meetings of a window go out here beside the next step
+  cudaEvent_t drained_ev = nullptr;
   // the step captured as a CUDA graph, replayed by stc_step_window; it holds
   // the pipeline's and the memtable's arguments by value, so anything that
   // changes them (a flush, the slice count) invalidates it
@@ -168,8 +178,18 @@ static void destroy_all(stc_ctx *c) {
   lsm_release(c->lsmh);
   for (void *v : c->allocs) cudaFree(v);
   c->allocs.clear();
+  if (c->drain_stream) cudaStreamSynchronize(c->drain_stream);
   if (c->st_host) cudaFreeHost(c->st_host);
   if (c->t_pinned) cudaFreeHost(c->t_pinned);
+  for (int i = 0; i < 2; i++) {
+    if (c->st_slot[i]) cudaFreeHost(c->st_slot[i]);
+    if (c->st_ev[i]) cudaEventDestroy(c->st_ev[i]);
+    if (c->core_ev[i]) cudaEventDestroy(c->core_ev[i]);
+    for (cudaEvent_t ev : c->wev[i])
+      if (ev) cudaEventDestroy(ev);
+  }
+  if (c->drained_ev) cudaEventDestroy(c->drained_ev);
+  if (c->drain_stream) cudaStreamDestroy(c->drain_stream);
   for (int i = 0; i < 2; i++) {
     if (c->graph[i]) cudaGraphExecDestroy(c->graph[i]);
     if (c->copy_ev[i]) cudaEventDestroy(c->copy_ev[i]);
@@ -285,7 +305,15 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
     e = cudaEventCreateWithFlags(&c->part_ev[i], cudaEventDisableTiming);
   for (int i = 0; i < PH_COUNT && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
   if (e == cudaSuccess) e = cudaMallocHost(&c->st_host, sizeof(DevState));
-  if (e == cudaSuccess) e = cudaMallocHost(&c->t_pinned, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMallocHost(&c->t_pinned, 2 * sizeof(uint32_t));
+  for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+    e = cudaMallocHost(&c->st_slot[i], sizeof(DevState));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->st_ev[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->core_ev[i]);
+    for (int j = 0; j < 3 && e == cudaSuccess; j++) e = cudaEventCreate(&c->wev[i][j]);
+  }
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->drain_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->drained_ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = schema_prepare();
   for (int i = 0; i < 2 && e == cudaSuccess; i++) {
     e = cudaMallocHost(&c->drain_stage[i], DRAIN_CHUNK);
@@ -394,13 +422,10 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
     for (int i = 0; i < 4; i++) H.map[i] = mbr[i];
     int least = 0, greatest = 0;
     cudaDeviceGetStreamPriorityRange(&least, &greatest);
-    if (ok && cudaStreamCreateWithPriority(&H.qstream, cudaStreamNonBlocking, greatest) != cudaSuccess) {
-      c->err = "query stream creation failed";
-      ok = false;
-    }
-    // query buffers now: allocating them later would wait for a step in flight
+    // query lanes (streams of the highest priority) and their buffers now:
+    // allocating them later would wait for a step in flight
     std::string qerr;
-    if (ok && lsm_query_reserve(H, 4096, ctf_count, qerr) != STC_OK) {
+    if (ok && lsm_query_reserve(H, 4096, ctf_count, greatest, qerr) != STC_OK) {
       c->err = qerr;
       ok = false;
     }
@@ -476,11 +501,14 @@ static stc_status flush_now(stc_ctx *c, uint32_t t) {
 }
 
 // The step's device work, in stream order (phase events only when not being
-// captured into a graph).
-static void issue_step(stc_ctx *c, bool events) {
+// captured into a graph). `tword` is the page-locked word holding the step's
+// time. The memtable append is part of it only when `append` is set: a
+// pipelined window issues it separately, after the flush decision of the
+// step before.
+static void issue_step(stc_ctx *c, bool events, bool append, const uint32_t *tword) {
   PipeDev &p = c->p;
   cudaStream_t s = c->stream;
-  step_begin(p, c->t_pinned, s);
+  step_begin(p, tword, s);
   if (events) cudaEventRecord(c->ev[PH_COPY], s);
   step_descend(p, s);
   // the border units (lookups, scan, sort by leaf) need the descent only:
@@ -525,14 +553,15 @@ static void issue_step(stc_ctx *c, bool events) {
   if (events) cudaEventRecord(c->ev[PH_INSERT], s);
   step_sweep(p, s);
   if (events) cudaEventRecord(c->ev[PH_SWEEP], s);
-  if (c->lsm_on) lsm_append(p, c->lsm, s);
+  if (append && c->lsm_on) lsm_append(p, c->lsm, s);
   if (events) cudaEventRecord(c->ev[PH_APPEND], s);
   if (schema) cudaStreamWaitEvent(s, c->join_ev, 0);
 }
 
-// Captures the step with positions in input buffer b (xy_own, xy_alt) as a
-// CUDA graph. Only this thread's work on the context's streams is captured:
-// a serving thread's queries on other streams go on meanwhile.
+// Captures the step's core (without the memtable append) with positions in
+// input buffer b (xy_own, xy_alt) and its time in t_pinned[b] as a CUDA
+// graph. Only this thread's work on the context's streams is captured: a
+// serving thread's queries on other streams go on meanwhile.
 static stc_status capture_step(stc_ctx *c, int b) {
   if (c->graph[b]) {
     cudaGraphExecDestroy(c->graph[b]);
@@ -544,7 +573,7 @@ static stc_status capture_step(stc_ctx *c, int b) {
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    issue_step(c, false);
+    issue_step(c, false, false, c->t_pinned + b);
     e = cudaStreamEndCapture(c->stream, &g);
   }
   if (e == cudaSuccess) e = cudaGraphInstantiate(&c->graph[b], g, 0);
@@ -559,27 +588,10 @@ static stc_status capture_step(stc_ctx *c, int b) {
   return STC_OK;
 }
 
-static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copied, bool graph = false, int gb = 0) {
-  PipeDev &p = c->p;
-  cudaStream_t s = c->stream;
-  p.xy = xy;
-  *c->t_pinned = t;  // the previous step has been waited for: nothing reads it now
-  unsigned long long launches0 = tl_launches;
-  if (graph) {
-    if (!c->graph_valid[gb]) {
-      stc_status gs = capture_step(c, gb);
-      if (gs != STC_OK) return gs;
-    }
-    cudaError_t e = cudaGraphLaunch(c->graph[gb], s);
-    if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window");
-    tl_launches += c->graph_kernels;
-  } else {
-    issue_step(c, true);
-  }
-  cudaEventRecord(c->ev[PH_SCHEMA], s);
-  stc_status rs = read_state(c, "stc_step");
-  if (rs != STC_OK) return rs;
+// Counters of the step whose state is in c->st_host.
+static void fill_stats(stc_ctx *c, uint32_t t, const float *phase, float step_ms, uint32_t launches) {
   const DevState &h = *c->st_host;
+  const PipeDev &p = c->p;
   stc_stats &o = c->stats;
   o.step = t;
   o.leaves = h.grids_stack_index;
@@ -596,29 +608,38 @@ static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copie
   o.pending = std::min<unsigned long long>(h.emit_count, p.E);
   o.splits = h.splits;
   o.merges = h.merges;
-  float ms[PH_COUNT] = {0};
-  if (!graph)  // a replayed graph records no phase events
-    for (int i = PH_COPY; i <= PH_SCHEMA; i++) cudaEventElapsedTime(&ms[i], c->ev[i - 1], c->ev[i]);
-  o.phase_ms[0] = ms[PH_PART];
-  o.phase_ms[1] = ms[PH_BORDER];
-  o.phase_ms[2] = ms[PH_REFINE];
-  o.phase_ms[3] = ms[PH_INSERT];
-  o.phase_ms[4] = ms[PH_SWEEP];
-  o.phase_ms[5] = ms[PH_SCHEMA];
-  o.phase_ms[6] = copied ? ms[PH_COPY] : 0.f;
-  o.phase_ms[7] = ms[PH_APPEND];
+  for (int i = 0; i < 8; i++) o.phase_ms[i] = phase ? phase[i] : 0.f;
   o.ambiguous_tests = (uint32_t)h.ambiguous;
-  o.kernel_launches = (uint32_t)(tl_launches - launches0);
+  o.kernel_launches = launches;
   o.schema_path = h.schema_path;
-  float tot = 0;
-  cudaEventElapsedTime(&tot, c->ev[PH_START], c->ev[PH_SCHEMA]);
-  o.step_ms = tot;
+  o.step_ms = step_ms;
+  o.memtable_keys = h.kv_count;
   c->stepped = true;
   c->last_t = t;
-  o.memtable_keys = h.kv_count;
-  // the reference flushes once a step leaves more keys than kv_restriction
-  // (cuda/geometry.cu:1752)
-  if (c->lsm_on && h.kv_count > c->cfg.kv_restriction) return flush_now(c, t);
+}
+
+// The reference flushes once a step leaves more keys than kv_restriction
+// (cuda/geometry.cu:1752).
+static bool flush_due(const stc_ctx *c) { return c->lsm_on && c->st_host->kv_count > c->cfg.kv_restriction; }
+
+static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copied) {
+  PipeDev &p = c->p;
+  cudaStream_t s = c->stream;
+  p.xy = xy;
+  c->t_pinned[0] = t;  // the previous step has been waited for: nothing reads it now
+  unsigned long long launches0 = tl_launches;
+  issue_step(c, true, true, c->t_pinned);
+  cudaEventRecord(c->ev[PH_SCHEMA], s);
+  stc_status rs = read_state(c, "stc_step");
+  if (rs != STC_OK) return rs;
+  float ms[PH_COUNT] = {0};
+  for (int i = PH_COPY; i <= PH_SCHEMA; i++) cudaEventElapsedTime(&ms[i], c->ev[i - 1], c->ev[i]);
+  const float phase[8] = {ms[PH_PART], ms[PH_BORDER], ms[PH_REFINE], ms[PH_INSERT],
+                          ms[PH_SWEEP], ms[PH_SCHEMA], copied ? ms[PH_COPY] : 0.f, ms[PH_APPEND]};
+  float tot = 0;
+  cudaEventElapsedTime(&tot, c->ev[PH_START], c->ev[PH_SCHEMA]);
+  fill_stats(c, t, phase, tot, (uint32_t)(tl_launches - launches0));
+  if (flush_due(c)) return flush_now(c, t);
   return STC_OK;
 }
 
@@ -643,6 +664,68 @@ extern "C" stc_status stc_step_device(stc_ctx *c, const double *xy_device, uint3
   return run_step(c, (const double2 *)xy_device, t, false);
 }
 
+// Copies emit records [from, from + k) to out on the drain stream once the
+// state copy of the step in buffer b has landed (the records are complete
+// then). Page-locked output takes direct copies; other memory goes through
+// the two pinned chunks (the host waits for each, while the GPU runs on).
+static cudaError_t drain_range(stc_ctx *c, int b, unsigned long long from, size_t k, stc_meeting *out,
+                               bool pinned_out) {
+  if (!k) return cudaSuccess;
+  cudaStream_t ds = c->drain_stream;
+  cudaError_t e = cudaStreamWaitEvent(ds, c->st_ev[b], 0);
+  const size_t bytes = k * sizeof(stc_meeting);
+  const uint8_t *src = (const uint8_t *)(c->p.emit + from);
+  if (pinned_out) return e == cudaSuccess ? copy_in_pieces(out, src, bytes, cudaMemcpyDeviceToHost, ds) : e;
+  const size_t nch = (bytes + DRAIN_CHUNK - 1) / DRAIN_CHUNK;
+  for (size_t i = 0; e == cudaSuccess && i <= nch; i++) {
+    if (i < nch) {
+      const size_t off = i * DRAIN_CHUNK, len = std::min(DRAIN_CHUNK, bytes - off);
+      e = cudaMemcpyAsync(c->drain_stage[i & 1], src + off, len, cudaMemcpyDeviceToHost, ds);
+      if (e == cudaSuccess) e = cudaEventRecord(c->drain_ev[i & 1], ds);
+    }
+    if (e == cudaSuccess && i > 0) {
+      const size_t j = i - 1, off = j * DRAIN_CHUNK, len = std::min(DRAIN_CHUNK, bytes - off);
+      e = cudaEventSynchronize(c->drain_ev[j & 1]);
+      if (e == cudaSuccess) memcpy((uint8_t *)out + off, c->drain_stage[j & 1], len);
+    }
+  }
+  return e;
+}
+
+// Moves the emit records [from, count) to the front of the emit buffer and
+// sets the device and host counts to count - from. Nothing may be writing
+// the emit buffer (no step in flight).
+static cudaError_t emit_keep_tail(stc_ctx *c, unsigned long long from, unsigned long long count) {
+  PipeDev &p = c->p;
+  cudaStream_t s = c->stream;
+  cudaError_t e = cudaStreamSynchronize(c->drain_stream);  // copies out of [0, from) are done
+  const unsigned long long left = count - from;
+  for (unsigned long long src = from; e == cudaSuccess && from && src < count; src += from) {
+    unsigned long long len = std::min<unsigned long long>(from, count - src);
+    e = cudaMemcpyAsync(p.emit + (src - from), p.emit + src, len * sizeof(stc_meeting), cudaMemcpyDeviceToDevice, s);
+  }
+  c->st_host->emit_count = left;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&p.st->emit_count, &c->st_host->emit_count, sizeof(left), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  c->stats.pending = left;
+  return e;
+}
+
+// A window of steps, pipelined one step deep: step i + 1 is queued on the
+// GPU before the host waits for step i's state, so the GPU does not idle
+// while the host reads a state, drains meetings or issues launches.
+//
+// Device order per step i: core(i) (everything but the memtable append),
+// then [flush after step i - 1, when due], append(i), state copy(i). The
+// host issues core(i + 1) right after append(i), then waits for state(i)
+// and decides step i's flush from it; the flush is queued behind core(i + 1)
+// and before append(i + 1). The core of a step never touches the memtable,
+// so the flush sees exactly the keys of steps <= i, as the reference's
+// per-step rule does. Emitted meetings stay in place in the emit buffer for
+// the whole window (nothing moves while a step is in flight) and go out on
+// the drain stream beside the next step; past half the buffer the pipeline
+// holds for one step so that the buffer can be emptied.
 extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_device, uint32_t steps, uint32_t t0,
                                       stc_meeting *out, size_t cap, size_t *n_out) {
   if (!c) return STC_ERR_INVALID_ARG;
@@ -650,50 +733,196 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   if (steps && !xy) return fail(c, STC_ERR_INVALID_ARG, "stc_step_window: null positions");
   if (out && !n_out) return fail(c, STC_ERR_INVALID_ARG, "stc_step_window: output without a count");
   if (c->failed) return STC_ERR_STATE;
+  if (!steps) return STC_OK;
   cudaSetDevice(c->device);
-  const size_t step_bytes = (size_t)c->p.N * sizeof(double2);
+  PipeDev &p = c->p;
+  cudaStream_t s = c->stream;
+  const size_t step_bytes = (size_t)p.N * sizeof(double2);
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-  // Two input buffers: while step i runs from one, the copy stream fills the
-  // other with step i + 1 (that buffer was last read by step i - 1, whose
-  // state has been read back, so it is done with it).
-  if (steps && (!c->xy_alt || !c->copy_stream)) {
+  if (!c->xy_alt || !c->copy_stream) {
     cudaError_t e = cudaSuccess;
-    if (!c->xy_alt) e = cudaMalloc(&c->xy_alt, step_bytes);
+    if (!c->xy_alt) {
+      e = cudaMalloc(&c->xy_alt, step_bytes);
+      if (e == cudaSuccess) c->allocs.push_back(c->xy_alt);
+    }
     if (e == cudaSuccess && !c->copy_stream) e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
     for (int b = 0; b < 2 && e == cudaSuccess; b++)
       if (!c->copy_ev[b]) e = cudaEventCreateWithFlags(&c->copy_ev[b], cudaEventDisableTiming);
     if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window buffers");
-    c->allocs.push_back(c->xy_alt);
   }
   double2 *const buf[2] = {c->xy_own, c->xy_alt};
-  const bool graphs = c->cfg.window_graphs == 1 || (c->cfg.window_graphs == 0 && c->p.N <= (1u << 21));
+  const bool graphs = c->cfg.window_graphs == 1 || (c->cfg.window_graphs == 0 && p.N <= (1u << 21));
+  bool pinned_out = false;
+  if (out && cap) {
+    cudaPointerAttributes pa;
+    pinned_out = cudaPointerGetAttributes(&pa, out) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+    cudaGetLastError();  // pageable memory is not an error
+  }
+  unsigned long long launches[2] = {0, 0};
+
+  // Positions of step i into buffer i & 1 on the copy stream, once the core
+  // of step i - 2 (the buffer's last reader) has run.
   auto fetch = [&](uint32_t i) -> cudaError_t {
-    cudaError_t e = copy_in_pieces(buf[i & 1], (const uint8_t *)xy + (size_t)i * step_bytes, step_bytes, kind,
-                                   c->copy_stream);
-    return e == cudaSuccess ? cudaEventRecord(c->copy_ev[i & 1], c->copy_stream) : e;
+    const int b = i & 1;
+    cudaError_t e = i >= 2 ? cudaStreamWaitEvent(c->copy_stream, c->core_ev[b], 0) : cudaSuccess;
+    if (e == cudaSuccess)
+      e = copy_in_pieces(buf[b], (const uint8_t *)xy + (size_t)i * step_bytes, step_bytes, kind, c->copy_stream);
+    return e == cudaSuccess ? cudaEventRecord(c->copy_ev[b], c->copy_stream) : e;
   };
-  size_t n = 0;
-  if (steps) {
-    cudaError_t e = fetch(0);
+  auto issue_core = [&](uint32_t i) -> stc_status {
+    const int b = i & 1;
+    c->t_pinned[b] = t0 + i;  // step i - 2, the word's last reader, has been waited for
+    const unsigned long long l0 = tl_launches;
+    cudaEventRecord(c->wev[b][0], s);
+    cudaError_t e = cudaStreamWaitEvent(s, c->copy_ev[b], 0);
     if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window copy-in");
+    if (graphs) {
+      if (!c->graph_valid[b]) {
+        stc_status gs = capture_step(c, b);
+        if (gs != STC_OK) return gs;
+      }
+      e = cudaGraphLaunch(c->graph[b], s);
+      if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window");
+      tl_launches += c->graph_kernels;
+    } else {
+      p.xy = buf[b];
+      issue_step(c, false, false, c->t_pinned + b);
+    }
+    cudaEventRecord(c->core_ev[b], s);
+    launches[b] = tl_launches - l0;
+    return STC_OK;
+  };
+  auto issue_tail = [&](uint32_t i) -> stc_status {
+    const int b = i & 1;
+    const unsigned long long l0 = tl_launches;
+    cudaEventRecord(c->wev[b][1], s);
+    if (c->lsm_on) lsm_append(p, c->lsm, s);
+    cudaEventRecord(c->wev[b][2], s);
+    cudaError_t e = cudaMemcpyAsync(c->st_slot[b], p.st, sizeof(DevState), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaEventRecord(c->st_ev[b], s);
+    launches[b] += tl_launches - l0;
+    return e == cudaSuccess ? STC_OK : cuda_fail(c, e, "stc_step_window");
+  };
+  // Waits for the state of step i and takes it over as the context's state.
+  auto take_state = [&](uint32_t i) -> stc_status {
+    const int b = i & 1;
+    cudaError_t e = cudaEventSynchronize(c->st_ev[b]);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window");
+    *c->st_host = *c->st_slot[b];
+    if (c->st_host->error) {
+      char m[320];
+      snprintf(m, sizeof(m), "stc_step_window: %s (code %u, info %u)", error_name(c->st_host->error),
+               c->st_host->error, c->st_host->error_info);
+      return fail(c, status_of(c->st_host->error), m);
+    }
+    float core = 0, app = 0;
+    cudaEventElapsedTime(&core, c->wev[b][0], c->core_ev[b]);
+    cudaEventElapsedTime(&app, c->wev[b][1], c->wev[b][2]);
+    float phase[8] = {0, 0, 0, 0, 0, 0, 0, app};
+    fill_stats(c, t0 + i, phase, core + app, (uint32_t)launches[b]);
+    return STC_OK;
+  };
+
+  size_t n = 0;
+  unsigned long long dpos = 0;  // emit records [0, dpos) are on their way to out
+  bool out_full = false;
+  stc_status rs = STC_OK;
+  uint32_t ran = 0;             // steps whose state has been taken
+  bool hold = false;            // empty the emit buffer before the next core
+  cudaError_t e = fetch(0);
+  if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window copy-in");
+  rs = issue_core(0);
+  if (rs == STC_OK && steps > 1) {
+    e = fetch(1);
+    if (e != cudaSuccess) rs = cuda_fail(c, e, "stc_step_window copy-in");
+  }
+  if (rs == STC_OK) rs = issue_tail(0);
+  if (rs != STC_OK) {
+    cudaStreamSynchronize(s);
+    return rs;
   }
   for (uint32_t i = 0; i < steps; i++) {
-    cudaEventRecord(c->ev[PH_START], c->stream);
-    cudaError_t e = cudaStreamWaitEvent(c->stream, c->copy_ev[i & 1], 0);
-    if (e == cudaSuccess && i + 1 < steps) e = fetch(i + 1);
-    if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window copy-in");
-    stc_status rs = run_step(c, buf[i & 1], t0 + i, true, graphs, (int)(i & 1));
-    if (rs != STC_OK) return rs;
-    if (out) {
-      size_t k = 0;
-      rs = stc_drain_meetings(c, out + n, cap - n, &k);
-      if (rs != STC_OK) return rs;
+    const bool ahead = i + 1 < steps && !hold;
+    if (ahead) {
+      rs = issue_core(i + 1);
+      if (rs == STC_OK && i + 2 < steps) {
+        e = fetch(i + 2);
+        if (e != cudaSuccess) rs = cuda_fail(c, e, "stc_step_window copy-in");
+      }
+    }
+    if (rs == STC_OK) rs = take_state(i);
+    if (rs == STC_OK) ran = i + 1;
+    if (rs == STC_OK && out && !out_full) {
+      const unsigned long long cnt = std::min<unsigned long long>(c->st_host->emit_count, p.E);
+      const size_t k = (size_t)std::min<unsigned long long>(cnt - dpos, cap - n);
+      e = drain_range(c, i & 1, dpos, k, out + n, pinned_out);
+      if (e != cudaSuccess) rs = cuda_fail(c, e, "stc_step_window drain");
+      dpos += k;
       n += k;
       *n_out = n;
-      if (c->st_host->emit_count) return fail(c, STC_ERR_CAPACITY, "stc_step_window: the output buffer is full");
+      out_full = dpos < cnt;
+    }
+    if (rs == STC_OK && flush_due(c)) rs = flush_now(c, t0 + i);
+    if (rs != STC_OK || out_full) {
+      // the step already queued behind this one is finished and taken, its
+      // meetings left pending; nothing is in flight when the call returns
+      if (ahead && !c->failed) {
+        stc_status r2 = issue_tail(i + 1);
+        if (r2 == STC_OK) r2 = take_state(i + 1);
+        if (r2 == STC_OK) ran = i + 2;
+        if (r2 == STC_OK && flush_due(c)) r2 = flush_now(c, t0 + i + 1);
+        if (rs == STC_OK) rs = r2;
+      }
+      cudaStreamSynchronize(s);
+      cudaStreamSynchronize(c->copy_stream);
+      cudaStreamSynchronize(c->drain_stream);
+      if (!c->failed && out) {
+        e = emit_keep_tail(c, dpos, std::min<unsigned long long>(c->st_host->emit_count, p.E));
+        if (e != cudaSuccess && rs == STC_OK) rs = cuda_fail(c, e, "stc_step_window drain");
+      }
+      if (rs == STC_OK) {
+        char m[160];
+        snprintf(m, sizeof(m), "stc_step_window: the output buffer is full after step %u; %u of %u steps ran",
+                 t0 + ran - 1, ran, steps);
+        rs = fail(c, STC_ERR_CAPACITY, m);
+        c->failed = false;  // a full output buffer leaves the context usable
+      }
+      return rs;
+    }
+    if (i + 1 < steps) {
+      if (!ahead) {
+        // held: every record emitted so far is drained or on its way out, and
+        // nothing is in flight; empty the buffer, then go on
+        e = emit_keep_tail(c, dpos, std::min<unsigned long long>(c->st_host->emit_count, p.E));
+        if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window drain");
+        dpos = 0;
+        hold = false;
+        rs = issue_core(i + 1);
+        if (rs == STC_OK && i + 2 < steps) {
+          e = fetch(i + 2);
+          if (e != cudaSuccess) rs = cuda_fail(c, e, "stc_step_window copy-in");
+        }
+        if (rs != STC_OK) {
+          cudaStreamSynchronize(s);
+          return rs;
+        }
+      }
+      rs = issue_tail(i + 1);
+      if (rs != STC_OK) {
+        cudaStreamSynchronize(s);
+        return rs;
+      }
+      // step i + 1 adds its meetings behind step i's; past half of the
+      // buffer, step i + 2 waits until the buffer has been emptied
+      if (out && c->st_host->emit_count > p.E / 2) hold = true;
     }
   }
-  if (steps) cudaStreamSynchronize(c->copy_stream);
+  cudaStreamSynchronize(c->copy_stream);
+  if (out) {
+    e = emit_keep_tail(c, dpos, std::min<unsigned long long>(c->st_host->emit_count, p.E));
+    if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window drain");
+  }
   return STC_OK;
 }
 
@@ -824,19 +1053,24 @@ static stc_status query_checks(stc_ctx *c, const char *who) {
 }
 
 namespace stc {
-// stc_query_batch with a bound on the match records held on the device (the
-// serving loop's admission); 0 = none.
-stc_status query_batch_limited(stc_ctx *c, const stc_query *queries, size_t nq, stc_contact *out, size_t cap,
-                               uint64_t *offsets, uint64_t *counts, size_t device_limit);
+// stc_query_batch on query lane `lane` (-1: any free lane) with a bound on the
+// match records held on the device at a time (the serving loop's
+// admission); 0 = none.
+stc_status query_batch_limited(stc_ctx *c, int lane, const stc_query *queries, size_t nq, stc_contact *out,
+                               size_t cap, uint64_t *offsets, uint64_t *counts, size_t device_limit);
+// Queries one device pass takes (larger batches run as several passes).
+size_t query_chunk(const stc_ctx *c);
 }
 
 extern "C" stc_status stc_query_batch(stc_ctx *c, const stc_query *queries, size_t nq, stc_contact *out,
                                       size_t cap, uint64_t *offsets, uint64_t *counts) {
-  return stc::query_batch_limited(c, queries, nq, out, cap, offsets, counts, 0);
+  return stc::query_batch_limited(c, -1, queries, nq, out, cap, offsets, counts, 0);
 }
 
-stc_status stc::query_batch_limited(stc_ctx *c, const stc_query *queries, size_t nq, stc_contact *out, size_t cap,
-                                    uint64_t *offsets, uint64_t *counts, size_t device_limit) {
+size_t stc::query_chunk(const stc_ctx *c) { return c && c->lsm_on ? lsm_query_chunk(c->lsmh) : 1; }
+
+stc_status stc::query_batch_limited(stc_ctx *c, int lane, const stc_query *queries, size_t nq, stc_contact *out,
+                                    size_t cap, uint64_t *offsets, uint64_t *counts, size_t device_limit) {
   stc_status st = query_checks(c, "stc_query_batch");
   if (st != STC_OK) return st;
   if ((!queries && nq) || !offsets || (!out && cap)) {
@@ -852,9 +1086,30 @@ stc_status stc::query_batch_limited(stc_ctx *c, const stc_query *queries, size_t
     }
   }
   std::string err;
-  st = lsm_query(c->lsmh, queries, nq, out, cap, offsets, counts, err, device_limit);
-  if (st != STC_OK) g_create_error = "stc_query_batch: " + err;
-  return st;
+  const size_t chunk = lsm_query_chunk(c->lsmh);
+  if (nq <= chunk) {
+    st = lsm_query(c->lsmh, lane, queries, nq, out, cap, offsets, counts, err, device_limit);
+    if (st != STC_OK) g_create_error = "stc_query_batch: " + err;
+    return st;
+  }
+  // queries x retained blocks must stay <= 65535 per device pass: the batch
+  // runs as several passes; each writes its matches behind the previous
+  // ones while the running total fits cap
+  std::vector<uint64_t> off(chunk + 1);
+  offsets[0] = 0;
+  for (size_t a = 0; a < nq; a += chunk) {
+    const size_t m = std::min(chunk, nq - a);
+    const uint64_t done = offsets[a];
+    const bool room = out && done <= cap;
+    st = lsm_query(c->lsmh, lane, queries + a, m, room ? out + done : nullptr, room ? cap - done : 0, off.data(),
+                   counts ? counts + a : nullptr, err, device_limit);
+    if (st != STC_OK) {
+      g_create_error = "stc_query_batch: " + err;
+      return st;
+    }
+    for (size_t i = 0; i < m; i++) offsets[a + i + 1] = done + off[i + 1];
+  }
+  return STC_OK;
 }
 
 static stc_status query_one(stc_ctx *c, const stc_query &q, stc_contact *out, size_t cap, size_t *n,

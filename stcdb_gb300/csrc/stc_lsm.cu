@@ -588,7 +588,7 @@ void lsm_init(LsmDev &L, cudaStream_t s) {
 }
 
 void lsm_append(const PipeDev &p, const LsmDev &L, cudaStream_t s) {
-  STC_KL k_lsm_append<<<GRID, 256, 0, s>>>(p.emit, p.E, L);
+  STC_KL k_lsm_append<<<lsm_grid(), 256, 0, s>>>(p.emit, p.E, L);
 }
 
 void lsmk::sort_keys(const LsmDev &L, unsigned long long K, uint32_t N, uint32_t max_end, uint32_t max_dur,
@@ -622,7 +622,7 @@ void lsmk::sort_keys(const LsmDev &L, unsigned long long K, uint32_t N, uint32_t
     // the sorted records' buffer is free until the final gather: it holds
     // the high words meanwhile
     uint32_t *hi = reinterpret_cast<uint32_t *>(L.brec);
-    STC_KL k_lsm_low_high<<<GRID, 256, 0, s>>>(L, K, sk[0], sk[1], hi, words[0], words[1], rank);
+    STC_KL k_lsm_low_high<<<lsm_grid(), 256, 0, s>>>(L, K, sk[0], sk[1], hi, words[0], words[1], rank);
     sort_words(L, sk[0], sk[1], sk[2], sk[3], sk[4], sk[5], 2, K, words[0].bits, s);
     STC_KL k_gather_u32<<<nblk(K), 256, 0, s>>>(hi, sk[3], sk[0], (uint32_t)K);
     sort_words(L, sk[0], sk[3], sk[2], sk[1], sk[4], sk[5], 2, K, words[1].bits, s);
@@ -631,12 +631,12 @@ void lsmk::sort_keys(const LsmDev &L, unsigned long long K, uint32_t N, uint32_t
     uint32_t *vbuf[2] = {sk[1], sk[3]};
     for (int w = 0; w < nw; w++) {
       uint32_t *vin = vbuf[w & 1], *vout = vbuf[(w + 1) & 1];
-      STC_KL k_lsm_word<<<GRID, 256, 0, s>>>(L, K, perm, sk[0], perm ? nullptr : vin, words[w]);
+      STC_KL k_lsm_word<<<lsm_grid(), 256, 0, s>>>(L, K, perm, sk[0], perm ? nullptr : vin, words[w]);
       sort_words(L, sk[0], perm ? perm : vin, sk[2], vout, sk[4], sk[5], 2, K, words[w].bits, s);
       perm = vout;
     }
   }
-  STC_KL k_lsm_gather<<<GRID, 256, 0, s>>>(L, K, perm);
+  STC_KL k_lsm_gather<<<lsm_grid(), 256, 0, s>>>(L, K, perm);
 }
 
 // Stable sort of n (key, value) words; returns the buffers holding the result.
@@ -663,7 +663,7 @@ stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState
   cudaMemsetAsync(L.obitmap, 0, STC_BITMAP_BYTES, s);
   // 1. object boxes -> oversize objects and STR midpoints; key partition flags
   STC_KL k_lsm_set_oid<<<nblk(N), 256, 0, s>>>(L);
-  STC_KL k_lsm_flags<<<GRID, 256, 0, s>>>(L, K);
+  STC_KL k_lsm_flags<<<lsm_grid(), 256, 0, s>>>(L, K);
   // 2. order objects by midpoint (x, then y): stable sort by y, then by x
   STC_KL k_lsm_set_counts<<<1, 1, 0, s>>>(L.n_dev, N, 0, K);
   sort_words(L, L.mid_lo, sk[0], sk[1], sk[2], sk[3], sk[4], 0, N, 32, s);
@@ -684,7 +684,7 @@ stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState
     sort_words(L, sk[0], sk[2], sk[1], sk[5], sk[3], sk[4], 1, R, 32, s);
     STC_KL k_slab_of<<<nblk(R), 256, 0, s>>>(sk[5], R, xcap, S, sk[0]);
     sort_words(L, sk[0], sk[5], sk[1], sk[2], sk[3], sk[4], 1, R, bits_for(S - 1), s);
-    STC_KL k_make_sid<<<STC_NUM_SMS, 512, F * sizeof(uint32_t), s>>>(L, sk[6], sk[2], z, R, xcap, ycap);
+    STC_KL k_make_sid<<<num_sms(), 512, F * sizeof(uint32_t), s>>>(L, sk[6], sk[2], z, R, xcap, ycap);
   }
   // 4. sort the keys: (over, sid, pid, target, duration, end)
   sort_keys(L, K, N, max_end, max_dur, bits_for(S * S + 1), s);
@@ -700,7 +700,7 @@ stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState
   cudaMemcpyAsync(L.ctf_first, first.data(), (F + 1) * sizeof(unsigned long long), cudaMemcpyHostToDevice, s);
   STC_KL k_lsm_limits_init<<<nblk(F), 256, 0, s>>>(L);
   STC_KL k_lsm_limits<<<dim3(F, LIM_PARTS), 256, 0, s>>>(L, K);
-  if (K > slim) STC_KL k_lsm_oversize<<<GRID, 256, 0, s>>>(L, slim, K);
+  if (K > slim) STC_KL k_lsm_oversize<<<lsm_grid(), 256, 0, s>>>(L, slim, K);
   std::vector<float4> lb(F);
   std::vector<uint2> lt(F);
   e = cudaMemcpyAsync(lb.data(), L.lim_box, F * sizeof(float4), cudaMemcpyDeviceToHost, s);
@@ -735,7 +735,7 @@ stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState
   cudaMemcpyAsync(L.ctfs, H.ctfs.data(), F * sizeof(stc_ctf), cudaMemcpyHostToDevice, s);
   // 7. bitmaps and packed keys
   if (total)
-    STC_KL k_encode_keys<<<GRID, ENC_GROUP, 0, s>>>(
+    STC_KL k_encode_keys<<<lsm_grid(), ENC_GROUP, 0, s>>>(
         EncodeArgs{L.brec, L.bbox, L.ctfs, L.ctf_first, L.sid, L.bitmaps, L.kbytes, total, slim, L.F, false});
   // 8. keep the sids of the block; empty the memtable
   cudaMemcpyAsync(L.bsid, L.sid, (size_t)N * sizeof(uint16_t), cudaMemcpyDeviceToDevice, s);

@@ -120,18 +120,13 @@ struct QueryRec {
   uint32_t q, pad;
 };
 
-struct LsmHost {
-  bool has_block = false;
-  uint32_t flushes = 0;
-  uint32_t next_index = 0;         // index of the next block a flush or compaction makes
-  stc_ctb_info info{};
-  std::vector<stc_ctf> ctfs;
-  // retained blocks (oldest first) and the query state
-  uint32_t retain = 8;
-  std::deque<CtbBlock> blocks;
-  std::shared_mutex blocks_mu;     // exclusive while the list changes
-  std::mutex query_mu;             // one query batch at a time
-  cudaStream_t qstream = nullptr;
+// The device and pinned buffers and the stream of one query batch in
+// flight. A context keeps QUERY_LANES of them, so that that many batches
+// (the serving loop's workers, direct stc_query_batch calls) run on the GPU
+// at the same time.
+struct QueryLane {
+  std::mutex mu;                   // held by the batch using the lane
+  cudaStream_t stream = nullptr;
   QBlock *d_qb = nullptr;          // [retain]
   stc_query *d_q = nullptr;
   size_t q_cap = 0;
@@ -152,6 +147,21 @@ struct LsmHost {
   unsigned long long *h_counts = nullptr;  // [hq_cap + 1]: per-query counts, then the match total
   QueryRec *h_recs = nullptr;
   size_t hrecs_cap = 0;
+};
+
+constexpr int QUERY_LANES = 2;
+
+struct LsmHost {
+  bool has_block = false;
+  uint32_t flushes = 0;
+  uint32_t next_index = 0;         // index of the next block a flush or compaction makes
+  stc_ctb_info info{};
+  std::vector<stc_ctf> ctfs;
+  // retained blocks (oldest first) and the query state
+  uint32_t retain = 8;
+  std::deque<CtbBlock> blocks;
+  std::shared_mutex blocks_mu;     // exclusive while the list changes
+  QueryLane lanes[QUERY_LANES];
   double map[4] = {0, 0, 0, 0};
 };
 
@@ -206,16 +216,22 @@ cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s);
 stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32_t count, uint32_t split,
                        uint32_t new_index, cudaStream_t s, float *ms, std::string &err);
 
-// Allocates the query buffers for batches of up to nq queries over blocks of
-// up to F CTFs (later batches then allocate nothing unless they need more).
-stc_status lsm_query_reserve(LsmHost &H, size_t nq, uint32_t F, std::string &err);
+// Creates the query lanes' streams (priority `priority`) and allocates their
+// buffers for batches of up to nq queries over blocks of up to F CTFs (later
+// batches then allocate nothing unless they need more).
+stc_status lsm_query_reserve(LsmHost &H, size_t nq, uint32_t F, int priority, std::string &err);
 
-// Runs a batch of queries over the retained blocks on H.qstream (see
-// stc_query_batch in include/stc.h). device_limit (0 = none) bounds the match
-// records the device output may hold: a batch with more matches is only
-// counted (offsets and counts filled, out untouched).
-stc_status lsm_query(LsmHost &H, const stc_query *q, size_t nq, stc_contact *out, size_t cap, uint64_t *offsets,
-                     uint64_t *counts, std::string &err, size_t device_limit = 0);
+// Queries one batch may hold (the plan grid and the per-(query, block) work
+// of the object kernel are bounded by queries x retained blocks <= 65535).
+size_t lsm_query_chunk(const LsmHost &H);
+
+// Runs a batch of at most lsm_query_chunk(H) queries over the retained blocks
+// on query lane `lane` (-1: the first free lane, else lane 0 once it frees)
+// (see stc_query_batch in include/stc.h). device_limit (0 = none) bounds the
+// match records the device output may hold: a batch with more matches is
+// only counted (offsets and counts filled, out untouched).
+stc_status lsm_query(LsmHost &H, int lane, const stc_query *q, size_t nq, stc_contact *out, size_t cap,
+                     uint64_t *offsets, uint64_t *counts, std::string &err, size_t device_limit = 0);
 
 // Host restatement of CTF::get_ctf_bits (tracing/step_merge.cpp:140-186);
 // returns false when the key would exceed 64 box bits or 128 key bits.

@@ -17,7 +17,7 @@ inline uint32_t bits_for(unsigned long long v) {
   return b;
 }
 
-constexpr unsigned GRID = STC_NUM_SMS * 8;  // grid-stride kernels over keys
+inline unsigned lsm_grid() { return (unsigned)num_sms() * 8; }  // grid-stride kernels over keys
 constexpr uint32_t OBOX_INIT = 100000000u;  // uint_box initial low (geometry/geometry.h:320-324)
 constexpr uint32_t LIM_PARTS = 32;          // blocks per CTF in k_lsm_limits
 constexpr uint32_t MAX_CTF = 3969;          // 63^2: sids 2..3970 fit the 12-bit sid field

@@ -81,8 +81,8 @@ __global__ void k_init_cands(Cand *c, unsigned long long C) {
 }
 
 void init_tables(PipeDev &p, cudaStream_t s) {
-  STC_KL k_init_slots<<<STC_NUM_SMS * 8, 256, 0, s>>>(p.slots, p.B);
-  STC_KL k_init_cands<<<STC_NUM_SMS * 8, 256, 0, s>>>(p.cset, p.C);
+  STC_KL k_init_slots<<<num_sms() * 8, 256, 0, s>>>(p.slots, p.B);
+  STC_KL k_init_cands<<<num_sms() * 8, 256, 0, s>>>(p.cset, p.C);
 }
 
 // Candidates that may occur twice in a step: walk with their minimum
@@ -105,7 +105,7 @@ __global__ void k_insert_ordered(PipeDev p) {
   }
 }
 
-void step_insert(PipeDev &p, cudaStream_t s) { STC_KL k_insert_ordered<<<STC_NUM_SMS * 4, 256, 0, s>>>(p); }
+void step_insert(PipeDev &p, cudaStream_t s) { STC_KL k_insert_ordered<<<num_sms() * 4, 256, 0, s>>>(p); }
 
 // Sweep (tracing/meeting.cpp:32-76, cuda/geometry.cu:595-736).
 
@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 6) k_sweep(PipeDev p, uint32_t 
 
 void step_sweep(PipeDev &p, cudaStream_t s) {
   for (uint32_t part = 0; part < p.slices; part++)
-    STC_KL k_sweep<<<STC_NUM_SMS * 6, SWEEP_THREADS, 0, s>>>(p, part, p.slices);
+    STC_KL k_sweep<<<num_sms() * 6, SWEEP_THREADS, 0, s>>>(p, part, p.slices);
 }
 
 }  // namespace stc

@@ -237,10 +237,10 @@ void step_leaf_order(PipeDev &p, cudaStream_t s) {
 
 void step_border(PipeDev &p, cudaStream_t s) {
   cudaMemsetAsync(p.bu_cnt, 0, (size_t)(p.G + 1) * sizeof(uint32_t), s);
-  STC_KL k_border_count<<<STC_NUM_SMS * 16, 128, 0, s>>>(p);
+  STC_KL k_border_count<<<num_sms() * 16, 128, 0, s>>>(p);
   exclusive_scan_u32(p.bcount, p.boff, p.N, &p.st->border_units, p.scan_tmp2, s);
   STC_KL k_check_units<<<1, 1, 0, s>>>(p);
-  STC_KL k_border_fill<<<STC_NUM_SMS * 16, 128, 0, s>>>(p);
+  STC_KL k_border_fill<<<num_sms() * 16, 128, 0, s>>>(p);
   int bits = 1;
   while ((1u << bits) < p.G && bits < 32) bits++;
   radix_sort_u32(p.bu_gid, p.iota, p.bu_sorted_gid, p.bu_sorted_pos, p.sort_ktmp2, p.sort_vtmp2,

@@ -841,7 +841,7 @@ cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
     STC_KL k_set_one<<<1, 1, 0, s>>>(L.n_dev + 3, total);
     e = cudaMemsetAsync(L.n_dev + 4, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
-    STC_KL k_index_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(B.keys, B.d_ctfs, F, B.cbase, B.ixg, B.ixs, B.ixf, total,
+    STC_KL k_index_cells<<<num_sms() * 8, 256, 0, s>>>(B.keys, B.d_ctfs, F, B.cbase, B.ixg, B.ixs, B.ixf, total,
                                                          sk[0], sk[1], sk[6], L.n_dev + 4);  // tables copied above
     unsigned long long max_end = 65535;
     e = cudaMemcpyAsync(&max_end, L.n_dev + 4, sizeof(max_end), cudaMemcpyDeviceToHost, s);
@@ -851,21 +851,21 @@ cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s) {
     while (eb < 16 && (max_end >> eb)) eb++;
     if (bits + eb <= 32) {
       // one sort of (cell << eb | end offset); the end offsets are the sorted keys' low bits
-      STC_KL k_index_keys<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[0], sk[6], (uint32_t)eb, total, sk[4]);
+      STC_KL k_index_keys<<<num_sms() * 8, 256, 0, s>>>(sk[0], sk[6], (uint32_t)eb, total, sk[4]);
       radix_sort_u32(sk[4], sk[1], sk[2], B.perm, sk[0], sk[5], L.n_dev + 3, (size_t)total, bits + eb, L.hist,
                      L.scan, s);
-      STC_KL k_index_ends<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[2], (uint32_t)eb, total, B.pend);
+      STC_KL k_index_ends<<<num_sms() * 8, 256, 0, s>>>(sk[2], (uint32_t)eb, total, B.pend);
       shift = (uint32_t)eb;
     } else {
       // stable sorts by end, then by cell
       radix_sort_u32(sk[6], sk[1], sk[2], sk[3], sk[4], sk[5], L.n_dev + 3, (size_t)total, 16, L.hist, L.scan, s);
-      STC_KL k_gather_cells<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[0], sk[3], sk[4], total);
+      STC_KL k_gather_cells<<<num_sms() * 8, 256, 0, s>>>(sk[0], sk[3], sk[4], total);
       radix_sort_u32(sk[4], sk[3], sk[2], B.perm, sk[0], sk[5], L.n_dev + 3, (size_t)total, bits, L.hist, L.scan,
                      s);
-      STC_KL k_gather_ends<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[6], B.perm, B.pend, total);
+      STC_KL k_gather_ends<<<num_sms() * 8, 256, 0, s>>>(sk[6], B.perm, B.pend, total);
     }
   }
-  STC_KL k_cell_starts<<<STC_NUM_SMS * 8, 256, 0, s>>>(sk[2], shift, total, ncells, B.cstart);
+  STC_KL k_cell_starts<<<num_sms() * 8, 256, 0, s>>>(sk[2], shift, total, ncells, B.cstart);
   e = cudaStreamSynchronize(s);  // the copies of cbase, ixg and ixs read this stack frame
   return e == cudaSuccess ? cudaGetLastError() : e;
 }
@@ -917,70 +917,62 @@ void lsm_release(LsmHost &H) {
   std::unique_lock<std::shared_mutex> lock(H.blocks_mu);
   for (CtbBlock &o : H.blocks) free_block(o);
   H.blocks.clear();
-  if (H.d_qb) cudaFree(H.d_qb);
-  if (H.d_q) cudaFree(H.d_q);
-  if (H.d_out) cudaFree(H.d_out);
-  if (H.d_count) cudaFree(H.d_count);
-  if (H.d_qcounts) cudaFree(H.d_qcounts);
-  H.d_qcounts = nullptr;
-  H.qc_cap = 0;
-  if (H.d_items) cudaFree(H.d_items);
-  if (H.d_iscan) cudaFree(H.d_iscan);
-  H.d_items = H.d_iscan = nullptr;
-  H.items_cap = H.iscan_cap = 0;
-  for (void *v : {(void *)H.h_qb, (void *)H.h_q, (void *)H.h_counts, (void *)H.h_recs})
-    if (v) cudaFreeHost(v);
-  H.h_qb = nullptr;
-  H.h_q = nullptr;
-  H.h_counts = nullptr;
-  H.h_recs = nullptr;
-  H.hq_cap = H.hrecs_cap = 0;
-  if (H.qstream) cudaStreamDestroy(H.qstream);
-  H.d_qb = nullptr;
-  H.d_q = nullptr;
-  H.d_out = nullptr;
-  H.d_count = nullptr;
-  H.qstream = nullptr;
-  H.q_cap = H.out_cap = 0;
+  for (QueryLane &Q : H.lanes) {
+    std::lock_guard<std::mutex> ql(Q.mu);
+    if (Q.stream) cudaStreamSynchronize(Q.stream);
+    for (void *v : {(void *)Q.d_qb, (void *)Q.d_q, (void *)Q.d_out, (void *)Q.d_count, (void *)Q.d_qcounts,
+                    (void *)Q.d_items, (void *)Q.d_iscan})
+      if (v) cudaFree(v);
+    for (void *v : {(void *)Q.h_qb, (void *)Q.h_q, (void *)Q.h_counts, (void *)Q.h_recs})
+      if (v) cudaFreeHost(v);
+    if (Q.stream) cudaStreamDestroy(Q.stream);
+    Q.d_qb = nullptr;
+    Q.d_q = nullptr;
+    Q.d_out = nullptr;
+    Q.d_count = Q.d_qcounts = nullptr;
+    Q.d_items = Q.d_iscan = nullptr;
+    Q.h_qb = nullptr;
+    Q.h_q = nullptr;
+    Q.h_counts = nullptr;
+    Q.h_recs = nullptr;
+    Q.stream = nullptr;
+    Q.q_cap = Q.out_cap = Q.qc_cap = Q.items_cap = Q.iscan_cap = Q.hq_cap = Q.hrecs_cap = 0;
+  }
 }
 
 // Device and pinned buffers of a batch of up to nq queries over H.retain
-// blocks of up to F CTFs. Allocations synchronise with the device (a step in
-// flight), so they are made once, before any step runs; batches that need
-// more grow them.
-cudaError_t query_buffers(LsmHost &H, size_t nq, uint32_t F) {
+// blocks of up to F CTFs on lane Q. Allocations synchronise with the device
+// (a step in flight), so they are made once, before any step runs; batches
+// that need more grow them.
+static cudaError_t query_buffers(const LsmHost &H, QueryLane &Q, size_t nq, uint32_t F) {
   cudaError_t e = cudaSuccess;
-  if (!H.d_qb) e = cudaMalloc(&H.d_qb, (size_t)std::max<uint32_t>(H.retain, 1) * sizeof(QBlock));
-  if (e == cudaSuccess && !H.h_qb)
-    e = cudaMallocHost((void **)&H.h_qb, (size_t)std::max<uint32_t>(H.retain, 1) * sizeof(QBlock));
-  if (e == cudaSuccess && !H.d_count) e = cudaMalloc(&H.d_count, sizeof(unsigned long long));
-  if (e == cudaSuccess && H.hq_cap < nq) {
-    size_t cap_q = H.hq_cap;
-    e = grow_pinned(&H.h_q, &H.hq_cap, nq);
-    if (e == cudaSuccess) e = grow_pinned(&H.h_counts, &cap_q, H.hq_cap + 1);
+  const size_t nb = std::max<uint32_t>(H.retain, 1);
+  if (!Q.d_qb) e = cudaMalloc(&Q.d_qb, nb * sizeof(QBlock));
+  if (e == cudaSuccess && !Q.h_qb) e = cudaMallocHost((void **)&Q.h_qb, nb * sizeof(QBlock));
+  if (e == cudaSuccess && !Q.d_count) e = cudaMalloc(&Q.d_count, sizeof(unsigned long long));
+  if (e == cudaSuccess && Q.hq_cap < nq) {
+    size_t cap_q = Q.hq_cap;
+    e = grow_pinned(&Q.h_q, &Q.hq_cap, nq);
+    if (e == cudaSuccess) e = grow_pinned(&Q.h_counts, &cap_q, Q.hq_cap + 1);
   }
-  if (e == cudaSuccess) e = grow(&H.d_q, &H.q_cap, nq);
-  if (e == cudaSuccess) e = grow(&H.d_qcounts, &H.qc_cap, nq);
-  if (e == cudaSuccess) e = grow(&H.d_out, &H.out_cap, std::max<size_t>(1 << 16, H.out_cap));
-  const size_t npairs = nq * (size_t)H.blocks.size() * ((size_t)F + 1) + 1;
-  if (e == cudaSuccess) e = grow(&H.d_items, &H.items_cap, npairs);
-  if (e == cudaSuccess) e = grow(&H.d_iscan, &H.iscan_cap, scan_tmp_words(npairs));
+  if (e == cudaSuccess) e = grow(&Q.d_q, &Q.q_cap, nq);
+  if (e == cudaSuccess) e = grow(&Q.d_qcounts, &Q.qc_cap, nq);
+  if (e == cudaSuccess) e = grow(&Q.d_out, &Q.out_cap, std::max<size_t>(1 << 16, Q.out_cap));
+  // size the plan for the retained-block limit, not today's count
+  const size_t npairs = nq * nb * ((size_t)F + 1) + 1;
+  if (e == cudaSuccess) e = grow(&Q.d_items, &Q.items_cap, npairs);
+  if (e == cudaSuccess) e = grow(&Q.d_iscan, &Q.iscan_cap, scan_tmp_words(npairs));
+  if (e == cudaSuccess) e = grow_pinned(&Q.h_recs, &Q.hrecs_cap, 1 << 16);
   return e;
 }
 
-stc_status lsm_query_reserve(LsmHost &H, size_t nq, uint32_t F, std::string &err) {
-  std::lock_guard<std::mutex> qlock(H.query_mu);
-  const size_t nb = H.blocks.size();
+stc_status lsm_query_reserve(LsmHost &H, size_t nq, uint32_t F, int priority, std::string &err) {
   cudaError_t e = cudaSuccess;
-  {
-    // size the plan for the retained-block limit, not today's count
-    const size_t npairs = nq * (size_t)std::max<uint32_t>(H.retain, 1) * ((size_t)F + 1) + 1;
-    e = grow(&H.d_items, &H.items_cap, npairs);
-    if (e == cudaSuccess) e = grow(&H.d_iscan, &H.iscan_cap, scan_tmp_words(npairs));
+  for (QueryLane &Q : H.lanes) {
+    std::lock_guard<std::mutex> ql(Q.mu);
+    if (e == cudaSuccess && !Q.stream) e = cudaStreamCreateWithPriority(&Q.stream, cudaStreamNonBlocking, priority);
+    if (e == cudaSuccess) e = query_buffers(H, Q, nq, F);
   }
-  if (e == cudaSuccess) e = query_buffers(H, nq, F);
-  if (e == cudaSuccess) e = grow_pinned(&H.h_recs, &H.hrecs_cap, 1 << 16);
-  (void)nb;
   // load the query kernels now: with lazy module loading their first launch
   // would load them then, which waits for a step in flight
   cudaFuncAttributes fa;
@@ -993,9 +985,31 @@ stc_status lsm_query_reserve(LsmHost &H, size_t nq, uint32_t F, std::string &err
   return STC_OK;
 }
 
-stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *out, size_t cap, uint64_t *offsets,
-                     uint64_t *counts, std::string &err, size_t device_limit) {
-  std::lock_guard<std::mutex> qlock(H.query_mu);
+size_t lsm_query_chunk(const LsmHost &H) { return std::max<size_t>(1, 65535 / std::max<uint32_t>(H.retain, 1)); }
+
+// The lane a batch runs on: `lane` when given, else the first lane no batch
+// holds, else lane 0 once it frees.
+static std::unique_lock<std::mutex> take_lane(LsmHost &H, int lane, QueryLane **out) {
+  if (lane >= 0 && lane < QUERY_LANES) {
+    *out = &H.lanes[lane];
+    return std::unique_lock<std::mutex>(H.lanes[lane].mu);
+  }
+  for (QueryLane &Q : H.lanes) {
+    std::unique_lock<std::mutex> l(Q.mu, std::try_to_lock);
+    if (l.owns_lock()) {
+      *out = &Q;
+      return l;
+    }
+  }
+  *out = &H.lanes[0];
+  return std::unique_lock<std::mutex>(H.lanes[0].mu);
+}
+
+stc_status lsm_query(LsmHost &H, int lane, const stc_query *qs, size_t nq, stc_contact *out, size_t cap,
+                     uint64_t *offsets, uint64_t *counts, std::string &err, size_t device_limit) {
+  QueryLane *Qp = nullptr;
+  std::unique_lock<std::mutex> qlock = take_lane(H, lane, &Qp);
+  QueryLane &Q = *Qp;
   std::shared_lock<std::shared_mutex> lock(H.blocks_mu);
   const uint32_t nb = (uint32_t)H.blocks.size();
   for (size_t i = 0; i <= nq; i++) offsets[i] = 0;
@@ -1006,7 +1020,7 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
     err = "query batch too large: queries x retained blocks must be <= 65535";
     return STC_ERR_INVALID_ARG;
   }
-  cudaStream_t s = H.qstream;
+  cudaStream_t s = Q.stream;
   uint32_t maxF = 0;
   for (uint32_t i = 0; i < nb; i++) maxF = std::max(maxF, H.blocks[i].info.ctf_count);
   // box-query plan: one count per (query, block, CTF or oversize buffer), then their exclusive scan
@@ -1014,12 +1028,12 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
     err = "query batch too large for the box-query plan";
     return STC_ERR_INVALID_ARG;
   }
-  cudaError_t e = query_buffers(H, nq, maxF);
+  cudaError_t e = query_buffers(H, Q, nq, maxF);
   if (e != cudaSuccess) {
     err = std::string("query buffers: ") + cudaGetErrorString(e);
     return STC_ERR_CUDA;
   }
-  QBlock *qb = H.h_qb;
+  QBlock *qb = Q.h_qb;
   for (uint32_t i = 0; i < nb; i++) {
     const CtbBlock &B = H.blocks[i];
     qb[i] = QBlock{B.keys, B.d_ctfs, B.sids, B.orec, B.obox, B.bitmaps, B.obitmap, B.perm, B.cstart, B.cbase, B.ixg,
@@ -1029,51 +1043,51 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
   }
   bool has_obj = false, has_box = false;
   for (size_t i = 0; i < nq; i++) ((qs[i].kind & 0xFFu) == STC_QUERY_BOX ? has_box : has_obj) = true;
-  memcpy(H.h_q, qs, nq * sizeof(stc_query));
-  e = cudaMemcpyAsync(H.d_qb, qb, nb * sizeof(QBlock), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(H.d_q, H.h_q, nq * sizeof(stc_query), cudaMemcpyHostToDevice, s);
+  memcpy(Q.h_q, qs, nq * sizeof(stc_query));
+  e = cudaMemcpyAsync(Q.d_qb, qb, nb * sizeof(QBlock), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(Q.d_q, Q.h_q, nq * sizeof(stc_query), cudaMemcpyHostToDevice, s);
   unsigned long long total = 0;
   bool over = false;  // more matches than device_limit: counted only
   for (int attempt = 0; attempt < 2 && e == cudaSuccess; attempt++) {
-    e = cudaMemsetAsync(H.d_count, 0, sizeof(unsigned long long), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(H.d_qcounts, 0, nq * sizeof(unsigned long long), s);
+    e = cudaMemsetAsync(Q.d_count, 0, sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(Q.d_qcounts, 0, nq * sizeof(unsigned long long), s);
     if (e != cudaSuccess) break;
     if (has_obj)
-      STC_KL k_query_object<<<dim3(nb, (unsigned)nq), QOBJ_THREADS, 0, s>>>(H.d_qb, H.d_q, H.d_out, H.out_cap,
-                                                                           H.d_count, H.d_qcounts);
+      STC_KL k_query_object<<<dim3(nb, (unsigned)nq), QOBJ_THREADS, 0, s>>>(Q.d_qb, Q.d_q, Q.d_out, Q.out_cap,
+                                                                           Q.d_count, Q.d_qcounts);
     if (has_box) {
       const uint32_t F1 = maxF + 1, P = (uint32_t)nq * nb * F1;
-      STC_KL k_box_plan<<<(P + 255) / 256, 256, 0, s>>>(H.d_qb, nb, H.d_q, (uint32_t)nq, F1, H.map[0], H.map[1],
-                                                        H.map[2], H.map[3], H.d_items, H.d_qcounts);
-      exclusive_scan_u32(H.d_items, H.d_items, (size_t)P + 1, nullptr, H.d_iscan, s);
-      STC_KL k_box_rows<<<STC_NUM_SMS * 16, QBOX_THREADS, 0, s>>>(H.d_qb, nb, H.d_q, (uint32_t)nq, F1, H.d_items,
-                                                                  H.d_out, H.out_cap, H.d_count, H.d_qcounts);
+      STC_KL k_box_plan<<<(P + 255) / 256, 256, 0, s>>>(Q.d_qb, nb, Q.d_q, (uint32_t)nq, F1, H.map[0], H.map[1],
+                                                        H.map[2], H.map[3], Q.d_items, Q.d_qcounts);
+      exclusive_scan_u32(Q.d_items, Q.d_items, (size_t)P + 1, nullptr, Q.d_iscan, s);
+      STC_KL k_box_rows<<<num_sms() * 16, QBOX_THREADS, 0, s>>>(Q.d_qb, nb, Q.d_q, (uint32_t)nq, F1, Q.d_items,
+                                                                Q.d_out, Q.out_cap, Q.d_count, Q.d_qcounts);
     }
     e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(H.h_counts + nq, H.d_count, sizeof(total), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(Q.h_counts + nq, Q.d_count, sizeof(total), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess && (counts || device_limit))
-      e = cudaMemcpyAsync(H.h_counts, H.d_qcounts, nq * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+      e = cudaMemcpyAsync(Q.h_counts, Q.d_qcounts, nq * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    total = H.h_counts[nq];
-    if (e == cudaSuccess && counts) memcpy(counts, H.h_counts, nq * sizeof(unsigned long long));
-    if (e != cudaSuccess || total <= H.out_cap) break;
+    total = Q.h_counts[nq];
+    if (e == cudaSuccess && counts) memcpy(counts, Q.h_counts, nq * sizeof(unsigned long long));
+    if (e != cudaSuccess || total <= Q.out_cap) break;
     if (device_limit && total > device_limit) {
       over = true;
       break;
     }
-    e = grow(&H.d_out, &H.out_cap, (size_t)total);  // too many matches: once more with room for all
+    e = grow(&Q.d_out, &Q.out_cap, (size_t)total);  // too many matches: once more with room for all
   }
   if (e != cudaSuccess) {
     err = std::string("query: ") + cudaGetErrorString(e);
     return STC_ERR_CUDA;
   }
   if (over) {
-    for (size_t i = 0; i < nq; i++) offsets[i + 1] = offsets[i] + H.h_counts[i];
+    for (size_t i = 0; i < nq; i++) offsets[i + 1] = offsets[i] + Q.h_counts[i];
     return STC_OK;
   }
   if (total) {
-    e = grow_pinned(&H.h_recs, &H.hrecs_cap, (size_t)total);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(H.h_recs, H.d_out, total * sizeof(QueryRec), cudaMemcpyDeviceToHost, s);
+    e = grow_pinned(&Q.h_recs, &Q.hrecs_cap, (size_t)total);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(Q.h_recs, Q.d_out, total * sizeof(QueryRec), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
       err = std::string("query read-back: ") + cudaGetErrorString(e);
@@ -1081,7 +1095,7 @@ stc_status lsm_query(LsmHost &H, const stc_query *qs, size_t nq, stc_contact *ou
     }
   }
   // group by query (counting sort)
-  const QueryRec *recs = H.h_recs;
+  const QueryRec *recs = Q.h_recs;
   for (unsigned long long i = 0; i < total; i++) offsets[recs[i].q + 1]++;
   for (size_t i = 0; i < nq; i++) offsets[i + 1] += offsets[i];
   if (total <= cap && out) {

@@ -424,12 +424,12 @@ __global__ void k_hit_mark(PipeDev p, uint32_t part) {
 }
 
 void step_pairs_part(PipeDev &p, uint32_t part, uint32_t parts, cudaStream_t s) {
-  STC_KL k_refine_a<<<STC_NUM_SMS * p.refine_bps, REFINE_THREADS, 0, s>>>(p, part, parts);
+  STC_KL k_refine_a<<<num_sms() * p.refine_bps, REFINE_THREADS, 0, s>>>(p, part, parts);
   STC_KL k_hit_mark<<<1, 1, 0, s>>>(p, part);
 }
 
 void step_hits_part(PipeDev &p, uint32_t part, uint32_t parts, cudaStream_t s) {
-  STC_KL k_hits<<<STC_NUM_SMS * p.hits_bps, 256, 0, s>>>(p, part, parts);
+  STC_KL k_hits<<<num_sms() * p.hits_bps, 256, 0, s>>>(p, part, parts);
 }
 
 }  // namespace stc

@@ -1,10 +1,14 @@
-// Request loop over stc_query_batch (stc_server_* in include/stc.h): one
-// thread answers submitted queries by continuous batching. Queries wait in
-// arrival order; a batch takes them while its device footprint (records,
-// counters and the output records reserved for queries that return
-// contacts) stays within the configured budget, and the device output is
-// bounded to that reservation, so a batch never holds more HBM than it was
-// admitted with.
+// Request loop over stc_query_batch (stc_server_* in include/stc.h): worker
+// threads answer submitted queries by continuous batching. Queries wait in
+// arrival order; an idle worker takes what has arrived as its batch, while
+// the device footprint of all batches in flight (records, counters and the
+// output records reserved for queries that return contacts) stays within the
+// configured budget, and runs it on its own query lane (stream and buffers).
+// With QUERY_LANES workers, queries that arrive while a batch is on the GPU
+// start at once on the other lane: batches overlap on the device instead of
+// queueing behind one another. The device output of a batch is bounded to
+// its reservation, so the batches in flight never hold more HBM than they
+// were admitted with.
 #include <time.h>
 
 #include <algorithm>
@@ -19,11 +23,14 @@
 
 namespace stc {
 void set_thread_error(const std::string &msg);
-stc_status query_batch_limited(stc_ctx *c, const stc_query *queries, size_t nq, stc_contact *out, size_t cap,
-                               uint64_t *offsets, uint64_t *counts, size_t device_limit);
+stc_status query_batch_limited(stc_ctx *c, int lane, const stc_query *queries, size_t nq, stc_contact *out,
+                               size_t cap, uint64_t *offsets, uint64_t *counts, size_t device_limit);
+size_t query_chunk(const stc_ctx *c);
 }
 
 namespace {
+
+constexpr int WORKERS = 2;  // one per query lane of the context (QUERY_LANES)
 
 double mono_now() {
   timespec ts;
@@ -53,13 +60,17 @@ struct Done {
 struct stc_server {
   stc_ctx *ctx = nullptr;
   stc_server_config cfg{};
+  size_t chunk = 1;                // queries one device pass takes
   std::mutex mu;
   std::condition_variable cv_in, cv_out;
   std::deque<Pending> pending;
   std::deque<Done> done;
-  std::thread th;
+  std::thread th[WORKERS];
   bool stopping = false;
   uint64_t next_ticket = 1;
+  uint32_t next_batch = 0;
+  uint64_t inflight_bytes = 0;     // admitted footprint of the batches on the GPU
+  uint32_t busy = 0;               // workers running a batch
   stc_server_stats stats{};
 };
 
@@ -67,23 +78,81 @@ static uint64_t footprint(const stc_server &s, const stc_query &q) {
   return QUERY_BYTES + ((q.kind & STC_QUERY_COUNT_ONLY) ? 0 : (uint64_t)s.cfg.result_cap * RECORD_BYTES);
 }
 
-static void serve(stc_server *s) {
+// Runs queries qs[0..n) on `lane` with room for `reserve` contacts and fills
+// their answers: a contact-returning query gets its contacts when it has at
+// most result_cap of them, else STC_ERR_CAPACITY with its count. When the
+// batch's matches exceed the reservation (some query is over its cap), the
+// queries within their caps run once more on their own; their matches fit
+// the reservation by construction.
+static void answer(stc_server *s, int lane, const std::vector<stc_query> &qs, std::vector<Done> &ready) {
+  const size_t n = qs.size();
+  const uint64_t rcap = s->cfg.result_cap;
+  size_t reserve = 0;
+  for (const stc_query &q : qs)
+    if (!(q.kind & STC_QUERY_COUNT_ONLY)) reserve += rcap;
+  std::vector<stc_contact> out(std::max<size_t>(reserve, 1));
+  std::vector<uint64_t> offsets(n + 1, 0), counts(n, 0);
+  stc_status st = stc::query_batch_limited(s->ctx, lane, qs.data(), n, out.data(), reserve, offsets.data(),
+                                           counts.data(), std::max<size_t>(reserve, 1));
+  bool wrote = st == STC_OK && offsets[n] <= reserve;
+  std::vector<size_t> again;  // contact queries within their cap, when the batch's output was not written
+  for (size_t i = 0; i < n; i++) {
+    Done &d = ready[i];
+    d.a.count = st == STC_OK ? counts[i] : 0;
+    d.a.contact_offset = 0;
+    d.a.stored = 0;
+    d.a.status = (uint32_t)st;
+    if (st != STC_OK || (qs[i].kind & STC_QUERY_COUNT_ONLY)) continue;
+    if (counts[i] > rcap) {
+      d.a.status = STC_ERR_CAPACITY;  // more contacts than its reservation
+    } else if (wrote) {
+      d.contacts.assign(out.begin() + (ptrdiff_t)offsets[i], out.begin() + (ptrdiff_t)offsets[i + 1]);
+      d.a.stored = (uint32_t)d.contacts.size();
+    } else {
+      again.push_back(i);
+    }
+  }
+  if (again.empty()) return;
+  std::vector<stc_query> q2(again.size());
+  for (size_t j = 0; j < again.size(); j++) q2[j] = qs[again[j]];
+  offsets.assign(q2.size() + 1, 0);
+  st = stc::query_batch_limited(s->ctx, lane, q2.data(), q2.size(), out.data(), reserve, offsets.data(), nullptr,
+                                std::max<size_t>(reserve, 1));
+  wrote = st == STC_OK && offsets[q2.size()] <= reserve;
+  for (size_t j = 0; j < again.size(); j++) {
+    Done &d = ready[again[j]];
+    if (!wrote) {
+      d.a.status = st != STC_OK ? (uint32_t)st : (uint32_t)STC_ERR_CAPACITY;  // the blocks changed meanwhile
+      continue;
+    }
+    d.contacts.assign(out.begin() + (ptrdiff_t)offsets[j], out.begin() + (ptrdiff_t)offsets[j + 1]);
+    d.a.stored = (uint32_t)d.contacts.size();
+  }
+}
+
+static void serve(stc_server *s, int lane) {
   std::vector<Pending> take;
   std::vector<stc_query> qs;
-  std::vector<stc_contact> out;
-  std::vector<uint64_t> offsets, counts;
-  uint32_t batch_no = 0;
   for (;;) {
     take.clear();
     uint64_t bytes = 0;
     bool cut = false;
+    uint32_t batch_no = 0;
     {
       std::unique_lock<std::mutex> lk(s->mu);
-      s->cv_in.wait(lk, [&] { return s->stopping || !s->pending.empty(); });
+      // work when queries wait and the first of them fits beside the
+      // batches in flight (alone, it is always admitted)
+      s->cv_in.wait(lk, [&] {
+        if (s->pending.empty()) return s->stopping;
+        return s->inflight_bytes == 0 ||
+               s->inflight_bytes + footprint(*s, s->pending.front().q) <= s->cfg.hbm_budget;
+      });
       if (s->pending.empty()) break;  // stopping, and everything answered
-      while (!s->pending.empty() && take.size() < s->cfg.max_batch) {
+      const uint64_t room = s->cfg.hbm_budget > s->inflight_bytes ? s->cfg.hbm_budget - s->inflight_bytes : 0;
+      const size_t most = std::min<size_t>(s->cfg.max_batch, s->chunk);
+      while (!s->pending.empty() && take.size() < most) {
         const uint64_t f = footprint(*s, s->pending.front().q);
-        if (!take.empty() && bytes + f > s->cfg.hbm_budget) {
+        if (!take.empty() && bytes + f > room) {
           cut = true;
           break;
         }
@@ -91,52 +160,37 @@ static void serve(stc_server *s) {
         take.push_back(s->pending.front());
         s->pending.pop_front();
       }
+      s->inflight_bytes += bytes;
+      if (++s->busy > 1) s->stats.overlapped_batches++;
+      batch_no = s->next_batch++;
     }
+    // the other worker may take what is left beside this batch
+    s->cv_in.notify_one();
     const size_t n = take.size();
-    size_t reserve = 0;
     qs.resize(n);
-    for (size_t i = 0; i < n; i++) {
-      qs[i] = take[i].q;
-      if (!(qs[i].kind & STC_QUERY_COUNT_ONLY)) reserve += s->cfg.result_cap;
-    }
-    out.resize(std::max<size_t>(reserve, 1));
-    offsets.assign(n + 1, 0);
-    counts.assign(n, 0);
-    const stc_status st = stc::query_batch_limited(s->ctx, qs.data(), n, out.data(), reserve, offsets.data(),
-                                                   counts.data(), std::max<size_t>(reserve, 1));
-    const double t_done = mono_now();
-    const bool wrote = st == STC_OK && offsets[n] <= reserve;
+    for (size_t i = 0; i < n; i++) qs[i] = take[i].q;
     std::vector<Done> ready(n);
+    answer(s, lane, qs, ready);
+    const double t_done = mono_now();
     for (size_t i = 0; i < n; i++) {
-      Done &d = ready[i];
-      d.a.ticket = take[i].ticket;
-      d.a.count = st == STC_OK ? counts[i] : 0;
-      d.a.contact_offset = 0;
-      d.a.stored = 0;
-      d.a.status = (uint32_t)st;
-      d.a.latency_ms = (t_done - take[i].arrival) * 1e3;
-      d.a.batch = batch_no;
-      d.a.batch_size = (uint32_t)n;
-      if (st == STC_OK && !(qs[i].kind & STC_QUERY_COUNT_ONLY)) {
-        if (wrote) {
-          d.contacts.assign(out.begin() + (ptrdiff_t)offsets[i], out.begin() + (ptrdiff_t)offsets[i + 1]);
-          d.a.stored = (uint32_t)d.contacts.size();
-        } else {
-          d.a.status = STC_ERR_CAPACITY;  // the batch's matches exceed its reservation
-        }
-      }
+      ready[i].a.ticket = take[i].ticket;
+      ready[i].a.latency_ms = (t_done - take[i].arrival) * 1e3;
+      ready[i].a.batch = batch_no;
+      ready[i].a.batch_size = (uint32_t)n;
     }
     {
       std::lock_guard<std::mutex> lk(s->mu);
       for (Done &d : ready) s->done.push_back(std::move(d));
+      s->inflight_bytes -= bytes;
       s->stats.answered += n;
       s->stats.batches++;
       s->stats.max_batch_queries = std::max<uint64_t>(s->stats.max_batch_queries, n);
       s->stats.max_batch_bytes = std::max<uint64_t>(s->stats.max_batch_bytes, bytes);
+      s->busy--;
       if (cut) s->stats.budget_cuts++;
     }
     s->cv_out.notify_all();
-    batch_no++;
+    s->cv_in.notify_all();  // memory freed: a waiting worker may admit now
   }
 }
 
@@ -156,11 +210,19 @@ extern "C" stc_status stc_server_start(stc_ctx *ctx, const stc_server_config *cf
   if (!s->cfg.max_batch) s->cfg.max_batch = 4096;
   if (!s->cfg.result_cap) s->cfg.result_cap = 1024;
   if (!s->cfg.hbm_budget) s->cfg.hbm_budget = 64ull << 20;
+  s->chunk = stc::query_chunk(ctx);
+  int started = 0;
   try {
-    s->th = std::thread(serve, s);
+    for (; started < WORKERS; started++) s->th[started] = std::thread(serve, s, started);
   } catch (...) {
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->stopping = true;
+    }
+    s->cv_in.notify_all();
+    for (int i = 0; i < started; i++) s->th[i].join();
     delete s;
-    stc::set_thread_error("stc_server_start: cannot start the serving thread");
+    stc::set_thread_error("stc_server_start: cannot start the serving threads");
     return STC_ERR_STATE;
   }
   *out = s;
@@ -194,9 +256,9 @@ extern "C" stc_status stc_server_poll(stc_server *s, stc_answer *out, size_t cap
     Done &d = s->done.front();
     if (used + d.contacts.size() > contacts_cap) {
       if (*n) break;  // the rest on the next poll
-      d.a.status = STC_ERR_CAPACITY;  // cannot ever fit this poll's buffer
-      d.a.stored = 0;
-      d.contacts.clear();
+      // the first answer alone does not fit: it stays queued for a poll
+      // with a larger contacts buffer (result_cap contacts always suffice)
+      return STC_ERR_CAPACITY;
     }
     d.a.contact_offset = used;
     if (!d.contacts.empty()) std::copy(d.contacts.begin(), d.contacts.end(), contacts + used);
@@ -221,7 +283,8 @@ extern "C" stc_status stc_server_stop(stc_server *s) {
     s->stopping = true;
   }
   s->cv_in.notify_all();
-  if (s->th.joinable()) s->th.join();
+  for (std::thread &t : s->th)
+    if (t.joinable()) t.join();
   delete s;
   return STC_OK;
 }

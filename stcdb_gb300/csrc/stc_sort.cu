@@ -2,11 +2,28 @@
 // CUB/thrust). The reference sorts with thrust::sort_by_key
 // (cuda/geometry.cu:1809-1907); here the partition step uses these kernels
 // to group object ids by quadtree leaf in pid order.
+#include <atomic>
+
 #include "stc_common.cuh"
 
 namespace stc {
 
 thread_local unsigned long long tl_launches = 0;
+
+int num_sms() {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) dev = 0;
+  std::atomic<int> *slot = dev < 64 ? &cache[dev] : nullptr;
+  int v = slot ? slot->load(std::memory_order_relaxed) : 0;
+  if (v > 0) return v;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+    cudaGetLastError();
+    v = 1;  // a device that cannot be asked gets minimal grids (its launches fail on their own)
+  }
+  if (slot) slot->store(v, std::memory_order_relaxed);
+  return v;
+}
 
 static constexpr int SCAN_THREADS = 256;
 static constexpr int SCAN_ITEMS = 8;

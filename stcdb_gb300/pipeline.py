@@ -154,7 +154,7 @@ class _ServerConfig(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_uint64), ("answered", ctypes.c_uint64), ("batches", ctypes.c_uint64),
                 ("max_batch_queries", ctypes.c_uint64), ("max_batch_bytes", ctypes.c_uint64),
-                ("budget_cuts", ctypes.c_uint64)]
+                ("budget_cuts", ctypes.c_uint64), ("overlapped_batches", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {name: int(getattr(self, name)) for name, _ in self._fields_}
@@ -360,8 +360,8 @@ class Pipeline:
         self._check(self._lib.stc_step_device(self._h, ctypes.c_void_p(xy_device_ptr), t))
 
     def step_window(self, xy, t0: int, out: np.ndarray | None = None) -> np.ndarray | None:
-        """Steps t0 .. t0 + len(xy) - 1 replayed from a captured CUDA graph
-        (stc_step_window). xy: a (steps, num_objects, 2) float64 numpy array
+        """Steps t0 .. t0 + len(xy) - 1 as one pipelined window
+        (stc_step_window: step i + 1 queued before step i's state is read). xy: a (steps, num_objects, 2) float64 numpy array
         in host memory, or (device pointer, steps) of that layout in device
         memory. With `out` (a MEETING_DTYPE array) each step's meetings are
         drained into it and the filled part is returned."""
@@ -556,7 +556,8 @@ def meetings_digest(m: np.ndarray) -> str:
 
 class Server:
     """stc_server_*: queries submitted from any thread are answered by the
-    library's serving thread in batches admitted by device footprint; answers
+    library's two worker threads in batches admitted by device footprint
+    (two batches may be on the GPU at once, each on its own stream); answers
     carry the latency from each query's arrival (seconds on the monotonic
     clock, as time.perf_counter on Linux)."""
 

@@ -125,36 +125,75 @@ def test_queries_area_restriction_100_ctfs(built_cuda):
 
 
 def test_queries_while_ingesting(built_cuda):
-    """A second thread queries while the main thread steps and flushes; every
-    call succeeds and object answers only name the object queried."""
+    """A second thread queries while the main thread steps and flushes: every
+    answer equals the oracle's answer over the blocks that existed when the
+    query ran (the blocks flushed before it started, or one or two more when
+    a flush ran meanwhile)."""
+    import oracle as orc
     tc = hotspot_grid(30000, n_hotspots=30, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=7)
     cfg = StcConfig(num_objects=30000, reach_distance=10.0, min_meet_time=3, grid_capacity=50, grid_amplify=1.2,
-                    num_meeting_buckets=1_500_000, kv_restriction=30_000, ctf_count=16, ctb_retain=2)
-    tr, mbr = trace_and_box(tc, 14)
-    errors, answered = [], [0]
+                    num_meeting_buckets=1_500_000, kv_restriction=30_000, ctf_count=16, ctb_retain=32)
+    steps = 14
+    tr, mbr = trace_and_box(tc, steps)
+    # the oracle's blocks, flush by flush
+    ref = orc.Oracle(cfg, mbr, tr[0])
+    lsm = orc.LsmOracle(cfg.num_objects, cfg.max_meet_time, cfg.ctf_count, cfg.area_restriction or 100.0,
+                        cfg.start_time + cfg.min_meet_time, mbr, 1 << 21)
+    blocks = []
+    try:
+        for t in range(steps):
+            lsm.append(ref.step(tr[t], t))
+            if lsm.kv_count() > cfg.kv_restriction:
+                lsm.flush(t)
+                blocks.append(lsm.read())
+    finally:
+        ref.close()
+        lsm.close()
+    assert 2 <= len(blocks) <= 32
+    errors, records = [], []
+    flushed = [0]  # blocks flushed by the steps that have returned
     stop = threading.Event()
     with Pipeline(cfg, mbr, tr[0]) as pipe:
         def worker():
             rng = np.random.default_rng(3)
             while not stop.is_set():
                 try:
-                    pid = int(rng.integers(0, 30000))
-                    r = pipe.query_object(pid)
-                    assert np.all(r["pid"] == pid)
-                    pipe.query_box((mbr[0], mbr[1], mbr[0] + 0.01, mbr[1] + 0.01), 0, 0xFFFFFFFF)
-                    answered[0] += 1
+                    q = np.zeros(1, QUERY_DTYPE)
+                    q["t_start"], q["t_end"] = 0, 0xFFFFFFFF
+                    if rng.random() < 0.5:
+                        q["kind"], q["pid"] = QUERY_OBJECT, int(rng.integers(0, 30000))
+                    else:
+                        x = mbr[0] + rng.random() * (mbr[2] - mbr[0] - 0.003)
+                        y = mbr[1] + rng.random() * (mbr[3] - mbr[1] - 0.003)
+                        q["kind"], q["box"] = QUERY_BOX, (x, y, x + 0.003, y + 0.002)
+                    f0 = flushed[0]
+                    got = pipe.query_batch(q)[0]
+                    records.append((q[0].copy(), got.copy(), f0, flushed[0]))
                 except Exception as e:  # noqa: BLE001 - reported below
                     errors.append(e)
                     return
         th = threading.Thread(target=worker)
         th.start()
         try:
-            for t in range(14):
+            for t in range(steps):
                 pipe.step(tr[t], t)
                 pipe.drain()
+                flushed[0] = pipe.stats().flushes
         finally:
             stop.set()
             th.join()
-        assert pipe.stats().flushes >= 2
+        assert pipe.stats().flushes == len(blocks)
     assert not errors, errors
-    assert answered[0] > 0
+    assert len(records) > 20
+    answered_with_blocks = 0
+    for q, got, f0, f1 in records:
+        g = sort_contacts(got).tobytes()
+        ok = False
+        for f in range(f0, min(f1 + 1, len(blocks)) + 1):
+            want = orc.query_blocks(blocks[:f], q[None])[0] if f else np.zeros(0, got.dtype)
+            if sort_contacts(want).tobytes() == g:
+                ok = True
+                break
+        assert ok, f"query {q} (flushes {f0}..{f1}): {len(got)} contacts match no block set of the oracle"
+        answered_with_blocks += f0 > 0
+    assert answered_with_blocks > 0

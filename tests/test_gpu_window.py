@@ -83,15 +83,69 @@ def test_windows_match_plain_steps(built_cuda, graphs):
             assert ga[k] == pa[k], f"block array {k} differs"
 
 
-def test_window_output_too_small_reports_capacity(built_cuda):
-    from stcdb_gb300.pipeline import StcError
-    tr, mbr = trace_and_box(hotspot_grid(20000, n_hotspots=20, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=4), 12)
-    cfg = StcConfig(num_objects=20000, reach_distance=10.0, min_meet_time=3, grid_capacity=50,
-                    num_meeting_buckets=1_000_000)
+def _plain_run(cfg, tr, mbr, steps):
     p = Pipeline(cfg, mbr, tr[0])
     try:
-        with pytest.raises(StcError) as e:
-            p.step_window(np.ascontiguousarray(tr, dtype=np.float64), 0, np.empty(1, MEETING_DTYPE))
-        assert e.value.status == 3  # STC_ERR_CAPACITY
+        got = []
+        for t in range(steps):
+            p.step(tr[t], t)
+            got.append(p.drain().copy())
+        return got
     finally:
         p.close()
+
+
+def test_window_output_too_small_reports_capacity(built_cuda):
+    """A full output buffer stops the window with STC_ERR_CAPACITY; the
+    context stays usable, the meetings that did not fit stay pending, and
+    everything equals plain steps up to the last step that ran."""
+    from stcdb_gb300.pipeline import StcError
+    tr, mbr = trace_and_box(hotspot_grid(20000, n_hotspots=20, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=4), 12)
+    tr = np.ascontiguousarray(tr, dtype=np.float64)
+    cfg = StcConfig(num_objects=20000, reach_distance=10.0, min_meet_time=3, grid_capacity=50,
+                    num_meeting_buckets=1_000_000)
+    plain = _plain_run(cfg, tr, mbr, 12)
+    cum = np.cumsum([len(m) for m in plain])
+    fill = int(np.argmax(cum > 1))  # the step whose meetings overflow a one-record buffer
+    assert cum[fill] > 1
+    p = Pipeline(cfg, mbr, tr[0])
+    try:
+        out = np.empty(1, MEETING_DTYPE)
+        with pytest.raises(StcError) as e:
+            p.step_window(tr, 0, out)
+        assert e.value.status == 3  # STC_ERR_CAPACITY
+        last = p.stats().step
+        assert fill <= last <= fill + 1  # at most one step beyond the one that filled the buffer
+        rest = p.drain()
+        got = np.concatenate([out[:1], rest])
+        want = np.concatenate(plain[:last + 1])
+        assert np.array_equal(_rows(got), _rows(want))
+        # the context goes on: the remaining steps equal the plain run's
+        more = p.step_window(tr[last + 1:], last + 1, np.empty(2_000_000, MEETING_DTYPE))
+        assert np.array_equal(_rows(more), _rows(np.concatenate(plain[last + 1:])))
+    finally:
+        p.close()
+
+
+@pytest.mark.parametrize("graphs", [1, 2])
+def test_window_small_emit_buffer(built_cuda, graphs):
+    """A window whose emit buffer passes half full holds the pipeline for a
+    step and empties the buffer; the meetings equal the plain run's."""
+    from dataclasses import replace
+    steps = 20
+    tr, mbr = trace_and_box(hotspot_grid(30000, n_hotspots=30, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=6),
+                            steps)
+    tr = np.ascontiguousarray(tr, dtype=np.float64)
+    cfg = StcConfig(num_objects=30000, reach_distance=10.0, min_meet_time=3, grid_capacity=50, grid_amplify=1.2,
+                    num_meeting_buckets=1_500_000, kv_restriction=40_000, ctf_count=16)
+    plain = _plain_run(cfg, tr, mbr, steps)
+    peak = max(len(m) for m in plain)
+    assert peak > 0
+    small = replace(cfg, emit_capacity=3 * peak, window_graphs=graphs)
+    p = Pipeline(small, mbr, tr[0])
+    try:
+        got = p.step_window(tr, 0, np.empty(2_000_000, MEETING_DTYPE)).copy()
+        assert p.stats().pending == 0
+    finally:
+        p.close()
+    assert np.array_equal(_rows(got), _rows(np.concatenate(plain)))

@@ -1,7 +1,7 @@
 """stc_sort_pairs_u32_noalloc (fixed library-owned scratch, no device
-allocation) against stc_sort_pairs_u32 (allocating) on the same inputs: two
-calls in a row with different inputs, so the second runs on scratch the
-first left behind. Kept in a file collected last."""
+allocation) against stc_sort_pairs_u32 (allocating) and numpy's stable sort
+on the same inputs: two calls in a row with different inputs, so the second
+runs on scratch the first left behind. Kept in a file collected last."""
 import ctypes
 
 import numpy as np
@@ -45,9 +45,14 @@ def test_noalloc_sort_matches_allocating_sort_twice(built_cuda):
         st_r, k_r, v_r = _sort(ref, keys, vals, bits)
         st_n, k_n, v_n = _sort(na, keys, vals, bits)
         assert st_r == 0 and st_n == 0, lib.stc_last_error(None)
-        # integer sort: bit-exact
+        # integer sort: bit-exact, against the allocating sort and against
+        # numpy's stable sort on the masked keys
         assert np.array_equal(k_n, k_r)
         assert np.array_equal(v_n, v_r)
+        mask = np.uint32((1 << bits) - 1) if bits < 32 else np.uint32(0xFFFFFFFF)
+        order = np.argsort(keys & mask, kind="stable")
+        assert np.array_equal(k_n, keys[order])
+        assert np.array_equal(v_n, vals[order])
 
 
 def test_noalloc_sort_rejects_more_than_its_scratch_holds(built_cuda):
