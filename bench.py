@@ -33,10 +33,11 @@ queries_under_ingest: K more steps (host input) while a serving thread answers
   a Poisson query stream (default 20,000/s; 60% object, 40% box queries) over
   the flushed block by continuous batching; queries return match counts, as
   the reference's searches do; p50/p99 latency from arrival.
-batched: uneven ingest windows (1M-3M objects, 0/30% hotspot, reach 5/10 m,
-  10-30 steps) run as plain steps and as graph-replayed windows
-  (stc_step_window) from fresh contexts: both rates, the speed-up and whether
-  the two emitted the same meetings (--no-batched skips it and autotune).
+batched: 64 uneven ingest windows (1M-20M objects log-uniform, 10-50 steps,
+  reach 5/10/20 m, 0-90% hotspot, lowered where the table would not fit) run
+  as plain steps and as pipelined windows (stc_step_window) from fresh
+  contexts: both rates, the speed-up and whether the two emitted the same
+  meetings (--no-batched skips it and autotune).
 autotune: stc_autotune on the hotspot-1M model: the leaf capacity and launch
   shape it picks and the device time per step before and after.
 sort: the library's radix sort on 100M random 32-bit pairs.
@@ -359,9 +360,12 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
     (stc_server_*), which answers them by continuous batching (whatever has
     arrived while a batch ran forms the next batch, admitted by device
     footprint). Latency = answer time - arrival time, both on the monotonic
-    clock. The main thread keeps stepping meanwhile (host input)."""
-    from stcdb_gb300.pipeline import QUERY_COUNT_ONLY
+    clock. The main thread keeps stepping meanwhile (host input). Object
+    queries return their contacts (who met the object, up to result_cap
+    each); box queries return match counts, as the reference's searches do."""
+    from stcdb_gb300.pipeline import QUERY_BOX, QUERY_COUNT_ONLY
     rng = np.random.default_rng(12345)
+    result_cap = 4096
     rate = float(args.query_rate)
     answers = []
     lags = []  # submit time - arrival time per query (the submitting thread's delay)
@@ -369,7 +373,14 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
     cur_t = [t0 - 1]
     done = threading.Event()
     errors = []
-    srv = pipe.server(max_batch=4096, result_cap=1024, hbm_budget=64 << 20)
+    srv = pipe.server(max_batch=4096, result_cap=result_cap, hbm_budget=64 << 20)
+    stored = [0]  # contacts returned to the bench
+
+    def take(cap, wait_ms):
+        a, c = srv.poll(cap=cap, contacts_cap=1 << 22, wait_ms=wait_ms)
+        if len(a):
+            answers.append(a)
+            stored[0] += int(a["stored"].sum())
 
     def server():
         next_arrival = time.perf_counter() + rng.exponential(1.0 / rate)
@@ -380,13 +391,11 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
                 arrivals.append(next_arrival)
                 next_arrival += rng.exponential(1.0 / rate)
             if not arrivals:
-                a, _ = srv.poll(cap=8192, wait_ms=0)
-                if len(a):
-                    answers.append(a)
+                take(8192, 0)
                 time.sleep(min(max(next_arrival - time.perf_counter(), 0.0), 0.0005))
                 continue
             qs = make_queries(rng, len(arrivals), N, mbr, cur_t[0])
-            qs["kind"] |= QUERY_COUNT_ONLY
+            qs["kind"] = np.where(qs["kind"] == QUERY_BOX, QUERY_BOX | QUERY_COUNT_ONLY, qs["kind"])
             try:
                 for q, t_arr in zip(qs, arrivals):
                     arrived[srv.submit(q[None], arrival=t_arr)] = t_arr
@@ -413,9 +422,7 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
     # the rest of what was submitted, then the loop's statistics
     deadline = time.perf_counter() + 30.0
     while sum(len(a) for a in answers) < srv.stats().submitted and time.perf_counter() < deadline:
-        a, _ = srv.poll(cap=65536, wait_ms=100)
-        if len(a):
-            answers.append(a)
+        take(65536, 100)
     sst = srv.stats()
     srv.stop()
     gc.enable()
@@ -423,8 +430,11 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
     if errors:
         return {"error": errors[0]}
     ans = np.concatenate(answers) if answers else np.zeros(0)
-    if len(ans) and (ans["status"] != 0).any():
-        return {"error": f"{int((ans['status'] != 0).sum())} queries failed"}
+    # an object query with more than result_cap contacts is answered with its
+    # count and STC_ERR_CAPACITY; any other status is a failure
+    over_cap = int((ans["status"] == 3).sum()) if len(ans) else 0
+    if len(ans) and ((ans["status"] != 0) & (ans["status"] != 3)).any():
+        return {"error": f"{int(((ans['status'] != 0) & (ans['status'] != 3)).sum())} queries failed"}
     lat_ms = ans["latency_ms"] if len(ans) else np.zeros(0)
     sizes = np.bincount(ans["batch"]) if len(ans) else np.zeros(0)
     # where the slowest answers come from: their batch (size, latency spread:
@@ -456,12 +466,15 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
             "slowest_batch": worst,
             "submit_lag_ms": {"p99": float(np.percentile(lag_ms, 99)) if len(lag_ms) else None,
                               "max": float(lag_ms.max()) if len(lag_ms) else None},
-            "contacts_per_query": float(ans["count"].mean()) if len(ans) else 0.0,
-            "server": {"loop": "stc_server (library thread, continuous batching)", "max_batch": 4096,
+            "matches_per_query": float(ans["count"].mean()) if len(ans) else 0.0,
+            "contacts_returned": stored[0], "object_queries_over_result_cap": over_cap,
+            "server": {"loop": "stc_server (two library worker threads, continuous batching, two query "
+                               "streams)", "max_batch": 4096, "result_cap": result_cap,
                        "hbm_budget_bytes": 64 << 20, "max_batch_queries": int(sst.max_batch_queries),
-                       "max_batch_bytes": int(sst.max_batch_bytes), "budget_cuts": int(sst.budget_cuts)},
-            "mix": "60% object (window 10-10000 steps), 40% box (50 m-5 km, window 10-3600 steps); "
-                   "match counts, as the reference's searches return",
+                       "max_batch_bytes": int(sst.max_batch_bytes), "budget_cuts": int(sst.budget_cuts),
+                       "overlapped_batches": int(sst.overlapped_batches)},
+            "mix": "60% object queries returning contacts (meets-whom, window 10-10000 steps), 40% box "
+                   "queries returning match counts (50 m-5 km, window 10-3600 steps)",
             "blocks": 1, "step_slices": args.serve_slices, "ingest_pos_updates_per_s": N * steps / wall,
             "ingest_device_ms_per_step": float(np.mean(step_ms))}
 
@@ -541,70 +554,146 @@ def sort_line(device, peak, n=100_000_000, reps=5):
             "achieved_gbs": b / (ms / 1e3) / 1e9, "frac_of_peak": b / (ms / 1e3) / 1e9 / peak, "sorted": ok}
 
 
-def batched_line(device, windows=4, seed=7):
-    """Uneven ingest windows: each window (seeded object count 1M-3M, 0 or
-    30% of objects in hotspots, reach 5 or 10 m, 10-30 steps) runs twice from
-    fresh contexts, as plain steps (stc_step_device: one launch per kernel)
-    and as one stc_step_window call (each step replayed from a captured CUDA
-    graph), positions resident in HBM and meetings drained into a page-locked
-    buffer every step in both. Both runs must emit the same meetings (sorted
-    sets compared); times are wall-clock from the first step to the last
-    drain."""
-    import numpy as np
+def _live_estimate(n, hot, reach):
+    """Live meeting pairs per step of the grid-graph walker on the 40 km map:
+    6.7 per object at 10M uniform objects and reach 10 m (measured), growing
+    with the density (N) and the reach disc (reach^2); a hotspot share h
+    multiplies it by 1 + 104 h^2 (3.5e7 live pairs measured at 1M objects
+    with h = 0.7, against 6.7e5 uniform)."""
+    return 6.7 * n * (n / 1e7) * (reach / 10.0) ** 2 * (1.0 + 104.0 * hot * hot)
+
+
+def _meeting_checksum(buf, k, device):
+    """(count, order-independent 64-bit checksum) of meetings buf[:k]:
+    every 32-byte record hashed as four 64-bit words, the hashes summed with
+    wrap-around, on the GPU."""
     import torch
-    from stcdb_gb300.pipeline import MEETING_DTYPE, Pipeline, StcConfig
+    if k == 0:
+        return 0, 0
+    w = torch.from_numpy(np.ascontiguousarray(buf[:k]).view(np.int64).reshape(-1, 4)).to(f"cuda:{device}")
+    c = torch.tensor([-7046029254386353131, -4658895280553007687, 7640891576956012809, -2398030916697513551],
+                     dtype=torch.int64, device=w.device)
+    h = w * c
+    x = h[:, 0] ^ (h[:, 1] >> 17) ^ (h[:, 2] << 13) ^ (h[:, 3] >> 29)
+    x = x * -7046029254386353131
+    x = x ^ (x >> 31)
+    return k, int(x.sum().item())
+
+
+def batched_line(device, windows=64, seed=7, live_cap=1.2e8):
+    """Uneven ingest windows of the batching configuration: `windows` windows,
+    each with a seeded object count log-uniform in 1M-20M, 10-50 steps, a
+    reach from {5, 10, 20} m and a share of objects in the 1000-hotspot model
+    uniform in 0-90%. Where a window's expected live pairs (_live_estimate)
+    would exceed live_cap the hotspot share is lowered (and, for the largest
+    windows, the reach), which the line reports per window: the full
+    configuration at 20M objects, 90% in hotspots and 20 m holds ~10^11 live
+    pairs, more than any table in HBM. Each window runs twice from fresh
+    contexts with positions in HBM: as plain steps (stc_step_device and a
+    drain per step; the host waits for every step) and as pipelined
+    stc_step_window calls (step i + 1 queued before step i's state is read;
+    steps of up to 2M objects replayed from captured graphs), both draining
+    into one page-locked buffer. The two runs must emit the same meetings:
+    their counts and order-independent checksums (_meeting_checksum) are
+    compared. Times are wall-clock over the steps and drains, checksums
+    excluded."""
+    import torch
+    from stcdb_gb300.pipeline import MEETING_DTYPE, Pipeline, StcConfig, StcError
     from stcdb_gb300.tracegen import DeviceTraceGenerator, hotspot_grid, uniform_grid
     rng = np.random.default_rng(seed)
-    cap = 16_000_000
+    cap = 48_000_000
     pinned = torch.empty(cap * MEETING_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
     buf = pinned.numpy().view(MEETING_DTYPE)
     per, same, pos, secs = [], True, 0, {"plain": 0.0, "window": 0.0}
     for w in range(windows):
-        n = int(round(10 ** rng.uniform(6.0, np.log10(3e6))))
-        hot = 0.3 if w % 2 else 0.0
-        reach = float(rng.choice([5.0, 10.0]))
-        steps = int(rng.integers(10, 31))
-        tcfg = hotspot_grid(n, hot_frac=hot, seed=seed + w) if hot else uniform_grid(n, seed=seed + w)
+        n = int(round(10 ** rng.uniform(6.0, np.log10(2e7))))
+        steps = int(rng.integers(10, 51))
+        reach = float(rng.choice([5.0, 10.0, 20.0]))
+        hot = float(rng.uniform(0.0, 0.9))
+        want = (reach, hot)
+        while _live_estimate(n, 0.0, reach) > live_cap and reach > 5.0:
+            reach /= 2
+        if _live_estimate(n, hot, reach) > live_cap:
+            base = _live_estimate(n, 0.0, reach)
+            hot = float(np.sqrt(max(live_cap / base - 1.0, 0.0) / 104.0))
+        live = _live_estimate(n, hot, reach)
+        B = 1 << max(22, int(np.ceil(np.log2(3.0 * live + 1))))
+        tcfg = hotspot_grid(n, hot_frac=hot, seed=seed + w) if hot > 0.005 else uniform_grid(n, seed=seed + w)
         gen = DeviceTraceGenerator(tcfg, device)
         mbr = gen.map_box(100.0)
         xy = torch.empty((steps, n, 2), dtype=torch.float64, device=f"cuda:{device}")
         gen.next_into(xy.data_ptr(), steps)
         gen.close()
-        cfg = StcConfig(num_objects=n, reach_distance=reach, min_meet_time=5, grid_capacity=200, grid_amplify=4.0,
-                        num_meeting_buckets=1 << 28, device=device)
+        cfg = StcConfig(num_objects=n, reach_distance=reach, min_meet_time=5, grid_capacity=200, grid_amplify=8.0,
+                        num_meeting_buckets=B, emit_capacity=max(4 * n, int(0.25 * live) + (1 << 22)),
+                        device=device)
         x0 = xy[0].cpu().numpy()
-        rows, rate = {}, {}
+        sums, rate, calls = {}, {}, 0
         for mode in ("plain", "window"):
             p = Pipeline(cfg, mbr, x0)
+            cnt, chk, fill, elapsed = 0, 0, 0, 0.0
+
+            def settle():
+                nonlocal cnt, chk, fill
+                a, b = _meeting_checksum(buf, fill, device)
+                cnt, chk, fill = cnt + a, (chk + b) & 0xFFFFFFFFFFFFFFFF, 0
+
             torch.cuda.synchronize(device)
-            t0 = time.perf_counter()
             if mode == "plain":
-                k = 0
                 for t in range(steps):
+                    t0 = time.perf_counter()
                     p.step_device(xy[t].data_ptr(), t)
-                    k += len(p.drain(out=buf[k:]))
+                    while True:
+                        fill += len(p.drain_some(buf[fill:]))
+                        if not p.stats().pending:
+                            break
+                        elapsed += time.perf_counter() - t0
+                        settle()
+                        t0 = time.perf_counter()
+                    elapsed += time.perf_counter() - t0
+                    if fill > cap // 2:
+                        settle()
             else:
-                k = len(p.step_window((xy.data_ptr(), steps), 0, buf))
-            dt = time.perf_counter() - t0
+                t = 0
+                while t < steps:
+                    t0 = time.perf_counter()
+                    try:
+                        fill += len(p.step_window((xy[t].data_ptr(), steps - t), t, buf[fill:]))
+                        t = steps
+                    except StcError as e:
+                        if e.status != 3:  # only a full output buffer is expected
+                            raise
+                        t = int(p.stats().step) + 1  # the steps that ran; their undrained meetings wait
+                        fill = cap  # the call filled the buffer
+                    elapsed += time.perf_counter() - t0
+                    calls += 1
+                    if fill > cap // 2 or t < steps:
+                        settle()
+                        while p.stats().pending:
+                            fill += len(p.drain_some(buf[fill:]))
+                            settle()
+            settle()
             p.close()
-            a = np.ascontiguousarray(buf[:k]).view(np.uint32).reshape(-1, 8)
-            rows[mode] = a[np.lexsort(a.T[::-1])] if k else a
-            rate[mode] = n * steps / dt
-            secs[mode] += dt
-        same &= np.array_equal(rows["plain"], rows["window"])
+            sums[mode] = (cnt, chk)
+            rate[mode] = n * steps / elapsed
+            secs[mode] += elapsed
+        same &= sums["plain"] == sums["window"]
         pos += n * steps
-        per.append({"objects": n, "hot_frac": hot, "reach_m": reach, "steps": steps, "meetings": len(rows["plain"]),
-                    "plain_pos_per_s": rate["plain"], "window_pos_per_s": rate["window"]})
+        per.append({"objects": n, "steps": steps, "hot_frac": round(hot, 4), "reach_m": reach,
+                    "drawn": {"reach_m": want[0], "hot_frac": round(want[1], 4)}, "table_slots": B,
+                    "meetings": sums["plain"][0], "same": sums["plain"] == sums["window"],
+                    "plain_pos_per_s": rate["plain"], "window_pos_per_s": rate["window"], "window_calls": calls})
         del xy
-    return {"windows": per, "plain_pos_per_s": pos / secs["plain"], "window_pos_per_s": pos / secs["window"],
-            "speedup": secs["plain"] / secs["window"], "same_meetings": bool(same),
-            "unit": "pos-updates/s"}
+    return {"windows": len(per), "plain_pos_per_s": pos / secs["plain"], "window_pos_per_s": pos / secs["window"],
+            "speedup": secs["plain"] / secs["window"], "same_meetings": bool(same), "unit": "pos-updates/s",
+            "per_window": per}
 
 
 def tune_line(device, steps=8):
     """stc_autotune on the hotspot-1M model (1M objects, 70% in 1000 Zipf
-    hotspots): leaf capacity among 50/100/200 (the workload's own 200 is the
-    base) and the refinement launch shape, scored on device time per step."""
+    hotspots): leaf capacity among 64/128/256/512 (the workload's own 200 is
+    the base) and the refinement launch shape, scored on device time per
+    step."""
     import numpy as np
     from stcdb_gb300.pipeline import autotune
     from stcdb_gb300.tracegen import TraceGenerator
@@ -614,7 +703,7 @@ def tune_line(device, steps=8):
     xy = np.stack([g.next() for _ in range(steps)])
     g.close()
     cfg = make_cfg(w, device=device)
-    chosen, rep = autotune(cfg, mbr, xy, capacities=[50, 100, 200])
+    chosen, rep = autotune(cfg, mbr, xy, capacities=[64, 128, 256, 512])
     return {"workload": "hotspot-1M", "steps": steps, "base_grid_capacity": cfg.grid_capacity,
             "grid_capacity": chosen.grid_capacity, "job_chunk": chosen.job_chunk,
             "refine_blocks_per_sm": chosen.refine_blocks_per_sm, "hits_blocks_per_sm": chosen.hits_blocks_per_sm,
@@ -634,22 +723,29 @@ def compaction_line(c, peak):
     return c
 
 
-def cpu_baseline(w, steps, threads, sample_note):
+def cpu_baseline(w, warmup, steps, threads, sample_note):
+    """The oracle's C restatement of the reference CPU path on `threads` host
+    threads: steps 0..warmup-1 untimed, then steps warmup..warmup+steps-1
+    timed (the step indices the GPU arm times)."""
     import oracle
     from stcdb_gb300.tracegen import TraceGenerator
     gen = TraceGenerator(make_trace_cfg(w, seed=1))
     mbr = gen.map_box(100.0)
-    xs = [gen.next().copy() for _ in range(steps + 1)]
+    x0 = gen.next().copy()
     cfg = make_cfg(w)
-    o = oracle.Oracle(cfg, mbr, xs[0], threads=threads)
-    o.step(xs[0], 0)  # first step: every pair is new
+    o = oracle.Oracle(cfg, mbr, x0, threads=threads)
+    o.step(x0, 0)
+    for t in range(1, warmup):
+        o.step(gen.next(), t)
+    xs = [gen.next().copy() for _ in range(steps)]
     t0 = time.perf_counter()
-    for t in range(1, steps + 1):
-        o.step(xs[t], t)
+    for k in range(steps):
+        o.step(xs[k], warmup + k)
     dt = time.perf_counter() - t0
     o.close()
+    gen.close()
     return {"value": w["objects"] * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": sample_note.format(steps=steps, seconds=round(dt, 2))}
+            "sample": sample_note.format(steps=steps, first=warmup, last=warmup + steps - 1, seconds=round(dt, 2))}
 
 
 def main():
@@ -694,11 +790,11 @@ def main():
         if rank != 0:
             return
         steps = args.steps
-        base = cpu_baseline(w, steps, threads,
-                            "oracle C port of the reference CPU path, {steps} full steps after one "
-                            "warm-up step ({seconds} s)")
+        base = cpu_baseline(w, args.warmup, steps, threads,
+                            "oracle C port of the reference CPU path, all host threads, steps {first}-{last} "
+                            "({steps} full steps) after the warm-up steps ({seconds} s)")
         line = {"metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": ws, "steps": steps,
-                "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "warmup": args.warmup, "ms_per_step": 1e3 * N / base["value"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64", "data": "synthetic (seeded grid-graph traces)", "impl": "reference",
                 "config": workload_cfg, "cpu_baseline": base,
                 "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -724,7 +820,7 @@ def main():
     launches = sum(s.kernel_launches for s in r["stats"])
     base = None
     if not args.no_cpu_baseline:
-        base = cpu_baseline(w, args.cpu_steps, threads,
+        base = cpu_baseline(w, 1, args.cpu_steps, threads,
                             "oracle C port of the reference CPU path, all host threads, {steps} full steps "
                             "of the same workload after one warm-up step ({seconds} s)")
     line = {
@@ -759,6 +855,13 @@ def main():
         "clocks": r["clocks"],
         "cpu_baseline": base,
     }
+    # the figures a reader of the line's tail needs, repeated last
+    q = r["queries"] or {}
+    line["summary"] = {"value": value, "e2e": e2e, "bit_exact": line["bit_exact"],
+                       "query_p50_ms": q.get("p50_ms"), "query_p99_ms": q.get("p99_ms"),
+                       "query_max_ms": q.get("max_ms"), "queries_per_s": q.get("qps"),
+                       "ingest_pos_updates_per_s_while_serving": q.get("ingest_pos_updates_per_s"),
+                       "roofline_frac": line["roofline"]["frac"]}
     print(json.dumps(line), flush=True)
 
 

@@ -100,7 +100,8 @@ typedef struct stc_config {
   /* Launch shape of the refinement (stc_autotune picks it; results do not
    * depend on it: new meetings take their slots by priority, not by
    * arrival). */
-  uint32_t job_chunk;            /* 32x32 pair tiles a warp takes at a time; 0 = 8, at most 64 */
+  uint32_t job_chunk;            /* refinement jobs (32 rows against their candidate ranges) a warp
+                                    takes at a time; 0 = 8, at most 64 */
   uint32_t refine_blocks_per_sm; /* pair-test blocks launched per SM; 0 = 8, at most 32 */
   uint32_t hits_blocks_per_sm;   /* table-update blocks launched per SM; 0 = 16, at most 64 */
   uint32_t window_graphs;        /* stc_step_window replays each step from a captured CUDA graph:

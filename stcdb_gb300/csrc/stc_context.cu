@@ -383,6 +383,8 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
             dalloc(c, &p.hit_bounds, STC_MAX_PARTS + 1) &&
             dalloc(c, &p.sort_hist2, radix_hist_words(nu)) && dalloc(c, &p.scan_tmp2, scan_words) &&
             dalloc(c, &p.grid_start, (size_t)p.G + 1) && dalloc(c, &p.pts, n) && dalloc(c, &p.fxy, n) &&
+            dalloc(c, &p.spts, n) && dalloc(c, &p.sorig, n) && dalloc(c, &p.shi, n) &&
+            dalloc(c, &p.lstrip, p.G) &&
             dalloc(c, &p.bcount, (size_t)n + 1) && dalloc(c, &p.boff, (size_t)n + 1) &&
             dalloc(c, &p.blist, n) && dalloc(c, &p.bres, 4 * (size_t)n) && dalloc(c, &p.sd.fbox, p.S) &&
             dalloc(c, &p.bu_gid, p.U_cap) && dalloc(c, &p.bu_pid, p.U_cap) && dalloc(c, &p.bu_sorted_gid, p.U_cap) &&
@@ -519,6 +521,7 @@ static void issue_step(stc_ctx *c, bool events, bool append, const uint32_t *two
   step_border(p, c->side);
   cudaEventRecord(c->join2_ev, c->side);
   step_leaf_order(p, s);
+  step_strips(p, s);
   if (events) cudaEventRecord(c->ev[PH_PART], s);
   cudaStreamWaitEvent(s, c->join2_ev, 0);
   step_jobs(p, s);

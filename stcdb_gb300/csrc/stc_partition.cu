@@ -8,6 +8,8 @@
 //               insert fills grids[] (tracing/filter.cpp:95-111)
 //   k_gather    leaf-ordered copy of the points as fp32 offsets from the leaf
 //               corner (for the refinement pre-filter) and fp32 lon/lat (MBR)
+//   k_strip_order  each leaf's kept members again in strip order (strips at
+//               least reach tall), the refinement's candidate ranges
 //   k_border    depth-first lookup of the top/right leaves within reach of a
 //               border point (tracing/filter.cpp:130-152), counted then filled
 //               in the reference's unit order (pid, then DFS order)
@@ -69,6 +71,78 @@ __global__ void k_gather(PipeDev p) {
   float2 f = make_float2(__double2float_rn(q.x), __double2float_rn(q.y));
   p.pts[i] = make_float4(lx, ly, metres_per_deg_lon_f(q.y), __uint_as_float(pid));
   p.fxy[pid] = f;
+}
+
+// Strip order of each leaf's kept members, for the refinement's candidate
+// ranges. The leaf is cut into H horizontal strips (H <= STRIPS_MAX) at
+// least s_min metres tall, s_min a little above reach. The reference's
+// distance takes dy / dpm_lat, a constant scale, so two members within reach
+// lie at most one strip apart: the candidates of a member are the members of
+// its own strip and the two beside it, one contiguous range in strip order.
+// Strip coordinates are computed in fp32 from the members' leaf offsets ly;
+// s_min covers their rounding (u * leaf height) and the product's with wide
+// margins (1e-4 relative plus 1e-6 of the leaf height plus 1 mm).
+// One warp per leaf: a counting sort by strip in shared memory (the order
+// within a strip does not matter: each pair is tested once, by its member
+// earlier in strip order, and its priority comes from the pid-order index).
+static constexpr uint32_t STRIPS_MAX = 64;
+
+__device__ __forceinline__ uint32_t member_strip(float ly, float inv, uint32_t H) {
+  float c = floorf(ly * inv);
+  c = fminf(fmaxf(c, 0.0f), (float)(H - 1));
+  return (uint32_t)c;
+}
+
+__global__ void __launch_bounds__(256) k_strip_order(PipeDev p) {
+  __shared__ uint32_t hist_all[8][STRIPS_MAX + 1];
+  const uint32_t lane = lane_id(), wid = threadIdx.x >> 5;
+  uint32_t *hist = hist_all[wid];
+  uint32_t *tmp = p.sort_ktmp;  // (strip << 16 | rank within strip) per member in pid order
+  const uint32_t nw = gridDim.x * 8;
+  for (uint32_t g = blockIdx.x * 8 + wid; g < p.G; g += nw) {
+    const uint32_t cnt = p.grid_count[g];
+    const uint32_t n = cnt < p.leaf_cap ? cnt : p.leaf_cap;
+    if (n == 0) continue;
+    const uint32_t base = p.grid_start[g];
+    const Node *o = &p.sd.nodes[p.sd.gid_node[g]];
+    const double h_deg = RN_SUB(o->hi_y, o->lo_y);
+    const float h_m = (float)h_deg * STC_SLAT_F;
+    const float s_min = (float)p.reach * 1.0001f + 1e-6f * h_m + 1e-3f;
+    float hf = floorf(h_m / s_min);
+    const uint32_t H = hf < 1.0f ? 1u : (hf > (float)STRIPS_MAX ? STRIPS_MAX : (uint32_t)hf);
+    const float inv = H > 1 ? (float)H / (float)h_deg : 0.0f;  // strips per degree from the low edge
+    for (uint32_t k = lane; k <= STRIPS_MAX; k += 32) hist[k] = 0;
+    __syncwarp();
+    for (uint32_t i = lane; i < n; i += 32) {
+      const uint32_t sidx = member_strip(p.pts[base + i].y, inv, H);
+      tmp[base + i] = sidx << 16 | atomicAdd(&hist[sidx], 1u);
+    }
+    __syncwarp();
+    // exclusive scan of the H <= 64 strip counts, two per lane
+    const uint32_t v0 = hist[2 * lane], v1 = hist[2 * lane + 1];
+    uint32_t x = v0 + v1;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+      if ((int)lane >= d) x += y;
+    }
+    x -= v0 + v1;
+    __syncwarp();
+    hist[2 * lane] = x;
+    hist[2 * lane + 1] = x + v0;
+    __syncwarp();
+    if (lane == 0) hist[H] = n;
+    __syncwarp();
+    for (uint32_t i = lane; i < n; i += 32) {
+      const uint32_t u = tmp[base + i], sidx = u >> 16;
+      const uint32_t k = hist[sidx] + (u & 0xFFFFu);
+      p.spts[base + k] = p.pts[base + i];
+      p.sorig[base + k] = i | sidx << 16;
+      p.shi[base + k] = hist[sidx + 2 < H ? sidx + 2 : H];
+    }
+    if (lane == 0) p.lstrip[g] = make_float2(inv, (float)H);
+    __syncwarp();
+  }
 }
 
 // box::distance(p, geography=true) <= reach (geometry/geometry.h:174-185),
@@ -215,8 +289,8 @@ __global__ void k_jobs(PipeDev p) {
   uint32_t n = cnt < p.leaf_cap ? cnt : p.leaf_cap;
   if (cnt > p.leaf_cap) atomicAdd(&p.st->overflow_objects, cnt - p.leaf_cap);
   uint32_t m = p.bu_cnt[g];
-  uint32_t R = (n + 31) / 32;
-  uint32_t jobs = n ? R * (R + 1) / 2 + ((m + 31) / 32) * R : 0;
+  // one job: 32 members (strip order) or 32 border units against their candidate ranges
+  uint32_t jobs = n ? (n + 31) / 32 + (m + 31) / 32 : 0;
   p.job_cnt[g] = jobs;
 }
 
@@ -233,6 +307,10 @@ void step_leaf_order(PipeDev &p, cudaStream_t s) {
                  p.sort_hist, p.scan_tmp, s);
   exclusive_scan_u32(p.grid_count, p.grid_start, (size_t)p.G + 1, nullptr, p.scan_tmp, s);
   STC_KL k_gather<<<nblk(p.N), 256, 0, s>>>(p);
+}
+
+void step_strips(PipeDev &p, cudaStream_t s) {
+  STC_KL k_strip_order<<<num_sms() * 8, 256, 0, s>>>(p);
 }
 
 void step_border(PipeDev &p, cudaStream_t s) {

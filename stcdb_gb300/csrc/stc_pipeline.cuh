@@ -33,6 +33,14 @@ struct PipeDev {
   uint32_t *grid_count, *grid_start;   // G, G+1
   float4 *pts;                          // N sorted: lx, ly, metres/deg lon, pid bits
   float2 *fxy;                          // N by pid: float lon, lat (MBR of new meetings)
+  // each leaf's kept members again, ordered by horizontal strip (strips at
+  // least reach tall): spts as pts; sorig = member index in pid order |
+  // strip << 16; shi = end (within the leaf) of the strip above the
+  // member's; lstrip[g] = (strips per degree of latitude from the leaf's
+  // low corner, strip count)
+  float4 *spts;
+  uint32_t *sorig, *shi;
+  float2 *lstrip;
   // border units
   uint32_t *bcount, *boff;              // N+1 (border units per pid, exclusive offsets)
   uint32_t *blist;                      // N: pids of border points (any order)
@@ -62,6 +70,8 @@ struct PipeDev {
 // candidates), then the leaf-order sort, leaf starts and gathered points
 void step_descend(PipeDev &p, cudaStream_t s);
 void step_leaf_order(PipeDev &p, cudaStream_t s);
+// each leaf's members in strip order (after step_leaf_order)
+void step_strips(PipeDev &p, cudaStream_t s);
 void step_border(PipeDev &p, cudaStream_t s);
 void step_jobs(PipeDev &p, cudaStream_t s);
 // stc_refine.cu

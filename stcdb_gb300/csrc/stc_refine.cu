@@ -1,12 +1,19 @@
 // Step kernel (b): proximity refinement fused with the first pass of the
 // meeting-table insert.
 //
-// Work tiles: for every leaf with n kept members (the first leaf_cap in pid
-// order, tracing/filter.cpp:100-104) the own-leaf pairs i < j form the upper
-// triangle of a 32 x 32 tiling, and the border units that target the leaf
-// (pid outside the leaf, tracing/filter.cpp:248-259) form extra row tiles
-// against all members. One warp runs one tile: rows in lanes, the 32 column
-// points broadcast with shuffles.
+// Work: every leaf's n kept members (the first leaf_cap in pid order,
+// tracing/filter.cpp:100-104) are ordered by horizontal strips at least
+// reach tall (stc_partition.cu, k_strip_order), so a pair within reach lies
+// in one strip or two adjacent ones. The reference tests every own-leaf pair
+// (pid < q, tracing/refinement.cpp:30) and every (border unit, member) pair
+// of the leaf (tracing/filter.cpp:248-259); pairs more than a strip apart are
+// farther than reach, so only the pairs in a member's candidate range -- the
+// members after it in strip order up to the end of the next strip, or for a
+// border unit the members of the strips beside its point -- can hit, and
+// only those are tested. A job is 32 rows (members or border units) of one
+// leaf, one per lane, each over its own contiguous candidate range. Each hit
+// keeps the reference's priority: the finding unit's rank and the member's
+// index in pid order.
 //
 // Distance decisions equal the reference's fp64 test
 // `p1->distance(p2, true) <= reach` (tracing/refinement.cpp:30-33,
@@ -172,7 +179,6 @@ __device__ __forceinline__ HitRec load_hit(const HitRec *r) {
 
 // One thread per hit, two hits in flight per thread: both records and both
 // home slots are requested before either is used.
-// Slice `part` of `parts` covers hits [nh * part / parts, nh * (part + 1) / parts).
 // Part `part` applies the hits the pair tests' part `part` appended:
 // [hit_bounds[part], hit_bounds[part + 1]).
 __global__ void __launch_bounds__(256) k_hits(PipeDev p, uint32_t part, uint32_t parts) {
@@ -215,131 +221,146 @@ struct Counters {
   uint32_t tests, exact, hits, amb;  // per thread; summed into 64-bit totals per warp
 };
 
-// One 32x32 tile. Rows: own members (own=true) or border units.
-// A tile's 32 column points, staged per warp in shared memory: the test loop
-// reads one broadcast (x, y) per column; pid and border data on a hit only.
-struct ColTile {
-  float2 xy[32];     // leaf-relative fp32 offsets
-  uint32_t pid[32];
-  uint32_t nb[32];   // border units of the column object (border tiles)
-  uint32_t off[32];
-};
+// Lower bound of strip value v among the strip ids (sorig >> 16, ascending)
+// of a leaf's n members in strip order.
+__device__ __forceinline__ uint32_t strip_lower_bound(const uint32_t *sorig, uint32_t n, uint32_t v) {
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if ((__ldg(&sorig[mid]) >> 16) < v) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
 
-__device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtile, uint32_t coltile, uint32_t n,
-                         uint32_t t, Counters &ct, HitRec *q, uint32_t &qn, HitWindow &w, ColTile &col) {
+// One job: 32 rows of leaf g, each against its candidate range of members
+// in strip order. Rows are the leaf's own members (own = true; row i tests
+// the members after it in its strip and the next, so every pair of members
+// at most one strip apart is tested once) or 32 border units targeting the
+// leaf (every member of the strips beside the unit's point). The lane's
+// candidates are read 32 at a time; hits are marked in a bitmask and turned
+// into records after each group.
+__device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblock, uint32_t n, uint32_t t,
+                         Counters &ct, HitRec *q, uint32_t &qn, HitWindow &w) {
   const uint32_t lane = lane_id();
-  const uint32_t base = p.grid_start[g];
   const uint32_t lt_mask = (1u << lane) - 1u;
-  // column points
-  uint32_t j = coltile * 32 + lane;
-  bool vc = j < n;
-  float4 cp = vc ? p.pts[base + j] : make_float4(0.f, 0.f, 0.f, 0.f);
-  // row points
-  float4 rp;
-  uint32_t pid1 = 0;
+  const uint32_t base = p.grid_start[g];
+  const Node *o = &p.sd.nodes[p.sd.gid_node[g]];
+  float4 rp = make_float4(0.f, 0.f, 0.f, 0.f);
+  uint32_t pid1 = 0, orig1 = 0, a = 0, b = 0, row_leaf = 0;
   unsigned long long rank = 0;
-  uint32_t i = rowtile * 32 + lane;
   bool vr;
   if (own) {
+    const uint32_t i = rowblock * 32 + lane;
     vr = i < n;
-    rp = vr ? p.pts[base + i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    pid1 = __float_as_uint(rp.w);
-    rank = pid1;  // own-leaf unit of pid1 is grid_check[pid1] (tracing/filter.cpp:107-109)
-  } else {
-    uint32_t ub = p.bu_start[g], ue = p.bu_start[g + 1];
-    uint32_t r = ub + i;
-    vr = r < ue;
-    rp = make_float4(0.f, 0.f, 0.f, 0.f);
     if (vr) {
-      uint32_t pos = p.bu_sorted_pos[r];
+      rp = __ldg(&p.spts[base + i]);
+      pid1 = __float_as_uint(rp.w);
+      orig1 = __ldg(&p.sorig[base + i]) & 0xFFFFu;
+      a = i + 1;
+      b = __ldg(&p.shi[base + i]);
+    }
+  } else {
+    const uint32_t ub = p.bu_start[g], ue = p.bu_start[g + 1];
+    const uint32_t r = ub + rowblock * 32 + lane;
+    vr = r < ue;
+    if (vr) {
+      const uint32_t pos = p.bu_sorted_pos[r];
       pid1 = p.bu_pid[pos];
       rank = (unsigned long long)p.N + pos;  // border units follow the N own units
-      const Node *o = &p.sd.nodes[p.sd.gid_node[g]];
-      double2 qq = p.xy[pid1];
+      const double2 qq = p.xy[pid1];
       rp = make_float4(__double2float_rn(RN_SUB(qq.x, o->lo_x)), __double2float_rn(RN_SUB(qq.y, o->lo_y)),
                        metres_per_deg_lon_f(qq.y), 0.f);
+      // A pair of a border row (pid1 outside leaf g) and a member occurs
+      // twice in this step iff the member also has a border unit targeting
+      // pid1's leaf.
+      row_leaf = p.leaf_gid[pid1];
+      // candidates: the members of the strips beside the point's
+      const float2 ls = __ldg(&p.lstrip[g]);
+      const int H = (int)ls.y;
+      const int c = (int)fminf(fmaxf(floorf(rp.y * ls.x), -4.0f), (float)H + 4.0f);
+      const int s0 = c - 1 < 0 ? 0 : c - 1, s1 = c + 1 > H - 1 ? H - 1 : c + 1;
+      if (s0 <= s1) {
+        a = strip_lower_bound(p.sorig + base, n, (uint32_t)s0);
+        b = strip_lower_bound(p.sorig + base, n, (uint32_t)s1 + 1);
+      }
     }
   }
-  // A pair of a border row (pid1 outside leaf g) and member cpid occurs twice
-  // in this step iff cpid also has a border unit targeting pid1's leaf.
-  uint32_t row_leaf = (!own && vr) ? p.leaf_gid[pid1] : 0u;
-  uint32_t col_nb = 0, col_off = 0;
-  if (!own && vc) {
-    uint32_t cpid0 = __float_as_uint(cp.w);
-    col_nb = p.bcount[cpid0];
-    col_off = col_nb ? p.boff[cpid0] : 0u;
-  }
-  // tile error margin
-  float mx = warp_max(fmaxf(fabsf(rp.x), fabsf(cp.x)));
-  float my = warp_max(fmaxf(fabsf(rp.y), fabsf(cp.y)));
+  // error margin: offsets of the members are within the leaf's extent; a
+  // border row's own offsets may exceed it
+  const float wx = (float)RN_SUB(o->hi_x, o->lo_x) * 1.000001f, wy = (float)RN_SUB(o->hi_y, o->lo_y) * 1.000001f;
+  const float mx = fmaxf(wx, warp_max(fabsf(rp.x))), my = fmaxf(wy, warp_max(fabsf(rp.y)));
   const float u = 5.9604645e-08f;
   const float r = (float)p.reach;
-  float E = 2.1f * u * (2.0f * mx * STC_SMAX_F + 2.0f * my * STC_SLAT_F);
-  float delta = 4.0f * E + 64.0f * u * r + 1e-6f * r;
-  float lo = fmaxf(r - delta, 0.0f);
-  float lo2 = lo * lo;
-  float hi2 = (r + delta) * (r + delta);
-  uint32_t kmax = n - coltile * 32;
-  if (kmax > 32) kmax = 32;
-  // stage the columns (the previous tile's reads are over)
-  __syncwarp();
-  col.xy[lane] = make_float2(cp.x, cp.y);
-  col.pid[lane] = __float_as_uint(cp.w);
-  col.nb[lane] = col_nb;
-  col.off[lane] = col_off;
-  __syncwarp();
-  // this lane tests columns k in [kstart, kmax): an own-leaf unit pairs pid1
-  // only with later members (tracing/refinement.cpp:30)
-  int kstart = !vr ? 64 : (own ? (int)i - (int)(coltile * 32) + 1 : 0);
-  if (kstart < 0) kstart = 0;
-  if (kstart < (int)kmax) ct.tests += kmax - (uint32_t)kstart;
-  // the column loop only marks hits (one bit per column); records are made
-  // afterwards, one per lane per round, so that the loop carries no warp vote
-  // or branch for them
-  uint32_t hitmask = 0;
-#pragma unroll 1
-  for (uint32_t k = 0; k < kmax; k++) {
-    const float2 c = col.xy[k];
-    float dx = (rp.x - c.x) * rp.z;
-    float dy = (rp.y - c.y) * STC_SLAT_F;
-    float d2 = dx * dx + dy * dy;
-    const bool valid = (int)k >= kstart;
-    bool hit = valid && d2 <= lo2;
-    if (valid && !hit && d2 < hi2) {
-      ct.exact++;
-      hit = exact_within(p, pid1, col.pid[k], ct.amb);
-    }
-    hitmask |= (uint32_t)hit << k;
-  }
-  ct.hits += __popc(hitmask);
-  while (__any_sync(0xffffffffu, hitmask != 0)) {
-    const bool has = hitmask != 0;
-    const uint32_t k = has ? (uint32_t)(__ffs(hitmask) - 1) : 0u;
-    hitmask &= hitmask - 1u;
-    const uint32_t hm = __ballot_sync(0xffffffffu, has);
-    if (has) {
-      const uint32_t cpid = col.pid[k];
-      HitRec h;
-      h.a = pid1 < cpid ? pid1 : cpid;
-      h.b = pid1 < cpid ? cpid : pid1;
-      h.order = (rank << STC_ORDER_SHIFT) | (coltile * 32 + k);
-      if (!own) {
-        const uint32_t cnb = col.nb[k], coff = col.off[k];
-        for (uint32_t u2 = 0; u2 < cnb; u2++)
-          if (p.bu_gid[coff + u2] == row_leaf) h.order |= DUP_BIT;
+  const float E = 2.1f * u * (2.0f * mx * STC_SMAX_F + 2.0f * my * STC_SLAT_F);
+  const float delta = 4.0f * E + 64.0f * u * r + 1e-6f * r;
+  const float lo = fmaxf(r - delta, 0.0f);
+  const float lo2 = lo * lo;
+  const float hi2 = (r + delta) * (r + delta);
+  const uint32_t len = b > a ? b - a : 0u;
+  ct.tests += len;
+  const uint32_t maxlen = __reduce_max_sync(0xffffffffu, len);
+  const float4 *cand = p.spts + base + a;
+  for (uint32_t k0 = 0; k0 < maxlen; k0 += 32) {
+    const uint32_t kn = maxlen - k0 < 32u ? maxlen - k0 : 32u;
+    // the column loop only marks hits (one bit per candidate); records are
+    // made afterwards, one per lane per round, so that the loop carries no
+    // warp vote or branch for them
+    uint32_t hitmask = 0;
+#pragma unroll 4
+    for (uint32_t kk = 0; kk < kn; kk++) {
+      const bool valid = k0 + kk < len;
+      const float4 c = valid ? __ldg(&cand[k0 + kk]) : make_float4(0.f, 0.f, 0.f, 0.f);
+      const uint32_t pid2 = __float_as_uint(c.w);
+      // the reference measures from the unit's point: an own pair from its
+      // lower pid (tracing/refinement.cpp:30), a border pair from the unit
+      const bool swap = own && pid2 < pid1;
+      const float dx = (rp.x - c.x) * (swap ? c.z : rp.z);
+      const float dy = (rp.y - c.y) * STC_SLAT_F;
+      const float d2 = dx * dx + dy * dy;
+      bool hit = valid && d2 <= lo2;
+      if (valid && !hit && d2 < hi2) {
+        ct.exact++;
+        hit = swap ? exact_within(p, pid2, pid1, ct.amb) : exact_within(p, pid1, pid2, ct.amb);
       }
-      q[qn + __popc(hm & lt_mask)] = h;
+      hitmask |= (uint32_t)hit << kk;
     }
-    qn += __popc(hm);
-    if (qn >= 32) {
-      flush_queue(p, q, 32, t, w);
-      uint32_t rest = qn - 32;
-      HitRec mv;
-      if (lane < rest) mv = q[32 + lane];
-      __syncwarp();
-      if (lane < rest) q[lane] = mv;
-      __syncwarp();
-      qn = rest;
+    ct.hits += __popc(hitmask);
+    while (__any_sync(0xffffffffu, hitmask != 0)) {
+      const bool has = hitmask != 0;
+      const uint32_t kk = has ? (uint32_t)(__ffs(hitmask) - 1) : 0u;
+      hitmask &= hitmask - 1u;
+      const uint32_t hm = __ballot_sync(0xffffffffu, has);
+      if (has) {
+        const uint32_t j = a + k0 + kk;
+        const uint32_t cpid = __float_as_uint(__ldg(&p.spts[base + j]).w);
+        const uint32_t corig = __ldg(&p.sorig[base + j]) & 0xFFFFu;
+        HitRec h;
+        h.a = pid1 < cpid ? pid1 : cpid;
+        h.b = pid1 < cpid ? cpid : pid1;
+        if (own) {
+          // the pair is found by the lower pid's own unit (rank = its pid) at
+          // the higher pid's place in the pid-ordered member list
+          h.order = ((unsigned long long)h.a << STC_ORDER_SHIFT) | (pid1 < cpid ? corig : orig1);
+        } else {
+          h.order = (rank << STC_ORDER_SHIFT) | corig;
+          const uint32_t cnb = p.bcount[cpid];
+          const uint32_t coff = cnb ? p.boff[cpid] : 0u;
+          for (uint32_t u2 = 0; u2 < cnb; u2++)
+            if (p.bu_gid[coff + u2] == row_leaf) h.order |= DUP_BIT;
+        }
+        q[qn + __popc(hm & lt_mask)] = h;
+      }
+      qn += __popc(hm);
+      if (qn >= 32) {
+        flush_queue(p, q, 32, t, w);
+        const uint32_t rest = qn - 32;
+        HitRec mv;
+        if (lane < rest) mv = q[32 + lane];
+        __syncwarp();
+        if (lane < rest) q[lane] = mv;
+        __syncwarp();
+        qn = rest;
+      }
     }
   }
 }
@@ -349,9 +370,7 @@ __device__ void run_tile(const PipeDev &p, uint32_t g, bool own, uint32_t rowtil
 __global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint32_t part, uint32_t parts) {
   const uint32_t t = p.st->step_t;
   __shared__ HitRec queues[REFINE_THREADS / 32][QCAP];
-  __shared__ ColTile cols[REFINE_THREADS / 32];
   HitRec *q = queues[threadIdx.x >> 5];
-  ColTile &col = cols[threadIdx.x >> 5];
   uint32_t qn = 0;  // warp-uniform queue length
   HitWindow w = {0, 0};
   const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -375,24 +394,12 @@ __global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint3
     uint32_t g = lo;
     for (unsigned long long job = j0; job < j1; job++) {
       while (p.job_start[g + 1] <= job) g++;
-      uint32_t local = (uint32_t)(job - p.job_start[g]);
-      uint32_t cnt = p.grid_count[g];
-      uint32_t n = cnt < p.leaf_cap ? cnt : p.leaf_cap;
-      uint32_t R = (n + 31) / 32;
-      uint32_t own = R * (R + 1) / 2;
-      if (local < own) {
-        // row-major upper triangle: row rc has R - rc tiles (fp32 estimate, exact fix-up)
-        float b2 = 2.0f * (float)R + 1.0f;
-        uint32_t rc = (uint32_t)fmaxf((b2 - sqrtf(fmaxf(b2 * b2 - 8.0f * (float)local, 0.0f))) * 0.5f, 0.0f);
-        if (rc > R - 1) rc = R - 1;
-        while (rc > 0 && rc * R - rc * (rc - 1) / 2 > local) rc--;
-        while ((rc + 1) * R - (rc + 1) * rc / 2 <= local) rc++;
-        uint32_t cc = rc + (local - (rc * R - rc * (rc - 1) / 2));
-        run_tile(p, g, true, rc, cc, n, t, ct, q, qn, w, col);
-      } else {
-        uint32_t b = local - own;
-        run_tile(p, g, false, b / R, b % R, n, t, ct, q, qn, w, col);
-      }
+      const uint32_t local = (uint32_t)(job - p.job_start[g]);
+      const uint32_t cnt = p.grid_count[g];
+      const uint32_t n = cnt < p.leaf_cap ? cnt : p.leaf_cap;
+      const uint32_t R = (n + 31) / 32;
+      if (local < R) run_rows(p, g, true, local, n, t, ct, q, qn, w);
+      else run_rows(p, g, false, local - R, n, t, ct, q, qn, w);
     }
   }
   if (qn) flush_queue(p, q, qn, t, w);

@@ -382,6 +382,14 @@ class Pipeline:
         self._check(self._lib.stc_get_stats(self._h, ctypes.byref(s)))
         return s
 
+    def drain_some(self, out: np.ndarray) -> np.ndarray:
+        """Up to len(out) pending meetings (stc_drain_meetings) into `out`, a
+        MEETING_DTYPE array; the rest stays pending. Returns the filled part."""
+        assert out.dtype == MEETING_DTYPE and out.flags.c_contiguous
+        n = ctypes.c_size_t()
+        self._check(self._lib.stc_drain_meetings(self._h, out.ctypes.data, len(out), ctypes.byref(n)))
+        return out[: n.value]
+
     def drain(self, out: np.ndarray | None = None) -> np.ndarray:
         """The meetings emitted since the last drain (stc_drain_meetings).
         One buffer sized to the pending count receives them; the copy runs
