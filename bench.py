@@ -33,8 +33,9 @@ queries_under_ingest: K more steps (host input) while a serving thread answers
   a Poisson query stream (default 20,000/s; 60% object, 40% box queries) over
   the flushed block by continuous batching; queries return match counts, as
   the reference's searches do; p50/p99 latency from arrival.
-batched: 64 uneven ingest windows (1M-20M objects log-uniform, 10-50 steps,
-  reach 5/10/20 m, 0-90% hotspot, lowered where the table would not fit) run
+batched: 64 uneven ingest windows (100k-2M objects log-uniform, a tenth of
+  the batching configuration's 1M-20M, which --batched-full runs; 10-50
+  steps, reach 5/10/20 m, 0-90% hotspot, lowered where the table would not fit) run
   as plain steps and as pipelined windows (stc_step_window) from fresh
   contexts: both rates, the speed-up and whether the two emitted the same
   meetings (--no-batched skips it and autotune).
@@ -580,9 +581,11 @@ def _meeting_checksum(buf, k, device):
     return k, int(x.sum().item())
 
 
-def batched_line(device, windows=64, seed=7, live_cap=1.2e8):
+def batched_line(device, windows=64, seed=7, live_cap=1.2e8, objects=(1e6, 2e7)):
     """Uneven ingest windows of the batching configuration: `windows` windows,
-    each with a seeded object count log-uniform in 1M-20M, 10-50 steps, a
+    each with a seeded object count log-uniform in `objects` (the
+    configuration's 1M-20M; the default bench line runs them at a tenth,
+    100k-2M, so that the line takes seconds), 10-50 steps, a
     reach from {5, 10, 20} m and a share of objects in the 1000-hotspot model
     uniform in 0-90%. Where a window's expected live pairs (_live_estimate)
     would exceed live_cap the hotspot share is lowered (and, for the largest
@@ -606,7 +609,7 @@ def batched_line(device, windows=64, seed=7, live_cap=1.2e8):
     buf = pinned.numpy().view(MEETING_DTYPE)
     per, same, pos, secs = [], True, 0, {"plain": 0.0, "window": 0.0}
     for w in range(windows):
-        n = int(round(10 ** rng.uniform(6.0, np.log10(2e7))))
+        n = int(round(10 ** rng.uniform(np.log10(objects[0]), np.log10(objects[1]))))
         steps = int(rng.integers(10, 51))
         reach = float(rng.choice([5.0, 10.0, 20.0]))
         hot = float(rng.uniform(0.0, 0.9))
@@ -684,7 +687,8 @@ def batched_line(device, windows=64, seed=7, live_cap=1.2e8):
                     "meetings": sums["plain"][0], "same": sums["plain"] == sums["window"],
                     "plain_pos_per_s": rate["plain"], "window_pos_per_s": rate["window"], "window_calls": calls})
         del xy
-    return {"windows": len(per), "plain_pos_per_s": pos / secs["plain"], "window_pos_per_s": pos / secs["window"],
+    return {"windows": len(per), "objects_range": [int(objects[0]), int(objects[1])],
+            "plain_pos_per_s": pos / secs["plain"], "window_pos_per_s": pos / secs["window"],
             "speedup": secs["plain"] / secs["window"], "same_meetings": bool(same), "unit": "pos-updates/s",
             "per_window": per}
 
@@ -757,7 +761,9 @@ def main():
     ap.add_argument("--workload", default="uniform-10M", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-steps", type=int, default=2, help="steps timed for the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-batched", action="store_true", help="skip the plain-versus-graph window comparison")
+    ap.add_argument("--no-batched", action="store_true", help="skip the plain-versus-window comparison")
+    ap.add_argument("--batched-full", action="store_true",
+                    help="batched line at the configuration's 1M-20M objects (tens of minutes) instead of 100k-2M")
     ap.add_argument("--query-rate", type=float, default=20000.0,
                     help="Poisson query arrivals per second during the serving phase (0: skip)")
     ap.add_argument("--step-slices", type=int, default=0,
@@ -842,7 +848,8 @@ def main():
         "trace_gen": r["trace_gen"],
         "compaction": compaction_line(r["compaction"], peak),
         "sort": sort_line(local, peak),
-        "batched": None if args.no_batched else batched_line(local),
+        "batched": None if args.no_batched else batched_line(
+            local, objects=(1e6, 2e7) if args.batched_full else (1e5, 2e6)),
         "autotune": None if args.no_batched else tune_line(local),
         "bit_exact": r["bit_exact"]["bit_exact"] if r["bit_exact"] else None,
         "bit_exact_check": r["bit_exact"],
