@@ -581,6 +581,64 @@ def _meeting_checksum(buf, k, device):
     return k, int(x.sum().item())
 
 
+def _batched_run(mode, cfg, mbr, x0, xy, steps, n, buf, cap, device):
+    """One window from a fresh context, as plain steps or as pipelined
+    stc_step_window calls, its meetings drained into the page-locked `buf`
+    (checksummed whenever half full). Returns ((count, checksum), rate, wall
+    seconds over steps and drains, window calls, live meetings after the
+    last step)."""
+    import torch
+    from stcdb_gb300.pipeline import Pipeline, StcError
+    p = Pipeline(cfg, mbr, x0)
+    cnt, chk, fill, elapsed, calls = 0, 0, 0, 0.0, 0
+
+    def settle():
+        nonlocal cnt, chk, fill
+        a, b = _meeting_checksum(buf, fill, device)
+        cnt, chk, fill = cnt + a, (chk + b) & 0xFFFFFFFFFFFFFFFF, 0
+
+    try:
+        torch.cuda.synchronize(device)
+        if mode == "plain":
+            for t in range(steps):
+                t0 = time.perf_counter()
+                p.step_device(xy[t].data_ptr(), t)
+                while True:
+                    fill += len(p.drain_some(buf[fill:]))
+                    if not p.stats().pending:
+                        break
+                    elapsed += time.perf_counter() - t0
+                    settle()
+                    t0 = time.perf_counter()
+                elapsed += time.perf_counter() - t0
+                if fill > cap // 2:
+                    settle()
+        else:
+            t = 0
+            while t < steps:
+                t0 = time.perf_counter()
+                try:
+                    fill += len(p.step_window((xy[t].data_ptr(), steps - t), t, buf[fill:]))
+                    t = steps
+                except StcError as e:
+                    if e.status != 3:  # only a full output buffer is expected
+                        raise
+                    t = int(p.stats().step) + 1  # the steps that ran; their undrained meetings wait
+                    fill = cap  # the call filled the buffer
+                elapsed += time.perf_counter() - t0
+                calls += 1
+                if fill > cap // 2 or t < steps:
+                    settle()
+                    while p.stats().pending:
+                        fill += len(p.drain_some(buf[fill:]))
+                        settle()
+        settle()
+        live = int(p.stats().taken_buckets)
+    finally:
+        p.close()
+    return (cnt, chk), n * steps / elapsed, elapsed, calls, live
+
+
 def batched_line(device, windows=64, seed=7, live_cap=1.2e8, objects=(1e6, 2e7)):
     """Uneven ingest windows of the batching configuration: `windows` windows,
     each with a seeded object count log-uniform in `objects` (the
@@ -601,7 +659,7 @@ def batched_line(device, windows=64, seed=7, live_cap=1.2e8, objects=(1e6, 2e7))
     compared. Times are wall-clock over the steps and drains, checksums
     excluded."""
     import torch
-    from stcdb_gb300.pipeline import MEETING_DTYPE, Pipeline, StcConfig, StcError
+    from stcdb_gb300.pipeline import MEETING_DTYPE, StcConfig, StcError
     from stcdb_gb300.tracegen import DeviceTraceGenerator, hotspot_grid, uniform_grid
     rng = np.random.default_rng(seed)
     cap = 48_000_000
@@ -620,7 +678,9 @@ def batched_line(device, windows=64, seed=7, live_cap=1.2e8, objects=(1e6, 2e7))
             base = _live_estimate(n, 0.0, reach)
             hot = float(np.sqrt(max(live_cap / base - 1.0, 0.0) / 104.0))
         live = _live_estimate(n, hot, reach)
-        B = 1 << max(22, int(np.ceil(np.log2(3.0 * live + 1))))
+        # the estimate is rough (hotspot draws vary): 8 slots per expected
+        # live pair keeps the load low even at several times the estimate
+        B = 1 << max(24, int(np.ceil(np.log2(8.0 * live + 1))))
         tcfg = hotspot_grid(n, hot_frac=hot, seed=seed + w) if hot > 0.005 else uniform_grid(n, seed=seed + w)
         gen = DeviceTraceGenerator(tcfg, device)
         mbr = gen.map_box(100.0)
@@ -631,63 +691,34 @@ def batched_line(device, windows=64, seed=7, live_cap=1.2e8, objects=(1e6, 2e7))
                         num_meeting_buckets=B, emit_capacity=max(4 * n, int(0.25 * live) + (1 << 22)),
                         device=device)
         x0 = xy[0].cpu().numpy()
-        sums, rate, calls = {}, {}, 0
-        for mode in ("plain", "window"):
-            p = Pipeline(cfg, mbr, x0)
-            cnt, chk, fill, elapsed = 0, 0, 0, 0.0
-
-            def settle():
-                nonlocal cnt, chk, fill
-                a, b = _meeting_checksum(buf, fill, device)
-                cnt, chk, fill = cnt + a, (chk + b) & 0xFFFFFFFFFFFFFFFF, 0
-
-            torch.cuda.synchronize(device)
-            if mode == "plain":
-                for t in range(steps):
-                    t0 = time.perf_counter()
-                    p.step_device(xy[t].data_ptr(), t)
-                    while True:
-                        fill += len(p.drain_some(buf[fill:]))
-                        if not p.stats().pending:
-                            break
-                        elapsed += time.perf_counter() - t0
-                        settle()
-                        t0 = time.perf_counter()
-                    elapsed += time.perf_counter() - t0
-                    if fill > cap // 2:
-                        settle()
-            else:
-                t = 0
-                while t < steps:
-                    t0 = time.perf_counter()
-                    try:
-                        fill += len(p.step_window((xy[t].data_ptr(), steps - t), t, buf[fill:]))
-                        t = steps
-                    except StcError as e:
-                        if e.status != 3:  # only a full output buffer is expected
-                            raise
-                        t = int(p.stats().step) + 1  # the steps that ran; their undrained meetings wait
-                        fill = cap  # the call filled the buffer
-                    elapsed += time.perf_counter() - t0
-                    calls += 1
-                    if fill > cap // 2 or t < steps:
-                        settle()
-                        while p.stats().pending:
-                            fill += len(p.drain_some(buf[fill:]))
-                            settle()
-            settle()
-            p.close()
-            sums[mode] = (cnt, chk)
-            rate[mode] = n * steps / elapsed
-            secs[mode] += elapsed
+        sums, rate, dts, calls, live_seen = {}, {}, {}, 0, 0
+        try:
+            for mode in ("plain", "window"):
+                sums[mode], rate[mode], dts[mode], c, live_seen = _batched_run(mode, cfg, mbr, x0, xy, steps, n,
+                                                                               buf, cap, device)
+                calls += c
+        except StcError as e:
+            # a window the library refuses (a table too small for its pairs)
+            # is reported, not timed
+            per.append({"objects": n, "steps": steps, "hot_frac": round(hot, 4), "reach_m": reach,
+                        "table_slots": B, "error": str(e)})
+            same = False
+            del xy
+            continue
+        for mode in dts:
+            secs[mode] += dts[mode]
         same &= sums["plain"] == sums["window"]
         pos += n * steps
         per.append({"objects": n, "steps": steps, "hot_frac": round(hot, 4), "reach_m": reach,
                     "drawn": {"reach_m": want[0], "hot_frac": round(want[1], 4)}, "table_slots": B,
+                    "live_estimate": int(live), "live_meetings": live_seen,
                     "meetings": sums["plain"][0], "same": sums["plain"] == sums["window"],
                     "plain_pos_per_s": rate["plain"], "window_pos_per_s": rate["window"], "window_calls": calls})
         del xy
+    if not pos:
+        return {"windows": len(per), "error": "no window ran", "per_window": per}
     return {"windows": len(per), "objects_range": [int(objects[0]), int(objects[1])],
+            "failed_windows": sum(1 for w in per if "error" in w),
             "plain_pos_per_s": pos / secs["plain"], "window_pos_per_s": pos / secs["window"],
             "speedup": secs["plain"] / secs["window"], "same_meetings": bool(same), "unit": "pos-updates/s",
             "per_window": per}

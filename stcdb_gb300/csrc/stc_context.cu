@@ -383,7 +383,7 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
             dalloc(c, &p.hit_bounds, STC_MAX_PARTS + 1) &&
             dalloc(c, &p.sort_hist2, radix_hist_words(nu)) && dalloc(c, &p.scan_tmp2, scan_words) &&
             dalloc(c, &p.grid_start, (size_t)p.G + 1) && dalloc(c, &p.pts, n) && dalloc(c, &p.fxy, n) &&
-            dalloc(c, &p.spts, n) && dalloc(c, &p.sorig, n) && dalloc(c, &p.shi, n) &&
+            dalloc(c, &p.spts, n) && dalloc(c, &p.sorig, n) && dalloc(c, &p.scand, n) &&
             dalloc(c, &p.lstrip, p.G) &&
             dalloc(c, &p.bcount, (size_t)n + 1) && dalloc(c, &p.boff, (size_t)n + 1) &&
             dalloc(c, &p.blist, n) && dalloc(c, &p.bres, 4 * (size_t)n) && dalloc(c, &p.sd.fbox, p.S) &&

@@ -77,20 +77,42 @@ __global__ void k_gather(PipeDev p) {
 // ranges. The leaf is cut into H horizontal strips (H <= STRIPS_MAX) at
 // least s_min metres tall, s_min a little above reach. The reference's
 // distance takes dy / dpm_lat, a constant scale, so two members within reach
-// lie at most one strip apart: the candidates of a member are the members of
-// its own strip and the two beside it, one contiguous range in strip order.
-// Strip coordinates are computed in fp32 from the members' leaf offsets ly;
-// s_min covers their rounding (u * leaf height) and the product's with wide
-// margins (1e-4 relative plus 1e-6 of the leaf height plus 1 mm).
-// One warp per leaf: a counting sort by strip in shared memory (the order
-// within a strip does not matter: each pair is tested once, by its member
-// earlier in strip order, and its priority comes from the pid-order index).
+// lie at most one strip apart. Within a strip of at most XSORT_MAX members
+// the members are ordered by longitude offset; |dx| * (metres per degree at
+// the first point's latitude) <= reach bounds |dx| by wx degrees, wx taken at
+// the leaf's smallest scale, so the partners of a member in an ordered strip
+// form one window of it, found by binary search. A larger strip (dense
+// hotspot leaves at the minimum width, where most pairs are within reach
+// anyway) keeps its members unordered and is taken whole.
+// Candidates of member i (own rows): the members after it in its strip up
+// to its window's end, and its window in the next strip; every pair at most
+// a strip apart and within wx is thereby tested once, by its member earlier
+// in (strip, longitude) order. Strip and window bounds are computed in fp32
+// from the members' leaf offsets; s_min and wx cover their rounding (u times
+// the leaf extent) and the scale's with wide margins (2e-4 relative plus 1e-6
+// of the leaf extent plus 1-2 mm).
+// One warp per leaf: a counting sort by strip in shared memory, then a rank
+// sort by longitude of each small strip with shuffles (the order within a
+// strip only decides which member of a pair tests it; each hit's priority
+// comes from the pid-order index).
 static constexpr uint32_t STRIPS_MAX = 64;
+static constexpr uint32_t XSORT_MAX = 128;
 
 __device__ __forceinline__ uint32_t member_strip(float ly, float inv, uint32_t H) {
   float c = floorf(ly * inv);
   c = fminf(fmaxf(c, 0.0f), (float)(H - 1));
   return (uint32_t)c;
+}
+
+// First index in [lo, hi) of a longitude-ordered strip whose offset is
+// greater than x (upper = true) or not below x (upper = false).
+__device__ __forceinline__ uint32_t x_bound(const float4 *pts, uint32_t lo, uint32_t hi, float x, bool upper) {
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    const float v = pts[mid].x;
+    if (upper ? v <= x : v < x) lo = mid + 1; else hi = mid;
+  }
+  return lo;
 }
 
 __global__ void __launch_bounds__(256) k_strip_order(PipeDev p) {
@@ -105,12 +127,17 @@ __global__ void __launch_bounds__(256) k_strip_order(PipeDev p) {
     if (n == 0) continue;
     const uint32_t base = p.grid_start[g];
     const Node *o = &p.sd.nodes[p.sd.gid_node[g]];
-    const double h_deg = RN_SUB(o->hi_y, o->lo_y);
-    const float h_m = (float)h_deg * STC_SLAT_F;
+    const double h_deg = RN_SUB(o->hi_y, o->lo_y), w_deg = RN_SUB(o->hi_x, o->lo_x);
+    const float h_m = (float)h_deg * STC_SLAT_F, w_m = (float)w_deg * STC_SMAX_F;
     const float s_min = (float)p.reach * 1.0001f + 1e-6f * h_m + 1e-3f;
     float hf = floorf(h_m / s_min);
     const uint32_t H = hf < 1.0f ? 1u : (hf > (float)STRIPS_MAX ? STRIPS_MAX : (uint32_t)hf);
     const float inv = H > 1 ? (float)H / (float)h_deg : 0.0f;  // strips per degree from the low edge
+    // smallest metres per degree of longitude of any first point of a pair
+    // (the leaf's latitudes, widened by 1e-3 degrees for border points)
+    const double lat = fmax(fabs(o->lo_y), fabs(o->hi_y)) + 1e-3;
+    const float s_lon = metres_per_deg_lon_f(lat < 89.0 ? lat : 89.0) * (1.0f - 1e-5f);
+    const float wx = ((float)p.reach * 1.0002f + 1e-6f * (w_m + h_m) + 2e-3f) / s_lon;
     for (uint32_t k = lane; k <= STRIPS_MAX; k += 32) hist[k] = 0;
     __syncwarp();
     for (uint32_t i = lane; i < n; i += 32) {
@@ -138,9 +165,69 @@ __global__ void __launch_bounds__(256) k_strip_order(PipeDev p) {
       const uint32_t k = hist[sidx] + (u & 0xFFFFu);
       p.spts[base + k] = p.pts[base + i];
       p.sorig[base + k] = i | sidx << 16;
-      p.shi[base + k] = hist[sidx + 2 < H ? sidx + 2 : H];
     }
-    if (lane == 0) p.lstrip[g] = make_float2(inv, (float)H);
+    __syncwarp();
+    // small strips in longitude order: each member's rank among the strip's
+    // (offset, position) pairs, its elements in four slots of 32 lanes
+    for (uint32_t sidx = 0; sidx < H; sidx++) {
+      const uint32_t st = hist[sidx], L = hist[sidx + 1] - st;
+      if (L > XSORT_MAX) continue;
+      const uint32_t slots = (L + 31) / 32;
+      float4 v[4];
+      uint32_t og[4], rk[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+        const uint32_t e = lane + 32u * m;
+        v[m] = e < L ? p.spts[base + st + e] : make_float4(0.f, 0.f, 0.f, 0.f);
+        og[m] = e < L ? p.sorig[base + st + e] : 0u;
+      }
+#pragma unroll
+      for (int m2 = 0; m2 < 4; m2++) {
+        if ((uint32_t)m2 >= slots) break;
+        for (uint32_t src = 0; src < 32; src++) {
+          const float xb = __shfl_sync(0xffffffffu, v[m2].x, src);
+          const uint32_t b = src + 32u * m2;
+          if (b >= L) break;
+#pragma unroll
+          for (int m = 0; m < 4; m++) {
+            const uint32_t a = lane + 32u * m;
+            rk[m] += (xb < v[m].x || (xb == v[m].x && b < a)) ? 1u : 0u;
+          }
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+        const uint32_t e = lane + 32u * m;
+        if (e < L) {
+          p.spts[base + st + rk[m]] = v[m];
+          p.sorig[base + st + rk[m]] = og[m] | STRIP_XSORTED;
+        }
+      }
+      __syncwarp();
+    }
+    // candidate ranges of every member (positions within the leaf)
+    const float4 *lp = p.spts + base;
+    for (uint32_t i = lane; i < n; i += 32) {
+      const uint32_t sidx = (p.sorig[base + i] >> 16) & 63u;
+      const float xi = lp[i].x;
+      const uint32_t en = hist[sidx + 1];
+      const bool xs = en - hist[sidx] <= XSORT_MAX;
+      const uint32_t e1 = xs ? x_bound(lp, i + 1, en, xi + wx, true) : en;
+      uint32_t a2 = 0, b2 = 0;
+      if (sidx + 1 < H) {
+        const uint32_t st2 = hist[sidx + 1], en2 = hist[sidx + 2];
+        if (en2 - st2 <= XSORT_MAX) {
+          a2 = x_bound(lp, st2, en2, xi - wx, false);
+          b2 = x_bound(lp, a2, en2, xi + wx, true);
+        } else {
+          a2 = st2;
+          b2 = en2;
+        }
+      }
+      p.scand[base + i] = make_uint2(e1 | a2 << 16, b2);
+    }
+    if (lane == 0) p.lstrip[g] = make_float4(inv, (float)H, wx, 0.0f);
     __syncwarp();
   }
 }

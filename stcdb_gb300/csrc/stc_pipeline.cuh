@@ -5,6 +5,9 @@
 
 namespace stc {
 
+// sorig flag: the member's strip is ordered by longitude offset
+#define STRIP_XSORTED (1u << 22)
+
 struct PipeDev {
   // sizes
   uint32_t N, leaf_cap, G, S;
@@ -34,13 +37,16 @@ struct PipeDev {
   float4 *pts;                          // N sorted: lx, ly, metres/deg lon, pid bits
   float2 *fxy;                          // N by pid: float lon, lat (MBR of new meetings)
   // each leaf's kept members again, ordered by horizontal strip (strips at
-  // least reach tall): spts as pts; sorig = member index in pid order |
-  // strip << 16; shi = end (within the leaf) of the strip above the
-  // member's; lstrip[g] = (strips per degree of latitude from the leaf's
-  // low corner, strip count)
+  // least reach tall) and, within a small strip, by longitude: spts as pts;
+  // sorig = member index in pid order | strip << 16 | STRIP_XSORTED;
+  // scand = the member's candidate ranges within the leaf: [i + 1, x & 0xFFFF)
+  // in its strip and [x >> 16, y) in the next; lstrip[g] = (strips per degree
+  // of latitude from the leaf's low corner, strip count, longitude window wx
+  // in degrees, 0)
   float4 *spts;
-  uint32_t *sorig, *shi;
-  float2 *lstrip;
+  uint32_t *sorig;
+  uint2 *scand;
+  float4 *lstrip;
   // border units
   uint32_t *bcount, *boff;              // N+1 (border units per pid, exclusive offsets)
   uint32_t *blist;                      // N: pids of border points (any order)

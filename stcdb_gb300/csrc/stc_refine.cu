@@ -3,17 +3,18 @@
 //
 // Work: every leaf's n kept members (the first leaf_cap in pid order,
 // tracing/filter.cpp:100-104) are ordered by horizontal strips at least
-// reach tall (stc_partition.cu, k_strip_order), so a pair within reach lies
-// in one strip or two adjacent ones. The reference tests every own-leaf pair
-// (pid < q, tracing/refinement.cpp:30) and every (border unit, member) pair
-// of the leaf (tracing/filter.cpp:248-259); pairs more than a strip apart are
-// farther than reach, so only the pairs in a member's candidate range -- the
-// members after it in strip order up to the end of the next strip, or for a
-// border unit the members of the strips beside its point -- can hit, and
-// only those are tested. A job is 32 rows (members or border units) of one
-// leaf, one per lane, each over its own contiguous candidate range. Each hit
-// keeps the reference's priority: the finding unit's rank and the member's
-// index in pid order.
+// reach tall and, within small strips, by longitude (stc_partition.cu,
+// k_strip_order). The reference tests every own-leaf pair (pid < q,
+// tracing/refinement.cpp:30) and every (border unit, member) pair of the
+// leaf (tracing/filter.cpp:248-259); a pair more than a strip apart, or
+// farther apart in longitude than the leaf's window wx, is farther than
+// reach, so only the pairs in a member's candidate windows -- the members
+// after it in its strip up to its window's end and its window in the next
+// strip, or for a border unit its window in the three strips beside its
+// point -- can hit, and only those are tested. A job is 32 rows (members or
+// border units) of one leaf, one per lane, each over its own contiguous
+// segments. Each hit keeps the reference's priority: the finding unit's
+// rank and the member's index in pid order.
 //
 // Distance decisions equal the reference's fp64 test
 // `p1->distance(p2, true) <= reach` (tracing/refinement.cpp:30-33,
@@ -221,24 +222,37 @@ struct Counters {
   uint32_t tests, exact, hits, amb;  // per thread; summed into 64-bit totals per warp
 };
 
-// Lower bound of strip value v among the strip ids (sorig >> 16, ascending)
-// of a leaf's n members in strip order.
+// Lower bound of strip value v among the strip ids ((sorig >> 16) & 63,
+// ascending) of a leaf's n members in strip order.
 __device__ __forceinline__ uint32_t strip_lower_bound(const uint32_t *sorig, uint32_t n, uint32_t v) {
   uint32_t lo = 0, hi = n;
   while (lo < hi) {
     const uint32_t mid = (lo + hi) >> 1;
-    if ((__ldg(&sorig[mid]) >> 16) < v) lo = mid + 1; else hi = mid;
+    if (((__ldg(&sorig[mid]) >> 16) & 63u) < v) lo = mid + 1; else hi = mid;
   }
   return lo;
 }
 
-// One job: 32 rows of leaf g, each against its candidate range of members
-// in strip order. Rows are the leaf's own members (own = true; row i tests
-// the members after it in its strip and the next, so every pair of members
-// at most one strip apart is tested once) or 32 border units targeting the
-// leaf (every member of the strips beside the unit's point). The lane's
-// candidates are read 32 at a time; hits are marked in a bitmask and turned
-// into records after each group.
+// First index in [lo, hi) of a longitude-ordered strip whose offset is
+// greater than x (upper) or not below x (!upper).
+__device__ __forceinline__ uint32_t strip_x_bound(const float4 *pts, uint32_t lo, uint32_t hi, float x, bool upper) {
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    const float v = __ldg(&pts[mid]).x;
+    if (upper ? v <= x : v < x) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// One job: 32 rows of leaf g, each against its candidate ranges of members
+// in (strip, longitude) order (stc_partition.cu, k_strip_order). Rows are
+// the leaf's own members (own = true; row i tests the members after it in
+// its strip up to its longitude window's end, and its window in the next
+// strip, so every pair of members within reach is tested once) or 32 border
+// units targeting the leaf (the members in the unit's longitude window in
+// the three strips beside its point). A lane's candidates come in up to
+// three contiguous segments, each read 32 at a time; hits are marked in a
+// bitmask and turned into records after each group.
 __device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblock, uint32_t n, uint32_t t,
                          Counters &ct, HitRec *q, uint32_t &qn, HitWindow &w) {
   const uint32_t lane = lane_id();
@@ -246,7 +260,8 @@ __device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblo
   const uint32_t base = p.grid_start[g];
   const Node *o = &p.sd.nodes[p.sd.gid_node[g]];
   float4 rp = make_float4(0.f, 0.f, 0.f, 0.f);
-  uint32_t pid1 = 0, orig1 = 0, a = 0, b = 0, row_leaf = 0;
+  uint32_t pid1 = 0, orig1 = 0, row_leaf = 0;
+  uint32_t sa[3] = {0, 0, 0}, sl[3] = {0, 0, 0};  // candidate segments: start, length
   unsigned long long rank = 0;
   bool vr;
   if (own) {
@@ -256,8 +271,12 @@ __device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblo
       rp = __ldg(&p.spts[base + i]);
       pid1 = __float_as_uint(rp.w);
       orig1 = __ldg(&p.sorig[base + i]) & 0xFFFFu;
-      a = i + 1;
-      b = __ldg(&p.shi[base + i]);
+      const uint2 c = __ldg(&p.scand[base + i]);
+      const uint32_t e1 = c.x & 0xFFFFu, a2 = c.x >> 16;
+      sa[0] = i + 1;
+      sl[0] = e1 > i + 1 ? e1 - (i + 1) : 0u;
+      sa[1] = a2;
+      sl[1] = c.y > a2 ? c.y - a2 : 0u;
     }
   } else {
     const uint32_t ub = p.bu_start[g], ue = p.bu_start[g + 1];
@@ -274,21 +293,33 @@ __device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblo
       // twice in this step iff the member also has a border unit targeting
       // pid1's leaf.
       row_leaf = p.leaf_gid[pid1];
-      // candidates: the members of the strips beside the point's
-      const float2 ls = __ldg(&p.lstrip[g]);
+      // candidates: the members in the point's longitude window of the
+      // strips beside its own (all of a strip too large to be ordered)
+      const float4 ls = __ldg(&p.lstrip[g]);
       const int H = (int)ls.y;
       const int c = (int)fminf(fmaxf(floorf(rp.y * ls.x), -4.0f), (float)H + 4.0f);
-      const int s0 = c - 1 < 0 ? 0 : c - 1, s1 = c + 1 > H - 1 ? H - 1 : c + 1;
-      if (s0 <= s1) {
-        a = strip_lower_bound(p.sorig + base, n, (uint32_t)s0);
-        b = strip_lower_bound(p.sorig + base, n, (uint32_t)s1 + 1);
+      const uint32_t *so = p.sorig + base;
+      const float4 *sp = p.spts + base;
+      int k = 0;
+      for (int sidx = c - 1; sidx <= c + 1; sidx++, k++) {
+        if (sidx < 0 || sidx >= H) continue;
+        const uint32_t st = strip_lower_bound(so, n, (uint32_t)sidx);
+        const uint32_t en = strip_lower_bound(so, n, (uint32_t)sidx + 1);
+        if (st >= en) continue;
+        uint32_t a = st, b = en;
+        if (__ldg(&so[st]) & STRIP_XSORTED) {
+          a = strip_x_bound(sp, st, en, rp.x - ls.z, false);
+          b = strip_x_bound(sp, a, en, rp.x + ls.z, true);
+        }
+        sa[k] = a;
+        sl[k] = b - a;
       }
     }
   }
   // error margin: offsets of the members are within the leaf's extent; a
   // border row's own offsets may exceed it
-  const float wx = (float)RN_SUB(o->hi_x, o->lo_x) * 1.000001f, wy = (float)RN_SUB(o->hi_y, o->lo_y) * 1.000001f;
-  const float mx = fmaxf(wx, warp_max(fabsf(rp.x))), my = fmaxf(wy, warp_max(fabsf(rp.y)));
+  const float wxl = (float)RN_SUB(o->hi_x, o->lo_x) * 1.000001f, wyl = (float)RN_SUB(o->hi_y, o->lo_y) * 1.000001f;
+  const float mx = fmaxf(wxl, warp_max(fabsf(rp.x))), my = fmaxf(wyl, warp_max(fabsf(rp.y)));
   const float u = 5.9604645e-08f;
   const float r = (float)p.reach;
   const float E = 2.1f * u * (2.0f * mx * STC_SMAX_F + 2.0f * my * STC_SLAT_F);
@@ -296,70 +327,73 @@ __device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblo
   const float lo = fmaxf(r - delta, 0.0f);
   const float lo2 = lo * lo;
   const float hi2 = (r + delta) * (r + delta);
-  const uint32_t len = b > a ? b - a : 0u;
-  ct.tests += len;
-  const uint32_t maxlen = __reduce_max_sync(0xffffffffu, len);
-  const float4 *cand = p.spts + base + a;
-  for (uint32_t k0 = 0; k0 < maxlen; k0 += 32) {
-    const uint32_t kn = maxlen - k0 < 32u ? maxlen - k0 : 32u;
-    // the column loop only marks hits (one bit per candidate); records are
-    // made afterwards, one per lane per round, so that the loop carries no
-    // warp vote or branch for them
-    uint32_t hitmask = 0;
+#pragma unroll 1
+  for (int seg = 0; seg < 3; seg++) {
+    const uint32_t a = sa[seg], len = sl[seg];
+    ct.tests += len;
+    const uint32_t maxlen = __reduce_max_sync(0xffffffffu, len);
+    const float4 *cand = p.spts + base + a;
+    for (uint32_t k0 = 0; k0 < maxlen; k0 += 32) {
+      const uint32_t kn = maxlen - k0 < 32u ? maxlen - k0 : 32u;
+      // the column loop only marks hits (one bit per candidate); records are
+      // made afterwards, one per lane per round, so that the loop carries no
+      // warp vote or branch for them
+      uint32_t hitmask = 0;
 #pragma unroll 4
-    for (uint32_t kk = 0; kk < kn; kk++) {
-      const bool valid = k0 + kk < len;
-      const float4 c = valid ? __ldg(&cand[k0 + kk]) : make_float4(0.f, 0.f, 0.f, 0.f);
-      const uint32_t pid2 = __float_as_uint(c.w);
-      // the reference measures from the unit's point: an own pair from its
-      // lower pid (tracing/refinement.cpp:30), a border pair from the unit
-      const bool swap = own && pid2 < pid1;
-      const float dx = (rp.x - c.x) * (swap ? c.z : rp.z);
-      const float dy = (rp.y - c.y) * STC_SLAT_F;
-      const float d2 = dx * dx + dy * dy;
-      bool hit = valid && d2 <= lo2;
-      if (valid && !hit && d2 < hi2) {
-        ct.exact++;
-        hit = swap ? exact_within(p, pid2, pid1, ct.amb) : exact_within(p, pid1, pid2, ct.amb);
-      }
-      hitmask |= (uint32_t)hit << kk;
-    }
-    ct.hits += __popc(hitmask);
-    while (__any_sync(0xffffffffu, hitmask != 0)) {
-      const bool has = hitmask != 0;
-      const uint32_t kk = has ? (uint32_t)(__ffs(hitmask) - 1) : 0u;
-      hitmask &= hitmask - 1u;
-      const uint32_t hm = __ballot_sync(0xffffffffu, has);
-      if (has) {
-        const uint32_t j = a + k0 + kk;
-        const uint32_t cpid = __float_as_uint(__ldg(&p.spts[base + j]).w);
-        const uint32_t corig = __ldg(&p.sorig[base + j]) & 0xFFFFu;
-        HitRec h;
-        h.a = pid1 < cpid ? pid1 : cpid;
-        h.b = pid1 < cpid ? cpid : pid1;
-        if (own) {
-          // the pair is found by the lower pid's own unit (rank = its pid) at
-          // the higher pid's place in the pid-ordered member list
-          h.order = ((unsigned long long)h.a << STC_ORDER_SHIFT) | (pid1 < cpid ? corig : orig1);
-        } else {
-          h.order = (rank << STC_ORDER_SHIFT) | corig;
-          const uint32_t cnb = p.bcount[cpid];
-          const uint32_t coff = cnb ? p.boff[cpid] : 0u;
-          for (uint32_t u2 = 0; u2 < cnb; u2++)
-            if (p.bu_gid[coff + u2] == row_leaf) h.order |= DUP_BIT;
+      for (uint32_t kk = 0; kk < kn; kk++) {
+        const bool valid = k0 + kk < len;
+        const float4 c = valid ? __ldg(&cand[k0 + kk]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const uint32_t pid2 = __float_as_uint(c.w);
+        // the reference measures from the unit's point: an own pair from its
+        // lower pid (tracing/refinement.cpp:30), a border pair from the unit
+        const bool swap = own && pid2 < pid1;
+        const float dx = (rp.x - c.x) * (swap ? c.z : rp.z);
+        const float dy = (rp.y - c.y) * STC_SLAT_F;
+        const float d2 = dx * dx + dy * dy;
+        bool hit = valid && d2 <= lo2;
+        if (valid && !hit && d2 < hi2) {
+          ct.exact++;
+          hit = swap ? exact_within(p, pid2, pid1, ct.amb) : exact_within(p, pid1, pid2, ct.amb);
         }
-        q[qn + __popc(hm & lt_mask)] = h;
+        hitmask |= (uint32_t)hit << kk;
       }
-      qn += __popc(hm);
-      if (qn >= 32) {
-        flush_queue(p, q, 32, t, w);
-        const uint32_t rest = qn - 32;
-        HitRec mv;
-        if (lane < rest) mv = q[32 + lane];
-        __syncwarp();
-        if (lane < rest) q[lane] = mv;
-        __syncwarp();
-        qn = rest;
+      ct.hits += __popc(hitmask);
+      while (__any_sync(0xffffffffu, hitmask != 0)) {
+        const bool has = hitmask != 0;
+        const uint32_t kk = has ? (uint32_t)(__ffs(hitmask) - 1) : 0u;
+        hitmask &= hitmask - 1u;
+        const uint32_t hm = __ballot_sync(0xffffffffu, has);
+        if (has) {
+          const uint32_t j = a + k0 + kk;
+          const uint32_t cpid = __float_as_uint(__ldg(&p.spts[base + j]).w);
+          const uint32_t corig = __ldg(&p.sorig[base + j]) & 0xFFFFu;
+          HitRec h;
+          h.a = pid1 < cpid ? pid1 : cpid;
+          h.b = pid1 < cpid ? cpid : pid1;
+          if (own) {
+            // the pair is found by the lower pid's own unit (rank = its pid)
+            // at the higher pid's place in the pid-ordered member list
+            h.order = ((unsigned long long)h.a << STC_ORDER_SHIFT) | (pid1 < cpid ? corig : orig1);
+          } else {
+            h.order = (rank << STC_ORDER_SHIFT) | corig;
+            const uint32_t cnb = p.bcount[cpid];
+            const uint32_t coff = cnb ? p.boff[cpid] : 0u;
+            for (uint32_t u2 = 0; u2 < cnb; u2++)
+              if (p.bu_gid[coff + u2] == row_leaf) h.order |= DUP_BIT;
+          }
+          q[qn + __popc(hm & lt_mask)] = h;
+        }
+        qn += __popc(hm);
+        if (qn >= 32) {
+          flush_queue(p, q, 32, t, w);
+          const uint32_t rest = qn - 32;
+          HitRec mv;
+          if (lane < rest) mv = q[32 + lane];
+          __syncwarp();
+          if (lane < rest) q[lane] = mv;
+          __syncwarp();
+          qn = rest;
+        }
       }
     }
   }
