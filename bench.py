@@ -73,6 +73,20 @@ WORKLOADS = {
                         buckets=1 << 28, kv_restriction=1 << 27, refine_bps=4, hits_bps=32),
     "hotspot-1M": dict(objects=1_000_000, hot=1000, reach=10.0, min_meet=5, grid_capacity=200, amplify=8.0,
                        buckets=1 << 28, kv_restriction=1 << 27),
+    # the hotspot model at larger object counts (live pairs grow with N^2)
+    # (the warm-up window holds its steps' meetings: emit buffers of 16 N)
+    "hotspot-2M": dict(objects=2_000_000, hot=1000, reach=10.0, min_meet=5, grid_capacity=200, amplify=8.0,
+                       buckets=1 << 29, kv_restriction=1 << 27, emit_per_object=16),
+    "hotspot-3M": dict(objects=3_000_000, hot=1000, reach=10.0, min_meet=5, grid_capacity=200, amplify=8.0,
+                       buckets=1 << 30, kv_restriction=1 << 27, emit_per_object=16),
+    # the stress configuration's model (90% of objects in 200 hotspots,
+    # sigma 150 m, reach 20 m, minimum meeting 3 steps) at the largest object
+    # count whose live pairs fit a table in HBM: its Zipf-weighted first
+    # hotspot alone holds ~17% of the hot objects, so live pairs grow as N^2
+    # (about 3e8 at 1M objects)
+    "stress-1M": dict(objects=1_000_000, hot=200, hot_frac=0.9, sigma_m=150.0, reach=20.0, min_meet=3,
+                      grid_capacity=200, amplify=32.0, buckets=1 << 30, kv_restriction=1 << 27,
+                      emit_per_object=32),
     "uniform-3M": dict(objects=3_000_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
                        buckets=1 << 26, kv_restriction=1 << 25),
     "uniform-100k": dict(objects=100_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
@@ -90,7 +104,8 @@ def dist_env():
 def make_trace_cfg(w, seed):
     from stcdb_gb300.tracegen import hotspot_grid, uniform_grid
     if w["hot"]:
-        return hotspot_grid(w["objects"], n_hotspots=w["hot"], seed=seed)
+        return hotspot_grid(w["objects"], n_hotspots=w["hot"], seed=seed, hot_frac=w.get("hot_frac", 0.7),
+                            sigma_m=w.get("sigma_m", 300.0))
     return uniform_grid(w["objects"], seed=seed)
 
 
@@ -100,6 +115,7 @@ def make_cfg(w, device=0, step_slices=0):
     return StcConfig(num_objects=w["objects"], reach_distance=w["reach"], min_meet_time=w["min_meet"],
                      grid_capacity=w["grid_capacity"], grid_amplify=w["amplify"], num_meeting_buckets=b,
                      device=device, kv_restriction=w["kv_restriction"], step_slices=step_slices,
+                     emit_capacity=w.get("emit_per_object", 0) * w["objects"],
                      refine_blocks_per_sm=w.get("refine_bps", 0), hits_blocks_per_sm=w.get("hits_bps", 0))
 
 
@@ -204,6 +220,22 @@ def run_gpu(args, w, rank, local):
         gen.next_into(stage.data_ptr(), n)
         host[lo:lo + n].copy_(stage[:n])
     gen.close()
+    # the host link's copy rates for one step's positions (page-locked host
+    # memory, CUDA events, best of three): the end-to-end rate cannot beat
+    # the step's input copy
+    link = {}
+    for name, src, dst in (("h2d", host[0], stage[0]), ("d2h", stage[0], host[0])):
+        best = None
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        link[name + "_gbs"] = 16.0 * N / (best / 1e3) / 1e9
+    link["bytes"] = 16 * N
     del stage
     hnp = HostSteps(host.numpy(), W + K)
     torch.cuda.synchronize()
@@ -284,7 +316,7 @@ def run_gpu(args, w, rank, local):
         compaction = dict(blocks=2, keys=keys_in, split=10, ms=cms, keys_per_s=keys_in / (cms / 1e3),
                           out_ctf_keys=int(out.ctf_kv_count), out_oversize_keys=int(out.oversize_kv_count))
     pipe.close()
-    return dict(stats=stats, dev_ms=dev_ms, wall_dev=wall_dev, wall_e2e=wall_e2e, e2e_stats=e2e_stats,
+    return dict(stats=stats, dev_ms=dev_ms, wall_dev=wall_dev, wall_e2e=wall_e2e, e2e_stats=e2e_stats, link=link,
                 d2h=d2h, clocks=clk.summary(), flush=flush, queries=queries, trace_gen=trace_gen,
                 compaction=compaction, bit_exact=bit_exact_check(args.workload, rank, checked, units, W + K))
 
@@ -815,7 +847,9 @@ def main():
     threads = os.cpu_count() or 1
     workload_cfg = {"workload": args.workload, "objects": N, "steps_per_run": args.steps,
                     "street_grid": "200x200 over 40 km, jitter 20 m", "speed_mps": [1, 15],
-                    "hotspots": w["hot"], "reach_m": w["reach"], "min_meet_steps": w["min_meet"],
+                    "hotspots": w["hot"], "hot_frac": w.get("hot_frac", 0.7) if w["hot"] else 0.0,
+                    "sigma_m": w.get("sigma_m", 300.0) if w["hot"] else None,
+                    "reach_m": w["reach"], "min_meet_steps": w["min_meet"],
                     "leaf_capacity": w["grid_capacity"], "grid_amplify": w["amplify"],
                     "launch_shape": {"refine_blocks_per_sm": w.get("refine_bps", 8),
                                      "hits_blocks_per_sm": w.get("hits_bps", 16)},
@@ -865,7 +899,7 @@ def main():
         "ms_per_step": r["dev_ms"] / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded grid-graph traces)", "config": workload_cfg,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 16 * N,
-                "d2h_bytes_per_step": int(r["d2h"] / K)},
+                "d2h_bytes_per_step": int(r["d2h"] / K), "host_link": r["link"]},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
@@ -874,6 +908,8 @@ def main():
                      "traffic_source": "ncu capture of k_refine_a + k_hits at 3M objects, scaled by hits",
                      "algorithmic_bytes": kb[dom], "launch_ms": phase_ms[dom]},
         "phase_ms": phase_ms,
+        "phase_gbs": {k: kb[k] / (phase_ms[k] / 1e3) / 1e9 for k in kb if phase_ms[k] > 0},
+        "phase_frac_of_peak": {k: kb[k] / (phase_ms[k] / 1e3) / 1e9 / peak for k in kb if phase_ms[k] > 0},
         "flush": flush_line(r["flush"], peak),
         "queries_under_ingest": r["queries"],
         "trace_gen": r["trace_gen"],

@@ -77,7 +77,8 @@ typedef struct stc_config {
   int32_t mbr_filter;            /* drop meetings whose MBR leaves the map box (cuda/geometry.cu:667-670) */
   uint64_t candidate_capacity;   /* new-meeting candidates per step; 0 = auto */
   uint64_t emit_capacity;        /* emitted meetings held between drains; 0 = auto */
-  uint64_t hit_capacity;         /* pairs buffered between refinement and table update; 0 = auto */
+  uint64_t hit_capacity;         /* pairs buffered between refinement and table update; 0 = auto:
+                                    max(4M, 8 n), grown after a step (or window) that found more */
   uint32_t device;               /* CUDA device ordinal */
   uint32_t flags;                /* STC_FLAG_* (0 for normal operation) */
   /* Memtable and flush into a contact tracing block (CTB) of CTFs, the
@@ -183,7 +184,8 @@ typedef struct stc_tune_result {
  * steps from a fresh context (memtable off) and is scored by the device time
  * of its steps after the first two; the leaf capacity is chosen first among
  * `capacities` (n_capacities values; null = {grid_capacity / 2,
- * grid_capacity, 2 * grid_capacity}), then job_chunk, refine_blocks_per_sm and
+ * grid_capacity, 2 * grid_capacity}; cfg's own grid_capacity is always tried
+ * and gives base_step_ms), then job_chunk, refine_blocks_per_sm and
  * hits_blocks_per_sm one after the other. The launch shape never changes
  * results; the leaf capacity is part of the reference's configuration (it
  * orders the reference's table inserts), so a run with the chosen capacity

@@ -384,7 +384,7 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
             dalloc(c, &p.sort_hist2, radix_hist_words(nu)) && dalloc(c, &p.scan_tmp2, scan_words) &&
             dalloc(c, &p.grid_start, (size_t)p.G + 1) && dalloc(c, &p.pts, n) && dalloc(c, &p.fxy, n) &&
             dalloc(c, &p.spts, n) && dalloc(c, &p.sorig, n) && dalloc(c, &p.scand, n) &&
-            dalloc(c, &p.lstrip, p.G) &&
+            dalloc(c, &p.lstrip, p.G) && dalloc(c, &p.cchunks, p.G) &&
             dalloc(c, &p.bcount, (size_t)n + 1) && dalloc(c, &p.boff, (size_t)n + 1) &&
             dalloc(c, &p.blist, n) && dalloc(c, &p.bres, 4 * (size_t)n) && dalloc(c, &p.sd.fbox, p.S) &&
             dalloc(c, &p.bu_gid, p.U_cap) && dalloc(c, &p.bu_pid, p.U_cap) && dalloc(c, &p.bu_sorted_gid, p.U_cap) &&
@@ -625,6 +625,30 @@ static void fill_stats(stc_ctx *c, uint32_t t, const float *phase, float step_ms
 // (cuda/geometry.cu:1752).
 static bool flush_due(const stc_ctx *c) { return c->lsm_on && c->st_host->kv_count > c->cfg.kv_restriction; }
 
+// With the automatic hit capacity (stc_config.hit_capacity 0) the hit buffer
+// grows to the largest step seen: hits beyond it are applied inside the pair
+// tests, which is correct but slow (they hold the pair-test warps on random
+// table accesses). Called only with no step in flight; a failed allocation
+// keeps the old buffer.
+static void grow_hits(stc_ctx *c, unsigned long long need) {
+  PipeDev &p = c->p;
+  if (c->cfg.hit_capacity || need <= p.hit_cap) return;
+  const unsigned long long cap = next_pow2(need + need / 4);
+  void *h = nullptr;
+  if (cudaMalloc(&h, cap * sizeof(HitRec)) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  for (void *&a : c->allocs)
+    if (a == (void *)p.hits) {
+      cudaFree(a);
+      a = h;
+    }
+  p.hits = (HitRec *)h;
+  p.hit_cap = cap;
+  c->graph_valid[0] = c->graph_valid[1] = false;  // the graphs hold the buffer by value
+}
+
 static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copied) {
   PipeDev &p = c->p;
   cudaStream_t s = c->stream;
@@ -642,6 +666,7 @@ static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copie
   float tot = 0;
   cudaEventElapsedTime(&tot, c->ev[PH_START], c->ev[PH_SCHEMA]);
   fill_stats(c, t, phase, tot, (uint32_t)(tl_launches - launches0));
+  grow_hits(c, c->st_host->hit_count);
   if (flush_due(c)) return flush_now(c, t);
   return STC_OK;
 }
@@ -828,6 +853,7 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   };
 
   size_t n = 0;
+  unsigned long long most_hits = 0;  // the window's largest step (hit buffer growth at its end)
   unsigned long long dpos = 0;  // emit records [0, dpos) are on their way to out
   bool out_full = false;
   stc_status rs = STC_OK;
@@ -856,6 +882,7 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
     }
     if (rs == STC_OK) rs = take_state(i);
     if (rs == STC_OK) ran = i + 1;
+    if (rs == STC_OK) most_hits = std::max(most_hits, c->st_host->hit_count);
     if (rs == STC_OK && out && !out_full) {
       const unsigned long long cnt = std::min<unsigned long long>(c->st_host->emit_count, p.E);
       const size_t k = (size_t)std::min<unsigned long long>(cnt - dpos, cap - n);
@@ -895,11 +922,15 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
     }
     if (i + 1 < steps) {
       if (!ahead) {
-        // held: every record emitted so far is drained or on its way out, and
-        // nothing is in flight; empty the buffer, then go on
-        e = emit_keep_tail(c, dpos, std::min<unsigned long long>(c->st_host->emit_count, p.E));
-        if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window drain");
-        dpos = 0;
+        // held: nothing is in flight; every record emitted so far is drained
+        // or on its way out, so the emit buffer can be emptied, and the hit
+        // buffer can grow to the window's largest step
+        if (out) {
+          e = emit_keep_tail(c, dpos, std::min<unsigned long long>(c->st_host->emit_count, p.E));
+          if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window drain");
+          dpos = 0;
+        }
+        grow_hits(c, most_hits);
         hold = false;
         rs = issue_core(i + 1);
         if (rs == STC_OK && i + 2 < steps) {
@@ -917,8 +948,11 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
         return rs;
       }
       // step i + 1 adds its meetings behind step i's; past half of the
-      // buffer, step i + 2 waits until the buffer has been emptied
+      // emit buffer, step i + 2 waits until the buffer has been emptied
       if (out && c->st_host->emit_count > p.E / 2) hold = true;
+      // a step found more hits than the hit buffer holds (the rest were
+      // applied inside its pair tests): grow it at the next step boundary
+      if (!c->cfg.hit_capacity && most_hits > p.hit_cap) hold = true;
     }
   }
   cudaStreamSynchronize(c->copy_stream);
@@ -926,6 +960,8 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
     e = emit_keep_tail(c, dpos, std::min<unsigned long long>(c->st_host->emit_count, p.E));
     if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window drain");
   }
+  cudaStreamSynchronize(s);
+  grow_hits(c, most_hits);
   return STC_OK;
 }
 

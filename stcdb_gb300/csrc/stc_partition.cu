@@ -13,7 +13,7 @@
 //   k_border    depth-first lookup of the top/right leaves within reach of a
 //               border point (tracing/filter.cpp:130-152), counted then filled
 //               in the reference's unit order (pid, then DFS order)
-//   k_jobs      per-leaf work tiles for the refinement
+//   k_jobs      per-leaf refinement jobs (32 rows x one chunk of candidates)
 #include "stc_pipeline.cuh"
 
 namespace stc {
@@ -171,7 +171,24 @@ __global__ void __launch_bounds__(256) k_strip_order(PipeDev p) {
     // (offset, position) pairs, its elements in four slots of 32 lanes
     for (uint32_t sidx = 0; sidx < H; sidx++) {
       const uint32_t st = hist[sidx], L = hist[sidx + 1] - st;
-      if (L > XSORT_MAX) continue;
+      if (L > XSORT_MAX || L < 2) continue;  // one member: in order already
+      if (L <= 32) {
+        // one member per lane (most strips)
+        const float4 v = lane < L ? p.spts[base + st + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const uint32_t og = lane < L ? p.sorig[base + st + lane] : 0u;
+        uint32_t rk = 0;
+        for (uint32_t b = 0; b < L; b++) {
+          const float xb = __shfl_sync(0xffffffffu, v.x, b);
+          rk += (xb < v.x || (xb == v.x && b < lane)) ? 1u : 0u;
+        }
+        __syncwarp();
+        if (lane < L) {
+          p.spts[base + st + rk] = v;
+          p.sorig[base + st + rk] = og | STRIP_XSORTED;
+        }
+        __syncwarp();
+        continue;
+      }
       const uint32_t slots = (L + 31) / 32;
       float4 v[4];
       uint32_t og[4], rk[4] = {0, 0, 0, 0};
@@ -206,27 +223,37 @@ __global__ void __launch_bounds__(256) k_strip_order(PipeDev p) {
       }
       __syncwarp();
     }
-    // candidate ranges of every member (positions within the leaf)
+    // candidate ranges of every member (positions within the leaf); the
+    // longest range of any 32-member row block sets the leaf's candidate
+    // chunks per row block (k_jobs)
     const float4 *lp = p.spts + base;
-    for (uint32_t i = lane; i < n; i += 32) {
-      const uint32_t sidx = (p.sorig[base + i] >> 16) & 63u;
-      const float xi = lp[i].x;
-      const uint32_t en = hist[sidx + 1];
-      const bool xs = en - hist[sidx] <= XSORT_MAX;
-      const uint32_t e1 = xs ? x_bound(lp, i + 1, en, xi + wx, true) : en;
-      uint32_t a2 = 0, b2 = 0;
-      if (sidx + 1 < H) {
-        const uint32_t st2 = hist[sidx + 1], en2 = hist[sidx + 2];
-        if (en2 - st2 <= XSORT_MAX) {
-          a2 = x_bound(lp, st2, en2, xi - wx, false);
-          b2 = x_bound(lp, a2, en2, xi + wx, true);
-        } else {
-          a2 = st2;
-          b2 = en2;
+    uint32_t longest = 0;
+    for (uint32_t i0 = 0; i0 < n; i0 += 32) {
+      const uint32_t i = i0 + lane;
+      uint32_t len = 0;
+      if (i < n) {
+        const uint32_t sidx = (p.sorig[base + i] >> 16) & 63u;
+        const float xi = lp[i].x;
+        const uint32_t en = hist[sidx + 1];
+        const bool xs = en - hist[sidx] <= XSORT_MAX;
+        const uint32_t e1 = xs ? x_bound(lp, i + 1, en, xi + wx, true) : en;
+        uint32_t a2 = 0, b2 = 0;
+        if (sidx + 1 < H) {
+          const uint32_t st2 = hist[sidx + 1], en2 = hist[sidx + 2];
+          if (en2 - st2 <= XSORT_MAX) {
+            a2 = x_bound(lp, st2, en2, xi - wx, false);
+            b2 = x_bound(lp, a2, en2, xi + wx, true);
+          } else {
+            a2 = st2;
+            b2 = en2;
+          }
         }
+        p.scand[base + i] = make_uint2(e1 | a2 << 16, b2);
+        len = (e1 - (i + 1)) + (b2 - a2);
       }
-      p.scand[base + i] = make_uint2(e1 | a2 << 16, b2);
+      longest = max(longest, __reduce_max_sync(0xffffffffu, len));
     }
+    if (lane == 0) p.cchunks[g] = max(1u, (longest + REFINE_CHUNK - 1) / REFINE_CHUNK);
     if (lane == 0) p.lstrip[g] = make_float4(inv, (float)H, wx, 0.0f);
     __syncwarp();
   }
@@ -376,8 +403,10 @@ __global__ void k_jobs(PipeDev p) {
   uint32_t n = cnt < p.leaf_cap ? cnt : p.leaf_cap;
   if (cnt > p.leaf_cap) atomicAdd(&p.st->overflow_objects, cnt - p.leaf_cap);
   uint32_t m = p.bu_cnt[g];
-  // one job: 32 members (strip order) or 32 border units against their candidate ranges
-  uint32_t jobs = n ? (n + 31) / 32 + (m + 31) / 32 : 0;
+  // one job: 32 members (strip order) or 32 border units against one chunk
+  // of REFINE_CHUNK positions of their candidate ranges (a border unit's
+  // ranges hold at most n members)
+  uint32_t jobs = n ? (n + 31) / 32 * p.cchunks[g] + (m + 31) / 32 * ((n + REFINE_CHUNK - 1) / REFINE_CHUNK) : 0;
   p.job_cnt[g] = jobs;
 }
 

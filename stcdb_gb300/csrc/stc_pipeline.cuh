@@ -7,6 +7,10 @@ namespace stc {
 
 // sorig flag: the member's strip is ordered by longitude offset
 #define STRIP_XSORTED (1u << 22)
+// Candidate positions per refinement job and lane: a row block's candidate
+// ranges are cut into chunks of this many, so that the n^2 / 2 pair tests of
+// a dense leaf spread over many warps.
+constexpr uint32_t REFINE_CHUNK = 256;
 
 struct PipeDev {
   // sizes
@@ -47,6 +51,7 @@ struct PipeDev {
   uint32_t *sorig;
   uint2 *scand;
   float4 *lstrip;
+  uint32_t *cchunks;                    // G: candidate chunks of REFINE_CHUNK per own row block
   // border units
   uint32_t *bcount, *boff;              // N+1 (border units per pid, exclusive offsets)
   uint32_t *blist;                      // N: pids of border points (any order)

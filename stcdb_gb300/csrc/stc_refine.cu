@@ -12,8 +12,9 @@
 // after it in its strip up to its window's end and its window in the next
 // strip, or for a border unit its window in the three strips beside its
 // point -- can hit, and only those are tested. A job is 32 rows (members or
-// border units) of one leaf, one per lane, each over its own contiguous
-// segments. Each hit keeps the reference's priority: the finding unit's
+// border units) of one leaf, one per lane, each over one chunk of
+// REFINE_CHUNK positions of its own contiguous segments (a dense leaf's
+// n^2 / 2 pair tests spread over many jobs). Each hit keeps the reference's priority: the finding unit's
 // rank and the member's index in pid order.
 //
 // Distance decisions equal the reference's fp64 test
@@ -253,8 +254,8 @@ __device__ __forceinline__ uint32_t strip_x_bound(const float4 *pts, uint32_t lo
 // the three strips beside its point). A lane's candidates come in up to
 // three contiguous segments, each read 32 at a time; hits are marked in a
 // bitmask and turned into records after each group.
-__device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblock, uint32_t n, uint32_t t,
-                         Counters &ct, HitRec *q, uint32_t &qn, HitWindow &w) {
+__device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblock, uint32_t chunk, uint32_t n,
+                         uint32_t t, Counters &ct, HitRec *q, uint32_t &qn, HitWindow &w) {
   const uint32_t lane = lane_id();
   const uint32_t lt_mask = (1u << lane) - 1u;
   const uint32_t base = p.grid_start[g];
@@ -314,6 +315,20 @@ __device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblo
         sa[k] = a;
         sl[k] = b - a;
       }
+    }
+  }
+  // this job's chunk: positions [chunk * REFINE_CHUNK, (chunk + 1) *
+  // REFINE_CHUNK) of the lane's segments taken one after the other
+  {
+    uint32_t skip = chunk * REFINE_CHUNK, take = REFINE_CHUNK;
+#pragma unroll
+    for (int seg = 0; seg < 3; seg++) {
+      const uint32_t d = min(skip, sl[seg]);
+      sa[seg] += d;
+      skip -= d;
+      const uint32_t tk = min(take, sl[seg] - d);
+      sl[seg] = tk;
+      take -= tk;
     }
   }
   // error margin: offsets of the members are within the leaf's extent; a
@@ -431,9 +446,13 @@ __global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint3
       const uint32_t local = (uint32_t)(job - p.job_start[g]);
       const uint32_t cnt = p.grid_count[g];
       const uint32_t n = cnt < p.leaf_cap ? cnt : p.leaf_cap;
-      const uint32_t R = (n + 31) / 32;
-      if (local < R) run_rows(p, g, true, local, n, t, ct, q, qn, w);
-      else run_rows(p, g, false, local - R, n, t, ct, q, qn, w);
+      const uint32_t R = (n + 31) / 32, cc = p.cchunks[g], own_jobs = R * cc;
+      if (local < own_jobs) {
+        run_rows(p, g, true, local / cc, local % cc, n, t, ct, q, qn, w);
+      } else {
+        const uint32_t ccb = (n + REFINE_CHUNK - 1) / REFINE_CHUNK, b = local - own_jobs;
+        run_rows(p, g, false, b / ccb, b % ccb, n, t, ct, q, qn, w);
+      }
     }
   }
   if (qn) flush_queue(p, q, qn, t, w);

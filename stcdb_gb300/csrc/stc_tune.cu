@@ -62,6 +62,8 @@ extern "C" stc_status stc_autotune(const stc_config *cfg, const double mbr[4], c
   std::vector<uint32_t> caps;
   if (n_capacities) caps.assign(capacities, capacities + n_capacities);
   else caps = {std::max<uint32_t>(cfg->grid_capacity / 2, 8u), cfg->grid_capacity, 2 * cfg->grid_capacity};
+  // the configuration's own capacity is always a candidate (it gives base_step_ms)
+  if (std::find(caps.begin(), caps.end(), cfg->grid_capacity) == caps.end()) caps.insert(caps.begin(), cfg->grid_capacity);
   stc_tune_result r;
   r.config = *cfg;
   r.trials = 0;
