@@ -410,7 +410,7 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
     stored = [0]  # contacts returned to the bench
 
     def take(cap, wait_ms):
-        a, c = srv.poll(cap=cap, contacts_cap=1 << 22, wait_ms=wait_ms)
+        a, c = srv.poll(cap=cap, contacts_cap=1 << 20, wait_ms=wait_ms)
         if len(a):
             answers.append(a)
             stored[0] += int(a["stored"].sum())

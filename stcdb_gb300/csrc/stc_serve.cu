@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <condition_variable>
 #include <deque>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -84,15 +85,31 @@ static uint64_t footprint(const stc_server &s, const stc_query &q) {
 // batch's matches exceed the reservation (some query is over its cap), the
 // queries within their caps run once more on their own; their matches fit
 // the reservation by construction.
-static void answer(stc_server *s, int lane, const std::vector<stc_query> &qs, std::vector<Done> &ready) {
+// A worker's host buffer for a batch's contacts: allocated once to the
+// largest reservation seen and never cleared (a batch's reservation runs to
+// tens of MB; allocating and zeroing it per batch cost milliseconds).
+struct ContactBuf {
+  std::unique_ptr<stc_contact[]> p;
+  size_t cap = 0;
+  stc_contact *at_least(size_t n) {
+    if (n > cap) {
+      p.reset(new stc_contact[n]);  // default-initialised: no zeroing
+      cap = n;
+    }
+    return p.get();
+  }
+};
+
+static void answer(stc_server *s, int lane, const std::vector<stc_query> &qs, std::vector<Done> &ready,
+                   ContactBuf &buf) {
   const size_t n = qs.size();
   const uint64_t rcap = s->cfg.result_cap;
   size_t reserve = 0;
   for (const stc_query &q : qs)
     if (!(q.kind & STC_QUERY_COUNT_ONLY)) reserve += rcap;
-  std::vector<stc_contact> out(std::max<size_t>(reserve, 1));
+  stc_contact *const out = buf.at_least(std::max<size_t>(reserve, 1));
   std::vector<uint64_t> offsets(n + 1, 0), counts(n, 0);
-  stc_status st = stc::query_batch_limited(s->ctx, lane, qs.data(), n, out.data(), reserve, offsets.data(),
+  stc_status st = stc::query_batch_limited(s->ctx, lane, qs.data(), n, out, reserve, offsets.data(),
                                            counts.data(), std::max<size_t>(reserve, 1));
   bool wrote = st == STC_OK && offsets[n] <= reserve;
   std::vector<size_t> again;  // contact queries within their cap, when the batch's output was not written
@@ -106,7 +123,7 @@ static void answer(stc_server *s, int lane, const std::vector<stc_query> &qs, st
     if (counts[i] > rcap) {
       d.a.status = STC_ERR_CAPACITY;  // more contacts than its reservation
     } else if (wrote) {
-      d.contacts.assign(out.begin() + (ptrdiff_t)offsets[i], out.begin() + (ptrdiff_t)offsets[i + 1]);
+      d.contacts.assign(out + offsets[i], out + offsets[i + 1]);
       d.a.stored = (uint32_t)d.contacts.size();
     } else {
       again.push_back(i);
@@ -116,7 +133,7 @@ static void answer(stc_server *s, int lane, const std::vector<stc_query> &qs, st
   std::vector<stc_query> q2(again.size());
   for (size_t j = 0; j < again.size(); j++) q2[j] = qs[again[j]];
   offsets.assign(q2.size() + 1, 0);
-  st = stc::query_batch_limited(s->ctx, lane, q2.data(), q2.size(), out.data(), reserve, offsets.data(), nullptr,
+  st = stc::query_batch_limited(s->ctx, lane, q2.data(), q2.size(), out, reserve, offsets.data(), nullptr,
                                 std::max<size_t>(reserve, 1));
   wrote = st == STC_OK && offsets[q2.size()] <= reserve;
   for (size_t j = 0; j < again.size(); j++) {
@@ -125,7 +142,7 @@ static void answer(stc_server *s, int lane, const std::vector<stc_query> &qs, st
       d.a.status = st != STC_OK ? (uint32_t)st : (uint32_t)STC_ERR_CAPACITY;  // the blocks changed meanwhile
       continue;
     }
-    d.contacts.assign(out.begin() + (ptrdiff_t)offsets[j], out.begin() + (ptrdiff_t)offsets[j + 1]);
+    d.contacts.assign(out + offsets[j], out + offsets[j + 1]);
     d.a.stored = (uint32_t)d.contacts.size();
   }
 }
@@ -133,6 +150,7 @@ static void answer(stc_server *s, int lane, const std::vector<stc_query> &qs, st
 static void serve(stc_server *s, int lane) {
   std::vector<Pending> take;
   std::vector<stc_query> qs;
+  ContactBuf buf;
   for (;;) {
     take.clear();
     uint64_t bytes = 0;
@@ -170,7 +188,7 @@ static void serve(stc_server *s, int lane) {
     qs.resize(n);
     for (size_t i = 0; i < n; i++) qs[i] = take[i].q;
     std::vector<Done> ready(n);
-    answer(s, lane, qs, ready);
+    answer(s, lane, qs, ready, buf);
     const double t_done = mono_now();
     for (size_t i = 0; i < n; i++) {
       ready[i].a.ticket = take[i].ticket;

@@ -589,17 +589,20 @@ class Server:
         return int(first.value)
 
     def poll(self, cap: int = 65536, contacts_cap: int = 0, wait_ms: int = 0) -> tuple:
-        """(answers, contacts) completed since the last poll."""
-        ans = np.empty(cap, ANSWER_DTYPE)
-        con = np.empty(max(contacts_cap, 1), CONTACT_DTYPE)
+        """(answers, contacts) completed since the last poll (copies; the
+        receiving buffers are kept between polls)."""
+        if getattr(self, "_ans", None) is None or len(self._ans) < cap:
+            self._ans = np.empty(cap, ANSWER_DTYPE)
+        if getattr(self, "_con", None) is None or len(self._con) < max(contacts_cap, 1):
+            self._con = np.empty(max(contacts_cap, 1), CONTACT_DTYPE)
         n = ctypes.c_size_t(0)
-        st = self._lib.stc_server_poll(self._h, ans.ctypes.data, cap, con.ctypes.data, contacts_cap,
+        st = self._lib.stc_server_poll(self._h, self._ans.ctypes.data, cap, self._con.ctypes.data, contacts_cap,
                                        ctypes.byref(n), int(wait_ms))
         if st != 0:
             raise StcError(st, "stc_server_poll")
-        a = ans[: n.value]
+        a = self._ans[: n.value].copy()
         used = int((a["contact_offset"] + a["stored"]).max()) if len(a) else 0
-        return a, con[:used]
+        return a, self._con[:used].copy()
 
     def stats(self) -> ServerStats:
         s = ServerStats()
