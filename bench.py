@@ -29,10 +29,11 @@ e2e: the same metric through the public C ABI with host input: windows of
   10 steps (stc_step_window), every step's positions copied from pinned host
   memory (the next step's while the current one runs) and its emitted
   meetings drained back to the host after it; wall clock.
-queries_under_ingest: K more steps (host input) while a serving thread answers
-  a Poisson query stream (default 20,000/s; 60% object, 40% box queries) over
-  the flushed block by continuous batching; queries return match counts, as
-  the reference's searches do; p50/p99 latency from arrival.
+queries_under_ingest: 2K more steps (host input, pipelined windows of 4
+  steps) while the library's serving workers answer a Poisson query stream
+  (default 20,000/s) over the flushed block by continuous batching: 60%
+  object queries returning their contacts, 40% box queries returning match
+  counts, as the reference's searches do; p50/p99 latency from arrival.
 batched: 64 uneven ingest windows (100k-2M objects log-uniform, a tenth of
   the batching configuration's 1M-20M, which --batched-full runs; 10-50
   steps, reach 5/10/20 m, 0-90% hotspot, lowered where the table would not fit) run
@@ -79,6 +80,8 @@ WORKLOADS = {
                        buckets=1 << 29, kv_restriction=1 << 27, emit_per_object=16),
     "hotspot-3M": dict(objects=3_000_000, hot=1000, reach=10.0, min_meet=5, grid_capacity=200, amplify=8.0,
                        buckets=1 << 30, kv_restriction=1 << 27, emit_per_object=16),
+    "hotspot-5M": dict(objects=5_000_000, hot=1000, reach=10.0, min_meet=5, grid_capacity=200, amplify=8.0,
+                       buckets=1 << 31, kv_restriction=1 << 27, emit_per_object=16),
     # the stress configuration's model (90% of objects in 200 hotspots,
     # sigma 150 m, reach 20 m, minimum meeting 3 steps) at the largest object
     # count whose live pairs fit a table in HBM: its Zipf-weighted first
@@ -86,7 +89,7 @@ WORKLOADS = {
     # (about 3e8 at 1M objects)
     "stress-1M": dict(objects=1_000_000, hot=200, hot_frac=0.9, sigma_m=150.0, reach=20.0, min_meet=3,
                       grid_capacity=200, amplify=32.0, buckets=1 << 30, kv_restriction=1 << 27,
-                      emit_per_object=32),
+                      emit_per_object=128),
     "uniform-3M": dict(objects=3_000_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
                        buckets=1 << 26, kv_restriction=1 << 25),
     "uniform-100k": dict(objects=100_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
@@ -183,6 +186,7 @@ def measured_peaks():
 
 
 E2E_WINDOW = 10  # steps per stc_step_window call of the end-to-end run
+SERVE_WINDOW = 4  # steps per stc_step_window call while the server answers queries
 
 
 class HostSteps:
@@ -444,11 +448,13 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
     th.start()
     step_ms = []
     w0 = time.perf_counter()
-    for t in range(t0, t0 + steps):
-        pipe.step(hnp[t], t)
-        pipe.drain(mout)
+    # ingest as pipelined windows (stc_step_window, host input, meetings
+    # drained into the page-locked buffer), as the end-to-end run does
+    for w0t in range(t0, t0 + steps, SERVE_WINDOW):
+        n = min(SERVE_WINDOW, t0 + steps - w0t)
+        pipe.step_window(hnp.arr[w0t - hnp.first:w0t - hnp.first + n], w0t, out=mout)
         step_ms.append(pipe.stats().step_ms)
-        cur_t[0] = t
+        cur_t[0] = w0t + n - 1
     wall = time.perf_counter() - w0
     done.set()
     th.join()
@@ -508,7 +514,8 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
                        "overlapped_batches": int(sst.overlapped_batches)},
             "mix": "60% object queries returning contacts (meets-whom, window 10-10000 steps), 40% box "
                    "queries returning match counts (50 m-5 km, window 10-3600 steps)",
-            "blocks": 1, "step_slices": args.serve_slices, "ingest_pos_updates_per_s": N * steps / wall,
+            "blocks": 1, "step_slices": args.serve_slices, "ingest_window_steps": SERVE_WINDOW,
+            "ingest_pos_updates_per_s": N * steps / wall,
             "ingest_device_ms_per_step": float(np.mean(step_ms))}
 
 
@@ -529,11 +536,12 @@ def max_over_ranks(args, v):
 
 
 # DRAM bytes (read + write) of the refinement phase (k_refine_a + k_hits)
-# per hit, from one ncu capture of both kernels on the 3M-object workload:
-# 1.414 GB for 6.09M hits. The traffic grows with the hits (records written
-# and read, one table slot and two positions per hit), so the 10M line scales
-# it by its own hit count.
-REFINE_DRAM_BYTES_PER_HIT = 1.414e9 / 6.085e6
+# per hit, from one ncu capture of each kernel on the 3M-object workload
+# (profiles/kernels_refine_hits_strips_uniform-3M.md): 347.7 MB for one of
+# the step's four parts, about a quarter of its 6.086M hits. The traffic
+# grows with the hits (records written and read, one table slot and two
+# positions per hit), so the 10M line scales it by its own hit count.
+REFINE_DRAM_BYTES_PER_HIT = 347.7e6 / (6.086e6 / 4)
 
 
 def kernel_bytes(s, N, B):
@@ -833,7 +841,7 @@ def main():
                     help="launches per long step kernel (stc_config.step_slices; 0 = 1)")
     ap.add_argument("--serve-steps", type=int, default=0,
                     help="ingest steps of the serving phase (0 = twice --steps)")
-    ap.add_argument("--serve-slices", type=int, default=8,
+    ap.add_argument("--serve-slices", type=int, default=1,
                     help="step slices while the serving phase answers queries (stc_set_step_slices)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
