@@ -12,11 +12,11 @@ slots (about 68M pairs are live per step, so the reference default of 2N
 slots would overflow). This is the pure-uniform window of the batching
 configuration (1M-20M objects, 0-90% hotspot) at the headline 10M objects.
 The 10M-object hotspot configuration (70% in 1000 Zipf hotspots, sigma
-300 m) does not fit one GPU: its live pairs grow with N^2 (measured 3.5e7
-at 1M objects, so ~3.5e9 at 10M), beyond any 32-byte-slot meeting table
-that fits in HBM. "hotspot-1M" runs that model at 1M objects; "uniform-3M"
-is the default workload at 3M objects (a few GB on the device, the case the
-kernel profiles are captured on).
+300 m) is out of reach of one GPU and of any reference check: its live pairs
+grow with N^2 (measured 24.1M, 97.0M and 212.6M per step at 1M, 2M and 3M
+objects, so about 2.4e9 at 10M). "hotspot-1M" (2M, 3M, 5M) runs that model
+at those counts; "uniform-3M" is the default workload at 3M objects (a few
+GB on the device, the case the kernel profiles are captured on).
 
 value: position updates per second with positions already resident in HBM
   (stc_step_device), summed device time of K steps (CUDA events on the
@@ -25,10 +25,12 @@ value: position updates per second with positions already resident in HBM
 Every step also appends its emitted meetings to the memtable (two directed
   keys each, as the reference's GPU step does); the JSON's "flush" times one
   flush of everything gathered over the run into 100 CTFs.
-e2e: the same metric through the public C ABI with host input: windows of
-  10 steps (stc_step_window), every step's positions copied from pinned host
-  memory (the next step's while the current one runs) and its emitted
-  meetings drained back to the host after it; wall clock.
+e2e: the same metric through the public C ABI with host input: pipelined
+  windows of 10 steps (stc_step_window), every step's positions copied from
+  pinned host memory (the next step's while the current one runs) and its
+  emitted meetings drained back to the host beside the next step; wall
+  clock. "host_link" gives the copy rates of one step's positions and
+  "windows" how busy the windows kept the GPU.
 queries_under_ingest: 2K more steps (host input, pipelined windows of 4
   steps) while the library's serving workers answer a Poisson query stream
   (default 20,000/s) over the flushed block by continuous batching: 60%
@@ -296,6 +298,11 @@ def run_gpu(args, w, rank, local):
         e2e_stats.append(pipe.stats())
     torch.cuda.synchronize()
     wall_e2e = time.perf_counter() - t1
+    e2e_busy = {"window_device_ms": [round(float(s.window_device_ms), 3) for s in e2e_stats],
+                "window_wall_ms": [round(float(s.window_wall_ms), 3) for s in e2e_stats],
+                "gpu_busy_frac": float(sum(s.window_device_ms for s in e2e_stats) /
+                                       max(sum(s.window_wall_ms for s in e2e_stats), 1e-9)),
+                "host_load_avg": list(os.getloadavg()), "host_cpus": os.cpu_count()}
     # one flush of everything the memtable gathered (W + 2K steps)
     keys = pipe.stats().memtable_keys
     pipe.flush()
@@ -321,6 +328,7 @@ def run_gpu(args, w, rank, local):
                           out_ctf_keys=int(out.ctf_kv_count), out_oversize_keys=int(out.oversize_kv_count))
     pipe.close()
     return dict(stats=stats, dev_ms=dev_ms, wall_dev=wall_dev, wall_e2e=wall_e2e, e2e_stats=e2e_stats, link=link,
+                e2e_busy=e2e_busy,
                 d2h=d2h, clocks=clk.summary(), flush=flush, queries=queries, trace_gen=trace_gen,
                 compaction=compaction, bit_exact=bit_exact_check(args.workload, rank, checked, units, W + K))
 
@@ -511,7 +519,9 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
                                "streams)", "max_batch": 4096, "result_cap": result_cap,
                        "hbm_budget_bytes": 64 << 20, "max_batch_queries": int(sst.max_batch_queries),
                        "max_batch_bytes": int(sst.max_batch_bytes), "budget_cuts": int(sst.budget_cuts),
-                       "overlapped_batches": int(sst.overlapped_batches)},
+                       "overlapped_batches": int(sst.overlapped_batches),
+                       "slowest_batch_wall_ms": sst.slowest_batch_wall_us / 1e3,
+                       "slowest_batch_gpu_ms": sst.slowest_batch_gpu_us / 1e3},
             "mix": "60% object queries returning contacts (meets-whom, window 10-10000 steps), 40% box "
                    "queries returning match counts (50 m-5 km, window 10-3600 steps)",
             "blocks": 1, "step_slices": args.serve_slices, "ingest_window_steps": SERVE_WINDOW,
@@ -907,7 +917,7 @@ def main():
         "ms_per_step": r["dev_ms"] / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded grid-graph traces)", "config": workload_cfg,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 16 * N,
-                "d2h_bytes_per_step": int(r["d2h"] / K), "host_link": r["link"]},
+                "d2h_bytes_per_step": int(r["d2h"] / K), "host_link": r["link"], "windows": r["e2e_busy"]},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,

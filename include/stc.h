@@ -148,6 +148,11 @@ typedef struct stc_stats {
   uint64_t memtable_keys;        /* directed keys in the memtable after the step (and any flush) */
   uint32_t flushes;              /* blocks flushed so far */
   float flush_ms;                /* device time of the last flush */
+  /* The last stc_step_window call: the device time of its steps (core and
+   * memtable append, flushes excluded) and the call's wall time on the host;
+   * their ratio is how busy the window kept the GPU. */
+  float window_device_ms;
+  float window_wall_ms;
 } stc_stats;
 
 /* Fills *cfg with the reference defaults for n objects (util/config.h:29-41,
@@ -388,6 +393,9 @@ typedef struct stc_server_stats {
   uint64_t max_batch_bytes;      /* largest admitted footprint */
   uint64_t budget_cuts;          /* batches closed by the budget before max_batch */
   uint64_t overlapped_batches;   /* batches that started while another batch was on the GPU */
+  uint64_t slowest_batch_wall_us;  /* the longest batch from its worker's start to its answers */
+  uint64_t slowest_batch_gpu_us;   /* that batch's span on its query stream (from its first copy to
+                                      the read-back of its counts, waits for SMs included) */
 } stc_server_stats;
 
 typedef struct stc_server stc_server;

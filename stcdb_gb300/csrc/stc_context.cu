@@ -5,6 +5,7 @@
 // from device memory inside the kernels), then copies the 128-byte control
 // block back once to report counters and errors.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -852,6 +853,8 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
     return STC_OK;
   };
 
+  const auto wall0 = std::chrono::steady_clock::now();
+  double busy_ms = 0;  // device time of the window's steps
   size_t n = 0;
   unsigned long long most_hits = 0;  // the window's largest step (hit buffer growth at its end)
   unsigned long long dpos = 0;  // emit records [0, dpos) are on their way to out
@@ -881,7 +884,10 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
       }
     }
     if (rs == STC_OK) rs = take_state(i);
-    if (rs == STC_OK) ran = i + 1;
+    if (rs == STC_OK) {
+      ran = i + 1;
+      busy_ms += c->stats.step_ms;
+    }
     if (rs == STC_OK) most_hits = std::max(most_hits, c->st_host->hit_count);
     if (rs == STC_OK && out && !out_full) {
       const unsigned long long cnt = std::min<unsigned long long>(c->st_host->emit_count, p.E);
@@ -962,6 +968,9 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   }
   cudaStreamSynchronize(s);
   grow_hits(c, most_hits);
+  c->stats.window_device_ms = (float)busy_ms;
+  c->stats.window_wall_ms =
+      (float)std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
   return STC_OK;
 }
 
@@ -1096,7 +1105,8 @@ namespace stc {
 // match records held on the device at a time (the serving loop's
 // admission); 0 = none.
 stc_status query_batch_limited(stc_ctx *c, int lane, const stc_query *queries, size_t nq, stc_contact *out,
-                               size_t cap, uint64_t *offsets, uint64_t *counts, size_t device_limit);
+                               size_t cap, uint64_t *offsets, uint64_t *counts, size_t device_limit,
+                               float *gpu_ms = nullptr);
 // Queries one device pass takes (larger batches run as several passes).
 size_t query_chunk(const stc_ctx *c);
 }
@@ -1109,7 +1119,8 @@ extern "C" stc_status stc_query_batch(stc_ctx *c, const stc_query *queries, size
 size_t stc::query_chunk(const stc_ctx *c) { return c && c->lsm_on ? lsm_query_chunk(c->lsmh) : 1; }
 
 stc_status stc::query_batch_limited(stc_ctx *c, int lane, const stc_query *queries, size_t nq, stc_contact *out,
-                                    size_t cap, uint64_t *offsets, uint64_t *counts, size_t device_limit) {
+                                    size_t cap, uint64_t *offsets, uint64_t *counts, size_t device_limit,
+                                    float *gpu_ms) {
   stc_status st = query_checks(c, "stc_query_batch");
   if (st != STC_OK) return st;
   if ((!queries && nq) || !offsets || (!out && cap)) {
@@ -1126,8 +1137,9 @@ stc_status stc::query_batch_limited(stc_ctx *c, int lane, const stc_query *queri
   }
   std::string err;
   const size_t chunk = lsm_query_chunk(c->lsmh);
+  if (gpu_ms) *gpu_ms = 0.f;
   if (nq <= chunk) {
-    st = lsm_query(c->lsmh, lane, queries, nq, out, cap, offsets, counts, err, device_limit);
+    st = lsm_query(c->lsmh, lane, queries, nq, out, cap, offsets, counts, err, device_limit, gpu_ms);
     if (st != STC_OK) g_create_error = "stc_query_batch: " + err;
     return st;
   }
@@ -1140,8 +1152,10 @@ stc_status stc::query_batch_limited(stc_ctx *c, int lane, const stc_query *queri
     const size_t m = std::min(chunk, nq - a);
     const uint64_t done = offsets[a];
     const bool room = out && done <= cap;
+    float ms = 0.f;
     st = lsm_query(c->lsmh, lane, queries + a, m, room ? out + done : nullptr, room ? cap - done : 0, off.data(),
-                   counts ? counts + a : nullptr, err, device_limit);
+                   counts ? counts + a : nullptr, err, device_limit, gpu_ms ? &ms : nullptr);
+    if (gpu_ms) *gpu_ms += ms;
     if (st != STC_OK) {
       g_create_error = "stc_query_batch: " + err;
       return st;

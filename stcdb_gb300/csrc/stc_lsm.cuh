@@ -127,6 +127,7 @@ struct QueryRec {
 struct QueryLane {
   std::mutex mu;                   // held by the batch using the lane
   cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // a batch's span on the stream
   QBlock *d_qb = nullptr;          // [retain]
   stc_query *d_q = nullptr;
   size_t q_cap = 0;
@@ -229,9 +230,12 @@ size_t lsm_query_chunk(const LsmHost &H);
 // on query lane `lane` (-1: the first free lane, else lane 0 once it frees)
 // (see stc_query_batch in include/stc.h). device_limit (0 = none) bounds the
 // match records the device output may hold: a batch with more matches is
-// only counted (offsets and counts filled, out untouched).
+// only counted (offsets and counts filled, out untouched). gpu_ms (optional)
+// receives the batch's span on its lane's stream, from its first copy to its
+// last (waits for SMs included).
 stc_status lsm_query(LsmHost &H, int lane, const stc_query *q, size_t nq, stc_contact *out, size_t cap,
-                     uint64_t *offsets, uint64_t *counts, std::string &err, size_t device_limit = 0);
+                     uint64_t *offsets, uint64_t *counts, std::string &err, size_t device_limit = 0,
+                     float *gpu_ms = nullptr);
 
 // Host restatement of CTF::get_ctf_bits (tracing/step_merge.cpp:140-186);
 // returns false when the key would exceed 64 box bits or 128 key bits.

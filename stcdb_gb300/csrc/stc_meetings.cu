@@ -125,17 +125,33 @@ __device__ __forceinline__ Slot load_slot_stream(const Slot *slots, unsigned lon
 
 // One slot: finalise a meeting claimed this step, keep an extended one, or
 // clear an ended one; returns whether the ended meeting is emitted.
+// A claimed slot's pair: its objects' float positions this step (both
+// requested before the slot is processed; a no-op for other slots).
+struct ClaimPos {
+  float2 fa, fb;
+};
+__device__ __forceinline__ ClaimPos claim_positions(const PipeDev &p, const Slot &s) {
+  ClaimPos c;
+  c.fa = c.fb = make_float2(0.f, 0.f);
+  if (s.key != STC_EMPTY_KEY && (s.key & STC_CLAIM_BIT)) {
+    uint32_t a, b;
+    cantor_decode(s.key & ~STC_CLAIM_BIT, &a, &b);
+    c.fa = __ldg(&p.fxy[a]);
+    c.fb = __ldg(&p.fxy[b]);
+  }
+  return c;
+}
+
 __device__ __forceinline__ bool sweep_slot(const PipeDev &p, uint32_t t, unsigned long long i, const Slot &s,
-                                           unsigned long long &active, unsigned long long &fresh) {
+                                           const ClaimPos &cp, unsigned long long &active,
+                                           unsigned long long &fresh) {
   if (s.key == STC_EMPTY_KEY) return false;
   if (s.key & STC_CLAIM_BIT) {
     // new meeting of this step (cuda/geometry.cu:480-489): start = end = t,
     // MBR = init, then both objects' positions
     Slot nm;
     nm.key = s.key & ~STC_CLAIM_BIT;
-    uint32_t a, b;
-    cantor_decode(nm.key, &a, &b);
-    float2 fa = p.fxy[a], fb = p.fxy[b];
+    const float2 fa = cp.fa, fb = cp.fb;
     nm.start = t;
     nm.end = t;
     nm.lo_x = fminf(STC_INIT_LO, fminf(fa.x, fb.x));
@@ -166,6 +182,7 @@ __device__ __forceinline__ bool sweep_slot(const PipeDev &p, uint32_t t, unsigne
 }
 
 static constexpr uint32_t SWEEP_THREADS = 256;
+static constexpr uint32_t SWEEP_BLOCKS_PER_SM = 5;
 static constexpr uint32_t SWEEP_WARPS = SWEEP_THREADS / 32;
 static constexpr uint32_t SWEEP_UNROLL = 2;                // slots per lane per pass
 static constexpr uint32_t WARP_TILE = 32 * SWEEP_UNROLL;   // slots per warp pass
@@ -194,7 +211,7 @@ __device__ __forceinline__ void flush_emits(const PipeDev &p, const stc_meeting 
 }
 
 // Slice `part` of `parts` sweeps slots [B * part / parts, B * (part + 1) / parts).
-__global__ void __launch_bounds__(SWEEP_THREADS, 6) k_sweep(PipeDev p, uint32_t part, uint32_t parts) {
+__global__ void __launch_bounds__(SWEEP_THREADS, SWEEP_BLOCKS_PER_SM) k_sweep(PipeDev p, uint32_t part, uint32_t parts) {
   const uint32_t t = p.st->step_t;
   __shared__ __align__(16) stc_meeting stage_all[SWEEP_WARPS][WARP_STAGE];
   const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
@@ -213,9 +230,14 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 6) k_sweep(PipeDev p, uint32_t 
       if (idx[u] < B) sl[u] = load_slot_stream(p.slots, idx[u]);
       else sl[u].key = STC_EMPTY_KEY;
     }
+    // the positions of every claimed slot of the pass are requested before
+    // any slot is processed
+    ClaimPos cp[SWEEP_UNROLL];
+#pragma unroll
+    for (uint32_t u = 0; u < SWEEP_UNROLL; u++) cp[u] = claim_positions(p, sl[u]);
 #pragma unroll
     for (uint32_t u = 0; u < SWEEP_UNROLL; u++) {
-      bool emit = idx[u] < B && sweep_slot(p, t, idx[u], sl[u], active, fresh);
+      bool emit = idx[u] < B && sweep_slot(p, t, idx[u], sl[u], cp[u], active, fresh);
       uint32_t ball = __ballot_sync(0xffffffffu, emit);
       if (emit) {
         stc_meeting m;
@@ -252,7 +274,7 @@ __global__ void __launch_bounds__(SWEEP_THREADS, 6) k_sweep(PipeDev p, uint32_t 
 
 void step_sweep(PipeDev &p, cudaStream_t s) {
   for (uint32_t part = 0; part < p.slices; part++)
-    STC_KL k_sweep<<<num_sms() * 6, SWEEP_THREADS, 0, s>>>(p, part, p.slices);
+    STC_KL k_sweep<<<num_sms() * SWEEP_BLOCKS_PER_SM, SWEEP_THREADS, 0, s>>>(p, part, p.slices);
 }
 
 }  // namespace stc

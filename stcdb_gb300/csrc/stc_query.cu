@@ -926,6 +926,9 @@ void lsm_release(LsmHost &H) {
     for (void *v : {(void *)Q.h_qb, (void *)Q.h_q, (void *)Q.h_counts, (void *)Q.h_recs})
       if (v) cudaFreeHost(v);
     if (Q.stream) cudaStreamDestroy(Q.stream);
+    if (Q.ev0) cudaEventDestroy(Q.ev0);
+    if (Q.ev1) cudaEventDestroy(Q.ev1);
+    Q.ev0 = Q.ev1 = nullptr;
     Q.d_qb = nullptr;
     Q.d_q = nullptr;
     Q.d_out = nullptr;
@@ -971,6 +974,8 @@ stc_status lsm_query_reserve(LsmHost &H, size_t nq, uint32_t F, int priority, st
   for (QueryLane &Q : H.lanes) {
     std::lock_guard<std::mutex> ql(Q.mu);
     if (e == cudaSuccess && !Q.stream) e = cudaStreamCreateWithPriority(&Q.stream, cudaStreamNonBlocking, priority);
+    if (e == cudaSuccess && !Q.ev0) e = cudaEventCreate(&Q.ev0);
+    if (e == cudaSuccess && !Q.ev1) e = cudaEventCreate(&Q.ev1);
     if (e == cudaSuccess) e = query_buffers(H, Q, nq, F);
   }
   // load the query kernels now: with lazy module loading their first launch
@@ -1006,7 +1011,7 @@ static std::unique_lock<std::mutex> take_lane(LsmHost &H, int lane, QueryLane **
 }
 
 stc_status lsm_query(LsmHost &H, int lane, const stc_query *qs, size_t nq, stc_contact *out, size_t cap,
-                     uint64_t *offsets, uint64_t *counts, std::string &err, size_t device_limit) {
+                     uint64_t *offsets, uint64_t *counts, std::string &err, size_t device_limit, float *gpu_ms) {
   QueryLane *Qp = nullptr;
   std::unique_lock<std::mutex> qlock = take_lane(H, lane, &Qp);
   QueryLane &Q = *Qp;
@@ -1044,6 +1049,7 @@ stc_status lsm_query(LsmHost &H, int lane, const stc_query *qs, size_t nq, stc_c
   bool has_obj = false, has_box = false;
   for (size_t i = 0; i < nq; i++) ((qs[i].kind & 0xFFu) == STC_QUERY_BOX ? has_box : has_obj) = true;
   memcpy(Q.h_q, qs, nq * sizeof(stc_query));
+  if (gpu_ms) cudaEventRecord(Q.ev0, s);
   e = cudaMemcpyAsync(Q.d_qb, qb, nb * sizeof(QBlock), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(Q.d_q, Q.h_q, nq * sizeof(stc_query), cudaMemcpyHostToDevice, s);
   unsigned long long total = 0;
@@ -1080,6 +1086,13 @@ stc_status lsm_query(LsmHost &H, int lane, const stc_query *qs, size_t nq, stc_c
   if (e != cudaSuccess) {
     err = std::string("query: ") + cudaGetErrorString(e);
     return STC_ERR_CUDA;
+  }
+  // the span up to the counts' read-back (the contacts' copy follows)
+  if (gpu_ms) {
+    cudaEventRecord(Q.ev1, s);
+    cudaEventSynchronize(Q.ev1);
+    *gpu_ms = 0.f;
+    cudaEventElapsedTime(gpu_ms, Q.ev0, Q.ev1);
   }
   if (over) {
     for (size_t i = 0; i < nq; i++) offsets[i + 1] = offsets[i] + Q.h_counts[i];

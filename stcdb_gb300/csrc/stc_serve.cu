@@ -25,7 +25,8 @@
 namespace stc {
 void set_thread_error(const std::string &msg);
 stc_status query_batch_limited(stc_ctx *c, int lane, const stc_query *queries, size_t nq, stc_contact *out,
-                               size_t cap, uint64_t *offsets, uint64_t *counts, size_t device_limit);
+                               size_t cap, uint64_t *offsets, uint64_t *counts, size_t device_limit,
+                               float *gpu_ms);
 size_t query_chunk(const stc_ctx *c);
 }
 
@@ -101,7 +102,7 @@ struct ContactBuf {
 };
 
 static void answer(stc_server *s, int lane, const std::vector<stc_query> &qs, std::vector<Done> &ready,
-                   ContactBuf &buf) {
+                   ContactBuf &buf, float *gpu_ms) {
   const size_t n = qs.size();
   const uint64_t rcap = s->cfg.result_cap;
   size_t reserve = 0;
@@ -110,7 +111,7 @@ static void answer(stc_server *s, int lane, const std::vector<stc_query> &qs, st
   stc_contact *const out = buf.at_least(std::max<size_t>(reserve, 1));
   std::vector<uint64_t> offsets(n + 1, 0), counts(n, 0);
   stc_status st = stc::query_batch_limited(s->ctx, lane, qs.data(), n, out, reserve, offsets.data(),
-                                           counts.data(), std::max<size_t>(reserve, 1));
+                                           counts.data(), std::max<size_t>(reserve, 1), gpu_ms);
   bool wrote = st == STC_OK && offsets[n] <= reserve;
   std::vector<size_t> again;  // contact queries within their cap, when the batch's output was not written
   for (size_t i = 0; i < n; i++) {
@@ -134,7 +135,7 @@ static void answer(stc_server *s, int lane, const std::vector<stc_query> &qs, st
   for (size_t j = 0; j < again.size(); j++) q2[j] = qs[again[j]];
   offsets.assign(q2.size() + 1, 0);
   st = stc::query_batch_limited(s->ctx, lane, q2.data(), q2.size(), out, reserve, offsets.data(), nullptr,
-                                std::max<size_t>(reserve, 1));
+                                std::max<size_t>(reserve, 1), nullptr);
   wrote = st == STC_OK && offsets[q2.size()] <= reserve;
   for (size_t j = 0; j < again.size(); j++) {
     Done &d = ready[again[j]];
@@ -188,7 +189,9 @@ static void serve(stc_server *s, int lane) {
     qs.resize(n);
     for (size_t i = 0; i < n; i++) qs[i] = take[i].q;
     std::vector<Done> ready(n);
-    answer(s, lane, qs, ready, buf);
+    const double t_start = mono_now();
+    float gpu_ms = 0.f;
+    answer(s, lane, qs, ready, buf, &gpu_ms);
     const double t_done = mono_now();
     for (size_t i = 0; i < n; i++) {
       ready[i].a.ticket = take[i].ticket;
@@ -204,6 +207,11 @@ static void serve(stc_server *s, int lane) {
       s->stats.batches++;
       s->stats.max_batch_queries = std::max<uint64_t>(s->stats.max_batch_queries, n);
       s->stats.max_batch_bytes = std::max<uint64_t>(s->stats.max_batch_bytes, bytes);
+      const uint64_t wall_us = (uint64_t)((t_done - t_start) * 1e6);
+      if (wall_us > s->stats.slowest_batch_wall_us) {
+        s->stats.slowest_batch_wall_us = wall_us;
+        s->stats.slowest_batch_gpu_us = (uint64_t)(gpu_ms * 1e3f);
+      }
       s->busy--;
       if (cut) s->stats.budget_cuts++;
     }

@@ -91,6 +91,8 @@ class StcStats(ctypes.Structure):
         ("memtable_keys", ctypes.c_uint64),
         ("flushes", ctypes.c_uint32),
         ("flush_ms", ctypes.c_float),
+        ("window_device_ms", ctypes.c_float),
+        ("window_wall_ms", ctypes.c_float),
     ]
 
     def as_dict(self) -> dict:
@@ -154,7 +156,8 @@ class _ServerConfig(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_uint64), ("answered", ctypes.c_uint64), ("batches", ctypes.c_uint64),
                 ("max_batch_queries", ctypes.c_uint64), ("max_batch_bytes", ctypes.c_uint64),
-                ("budget_cuts", ctypes.c_uint64), ("overlapped_batches", ctypes.c_uint64)]
+                ("budget_cuts", ctypes.c_uint64), ("overlapped_batches", ctypes.c_uint64),
+                ("slowest_batch_wall_us", ctypes.c_uint64), ("slowest_batch_gpu_us", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {name: int(getattr(self, name)) for name, _ in self._fields_}
