@@ -315,7 +315,8 @@ def run_gpu(args, w, rank, local):
     # Poisson query stream over the flushed block
     queries = None
     if args.query_rate > 0:
-        queries = serve_under_ingest(args, pipe, hnp, W + 2 * K, S, N, mbr, mnp)
+        queries = serve_under_ingest(args, pipe, hnp, W + 2 * K, S, N, mbr, mnp,
+                                     dev if args.serve_device_input else None)
     # compaction: the serving steps' keys become a second block; both merge
     # into one block of split x split CTFs (100 CTFs, as a flush makes)
     compaction = None
@@ -400,7 +401,7 @@ def make_queries(rng, n, N, mbr, t_now):
     return q
 
 
-def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
+def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None, dev_steps=None):
     """Queries arrive as a Poisson stream and go to the library's request loop
     (stc_server_*), which answers them by continuous batching (whatever has
     arrived while a batch ran forms the next batch, admitted by device
@@ -460,7 +461,11 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None):
     # drained into the page-locked buffer), as the end-to-end run does
     for w0t in range(t0, t0 + steps, SERVE_WINDOW):
         n = min(SERVE_WINDOW, t0 + steps - w0t)
-        pipe.step_window(hnp.arr[w0t - hnp.first:w0t - hnp.first + n], w0t, out=mout)
+        if dev_steps is not None:  # positions already in HBM (no host link traffic)
+            k = (w0t - t0) % (dev_steps.shape[0] - SERVE_WINDOW + 1)
+            pipe.step_window((dev_steps[k].data_ptr(), n), w0t, out=mout)
+        else:
+            pipe.step_window(hnp.arr[w0t - hnp.first:w0t - hnp.first + n], w0t, out=mout)
         step_ms.append(pipe.stats().step_ms)
         cur_t[0] = w0t + n - 1
     wall = time.perf_counter() - w0
@@ -851,6 +856,9 @@ def main():
                     help="launches per long step kernel (stc_config.step_slices; 0 = 1)")
     ap.add_argument("--serve-steps", type=int, default=0,
                     help="ingest steps of the serving phase (0 = twice --steps)")
+    ap.add_argument("--serve-device-input", action="store_true",
+                    help="serving-phase ingest from positions in HBM (the run's device steps again) "
+                         "instead of host input")
     ap.add_argument("--serve-slices", type=int, default=1,
                     help="step slices while the serving phase answers queries (stc_set_step_slices)")
     args = ap.parse_args()

@@ -33,6 +33,10 @@ void set_thread_error(const std::string &msg) { g_create_error = msg; }
 
 static constexpr size_t DRAIN_CHUNK = (size_t)8 << 20;  // bytes per pinned staging chunk of a drain
 static constexpr uint32_t PAIR_PARTS = 4;                // parts of the pair tests (more while serving)
+// Input buffers of a pipelined window: the positions of step i + 3 are
+// copied in as soon as step i (that buffer's last reader) has run, two steps
+// before they are needed, so that a slow or uneven host link has slack.
+static constexpr int WIN_BUFS = 3;
 
 // A large host<->device copy of a step or drain as pieces of COPY_PIECE
 // bytes: the copy engine takes them one by one, so that the small copies of
@@ -68,25 +72,25 @@ struct stc_ctx {
   // page-locked times of the steps being issued, one word per input buffer
   // (step_begin copies it): a window issues step i + 1 before step i has run
   uint32_t *t_pinned = nullptr;
-  // pipelined windows (stc_step_window): per input buffer b, the state read
-  // back after that step's memtable append, and the step's events
+  // pipelined windows (stc_step_window): per step parity, the state read
+  // back after that step's memtable append and the step's events; per input
+  // buffer, the end of the core that read it
   DevState *st_slot[2] = {nullptr, nullptr};
-  cudaEvent_t st_ev[2] = {nullptr, nullptr};      // the state copy of the step in buffer b has landed
-  cudaEvent_t core_ev[2] = {nullptr, nullptr};    // end of the step's core: its input buffer is free
+  cudaEvent_t st_ev[2] = {nullptr, nullptr};      // the state copy of the step of that parity has landed
+  cudaEvent_t core_ev[WIN_BUFS] = {};             // end of the step's core: its input buffer is free
   cudaEvent_t wev[2][3] = {};                     // start of the core, start and end of the append
   cudaStream_t drain_stream = nullptr;            // meetings of a window go out here beside the next step
   cudaEvent_t drained_ev = nullptr;
-  // the step captured as a CUDA graph, replayed by stc_step_window; it holds
-  // the pipeline's and the memtable's arguments by value, so anything that
-  // changes them (a flush, the slice count) invalidates it
-  // one graph per input buffer: a window with host input fills the other
-  // buffer (copy stream) while a step runs
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
-  bool graph_valid[2] = {false, false};
+  // the step's core captured as a CUDA graph, replayed by stc_step_window;
+  // it holds the pipeline's arguments by value, so anything that changes
+  // them (a flush, the slice count, a larger hit buffer) invalidates it; one
+  // graph per input buffer
+  cudaGraphExec_t graph[WIN_BUFS] = {};
+  bool graph_valid[WIN_BUFS] = {};
   uint32_t graph_kernels = 0;
-  double2 *xy_alt = nullptr;     // second input buffer of a window (allocated on first use)
+  double2 *xy_win[WIN_BUFS - 1] = {};  // a window's other input buffers (allocated on first use)
   cudaStream_t copy_stream = nullptr;
-  cudaEvent_t copy_ev[2] = {nullptr, nullptr};
+  cudaEvent_t copy_ev[WIN_BUFS] = {};
   std::vector<void *> allocs;
   stc_stats stats;
   uint32_t last_t = 0;
@@ -185,15 +189,15 @@ static void destroy_all(stc_ctx *c) {
   for (int i = 0; i < 2; i++) {
     if (c->st_slot[i]) cudaFreeHost(c->st_slot[i]);
     if (c->st_ev[i]) cudaEventDestroy(c->st_ev[i]);
-    if (c->core_ev[i]) cudaEventDestroy(c->core_ev[i]);
     for (cudaEvent_t ev : c->wev[i])
       if (ev) cudaEventDestroy(ev);
   }
   if (c->drained_ev) cudaEventDestroy(c->drained_ev);
   if (c->drain_stream) cudaStreamDestroy(c->drain_stream);
-  for (int i = 0; i < 2; i++) {
+  for (int i = 0; i < WIN_BUFS; i++) {
     if (c->graph[i]) cudaGraphExecDestroy(c->graph[i]);
     if (c->copy_ev[i]) cudaEventDestroy(c->copy_ev[i]);
+    if (c->core_ev[i]) cudaEventDestroy(c->core_ev[i]);
   }
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   for (int i = 0; i < 2; i++) {
@@ -306,13 +310,13 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
     e = cudaEventCreateWithFlags(&c->part_ev[i], cudaEventDisableTiming);
   for (int i = 0; i < PH_COUNT && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
   if (e == cudaSuccess) e = cudaMallocHost(&c->st_host, sizeof(DevState));
-  if (e == cudaSuccess) e = cudaMallocHost(&c->t_pinned, 2 * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMallocHost(&c->t_pinned, WIN_BUFS * sizeof(uint32_t));
   for (int i = 0; i < 2 && e == cudaSuccess; i++) {
     e = cudaMallocHost(&c->st_slot[i], sizeof(DevState));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->st_ev[i], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreate(&c->core_ev[i]);
     for (int j = 0; j < 3 && e == cudaSuccess; j++) e = cudaEventCreate(&c->wev[i][j]);
   }
+  for (int i = 0; i < WIN_BUFS && e == cudaSuccess; i++) e = cudaEventCreate(&c->core_ev[i]);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->drain_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->drained_ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = schema_prepare();
@@ -481,8 +485,16 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
   return STC_OK;
 }
 
+static void invalidate_graphs(stc_ctx *c) {
+  for (bool &v : c->graph_valid) v = false;
+}
+
+// Input buffer b of a window: the context's own copy target, then the
+// buffers allocated for windows.
+static double2 *window_buffer(stc_ctx *c, int b) { return b ? c->xy_win[b - 1] : c->xy_own; }
+
 static stc_status flush_now(stc_ctx *c, uint32_t t) {
-  c->graph_valid[0] = c->graph_valid[1] = false;  // the memtable's arguments change
+  invalidate_graphs(c);  // the memtable's arguments change
   cudaEventRecord(c->ev[PH_FLUSH0], c->stream);
   unsigned long long launches0 = tl_launches;
   std::string err;
@@ -563,7 +575,7 @@ static void issue_step(stc_ctx *c, bool events, bool append, const uint32_t *two
 }
 
 // Captures the step's core (without the memtable append) with positions in
-// input buffer b (xy_own, xy_alt) and its time in t_pinned[b] as a CUDA
+// window input buffer b and its time in t_pinned[b] as a CUDA
 // graph. Only this thread's work on the context's streams is captured: a
 // serving thread's queries on other streams go on meanwhile.
 static stc_status capture_step(stc_ctx *c, int b) {
@@ -572,7 +584,7 @@ static stc_status capture_step(stc_ctx *c, int b) {
     c->graph[b] = nullptr;
   }
   c->graph_valid[b] = false;
-  c->p.xy = b ? c->xy_alt : c->xy_own;
+  c->p.xy = window_buffer(c, b);
   const unsigned long long l0 = tl_launches;
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
@@ -647,7 +659,7 @@ static void grow_hits(stc_ctx *c, unsigned long long need) {
     }
   p.hits = (HitRec *)h;
   p.hit_cap = cap;
-  c->graph_valid[0] = c->graph_valid[1] = false;  // the graphs hold the buffer by value
+  invalidate_graphs(c);  // the graphs hold the buffer by value
 }
 
 static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copied) {
@@ -743,7 +755,9 @@ static cudaError_t emit_keep_tail(stc_ctx *c, unsigned long long from, unsigned 
 
 // A window of steps, pipelined one step deep: step i + 1 is queued on the
 // GPU before the host waits for step i's state, so the GPU does not idle
-// while the host reads a state, drains meetings or issues launches.
+// while the host reads a state, drains meetings or issues launches. The
+// positions of step i + 3 are copied in once step i has run (three input
+// buffers), two steps before they are needed.
 //
 // Device order per step i: core(i) (everything but the memtable append),
 // then [flush after step i - 1, when due], append(i), state copy(i). The
@@ -768,18 +782,18 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   cudaStream_t s = c->stream;
   const size_t step_bytes = (size_t)p.N * sizeof(double2);
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-  if (!c->xy_alt || !c->copy_stream) {
+  if (!c->xy_win[WIN_BUFS - 2] || !c->copy_stream) {
     cudaError_t e = cudaSuccess;
-    if (!c->xy_alt) {
-      e = cudaMalloc(&c->xy_alt, step_bytes);
-      if (e == cudaSuccess) c->allocs.push_back(c->xy_alt);
-    }
+    for (int b = 0; b < WIN_BUFS - 1 && e == cudaSuccess; b++)
+      if (!c->xy_win[b]) {
+        e = cudaMalloc(&c->xy_win[b], step_bytes);
+        if (e == cudaSuccess) c->allocs.push_back(c->xy_win[b]);
+      }
     if (e == cudaSuccess && !c->copy_stream) e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
-    for (int b = 0; b < 2 && e == cudaSuccess; b++)
+    for (int b = 0; b < WIN_BUFS && e == cudaSuccess; b++)
       if (!c->copy_ev[b]) e = cudaEventCreateWithFlags(&c->copy_ev[b], cudaEventDisableTiming);
     if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window buffers");
   }
-  double2 *const buf[2] = {c->xy_own, c->xy_alt};
   const bool graphs = c->cfg.window_graphs == 1 || (c->cfg.window_graphs == 0 && p.N <= (1u << 21));
   bool pinned_out = false;
   if (out && cap) {
@@ -789,20 +803,23 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   }
   unsigned long long launches[2] = {0, 0};
 
-  // Positions of step i into buffer i & 1 on the copy stream, once the core
-  // of step i - 2 (the buffer's last reader) has run.
+  // Positions of step i into buffer i % WIN_BUFS on the copy stream, once
+  // the core of step i - WIN_BUFS (the buffer's last reader) has run.
   auto fetch = [&](uint32_t i) -> cudaError_t {
-    const int b = i & 1;
-    cudaError_t e = i >= 2 ? cudaStreamWaitEvent(c->copy_stream, c->core_ev[b], 0) : cudaSuccess;
+    const int b = (int)(i % WIN_BUFS);
+    cudaError_t e = i >= (uint32_t)WIN_BUFS ? cudaStreamWaitEvent(c->copy_stream, c->core_ev[b], 0) : cudaSuccess;
     if (e == cudaSuccess)
-      e = copy_in_pieces(buf[b], (const uint8_t *)xy + (size_t)i * step_bytes, step_bytes, kind, c->copy_stream);
+      e = copy_in_pieces(window_buffer(c, b), (const uint8_t *)xy + (size_t)i * step_bytes, step_bytes, kind,
+                         c->copy_stream);
     return e == cudaSuccess ? cudaEventRecord(c->copy_ev[b], c->copy_stream) : e;
   };
+  // (per step: events and state copy by parity i & 1, input buffer, its
+  // copy event, time word and graph by i % WIN_BUFS)
   auto issue_core = [&](uint32_t i) -> stc_status {
-    const int b = i & 1;
-    c->t_pinned[b] = t0 + i;  // step i - 2, the word's last reader, has been waited for
+    const int par = i & 1, b = (int)(i % WIN_BUFS);
+    c->t_pinned[b] = t0 + i;  // step i - WIN_BUFS, the word's last reader, has been waited for
     const unsigned long long l0 = tl_launches;
-    cudaEventRecord(c->wev[b][0], s);
+    cudaEventRecord(c->wev[par][0], s);
     cudaError_t e = cudaStreamWaitEvent(s, c->copy_ev[b], 0);
     if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window copy-in");
     if (graphs) {
@@ -814,11 +831,11 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
       if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window");
       tl_launches += c->graph_kernels;
     } else {
-      p.xy = buf[b];
+      p.xy = window_buffer(c, b);
       issue_step(c, false, false, c->t_pinned + b);
     }
     cudaEventRecord(c->core_ev[b], s);
-    launches[b] = tl_launches - l0;
+    launches[par] = tl_launches - l0;
     return STC_OK;
   };
   auto issue_tail = [&](uint32_t i) -> stc_status {
@@ -846,7 +863,7 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
       return fail(c, status_of(c->st_host->error), m);
     }
     float core = 0, app = 0;
-    cudaEventElapsedTime(&core, c->wev[b][0], c->core_ev[b]);
+    cudaEventElapsedTime(&core, c->wev[b][0], c->core_ev[i % WIN_BUFS]);
     cudaEventElapsedTime(&app, c->wev[b][1], c->wev[b][2]);
     float phase[8] = {0, 0, 0, 0, 0, 0, 0, app};
     fill_stats(c, t0 + i, phase, core + app, (uint32_t)launches[b]);
@@ -865,8 +882,8 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   cudaError_t e = fetch(0);
   if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window copy-in");
   rs = issue_core(0);
-  if (rs == STC_OK && steps > 1) {
-    e = fetch(1);
+  for (uint32_t k = 1; rs == STC_OK && k < (uint32_t)WIN_BUFS && k < steps; k++) {
+    e = fetch(k);
     if (e != cudaSuccess) rs = cuda_fail(c, e, "stc_step_window copy-in");
   }
   if (rs == STC_OK) rs = issue_tail(0);
@@ -878,8 +895,8 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
     const bool ahead = i + 1 < steps && !hold;
     if (ahead) {
       rs = issue_core(i + 1);
-      if (rs == STC_OK && i + 2 < steps) {
-        e = fetch(i + 2);
+      if (rs == STC_OK && i + WIN_BUFS < steps) {
+        e = fetch(i + WIN_BUFS);
         if (e != cudaSuccess) rs = cuda_fail(c, e, "stc_step_window copy-in");
       }
     }
@@ -939,8 +956,8 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
         grow_hits(c, most_hits);
         hold = false;
         rs = issue_core(i + 1);
-        if (rs == STC_OK && i + 2 < steps) {
-          e = fetch(i + 2);
+        if (rs == STC_OK && i + WIN_BUFS < steps) {
+          e = fetch(i + WIN_BUFS);
           if (e != cudaSuccess) rs = cuda_fail(c, e, "stc_step_window copy-in");
         }
         if (rs != STC_OK) {
@@ -1237,7 +1254,7 @@ extern "C" stc_status stc_set_step_slices(stc_ctx *c, uint32_t slices) {
   if (!c) return STC_ERR_INVALID_ARG;
   c->cfg.step_slices = slices;
   c->p.slices = std::min<uint32_t>(std::max<uint32_t>(slices, 1u), 64u);
-  c->graph_valid[0] = c->graph_valid[1] = false;
+  invalidate_graphs(c);
   return STC_OK;
 }
 
@@ -1267,7 +1284,7 @@ extern "C" stc_status stc_load_ctb(stc_ctx *c, uint32_t index, const char *dir, 
   if (!c->lsm_on) return fail(c, STC_ERR_INVALID_ARG, "stc_load_ctb: the memtable is off (kv_restriction 0)");
   if (c->failed) return STC_ERR_STATE;
   cudaSetDevice(c->device);
-  c->graph_valid[0] = c->graph_valid[1] = false;
+  invalidate_graphs(c);
   std::string err;
   stc_status st = lsm_load_block(c->lsm, c->lsmh, index, dir, prefix, c->stream, err);
   if (st != STC_OK) c->err = "stc_load_ctb: " + err;
