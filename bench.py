@@ -291,15 +291,18 @@ def run_gpu(args, w, rank, local):
     barrier(args)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    for c0 in range(0, K, win):
-        n = min(win, K - c0)
-        m = pipe.step_window(hnp.arr[c0:c0 + n], W + K + c0, out=mnp)
-        d2h += m.nbytes + 128 * n
-        e2e_stats.append(pipe.stats())
-    torch.cuda.synchronize()
+    with ClockSampler(local) as e2e_clk:
+        for c0 in range(0, K, win):
+            n = min(win, K - c0)
+            m = pipe.step_window(hnp.arr[c0:c0 + n], W + K + c0, out=mnp)
+            d2h += m.nbytes + 128 * n
+            e2e_stats.append(pipe.stats())
+        torch.cuda.synchronize()
     wall_e2e = time.perf_counter() - t1
     e2e_busy = {"window_device_ms": [round(float(s.window_device_ms), 3) for s in e2e_stats],
+                "window_input_wait_ms": [round(float(s.window_input_wait_ms), 3) for s in e2e_stats],
                 "window_wall_ms": [round(float(s.window_wall_ms), 3) for s in e2e_stats],
+                "clocks": e2e_clk.summary(),
                 "gpu_busy_frac": float(sum(s.window_device_ms for s in e2e_stats) /
                                        max(sum(s.window_wall_ms for s in e2e_stats), 1e-9)),
                 "host_load_avg": list(os.getloadavg()), "host_cpus": os.cpu_count()}
@@ -456,6 +459,7 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None, dev_steps=
     gc.disable()  # no collector pause holds the interpreter lock while serving
     th.start()
     step_ms = []
+    win_ms = []  # (device ms, input wait ms, steps) of each ingest window
     w0 = time.perf_counter()
     # ingest as pipelined windows (stc_step_window, host input, meetings
     # drained into the page-locked buffer), as the end-to-end run does
@@ -466,7 +470,9 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None, dev_steps=
             pipe.step_window((dev_steps[k].data_ptr(), n), w0t, out=mout)
         else:
             pipe.step_window(hnp.arr[w0t - hnp.first:w0t - hnp.first + n], w0t, out=mout)
-        step_ms.append(pipe.stats().step_ms)
+        ws = pipe.stats()
+        step_ms.append(ws.step_ms)
+        win_ms.append((ws.window_device_ms, ws.window_input_wait_ms, n))
         cur_t[0] = w0t + n - 1
     wall = time.perf_counter() - w0
     done.set()
@@ -531,7 +537,9 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None, dev_steps=
                    "queries returning match counts (50 m-5 km, window 10-3600 steps)",
             "blocks": 1, "step_slices": args.serve_slices, "ingest_window_steps": SERVE_WINDOW,
             "ingest_pos_updates_per_s": N * steps / wall,
-            "ingest_device_ms_per_step": float(np.mean(step_ms))}
+            "ingest_device_ms_per_step": float(np.mean(step_ms)),
+            "ingest_window_device_ms_per_step": sum(d for d, _, _ in win_ms) / max(sum(n for _, _, n in win_ms), 1),
+            "ingest_input_wait_ms_per_step": sum(w for _, w, _ in win_ms) / max(sum(n for _, _, n in win_ms), 1)}
 
 
 def barrier(args):

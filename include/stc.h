@@ -150,9 +150,12 @@ typedef struct stc_stats {
   float flush_ms;                /* device time of the last flush */
   /* The last stc_step_window call: the device time of its steps (core and
    * memtable append, flushes excluded) and the call's wall time on the host;
-   * their ratio is how busy the window kept the GPU. */
+   * their ratio is how busy the window kept the GPU. window_input_wait_ms is
+   * the part of the device time its steps spent waiting for their positions'
+   * copy (a slow host link shows here). */
   float window_device_ms;
   float window_wall_ms;
+  float window_input_wait_ms;
 } stc_stats;
 
 /* Fills *cfg with the reference defaults for n objects (util/config.h:29-41,

@@ -64,12 +64,15 @@ struct NodeMeta {
 };
 
 // One pair within reach found by the refinement, waiting to be applied to
-// the meeting table: the pair (a < b; a = STC_NONE marks an unused record)
-// and its priority. The key is cantor(a, b) and the MBR contribution the two
-// objects' float positions of the step (fxy), both rebuilt when applied.
-struct __align__(16) HitRec {
+// the meeting table: the pair (a < b; a = STC_NONE marks an unused record),
+// its priority and its MBR contribution, the box of the two objects' float
+// positions of the step (fxy; lo = fminf(a's, b's), hi = fmaxf(a's, b's)).
+// The key cantor(a, b) is rebuilt when applied. Carrying the box saves the
+// table update two dependent random reads of fxy per extended meeting.
+struct __align__(32) HitRec {
   uint32_t a, b;
   unsigned long long order;  // bit 63: the pair may occur twice this step
+  float lo_x, lo_y, hi_x, hi_y;
 };
 
 struct __align__(16) U128 {

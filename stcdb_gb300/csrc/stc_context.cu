@@ -78,7 +78,8 @@ struct stc_ctx {
   DevState *st_slot[2] = {nullptr, nullptr};
   cudaEvent_t st_ev[2] = {nullptr, nullptr};      // the state copy of the step of that parity has landed
   cudaEvent_t core_ev[WIN_BUFS] = {};             // end of the step's core: its input buffer is free
-  cudaEvent_t wev[2][3] = {};                     // start of the core, start and end of the append
+  cudaEvent_t wev[2][4] = {};                     // start of the core, start and end of the append,
+                                                  // core's start once its positions are in
   cudaStream_t drain_stream = nullptr;            // meetings of a window go out here beside the next step
   cudaEvent_t drained_ev = nullptr;
   // the step's core captured as a CUDA graph, replayed by stc_step_window;
@@ -314,7 +315,7 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
   for (int i = 0; i < 2 && e == cudaSuccess; i++) {
     e = cudaMallocHost(&c->st_slot[i], sizeof(DevState));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->st_ev[i], cudaEventDisableTiming);
-    for (int j = 0; j < 3 && e == cudaSuccess; j++) e = cudaEventCreate(&c->wev[i][j]);
+    for (int j = 0; j < 4 && e == cudaSuccess; j++) e = cudaEventCreate(&c->wev[i][j]);
   }
   for (int i = 0; i < WIN_BUFS && e == cudaSuccess; i++) e = cudaEventCreate(&c->core_ev[i]);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->drain_stream, cudaStreamNonBlocking);
@@ -388,6 +389,7 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
             dalloc(c, &p.hit_bounds, STC_MAX_PARTS + 1) &&
             dalloc(c, &p.sort_hist2, radix_hist_words(nu)) && dalloc(c, &p.scan_tmp2, scan_words) &&
             dalloc(c, &p.grid_start, (size_t)p.G + 1) && dalloc(c, &p.pts, n) && dalloc(c, &p.fxy, n) &&
+            dalloc(c, &p.gfxy, n) && dalloc(c, &p.sfxy, n) &&
             dalloc(c, &p.spts, n) && dalloc(c, &p.sorig, n) && dalloc(c, &p.scand, n) &&
             dalloc(c, &p.lstrip, p.G) && dalloc(c, &p.cchunks, p.G) &&
             dalloc(c, &p.bcount, (size_t)n + 1) && dalloc(c, &p.boff, (size_t)n + 1) &&
@@ -802,6 +804,7 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
     cudaGetLastError();  // pageable memory is not an error
   }
   unsigned long long launches[2] = {0, 0};
+  double wait_ms = 0;  // device time of the window's steps spent waiting for their positions
 
   // Positions of step i into buffer i % WIN_BUFS on the copy stream, once
   // the core of step i - WIN_BUFS (the buffer's last reader) has run.
@@ -822,6 +825,7 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
     cudaEventRecord(c->wev[par][0], s);
     cudaError_t e = cudaStreamWaitEvent(s, c->copy_ev[b], 0);
     if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window copy-in");
+    cudaEventRecord(c->wev[par][3], s);
     if (graphs) {
       if (!c->graph_valid[b]) {
         stc_status gs = capture_step(c, b);
@@ -862,9 +866,11 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
                c->st_host->error, c->st_host->error_info);
       return fail(c, status_of(c->st_host->error), m);
     }
-    float core = 0, app = 0;
+    float core = 0, app = 0, wait = 0;
     cudaEventElapsedTime(&core, c->wev[b][0], c->core_ev[i % WIN_BUFS]);
     cudaEventElapsedTime(&app, c->wev[b][1], c->wev[b][2]);
+    cudaEventElapsedTime(&wait, c->wev[b][0], c->wev[b][3]);
+    wait_ms += wait;
     float phase[8] = {0, 0, 0, 0, 0, 0, 0, app};
     fill_stats(c, t0 + i, phase, core + app, (uint32_t)launches[b]);
     return STC_OK;
@@ -986,6 +992,7 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   cudaStreamSynchronize(s);
   grow_hits(c, most_hits);
   c->stats.window_device_ms = (float)busy_ms;
+  c->stats.window_input_wait_ms = (float)wait_ms;
   c->stats.window_wall_ms =
       (float)std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
   return STC_OK;

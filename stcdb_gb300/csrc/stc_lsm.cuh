@@ -140,13 +140,15 @@ struct QueryLane {
   size_t items_cap = 0;
   uint32_t *d_iscan = nullptr;     // scan scratch
   size_t iscan_cap = 0;
-  // pinned host staging of a batch's copies (pageable copies would wait on
-  // the driver's staging path, which a stepping thread's copies hold)
-  QBlock *h_qb = nullptr;          // [retain]
-  stc_query *h_q = nullptr;
+  // Mapped pinned host buffers of a batch's inputs and results. Kernels on
+  // the lane's stream read and write them over the host link directly, so a
+  // batch never queues on a copy engine behind a step's position copy (tens
+  // to hundreds of MB) or a drain. m_* are their device-side addresses.
+  QBlock *h_qb = nullptr, *m_qb = nullptr;                // [retain]
+  stc_query *h_q = nullptr, *m_q = nullptr;
   size_t hq_cap = 0;
-  unsigned long long *h_counts = nullptr;  // [hq_cap + 1]: per-query counts, then the match total
-  QueryRec *h_recs = nullptr;
+  unsigned long long *h_counts = nullptr, *m_counts = nullptr;  // [hq_cap + 1]: per-query counts, then the total
+  QueryRec *h_recs = nullptr, *m_recs = nullptr;
   size_t hrecs_cap = 0;
 };
 

@@ -70,6 +70,7 @@ __global__ void k_gather(PipeDev p) {
   float ly = __double2float_rn(RN_SUB(q.y, o->lo_y));
   float2 f = make_float2(__double2float_rn(q.x), __double2float_rn(q.y));
   p.pts[i] = make_float4(lx, ly, metres_per_deg_lon_f(q.y), __uint_as_float(pid));
+  p.gfxy[i] = f;
   p.fxy[pid] = f;
 }
 
@@ -164,6 +165,7 @@ __global__ void __launch_bounds__(256) k_strip_order(PipeDev p) {
       const uint32_t u = tmp[base + i], sidx = u >> 16;
       const uint32_t k = hist[sidx] + (u & 0xFFFFu);
       p.spts[base + k] = p.pts[base + i];
+      p.sfxy[base + k] = p.gfxy[base + i];
       p.sorig[base + k] = i | sidx << 16;
     }
     __syncwarp();
@@ -175,6 +177,7 @@ __global__ void __launch_bounds__(256) k_strip_order(PipeDev p) {
       if (L <= 32) {
         // one member per lane (most strips)
         const float4 v = lane < L ? p.spts[base + st + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float2 f = lane < L ? p.sfxy[base + st + lane] : make_float2(0.f, 0.f);
         const uint32_t og = lane < L ? p.sorig[base + st + lane] : 0u;
         uint32_t rk = 0;
         for (uint32_t b = 0; b < L; b++) {
@@ -184,6 +187,7 @@ __global__ void __launch_bounds__(256) k_strip_order(PipeDev p) {
         __syncwarp();
         if (lane < L) {
           p.spts[base + st + rk] = v;
+          p.sfxy[base + st + rk] = f;
           p.sorig[base + st + rk] = og | STRIP_XSORTED;
         }
         __syncwarp();
@@ -191,11 +195,13 @@ __global__ void __launch_bounds__(256) k_strip_order(PipeDev p) {
       }
       const uint32_t slots = (L + 31) / 32;
       float4 v[4];
+      float2 f[4];
       uint32_t og[4], rk[4] = {0, 0, 0, 0};
 #pragma unroll
       for (int m = 0; m < 4; m++) {
         const uint32_t e = lane + 32u * m;
         v[m] = e < L ? p.spts[base + st + e] : make_float4(0.f, 0.f, 0.f, 0.f);
+        f[m] = e < L ? p.sfxy[base + st + e] : make_float2(0.f, 0.f);
         og[m] = e < L ? p.sorig[base + st + e] : 0u;
       }
 #pragma unroll
@@ -218,6 +224,7 @@ __global__ void __launch_bounds__(256) k_strip_order(PipeDev p) {
         const uint32_t e = lane + 32u * m;
         if (e < L) {
           p.spts[base + st + rk[m]] = v[m];
+          p.sfxy[base + st + rk[m]] = f[m];
           p.sorig[base + st + rk[m]] = og[m] | STRIP_XSORTED;
         }
       }

@@ -40,6 +40,8 @@ struct PipeDev {
   uint32_t *grid_count, *grid_start;   // G, G+1
   float4 *pts;                          // N sorted: lx, ly, metres/deg lon, pid bits
   float2 *fxy;                          // N by pid: float lon, lat (MBR of new meetings)
+  float2 *gfxy;                         // N in leaf order (pid order within a leaf): fxy of each member
+  float2 *sfxy;                         // N in strip order (as spts): fxy of each member
   // each leaf's kept members again, ordered by horizontal strip (strips at
   // least reach tall) and, within a small strip, by longitude: spts as pts;
   // sorig = member index in pid order | strip << 16 | STRIP_XSORTED;

@@ -727,16 +727,57 @@ __global__ void __launch_bounds__(QBOX_THREADS) k_box_rows(const QBlock *qb, uin
   }
 }
 
-// Pinned host buffer of at least `need` elements (contents not kept).
+// Mapped pinned host buffer of at least `need` elements (contents not kept):
+// *p is its host address, *m the address kernels use.
 template <typename T>
-cudaError_t grow_pinned(T **p, size_t *cap, size_t need) {
+cudaError_t grow_mapped(T **p, T **m, size_t *cap, size_t need) {
   if (*cap >= need) return cudaSuccess;
   size_t n = std::max<size_t>(need, 2 * *cap);
   if (*p) cudaFreeHost(*p);
-  *p = nullptr;
-  cudaError_t e = cudaMallocHost((void **)p, n * sizeof(T));
+  *p = *m = nullptr;
+  cudaError_t e = cudaHostAlloc((void **)p, n * sizeof(T), cudaHostAllocMapped | cudaHostAllocPortable);
+  if (e == cudaSuccess) e = cudaHostGetDevicePointer((void **)m, *p, 0);
+  if (e != cudaSuccess && *p) {
+    cudaFreeHost(*p);
+    *p = *m = nullptr;
+  }
   *cap = e == cudaSuccess ? n : 0;
   return e;
+}
+
+// Copies `words` 8-byte words between device memory and mapped host memory
+// with ordinary loads and stores, which cross the host link without a copy
+// engine.
+__global__ void k_link_copy(unsigned long long *__restrict__ dst, const unsigned long long *__restrict__ src,
+                            size_t words) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+// A batch's per-query match counts, then its total, into mapped host memory.
+__global__ void k_counts_out(unsigned long long *__restrict__ dst, const unsigned long long *__restrict__ qcounts,
+                             size_t nq, const unsigned long long *__restrict__ total) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i <= nq; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = i < nq ? qcounts[i] : *total;
+}
+
+constexpr unsigned LINK_THREADS = 256;
+
+unsigned link_blocks(size_t words) {
+  return (unsigned)std::min<size_t>(std::max<size_t>((words + LINK_THREADS - 1) / LINK_THREADS, 1),
+                                    (size_t)num_sms() * 4);
+}
+
+// Stream-ordered copy of `bytes` (a multiple of 8) between device memory and
+// mapped host memory.
+template <typename T>
+cudaError_t link_copy(T *dst, const T *src, size_t bytes, cudaStream_t s) {
+  static_assert(sizeof(T) % 8 == 0, "link copies move 8-byte words");
+  const size_t words = bytes / 8;
+  if (words == 0) return cudaSuccess;
+  k_link_copy<<<link_blocks(words), LINK_THREADS, 0, s>>>((unsigned long long *)dst,
+                                                          (const unsigned long long *)src, words);
+  return cudaGetLastError();
 }
 
 template <typename T>
@@ -934,10 +975,10 @@ void lsm_release(LsmHost &H) {
     Q.d_out = nullptr;
     Q.d_count = Q.d_qcounts = nullptr;
     Q.d_items = Q.d_iscan = nullptr;
-    Q.h_qb = nullptr;
-    Q.h_q = nullptr;
-    Q.h_counts = nullptr;
-    Q.h_recs = nullptr;
+    Q.h_qb = Q.m_qb = nullptr;
+    Q.h_q = Q.m_q = nullptr;
+    Q.h_counts = Q.m_counts = nullptr;
+    Q.h_recs = Q.m_recs = nullptr;
     Q.stream = nullptr;
     Q.q_cap = Q.out_cap = Q.qc_cap = Q.items_cap = Q.iscan_cap = Q.hq_cap = Q.hrecs_cap = 0;
   }
@@ -951,12 +992,13 @@ static cudaError_t query_buffers(const LsmHost &H, QueryLane &Q, size_t nq, uint
   cudaError_t e = cudaSuccess;
   const size_t nb = std::max<uint32_t>(H.retain, 1);
   if (!Q.d_qb) e = cudaMalloc(&Q.d_qb, nb * sizeof(QBlock));
-  if (e == cudaSuccess && !Q.h_qb) e = cudaMallocHost((void **)&Q.h_qb, nb * sizeof(QBlock));
+  size_t cap_qb = Q.h_qb ? nb : 0;
+  if (e == cudaSuccess) e = grow_mapped(&Q.h_qb, &Q.m_qb, &cap_qb, nb);
   if (e == cudaSuccess && !Q.d_count) e = cudaMalloc(&Q.d_count, sizeof(unsigned long long));
   if (e == cudaSuccess && Q.hq_cap < nq) {
     size_t cap_q = Q.hq_cap;
-    e = grow_pinned(&Q.h_q, &Q.hq_cap, nq);
-    if (e == cudaSuccess) e = grow_pinned(&Q.h_counts, &cap_q, Q.hq_cap + 1);
+    e = grow_mapped(&Q.h_q, &Q.m_q, &Q.hq_cap, nq);
+    if (e == cudaSuccess) e = grow_mapped(&Q.h_counts, &Q.m_counts, &cap_q, Q.hq_cap + 1);
   }
   if (e == cudaSuccess) e = grow(&Q.d_q, &Q.q_cap, nq);
   if (e == cudaSuccess) e = grow(&Q.d_qcounts, &Q.qc_cap, nq);
@@ -965,7 +1007,7 @@ static cudaError_t query_buffers(const LsmHost &H, QueryLane &Q, size_t nq, uint
   const size_t npairs = nq * nb * ((size_t)F + 1) + 1;
   if (e == cudaSuccess) e = grow(&Q.d_items, &Q.items_cap, npairs);
   if (e == cudaSuccess) e = grow(&Q.d_iscan, &Q.iscan_cap, scan_tmp_words(npairs));
-  if (e == cudaSuccess) e = grow_pinned(&Q.h_recs, &Q.hrecs_cap, 1 << 16);
+  if (e == cudaSuccess) e = grow_mapped(&Q.h_recs, &Q.m_recs, &Q.hrecs_cap, 1 << 16);
   return e;
 }
 
@@ -981,7 +1023,8 @@ stc_status lsm_query_reserve(LsmHost &H, size_t nq, uint32_t F, int priority, st
   // load the query kernels now: with lazy module loading their first launch
   // would load them then, which waits for a step in flight
   cudaFuncAttributes fa;
-  for (const void *k : {(const void *)k_query_object, (const void *)k_box_plan, (const void *)k_box_rows})
+  for (const void *k : {(const void *)k_query_object, (const void *)k_box_plan, (const void *)k_box_rows,
+                        (const void *)k_link_copy, (const void *)k_counts_out})
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k);
   if (e != cudaSuccess) {
     err = std::string("query buffers: ") + cudaGetErrorString(e);
@@ -1050,8 +1093,8 @@ stc_status lsm_query(LsmHost &H, int lane, const stc_query *qs, size_t nq, stc_c
   for (size_t i = 0; i < nq; i++) ((qs[i].kind & 0xFFu) == STC_QUERY_BOX ? has_box : has_obj) = true;
   memcpy(Q.h_q, qs, nq * sizeof(stc_query));
   if (gpu_ms) cudaEventRecord(Q.ev0, s);
-  e = cudaMemcpyAsync(Q.d_qb, qb, nb * sizeof(QBlock), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(Q.d_q, Q.h_q, nq * sizeof(stc_query), cudaMemcpyHostToDevice, s);
+  e = link_copy(Q.d_qb, Q.m_qb, nb * sizeof(QBlock), s);
+  if (e == cudaSuccess) e = link_copy(Q.d_q, Q.m_q, nq * sizeof(stc_query), s);
   unsigned long long total = 0;
   bool over = false;  // more matches than device_limit: counted only
   for (int attempt = 0; attempt < 2 && e == cudaSuccess; attempt++) {
@@ -1070,9 +1113,10 @@ stc_status lsm_query(LsmHost &H, int lane, const stc_query *qs, size_t nq, stc_c
                                                                 Q.d_out, Q.out_cap, Q.d_count, Q.d_qcounts);
     }
     e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(Q.h_counts + nq, Q.d_count, sizeof(total), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess && (counts || device_limit))
-      e = cudaMemcpyAsync(Q.h_counts, Q.d_qcounts, nq * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) {
+      k_counts_out<<<link_blocks(nq + 1), LINK_THREADS, 0, s>>>(Q.m_counts, Q.d_qcounts, nq, Q.d_count);
+      e = cudaGetLastError();
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     total = Q.h_counts[nq];
     if (e == cudaSuccess && counts) memcpy(counts, Q.h_counts, nq * sizeof(unsigned long long));
@@ -1099,8 +1143,8 @@ stc_status lsm_query(LsmHost &H, int lane, const stc_query *qs, size_t nq, stc_c
     return STC_OK;
   }
   if (total) {
-    e = grow_pinned(&Q.h_recs, &Q.hrecs_cap, (size_t)total);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(Q.h_recs, Q.d_out, total * sizeof(QueryRec), cudaMemcpyDeviceToHost, s);
+    e = grow_mapped(&Q.h_recs, &Q.m_recs, &Q.hrecs_cap, (size_t)total);
+    if (e == cudaSuccess) e = link_copy(Q.m_recs, Q.d_out, total * sizeof(QueryRec), s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
       err = std::string("query read-back: ") + cudaGetErrorString(e);

@@ -105,14 +105,13 @@ __device__ void process_hit_at(const PipeDev &p, const HitRec &h, unsigned long 
     Slot *s = &p.slots[slot];
     if (kv.lo == key) {  // tracing/refinement.cpp:40-42 (+ MBR, cuda/geometry.cu:474-478)
       s->end = t;
-      // both objects' float positions this step; the MBR only grows during a
-      // step, so a stale read can only cause an extra atomic
-      const float2 fa = p.fxy[h.a], fb = p.fxy[h.b];
-      const float lx = fminf(fa.x, fb.x), ly = fminf(fa.y, fb.y), hx = fmaxf(fa.x, fb.x), hy = fmaxf(fa.y, fb.y);
-      if (lx < mbr.x) atomic_min_f(&s->lo_x, lx);
-      if (ly < mbr.y) atomic_min_f(&s->lo_y, ly);
-      if (hx > mbr.z) atomic_max_f(&s->hi_x, hx);
-      if (hy > mbr.w) atomic_max_f(&s->hi_y, hy);
+      // the box of both objects' float positions this step comes with the
+      // record; the MBR only grows during a step, so a stale read of it can
+      // only cause an extra atomic
+      if (h.lo_x < mbr.x) atomic_min_f(&s->lo_x, h.lo_x);
+      if (h.lo_y < mbr.y) atomic_min_f(&s->lo_y, h.lo_y);
+      if (h.hi_x > mbr.z) atomic_max_f(&s->hi_x, h.hi_x);
+      if (h.hi_y > mbr.w) atomic_max_f(&s->hi_y, h.hi_y);
       return;
     }
     if (kv.lo == STC_EMPTY_KEY || (kv.lo & STC_CLAIM_BIT)) {  // empty before this step: a new key
@@ -171,11 +170,16 @@ __device__ __forceinline__ void flush_queue(const PipeDev &p, HitRec *q, uint32_
 
 __device__ __forceinline__ HitRec load_hit(const HitRec *r) {
   // streamed once: evict-first loads keep L2 for the table and positions
-  ulonglong2 v = __ldcs((const ulonglong2 *)r);
+  const ulonglong2 v = __ldcs((const ulonglong2 *)r);
+  const float4 m = __ldcs((const float4 *)&r->lo_x);
   HitRec h;
   h.a = (uint32_t)v.x;
   h.b = (uint32_t)(v.x >> 32);
   h.order = v.y;
+  h.lo_x = m.x;
+  h.lo_y = m.y;
+  h.hi_x = m.z;
+  h.hi_y = m.w;
   return h;
 }
 
@@ -261,6 +265,7 @@ __device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblo
   const uint32_t base = p.grid_start[g];
   const Node *o = &p.sd.nodes[p.sd.gid_node[g]];
   float4 rp = make_float4(0.f, 0.f, 0.f, 0.f);
+  float2 fr = make_float2(0.f, 0.f);  // the row object's float position (fxy)
   uint32_t pid1 = 0, orig1 = 0, row_leaf = 0;
   uint32_t sa[3] = {0, 0, 0}, sl[3] = {0, 0, 0};  // candidate segments: start, length
   unsigned long long rank = 0;
@@ -270,6 +275,7 @@ __device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblo
     vr = i < n;
     if (vr) {
       rp = __ldg(&p.spts[base + i]);
+      fr = __ldg(&p.sfxy[base + i]);
       pid1 = __float_as_uint(rp.w);
       orig1 = __ldg(&p.sorig[base + i]) & 0xFFFFu;
       const uint2 c = __ldg(&p.scand[base + i]);
@@ -288,6 +294,7 @@ __device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblo
       pid1 = p.bu_pid[pos];
       rank = (unsigned long long)p.N + pos;  // border units follow the N own units
       const double2 qq = p.xy[pid1];
+      fr = make_float2(__double2float_rn(qq.x), __double2float_rn(qq.y));
       rp = make_float4(__double2float_rn(RN_SUB(qq.x, o->lo_x)), __double2float_rn(RN_SUB(qq.y, o->lo_y)),
                        metres_per_deg_lon_f(qq.y), 0.f);
       // A pair of a border row (pid1 outside leaf g) and a member occurs
@@ -382,9 +389,15 @@ __device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblo
           const uint32_t j = a + k0 + kk;
           const uint32_t cpid = __float_as_uint(__ldg(&p.spts[base + j]).w);
           const uint32_t corig = __ldg(&p.sorig[base + j]) & 0xFFFFu;
+          const float2 fc = __ldg(&p.sfxy[base + j]);
+          const float2 fa = pid1 < cpid ? fr : fc, fb = pid1 < cpid ? fc : fr;
           HitRec h;
           h.a = pid1 < cpid ? pid1 : cpid;
           h.b = pid1 < cpid ? cpid : pid1;
+          h.lo_x = fminf(fa.x, fb.x);
+          h.lo_y = fminf(fa.y, fb.y);
+          h.hi_x = fmaxf(fa.x, fb.x);
+          h.hi_y = fmaxf(fa.y, fb.y);
           if (own) {
             // the pair is found by the lower pid's own unit (rank = its pid)
             // at the higher pid's place in the pid-ordered member list
