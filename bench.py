@@ -88,10 +88,10 @@ WORKLOADS = {
     # sigma 150 m, reach 20 m, minimum meeting 3 steps) at the largest object
     # count whose live pairs fit a table in HBM: its Zipf-weighted first
     # hotspot alone holds ~17% of the hot objects, so live pairs grow as N^2
-    # (about 3e8 at 1M objects)
+    # (about 3e8 at 1M objects); its blocks carry 512 x 512 map bitmaps
     "stress-1M": dict(objects=1_000_000, hot=200, hot_frac=0.9, sigma_m=150.0, reach=20.0, min_meet=3,
                       grid_capacity=200, amplify=32.0, buckets=1 << 30, kv_restriction=1 << 27,
-                      emit_per_object=128),
+                      emit_per_object=128, bitmap_edge=512),
     "uniform-3M": dict(objects=3_000_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
                        buckets=1 << 26, kv_restriction=1 << 25),
     "uniform-100k": dict(objects=100_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
@@ -121,7 +121,8 @@ def make_cfg(w, device=0, step_slices=0):
                      grid_capacity=w["grid_capacity"], grid_amplify=w["amplify"], num_meeting_buckets=b,
                      device=device, kv_restriction=w["kv_restriction"], step_slices=step_slices,
                      emit_capacity=w.get("emit_per_object", 0) * w["objects"],
-                     refine_blocks_per_sm=w.get("refine_bps", 0), hits_blocks_per_sm=w.get("hits_bps", 0))
+                     refine_blocks_per_sm=w.get("refine_bps", 0), hits_blocks_per_sm=w.get("hits_bps", 0),
+                     bitmap_edge=w.get("bitmap_edge", 0))
 
 
 class ClockSampler:
@@ -888,7 +889,8 @@ def main():
                     "launch_shape": {"refine_blocks_per_sm": w.get("refine_bps", 8),
                                      "hits_blocks_per_sm": w.get("hits_bps", 16)},
                     "meeting_buckets": make_cfg(w).resolved().num_meeting_buckets,
-                    "memtable": f"on, flush past {w['kv_restriction']} directed keys, 100 CTFs",
+                    "memtable": f"on, flush past {w['kv_restriction']} directed keys, 100 CTFs, "
+                                f"{w.get('bitmap_edge', 256)}x{w.get('bitmap_edge', 256)} map bitmaps",
                     "l2": "inputs and table larger than L2; no flush", "parallelism": f"replicas x{ws}"}
 
     if args.impl == "reference":

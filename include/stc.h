@@ -109,6 +109,10 @@ typedef struct stc_config {
                                     0 = when num_objects <= 2^21 (where per-kernel launch costs
                                     show; a replayed graph ran a 10M-object step 10% slower than
                                     direct launches), 1 = always, 2 = never */
+  uint32_t bitmap_edge;          /* edge of a block's map bitmap, the oversize buffer's spatial
+                                    bitmap over the map box (DEFAULT_bitmap_edge, util/util.h:47,
+                                    a compile-time 256 in the reference): bitmap_edge^2 bits;
+                                    0 = 256; a multiple of 32 from 32 to 1024 */
 } stc_config;
 
 /* Replay quadtree splits/merges on one device thread only (tests compare it
@@ -277,12 +281,18 @@ typedef struct stc_ctb_info {
   uint32_t oversize_oid_count;   /* the reference's counter: oversize objects plus meetings
                                     longer than max_meet_time */
   uint32_t o_start_time_min, o_start_time_max, o_end_time_min, o_end_time_max;  /* oversize buffer */
+  uint32_t bitmap_edge;          /* edge of its map bitmap (stc_config.bitmap_edge) */
+  uint32_t pad;
 } stc_ctb_info;
 
-/* Bytes of one bitmap slot: 256 x 256 bits (workbench bit_count,
- * tracing/filter.cpp:72-73). CTF i's bitmap is slot i; its first
- * bitmap_bytes bytes are used. */
+/* Bytes of one CTF bitmap slot: 256 x 256 bits, room for the largest CTF
+ * grid (x_grid, y_grid <= 255, tracing/step_merge.cpp:175-181). CTF i's
+ * bitmap is slot i; its first bitmap_bytes bytes are used. */
 #define STC_BITMAP_BYTES 8192u
+/* Bytes of a block's map bitmap (the oversize buffer's, cells of the map box
+ * on an edge x edge grid, bit i + j * edge; tracing/step_merge.cpp:52-59):
+ * 8192 at the default edge of 256. */
+#define STC_MAP_BITMAP_BYTES(edge) ((size_t)(edge) * (size_t)(edge) / 8u)
 
 /* Flushes the memtable now if it holds any key (*flushed = 1) -- the
  * reference flushes only past kv_restriction; this also ends a run. */
@@ -297,7 +307,7 @@ stc_status stc_get_ctb(stc_ctx *ctx, stc_ctb_info *info);
  * little-endian); sids[num_objects] (0 no key, 1 oversize, 2.. CTF + 2);
  * oversize_keys[2 * oversize_kv_count] (128-bit keys pid:26 | target:26 |
  * duration:32 | end:32 as (low, high) 64-bit halves, util.h:47-52);
- * oversize_boxes[4 * oversize_kv_count]; oversize_bitmap[STC_BITMAP_BYTES]. */
+ * oversize_boxes[4 * oversize_kv_count]; oversize_bitmap[STC_MAP_BITMAP_BYTES(bitmap_edge)]. */
 stc_status stc_read_ctb(stc_ctx *ctx, stc_ctf *ctfs, uint8_t *bitmaps, uint8_t *keys, uint16_t *sids,
                         uint64_t *oversize_keys, float *oversize_boxes, uint8_t *oversize_bitmap);
 

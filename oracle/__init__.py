@@ -95,6 +95,8 @@ def _lib():
     lib.lsm_serialize_mbr.restype = ctypes.c_uint64
     lib.lsm_pack_key.argtypes = [ctypes.c_uint64] * 5 + [ctypes.c_void_p, ctypes.c_void_p]
     lib.lsm_o_bitmap.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.lsm_o_bitmap_edge.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]
+    lib.lsm_set_bitmap_edge.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
     lib.lsm_decode_key.argtypes = [ctypes.c_void_p] * 8
     lib.lsm_query_object_block.argtypes = [ctypes.c_void_p] * 6 + [ctypes.c_uint32] * 3 + [
         ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t]
@@ -181,7 +183,7 @@ class LsmOracle:
     meetings with append(); flush(t) builds a block readable with read()."""
 
     def __init__(self, num_objects: int, max_meet_time: int, ctf_count: int, area_restriction: float,
-                 first_end_time_min: int, mbr, capacity: int):
+                 first_end_time_min: int, mbr, capacity: int, bitmap_edge: int = 0):
         self._lib = lib()
         self._n = num_objects
         self._map = np.ascontiguousarray(mbr, dtype=np.float64)
@@ -189,6 +191,9 @@ class LsmOracle:
                                        first_end_time_min, self._map.ctypes.data, capacity)
         if not self._h:
             raise MemoryError("lsm_create failed")
+        if bitmap_edge and self._lib.lsm_set_bitmap_edge(self._h, bitmap_edge) != 0:
+            self.close()
+            raise ValueError(f"bitmap_edge {bitmap_edge}: a multiple of 32 up to 1024")
 
     def append(self, meetings: np.ndarray) -> None:
         m = np.ascontiguousarray(meetings, dtype=MEETING_DTYPE)
@@ -246,12 +251,16 @@ def pack_key(pid_field: int, target: int, duration: int, end: int, value_mbr: in
     return bytes(out[: int(ctf["key_bit"][0]) // 8])
 
 
-def o_bitmap(boxes: np.ndarray, map_box) -> np.ndarray:
-    bm = np.zeros(8192, np.uint8)
+def o_bitmap(boxes: np.ndarray, map_box, edge: int = 256) -> np.ndarray:
+    """The map bitmap (edge x edge bits) of a set of oversize key boxes."""
+    bm = np.zeros(edge * edge // 8, np.uint8)
     m = np.ascontiguousarray(map_box, np.float64)
     for b in np.ascontiguousarray(boxes, np.float32).reshape(-1, 4):
         bb = np.ascontiguousarray(b)
-        lib().lsm_o_bitmap(bb.ctypes.data, m.ctypes.data, bm.ctypes.data)
+        if edge == 256:
+            lib().lsm_o_bitmap(bb.ctypes.data, m.ctypes.data, bm.ctypes.data)
+        else:
+            lib().lsm_o_bitmap_edge(bb.ctypes.data, m.ctypes.data, edge, bm.ctypes.data)
     return bm
 
 

@@ -369,9 +369,13 @@ extern "C" cmp_result *cmp_compact(const cmp_block *blocks, uint32_t m, uint32_t
     if (a.dur != b.dur) return a.dur < b.dur;
     return a.end < b.end;
   });
-  R->obitmap.assign(8192, 0);
+  // the map bitmap: every input block's (all of one edge), then the merged
+  // oversize keys' cells
+  const uint32_t edge = blocks[0].info.bitmap_edge ? blocks[0].info.bitmap_edge : 256;
+  const size_t obm_bytes = (size_t)edge * edge / 8;
+  R->obitmap.assign(obm_bytes, 0);
   for (uint32_t i = 0; i < m; i++)
-    for (uint32_t b = 0; b < 8192; b++) R->obitmap[b] |= blocks[i].obitmap[b];
+    for (size_t b = 0; b < obm_bytes; b++) R->obitmap[b] |= blocks[i].obitmap[b];
   uint32_t osmin = 1u << 30, osmax = 0;
   R->okeys.resize(2 * ov.size());
   R->oboxes.resize(4 * ov.size());
@@ -380,7 +384,7 @@ extern "C" cmp_result *cmp_compact(const cmp_block *blocks, uint32_t m, uint32_t
     uint32_t st = r.end - r.dur;
     osmin = std::min(osmin, st);
     osmax = std::max(osmax, st);
-    lsm_o_bitmap(r.box, map, R->obitmap.data());
+    lsm_o_bitmap_edge(r.box, map, edge, R->obitmap.data());
     R->okeys[2 * k] = ((uint64_t)r.dur << 32) | (uint32_t)(r.end - o_etm);
     R->okeys[2 * k + 1] = ((uint64_t)r.oid << 26) | r.target;
     memcpy(&R->oboxes[4 * k], r.box, sizeof(r.box));
@@ -408,6 +412,7 @@ extern "C" cmp_result *cmp_compact(const cmp_block *blocks, uint32_t m, uint32_t
   in.o_start_time_max = osmax;
   in.o_end_time_min = o_etm;
   in.o_end_time_max = o_etmax;
+  in.bitmap_edge = edge;
   return R;
 }
 

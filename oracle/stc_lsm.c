@@ -126,23 +126,27 @@ void lsm_pack_key(uint64_t pid_field, uint64_t target, uint64_t duration, uint64
   for (uint32_t i = 0; i < c->key_bit / 8u; i++) out[i] = (uint8_t)(k >> (8 * i));
 }
 
-/* cuda_write_o_bitmap (cuda/geometry.cu:935-955): cells of a box on the
- * 256 x 256 map grid, in double. The GPU kernel has no bound on the cell
- * index; cells past the last bit of the bitmap are skipped here. */
-void lsm_o_bitmap(const float b[4], const double map[4], uint8_t *bitmap) {
-  uint32_t low0 = d2u32((b[0] - map[0]) / (map[2] - map[0]) * 256);
-  uint32_t low1 = d2u32((b[1] - map[1]) / (map[3] - map[1]) * 256);
-  uint32_t high0 = d2u32((b[2] - map[0]) / (map[2] - map[0]) * 256);
-  uint32_t high1 = d2u32((b[3] - map[1]) / (map[3] - map[1]) * 256);
+/* cuda_write_o_bitmap (cuda/geometry.cu:904-923): cells of a box on the
+ * edge x edge map grid (edge = DEFAULT_bitmap_edge, util/util.h:47, 256 in
+ * the reference), in double. The GPU kernel has no bound on the cell index;
+ * cells past the last bit of the bitmap are skipped here. */
+void lsm_o_bitmap_edge(const float b[4], const double map[4], uint32_t edge, uint8_t *bitmap) {
+  const uint64_t bits = (uint64_t)edge * edge;
+  uint32_t low0 = d2u32((b[0] - map[0]) / (map[2] - map[0]) * edge);
+  uint32_t low1 = d2u32((b[1] - map[1]) / (map[3] - map[1]) * edge);
+  uint32_t high0 = d2u32((b[2] - map[0]) / (map[2] - map[0]) * edge);
+  uint32_t high1 = d2u32((b[3] - map[1]) / (map[3] - map[1]) * edge);
   /* (i, j) past either bound gives a bit past the bitmap */
-  if (high0 > 65535) high0 = 65535;
-  if (high1 > 255) high1 = 255;
+  if (high0 > bits - 1) high0 = (uint32_t)(bits - 1);
+  if (high1 > edge - 1) high1 = edge - 1;
   for (uint64_t i = low0; i <= high0; i++)
     for (uint64_t j = low1; j <= high1; j++) {
-      uint64_t bit = i + j * 256;
-      if (bit < 65536) bitmap[bit / 8] |= (uint8_t)(1u << (bit % 8));
+      uint64_t bit = i + j * edge;
+      if (bit < bits) bitmap[bit / 8] |= (uint8_t)(1u << (bit % 8));
     }
 }
+
+void lsm_o_bitmap(const float b[4], const double map[4], uint8_t *bitmap) { lsm_o_bitmap_edge(b, map, 256, bitmap); }
 
 /* ---- memtable and flush ------------------------------------------------ */
 
@@ -166,7 +170,8 @@ struct lsm_oracle {
   int has_block;
   stc_ctb_info info;
   stc_ctf *ctfs;
-  uint8_t *bitmaps, *kbytes, obitmap[8192];
+  uint8_t *bitmaps, *kbytes, *obitmap;
+  uint32_t edge;  /* map bitmap edge */
   uint16_t *bsids;
   okey *bkeys;  /* sorted: CTF keys, then oversize keys */
   char err[160];
@@ -204,8 +209,10 @@ lsm_oracle *lsm_create(uint32_t n, uint32_t max_meet_time, uint32_t ctf_count, d
   o->ctfs = (stc_ctf *)calloc(ctf_count, sizeof(stc_ctf));
   o->bitmaps = (uint8_t *)calloc((size_t)ctf_count, 8192);
   o->kbytes = (uint8_t *)malloc(capacity * 16 + 16);
+  o->edge = 256;
+  o->obitmap = (uint8_t *)calloc(8192, 1);
   if (!o->keys || !o->bkeys || !o->cnt || !o->obox || !o->sid || !o->bsids || !o->ctfs || !o->bitmaps ||
-      !o->kbytes) {
+      !o->kbytes || !o->obitmap) {
     lsm_destroy(o);
     return NULL;
   }
@@ -217,8 +224,18 @@ lsm_oracle *lsm_create(uint32_t n, uint32_t max_meet_time, uint32_t ctf_count, d
 void lsm_destroy(lsm_oracle *o) {
   if (!o) return;
   free(o->keys); free(o->bkeys); free(o->cnt); free(o->obox); free(o->sid); free(o->bsids);
-  free(o->ctfs); free(o->bitmaps); free(o->kbytes);
+  free(o->ctfs); free(o->bitmaps); free(o->kbytes); free(o->obitmap);
   free(o);
+}
+
+int lsm_set_bitmap_edge(lsm_oracle *o, uint32_t edge) {
+  if (edge == 0 || edge % 32 || edge > 1024) return -1;
+  uint8_t *bm = (uint8_t *)calloc((size_t)edge * edge / 8, 1);
+  if (!bm) return -1;
+  free(o->obitmap);
+  o->obitmap = bm;
+  o->edge = edge;
+  return 0;
 }
 
 const char *lsm_error(const lsm_oracle *o) { return o->err; }
@@ -414,14 +431,14 @@ int lsm_flush(lsm_oracle *o, uint32_t cur_time) {
     }
   }
   /* oversize buffer: time limits (get_o_limit, :957-1010) and map bitmap */
-  memset(o->obitmap, 0, sizeof(o->obitmap));
+  memset(o->obitmap, 0, (size_t)o->edge * o->edge / 8);
   uint32_t osmin = 1u << 30, osmax = 0;
   for (uint64_t k = slim; k < o->kv; k++) {
     const okey *e = &o->bkeys[k];
     uint32_t st = e->end + o->end_time_min - e->dur;
     if (st < osmin) osmin = st;
     if (st > osmax) osmax = st;
-    lsm_o_bitmap(e->box, o->map, o->obitmap);
+    lsm_o_bitmap_edge(e->box, o->map, o->edge, o->obitmap);
   }
   memcpy(o->bsids, o->sid, N * sizeof(uint16_t));
   stc_ctb_info *in = &o->info;
@@ -439,6 +456,7 @@ int lsm_flush(lsm_oracle *o, uint32_t cur_time) {
   in->o_start_time_max = osmax;
   in->o_end_time_min = o->end_time_min;
   in->o_end_time_max = cur_time;
+  in->bitmap_edge = o->edge;
   o->has_block = 1;
   free(cap);
   free(first);
@@ -475,7 +493,7 @@ int lsm_read_ctb(const lsm_oracle *o, stc_ctf *ctfs, uint8_t *bitmaps, uint8_t *
     }
     if (oboxes) memcpy(oboxes + 4 * i, e->box, 4 * sizeof(float));
   }
-  if (obitmap) memcpy(obitmap, o->obitmap, sizeof(o->obitmap));
+  if (obitmap) memcpy(obitmap, o->obitmap, (size_t)o->edge * o->edge / 8);
   return 0;
 }
 

@@ -70,7 +70,10 @@ int lsm_ctf_bits(const float mbr[4], const double map[4], uint32_t num_objects, 
 uint64_t lsm_serialize_mbr(const float b[4], const stc_ctf *c);
 void lsm_pack_key(uint64_t pid_field, uint64_t target, uint64_t duration, uint64_t end, uint64_t value_mbr,
                   const stc_ctf *c, uint8_t *out);
-void lsm_o_bitmap(const float b[4], const double map[4], uint8_t *bitmap);
+void lsm_o_bitmap(const float b[4], const double map[4], uint8_t *bitmap);  /* edge 256 */
+void lsm_o_bitmap_edge(const float b[4], const double map[4], uint32_t edge, uint8_t *bitmap);
+/* map bitmap edge of the blocks flushed from now on (default 256) */
+int lsm_set_bitmap_edge(lsm_oracle *o, uint32_t edge);
 void lsm_decode_key(const uint8_t *key, const stc_ctf *c, uint32_t *oid, uint32_t *target, uint32_t *duration,
                     uint32_t *end, uint64_t *value_mbr, double box[4]);
 /* queries on one block read out as stc_read_ctb lays it out; n: matches so

@@ -240,9 +240,9 @@ __global__ void k_cmp_limits_init(float4 *lim_box, uint2 *lim_time, uint32_t F) 
   lim_time[c] = make_uint2(1u << 30, 1u);  // merge_dump starts the start-time maximum at 1 (:989)
 }
 
-__global__ void k_cmp_or_bitmap(const uint32_t *in, uint32_t *out) {
+__global__ void k_cmp_or_bitmap(const uint32_t *in, uint32_t *out, uint32_t words) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < STC_BITMAP_BYTES / 4) out[i] |= in[i];
+  if (i < words) out[i] |= in[i];
 }
 
 __global__ void k_cmp_state_init(DevState *st) {
@@ -446,8 +446,9 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
   }
   CtbBlock B;
   const size_t no_out = (size_t)n_over;
-  e = cudaMalloc(&B.obitmap, STC_BITMAP_BYTES);
-  if (e == cudaSuccess) e = cudaMemsetAsync(B.obitmap, 0, STC_BITMAP_BYTES, s);
+  const size_t obm_bytes = STC_MAP_BITMAP_BYTES(L.edge);
+  e = cudaMalloc(&B.obitmap, obm_bytes);
+  if (e == cudaSuccess) e = cudaMemsetAsync(B.obitmap, 0, obm_bytes, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(C.ctf_first, cfirst.data(), (F2 + 1) * sizeof(unsigned long long),
                                             cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) {
@@ -458,7 +459,7 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
   STC_KL k_cmp_limits_init<<<nblk(F2), 256, 0, s>>>(C.lim_box, C.lim_time, F2);
   if (slim) STC_KL k_lsm_limits<<<dim3(F2, LIM_PARTS), 256, 0, s>>>(C, slim);
   for (const CtbBlock *b : in)
-    STC_KL k_cmp_or_bitmap<<<nblk(STC_BITMAP_BYTES / 4), 256, 0, s>>>(b->obitmap, B.obitmap);
+    STC_KL k_cmp_or_bitmap<<<nblk(obm_bytes / 4), 256, 0, s>>>(b->obitmap, B.obitmap, (uint32_t)(obm_bytes / 4));
   if (T > slim) {
     LsmDev O = C;
     O.end_time_min = o_etm;
@@ -522,6 +523,7 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
   B.info.o_start_time_max = st.lsm_os_max;
   B.info.o_end_time_min = o_etm;
   B.info.o_end_time_max = o_etmax;
+  B.info.bitmap_edge = L.edge;
   e = cudaMalloc(&B.keys, off + 32);
   if (e == cudaSuccess) e = cudaMalloc(&B.d_ctfs, F2 * sizeof(stc_ctf));
   if (e == cudaSuccess) e = cudaMalloc(&B.bitmaps, (size_t)F2 * STC_BITMAP_BYTES);

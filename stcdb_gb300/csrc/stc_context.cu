@@ -289,6 +289,11 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
                      "num_objects < 2^26, kv_capacity > kv_restriction, both < 2^31)";
     return STC_ERR_INVALID_ARG;
   }
+  if (k.bitmap_edge % 32 || k.bitmap_edge > 1024) {
+    g_create_error = "stc_create: bitmap_edge must be 0 (256) or a multiple of 32 up to 1024";
+    return STC_ERR_INVALID_ARG;
+  }
+  const uint32_t bm_edge = k.bitmap_edge ? k.bitmap_edge : 256;  // util/util.h:47
   stc_ctx *c = new (std::nothrow) stc_ctx();
   if (!c) {
     g_create_error = "stc_create: out of host memory";
@@ -411,6 +416,7 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
     L.end_time_min = k.start_time + k.min_meet_time;  // tracing/process.cpp:404
     L.area = k.area_restriction > 0 ? k.area_restriction : 100.0;  // process.cpp:408-411: 100 = no cut
     L.map[0] = mbr[0]; L.map[1] = mbr[1]; L.map[2] = mbr[2]; L.map[3] = mbr[3];
+    L.edge = bm_edge;
     // a step adds at most two keys per emitted meeting, so the default never overflows
     L.cap = k.kv_capacity ? k.kv_capacity
                           : std::min<unsigned long long>(k.kv_restriction + 2 * p.E, (1ull << 31) - 1);
@@ -423,11 +429,12 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
          dalloc(c, &L.mid_hi, n) && dalloc(c, &L.ctf_cap, ctf_count) && dalloc(c, &L.ctf_first, ctf_count + 1) &&
          dalloc(c, &L.ctfs, ctf_count) && dalloc(c, &L.lim_box, ctf_count) && dalloc(c, &L.lim_time, ctf_count) &&
          dalloc(c, &L.bitmaps, (size_t)ctf_count * (STC_BITMAP_BYTES / 4)) &&
-         dalloc(c, &L.obitmap, STC_BITMAP_BYTES / 4) && dalloc(c, &L.kbytes, 16 * (size_t)L.cap);
+         dalloc(c, &L.obitmap, STC_MAP_BITMAP_BYTES(bm_edge) / 4) && dalloc(c, &L.kbytes, 16 * (size_t)L.cap);
     for (int i = 0; ok && i < 7; i++) ok = dalloc(c, &L.sk[i], w);
     L.st = p.st;
     LsmHost &H = c->lsmh;
     H.retain = k.ctb_retain ? k.ctb_retain : 8;
+    H.edge = bm_edge;
     for (int i = 0; i < 4; i++) H.map[i] = mbr[i];
     int least = 0, greatest = 0;
     cudaDeviceGetStreamPriorityRange(&least, &greatest);
@@ -1092,7 +1099,7 @@ extern "C" stc_status stc_read_ctb(stc_ctx *c, stc_ctf *ctfs, uint8_t *bitmaps, 
     e = cudaMemcpyAsync(keys, L.kbytes, in.key_bytes, cudaMemcpyDeviceToHost, s);
   if (sids && e == cudaSuccess) e = cudaMemcpyAsync(sids, L.bsid, (size_t)L.N * 2, cudaMemcpyDeviceToHost, s);
   if (oversize_bitmap && e == cudaSuccess)
-    e = cudaMemcpyAsync(oversize_bitmap, L.obitmap, STC_BITMAP_BYTES, cudaMemcpyDeviceToHost, s);
+    e = cudaMemcpyAsync(oversize_bitmap, L.obitmap, STC_MAP_BITMAP_BYTES(L.edge), cudaMemcpyDeviceToHost, s);
   std::vector<uint4> orec;
   const size_t no = (size_t)in.oversize_kv_count;
   if (no && oversize_keys && e == cudaSuccess) {

@@ -327,9 +327,10 @@ __global__ void k_lsm_limits(LsmDev L, unsigned long long K) {
   }
 }
 
-// get_o_limit and cuda_write_o_bitmap (cuda/geometry.cu:935-1010): start
-// times of the oversize keys and the 256 x 256 map bitmap of their boxes (in
-// double, relative to the map box). Cells past the bitmap are skipped.
+// get_o_limit and cuda_write_o_bitmap (cuda/geometry.cu:904-955): start
+// times of the oversize keys and the edge x edge map bitmap of their boxes
+// (in double, relative to the map box; edge is the reference's
+// DEFAULT_bitmap_edge, util/util.h:47). Cells past the bitmap are skipped.
 __global__ void k_lsm_oversize(LsmDev L, unsigned long long a, unsigned long long b) {
   uint32_t smin = 1u << 30, smax = 0;
   for (unsigned long long k = a + (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; k < b;
@@ -340,16 +341,19 @@ __global__ void k_lsm_oversize(LsmDev L, unsigned long long a, unsigned long lon
     smin = min(smin, start);
     smax = max(smax, start);
     double wx = __dsub_rn(L.map[2], L.map[0]), wy = __dsub_rn(L.map[3], L.map[1]);
-    uint32_t low0 = d2u_cell(__dmul_rn(__ddiv_rn(__dsub_rn((double)bx.x, L.map[0]), wx), 256.0));
-    uint32_t low1 = d2u_cell(__dmul_rn(__ddiv_rn(__dsub_rn((double)bx.y, L.map[1]), wy), 256.0));
-    uint32_t high0 = d2u_cell(__dmul_rn(__ddiv_rn(__dsub_rn((double)bx.z, L.map[0]), wx), 256.0));
-    uint32_t high1 = d2u_cell(__dmul_rn(__ddiv_rn(__dsub_rn((double)bx.w, L.map[1]), wy), 256.0));
-    high0 = min(high0, 65535u);
-    high1 = min(high1, 255u);
+    const double E = (double)L.edge;
+    const uint32_t bits = L.edge * L.edge;
+    uint32_t low0 = d2u_cell(__dmul_rn(__ddiv_rn(__dsub_rn((double)bx.x, L.map[0]), wx), E));
+    uint32_t low1 = d2u_cell(__dmul_rn(__ddiv_rn(__dsub_rn((double)bx.y, L.map[1]), wy), E));
+    uint32_t high0 = d2u_cell(__dmul_rn(__ddiv_rn(__dsub_rn((double)bx.z, L.map[0]), wx), E));
+    uint32_t high1 = d2u_cell(__dmul_rn(__ddiv_rn(__dsub_rn((double)bx.w, L.map[1]), wy), E));
+    // (i, j) past either bound gives a bit past the bitmap
+    high0 = min(high0, bits - 1u);
+    high1 = min(high1, L.edge - 1u);
     for (uint32_t i = low0; i <= high0; i++)
       for (uint32_t j = low1; j <= high1; j++) {
-        uint32_t bit = i + j * 256u;
-        if (bit < 65536u) atomicOr(&L.obitmap[bit >> 5], 1u << (bit & 31u));
+        uint32_t bit = i + j * L.edge;
+        if (bit < bits) atomicOr(&L.obitmap[bit >> 5], 1u << (bit & 31u));
       }
   }
 #pragma unroll
@@ -660,7 +664,7 @@ stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState
   STC_KL k_lsm_flush_begin<<<1, 1, 0, s>>>(L.st);
   cudaMemsetAsync(L.ctf_cap, 0, (size_t)F * sizeof(uint32_t), s);
   cudaMemsetAsync(L.bitmaps, 0, (size_t)F * STC_BITMAP_BYTES, s);
-  cudaMemsetAsync(L.obitmap, 0, STC_BITMAP_BYTES, s);
+  cudaMemsetAsync(L.obitmap, 0, STC_MAP_BITMAP_BYTES(L.edge), s);
   // 1. object boxes -> oversize objects and STR midpoints; key partition flags
   STC_KL k_lsm_set_oid<<<nblk(N), 256, 0, s>>>(L);
   STC_KL k_lsm_flags<<<lsm_grid(), 256, 0, s>>>(L, K);
@@ -754,6 +758,7 @@ stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState
   in.o_start_time_max = st_host->lsm_os_max;
   in.o_end_time_min = L.end_time_min;
   in.o_end_time_max = t;
+  in.bitmap_edge = L.edge;
   reset_memtable(L, s);  // after the encode on the same stream, which reads the sids
   if ((e = read_state()) != cudaSuccess) return cuda_err(e, "flush", err);
   H.info = in;

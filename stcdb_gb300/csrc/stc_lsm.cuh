@@ -26,6 +26,7 @@ namespace stc {
 struct LsmDev {
   uint32_t N, max_meet, F, split;
   uint32_t end_time_min;
+  uint32_t edge;                   // map bitmap edge (bitmap_edge)
   double area;
   double map[4];
   unsigned long long cap;          // memtable capacity (directed keys)
@@ -49,7 +50,7 @@ struct LsmDev {
   float4 *lim_box;                 // [F] per-CTF box
   uint2 *lim_time;                 // [F] per-CTF start min, max
   uint32_t *bitmaps;               // [F * 2048]
-  uint32_t *obitmap;               // [2048]
+  uint32_t *obitmap;               // [edge * edge / 32]
   uint8_t *kbytes;                 // packed CTF keys (16 * cap bytes)
 };
 
@@ -81,7 +82,7 @@ struct CtbBlock {
   uint16_t *sids = nullptr;        // [N]
   uint4 *orec = nullptr;           // oversize keys (pid, target, duration, end offset), sorted
   float4 *obox = nullptr;
-  uint32_t *obitmap = nullptr;     // [2048]
+  uint32_t *obitmap = nullptr;     // [edge * edge / 32]: map bitmap
   // spatial index of the CTF keys: per CTF, dense cells (gx + 1) x (gy + 1)
   // of the low corner of each key's box, then one wide slot
   uint32_t *perm = nullptr;        // block key positions sorted by dense cell id
@@ -111,7 +112,7 @@ struct QBlock {
   const double2 *ixs;
   const uint16_t *pend;
   unsigned long long n_over;
-  uint32_t F, index, o_end_time_min, pad;
+  uint32_t F, index, o_end_time_min, edge;  // edge: of the map bitmap
 };
 
 // One match on the device: the contact and the query it answers.
@@ -162,6 +163,7 @@ struct LsmHost {
   std::vector<stc_ctf> ctfs;
   // retained blocks (oldest first) and the query state
   uint32_t retain = 8;
+  uint32_t edge = 256;             // map bitmap edge of every block (bitmap_edge)
   std::deque<CtbBlock> blocks;
   std::shared_mutex blocks_mu;     // exclusive while the list changes
   QueryLane lanes[QUERY_LANES];

@@ -485,14 +485,15 @@ constexpr uint32_t SEQ_BITMAP_CELLS = 1024;  // larger windows skip the per-thre
 
 // Any set bit in cells [i0, i1] x [j0, j1] (one thread); windows of more than
 // SEQ_BITMAP_CELLS cells are taken as hit (the bitmap only prunes).
-__device__ bool any_bit_seq(const uint32_t *bm, int i0, int i1, int j0, int j1, uint32_t xg) {
+// Bits past `nbits` (the bitmap's size) read as clear.
+__device__ bool any_bit_seq(const uint32_t *bm, int i0, int i1, int j0, int j1, uint32_t xg, long long nbits) {
   long long ni = (long long)i1 - i0 + 1, nj = (long long)j1 - j0 + 1;
   if (ni <= 0 || nj <= 0) return false;
   if (ni * nj > SEQ_BITMAP_CELLS) return true;
   for (long long j = j0; j <= j1; j++)
     for (long long i = i0; i <= i1; i++) {
       long long bit = i + j * (long long)xg;
-      if (bit >= 0 && bit < 65536 && ((__ldg(&bm[bit >> 5]) >> (bit & 31)) & 1u)) return true;
+      if (bit >= 0 && bit < nbits && ((__ldg(&bm[bit >> 5]) >> (bit & 31)) & 1u)) return true;
     }
   return false;
 }
@@ -584,9 +585,10 @@ __global__ void k_box_plan(const QBlock *qb, uint32_t nb, const stc_query *qs, u
       if (c == b.F) {  // oversize buffer: the map bitmap prunes
         if (b.n_over) {
           int i0, i1, j0, j1;
-          cell_range(q.box[0], q.box[2], m0x, m1x, 256, i0, i1);
-          cell_range(q.box[1], q.box[3], m0y, m1y, 256, j0, j1);
-          if (any_bit_seq(b.obitmap, i0, i1, j0, j1, 256)) n = (uint32_t)((b.n_over + OV_CHUNK - 1) / OV_CHUNK);
+          cell_range(q.box[0], q.box[2], m0x, m1x, b.edge, i0, i1);
+          cell_range(q.box[1], q.box[3], m0y, m1y, b.edge, j0, j1);
+          if (any_bit_seq(b.obitmap, i0, i1, j0, j1, b.edge, (long long)b.edge * b.edge))
+            n = (uint32_t)((b.n_over + OV_CHUNK - 1) / OV_CHUNK);
         }
       } else {
         const stc_ctf &t = b.ctfs[c];
@@ -603,7 +605,8 @@ __global__ void k_box_plan(const QBlock *qb, uint32_t nb, const stc_query *qs, u
             int bi0, bi1, bj0, bj1;  // the bitmap's cells
             cell_range(x.wide[0], x.wide[2], t.mbr[0], t.mbr[2], t.x_grid, bi0, bi1);
             cell_range(x.wide[1], x.wide[3], t.mbr[1], t.mbr[3], t.y_grid, bj0, bj1);
-            if (any_bit_seq(b.bitmaps + (size_t)c * (STC_BITMAP_BYTES / 4), bi0, bi1, bj0, bj1, t.x_grid)) {
+            if (any_bit_seq(b.bitmaps + (size_t)c * (STC_BITMAP_BYTES / 4), bi0, bi1, bj0, bj1, t.x_grid,
+                            8ll * STC_BITMAP_BYTES)) {
               n = 1;  // the wide list
               for (uint32_t lv = 0; lv < x.levels; lv++) {
                 int cj0;
@@ -922,7 +925,7 @@ stc_status lsm_store_block(const LsmDev &L, LsmHost &H, cudaStream_t s, std::str
   if (e == cudaSuccess) e = cudaMalloc(&B.sids, (size_t)L.N * sizeof(uint16_t));
   if (e == cudaSuccess) e = cudaMalloc(&B.orec, std::max<size_t>(no, 1) * sizeof(uint4));
   if (e == cudaSuccess) e = cudaMalloc(&B.obox, std::max<size_t>(no, 1) * sizeof(float4));
-  if (e == cudaSuccess) e = cudaMalloc(&B.obitmap, STC_BITMAP_BYTES);
+  if (e == cudaSuccess) e = cudaMalloc(&B.obitmap, STC_MAP_BITMAP_BYTES(L.edge));
   if (e == cudaSuccess) e = cudaMemsetAsync(B.keys + H.info.key_bytes, 0, 32, s);
   if (e == cudaSuccess && H.info.key_bytes)
     e = cudaMemcpyAsync(B.keys, L.kbytes, H.info.key_bytes, cudaMemcpyDeviceToDevice, s);
@@ -933,7 +936,8 @@ stc_status lsm_store_block(const LsmDev &L, LsmHost &H, cudaStream_t s, std::str
     e = cudaMemcpyAsync(B.orec, L.brec + H.info.ctf_kv_count, no * sizeof(uint4), cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess && no)
     e = cudaMemcpyAsync(B.obox, L.bbox + H.info.ctf_kv_count, no * sizeof(float4), cudaMemcpyDeviceToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(B.obitmap, L.obitmap, STC_BITMAP_BYTES, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(B.obitmap, L.obitmap, STC_MAP_BITMAP_BYTES(L.edge), cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = build_index(L, B, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
@@ -1087,7 +1091,7 @@ stc_status lsm_query(LsmHost &H, int lane, const stc_query *qs, size_t nq, stc_c
     qb[i] = QBlock{B.keys, B.d_ctfs, B.sids, B.orec, B.obox, B.bitmaps, B.obitmap, B.perm, B.cstart, B.cbase, B.ixg,
                    B.ixs, B.pend,
                    (unsigned long long)B.info.oversize_kv_count, B.info.ctf_count, B.info.index,
-                   B.info.o_end_time_min, 0};
+                   B.info.o_end_time_min, B.info.bitmap_edge ? B.info.bitmap_edge : 256u};
   }
   bool has_obj = false, has_box = false;
   for (size_t i = 0; i < nq; i++) ((qs[i].kind & 0xFFu) == STC_QUERY_BOX ? has_box : has_obj) = true;
@@ -1192,6 +1196,9 @@ inline void put16(uint8_t *b, size_t off, uint16_t v) { memcpy(b + off, &v, 2); 
 inline uint32_t get32(const uint8_t *b, size_t off) { uint32_t v; memcpy(&v, b + off, 4); return v; }
 inline uint16_t get16(const uint8_t *b, size_t off) { uint16_t v; memcpy(&v, b + off, 2); return v; }
 
+// Bytes of a block's map bitmap.
+size_t map_bitmap_bytes(const stc_ctb_info &in) { return STC_MAP_BITMAP_BYTES(in.bitmap_edge ? in.bitmap_edge : 256); }
+
 std::string ctb_path(const std::string &dir, const std::string &prefix, const char *kind, uint32_t ctb, long ctf) {
   std::string p = dir + "/" + prefix + kind + std::to_string(ctb);
   if (ctf >= 0) p += "-" + std::to_string(ctf);
@@ -1260,7 +1267,7 @@ stc_status lsm_write_block(LsmHost &H, uint32_t index, uint32_t N, const std::st
   const stc_ctb_info &in = B->info;
   const uint32_t F = in.ctf_count;
   const size_t no = (size_t)in.oversize_kv_count;
-  std::vector<uint8_t> keys(in.key_bytes), bitmaps((size_t)F * STC_BITMAP_BYTES), obitmap(STC_BITMAP_BYTES);
+  std::vector<uint8_t> keys(in.key_bytes), bitmaps((size_t)F * STC_BITMAP_BYTES), obitmap(map_bitmap_bytes(in));
   std::vector<uint16_t> sids(N);
   std::vector<uint4> orec(no);
   std::vector<float4> obox(no);
@@ -1270,7 +1277,7 @@ stc_status lsm_write_block(LsmHost &H, uint32_t index, uint32_t N, const std::st
   if (e == cudaSuccess) e = cudaMemcpy(sids.data(), B->sids, (size_t)N * 2, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && no) e = cudaMemcpy(orec.data(), B->orec, no * sizeof(uint4), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && no) e = cudaMemcpy(obox.data(), B->obox, no * sizeof(float4), cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess) e = cudaMemcpy(obitmap.data(), B->obitmap, STC_BITMAP_BYTES, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(obitmap.data(), B->obitmap, obitmap.size(), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) {
     err = std::string("reading the block: ") + cudaGetErrorString(e);
     return STC_ERR_CUDA;
@@ -1287,7 +1294,7 @@ stc_status lsm_write_block(LsmHost &H, uint32_t index, uint32_t N, const std::st
       return STC_ERR_INVALID_ARG;
     }
   }
-  std::vector<uint8_t> ctb(REF_CTB_BYTES + (size_t)N * 2 + no * 32 + STC_BITMAP_BYTES, 0);
+  std::vector<uint8_t> ctb(REF_CTB_BYTES + (size_t)N * 2 + no * 32 + obitmap.size(), 0);
   uint8_t *h = ctb.data();
   put32(h, REF_OBUF + 0, (uint32_t)no);
   put32(h, REF_OBUF + 32, in.o_start_time_min);
@@ -1305,7 +1312,7 @@ stc_status lsm_write_block(LsmHost &H, uint32_t index, uint32_t N, const std::st
   off += no * 16;
   memcpy(h + off, obox.data(), no * 16);
   off += no * 16;
-  memcpy(h + off, obitmap.data(), STC_BITMAP_BYTES);
+  memcpy(h + off, obitmap.data(), obitmap.size());
   std::string pc = ctb_path(dir, prefix, "_CTB", index, -1);
   if (!write_file(pc, ctb.data(), ctb.size(), nullptr, 0)) {
     err = "cannot write " + pc;
@@ -1342,7 +1349,7 @@ stc_status lsm_read_block(LsmHost &H, uint32_t index, uint32_t N, stc_ctf *ctfs,
   if (bitmaps) e = cudaMemcpy(bitmaps, B->bitmaps, (size_t)in.ctf_count * STC_BITMAP_BYTES, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && keys && in.key_bytes) e = cudaMemcpy(keys, B->keys, in.key_bytes, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && sids) e = cudaMemcpy(sids, B->sids, (size_t)N * 2, cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess && obitmap) e = cudaMemcpy(obitmap, B->obitmap, STC_BITMAP_BYTES, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && obitmap) e = cudaMemcpy(obitmap, B->obitmap, map_bitmap_bytes(in), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && oboxes && no) e = cudaMemcpy(oboxes, B->obox, no * sizeof(float4), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && okeys && no) {
     std::vector<uint4> orec(no);
@@ -1381,9 +1388,10 @@ stc_status lsm_load_block(const LsmDev &L, LsmHost &H, uint32_t index, const std
     return STC_ERR_INVALID_ARG;
   }
   const size_t no = get32(ctb.data(), REF_OBUF);
-  if (ctb.size() != REF_CTB_BYTES + (size_t)N * 2 + no * 32 + STC_BITMAP_BYTES) {
-    err = pc + ": size does not match " + std::to_string(N) + " objects and " + std::to_string(no) +
-          " oversize keys";
+  const size_t obm_bytes = STC_MAP_BITMAP_BYTES(H.edge);  // the file does not record the edge
+  if (ctb.size() != REF_CTB_BYTES + (size_t)N * 2 + no * 32 + obm_bytes) {
+    err = pc + ": size does not match " + std::to_string(N) + " objects, " + std::to_string(no) +
+          " oversize keys and a map bitmap of edge " + std::to_string(H.edge);
     return STC_ERR_INVALID_ARG;
   }
   CtbBlock B;
@@ -1447,13 +1455,14 @@ stc_status lsm_load_block(const LsmDev &L, LsmHost &H, uint32_t index, const std
   in.o_start_time_max = get32(h, REF_OBUF + 36);
   in.o_end_time_min = get32(h, REF_OBUF + 40);
   in.o_end_time_max = get32(h, REF_OBUF + 44);
+  in.bitmap_edge = H.edge;
   cudaError_t e = cudaMalloc(&B.keys, keys.size() + 32);
   if (e == cudaSuccess) e = cudaMalloc(&B.d_ctfs, F * sizeof(stc_ctf));
   if (e == cudaSuccess) e = cudaMalloc(&B.bitmaps, bitmaps.size());
   if (e == cudaSuccess) e = cudaMalloc(&B.sids, (size_t)N * 2);
   if (e == cudaSuccess) e = cudaMalloc(&B.orec, std::max<size_t>(no, 1) * sizeof(uint4));
   if (e == cudaSuccess) e = cudaMalloc(&B.obox, std::max<size_t>(no, 1) * sizeof(float4));
-  if (e == cudaSuccess) e = cudaMalloc(&B.obitmap, STC_BITMAP_BYTES);
+  if (e == cudaSuccess) e = cudaMalloc(&B.obitmap, obm_bytes);
   if (e == cudaSuccess) e = cudaMemsetAsync(B.keys + keys.size(), 0, 32, s);
   if (e == cudaSuccess && !keys.empty()) e = cudaMemcpyAsync(B.keys, keys.data(), keys.size(), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(B.d_ctfs, B.ctfs.data(), F * sizeof(stc_ctf), cudaMemcpyHostToDevice, s);
@@ -1461,7 +1470,7 @@ stc_status lsm_load_block(const LsmDev &L, LsmHost &H, uint32_t index, const std
   if (e == cudaSuccess) e = cudaMemcpyAsync(B.sids, sids.data(), (size_t)N * 2, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && no) e = cudaMemcpyAsync(B.orec, orec.data(), no * sizeof(uint4), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && no) e = cudaMemcpyAsync(B.obox, obox.data(), no * sizeof(float4), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(B.obitmap, obm, STC_BITMAP_BYTES, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(B.obitmap, obm, obm_bytes, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = build_index(L, B, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {

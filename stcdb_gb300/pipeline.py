@@ -58,6 +58,7 @@ class _Config(ctypes.Structure):
         ("refine_blocks_per_sm", ctypes.c_uint32),
         ("hits_blocks_per_sm", ctypes.c_uint32),
         ("window_graphs", ctypes.c_uint32),
+        ("bitmap_edge", ctypes.c_uint32),
     ]
 
 
@@ -121,6 +122,8 @@ class StcCtbInfo(ctypes.Structure):
         ("o_start_time_max", ctypes.c_uint32),
         ("o_end_time_min", ctypes.c_uint32),
         ("o_end_time_max", ctypes.c_uint32),
+        ("bitmap_edge", ctypes.c_uint32),
+        ("pad", ctypes.c_uint32),
     ]
 
     def as_dict(self) -> dict:
@@ -135,7 +138,13 @@ CTF_DTYPE = np.dtype([("mbr", "<f4", (4,)), ("kv_count", "<u4"), ("start_time_mi
                       ("mbr_bit", "<u2"), ("x_grid", "<u2"), ("y_grid", "<u2"), ("pad", "<u4"),
                       ("first_key", "<u8"), ("key_offset", "<u8")])
 assert CTF_DTYPE.itemsize == 80
-BITMAP_BYTES = 8192  # STC_BITMAP_BYTES
+BITMAP_BYTES = 8192  # STC_BITMAP_BYTES: one CTF bitmap slot
+
+
+def map_bitmap_bytes(edge: int) -> int:
+    """STC_MAP_BITMAP_BYTES: bytes of a block's map bitmap of edge x edge bits."""
+    edge = int(edge) or 256
+    return edge * edge // 8
 
 # stc_contact and stc_query (include/stc.h)
 CONTACT_DTYPE = np.dtype([("pid", "<u4"), ("target", "<u4"), ("start", "<u4"), ("end", "<u4"),
@@ -179,7 +188,7 @@ def ctb_buffers(info: StcCtbInfo, num_objects: int) -> dict:
                 sids=np.zeros(num_objects, np.uint16),
                 oversize_keys=np.zeros(2 * max(int(info.oversize_kv_count), 1), np.uint64),
                 oversize_boxes=np.zeros(4 * max(int(info.oversize_kv_count), 1), np.float32),
-                oversize_bitmap=np.zeros(BITMAP_BYTES, np.uint8))
+                oversize_bitmap=np.zeros(map_bitmap_bytes(info.bitmap_edge), np.uint8))
 
 
 def ctb_trim(info: StcCtbInfo, bufs: dict) -> dict:
@@ -221,6 +230,7 @@ class StcConfig:
     refine_blocks_per_sm: int = 0  # 0 = 8
     hits_blocks_per_sm: int = 0    # 0 = 16
     window_graphs: int = 0    # step_window replays a captured graph: 0 = up to 2^21 objects, 1 = always, 2 = never
+    bitmap_edge: int = 0      # edge of a block's map bitmap (oversize buffer); 0 = 256
 
     def resolved(self) -> "StcConfig":
         if self.num_meeting_buckets == 0:

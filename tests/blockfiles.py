@@ -77,7 +77,7 @@ def ctb_file(info, blk, lay, ctb_times=(0, 0, 0, 0)) -> bytes:
             blk["oversize_boxes"].astype("<f4").tobytes() + blk["oversize_bitmap"].tobytes())
 
 
-def parse_ctb_file(data: bytes, lay, num_objects: int) -> dict:
+def parse_ctb_file(data: bytes, lay, num_objects: int, bitmap_edge: int = 256) -> dict:
     ob = lay["CTB.o_buffer"][0]
     out = {f: int(_get(data, lay["CTB." + f][0], "<u4")[0])
            for f in ("start_time_min", "start_time_max", "end_time_min", "end_time_max")}
@@ -92,7 +92,8 @@ def parse_ctb_file(data: bytes, lay, num_objects: int) -> dict:
     off += 16 * n
     out["oversize_boxes"] = _get(data, off, "<f4", 4 * n).copy()
     off += 16 * n
-    out["oversize_bitmap"] = np.frombuffer(data[off:off + 8192], np.uint8).copy()
+    nb = bitmap_edge * bitmap_edge // 8
+    out["oversize_bitmap"] = np.frombuffer(data[off:off + nb], np.uint8).copy()
     return out
 
 

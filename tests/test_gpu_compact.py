@@ -28,12 +28,12 @@ def _same_block(g, o, what):
         assert a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8)), f"{what}: {k} differs"
 
 
-def _run(max_meet, steps=14, n=30000):
+def _run(max_meet, steps=14, n=30000, edge=0):
     """A run that flushes several blocks and keeps them all."""
     tc = hotspot_grid(n, n_hotspots=30, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=11)
     cfg = StcConfig(num_objects=n, reach_distance=10.0, min_meet_time=3, max_meet_time=max_meet, grid_capacity=50,
                     grid_amplify=1.2, num_meeting_buckets=1_500_000, kv_restriction=60_000, ctf_count=16,
-                    ctb_retain=16)
+                    ctb_retain=16, bitmap_edge=edge)
     tr, mbr = trace_and_box(tc, steps)
     pipe = Pipeline(cfg, mbr, tr[0])
     for t in range(steps):
@@ -57,10 +57,10 @@ def _queries(rng, blk, mbr, n_obj=150, n_box=60):
     return qs
 
 
-@pytest.mark.parametrize("max_meet,split", [(4096, 4), (6, 5), (6, 1)])
-def test_compaction_is_the_oracles(built_cuda, max_meet, split):
+@pytest.mark.parametrize("max_meet,split,edge", [(4096, 4, 0), (6, 5, 0), (6, 1, 0), (6, 5, 512)])
+def test_compaction_is_the_oracles(built_cuda, max_meet, split, edge):
     import oracle as orc
-    cfg, mbr, pipe, _ = _run(max_meet)
+    cfg, mbr, pipe, _ = _run(max_meet, edge=edge)
     try:
         infos = [pipe.block_info(i) for i in range(64) if _retained(pipe, i)]
         assert len(infos) >= 4
@@ -99,8 +99,9 @@ def _retained(pipe, i):
         return False
 
 
-def test_compacted_block_files_load_back(built_cuda, tmp_path):
-    cfg, mbr, pipe, xy0 = _run(6)
+@pytest.mark.parametrize("edge", [0, 512])
+def test_compacted_block_files_load_back(built_cuda, tmp_path, edge):
+    cfg, mbr, pipe, xy0 = _run(6, edge=edge)
     try:
         new, _ = pipe.compact(0, 3, 7)  # 49 CTFs in a context of 16
         info, blk = pipe.read_block(new)
@@ -115,6 +116,8 @@ def test_compacted_block_files_load_back(built_cuda, tmp_path):
             fresh.load_ctb(new, d, "c")
             li, lb = fresh.read_block(new)
             assert int(li.ctf_count) == 49 and lb["keys"].tobytes() == blk["keys"].tobytes()
+            assert lb["oversize_bitmap"].tobytes() == blk["oversize_bitmap"].tobytes()
+            assert len(lb["oversize_bitmap"]) == (edge or 256) ** 2 // 8
             got = fresh.query_batch(qs)
             for i in range(len(qs)):
                 assert sort_contacts(got[i]).tobytes() == sort_contacts(want[i]).tobytes(), f"query {i}"

@@ -29,7 +29,7 @@ def _run(cfg, tcfg, steps):
     pipe = Pipeline(cfg, mbr, tr[0])
     ref = orc.Oracle(cfg, mbr, tr[0])
     lsm = orc.LsmOracle(cfg.num_objects, cfg.max_meet_time, cfg.ctf_count or 100, cfg.area_restriction or 100.0,
-                        cfg.start_time + cfg.min_meet_time, mbr, 1 << 21)
+                        cfg.start_time + cfg.min_meet_time, mbr, 1 << 21, bitmap_edge=cfg.bitmap_edge)
     blocks = 0
     try:
         for t in range(steps):
@@ -68,6 +68,18 @@ def test_flush_hotspot_long_meetings(built_cuda):
     assert _run(cfg, tc, 15) >= 2
 
 
+@pytest.mark.parametrize("edge", [512, 96])
+def test_flush_map_bitmap_edge(built_cuda, edge):
+    """A map bitmap other than the reference's 256 x 256 (the stress
+    configuration's 512 x 512; 96, not a power of two): the oversize buffer's
+    bitmap has edge^2 bits, the rest of the block is unchanged."""
+    tc = hotspot_grid(30000, n_hotspots=30, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=11)
+    cfg = StcConfig(num_objects=30000, reach_distance=10.0, min_meet_time=3, max_meet_time=6, grid_capacity=50,
+                    grid_amplify=1.2, num_meeting_buckets=1_500_000, kv_restriction=60_000, ctf_count=16,
+                    bitmap_edge=edge)
+    assert _run(cfg, tc, 8) >= 1
+
+
 def test_flush_area_restriction(built_cuda):
     """Objects whose box of all meetings is larger than the area restriction
     (the reference's smallest table entry) go to the oversize buffer."""
@@ -90,6 +102,9 @@ def test_flush_rejects_bad_config_and_off_memtable(built_cuda):
     tr, mbr = trace_and_box(uniform_grid(2000, seed=1), 1)
     with pytest.raises(StcError):
         Pipeline(StcConfig(num_objects=2000, kv_restriction=1000, ctf_count=10), mbr, tr[0])
+    for edge in (100, 2048):  # not a multiple of 32; too large
+        with pytest.raises(StcError):
+            Pipeline(StcConfig(num_objects=2000, kv_restriction=1000, bitmap_edge=edge), mbr, tr[0])
     with Pipeline(StcConfig(num_objects=2000), mbr, tr[0]) as p:
         with pytest.raises(StcError):
             p.flush()

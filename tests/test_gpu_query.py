@@ -22,7 +22,7 @@ def _ingest(cfg, tcfg, steps, retain):
     pipe = Pipeline(cfg, mbr, tr[0])
     ref = orc.Oracle(cfg, mbr, tr[0])
     lsm = orc.LsmOracle(cfg.num_objects, cfg.max_meet_time, cfg.ctf_count or 100, cfg.area_restriction or 100.0,
-                        cfg.start_time + cfg.min_meet_time, mbr, 1 << 21)
+                        cfg.start_time + cfg.min_meet_time, mbr, 1 << 21, bitmap_edge=cfg.bitmap_edge)
     blocks = []
     try:
         for t in range(steps):
@@ -91,11 +91,15 @@ def _compare(pipe, blocks, qs):
     return total
 
 
-def test_queries_hotspot_with_oversize(built_cuda):
+@pytest.mark.parametrize("edge", [0, 512])
+def test_queries_hotspot_with_oversize(built_cuda, edge):
+    """Oversize keys in every block; box queries prune the oversize buffer by
+    the block's map bitmap (256 x 256 by default, 512 x 512 as in the stress
+    configuration)."""
     tc = hotspot_grid(30000, n_hotspots=30, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=11)
     cfg = StcConfig(num_objects=30000, reach_distance=10.0, min_meet_time=3, max_meet_time=6, grid_capacity=50,
                     grid_amplify=1.2, num_meeting_buckets=1_500_000, kv_restriction=40_000, ctf_count=16,
-                    ctb_retain=3)
+                    ctb_retain=3, bitmap_edge=edge)
     pipe, blocks, mbr = _ingest(cfg, tc, 15, 3)
     try:
         rng = np.random.default_rng(1)

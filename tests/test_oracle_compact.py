@@ -25,7 +25,8 @@ def _pin():
     for i in range(m):
         p = f"in{i}_"
         info = StcCtbInfo()
-        ctypes.memmove(ctypes.byref(info), z[p + "info"].tobytes(), ctypes.sizeof(info))
+        raw = z[p + "info"].tobytes()  # the fixture predates the info's bitmap_edge (0 reads as 256)
+        ctypes.memmove(ctypes.byref(info), raw, min(len(raw), ctypes.sizeof(info)))
         b = {"ctfs": z[p + "ctfs"], "keys": z[p + "keys"], "sids": z[p + "sids"],
              "oversize_keys": np.zeros(0, np.uint64), "oversize_boxes": np.zeros(0, np.float32),
              "oversize_bitmap": z[p + "oversize_bitmap"]}

@@ -52,6 +52,39 @@ def test_oversize_bitmap_and_times_match_reference_host_code(built):
         assert [int(starts.min()), int(starts.max())] == [int(v) for v in z[s + "_o_times"]]
 
 
+def test_map_bitmap_edge_scales_the_pinned_256(built):
+    """The map bitmap at edges 512 and 1024 (bitmap_edge; the reference fixes
+    256 at compile time) against the 256 one pinned above: the cell of a
+    coordinate at edge 256 * 2^k is 2^k times its cell at 256 plus a
+    remainder (multiplying by a power of two is exact in double), so for
+    boxes inside the map the 2^k x 2^k blocks of the larger bitmap OR
+    together into the 256 x 256 one."""
+    import oracle
+    z = np.load(PIN)
+    rng = np.random.default_rng(3)
+    checked = 0
+    for s in _sets(z):
+        mp = z[s + "_map"]
+        boxes = np.asarray(z[s + "_oboxes"], np.float32).reshape(-1, 4)
+        # fixture boxes inside the map, and random ones from points to wide boxes
+        inside = boxes[(boxes[:, 0] >= mp[0]) & (boxes[:, 1] >= mp[1]) & (boxes[:, 2] < mp[2]) & (boxes[:, 3] < mp[3])]
+        lo = rng.random((200, 2)) * 0.9
+        wh = rng.random((200, 2)) ** 4 * 0.09
+        rnd = np.concatenate([mp[0] + (mp[2] - mp[0]) * np.stack([lo[:, 0], lo[:, 0] + wh[:, 0]], 1),
+                              mp[1] + (mp[3] - mp[1]) * np.stack([lo[:, 1], lo[:, 1] + wh[:, 1]], 1)], 1)
+        rnd = rnd[:, [0, 2, 1, 3]].astype(np.float32)
+        rnd = rnd[(rnd[:, 2] < mp[2]) & (rnd[:, 3] < mp[3])]
+        for bx in (inside, rnd):
+            base = np.unpackbits(oracle.o_bitmap(bx, mp, 256), bitorder="little").reshape(256, 256)
+            for k in (1, 2):
+                e = 256 << k
+                big = np.unpackbits(oracle.o_bitmap(bx, mp, e), bitorder="little").reshape(e, e)
+                down = big.reshape(256, 1 << k, 256, 1 << k).any(axis=(1, 3))
+                assert np.array_equal(down, base.astype(bool)), (s, e)
+                checked += int(base.sum())
+    assert checked > 1000
+
+
 def test_live_reference_pin_when_available(built):
     """Re-runs the reference host code on fresh cases where its build exists."""
     import oracle
