@@ -262,16 +262,18 @@ def run_gpu(args, w, rank, local):
             pipe.step_device(dev[t].data_ptr(), t)
             checked.append(pipe.drain())
     stats = []
+    clk = ClockSampler(local).__enter__()  # sampling before the first timed step
+    time.sleep(0.2)
     barrier(args)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    with ClockSampler(local) as clk:
-        for t in range(W, W + K):
-            pipe.step_device(dev[t].data_ptr(), t)
-            stats.append(pipe.stats())
-            checked.append(pipe.drain())
-        torch.cuda.synchronize()
+    for t in range(W, W + K):
+        pipe.step_device(dev[t].data_ptr(), t)
+        stats.append(pipe.stats())
+        checked.append(pipe.drain())
+    torch.cuda.synchronize()
     wall_dev = time.perf_counter() - t0
+    clk.__exit__(None, None, None)
     checked = np.concatenate([meeting_rows(m) for m in checked])
     units = {W + i: int(s.checking_units) for i, s in enumerate(stats)}
     barrier(args)
@@ -291,15 +293,19 @@ def run_gpu(args, w, rank, local):
     d2h = 0
     barrier(args)
     torch.cuda.synchronize()
+    # the clock sampler starts and stops outside the timed region (starting
+    # nvidia-smi takes tens of milliseconds)
+    e2e_clk = ClockSampler(local).__enter__()
+    time.sleep(0.2)
     t1 = time.perf_counter()
-    with ClockSampler(local) as e2e_clk:
-        for c0 in range(0, K, win):
-            n = min(win, K - c0)
-            m = pipe.step_window(hnp.arr[c0:c0 + n], W + K + c0, out=mnp)
-            d2h += m.nbytes + 128 * n
-            e2e_stats.append(pipe.stats())
-        torch.cuda.synchronize()
+    for c0 in range(0, K, win):
+        n = min(win, K - c0)
+        m = pipe.step_window(hnp.arr[c0:c0 + n], W + K + c0, out=mnp)
+        d2h += m.nbytes + 128 * n
+        e2e_stats.append(pipe.stats())
+    torch.cuda.synchronize()
     wall_e2e = time.perf_counter() - t1
+    e2e_clk.__exit__(None, None, None)
     e2e_busy = {"window_device_ms": [round(float(s.window_device_ms), 3) for s in e2e_stats],
                 "window_input_wait_ms": [round(float(s.window_input_wait_ms), 3) for s in e2e_stats],
                 "window_wall_ms": [round(float(s.window_wall_ms), 3) for s in e2e_stats],

@@ -92,6 +92,8 @@ struct stc_ctx {
   double2 *xy_win[WIN_BUFS - 1] = {};  // a window's other input buffers (allocated on first use)
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t copy_ev[WIN_BUFS] = {};
+  cudaEvent_t sweep_ev[2] = {};    // a window step's sweep start (its next inputs' copy waits for it)
+  cudaEvent_t gate_ev = nullptr;   // recorded by issue_step before the insert and sweep, when set
   std::vector<void *> allocs;
   stc_stats stats;
   uint32_t last_t = 0;
@@ -201,6 +203,8 @@ static void destroy_all(stc_ctx *c) {
     if (c->core_ev[i]) cudaEventDestroy(c->core_ev[i]);
   }
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  for (cudaEvent_t ev : c->sweep_ev)
+    if (ev) cudaEventDestroy(ev);
   for (int i = 0; i < 2; i++) {
     if (c->drain_stage[i]) cudaFreeHost(c->drain_stage[i]);
     if (c->drain_ev[i]) cudaEventDestroy(c->drain_ev[i]);
@@ -574,6 +578,7 @@ static void issue_step(stc_ctx *c, bool events, bool append, const uint32_t *two
   }
   cudaStreamWaitEvent(s, c->hits_ev, 0);
   if (events) cudaEventRecord(c->ev[PH_REFINE], s);
+  if (c->gate_ev) cudaEventRecord(c->gate_ev, s);
   step_insert(p, s);
   if (events) cudaEventRecord(c->ev[PH_INSERT], s);
   step_sweep(p, s);
@@ -801,6 +806,8 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
     if (e == cudaSuccess && !c->copy_stream) e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
     for (int b = 0; b < WIN_BUFS && e == cudaSuccess; b++)
       if (!c->copy_ev[b]) e = cudaEventCreateWithFlags(&c->copy_ev[b], cudaEventDisableTiming);
+    for (int b = 0; b < 2 && e == cudaSuccess; b++)
+      if (!c->sweep_ev[b]) e = cudaEventCreateWithFlags(&c->sweep_ev[b], cudaEventDisableTiming);
     if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window buffers");
   }
   const bool graphs = c->cfg.window_graphs == 1 || (c->cfg.window_graphs == 0 && p.N <= (1u << 21));
@@ -814,10 +821,19 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   double wait_ms = 0;  // device time of the window's steps spent waiting for their positions
 
   // Positions of step i into buffer i % WIN_BUFS on the copy stream, once
-  // the core of step i - WIN_BUFS (the buffer's last reader) has run.
+  // the core of step i - WIN_BUFS (the buffer's last reader) has run and the
+  // step queued last (i - 2) has reached its sweep: the copy then runs beside
+  // the sweep, which streams the table with evict-first accesses, instead of
+  // beside the pair tests and table update, whose leaf data and slots it
+  // would push out of L2 (host input cost 0.4-0.6 ms a step at 10M objects
+  // that way, 0.1-0.3 ms this way).
   auto fetch = [&](uint32_t i) -> cudaError_t {
     const int b = (int)(i % WIN_BUFS);
     cudaError_t e = i >= (uint32_t)WIN_BUFS ? cudaStreamWaitEvent(c->copy_stream, c->core_ev[b], 0) : cudaSuccess;
+    // and runs beside the sweep of the step queued last (i - 2), not beside
+    // its pair tests and table update
+    if (e == cudaSuccess && i >= (uint32_t)WIN_BUFS && !graphs)
+      e = cudaStreamWaitEvent(c->copy_stream, c->sweep_ev[(i - 2) & 1], 0);
     if (e == cudaSuccess)
       e = copy_in_pieces(window_buffer(c, b), (const uint8_t *)xy + (size_t)i * step_bytes, step_bytes, kind,
                          c->copy_stream);
@@ -843,7 +859,9 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
       tl_launches += c->graph_kernels;
     } else {
       p.xy = window_buffer(c, b);
+      c->gate_ev = c->sweep_ev[par];
       issue_step(c, false, false, c->t_pinned + b);
+      c->gate_ev = nullptr;
     }
     cudaEventRecord(c->core_ev[b], s);
     launches[par] = tl_launches - l0;
