@@ -822,7 +822,8 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
 
   // Positions of step i into buffer i % WIN_BUFS on the copy stream, once
   // the core of step i - WIN_BUFS (the buffer's last reader) has run and the
-  // step queued last (i - 2) has reached its sweep: the copy then runs beside
+  // step queued last (i - 2, or step 0 for steps 1 and 2, whose copies are
+  // queued right after it) has reached its sweep: the copy then runs beside
   // the sweep, which streams the table with evict-first accesses, instead of
   // beside the pair tests and table update, whose leaf data and slots it
   // would push out of L2 (host input cost 0.4-0.6 ms a step at 10M objects
@@ -830,10 +831,10 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   auto fetch = [&](uint32_t i) -> cudaError_t {
     const int b = (int)(i % WIN_BUFS);
     cudaError_t e = i >= (uint32_t)WIN_BUFS ? cudaStreamWaitEvent(c->copy_stream, c->core_ev[b], 0) : cudaSuccess;
-    // and runs beside the sweep of the step queued last (i - 2), not beside
-    // its pair tests and table update
-    if (e == cudaSuccess && i >= (uint32_t)WIN_BUFS && !graphs)
-      e = cudaStreamWaitEvent(c->copy_stream, c->sweep_ev[(i - 2) & 1], 0);
+    // and runs beside the sweep of the step queued last (i - 2; step 0 for
+    // the window's first inputs), not beside its pair tests and table update
+    if (e == cudaSuccess && i >= 1 && !graphs)
+      e = cudaStreamWaitEvent(c->copy_stream, c->sweep_ev[(i >= 2 ? i - 2 : 0) & 1], 0);
     if (e == cudaSuccess)
       e = copy_in_pieces(window_buffer(c, b), (const uint8_t *)xy + (size_t)i * step_bytes, step_bytes, kind,
                          c->copy_stream);
