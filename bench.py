@@ -567,11 +567,12 @@ def max_over_ranks(args, v):
 
 # DRAM bytes (read + write) of the refinement phase (k_refine_a + k_hits)
 # per hit, from one ncu capture of each kernel on the 3M-object workload
-# (profiles/kernels_refine_hits_strips_uniform-3M.md): 347.7 MB for one of
-# the step's four parts, about a quarter of its 6.086M hits. The traffic
-# grows with the hits (records written and read, one table slot and two
-# positions per hit), so the 10M line scales it by its own hit count.
-REFINE_DRAM_BYTES_PER_HIT = 347.7e6 / (6.086e6 / 4)
+# (profiles/kernels_refine_hits_strips_uniform-3M.md): 388.5 MB (reads and
+# writes of both kernels) for one of the step's four parts, about a quarter
+# of its 6.086M hits. The traffic grows with the hits (32-byte records
+# written and read, one table slot per hit), so the 10M line scales it by
+# its own hit count.
+REFINE_DRAM_BYTES_PER_HIT = (54.36e6 + 33.70e6 + 264.20e6 + 36.23e6) / (6.086e6 / 4)
 
 
 def kernel_bytes(s, N, B):
