@@ -243,6 +243,17 @@ def run_gpu(args, w, rank, local):
             best = ms if best is None else min(best, ms)
         link[name + "_gbs"] = 16.0 * N / (best / 1e3) / 1e9
     link["bytes"] = 16 * N
+    # each end-to-end step's own input copy once, in order (the rate can
+    # differ across the page-locked allocation)
+    rates = []
+    for k in range(K):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        stage[0].copy_(host[k], non_blocking=True)
+        e1.record()
+        e1.synchronize()
+        rates.append(16.0 * N / (e0.elapsed_time(e1) / 1e3) / 1e9)
+    link["h2d_gbs_e2e_steps"] = {"min": min(rates), "median": float(np.median(rates)), "max": max(rates)}
     del stage
     hnp = HostSteps(host.numpy(), W + K)
     torch.cuda.synchronize()
