@@ -1,5 +1,6 @@
 """stc_step_window (each step replayed from a captured CUDA graph) against the
-plain step-by-step pipeline: uneven windows, host and device input, flushes
+plain step-by-step pipeline: uneven windows, pageable and page-locked host
+input and device input, flushes
 inside windows (the graph is captured again after each), a change of the
 slice count between windows. Meetings, statistics and every flushed block
 must be identical."""
@@ -52,16 +53,21 @@ def test_windows_match_plain_steps(built_cuda, graphs):
     from dataclasses import replace
     win = Pipeline(replace(cfg, window_graphs=graphs), mbr, tr[0])
     dev = torch.from_numpy(tr).cuda()
+    # page-locked host input (plain DMA) besides pageable host input (staged
+    # by the driver)
+    pinned = torch.from_numpy(tr).pin_memory().numpy()
     try:
         got_win = []
         t0 = 0
-        # (steps, slices, device input)
-        for w, slices, on_device in [(1, 1, False), (4, 1, True), (7, 3, False), (2, 3, True), (6, 1, False),
-                                     (4, 2, True)]:
+        # (steps, slices, input: pageable host, page-locked host, device)
+        for w, slices, src in [(1, 1, "host"), (4, 1, "device"), (7, 3, "pinned"), (2, 3, "device"), (6, 1, "host"),
+                               (4, 2, "pinned")]:
             win.set_step_slices(slices)
             out = np.empty(2_000_000, MEETING_DTYPE)
-            if on_device:
+            if src == "device":
                 got = win.step_window((dev[t0].data_ptr(), w), t0, out)
+            elif src == "pinned":
+                got = win.step_window(pinned[t0:t0 + w], t0, out)
             else:
                 got = win.step_window(tr[t0:t0 + w], t0, out)
             got_win.append(got.copy())
