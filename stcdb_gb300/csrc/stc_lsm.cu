@@ -70,7 +70,7 @@ __global__ void k_lsm_append(const stc_meeting *emit, unsigned long long E, LsmD
 #pragma unroll
     for (int k = 0; k < 2; k++) {
       uint32_t pid = k ? m.pid_hi : m.pid_lo;
-      if (atomicAdd(&L.cnt[pid], 1u) == 0u) atomicAdd(&st->lsm_sid_count, 1u);
+      atomicAdd(&L.cnt[pid], 1u);  // objects with keys are counted at the flush
       atomicMin(&L.obox[pid].x, lo0);
       atomicMax(&L.obox[pid].z, hi0);
       atomicMin(&L.obox[pid].y, lo1);
@@ -101,6 +101,10 @@ __global__ void k_lsm_set_counts(unsigned long long *n_dev, unsigned long long a
 // high x, y from the high y taken twice, as the reference does).
 __global__ void k_lsm_set_oid(LsmDev L) {
   uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+  // objects with at least one key (the reference counts them as their first
+  // key arrives; counted here once instead of at every append)
+  const unsigned has = __ballot_sync(0xffffffffu, id < L.N && L.cnt[id] >= 1u);
+  if ((threadIdx.x & 31u) == 0 && has) atomicAdd(&L.st->lsm_sid_count, (uint32_t)__popc(has));
   if (id >= L.N) return;
   uint32_t mx = 0, my = 0;
   if (L.cnt[id] >= 1u) {
