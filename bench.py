@@ -202,36 +202,6 @@ class HostSteps:
         return self.arr[t - self.first]
 
 
-def host_steps_buffer(shape):
-    """Page-locked host memory for the end-to-end and serving inputs:
-    anonymous memory advised for transparent huge pages and registered with
-    cudaHostRegister (fewer, larger pages for the copy engines to translate
-    than the pinned allocator's; measured 0.03-0.07 ms a step faster at 10M
-    objects), or the pinned allocator where that is not available. Returns
-    (torch tensor, how it was allocated)."""
-    import ctypes
-    import torch
-    nbytes = int(np.prod(shape)) * 8
-    try:
-        libc = ctypes.CDLL(None, use_errno=True)
-        libc.mmap.restype = ctypes.c_void_p
-        libc.mmap.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                              ctypes.c_long]
-        libc.madvise.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
-        # PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS (Linux)
-        addr = libc.mmap(None, nbytes, 0x3, 0x22, -1, 0)
-        if not addr or addr == ctypes.c_void_p(-1).value:
-            raise OSError("mmap failed")
-        libc.madvise(addr, nbytes, 14)  # MADV_HUGEPAGE; advisory
-        arr = np.ctypeslib.as_array((ctypes.c_double * (nbytes // 8)).from_address(addr)).reshape(shape)
-        arr.fill(0.0)  # back the pages before they are registered
-        if int(torch.cuda.cudart().cudaHostRegister(addr, nbytes, 0)) != 0:
-            raise OSError("cudaHostRegister failed")
-        return torch.from_numpy(arr), "anonymous memory advised for huge pages, cudaHostRegister"
-    except Exception:
-        return torch.empty(shape, dtype=torch.float64, pin_memory=True), "torch pinned allocator"
-
-
 def run_gpu(args, w, rank, local):
     import torch
     from stcdb_gb300.pipeline import Pipeline
@@ -250,7 +220,7 @@ def run_gpu(args, w, rank, local):
     gen.next_into(dev.data_ptr(), W + K)
     gen_ms = gen.last_ms
     S = args.serve_steps if args.serve_steps > 0 else 2 * K
-    host, host_alloc = host_steps_buffer((K + S, N, 2))
+    host = torch.empty((K + S, N, 2), dtype=torch.float64, pin_memory=True)
     stage = torch.empty((K, N, 2), dtype=torch.float64, device=f"cuda:{local}")
     for lo in range(0, K + S, K):
         n = min(K, K + S - lo)
@@ -273,7 +243,6 @@ def run_gpu(args, w, rank, local):
             best = ms if best is None else min(best, ms)
         link[name + "_gbs"] = 16.0 * N / (best / 1e3) / 1e9
     link["bytes"] = 16 * N
-    link["host_buffer"] = host_alloc
     # each end-to-end step's own input copy once, in order (the rate can
     # differ across the page-locked allocation)
     rates = []
