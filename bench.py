@@ -36,6 +36,9 @@ queries_under_ingest: 2K more steps (host input, pipelined windows of 4
   (default 20,000/s) over the flushed block by continuous batching: 60%
   object queries returning their contacts, 40% box queries returning match
   counts, as the reference's searches do; p50/p99 latency from arrival.
+queries_under_ingest_hbm_input: the same for 2K further steps whose
+  positions are already in HBM (as for `value`), over the two blocks flushed
+  by then: the serving's own cost to ingest, without the host link's.
 batched: 64 uneven ingest windows (100k-2M objects log-uniform, a tenth of
   the batching configuration's 1M-20M, which --batched-full runs; 10-50
   steps, reach 5/10/20 m, 0-90% hotspot, lowered where the table would not fit) run
@@ -226,6 +229,12 @@ def run_gpu(args, w, rank, local):
         n = min(K, K + S - lo)
         gen.next_into(stage.data_ptr(), n)
         host[lo:lo + n].copy_(stage[:n])
+    # S more steps kept in HBM: the second serving run ingests them without
+    # the host link
+    dev_serve = None
+    if args.query_rate > 0:
+        dev_serve = torch.empty((S, N, 2), dtype=torch.float64, device=f"cuda:{local}")
+        gen.next_into(dev_serve.data_ptr(), S)
     gen.close()
     # the host link's copy rates for one step's positions (page-locked host
     # memory, CUDA events, best of three): the end-to-end rate cannot beat
@@ -334,15 +343,20 @@ def run_gpu(args, w, rank, local):
                  ctfs=int(info.ctf_count), steps=W + 2 * K)
     # queries under ingest: K more steps while a serving thread answers a
     # Poisson query stream over the flushed block
-    queries = None
+    queries = queries_hbm = None
     if args.query_rate > 0:
-        queries = serve_under_ingest(args, pipe, hnp, W + 2 * K, S, N, mbr, mnp,
-                                     dev if args.serve_device_input else None)
-    # compaction: the serving steps' keys become a second block; both merge
-    # into one block of split x split CTFs (100 CTFs, as a flush makes)
+        queries = serve_under_ingest(args, pipe, hnp, W + 2 * K, S, N, mbr, mnp)
+        # the same with the ingest's positions already in HBM (the input
+        # `value` is measured with), over the two blocks flushed by then
+        pipe.flush()
+        queries_hbm = serve_under_ingest(args, pipe, hnp, W + 2 * K + S, S, N, mbr, mnp, dev_serve)
+        del dev_serve
+    # compaction: the first serving run's keys are the second block; the
+    # first two blocks merge into one block of split x split CTFs (100 CTFs,
+    # as a flush makes)
     compaction = None
     if pipe.flush():
-        b0, b1 = pipe.block_info(info.index), pipe.ctb_info()
+        b0, b1 = pipe.block_info(info.index), pipe.block_info(info.index + 1)
         keys_in = int(b0.kv_count) + int(b1.kv_count)
         new, cms = pipe.compact(int(info.index), 2, 10)
         out = pipe.block_info(new)
@@ -351,7 +365,8 @@ def run_gpu(args, w, rank, local):
     pipe.close()
     return dict(stats=stats, dev_ms=dev_ms, wall_dev=wall_dev, wall_e2e=wall_e2e, e2e_stats=e2e_stats, link=link,
                 e2e_busy=e2e_busy,
-                d2h=d2h, clocks=clk.summary(), flush=flush, queries=queries, trace_gen=trace_gen,
+                d2h=d2h, clocks=clk.summary(), flush=flush, queries=queries, queries_hbm=queries_hbm,
+                trace_gen=trace_gen,
                 compaction=compaction, bit_exact=bit_exact_check(args.workload, rank, checked, units, W + K))
 
 
@@ -484,8 +499,7 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None, dev_steps=
     for w0t in range(t0, t0 + steps, SERVE_WINDOW):
         n = min(SERVE_WINDOW, t0 + steps - w0t)
         if dev_steps is not None:  # positions already in HBM (no host link traffic)
-            k = (w0t - t0) % (dev_steps.shape[0] - SERVE_WINDOW + 1)
-            pipe.step_window((dev_steps[k].data_ptr(), n), w0t, out=mout)
+            pipe.step_window((dev_steps[w0t - t0].data_ptr(), n), w0t, out=mout)
         else:
             pipe.step_window(hnp.arr[w0t - hnp.first:w0t - hnp.first + n], w0t, out=mout)
         ws = pipe.stats()
@@ -553,7 +567,8 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None, dev_steps=
                        "slowest_batch_gpu_ms": sst.slowest_batch_gpu_us / 1e3},
             "mix": "60% object queries returning contacts (meets-whom, window 10-10000 steps), 40% box "
                    "queries returning match counts (50 m-5 km, window 10-3600 steps)",
-            "blocks": 1, "step_slices": args.serve_slices, "ingest_window_steps": SERVE_WINDOW,
+            "blocks": int(pipe.stats().flushes), "input": "HBM" if dev_steps is not None else "host (page-locked)",
+            "step_slices": args.serve_slices, "ingest_window_steps": SERVE_WINDOW,
             "ingest_pos_updates_per_s": N * steps / wall,
             "ingest_device_ms_per_step": float(np.mean(step_ms)),
             "ingest_window_device_ms_per_step": sum(d for d, _, _ in win_ms) / max(sum(n for _, _, n in win_ms), 1),
@@ -883,9 +898,6 @@ def main():
                     help="launches per long step kernel (stc_config.step_slices; 0 = 1)")
     ap.add_argument("--serve-steps", type=int, default=0,
                     help="ingest steps of the serving phase (0 = twice --steps)")
-    ap.add_argument("--serve-device-input", action="store_true",
-                    help="serving-phase ingest from positions in HBM (the run's device steps again) "
-                         "instead of host input")
     ap.add_argument("--serve-slices", type=int, default=1,
                     help="step slices while the serving phase answers queries (stc_set_step_slices)")
     args = ap.parse_args()
@@ -966,6 +978,7 @@ def main():
         "phase_frac_of_peak": {k: kb[k] / (phase_ms[k] / 1e3) / 1e9 / peak for k in kb if phase_ms[k] > 0},
         "flush": flush_line(r["flush"], peak),
         "queries_under_ingest": r["queries"],
+        "queries_under_ingest_hbm_input": r["queries_hbm"],
         "trace_gen": r["trace_gen"],
         "compaction": compaction_line(r["compaction"], peak),
         "sort": sort_line(local, peak),
@@ -989,6 +1002,9 @@ def main():
                        "query_p50_ms": q.get("p50_ms"), "query_p99_ms": q.get("p99_ms"),
                        "query_max_ms": q.get("max_ms"), "queries_per_s": q.get("qps"),
                        "ingest_pos_updates_per_s_while_serving": q.get("ingest_pos_updates_per_s"),
+                       "ingest_pos_updates_per_s_while_serving_hbm_input":
+                           (r["queries_hbm"] or {}).get("ingest_pos_updates_per_s"),
+                       "query_p99_ms_hbm_input": (r["queries_hbm"] or {}).get("p99_ms"),
                        "roofline_frac": line["roofline"]["frac"]}
     print(json.dumps(line), flush=True)
 
