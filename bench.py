@@ -328,6 +328,7 @@ def run_gpu(args, w, rank, local):
     e2e_clk.__exit__(None, None, None)
     e2e_busy = {"window_device_ms": [round(float(s.window_device_ms), 3) for s in e2e_stats],
                 "window_input_wait_ms": [round(float(s.window_input_wait_ms), 3) for s in e2e_stats],
+                "window_copy_ms": [round(float(s.window_copy_ms), 3) for s in e2e_stats],
                 "window_wall_ms": [round(float(s.window_wall_ms), 3) for s in e2e_stats],
                 "clocks": e2e_clk.summary(),
                 "gpu_busy_frac": float(sum(s.window_device_ms for s in e2e_stats) /
@@ -504,7 +505,7 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None, dev_steps=
             pipe.step_window(hnp.arr[w0t - hnp.first:w0t - hnp.first + n], w0t, out=mout)
         ws = pipe.stats()
         step_ms.append(ws.step_ms)
-        win_ms.append((ws.window_device_ms, ws.window_input_wait_ms, n))
+        win_ms.append((ws.window_device_ms, ws.window_input_wait_ms, n, ws.window_copy_ms))
         cur_t[0] = w0t + n - 1
     wall = time.perf_counter() - w0
     done.set()
@@ -571,8 +572,9 @@ def serve_under_ingest(args, pipe, hnp, t0, steps, N, mbr, mout=None, dev_steps=
             "step_slices": args.serve_slices, "ingest_window_steps": SERVE_WINDOW,
             "ingest_pos_updates_per_s": N * steps / wall,
             "ingest_device_ms_per_step": float(np.mean(step_ms)),
-            "ingest_window_device_ms_per_step": sum(d for d, _, _ in win_ms) / max(sum(n for _, _, n in win_ms), 1),
-            "ingest_input_wait_ms_per_step": sum(w for _, w, _ in win_ms) / max(sum(n for _, _, n in win_ms), 1)}
+            "ingest_window_device_ms_per_step": sum(x[0] for x in win_ms) / max(sum(x[2] for x in win_ms), 1),
+            "ingest_input_wait_ms_per_step": sum(x[1] for x in win_ms) / max(sum(x[2] for x in win_ms), 1),
+            "ingest_input_copy_ms_per_step": sum(x[3] for x in win_ms) / max(sum(x[2] for x in win_ms), 1)}
 
 
 def barrier(args):

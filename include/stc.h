@@ -160,6 +160,7 @@ typedef struct stc_stats {
   float window_device_ms;
   float window_wall_ms;
   float window_input_wait_ms;
+  float window_copy_ms;          /* the window's input copies, start to end (each beside a step) */
 } stc_stats;
 
 /* Fills *cfg with the reference defaults for n objects (util/config.h:29-41,

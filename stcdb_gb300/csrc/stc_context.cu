@@ -92,6 +92,10 @@ struct stc_ctx {
   double2 *xy_win[WIN_BUFS - 1] = {};  // a window's other input buffers (allocated on first use)
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t copy_ev[WIN_BUFS] = {};
+  // start and end of each input copy (its duration in the window's
+  // statistics), a ring of twice WIN_BUFS so that step i's are read before
+  // step i + 2 * WIN_BUFS records them again
+  cudaEvent_t copy_t0[2 * WIN_BUFS] = {}, copy_t1[2 * WIN_BUFS] = {};
   cudaEvent_t sweep_ev[2] = {};    // a window step's sweep start (its next inputs' copy waits for it)
   cudaEvent_t gate_ev = nullptr;   // recorded by issue_step before the insert and sweep, when set
   std::vector<void *> allocs;
@@ -205,6 +209,10 @@ static void destroy_all(stc_ctx *c) {
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   for (cudaEvent_t ev : c->sweep_ev)
     if (ev) cudaEventDestroy(ev);
+  for (int i = 0; i < 2 * WIN_BUFS; i++) {
+    if (c->copy_t0[i]) cudaEventDestroy(c->copy_t0[i]);
+    if (c->copy_t1[i]) cudaEventDestroy(c->copy_t1[i]);
+  }
   for (int i = 0; i < 2; i++) {
     if (c->drain_stage[i]) cudaFreeHost(c->drain_stage[i]);
     if (c->drain_ev[i]) cudaEventDestroy(c->drain_ev[i]);
@@ -806,6 +814,10 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
     if (e == cudaSuccess && !c->copy_stream) e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
     for (int b = 0; b < WIN_BUFS && e == cudaSuccess; b++)
       if (!c->copy_ev[b]) e = cudaEventCreateWithFlags(&c->copy_ev[b], cudaEventDisableTiming);
+    for (int b = 0; b < 2 * WIN_BUFS && e == cudaSuccess; b++) {
+      if (!c->copy_t0[b]) e = cudaEventCreate(&c->copy_t0[b]);
+      if (e == cudaSuccess && !c->copy_t1[b]) e = cudaEventCreate(&c->copy_t1[b]);
+    }
     for (int b = 0; b < 2 && e == cudaSuccess; b++)
       if (!c->sweep_ev[b]) e = cudaEventCreateWithFlags(&c->sweep_ev[b], cudaEventDisableTiming);
     if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window buffers");
@@ -819,6 +831,7 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   }
   unsigned long long launches[2] = {0, 0};
   double wait_ms = 0;  // device time of the window's steps spent waiting for their positions
+  double copy_ms = 0;  // durations of the steps' input copies
 
   // Positions of step i into buffer i % WIN_BUFS on the copy stream, once
   // the core of step i - WIN_BUFS (the buffer's last reader) has run and the
@@ -835,9 +848,11 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
     // the window's first inputs), not beside its pair tests and table update
     if (e == cudaSuccess && i >= 1 && !graphs)
       e = cudaStreamWaitEvent(c->copy_stream, c->sweep_ev[(i >= 2 ? i - 2 : 0) & 1], 0);
+    if (e == cudaSuccess) e = cudaEventRecord(c->copy_t0[i % (2 * WIN_BUFS)], c->copy_stream);
     if (e == cudaSuccess)
       e = copy_in_pieces(window_buffer(c, b), (const uint8_t *)xy + (size_t)i * step_bytes, step_bytes, kind,
                          c->copy_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c->copy_t1[i % (2 * WIN_BUFS)], c->copy_stream);
     return e == cudaSuccess ? cudaEventRecord(c->copy_ev[b], c->copy_stream) : e;
   };
   // (per step: events and state copy by parity i & 1, input buffer, its
@@ -897,6 +912,11 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
     cudaEventElapsedTime(&app, c->wev[b][1], c->wev[b][2]);
     cudaEventElapsedTime(&wait, c->wev[b][0], c->wev[b][3]);
     wait_ms += wait;
+    // step i's copy ended before its core began, which has run
+    float cp = 0;
+    if (cudaEventElapsedTime(&cp, c->copy_t0[i % (2 * WIN_BUFS)], c->copy_t1[i % (2 * WIN_BUFS)]) == cudaSuccess)
+      copy_ms += cp;
+    cudaGetLastError();
     float phase[8] = {0, 0, 0, 0, 0, 0, 0, app};
     fill_stats(c, t0 + i, phase, core + app, (uint32_t)launches[b]);
     return STC_OK;
@@ -1019,6 +1039,7 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   grow_hits(c, most_hits);
   c->stats.window_device_ms = (float)busy_ms;
   c->stats.window_input_wait_ms = (float)wait_ms;
+  c->stats.window_copy_ms = (float)copy_ms;
   c->stats.window_wall_ms =
       (float)std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
   return STC_OK;

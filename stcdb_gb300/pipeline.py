@@ -95,6 +95,7 @@ class StcStats(ctypes.Structure):
         ("window_device_ms", ctypes.c_float),
         ("window_wall_ms", ctypes.c_float),
         ("window_input_wait_ms", ctypes.c_float),
+        ("window_copy_ms", ctypes.c_float),
     ]
 
     def as_dict(self) -> dict:
