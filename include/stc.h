@@ -209,9 +209,12 @@ stc_status stc_autotune(const stc_config *cfg, const double mbr[4], const double
 /* Processes a window of `steps` consecutive steps t0, t0 + 1, ...: xy holds
  * steps x num_objects (lon, lat) f64 pairs, layout [step][oid], in host
  * memory (on_device 0) or device memory (on_device 1). Each step's positions
- * are copied in as soon as the step three before it has run (three input
- * buffers), and the window is pipelined one step deep: step i + 1 is queued on the GPU before the host reads step i's
- * state, so the GPU does not wait for the host between steps. The memtable
+ * are copied into one of three input buffers once the step three before it
+ * has run, beside the sweep of the step queued before it (page-locked host
+ * memory is copied by DMA; pageable memory is staged by the driver), and the
+ * window is pipelined one step deep: step i + 1 is queued on the GPU before
+ * the host reads step i's state, so the GPU does not wait for the host
+ * between steps. The memtable
  * append of step i + 1 is queued only after step i's flush decision (a flush
  * runs behind the next step's core, which never touches the memtable), so
  * results equal those of stc_step called step by step, flushes included.
