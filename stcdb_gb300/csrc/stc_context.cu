@@ -841,7 +841,12 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   // beside the pair tests and table update, whose leaf data and slots it
   // would push out of L2 (host input cost 0.4-0.6 ms a step at 10M objects
   // that way, 0.1-0.3 ms this way).
+  // Device input without graphs is read where it lies (as stc_step_device
+  // reads it): no copy beside the steps (a 160 MB device-to-device copy took
+  // 1.5 ms beside a 10M-object step against 0.05 ms alone).
+  const bool direct = on_device && !graphs;
   auto fetch = [&](uint32_t i) -> cudaError_t {
+    if (direct) return cudaSuccess;
     const int b = (int)(i % WIN_BUFS);
     cudaError_t e = i >= (uint32_t)WIN_BUFS ? cudaStreamWaitEvent(c->copy_stream, c->core_ev[b], 0) : cudaSuccess;
     // and runs beside the sweep of the step queued last (i - 2; step 0 for
@@ -862,7 +867,7 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
     c->t_pinned[b] = t0 + i;  // step i - WIN_BUFS, the word's last reader, has been waited for
     const unsigned long long l0 = tl_launches;
     cudaEventRecord(c->wev[par][0], s);
-    cudaError_t e = cudaStreamWaitEvent(s, c->copy_ev[b], 0);
+    cudaError_t e = direct ? cudaSuccess : cudaStreamWaitEvent(s, c->copy_ev[b], 0);
     if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window copy-in");
     cudaEventRecord(c->wev[par][3], s);
     if (graphs) {
@@ -874,7 +879,7 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
       if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window");
       tl_launches += c->graph_kernels;
     } else {
-      p.xy = window_buffer(c, b);
+      p.xy = direct ? (const double2 *)((const uint8_t *)xy + (size_t)i * step_bytes) : window_buffer(c, b);
       c->gate_ev = c->sweep_ev[par];
       issue_step(c, false, false, c->t_pinned + b);
       c->gate_ev = nullptr;
@@ -914,7 +919,8 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
     wait_ms += wait;
     // step i's copy ended before its core began, which has run
     float cp = 0;
-    if (cudaEventElapsedTime(&cp, c->copy_t0[i % (2 * WIN_BUFS)], c->copy_t1[i % (2 * WIN_BUFS)]) == cudaSuccess)
+    if (!direct &&
+        cudaEventElapsedTime(&cp, c->copy_t0[i % (2 * WIN_BUFS)], c->copy_t1[i % (2 * WIN_BUFS)]) == cudaSuccess)
       copy_ms += cp;
     cudaGetLastError();
     float phase[8] = {0, 0, 0, 0, 0, 0, 0, app};
