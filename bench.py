@@ -95,6 +95,11 @@ WORKLOADS = {
     "stress-1M": dict(objects=1_000_000, hot=200, hot_frac=0.9, sigma_m=150.0, reach=20.0, min_meet=3,
                       grid_capacity=200, amplify=32.0, buckets=1 << 30, kv_restriction=1 << 27,
                       emit_per_object=128, bitmap_edge=512),
+    # the same with blocks of 2^28 keys, four of which (about 2^30 keys, the
+    # stress configuration's largest runs) are compacted at the end
+    "stress-1M-lsm": dict(objects=1_000_000, hot=200, hot_frac=0.9, sigma_m=150.0, reach=20.0, min_meet=3,
+                          grid_capacity=200, amplify=32.0, buckets=1 << 30, kv_restriction=1 << 28,
+                          emit_per_object=128, bitmap_edge=512, compact_blocks=4),
     "uniform-3M": dict(objects=3_000_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
                        buckets=1 << 26, kv_restriction=1 << 25),
     "uniform-100k": dict(objects=100_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
@@ -352,17 +357,22 @@ def run_gpu(args, w, rank, local):
         pipe.flush()
         queries_hbm = serve_under_ingest(args, pipe, hnp, W + 2 * K + S, S, N, mbr, mnp, dev_serve)
         del dev_serve
-    # compaction: the first serving run's keys are the second block; the
-    # first two blocks merge into one block of split x split CTFs (100 CTFs,
-    # as a flush makes)
+    # compaction: the last `compact_blocks` (2) blocks flushed merge into one
+    # block of split x split CTFs (100 CTFs, as a flush makes)
     compaction = None
-    if pipe.flush():
-        b0, b1 = pipe.block_info(info.index), pipe.block_info(info.index + 1)
-        keys_in = int(b0.kv_count) + int(b1.kv_count)
-        new, cms = pipe.compact(int(info.index), 2, 10)
-        out = pipe.block_info(new)
-        compaction = dict(blocks=2, keys=keys_in, split=10, ms=cms, keys_per_s=keys_in / (cms / 1e3),
-                          out_ctf_keys=int(out.ctf_kv_count), out_oversize_keys=int(out.oversize_kv_count))
+    pipe.flush()
+    m = w.get("compact_blocks", 2)
+    last = int(pipe.stats().flushes) - 1  # no block merged yet: block i is the i-th flush
+    if last + 1 >= m:
+        first = last - m + 1
+        keys_in = sum(int(pipe.block_info(first + j).kv_count) for j in range(m))
+        try:
+            new, cms = pipe.compact(first, m, 10)
+            out = pipe.block_info(new)
+            compaction = dict(blocks=m, keys=keys_in, split=10, ms=cms, keys_per_s=keys_in / (cms / 1e3),
+                              out_ctf_keys=int(out.ctf_kv_count), out_oversize_keys=int(out.oversize_kv_count))
+        except Exception as e:  # noqa: BLE001 - e.g. no room for the merge; reported in the line
+            compaction = dict(blocks=m, keys=keys_in, error=str(e))
     pipe.close()
     return dict(stats=stats, dev_ms=dev_ms, wall_dev=wall_dev, wall_e2e=wall_e2e, e2e_stats=e2e_stats, link=link,
                 e2e_busy=e2e_busy,
@@ -848,8 +858,8 @@ def tune_line(device, steps=8):
 def compaction_line(c, peak):
     """Merge throughput; algorithmic bytes 2 x 32 per merged key (read and
     write each key and its box once)."""
-    if not c:
-        return None
+    if not c or "error" in c:
+        return c
     b = 64.0 * c["keys"]
     c = dict(c)
     c.update(algorithmic_bytes=b, achieved_gbs=b / (c["ms"] / 1e3) / 1e9,
