@@ -106,9 +106,11 @@ typedef struct stc_config {
   uint32_t refine_blocks_per_sm; /* pair-test blocks launched per SM; 0 = 8, at most 32 */
   uint32_t hits_blocks_per_sm;   /* table-update blocks launched per SM; 0 = 16, at most 64 */
   uint32_t window_graphs;        /* stc_step_window replays each step from a captured CUDA graph:
-                                    0 = when num_objects <= 2^21 (where per-kernel launch costs
-                                    show; a replayed graph ran a 10M-object step 10% slower than
-                                    direct launches), 1 = always, 2 = never */
+                                    0 = automatic: when the context's last step took under 1.5 ms
+                                    of device time (up to 2^21 objects), or, before any step, up to
+                                    2^18 objects (graphs save launch costs on short steps; a
+                                    replayed graph ran long steps up to 10% slower than direct
+                                    launches); 1 = always, 2 = never */
   uint32_t bitmap_edge;          /* edge of a block's map bitmap, the oversize buffer's spatial
                                     bitmap over the map box (DEFAULT_bitmap_edge, util/util.h:47,
                                     a compile-time 256 in the reference): bitmap_edge^2 bits;

@@ -822,7 +822,14 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
       if (!c->sweep_ev[b]) e = cudaEventCreateWithFlags(&c->sweep_ev[b], cudaEventDisableTiming);
     if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window buffers");
   }
-  const bool graphs = c->cfg.window_graphs == 1 || (c->cfg.window_graphs == 0 && p.N <= (1u << 21));
+  // Automatic choice: graphs where launch costs show, i.e. for short steps.
+  // The last step's device time decides when there is one (graphs below
+  // 1.5 ms); a fresh context goes by its object count (2^18 or fewer). A
+  // replayed graph ran long steps slower than direct launches (10M objects:
+  // 15.75 against 14.33 ms; dense windows of 0.3-2M objects up to 14%).
+  const float last_ms = c->stats.step_ms;
+  const bool graphs_auto = last_ms > 0.f ? (last_ms < 1.5f && p.N <= (1u << 21)) : p.N <= (1u << 18);
+  const bool graphs = c->cfg.window_graphs == 1 || (c->cfg.window_graphs == 0 && graphs_auto);
   bool pinned_out = false;
   if (out && cap) {
     cudaPointerAttributes pa;

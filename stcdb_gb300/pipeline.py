@@ -230,7 +230,7 @@ class StcConfig:
     job_chunk: int = 0        # refinement launch shape (results do not depend on it); 0 = 8
     refine_blocks_per_sm: int = 0  # 0 = 8
     hits_blocks_per_sm: int = 0    # 0 = 16
-    window_graphs: int = 0    # step_window replays a captured graph: 0 = up to 2^21 objects, 1 = always, 2 = never
+    window_graphs: int = 0    # step_window replays captured graphs: 0 = for short steps (automatic), 1 = always, 2 = never
     bitmap_edge: int = 0      # edge of a block's map bitmap (oversize buffer); 0 = 256
 
     def resolved(self) -> "StcConfig":
