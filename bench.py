@@ -100,6 +100,11 @@ WORKLOADS = {
     "stress-1M-lsm": dict(objects=1_000_000, hot=200, hot_frac=0.9, sigma_m=150.0, reach=20.0, min_meet=3,
                           grid_capacity=200, amplify=32.0, buckets=1 << 30, kv_restriction=1 << 28,
                           emit_per_object=128, bitmap_edge=512, compact_blocks=4),
+    # the hotspot model at the headline's 10M objects: about 2.2e9 live pairs
+    # a step (2^32 table slots, 137 GB; hit buffer of 2.5e9 records, 80 GB);
+    # the memtable stays off to leave room (no flush, no queries)
+    "hotspot-10M": dict(objects=10_000_000, hot=1000, reach=10.0, min_meet=5, grid_capacity=200, amplify=8.0,
+                        buckets=1 << 32, kv_restriction=0, emit_per_object=16, hit_capacity=2_500_000_000),
     "uniform-3M": dict(objects=3_000_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
                        buckets=1 << 26, kv_restriction=1 << 25),
     "uniform-100k": dict(objects=100_000, hot=0, reach=10.0, min_meet=5, grid_capacity=200, amplify=2.0,
@@ -130,7 +135,7 @@ def make_cfg(w, device=0, step_slices=0):
                      device=device, kv_restriction=w["kv_restriction"], step_slices=step_slices,
                      emit_capacity=w.get("emit_per_object", 0) * w["objects"],
                      refine_blocks_per_sm=w.get("refine_bps", 0), hits_blocks_per_sm=w.get("hits_bps", 0),
-                     bitmap_edge=w.get("bitmap_edge", 0))
+                     bitmap_edge=w.get("bitmap_edge", 0), hit_capacity=w.get("hit_capacity", 0))
 
 
 class ClockSampler:
@@ -237,7 +242,7 @@ def run_gpu(args, w, rank, local):
     # S more steps kept in HBM: the second serving run ingests them without
     # the host link
     dev_serve = None
-    if args.query_rate > 0:
+    if args.query_rate > 0 and w["kv_restriction"]:
         dev_serve = torch.empty((S, N, 2), dtype=torch.float64, device=f"cuda:{local}")
         gen.next_into(dev_serve.data_ptr(), S)
     gen.close()
@@ -340,17 +345,20 @@ def run_gpu(args, w, rank, local):
                                        max(sum(s.window_wall_ms for s in e2e_stats), 1e-9)),
                 "host_load_avg": list(os.getloadavg()), "host_cpus": os.cpu_count()}
     # one flush of everything the memtable gathered (W + 2K steps)
-    keys = pipe.stats().memtable_keys
-    pipe.flush()
-    fs = pipe.stats()
-    info = pipe.ctb_info()
-    flush = dict(keys=int(keys), ms=float(fs.flush_ms), ctf_keys=int(info.ctf_kv_count),
-                 oversize_keys=int(info.oversize_kv_count), key_bytes=int(info.key_bytes),
-                 ctfs=int(info.ctf_count), steps=W + 2 * K)
+    lsm = bool(w["kv_restriction"])  # a workload may run without the memtable (and its queries)
+    flush = None
+    if lsm:
+        keys = pipe.stats().memtable_keys
+        pipe.flush()
+        fs = pipe.stats()
+        info = pipe.ctb_info()
+        flush = dict(keys=int(keys), ms=float(fs.flush_ms), ctf_keys=int(info.ctf_kv_count),
+                     oversize_keys=int(info.oversize_kv_count), key_bytes=int(info.key_bytes),
+                     ctfs=int(info.ctf_count), steps=W + 2 * K)
     # queries under ingest: K more steps while a serving thread answers a
     # Poisson query stream over the flushed block
     queries = queries_hbm = None
-    if args.query_rate > 0:
+    if args.query_rate > 0 and lsm:
         queries = serve_under_ingest(args, pipe, hnp, W + 2 * K, S, N, mbr, mnp)
         # the same with the ingest's positions already in HBM (the input
         # `value` is measured with), over the two blocks flushed by then
@@ -360,10 +368,11 @@ def run_gpu(args, w, rank, local):
     # compaction: the last `compact_blocks` (2) blocks flushed merge into one
     # block of split x split CTFs (100 CTFs, as a flush makes)
     compaction = None
-    pipe.flush()
+    if lsm:
+        pipe.flush()
     m = w.get("compact_blocks", 2)
     last = int(pipe.stats().flushes) - 1  # no block merged yet: block i is the i-th flush
-    if last + 1 >= m:
+    if lsm and last + 1 >= m:
         first = last - m + 1
         keys_in = sum(int(pipe.block_info(first + j).kv_count) for j in range(m))
         try:
@@ -626,8 +635,8 @@ def kernel_bytes(s, N, B):
 def flush_line(f, peak):
     """One memtable flush: algorithmic bytes 64 per key (key + box read and
     written once) plus the packed keys and the bitmap slots written."""
-    if not f["keys"]:
-        return dict(f)
+    if not f or not f["keys"]:
+        return dict(f) if f else None
     ab = 64.0 * f["keys"] + f["key_bytes"] + 8192.0 * (f["ctfs"] + 1)
     gbs = ab / (f["ms"] / 1e3) / 1e9
     return dict(f, keys_per_s=f["keys"] / (f["ms"] / 1e3), algorithmic_bytes=ab, achieved_gbs=gbs,
@@ -931,8 +940,9 @@ def main():
                     "launch_shape": {"refine_blocks_per_sm": w.get("refine_bps", 8),
                                      "hits_blocks_per_sm": w.get("hits_bps", 16)},
                     "meeting_buckets": make_cfg(w).resolved().num_meeting_buckets,
-                    "memtable": f"on, flush past {w['kv_restriction']} directed keys, 100 CTFs, "
-                                f"{w.get('bitmap_edge', 256)}x{w.get('bitmap_edge', 256)} map bitmaps",
+                    "memtable": (f"on, flush past {w['kv_restriction']} directed keys, 100 CTFs, "
+                                 f"{w.get('bitmap_edge', 256)}x{w.get('bitmap_edge', 256)} map bitmaps"
+                                 if w["kv_restriction"] else "off"),
                     "l2": "inputs and table larger than L2; no flush", "parallelism": f"replicas x{ws}"}
 
     if args.impl == "reference":
