@@ -120,6 +120,11 @@ typedef struct stc_config {
 /* Replay quadtree splits/merges on one device thread only (tests compare it
  * with the default parallel replay). */
 #define STC_FLAG_SERIAL_SCHEMA 1u
+/* How the pair tests hand over their hits (results do not depend on it; by
+ * default the library picks by the last step's hits per checking unit):
+ * straight to the hit buffer, or through a per-warp queue. Tests force each. */
+#define STC_FLAG_DIRECT_HITS 2u
+#define STC_FLAG_QUEUED_HITS 4u
 
 /* One finished meeting. pid_lo < pid_hi; start/end are the first and last
  * step in which the pair was within reach; mbr is the float bounding box of

@@ -29,6 +29,7 @@ struct PipeDev {
   int mbr_filter;
   uint32_t slices;                 // launches per long step kernel (stc_config.step_slices)
   uint32_t job_chunk;              // refinement jobs a warp takes at a time (stc_config.job_chunk)
+  uint32_t direct_hits;            // pair tests write hit records directly (dense steps), not via a queue
   uint32_t refine_bps, hits_bps;   // blocks per SM of the pair tests and of the table update
   // state
   DevState *st;

@@ -168,6 +168,30 @@ __device__ __forceinline__ void flush_queue(const PipeDev &p, HitRec *q, uint32_
   __syncwarp();
 }
 
+// Direct emission: the round's records (one per lane with has set; hm =
+// the ballot of has) go straight to the hit buffer at consecutive positions
+// of the warp's window, a new window of HIT_CHUNK reserved when the round
+// does not fit; records past the buffer are processed here.
+__device__ __forceinline__ void emit_round(const PipeDev &p, const HitRec &h, bool has, uint32_t hm, uint32_t t,
+                                           HitWindow &w) {
+  const uint32_t lane = lane_id(), cnt = __popc(hm);
+  if (w.end - w.next < cnt) {
+    for (unsigned long long i = w.next + lane; i < w.end; i += 32)
+      if (i < p.hit_cap) p.hits[i].a = STC_NONE;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&p.st->hit_count, (unsigned long long)HIT_CHUNK);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    w.next = base;
+    w.end = base + HIT_CHUNK;
+  }
+  if (has) {
+    const unsigned long long pos = w.next + __popc(hm & ((1u << lane) - 1u));
+    if (pos < p.hit_cap) p.hits[pos] = h;
+    else process_hit(p, h, t);
+  }
+  w.next += cnt;
+}
+
 __device__ __forceinline__ HitRec load_hit(const HitRec *r) {
   // streamed once: evict-first loads keep L2 for the table and positions
   const ulonglong2 v = __ldcs((const ulonglong2 *)r);
@@ -258,6 +282,10 @@ __device__ __forceinline__ uint32_t strip_x_bound(const float4 *pts, uint32_t lo
 // the three strips beside its point). A lane's candidates come in up to
 // three contiguous segments, each read 32 at a time; hits are marked in a
 // bitmask and turned into records after each group.
+// DIRECT: records go straight to the hit buffer (emit_round) instead of
+// through the warp's shared-memory queue; it pays where rows have many hits
+// (dense leaves) and costs registers elsewhere.
+template <bool DIRECT>
 __device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblock, uint32_t chunk, uint32_t n,
                          uint32_t t, Counters &ct, HitRec *q, uint32_t &qn, HitWindow &w) {
   const uint32_t lane = lane_id();
@@ -385,13 +413,13 @@ __device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblo
         const uint32_t kk = has ? (uint32_t)(__ffs(hitmask) - 1) : 0u;
         hitmask &= hitmask - 1u;
         const uint32_t hm = __ballot_sync(0xffffffffu, has);
+        HitRec h;
         if (has) {
           const uint32_t j = a + k0 + kk;
           const uint32_t cpid = __float_as_uint(__ldg(&p.spts[base + j]).w);
           const uint32_t corig = __ldg(&p.sorig[base + j]) & 0xFFFFu;
           const float2 fc = __ldg(&p.sfxy[base + j]);
           const float2 fa = pid1 < cpid ? fr : fc, fb = pid1 < cpid ? fc : fr;
-          HitRec h;
           h.a = pid1 < cpid ? pid1 : cpid;
           h.b = pid1 < cpid ? cpid : pid1;
           h.lo_x = fminf(fa.x, fb.x);
@@ -409,18 +437,22 @@ __device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblo
             for (uint32_t u2 = 0; u2 < cnb; u2++)
               if (p.bu_gid[coff + u2] == row_leaf) h.order |= DUP_BIT;
           }
-          q[qn + __popc(hm & lt_mask)] = h;
+          if (!DIRECT) q[qn + __popc(hm & lt_mask)] = h;
         }
-        qn += __popc(hm);
-        if (qn >= 32) {
-          flush_queue(p, q, 32, t, w);
-          const uint32_t rest = qn - 32;
-          HitRec mv;
-          if (lane < rest) mv = q[32 + lane];
-          __syncwarp();
-          if (lane < rest) q[lane] = mv;
-          __syncwarp();
-          qn = rest;
+        if (DIRECT) {
+          emit_round(p, h, has, hm, t, w);
+        } else {
+          qn += __popc(hm);
+          if (qn >= 32) {
+            flush_queue(p, q, 32, t, w);
+            const uint32_t rest = qn - 32;
+            HitRec mv;
+            if (lane < rest) mv = q[32 + lane];
+            __syncwarp();
+            if (lane < rest) q[lane] = mv;
+            __syncwarp();
+            qn = rest;
+          }
         }
       }
     }
@@ -429,10 +461,11 @@ __device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblo
 
 // Slice `part` of `parts` runs job chunks [C * part / parts, C * (part + 1) / parts)
 // of the C = ceil(jobs / p.job_chunk) chunks.
+template <bool DIRECT>
 __global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint32_t part, uint32_t parts) {
   const uint32_t t = p.st->step_t;
-  __shared__ HitRec queues[REFINE_THREADS / 32][QCAP];
-  HitRec *q = queues[threadIdx.x >> 5];
+  __shared__ HitRec queues[DIRECT ? 1 : REFINE_THREADS / 32][QCAP];
+  HitRec *q = queues[DIRECT ? 0 : threadIdx.x >> 5];
   uint32_t qn = 0;  // warp-uniform queue length
   HitWindow w = {0, 0};
   const unsigned long long warp = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -461,14 +494,14 @@ __global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint3
       const uint32_t n = cnt < p.leaf_cap ? cnt : p.leaf_cap;
       const uint32_t R = (n + 31) / 32, cc = p.cchunks[g], own_jobs = R * cc;
       if (local < own_jobs) {
-        run_rows(p, g, true, local / cc, local % cc, n, t, ct, q, qn, w);
+        run_rows<DIRECT>(p, g, true, local / cc, local % cc, n, t, ct, q, qn, w);
       } else {
         const uint32_t ccb = (n + REFINE_CHUNK - 1) / REFINE_CHUNK, b = local - own_jobs;
-        run_rows(p, g, false, b / ccb, b % ccb, n, t, ct, q, qn, w);
+        run_rows<DIRECT>(p, g, false, b / ccb, b % ccb, n, t, ct, q, qn, w);
       }
     }
   }
-  if (qn) flush_queue(p, q, qn, t, w);
+  if (!DIRECT && qn) flush_queue(p, q, qn, t, w);
   for (unsigned long long i = w.next + lane_id(); i < w.end; i += 32)
     if (i < p.hit_cap) p.hits[i].a = STC_NONE;
   // reduce counters per warp (64-bit sums)
@@ -497,7 +530,10 @@ __global__ void k_hit_mark(PipeDev p, uint32_t part) {
 }
 
 void step_pairs_part(PipeDev &p, uint32_t part, uint32_t parts, cudaStream_t s) {
-  STC_KL k_refine_a<<<num_sms() * p.refine_bps, REFINE_THREADS, 0, s>>>(p, part, parts);
+  if (p.direct_hits)
+    STC_KL k_refine_a<true><<<num_sms() * p.refine_bps, REFINE_THREADS, 0, s>>>(p, part, parts);
+  else
+    STC_KL k_refine_a<false><<<num_sms() * p.refine_bps, REFINE_THREADS, 0, s>>>(p, part, parts);
   STC_KL k_hit_mark<<<1, 1, 0, s>>>(p, part);
 }
 

@@ -43,6 +43,23 @@ def test_launch_shape_leaves_results_unchanged(built_cuda):
             assert np.array_equal(gm, wm), f"step {t}: meetings differ with {shape}"
 
 
+@pytest.mark.parametrize("small_hit_buffer", [False, True])
+def test_hit_emission_forms_give_the_same_results(built_cuda, small_hit_buffer):
+    """The pair tests' two ways of handing over hits (straight to the hit
+    buffer, or through a per-warp queue; the library picks by density) give
+    the same meetings and counters every step, also when the hit buffer is
+    too small and hits are applied inside the pair tests."""
+    tr, mbr = trace_and_box(hotspot_grid(30000, n_hotspots=30, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=9), 14)
+    base = StcConfig(num_objects=30000, reach_distance=10.0, min_meet_time=3, grid_capacity=50, grid_amplify=1.5,
+                     num_meeting_buckets=1_500_000, hit_capacity=4096 if small_hit_buffer else 0)
+    direct = _run(StcConfig(**{**base.__dict__, "flags": 2}), tr, mbr)  # STC_FLAG_DIRECT_HITS
+    queued = _run(StcConfig(**{**base.__dict__, "flags": 4}), tr, mbr)  # STC_FLAG_QUEUED_HITS
+    assert sum(len(m) for m, _, _ in queued) > 0
+    for t, ((gm, gh, gb), (wm, wh, wb)) in enumerate(zip(direct, queued)):
+        assert gh == wh and gb == wb, f"step {t}: counters differ"
+        assert np.array_equal(gm, wm), f"step {t}: meetings differ"
+
+
 def test_autotune_picks_a_runnable_setting(built_cuda):
     tr, mbr = trace_and_box(hotspot_grid(30000, n_hotspots=30, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=10), 6)
     cfg = StcConfig(num_objects=30000, reach_distance=10.0, min_meet_time=3, grid_capacity=50, grid_amplify=2.0,
