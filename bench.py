@@ -48,6 +48,10 @@ batched: 64 uneven ingest windows (100k-2M objects log-uniform, a tenth of
 autotune: stc_autotune on the hotspot-1M model: the leaf capacity and launch
   shape it picks and the device time per step before and after.
 sort: the library's radix sort on 100M random 32-bit pairs.
+table_random_access: the rate at which HBM serves random 32-byte slot reads,
+  each with a store to its slot, over a table of the workload's size
+  (stc_measure_random_access), one access per hit of a step, and the refine
+  phase's hits per second against it: the table update's ceiling.
 --impl reference: the oracle's C restatement of the reference CPU path with
   all host threads (the reference's own sources are not on the GPU host).
 """
@@ -673,6 +677,35 @@ def sort_line(device, peak, n=100_000_000, reps=5):
             "achieved_gbs": b / (ms / 1e3) / 1e9, "frac_of_peak": b / (ms / 1e3) / 1e9 / peak, "sorted": ok}
 
 
+def random_access_line(device, buckets, hits, refine_ms):
+    """The meeting-table update's random-access ceiling: stc_measure_random_access
+    on a table of the workload's size (2^round(log2 B) 32-byte slots, at most
+    2^30) with as many accesses as the step has hits. Every hit reads its home
+    slot, a random 32-byte sector of the table, and writes it (its end time
+    or its claim); HBM serves such accesses at this rate, far below its copy
+    bandwidth.
+    `refine_frac` = the refine phase's hits per second (pair tests and table
+    update together) / the ceiling: how close the phase is to one random slot
+    access per hit at the measured rate."""
+    import ctypes
+    from stcdb_gb300._lib import load_library
+    lib = load_library("libstc")
+    f = lib.stc_measure_random_access
+    f.argtypes = [ctypes.c_uint32, ctypes.c_ulonglong, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)]
+    f.restype = ctypes.c_int
+    log2 = min(max(int(round(np.log2(max(buckets, 1024)))), 10), 30)
+    n = max(int(hits), 1 << 20)
+    ms = ctypes.c_float(0.0)
+    if f(log2, n, device, ctypes.byref(ms)) != 0 or ms.value <= 0:
+        return {"error": lib.stc_last_error(None).decode(errors="replace")}
+    ceiling = n / (ms.value / 1e3)
+    line = {"table_bytes": 32 << log2, "accesses": n, "ms": ms.value, "accesses_per_s": ceiling}
+    if refine_ms > 0 and hits > 0:
+        line["refine_hits_per_s"] = hits / (refine_ms / 1e3)
+        line["refine_frac"] = line["refine_hits_per_s"] / ceiling
+    return line
+
+
 def _live_estimate(n, hot, reach):
     """Live meeting pairs per step of the grid-graph walker on the 40 km map:
     6.7 per object at 10M uniform objects and reach 10 m (measured), growing
@@ -1004,6 +1037,8 @@ def main():
         "trace_gen": r["trace_gen"],
         "compaction": compaction_line(r["compaction"], peak),
         "sort": sort_line(local, peak),
+        "table_random_access": random_access_line(local, B, sum(s.hits for s in r["stats"]) / K,
+                                                  phase_ms["refine"]),
         "batched": None if args.no_batched else batched_line(
             local, objects=(1e6, 2e7) if args.batched_full else (1e5, 2e6)),
         "autotune": None if args.no_batched else tune_line(local),

@@ -564,6 +564,18 @@ stc_status stc_sort_pairs_u32_noalloc(const uint32_t *keys, const uint32_t *valu
  * stc_sort_pairs_u32 sets it; stc_sort_pairs_u32_noalloc leaves it as it is. */
 float stc_last_sort_ms(void);
 
+/* Random-access ceiling of the meeting-table update on CUDA device
+ * `device`: `accesses` reads of the first 16 bytes of random slots of a table
+ * of 2^table_log2 32-byte slots (10..32; the slot of access i is a hash of
+ * i), each followed by a store of the slot's end word -- the pattern of the
+ * table update, where a hit reads its home slot and writes it. The table
+ * (32 << table_log2 bytes) is allocated, filled and freed inside the call.
+ * *ms = the best device time of three timed runs after one warm-up run.
+ * A bench utility for the table update's roofline; no counterpart in the
+ * reference. Errors: stc_last_error(NULL). */
+stc_status stc_measure_random_access(uint32_t table_log2, unsigned long long accesses, uint32_t device,
+                                     float *ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -164,3 +164,77 @@ extern "C" stc_status stc_sort_pairs_u32_noalloc(const uint32_t *keys, const uin
 }
 
 extern "C" float stc_last_sort_ms(void) { return t_last_sort_ms; }
+
+namespace {
+
+// Slot s of the probe table holds key mix64(s).
+__global__ void k_ra_init(Slot *slots, unsigned long long n) {
+  for (unsigned long long s = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; s < n;
+       s += (unsigned long long)gridDim.x * blockDim.x) {
+    Slot v = {};
+    v.key = mix64(s);
+    slots[s] = v;
+  }
+}
+
+// Access i reads the first 16 bytes of slot mix64(i + salt) & mask at L2 and
+// stores its end word: the access pattern of the meeting-table update, where
+// a hit reads its home slot and writes it (an extension its end time, a new
+// meeting its claim).
+__global__ void k_ra_access(Slot *slots, unsigned long long mask, unsigned long long n,
+                            unsigned long long salt, uint32_t t, unsigned long long *sink) {
+  unsigned long long acc = 0;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const unsigned long long s = mix64(i + salt) & mask;
+    const ulonglong2 v = __ldcg((const ulonglong2 *)&slots[s]);
+    acc += v.x;
+    slots[s].end = t + (uint32_t)v.y;
+  }
+  if (acc == 0x5A5A5A5A5A5A5A5Aull) *sink = acc;  // keeps the loads
+}
+
+}  // namespace
+
+extern "C" stc_status stc_measure_random_access(uint32_t table_log2, unsigned long long accesses,
+                                                uint32_t device, float *ms) {
+  if (table_log2 < 10 || table_log2 > 32 || accesses == 0 || accesses > (1ull << 34) || !ms) {
+    set_thread_error("stc_measure_random_access: invalid arguments");
+    return STC_ERR_INVALID_ARG;
+  }
+  *ms = 0.0f;
+  const unsigned long long n = 1ull << table_log2;
+  cudaError_t e = cudaSetDevice((int)device);
+  Slot *slots = nullptr;
+  unsigned long long *sink = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (e == cudaSuccess) e = cudaMalloc(&slots, n * sizeof(Slot));
+  if (e == cudaSuccess) e = cudaMalloc(&sink, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  float best = 0.0f;
+  if (e == cudaSuccess) {
+    const int grid = num_sms() * 16;
+    STC_KL k_ra_init<<<grid, 256>>>(slots, n);
+    for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {  // one warm-up, three timed
+      cudaEventRecord(a, 0);
+      STC_KL k_ra_access<<<grid, 256>>>(slots, n - 1, accesses, 0x9E3779B97F4A7C15ull * (rep + 1), rep, sink);
+      cudaEventRecord(b, 0);
+      e = cudaEventSynchronize(b);
+      float t = 0.0f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+      if (e == cudaSuccess && rep > 0 && (best == 0.0f || t < best)) best = t;
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+  }
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  cudaFree(slots);
+  cudaFree(sink);
+  if (e != cudaSuccess) {
+    set_thread_error(std::string("stc_measure_random_access: ") + cudaGetErrorString(e));
+    return STC_ERR_CUDA;
+  }
+  *ms = best;
+  return STC_OK;
+}

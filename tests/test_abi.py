@@ -42,3 +42,17 @@ def test_defaults_and_validation(built_cuda):
     st = lib.stc_create(ctypes.byref(c), mbr.ctypes.data, xy.ctypes.data, 1000, ctypes.byref(h))
     assert st == 1 and not h.value
     assert b"invalid" in lib.stc_last_error(None)
+
+
+def test_random_access_probe_validates_arguments(built_cuda):
+    from stcdb_gb300._lib import load_library
+    lib = load_library("libstc")
+    f = lib.stc_measure_random_access
+    f.argtypes = [ctypes.c_uint32, ctypes.c_ulonglong, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)]
+    f.restype = ctypes.c_int
+    ms = ctypes.c_float(-1.0)
+    assert f(9, 1000, 0, ctypes.byref(ms)) == 1       # table below 2^10 slots
+    assert f(33, 1000, 0, ctypes.byref(ms)) == 1      # table above 2^32 slots
+    assert f(20, 0, 0, ctypes.byref(ms)) == 1         # no accesses
+    assert f(20, 1000, 0, None) == 1                  # no result pointer
+    assert b"invalid" in lib.stc_last_error(None)

@@ -53,3 +53,18 @@ def test_sort_pairs_rejects_bad_arguments(built_cuda):
     f = _sort_fn(lib)
     assert f(None, None, None, None, 10, 8, 0) == 1
     assert f(1, 2, 3, 4, 10, 0, 0) == 1  # key_bits out of range, rejected before any device call
+
+
+def test_random_access_probe_runs(built_cuda):
+    """stc_measure_random_access (the table update's random-access ceiling
+    used by bench.py) runs and reports a positive device time that grows
+    with the number of accesses."""
+    from stcdb_gb300._lib import load_library
+    lib = load_library("libstc")
+    f = lib.stc_measure_random_access
+    f.argtypes = [ctypes.c_uint32, ctypes.c_ulonglong, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)]
+    f.restype = ctypes.c_int
+    small, large = ctypes.c_float(0.0), ctypes.c_float(0.0)
+    assert f(24, 1 << 20, 0, ctypes.byref(small)) == 0
+    assert f(24, 1 << 24, 0, ctypes.byref(large)) == 0
+    assert 0.0 < small.value < large.value
