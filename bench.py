@@ -626,14 +626,22 @@ def max_over_ranks(args, v):
 REFINE_DRAM_BYTES_PER_HIT = (54.36e6 + 33.70e6 + 264.20e6 + 36.23e6) / (6.086e6 / 4)
 
 
-def kernel_bytes(s, N, B):
+def kernel_bytes(s, N, B, prev_live=None):
     """Algorithmic bytes per launch of the step's kernels.
     partition: 36 N (read positions, write leaf-ordered points, id map)
     refine:    16 N + 16 H + 8 Q plus the fused probe, 64 B per hit
-    sweep:     32 B per table slot + 64 B per emitted meeting"""
+    sweep:     32 B per table slot read, 32 B per slot it writes (each new
+               meeting's claim finalised, each meeting not hit this step
+               cleared) + 64 B per emitted meeting. A meeting stays live only
+               when hit, so the cleared ones are the previous step's live
+               meetings less this step's extensions (hits - new);
+               `prev_live` defaults to this step's live count."""
     H, Q = s.border_units, s.hits
+    new = s.new_candidates
+    prev = s.taken_buckets if prev_live is None else prev_live
+    cleared = max(prev - (Q - new), 0)
     return {"partition": 36.0 * N, "refine": 16.0 * N + 16.0 * H + 72.0 * Q,
-            "sweep": 32.0 * B + 64.0 * s.emitted}
+            "sweep": 32.0 * B + 32.0 * (new + cleared) + 64.0 * s.emitted}
 
 
 def flush_line(f, peak):
@@ -1006,7 +1014,9 @@ def main():
     B = make_cfg(w).resolved().num_meeting_buckets
     phase_names = ["partition", "border", "refine", "insert", "sweep", "schema", "copy_in", "memtable"]
     phase_ms = {nm: sum(s.phase_ms[i] for s in r["stats"]) / K for i, nm in enumerate(phase_names)}
-    kb = {k: sum(kernel_bytes(s, N, B)[k] for s in r["stats"]) / K for k in ("partition", "refine", "sweep")}
+    st = r["stats"]
+    kb = {k: sum(kernel_bytes(x, N, B, st[i - 1].taken_buckets if i else None)[k] for i, x in enumerate(st)) / K
+          for k in ("partition", "refine", "sweep")}
     dom = max(("refine", "sweep", "partition"), key=lambda k: phase_ms[k])
     achieved = kb[dom] / (phase_ms[dom] / 1e3) / 1e9
     launches = sum(s.kernel_launches for s in r["stats"])
