@@ -139,7 +139,7 @@ def make_cfg(w, device=0, step_slices=0):
                      device=device, kv_restriction=w["kv_restriction"], step_slices=step_slices,
                      emit_capacity=w.get("emit_per_object", 0) * w["objects"],
                      refine_blocks_per_sm=w.get("refine_bps", 0), hits_blocks_per_sm=w.get("hits_bps", 0),
-                     bitmap_edge=w.get("bitmap_edge", 0), hit_capacity=w.get("hit_capacity", 0))
+                     refine_chunk=w.get("refine_chunk", 0), bitmap_edge=w.get("bitmap_edge", 0), hit_capacity=w.get("hit_capacity", 0))
 
 
 class ClockSampler:
@@ -900,7 +900,7 @@ def tune_line(device, steps=8):
     chosen, rep = autotune(cfg, mbr, xy, capacities=[64, 128, 256, 512])
     return {"workload": "hotspot-1M", "steps": steps, "base_grid_capacity": cfg.grid_capacity,
             "grid_capacity": chosen.grid_capacity, "job_chunk": chosen.job_chunk,
-            "refine_blocks_per_sm": chosen.refine_blocks_per_sm, "hits_blocks_per_sm": chosen.hits_blocks_per_sm,
+            "refine_chunk": chosen.refine_chunk, "refine_blocks_per_sm": chosen.refine_blocks_per_sm, "hits_blocks_per_sm": chosen.hits_blocks_per_sm,
             "base_step_ms": rep["base_step_ms"], "best_step_ms": rep["best_step_ms"],
             "speedup": rep["base_step_ms"] / rep["best_step_ms"], "trials": rep["trials"]}
 
@@ -979,7 +979,8 @@ def main():
                     "reach_m": w["reach"], "min_meet_steps": w["min_meet"],
                     "leaf_capacity": w["grid_capacity"], "grid_amplify": w["amplify"],
                     "launch_shape": {"refine_blocks_per_sm": w.get("refine_bps", 8),
-                                     "hits_blocks_per_sm": w.get("hits_bps", 16)},
+                                     "hits_blocks_per_sm": w.get("hits_bps", 16),
+                                     "refine_chunk": w.get("refine_chunk", 256)},
                     "meeting_buckets": make_cfg(w).resolved().num_meeting_buckets,
                     "memtable": (f"on, flush past {w['kv_restriction']} directed keys, 100 CTFs, "
                                  f"{w.get('bitmap_edge', 256)}x{w.get('bitmap_edge', 256)} map bitmaps"

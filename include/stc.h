@@ -115,6 +115,9 @@ typedef struct stc_config {
                                     bitmap over the map box (DEFAULT_bitmap_edge, util/util.h:47,
                                     a compile-time 256 in the reference): bitmap_edge^2 bits;
                                     0 = 256; a multiple of 32 from 32 to 1024 */
+  uint32_t refine_chunk;         /* refinement tile length: a job tests 32 rows against this many
+                                    positions of their candidate windows (launch shape, results do
+                                    not depend on it); 0 = 256; a multiple of 32 from 32 to 4096 */
 } stc_config;
 
 /* Replay quadtree splits/merges on one device thread only (tests compare it
@@ -191,7 +194,8 @@ stc_status stc_step_device(stc_ctx *ctx, const double *xy_device, uint32_t t);
 /* Result of stc_autotune. */
 typedef struct stc_tune_result {
   stc_config config;             /* the configuration given, with the chosen grid_capacity,
-                                    job_chunk, refine_blocks_per_sm and hits_blocks_per_sm */
+                                    job_chunk, refine_chunk, refine_blocks_per_sm and
+                                    hits_blocks_per_sm */
   float base_step_ms;            /* device time per timed step of the configuration given */
   float best_step_ms;            /* the same for the chosen one */
   uint32_t trials;               /* candidate settings run */
@@ -205,8 +209,9 @@ typedef struct stc_tune_result {
  * of its steps after the first two; the leaf capacity is chosen first among
  * `capacities` (n_capacities values; null = {grid_capacity / 2,
  * grid_capacity, 2 * grid_capacity}; cfg's own grid_capacity is always tried
- * and gives base_step_ms), then job_chunk, refine_blocks_per_sm and
- * hits_blocks_per_sm one after the other. The launch shape never changes
+ * and gives base_step_ms), then job_chunk (2-32), refine_chunk (the tile
+ * length, 64-512), refine_blocks_per_sm and hits_blocks_per_sm one after the
+ * other. The launch shape never changes
  * results; the leaf capacity is part of the reference's configuration (it
  * orders the reference's table inserts), so a run with the chosen capacity
  * matches the reference run with that capacity. */

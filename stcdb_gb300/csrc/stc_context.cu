@@ -301,6 +301,10 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
                      "num_objects < 2^26, kv_capacity > kv_restriction, both < 2^31)";
     return STC_ERR_INVALID_ARG;
   }
+  if (k.refine_chunk % 32 || k.refine_chunk > 4096) {
+    g_create_error = "stc_create: refine_chunk must be 0 (256) or a multiple of 32 up to 4096";
+    return STC_ERR_INVALID_ARG;
+  }
   if (k.bitmap_edge % 32 || k.bitmap_edge > 1024) {
     g_create_error = "stc_create: bitmap_edge must be 0 (256) or a multiple of 32 up to 1024";
     return STC_ERR_INVALID_ARG;
@@ -385,6 +389,7 @@ static stc_status create_ctx(const stc_config *cfg, const double mbr[4], const d
   p.mbr_filter = k.mbr_filter;
   p.slices = std::min<uint32_t>(std::max<uint32_t>(k.step_slices, 1u), 64u);
   p.job_chunk = k.job_chunk ? std::min<uint32_t>(k.job_chunk, 64u) : 8u;
+  p.refine_chunk = k.refine_chunk ? k.refine_chunk : REFINE_CHUNK_DEFAULT;
   p.refine_bps = k.refine_blocks_per_sm ? std::min<uint32_t>(k.refine_blocks_per_sm, 32u) : 8u;
   p.hits_bps = k.hits_blocks_per_sm ? std::min<uint32_t>(k.hits_blocks_per_sm, 64u) : 16u;
 

@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(256) k_strip_order(PipeDev p) {
       }
       longest = max(longest, __reduce_max_sync(0xffffffffu, len));
     }
-    if (lane == 0) p.cchunks[g] = max(1u, (longest + REFINE_CHUNK - 1) / REFINE_CHUNK);
+    if (lane == 0) p.cchunks[g] = max(1u, (longest + p.refine_chunk - 1) / p.refine_chunk);
     if (lane == 0) p.lstrip[g] = make_float4(inv, (float)H, wx, 0.0f);
     __syncwarp();
   }
@@ -411,9 +411,9 @@ __global__ void k_jobs(PipeDev p) {
   if (cnt > p.leaf_cap) atomicAdd(&p.st->overflow_objects, cnt - p.leaf_cap);
   uint32_t m = p.bu_cnt[g];
   // one job: 32 members (strip order) or 32 border units against one chunk
-  // of REFINE_CHUNK positions of their candidate ranges (a border unit's
+  // of refine_chunk positions of their candidate ranges (a border unit's
   // ranges hold at most n members)
-  uint32_t jobs = n ? (n + 31) / 32 * p.cchunks[g] + (m + 31) / 32 * ((n + REFINE_CHUNK - 1) / REFINE_CHUNK) : 0;
+  uint32_t jobs = n ? (n + 31) / 32 * p.cchunks[g] + (m + 31) / 32 * ((n + p.refine_chunk - 1) / p.refine_chunk) : 0;
   p.job_cnt[g] = jobs;
 }
 

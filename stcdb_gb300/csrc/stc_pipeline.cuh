@@ -10,7 +10,7 @@ namespace stc {
 // Candidate positions per refinement job and lane: a row block's candidate
 // ranges are cut into chunks of this many, so that the n^2 / 2 pair tests of
 // a dense leaf spread over many warps.
-constexpr uint32_t REFINE_CHUNK = 256;
+constexpr uint32_t REFINE_CHUNK_DEFAULT = 256;  // stc_config.refine_chunk = 0
 
 struct PipeDev {
   // sizes
@@ -30,6 +30,7 @@ struct PipeDev {
   uint32_t slices;                 // launches per long step kernel (stc_config.step_slices)
   uint32_t job_chunk;              // refinement jobs a warp takes at a time (stc_config.job_chunk)
   uint32_t direct_hits;            // pair tests write hit records directly (dense steps), not via a queue
+  uint32_t refine_chunk;               // candidate positions per refinement job (a multiple of 32)
   uint32_t refine_bps, hits_bps;   // blocks per SM of the pair tests and of the table update
   // state
   DevState *st;
@@ -54,7 +55,7 @@ struct PipeDev {
   uint32_t *sorig;
   uint2 *scand;
   float4 *lstrip;
-  uint32_t *cchunks;                    // G: candidate chunks of REFINE_CHUNK per own row block
+  uint32_t *cchunks;                    // G: candidate chunks of refine_chunk per own row block
   // border units
   uint32_t *bcount, *boff;              // N+1 (border units per pid, exclusive offsets)
   uint32_t *blist;                      // N: pids of border points (any order)

@@ -13,7 +13,7 @@
 // strip, or for a border unit its window in the three strips beside its
 // point -- can hit, and only those are tested. A job is 32 rows (members or
 // border units) of one leaf, one per lane, each over one chunk of
-// REFINE_CHUNK positions of its own contiguous segments (a dense leaf's
+// refine_chunk positions of its own contiguous segments (a dense leaf's
 // n^2 / 2 pair tests spread over many jobs). Each hit keeps the reference's priority: the finding unit's
 // rank and the member's index in pid order.
 //
@@ -352,10 +352,10 @@ __device__ void run_rows(const PipeDev &p, uint32_t g, bool own, uint32_t rowblo
       }
     }
   }
-  // this job's chunk: positions [chunk * REFINE_CHUNK, (chunk + 1) *
-  // REFINE_CHUNK) of the lane's segments taken one after the other
+  // this job's chunk: positions [chunk * refine_chunk, (chunk + 1) *
+  // refine_chunk) of the lane's segments taken one after the other
   {
-    uint32_t skip = chunk * REFINE_CHUNK, take = REFINE_CHUNK;
+    uint32_t skip = chunk * p.refine_chunk, take = p.refine_chunk;
 #pragma unroll
     for (int seg = 0; seg < 3; seg++) {
       const uint32_t d = min(skip, sl[seg]);
@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(REFINE_THREADS, 4) k_refine_a(PipeDev p, uint3
       if (local < own_jobs) {
         run_rows<DIRECT>(p, g, true, local / cc, local % cc, n, t, ct, q, qn, w);
       } else {
-        const uint32_t ccb = (n + REFINE_CHUNK - 1) / REFINE_CHUNK, b = local - own_jobs;
+        const uint32_t ccb = (n + p.refine_chunk - 1) / p.refine_chunk, b = local - own_jobs;
         run_rows<DIRECT>(p, g, false, b / ccb, b % ccb, n, t, ct, q, qn, w);
       }
     }

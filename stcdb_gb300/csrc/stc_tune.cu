@@ -92,14 +92,17 @@ extern "C" stc_status stc_autotune(const stc_config *cfg, const double mbr[4], c
   stc_config k = base;
   k.grid_capacity = r.config.grid_capacity;
   k.job_chunk = cfg->job_chunk ? cfg->job_chunk : 8;  // 0 means these built-in values
+  k.refine_chunk = cfg->refine_chunk ? cfg->refine_chunk : 256;
   k.refine_blocks_per_sm = cfg->refine_blocks_per_sm ? cfg->refine_blocks_per_sm : 8;
   k.hits_blocks_per_sm = cfg->hits_blocks_per_sm ? cfg->hits_blocks_per_sm : 16;
-  const uint32_t job_chunks[] = {2, 4, 8, 16, 32}, refine_bps[] = {4, 8, 16}, hits_bps[] = {8, 16, 32};
+  const uint32_t job_chunks[] = {2, 4, 8, 16, 32}, refine_chunks[] = {64, 128, 256, 512},
+                 refine_bps[] = {4, 8, 16}, hits_bps[] = {8, 16, 32};
   struct Field {
     uint32_t stc_config::*f;
     const uint32_t *vals;
     int n;
   } fields[] = {{&stc_config::job_chunk, job_chunks, 5},
+                {&stc_config::refine_chunk, refine_chunks, 4},
                 {&stc_config::refine_blocks_per_sm, refine_bps, 3},
                 {&stc_config::hits_blocks_per_sm, hits_bps, 3}};
   for (const Field &fd : fields) {
@@ -118,6 +121,7 @@ extern "C" stc_status stc_autotune(const stc_config *cfg, const double mbr[4], c
     k.*(fd.f) = keep;
   }
   r.config.job_chunk = k.job_chunk;
+  r.config.refine_chunk = k.refine_chunk;
   r.config.refine_blocks_per_sm = k.refine_blocks_per_sm;
   r.config.hits_blocks_per_sm = k.hits_blocks_per_sm;
   r.best_step_ms = (float)(best / (steps - TUNE_WARM));

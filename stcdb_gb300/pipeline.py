@@ -59,6 +59,7 @@ class _Config(ctypes.Structure):
         ("hits_blocks_per_sm", ctypes.c_uint32),
         ("window_graphs", ctypes.c_uint32),
         ("bitmap_edge", ctypes.c_uint32),
+        ("refine_chunk", ctypes.c_uint32),
     ]
 
 
@@ -232,6 +233,7 @@ class StcConfig:
     hits_blocks_per_sm: int = 0    # 0 = 16
     window_graphs: int = 0    # step_window replays captured graphs: 0 = for short steps (automatic), 1 = always, 2 = never
     bitmap_edge: int = 0      # edge of a block's map bitmap (oversize buffer); 0 = 256
+    refine_chunk: int = 0     # refinement tile length, candidate positions per job (launch shape); 0 = 256
 
     def resolved(self) -> "StcConfig":
         if self.num_meeting_buckets == 0:
@@ -264,7 +266,7 @@ def autotune(cfg: StcConfig, mbr, xy_steps: np.ndarray, capacities=None) -> tupl
     if st != 0:
         raise StcError(st, lib.stc_last_error(None).decode())
     chosen = replace(cfg, grid_capacity=int(r.config.grid_capacity), job_chunk=int(r.config.job_chunk),
-                     refine_blocks_per_sm=int(r.config.refine_blocks_per_sm),
+                     refine_chunk=int(r.config.refine_chunk), refine_blocks_per_sm=int(r.config.refine_blocks_per_sm),
                      hits_blocks_per_sm=int(r.config.hits_blocks_per_sm))
     return chosen, {"base_step_ms": float(r.base_step_ms), "best_step_ms": float(r.best_step_ms),
                     "trials": int(r.trials)}

@@ -56,3 +56,17 @@ def test_random_access_probe_validates_arguments(built_cuda):
     assert f(20, 0, 0, ctypes.byref(ms)) == 1         # no accesses
     assert f(20, 1000, 0, None) == 1                  # no result pointer
     assert b"invalid" in lib.stc_last_error(None)
+
+
+def test_refine_chunk_validated_before_any_device_call(built_cuda):
+    from stcdb_gb300.pipeline import _Config, _lib
+    lib = _lib()
+    mbr = np.array([0.0, 0.0, 1.0, 1.0])
+    xy = np.zeros((1000, 2))
+    for bad in (100, 4128):  # not a multiple of 32; above 4096
+        c = _Config()
+        lib.stc_config_default(ctypes.byref(c), 1000)
+        c.refine_chunk = bad
+        h = ctypes.c_void_p()
+        assert lib.stc_create(ctypes.byref(c), mbr.ctypes.data, xy.ctypes.data, 1000, ctypes.byref(h)) == 1
+        assert not h.value and b"refine_chunk" in lib.stc_last_error(None)
