@@ -358,7 +358,8 @@ def run_gpu(args, w, rank, local):
         info = pipe.ctb_info()
         flush = dict(keys=int(keys), ms=float(fs.flush_ms), ctf_keys=int(info.ctf_kv_count),
                      oversize_keys=int(info.oversize_kv_count), key_bytes=int(info.key_bytes),
-                     ctfs=int(info.ctf_count), steps=W + 2 * K)
+                     ctfs=int(info.ctf_count), steps=W + 2 * K,
+                     stages_ms=dict(zip(FLUSH_STAGES, (float(x) for x in fs.flush_stage_ms))))
     # queries under ingest: K more steps while a serving thread answers a
     # Poisson query stream over the flushed block
     queries = queries_hbm = None
@@ -383,7 +384,9 @@ def run_gpu(args, w, rank, local):
             new, cms = pipe.compact(first, m, 10)
             out = pipe.block_info(new)
             compaction = dict(blocks=m, keys=keys_in, split=10, ms=cms, keys_per_s=keys_in / (cms / 1e3),
-                              out_ctf_keys=int(out.ctf_kv_count), out_oversize_keys=int(out.oversize_kv_count))
+                              out_ctf_keys=int(out.ctf_kv_count), out_oversize_keys=int(out.oversize_kv_count),
+                              stages_ms=dict(zip(COMPACT_STAGES,
+                                                 (float(x) for x in pipe.stats().compact_stage_ms))))
         except Exception as e:  # noqa: BLE001 - e.g. no room for the merge; reported in the line
             compaction = dict(blocks=m, keys=keys_in, error=str(e))
     pipe.close()
@@ -644,15 +647,31 @@ def kernel_bytes(s, N, B, prev_live=None):
             "sweep": 32.0 * B + 32.0 * (new + cleared) + 64.0 * s.emitted}
 
 
+FLUSH_STAGES = ("object_order", "key_sort", "ctf_limits", "encode", "store_and_index")
+
+
 def flush_line(f, peak):
     """One memtable flush: algorithmic bytes 64 per key (key + box read and
-    written once) plus the packed keys and the bitmap slots written."""
+    written once) plus the packed keys and the bitmap slots written. Its
+    stages (stc_stats.flush_stage_ms): the object order (oversize cut, STR
+    sorts, slabs, sids), the key sort, the per-CTF limits and metadata, the
+    key encoding (each CTF key's record and box read once, 32 B, and its
+    packed bytes written: `encode_gbs`) and the block's store with its query
+    index."""
     if not f or not f["keys"]:
         return dict(f) if f else None
     ab = 64.0 * f["keys"] + f["key_bytes"] + 8192.0 * (f["ctfs"] + 1)
     gbs = ab / (f["ms"] / 1e3) / 1e9
-    return dict(f, keys_per_s=f["keys"] / (f["ms"] / 1e3), algorithmic_bytes=ab, achieved_gbs=gbs,
-                frac_of_peak=gbs / peak)
+    out = dict(f, keys_per_s=f["keys"] / (f["ms"] / 1e3), algorithmic_bytes=ab, achieved_gbs=gbs,
+               frac_of_peak=gbs / peak)
+    st = f.get("stages_ms") or {}
+    if st.get("encode", 0) > 0:
+        eb = 32.0 * f["ctf_keys"] + f["key_bytes"]
+        out["encode_gbs"] = eb / (st["encode"] / 1e3) / 1e9
+        out["encode_frac_of_peak"] = out["encode_gbs"] / peak
+    if st.get("key_sort", 0) > 0:
+        out["key_sort_keys_per_s"] = f["keys"] / (st["key_sort"] / 1e3)
+    return out
 
 
 def sort_line(device, peak, n=100_000_000, reps=5):
@@ -905,9 +924,16 @@ def tune_line(device, steps=8):
             "speedup": rep["base_step_ms"] / rep["best_step_ms"], "trials": rep["trials"]}
 
 
+COMPACT_STAGES = ("scratch_alloc", "decode", "object_order", "key_sort", "ctf_limits_and_alloc", "encode",
+                  "index")
+
+
 def compaction_line(c, peak):
     """Merge throughput; algorithmic bytes 2 x 32 per merged key (read and
-    write each key and its box once)."""
+    write each key and its box once). Its stages (stc_stats.compact_stage_ms):
+    scratch allocation, the inputs' decode, the object order, the key sort,
+    the CTF limits and metadata with the new block's allocation, the key
+    encoding and the query index (host work between them included)."""
     if not c or "error" in c:
         return c
     b = 64.0 * c["keys"]

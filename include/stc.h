@@ -171,6 +171,16 @@ typedef struct stc_stats {
   float window_wall_ms;
   float window_input_wait_ms;
   float window_copy_ms;          /* the window's input copies, start to end (each beside a step) */
+  /* The last flush's stages (device time on the library's stream, the host's
+   * reads of the device state between them included): object order (oversize
+   * cut, STR sorts, slabs, sids), key sort, per-CTF limits and metadata, key
+   * encoding with the bitmaps, and the block's store with its query index. */
+  float flush_stage_ms[5];
+  /* The last stc_compact's stages (device time on the library's stream, host
+   * work between them included): scratch allocation, decode of the inputs,
+   * STR order and sids, key sort, per-CTF limits and metadata with the new
+   * block's allocation, key encoding with the bitmaps, and the query index. */
+  float compact_stage_ms[7];
 } stc_stats;
 
 /* Fills *cfg with the reference defaults for n objects (util/config.h:29-41,

@@ -273,7 +273,7 @@ struct Scratch {
 }  // namespace
 
 stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32_t count, uint32_t split,
-                       uint32_t new_index, cudaStream_t s, float *ms, std::string &err) {
+                       uint32_t new_index, cudaStream_t s, float *ms, std::string &err, float *stages) {
   const uint32_t N = L.N, S = split, F2 = split * split;
   if (count == 0 || split == 0 || F2 > MAX_CTF) {
     err = "compact: count must be >= 1 and split in 1..63";
@@ -317,6 +317,18 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
   cudaEventCreate(&ev0);
   cudaEventCreate(&ev1);
   cudaEventRecord(ev0, s);
+  // stage marks: the ends of the first COMPACT_STAGES - 1 stages (ev1 ends the last)
+  struct Marks {
+    cudaEvent_t ev[COMPACT_STAGES - 1] = {};
+    Marks() {
+      for (cudaEvent_t &x : ev) cudaEventCreate(&x);
+    }
+    ~Marks() {
+      for (cudaEvent_t x : ev)
+        if (x) cudaEventDestroy(x);
+    }
+  } marks;
+  auto mark = [&](int i) { cudaEventRecord(marks.ev[i], s); };
   Scratch sc;
   LsmDev C = L;  // configuration; every array below is the compaction's own
   C.F = F2;
@@ -349,6 +361,7 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
     err = "compact: device memory for the merge scratch";
     return STC_ERR_CAPACITY;
   }
+  mark(0);
   // 1. sids, oversize records of the inputs, decode of the CTF keys
   std::vector<InCtf> ic;
   std::vector<const uint16_t *> sid_ptrs;
@@ -399,6 +412,7 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
   }
   if (nk)
     STC_KL k_cmp_decode<<<lsm_grid(), 256, 0, s>>>(d_ic, nc, nk, no, N, etm, o_etm, ob, C.rec, C.box, C.over, C.st);
+  mark(1);
   // 2. STR: objects by x midpoint, x slabs by y midpoint (:843-942)
   uint32_t **sk = C.sk;
   STC_KL k_cmp_mid<<<nblk(N), 256, 0, s>>>(ob, N, sk[5], C.mid_lo, sk[0], C.st);
@@ -428,8 +442,10 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
     sort_words(C, sk[0], sk[5], sk[1], sk[2], sk[3], sk[4], 1, n_str, bits_for(S - 1), s);
     STC_KL k_make_sid<<<num_sms(), 512, F2 * sizeof(uint32_t), s>>>(C, sk[6], sk[2], 0, n_str, xcap, ycap);
   }
+  mark(2);
   // 3. all records by (oversize, sid, oid, target, duration, end), stable
   sort_keys(C, T, N, st.lsm_max_end, st.lsm_max_dur, bits_for(F2 + 1), s);
+  mark(3);
   // 4. CTF ranges and limits (:944-1004), oversize times and bitmap
   std::vector<uint32_t> cap(F2);
   e = cudaMemcpyAsync(cap.data(), C.ctf_cap, F2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
@@ -538,11 +554,13 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
     e = cudaMemcpyAsync(B.orec, C.brec + slim, no_out * sizeof(uint4), cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess && no_out)
     e = cudaMemcpyAsync(B.obox, C.bbox + slim, no_out * sizeof(float4), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) mark(4);
   if (e == cudaSuccess && slim)
     // bitmaps (:1015-1035: cells clamped to the grid on each axis) and packed
     // keys (:1048-1060: oid, target, duration, end offset, box; fields added)
     STC_KL k_encode_keys<<<lsm_grid(), ENC_GROUP, 0, s>>>(
         EncodeArgs{C.brec, C.bbox, B.d_ctfs, C.ctf_first, nullptr, B.bitmaps, B.keys, slim, slim, F2, true});
+  if (e == cudaSuccess) mark(5);
   if (e == cudaSuccess) e = build_index(C, B, s);
   if (e == cudaSuccess) e = cudaEventRecord(ev1, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -555,6 +573,16 @@ stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32
     return e == cudaErrorMemoryAllocation ? STC_ERR_CAPACITY : STC_ERR_CUDA;
   }
   if (ms) cudaEventElapsedTime(ms, ev0, ev1);
+  if (stages) {
+    cudaEvent_t b[COMPACT_STAGES + 1] = {ev0};
+    for (int i = 0; i < COMPACT_STAGES - 1; i++) b[i + 1] = marks.ev[i];
+    b[COMPACT_STAGES] = ev1;
+    for (int i = 0; i < COMPACT_STAGES; i++) {
+      stages[i] = 0.0f;
+      cudaEventElapsedTime(&stages[i], b[i], b[i + 1]);
+    }
+    cudaGetLastError();
+  }
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
   // 7. the merged block takes the place of its inputs

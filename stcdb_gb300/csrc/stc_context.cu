@@ -23,7 +23,7 @@ namespace {
 thread_local std::string g_create_error = "no error";
 
 enum Phase { PH_START = 0, PH_COPY, PH_PART, PH_BORDER, PH_REFINE, PH_INSERT, PH_SWEEP, PH_APPEND, PH_SCHEMA,
-             PH_FLUSH0, PH_FLUSH1, PH_COUNT };
+             PH_FLUSH0, PH_FL_OBJECTS, PH_FL_SORT, PH_FL_META, PH_FL_ENCODE, PH_FLUSH1, PH_COUNT };
 
 }  // namespace
 
@@ -524,7 +524,7 @@ static stc_status flush_now(stc_ctx *c, uint32_t t) {
   cudaEventRecord(c->ev[PH_FLUSH0], c->stream);
   unsigned long long launches0 = tl_launches;
   std::string err;
-  stc_status rs = lsm_flush(c->lsm, c->lsmh, t, c->stream, c->st_host, err);
+  stc_status rs = lsm_flush(c->lsm, c->lsmh, t, c->stream, c->st_host, err, &c->ev[PH_FL_OBJECTS]);
   if (rs != STC_OK) return fail(c, rs, "stc flush: " + err);
   if (c->st_host->error) return read_state(c, "stc flush");
   rs = lsm_store_block(c->lsm, c->lsmh, c->stream, err);
@@ -535,6 +535,11 @@ static stc_status flush_now(stc_ctx *c, uint32_t t) {
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev[PH_FLUSH0], c->ev[PH_FLUSH1]);
   c->stats.flush_ms = ms;
+  for (int i = 0; i < 5; i++) {
+    float st = 0;
+    cudaEventElapsedTime(&st, c->ev[PH_FLUSH0 + i], c->ev[PH_FLUSH0 + i + 1]);
+    c->stats.flush_stage_ms[i] = st;
+  }
   c->stats.flushes = c->lsmh.flushes;
   c->stats.memtable_keys = c->st_host->kv_count;
   c->stats.kernel_launches += (uint32_t)(tl_launches - launches0);
@@ -1362,7 +1367,8 @@ extern "C" stc_status stc_compact(stc_ctx *c, uint32_t first_index, uint32_t cou
   std::string err;
   float ms = 0.0f;
   const uint32_t idx = c->lsmh.next_index;
-  stc_status st = lsm_compact(c->lsm, c->lsmh, first_index, count, split, idx, c->stream, &ms, err);
+  stc_status st = lsm_compact(c->lsm, c->lsmh, first_index, count, split, idx, c->stream, &ms, err,
+                              c->stats.compact_stage_ms);
   if (st != STC_OK) {
     c->err = "stc_compact: " + err;
     return st;

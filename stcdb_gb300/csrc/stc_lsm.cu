@@ -653,7 +653,11 @@ void lsmk::sort_words(const LsmDev &L, const uint32_t *k, const uint32_t *v, uin
   radix_sort_u32(k, v, ko, vo, kt, vt, L.n_dev + count_slot, n, (int)bits, L.hist, L.scan, s);
 }
 
-stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState *st_host, std::string &err) {
+stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState *st_host, std::string &err,
+                     const cudaEvent_t *marks) {
+  auto mark = [&](int i) {
+    if (marks) cudaEventRecord(marks[i], s);
+  };
   cudaError_t e;
   auto read_state = [&]() -> cudaError_t {
     cudaError_t r = cudaMemcpyAsync(st_host, L.st, sizeof(DevState), cudaMemcpyDeviceToHost, s);
@@ -694,8 +698,10 @@ stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState
     sort_words(L, sk[0], sk[5], sk[1], sk[2], sk[3], sk[4], 1, R, bits_for(S - 1), s);
     STC_KL k_make_sid<<<num_sms(), 512, F * sizeof(uint32_t), s>>>(L, sk[6], sk[2], z, R, xcap, ycap);
   }
+  mark(0);
   // 4. sort the keys: (over, sid, pid, target, duration, end)
   sort_keys(L, K, N, max_end, max_dur, bits_for(S * S + 1), s);
+  mark(1);
   // 5. CTF key ranges
   std::vector<uint32_t> cap(F);
   e = cudaMemcpyAsync(cap.data(), L.ctf_cap, (size_t)F * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
@@ -741,10 +747,12 @@ stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState
     return STC_ERR_CAPACITY;
   }
   cudaMemcpyAsync(L.ctfs, H.ctfs.data(), F * sizeof(stc_ctf), cudaMemcpyHostToDevice, s);
+  mark(2);
   // 7. bitmaps and packed keys
   if (total)
     STC_KL k_encode_keys<<<lsm_grid(), ENC_GROUP, 0, s>>>(
         EncodeArgs{L.brec, L.bbox, L.ctfs, L.ctf_first, L.sid, L.bitmaps, L.kbytes, total, slim, L.F, false});
+  mark(3);
   // 8. keep the sids of the block; empty the memtable
   cudaMemcpyAsync(L.bsid, L.sid, (size_t)N * sizeof(uint16_t), cudaMemcpyDeviceToDevice, s);
   stc_ctb_info in{};

@@ -182,7 +182,11 @@ void lsm_append(const PipeDev &p, const LsmDev &L, cudaStream_t s);
 
 // Flushes the memtable at step t into a block. st_host is a pinned DevState
 // mirror used for read-backs. On failure returns a status and sets err.
-stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState *st_host, std::string &err);
+// marks (optional): four events recorded on s after the object order (STR
+// sort, slabs, sids), the key sort, the CTF limits and metadata, and the key
+// encoding.
+stc_status lsm_flush(LsmDev &L, LsmHost &H, uint32_t t, cudaStream_t s, DevState *st_host, std::string &err,
+                     const cudaEvent_t *marks = nullptr);
 
 // Copies the block just flushed into its own allocations, builds its cell
 // index and appends it to the retained blocks, dropping the oldest beyond
@@ -218,8 +222,13 @@ cudaError_t build_index(const LsmDev &L, CtbBlock &B, cudaStream_t s);
 // tools/compaction.cpp:729-1206), which takes their place in the retained
 // list under index new_index. L supplies the configuration (objects,
 // max_meet_time, map); the merge allocates its own scratch. ms: device time.
+// stages (optional, COMPACT_STAGES floats): the device time of the scratch
+// allocation, the inputs' decode, the STR order, the key sort, the CTF
+// limits and metadata with the new block's allocation, the key encoding and
+// the query index.
+constexpr int COMPACT_STAGES = 7;
 stc_status lsm_compact(const LsmDev &L, LsmHost &H, uint32_t first_index, uint32_t count, uint32_t split,
-                       uint32_t new_index, cudaStream_t s, float *ms, std::string &err);
+                       uint32_t new_index, cudaStream_t s, float *ms, std::string &err, float *stages = nullptr);
 
 // Creates the query lanes' streams (priority `priority`) and allocates their
 // buffers for batches of up to nq queries over blocks of up to F CTFs (later

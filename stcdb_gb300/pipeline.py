@@ -97,6 +97,8 @@ class StcStats(ctypes.Structure):
         ("window_wall_ms", ctypes.c_float),
         ("window_input_wait_ms", ctypes.c_float),
         ("window_copy_ms", ctypes.c_float),
+        ("flush_stage_ms", ctypes.c_float * 5),
+        ("compact_stage_ms", ctypes.c_float * 7),
     ]
 
     def as_dict(self) -> dict:
