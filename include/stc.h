@@ -128,6 +128,10 @@ typedef struct stc_config {
  * straight to the hit buffer, or through a per-warp queue. Tests force each. */
 #define STC_FLAG_DIRECT_HITS 2u
 #define STC_FLAG_QUEUED_HITS 4u
+/* stc_step_window copies page-locked host input with a copy engine instead
+ * of having each step's descent read it from the host pages (the default
+ * without graphs and while no request loop is attached). Tests force it. */
+#define STC_FLAG_COPY_INPUT 8u
 
 /* One finished meeting. pid_lo < pid_hi; start/end are the first and last
  * step in which the pair was within reach; mbr is the float bounding box of
@@ -230,11 +234,16 @@ stc_status stc_autotune(const stc_config *cfg, const double mbr[4], const double
 
 /* Processes a window of `steps` consecutive steps t0, t0 + 1, ...: xy holds
  * steps x num_objects (lon, lat) f64 pairs, layout [step][oid], in host
- * memory (on_device 0) or device memory (on_device 1). Each step's positions
- * are copied into one of three input buffers once the step three before it
- * has run, beside the sweep of the step queued before it (page-locked host
- * memory is copied by DMA; pageable memory is staged by the driver), and the
- * window is pipelined one step deep: step i + 1 is queued on the GPU before
+ * memory (on_device 0) or device memory (on_device 1). Device input is read
+ * where it lies. Page-locked host input (the whole range in one page-locked
+ * allocation) is read from the host pages by each step's descent, which
+ * writes the device copy the rest of the step reads, unless the steps replay
+ * graphs, a request loop (stc_server) is attached to the context, or
+ * STC_FLAG_COPY_INPUT is set. Otherwise each step's positions are copied into
+ * one of three input buffers once the step three before it has run, beside
+ * the sweep of the step queued before it (page-locked host memory by DMA,
+ * pageable memory staged by the driver). The window is pipelined one step
+ * deep: step i + 1 is queued on the GPU before
  * the host reads step i's state, so the GPU does not wait for the host
  * between steps. The memtable
  * append of step i + 1 is queued only after step i's flush decision (a flush

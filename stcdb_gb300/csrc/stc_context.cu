@@ -5,6 +5,7 @@
 // from device memory inside the kernels), then copies the 128-byte control
 // block back once to report counters and errors.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -50,6 +51,7 @@ static cudaError_t copy_in_pieces(void *dst, const void *src, size_t bytes, cuda
 }
 
 struct stc_ctx {
+  std::atomic<int> servers{0};  // request loops (stc_server) attached to the context
   stc_config cfg;
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -885,8 +887,27 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   // reads it): no copy beside the steps (a 160 MB device-to-device copy took
   // 1.5 ms beside a 10M-object step against 0.05 ms alone).
   const bool direct = on_device && !graphs;
+  // Page-locked host input without graphs: the descent of each step reads
+  // its positions from the host pages and writes the device copy the rest
+  // of the step reads. A copy engine's 160 MB copy beside a 10M-object step
+  // took 0.9 ms on some hosts and 3-9 ms on others (the same copy alone:
+  // 0.8 ms); the descent's reads cost about 1 ms a step everywhere. Not
+  // while a request loop is attached: its batches move their queries and
+  // answers through mapped host memory too, and waited behind the descent's
+  // reads (query p99 under ingest 2.5-4.7 against 1.8-1.9 ms). Both ends of
+  // the range must lie in page-locked memory mapped for the device.
+  const double2 *host_in = nullptr;
+  if (!on_device && !graphs && !(c->cfg.flags & STC_FLAG_COPY_INPUT) && c->servers.load() == 0) {
+    cudaPointerAttributes a0, a1;
+    const uint8_t *last = (const uint8_t *)xy + (size_t)steps * step_bytes - 1;
+    if (cudaPointerGetAttributes(&a0, xy) == cudaSuccess && cudaPointerGetAttributes(&a1, last) == cudaSuccess &&
+        a0.type == cudaMemoryTypeHost && a1.type == cudaMemoryTypeHost && a0.devicePointer && a1.devicePointer &&
+        (const uint8_t *)a1.devicePointer - (const uint8_t *)a0.devicePointer == last - (const uint8_t *)xy)
+      host_in = (const double2 *)a0.devicePointer;
+    cudaGetLastError();
+  }
   auto fetch = [&](uint32_t i) -> cudaError_t {
-    if (direct) return cudaSuccess;
+    if (direct || host_in) return cudaSuccess;
     const int b = (int)(i % WIN_BUFS);
     cudaError_t e = i >= (uint32_t)WIN_BUFS ? cudaStreamWaitEvent(c->copy_stream, c->core_ev[b], 0) : cudaSuccess;
     // and runs beside the sweep of the step queued last (i - 2; step 0 for
@@ -907,7 +928,7 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
     c->t_pinned[b] = t0 + i;  // step i - WIN_BUFS, the word's last reader, has been waited for
     const unsigned long long l0 = tl_launches;
     cudaEventRecord(c->wev[par][0], s);
-    cudaError_t e = direct ? cudaSuccess : cudaStreamWaitEvent(s, c->copy_ev[b], 0);
+    cudaError_t e = (direct || host_in) ? cudaSuccess : cudaStreamWaitEvent(s, c->copy_ev[b], 0);
     if (e != cudaSuccess) return cuda_fail(c, e, "stc_step_window copy-in");
     cudaEventRecord(c->wev[par][3], s);
     if (graphs) {
@@ -920,9 +941,11 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
       tl_launches += c->graph_kernels;
     } else {
       p.xy = direct ? (const double2 *)((const uint8_t *)xy + (size_t)i * step_bytes) : window_buffer(c, b);
+      p.xy_in = host_in ? (const double2 *)((const uint8_t *)host_in + (size_t)i * step_bytes) : nullptr;
       c->gate_ev = c->sweep_ev[par];
       issue_step(c, false, false, c->t_pinned + b);
       c->gate_ev = nullptr;
+      p.xy_in = nullptr;
     }
     cudaEventRecord(c->core_ev[b], s);
     launches[par] = tl_launches - l0;
@@ -959,7 +982,7 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
     wait_ms += wait;
     // step i's copy ended before its core began, which has run
     float cp = 0;
-    if (!direct &&
+    if (!direct && !host_in &&
         cudaEventElapsedTime(&cp, c->copy_t0[i % (2 * WIN_BUFS)], c->copy_t1[i % (2 * WIN_BUFS)]) == cudaSuccess)
       copy_ms += cp;
     cudaGetLastError();
@@ -1226,6 +1249,12 @@ stc_status query_batch_limited(stc_ctx *c, int lane, const stc_query *queries, s
                                float *gpu_ms = nullptr);
 // Queries one device pass takes (larger batches run as several passes).
 size_t query_chunk(const stc_ctx *c);
+// A request loop attaches (+1) to or detaches (-1) from the context.
+void server_attach(stc_ctx *c, int d);
+}
+
+void stc::server_attach(stc_ctx *c, int d) {
+  if (c) c->servers += d;
 }
 
 extern "C" stc_status stc_query_batch(stc_ctx *c, const stc_query *queries, size_t nq, stc_contact *out,

@@ -30,7 +30,13 @@ __device__ __forceinline__ double dpml_fast_d(double lat) {
 __global__ void k_descend(PipeDev p) {
   uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x;
   if (pid >= p.N) return;
-  double2 q = p.xy[pid];
+  double2 q;
+  if (p.xy_in) {
+    q = p.xy_in[pid];
+    const_cast<double2 *>(p.xy)[pid] = q;
+  } else {
+    q = p.xy[pid];
+  }
   uint32_t cur = 0, lv = 0;
   NodeMeta m = p.sd.meta[0];
   if (m.type != NODE_LEAF) {

@@ -37,6 +37,8 @@ struct PipeDev {
   SchemaDev sd;
   SchemaWork sw;
   const double2 *xy;               // positions of the current step
+  const double2 *xy_in = nullptr;  // when set: page-locked host positions the descent reads and
+                                   // copies to xy (a buffer of the context's own)
   // partition
   uint32_t *leaf_gid, *lastvalid, *iota, *sorted_gid, *sorted_pid, *sort_ktmp, *sort_vtmp, *sort_hist;
   uint32_t *grid_count, *grid_start;   // G, G+1

@@ -28,6 +28,7 @@ stc_status query_batch_limited(stc_ctx *c, int lane, const stc_query *queries, s
                                size_t cap, uint64_t *offsets, uint64_t *counts, size_t device_limit,
                                float *gpu_ms);
 size_t query_chunk(const stc_ctx *c);
+void server_attach(stc_ctx *c, int d);
 }
 
 namespace {
@@ -251,6 +252,7 @@ extern "C" stc_status stc_server_start(stc_ctx *ctx, const stc_server_config *cf
     stc::set_thread_error("stc_server_start: cannot start the serving threads");
     return STC_ERR_STATE;
   }
+  stc::server_attach(ctx, 1);
   *out = s;
   return STC_OK;
 }
@@ -311,6 +313,7 @@ extern "C" stc_status stc_server_stop(stc_server *s) {
   s->cv_in.notify_all();
   for (std::thread &t : s->th)
     if (t.joinable()) t.join();
+  stc::server_attach(s->ctx, -1);
   delete s;
   return STC_OK;
 }

@@ -29,8 +29,11 @@ def _blocks(p):
     return out
 
 
-@pytest.mark.parametrize("graphs", [1, 2])  # replayed graphs, direct launches
-def test_windows_match_plain_steps(built_cuda, graphs):
+# replayed graphs; direct launches, whose descent reads page-locked host
+# input from the host pages; direct launches with that input copied in
+# (STC_FLAG_COPY_INPUT)
+@pytest.mark.parametrize("graphs,flags", [(1, 0), (2, 0), (2, 8)])
+def test_windows_match_plain_steps(built_cuda, graphs, flags):
     import torch
     steps = 24
     tc = hotspot_grid(30000, n_hotspots=30, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=11)
@@ -51,10 +54,10 @@ def test_windows_match_plain_steps(built_cuda, graphs):
         plain.close()
 
     from dataclasses import replace
-    win = Pipeline(replace(cfg, window_graphs=graphs), mbr, tr[0])
+    win = Pipeline(replace(cfg, window_graphs=graphs, flags=flags), mbr, tr[0])
     dev = torch.from_numpy(tr).cuda()
-    # page-locked host input (plain DMA) besides pageable host input (staged
-    # by the driver)
+    # page-locked host input (read by the descent, or copied by DMA) besides
+    # pageable host input (staged by the driver)
     pinned = torch.from_numpy(tr).pin_memory().numpy()
     try:
         got_win = []
@@ -155,3 +158,30 @@ def test_window_small_emit_buffer(built_cuda, graphs):
     finally:
         p.close()
     assert np.array_equal(_rows(got), _rows(np.concatenate(plain)))
+
+
+def test_page_locked_input_path(built_cuda):
+    """Without graphs, page-locked host input is read by each step's descent
+    (no input copies: window_copy_ms stays 0); with STC_FLAG_COPY_INPUT, or
+    while a request loop is attached, it is copied in as before."""
+    import torch
+    from dataclasses import replace
+    steps = 8
+    tc = hotspot_grid(20000, n_hotspots=20, box_m=3000.0, grid_n=16, sigma_m=120.0, seed=12)
+    cfg = StcConfig(num_objects=20000, reach_distance=10.0, min_meet_time=3, grid_capacity=50, grid_amplify=1.5,
+                    num_meeting_buckets=1_000_000, kv_restriction=50_000, window_graphs=2)
+    tr, mbr = trace_and_box(tc, steps)
+    pinned = torch.from_numpy(np.ascontiguousarray(tr, dtype=np.float64)).pin_memory().numpy()
+    out = np.empty(1_000_000, MEETING_DTYPE)
+    for flags, serve, copies in [(0, False, False), (8, False, True), (0, True, True)]:
+        p = Pipeline(replace(cfg, flags=flags), mbr, tr[0])
+        srv = p.server() if serve else None
+        try:
+            p.step_window(pinned[0:2], 0, out)  # the first window after the context's own step 0
+            p.step_window(pinned[2:steps], 2, out)
+            ms = p.stats().window_copy_ms
+            assert (ms > 0) == copies, (flags, serve, ms)
+        finally:
+            if srv is not None:
+                srv.stop()
+            p.close()
