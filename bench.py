@@ -26,11 +26,11 @@ Every step also appends its emitted meetings to the memtable (two directed
   keys each, as the reference's GPU step does); the JSON's "flush" times one
   flush of everything gathered over the run into 100 CTFs.
 e2e: the same metric through the public C ABI with host input: pipelined
-  windows of 10 steps (stc_step_window), every step's positions copied from
-  pinned host memory (the next step's while the current one runs) and its
-  emitted meetings drained back to the host beside the next step; wall
-  clock. "host_link" gives the copy rates of one step's positions and
-  "windows" how busy the windows kept the GPU.
+  windows of 10 steps (stc_step_window), every step's positions read from
+  pinned host memory by the step's descent (copied in by a copy engine while
+  a request loop is attached) and its emitted meetings drained back to the
+  host beside the next step; wall clock. "host_link" gives the copy rates of
+  one step's positions and "windows" how busy the windows kept the GPU.
 queries_under_ingest: 2K more steps (host input, pipelined windows of 4
   steps) while the library's serving workers answer a Poisson query stream
   (default 20,000/s) over the flushed block by continuous batching: 60%
@@ -314,9 +314,9 @@ def run_gpu(args, w, rank, local):
     dev_ms = sum(s.step_ms for s in stats)
     # end to end: host positions in, meetings out, through the C ABI, in
     # windows of up to E2E_WINDOW steps (stc_step_window: each step's
-    # positions copied from page-locked host memory while the step before
-    # runs, its meetings drained after it); the meetings land in a reused
-    # page-locked buffer, as a server would keep one
+    # positions read from page-locked host memory by its descent, its
+    # meetings drained after it); the meetings land in a reused page-locked
+    # buffer, as a server would keep one
     from stcdb_gb300.pipeline import MEETING_DTYPE
     per_step = max(max(s.emitted for s in stats), 1)
     win = min(K, E2E_WINDOW)
