@@ -18,7 +18,10 @@ from ._lib import load_library
 MEETING_DTYPE = np.dtype([("pid_lo", "<u4"), ("pid_hi", "<u4"), ("start", "<u4"), ("end", "<u4"),
                           ("mbr", "<f4", (4,))])
 
-FLAG_SERIAL_SCHEMA = 1
+FLAG_SERIAL_SCHEMA = 1   # STC_FLAG_* of include/stc.h
+FLAG_DIRECT_HITS = 2
+FLAG_QUEUED_HITS = 4
+FLAG_COPY_INPUT = 8
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "CUDA", 3: "CAPACITY", 4: "TIMEOUT", 5: "UNSUPPORTED", 6: "STATE"}
 

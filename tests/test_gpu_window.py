@@ -7,7 +7,7 @@ must be identical."""
 import numpy as np
 import pytest
 
-from stcdb_gb300.pipeline import MEETING_DTYPE, Pipeline, StcConfig
+from stcdb_gb300.pipeline import FLAG_COPY_INPUT, MEETING_DTYPE, Pipeline, StcConfig
 from stcdb_gb300.tracegen import hotspot_grid
 
 from parity import trace_and_box
@@ -32,7 +32,7 @@ def _blocks(p):
 # replayed graphs; direct launches, whose descent reads page-locked host
 # input from the host pages; direct launches with that input copied in
 # (STC_FLAG_COPY_INPUT)
-@pytest.mark.parametrize("graphs,flags", [(1, 0), (2, 0), (2, 8)])
+@pytest.mark.parametrize("graphs,flags", [(1, 0), (2, 0), (2, FLAG_COPY_INPUT)])
 def test_windows_match_plain_steps(built_cuda, graphs, flags):
     import torch
     steps = 24
@@ -173,7 +173,7 @@ def test_page_locked_input_path(built_cuda):
     tr, mbr = trace_and_box(tc, steps)
     pinned = torch.from_numpy(np.ascontiguousarray(tr, dtype=np.float64)).pin_memory().numpy()
     out = np.empty(1_000_000, MEETING_DTYPE)
-    for flags, serve, copies in [(0, False, False), (8, False, True), (0, True, True)]:
+    for flags, serve, copies in [(0, False, False), (FLAG_COPY_INPUT, False, True), (0, True, True)]:
         p = Pipeline(replace(cfg, flags=flags), mbr, tr[0])
         srv = p.server() if serve else None
         try:
