@@ -174,7 +174,8 @@ typedef struct stc_stats {
   float window_device_ms;
   float window_wall_ms;
   float window_input_wait_ms;
-  float window_copy_ms;          /* the window's input copies, start to end (each beside a step) */
+  float window_copy_ms;          /* the window's input copies, start to end (each beside a step);
+                                    0 when the steps' descent read the input from the host pages */
   /* The last flush's stages (device time on the library's stream, the host's
    * reads of the device state between them included): object order (oversize
    * cut, STR sorts, slabs, sids), key sort, per-CTF limits and metadata, key
