@@ -113,3 +113,71 @@ def test_drain_into_pinned_buffer(built_cuda):
             assert np.array_equal(sort_meetings(c.drain(small)), want)  # too small: falls back to its own buffer
             total += len(want)
     assert total > 16
+
+
+# Map box with dyadic corners: every quadtree split line, (lo + hi) / 2 at
+# every depth, is an exact double, so objects can sit exactly on them.
+DYADIC_BOX = np.array([-87.75, 41.75, -87.25, 42.25])
+
+
+def _degenerate_trace(n, steps, seed):
+    """Objects in a 0.004 x 0.004 degree patch around the root's split point,
+    random-walking about 3 m a step, except: 150 coincident at the root's
+    split point; 150 on its vertical and 150 on its horizontal split line;
+    150 on deeper vertical split lines (depths 9-11); 20 at corners of the map
+    box."""
+    rng = np.random.default_rng(seed)
+    cx, cy, h = -87.5, 42.0, 0.002
+    base = np.column_stack([rng.uniform(cx - h, cx + h, n), rng.uniform(cy - h, cy + h, n)])
+    g = np.arange(n)
+    on_point, on_x, on_y, deep = g < 150, (g >= 150) & (g < 300), (g >= 300) & (g < 450), (g >= 450) & (g < 600)
+    corner = (g >= 600) & (g < 620)
+    lines = cx + np.array([-2.0 ** -10, -2.0 ** -11, -2.0 ** -12, 2.0 ** -12, 2.0 ** -11, 2.0 ** -10])
+    out = np.empty((steps, n, 2))
+    for t in range(steps):
+        if t:
+            base = base + rng.normal(0.0, 3e-5, (n, 2))
+        p = base.copy()
+        p[on_point] = (cx, cy)
+        p[on_x, 0] = cx
+        p[on_y, 1] = cy
+        p[deep, 0] = lines[g[deep] % len(lines)]
+        p[corner] = np.column_stack([np.where(g[corner] % 2 == 0, DYADIC_BOX[2], DYADIC_BOX[0]),
+                                     np.where(g[corner] % 4 < 2, DYADIC_BOX[3], DYADIC_BOX[1])])
+        out[t] = p
+    return out
+
+
+def _check_trace(cfg, tr, mbr):
+    total = 0
+    for t, g, o, gs, os_ in run_pair(cfg, tr, mbr):
+        assert gs.checking_units == os_.checking_units, f"step {t}: units {gs.checking_units} vs {os_.checking_units}"
+        assert gs.hits == os_.hits, f"step {t}: hits {gs.hits} vs {os_.hits}"
+        assert gs.overflow_objects == os_.overflow_objects, f"step {t}: overflow differs"
+        assert gs.leaves == os_.leaves and gs.schema_nodes == os_.schema_nodes, f"step {t}: schema differs"
+        assert np.array_equal(g, o), f"step {t}: " + describe_diff(g, o)
+        total += len(o)
+    return total
+
+
+def test_degenerate_positions(built_cuda):
+    """Coincident objects (every pair within reach; their leaf splits down to
+    twice the reach and drops the members past its capacity), objects exactly
+    on split lines (the descent's tie rule: a coordinate equal to the split
+    goes low) and at the map box's corners, against the oracle step by step."""
+    tr = _degenerate_trace(3000, 8, 21)
+    cfg = StcConfig(num_objects=3000, reach_distance=10.0, min_meet_time=3, grid_capacity=20, grid_amplify=1.5,
+                    num_meeting_buckets=400_000)
+    assert _check_trace(cfg, tr, DYADIC_BOX) > 1000
+
+
+@pytest.mark.parametrize("n", [1, 2])
+def test_one_and_two_objects(built_cuda, n):
+    """One object (no pairs) and two objects together for five steps, then
+    apart: the one meeting is emitted when it ends."""
+    tr = np.tile(np.array([[-87.5, 42.0]]), (7, n, 1))
+    if n == 2:
+        tr[:, 1, 0] += 2e-5        # about 1.7 m apart
+        tr[5:, 1, 0] += 0.01       # then about 800 m
+    cfg = StcConfig(num_objects=n, reach_distance=10.0, min_meet_time=3, grid_capacity=20, num_meeting_buckets=64)
+    assert _check_trace(cfg, tr, DYADIC_BOX) == (1 if n == 2 else 0)
