@@ -1006,7 +1006,7 @@ def main():
                     "leaf_capacity": w["grid_capacity"], "grid_amplify": w["amplify"],
                     "launch_shape": {"refine_blocks_per_sm": w.get("refine_bps", 8),
                                      "hits_blocks_per_sm": w.get("hits_bps", 16),
-                                     "refine_chunk": w.get("refine_chunk", 256)},
+                                     "refine_chunk": w.get("refine_chunk") or "by density (64 or 256)"},
                     "meeting_buckets": make_cfg(w).resolved().num_meeting_buckets,
                     "memtable": (f"on, flush past {w['kv_restriction']} directed keys, 100 CTFs, "
                                  f"{w.get('bitmap_edge', 256)}x{w.get('bitmap_edge', 256)} map bitmaps"

@@ -117,7 +117,9 @@ typedef struct stc_config {
                                     0 = 256; a multiple of 32 from 32 to 1024 */
   uint32_t refine_chunk;         /* refinement tile length: a job tests 32 rows against this many
                                     positions of their candidate windows (launch shape, results do
-                                    not depend on it); 0 = 256; a multiple of 32 from 32 to 4096 */
+                                    not depend on it); a multiple of 32 from 32 to 4096; 0 =
+                                    automatic, per step: 64 when the step before tested more than 16
+                                    candidates per checking unit (dense leaves), else 256 */
 } stc_config;
 
 /* Replay quadtree splits/merges on one device thread only (tests compare it
@@ -225,8 +227,8 @@ typedef struct stc_tune_result {
  * `capacities` (n_capacities values; null = {grid_capacity / 2,
  * grid_capacity, 2 * grid_capacity}; cfg's own grid_capacity is always tried
  * and gives base_step_ms), then job_chunk (2-32), refine_chunk (the tile
- * length, 64-512), refine_blocks_per_sm and hits_blocks_per_sm one after the
- * other. The launch shape never changes
+ * length: the automatic choice or 64-512), refine_blocks_per_sm and
+ * hits_blocks_per_sm one after the other. The launch shape never changes
  * results; the leaf capacity is part of the reference's configuration (it
  * orders the reference's table inserts), so a run with the chosen capacity
  * matches the reference run with that capacity. */

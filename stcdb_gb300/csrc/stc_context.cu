@@ -717,9 +717,32 @@ static void choose_hit_emission(stc_ctx *c) {
   }
 }
 
+// Tile length of the refinement's jobs when stc_config.refine_chunk is 0:
+// 64 candidates when the last step tested more than 16 candidates per
+// checking unit (dense leaves have long candidate windows, and 256-long
+// tiles left the tail of the pair tests to a few warps: hotspot-1M 8.46 ->
+// 6.18 ms a step; hotspot-3M, bound by the table update, within 0.3%), else
+// 256 (uniform-10M, 7.9 tests per unit: 64-long tiles cost 0.29 ms a step).
+// Results do not depend on it.
+static constexpr unsigned long long SHORT_TILE_TESTS_PER_UNIT = 16;
+static void choose_refine_chunk(stc_ctx *c) {
+  PipeDev &p = c->p;
+  uint32_t chunk = c->cfg.refine_chunk;
+  if (!chunk) {
+    const DevState &st = *c->st_host;  // the last step's counters
+    chunk = st.tests > SHORT_TILE_TESTS_PER_UNIT * ((unsigned long long)p.N + st.border_units) ? 64u
+                                                                                           : REFINE_CHUNK_DEFAULT;
+  }
+  if (chunk != p.refine_chunk) {
+    p.refine_chunk = chunk;
+    invalidate_graphs(c);  // the captured steps carry the tile length
+  }
+}
+
 static stc_status run_step(stc_ctx *c, const double2 *xy, uint32_t t, bool copied) {
   PipeDev &p = c->p;
   choose_hit_emission(c);
+  choose_refine_chunk(c);
   cudaStream_t s = c->stream;
   p.xy = xy;
   c->t_pinned[0] = t;  // the previous step has been waited for: nothing reads it now
@@ -834,6 +857,7 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   if (c->failed) return STC_ERR_STATE;
   if (!steps) return STC_OK;
   choose_hit_emission(c);  // for the whole window
+  choose_refine_chunk(c);
   cudaSetDevice(c->device);
   PipeDev &p = c->p;
   cudaStream_t s = c->stream;

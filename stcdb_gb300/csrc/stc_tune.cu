@@ -92,7 +92,7 @@ extern "C" stc_status stc_autotune(const stc_config *cfg, const double mbr[4], c
   stc_config k = base;
   k.grid_capacity = r.config.grid_capacity;
   k.job_chunk = cfg->job_chunk ? cfg->job_chunk : 8;  // 0 means these built-in values
-  k.refine_chunk = cfg->refine_chunk ? cfg->refine_chunk : 256;
+  k.refine_chunk = cfg->refine_chunk;  // 0: the per-step automatic choice, itself a candidate
   k.refine_blocks_per_sm = cfg->refine_blocks_per_sm ? cfg->refine_blocks_per_sm : 8;
   k.hits_blocks_per_sm = cfg->hits_blocks_per_sm ? cfg->hits_blocks_per_sm : 16;
   const uint32_t job_chunks[] = {2, 4, 8, 16, 32}, refine_chunks[] = {64, 128, 256, 512},

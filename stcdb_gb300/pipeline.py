@@ -238,7 +238,7 @@ class StcConfig:
     hits_blocks_per_sm: int = 0    # 0 = 16
     window_graphs: int = 0    # step_window replays captured graphs: 0 = for short steps (automatic), 1 = always, 2 = never
     bitmap_edge: int = 0      # edge of a block's map bitmap (oversize buffer); 0 = 256
-    refine_chunk: int = 0     # refinement tile length, candidate positions per job (launch shape); 0 = 256
+    refine_chunk: int = 0     # refinement tile length, candidate positions per job (launch shape); 0 = by density
 
     def resolved(self) -> "StcConfig":
         if self.num_meeting_buckets == 0:

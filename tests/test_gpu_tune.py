@@ -37,7 +37,8 @@ def test_launch_shape_leaves_results_unchanged(built_cuda):
     assert sum(len(m) for m, _, _ in want) > 0
     for shape in [dict(job_chunk=1, refine_blocks_per_sm=2, hits_blocks_per_sm=64),
                   dict(job_chunk=64, refine_blocks_per_sm=32, hits_blocks_per_sm=1),
-                  dict(refine_chunk=32), dict(refine_chunk=96, job_chunk=3), dict(refine_chunk=4096)]:
+                  dict(refine_chunk=32), dict(refine_chunk=96, job_chunk=3), dict(refine_chunk=4096),
+                  dict(refine_chunk=256)]:
         got = _run(StcConfig(**{**base.__dict__, **shape}), tr, mbr)
         for t, ((gm, gh, gb), (wm, wh, wb)) in enumerate(zip(got, want)):
             assert gh == wh and gb == wb, f"step {t}: counters differ with {shape}"
@@ -67,8 +68,8 @@ def test_autotune_picks_a_runnable_setting(built_cuda):
                     num_meeting_buckets=1_500_000)
     chosen, rep = autotune(cfg, mbr, np.stack(tr), capacities=[25, 50, 100])
     assert chosen.grid_capacity in (25, 50, 100)
-    assert chosen.job_chunk in (2, 4, 8, 16, 32) and chosen.refine_chunk in (64, 128, 256, 512)
+    assert chosen.job_chunk in (2, 4, 8, 16, 32) and chosen.refine_chunk in (0, 64, 128, 256, 512)
     assert chosen.refine_blocks_per_sm in (4, 8, 16) and chosen.hits_blocks_per_sm in (8, 16, 32)
-    assert rep["trials"] == 3 + 4 + 3 + 2 + 2
+    assert rep["trials"] == 3 + 4 + 4 + 2 + 2
     assert 0 < rep["best_step_ms"] <= rep["base_step_ms"]
     assert len(_run(chosen, tr, mbr)) == len(tr)
