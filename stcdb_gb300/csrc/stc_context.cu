@@ -856,8 +856,6 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   if (out && !n_out) return fail(c, STC_ERR_INVALID_ARG, "stc_step_window: output without a count");
   if (c->failed) return STC_ERR_STATE;
   if (!steps) return STC_OK;
-  choose_hit_emission(c);  // for the whole window
-  choose_refine_chunk(c);
   cudaSetDevice(c->device);
   PipeDev &p = c->p;
   cudaStream_t s = c->stream;
@@ -949,6 +947,11 @@ extern "C" stc_status stc_step_window(stc_ctx *c, const double *xy, int on_devic
   // copy event, time word and graph by i % WIN_BUFS)
   auto issue_core = [&](uint32_t i) -> stc_status {
     const int par = i & 1, b = (int)(i % WIN_BUFS);
+    // launch forms by the density of the latest step whose state has been
+    // taken (i - 2, or the step before the window): the hits' hand-over form
+    // and the pair tests' tile length
+    choose_hit_emission(c);
+    choose_refine_chunk(c);
     c->t_pinned[b] = t0 + i;  // step i - WIN_BUFS, the word's last reader, has been waited for
     const unsigned long long l0 = tl_launches;
     cudaEventRecord(c->wev[par][0], s);
