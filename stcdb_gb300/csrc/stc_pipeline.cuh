@@ -10,7 +10,7 @@ namespace stc {
 // Candidate positions per refinement job and lane: a row block's candidate
 // ranges are cut into chunks of this many, so that the n^2 / 2 pair tests of
 // a dense leaf spread over many warps.
-constexpr uint32_t REFINE_CHUNK_DEFAULT = 256;  // stc_config.refine_chunk = 0
+constexpr uint32_t REFINE_CHUNK_DEFAULT = 256;  // tile length before the first step's density is known
 
 struct PipeDev {
   // sizes
